@@ -1,0 +1,637 @@
+// Oracle for the 2D shallow-water ODE right-hand side and its time stepping.
+//
+// TEST INFRASTRUCTURE ONLY.  This header is a CPU (FP64, optionally OpenMP)
+// restatement of Hydrograd.jl's hot path.  It exists to check the CUDA product
+// path and to time a CPU baseline; nothing in the shipped library includes,
+// links or calls it.  Every function cites the reference file:line it follows
+// (paths are relative to the Hydrograd.jl project root).
+//
+// Parity pin: the restatement is checked against the reference's own shipped
+// golden data (forward-simulation truth JSON: S0_cells_truth, friction_x/y
+// truth, steady-state xi_truth; ManningN sensitivity Jacobians) by the tests
+// under tests/, using fixtures generated by tests/golden/make_golden.py.
+//
+// The scalar type T is templated so that a forward-mode dual number
+// (hgo::Dual<N>, see dual.hpp) reproduces what ForwardDiff.jl computes through
+// the same code.  Build with -ffp-contract=off so that no a*b+c is fused: Julia
+// does not contract either, and the x86 build and the aarch64 build then agree.
+#pragma once
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <cstdint>
+#include <map>
+#include <stdexcept>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "dual.hpp"
+
+namespace hgo {
+
+// Boundary types (src/fvm/boundary_conditions/bc_2D.jl:154-260).
+enum BcType : int { BC_WALL = 0, BC_SYMM = 1, BC_INLETQ = 2, BC_EXITH = 3 };
+
+// eps(Float64): the smooth_* helpers add eps(T) (src/utilities/smooth_functions.jl:4-52).
+// For a dual number ForwardDiff's eps(Dual) is eps of the value type, i.e. this constant.
+constexpr double kEps = 2.220446049250313e-16;
+
+template <class T> inline T smooth_abs(const T& x) { using std::sqrt; return sqrt(x * x + kEps); }   // smooth_functions.jl:4-12
+template <class T> inline T smooth_sqrt(const T& x) { using std::sqrt; return sqrt(x + kEps); }      // smooth_functions.jl:39-44
+template <class T> inline T smooth_pow2(const T& x) { T y = x + kEps; return y * y; }               // smooth_functions.jl:47-52 (n = 2)
+
+// ---------------------------------------------------------------------------
+// Mesh topology and geometry.
+// Restates SRH_2D_SRHGeom.jl:251-382 (edge numbering, boundary edges, default
+// wall) and mesh_2D.jl:75-652 (ghost cells, neighbours, areas, centroids,
+// outward cell normals, face normals/lengths).  Ids are 0-based here; the
+// reference's 1-based ids are kept in the same relative order.
+// ---------------------------------------------------------------------------
+struct NodeString {
+  int id;                 // NodeString id as in the .srhgeom file (1-based in SRH-2D)
+  int bc;                 // BcType, or -1 for a NodeString that is not a boundary (monitoring line)
+  std::vector<int> nodes; // 0-based node ids, in file order
+};
+
+struct Mesh {
+  int nCells = 0, nNodes = 0, nFaces = 0, maxNodes = 8;
+  std::vector<double> nodeX, nodeY, nodeZ;
+  std::vector<int> cellNodesCount;       // [nCells]
+  std::vector<int> cellNodes;            // [nCells*8] 0-based node ids
+  std::vector<int> cellFaces;            // [nCells*8] 0-based face ids (sign dropped, mesh_2D.jl:161)
+  std::vector<int> cellFaceSign;         // [nCells*8] +1 / -1 as elementEdgesList before abs
+  std::vector<std::array<int, 2>> faceNodes;   // sorted (min,max) node ids (SRH_2D_SRHGeom.jl:271)
+  std::vector<std::vector<int>> faceCells;     // 1 or 2 cells in creation order (SRH_2D_SRHGeom.jl:278,284)
+  std::vector<char> faceIsBoundary;            // mesh_2D.jl:265-276
+  // Boundaries, keyed by boundary id; faces in NodeString order (SRH_2D_SRHGeom.jl:304-349).
+  std::map<int, std::vector<int>> boundaryFaces;
+  std::map<int, std::vector<int>> boundaryDirs;  // +1 when the face normal points out (mesh_2D.jl:141-158)
+  std::map<int, int> boundaryType;               // BcType per boundary id
+  std::vector<int> allBoundaryFaces;             // ghost g <-> allBoundaryFaces[g]
+  std::vector<int> faceGhost;                    // [nFaces] ghost id or -1
+  std::vector<int> faceBoundaryId;               // [nFaces] boundary id or 0 (internal)
+  std::vector<int> cellNeighbors;                // [nCells*8] neighbour cell id, or ghost id for boundary faces
+  // Geometry (mesh_2D.jl:456-652)
+  std::vector<double> cellAreas, cellCx, cellCy;
+  std::vector<double> cellNormals;   // [nCells*8*2] outward normal of cell edge i (node i -> node i+1)
+  std::vector<double> cellDist;      // [nCells*8]
+  std::vector<double> faceNx, faceNy, faceLengths;
+};
+
+// Build the mesh from node coordinates, cell node lists (0-based node ids,
+// counter-clockwise) and NodeStrings.
+inline Mesh build_mesh(int nNodes, const double* x, const double* y, const double* z, int nCells,
+                       const int* cellNodesCount, const int* cellNodes8,
+                       const std::vector<NodeString>& strings) {
+  Mesh m;
+  m.nNodes = nNodes;
+  m.nCells = nCells;
+  m.nodeX.assign(x, x + nNodes);
+  m.nodeY.assign(y, y + nNodes);
+  m.nodeZ.assign(z, z + nNodes);
+  m.cellNodesCount.assign(cellNodesCount, cellNodesCount + nCells);
+  m.cellNodes.assign(cellNodes8, cellNodes8 + (size_t)nCells * 8);
+
+  // Edges: SRH_2D_SRHGeom.jl:251-287.  Edge ids are handed out in the order
+  // edges are first met while looping cells and their edges.
+  std::unordered_map<uint64_t, int> edges;
+  edges.reserve((size_t)nCells * 4);
+  auto key = [](int a, int b) -> uint64_t { return ((uint64_t)(uint32_t)a << 32) | (uint32_t)b; };
+  for (int c = 0; c < nCells; ++c) {
+    int n = m.cellNodesCount[c];
+    for (int i = 0; i < n; ++i) {
+      int n1 = m.cellNodes[(size_t)c * 8 + i];
+      int n2 = m.cellNodes[(size_t)c * 8 + (i + 1) % n];
+      int a = std::min(n1, n2), b = std::max(n1, n2);
+      auto it = edges.find(key(a, b));
+      if (it == edges.end()) {
+        int id = (int)m.faceNodes.size();
+        edges.emplace(key(a, b), id);
+        m.faceNodes.push_back({a, b});
+        m.faceCells.push_back({c});
+      } else {
+        if (m.faceCells[it->second].size() != 1) throw std::runtime_error("edge shared by more than two cells");
+        m.faceCells[it->second].push_back(c);
+      }
+    }
+  }
+  m.nFaces = (int)m.faceNodes.size();
+  m.faceIsBoundary.assign(m.nFaces, 0);
+  for (int f = 0; f < m.nFaces; ++f) m.faceIsBoundary[f] = m.faceCells[f].size() == 1;
+
+  // elementEdgesList with sign: + when (n1,n2) is the sorted key (SRH_2D_SRHGeom.jl:355-377).
+  m.cellFaces.assign((size_t)nCells * 8, 0);
+  m.cellFaceSign.assign((size_t)nCells * 8, 0);
+  for (int c = 0; c < nCells; ++c) {
+    int n = m.cellNodesCount[c];
+    for (int i = 0; i < n; ++i) {
+      int n1 = m.cellNodes[(size_t)c * 8 + i];
+      int n2 = m.cellNodes[(size_t)c * 8 + (i + 1) % n];
+      int a = std::min(n1, n2), b = std::max(n1, n2);
+      int id = edges.at(key(a, b));
+      m.cellFaces[(size_t)c * 8 + i] = id;
+      m.cellFaceSign[(size_t)c * 8 + i] = (n1 < n2) ? 1 : -1;
+    }
+  }
+
+  // Boundary edges from NodeStrings (SRH_2D_SRHGeom.jl:303-338); monitoring
+  // lines (bc < 0) are skipped; an edge not found is a mesh error.
+  std::vector<char> used(m.nFaces, 0);
+  int nBoundaryStrings = 0;
+  for (const auto& s : strings) {
+    if (s.bc < 0) continue;
+    ++nBoundaryStrings;
+    std::vector<int> list;
+    for (size_t i = 0; i + 1 < s.nodes.size(); ++i) {
+      int a = std::min(s.nodes[i], s.nodes[i + 1]), b = std::max(s.nodes[i], s.nodes[i + 1]);
+      auto it = edges.find(key(a, b));
+      if (it == edges.end()) throw std::runtime_error("NodeString edge not found in mesh");
+      list.push_back(it->second);
+      used[it->second] = 1;
+    }
+    m.boundaryFaces[s.id] = list;
+    m.boundaryType[s.id] = s.bc;
+  }
+  // Default wall boundary for unused boundary edges (SRH_2D_SRHGeom.jl:344-349; mesh_2D.jl:172-181).
+  std::vector<int> unused;
+  for (int f = 0; f < m.nFaces; ++f)
+    if (m.faceIsBoundary[f] && !used[f]) unused.push_back(f);
+  if (!unused.empty()) {
+    int defaultId = nBoundaryStrings + 1;
+    m.boundaryFaces[defaultId] = unused;
+    m.boundaryType[defaultId] = BC_WALL;
+  }
+  // Directions (mesh_2D.jl:141-158): -1 when the owning cell walks the edge
+  // against its sorted node order, i.e. the face normal points inward.
+  for (auto& kv : m.boundaryFaces) {
+    std::vector<int> dirs(kv.second.size(), 1);
+    for (size_t i = 0; i < kv.second.size(); ++i) {
+      int f = kv.second[i];
+      if (!m.faceIsBoundary[f]) throw std::runtime_error("NodeString edge is not a boundary edge");
+      int c = m.faceCells[f][0];
+      for (int k = 0; k < m.cellNodesCount[c]; ++k)
+        if (m.cellFaces[(size_t)c * 8 + k] == f && m.cellFaceSign[(size_t)c * 8 + k] < 0) dirs[i] = -1;
+    }
+    m.boundaryDirs[kv.first] = dirs;
+  }
+  // Ghost cells: one per boundary face.  The reference numbers them in Julia
+  // Dict iteration order (SRH_2D_SRHGeom.jl:290); ghost numbering is internal
+  // and never changes a result, so ascending face id is used here.
+  m.faceGhost.assign(m.nFaces, -1);
+  for (int f = 0; f < m.nFaces; ++f)
+    if (m.faceIsBoundary[f]) {
+      m.faceGhost[f] = (int)m.allBoundaryFaces.size();
+      m.allBoundaryFaces.push_back(f);
+    }
+  m.faceBoundaryId.assign(m.nFaces, 0);
+  for (auto& kv : m.boundaryFaces)
+    for (int f : kv.second) m.faceBoundaryId[f] = kv.first;
+  for (int f = 0; f < m.nFaces; ++f)
+    if (m.faceIsBoundary[f] && m.faceBoundaryId[f] == 0) throw std::runtime_error("boundary face without boundary");
+
+  // Neighbours (mesh_2D.jl:229-254).
+  m.cellNeighbors.assign((size_t)nCells * 8, -1);
+  for (int c = 0; c < nCells; ++c)
+    for (int i = 0; i < m.cellNodesCount[c]; ++i) {
+      int f = m.cellFaces[(size_t)c * 8 + i];
+      const auto& fc = m.faceCells[f];
+      if (fc.size() == 2) m.cellNeighbors[(size_t)c * 8 + i] = (fc[0] == c) ? fc[1] : fc[0];
+      else m.cellNeighbors[(size_t)c * 8 + i] = m.faceGhost[f];
+    }
+
+  // Geometry (mesh_2D.jl:456-547).
+  m.cellAreas.assign(nCells, 0.0);
+  m.cellCx.assign(nCells, 0.0);
+  m.cellCy.assign(nCells, 0.0);
+  m.cellNormals.assign((size_t)nCells * 16, 0.0);
+  for (int c = 0; c < nCells; ++c) {
+    int n = m.cellNodesCount[c];
+    double area = 0.0, cx = 0.0, cy = 0.0, asum = 0.0;
+    for (int i = 0; i < n; ++i) {   // compute_polygon_area_srhgeom, mesh_2D.jl:600-616
+      int a = m.cellNodes[(size_t)c * 8 + i], b = m.cellNodes[(size_t)c * 8 + (i + 1) % n];
+      area += m.nodeX[a] * m.nodeY[b] - m.nodeX[b] * m.nodeY[a];
+    }
+    if (area < 0) throw std::runtime_error("cell nodes are not counter-clockwise");
+    m.cellAreas[c] = std::fabs(area) / 2;
+    for (int i = 0; i < n; ++i) {   // compute_polygon_centroid_srhgeom, mesh_2D.jl:619-634
+      int a = m.cellNodes[(size_t)c * 8 + i], b = m.cellNodes[(size_t)c * 8 + (i + 1) % n];
+      double x1 = m.nodeX[a], y1 = m.nodeY[a], x2 = m.nodeX[b], y2 = m.nodeY[b];
+      double cross = x1 * y2 - x2 * y1;
+      cx += (x1 + x2) * cross;
+      cy += (y1 + y2) * cross;
+      asum += cross;
+    }
+    double a2 = std::fabs(asum) / 2;
+    m.cellCx[c] = cx / (6 * a2);
+    m.cellCy[c] = cy / (6 * a2);
+    for (int i = 0; i < n; ++i) {   // compute_face_normals_srhgeom, mesh_2D.jl:550-575
+      int a = m.cellNodes[(size_t)c * 8 + i], b = m.cellNodes[(size_t)c * 8 + (i + 1) % n];
+      double fx = m.nodeX[b] - m.nodeX[a], fy = m.nodeY[b] - m.nodeY[a];
+      double nx = fy, ny = -fx;
+      double len = std::sqrt(nx * nx + ny * ny);
+      m.cellNormals[(size_t)c * 16 + 2 * i] = nx / len;
+      m.cellNormals[(size_t)c * 16 + 2 * i + 1] = ny / len;
+    }
+  }
+  m.faceNx.assign(m.nFaces, 0.0);
+  m.faceNy.assign(m.nFaces, 0.0);
+  m.faceLengths.assign(m.nFaces, 0.0);
+  for (int f = 0; f < m.nFaces; ++f) {   // compute_face_normal_srhgeom, mesh_2D.jl:637-652
+    int a = m.faceNodes[f][0], b = m.faceNodes[f][1];
+    double nx = m.nodeY[b] - m.nodeY[a], ny = -(m.nodeX[b] - m.nodeX[a]);
+    double len = std::sqrt(nx * nx + ny * ny);
+    m.faceNx[f] = nx / len;
+    m.faceNy[f] = ny / len;
+    m.faceLengths[f] = len;
+  }
+  m.cellDist.assign((size_t)nCells * 8, 0.0);
+  for (int c = 0; c < nCells; ++c)   // mesh_2D.jl:494-530
+    for (int i = 0; i < m.cellNodesCount[c]; ++i) {
+      int f = m.cellFaces[(size_t)c * 8 + i];
+      double dx, dy;
+      if (m.faceIsBoundary[f]) {
+        int a = m.faceNodes[f][0], b = m.faceNodes[f][1];
+        dx = m.cellCx[c] - (m.nodeX[a] + m.nodeX[b]) / 2;
+        dy = m.cellCy[c] - (m.nodeY[a] + m.nodeY[b]) / 2;
+      } else {
+        int nb = m.cellNeighbors[(size_t)c * 8 + i];
+        dx = m.cellCx[c] - m.cellCx[nb];
+        dy = m.cellCy[c] - m.cellCy[nb];
+      }
+      m.cellDist[(size_t)c * 8 + i] = std::sqrt(dx * dx + dy * dy);
+    }
+  return m;
+}
+
+// Boundary-condition tables (bc_2D.jl:50-570): per boundary of each type, its
+// faces, ghosts, internal cells and outward normals (face_direction .* face_normal).
+struct BcGroup {
+  int boundaryId;
+  std::vector<int> faces, ghosts, internals;
+  std::vector<double> onx, ony, lengths;
+};
+struct Bcs {
+  std::vector<BcGroup> inletQ, exitH, wall, symm;
+};
+
+inline Bcs build_bcs(const Mesh& m) {
+  Bcs b;
+  for (auto& kv : m.boundaryFaces) {   // boundary ids in ascending order, as compute_boundary_indices_2D! loops 1:numOfBoundaries
+    BcGroup g;
+    g.boundaryId = kv.first;
+    const auto& dirs = m.boundaryDirs.at(kv.first);
+    for (size_t i = 0; i < kv.second.size(); ++i) {
+      int f = kv.second[i];
+      g.faces.push_back(f);
+      g.ghosts.push_back(m.faceGhost[f]);
+      g.internals.push_back(m.faceCells[f][0]);
+      g.onx.push_back(dirs[i] * m.faceNx[f]);
+      g.ony.push_back(dirs[i] * m.faceNy[f]);
+      g.lengths.push_back(m.faceLengths[f]);
+    }
+    switch (m.boundaryType.at(kv.first)) {
+      case BC_INLETQ: b.inletQ.push_back(g); break;
+      case BC_EXITH: b.exitH.push_back(g); break;
+      case BC_SYMM: b.symm.push_back(g); break;
+      default: b.wall.push_back(g); break;
+    }
+  }
+  return b;
+}
+
+// ---------------------------------------------------------------------------
+// Bed data (process_bed_2D.jl:46-66; fvm_schemes_2D.jl:111-138,197-213,253-275).
+// ---------------------------------------------------------------------------
+template <class T>
+struct BedData {
+  std::vector<T> zbGhost, zbFaces, S0x, S0y;
+};
+
+template <class T>
+BedData<T> update_bed_data(const Mesh& m, const T* zb) {
+  BedData<T> d;
+  d.zbGhost.resize(m.allBoundaryFaces.size());
+  for (size_t g = 0; g < m.allBoundaryFaces.size(); ++g)          // update_ghost_cells_scalar
+    d.zbGhost[g] = zb[m.faceCells[m.allBoundaryFaces[g]][0]];
+  d.zbFaces.resize(m.nFaces);
+  for (int f = 0; f < m.nFaces; ++f) {                            // cells_to_faces_scalar
+    const auto& fc = m.faceCells[f];
+    d.zbFaces[f] = fc.size() == 2 ? (zb[fc[0]] + zb[fc[1]]) / 2.0 : zb[fc[0]];
+  }
+  d.S0x.resize(m.nCells);
+  d.S0y.resize(m.nCells);
+  for (int c = 0; c < m.nCells; ++c) {                            // compute_cell_gradient_from_faces
+    T gx = T(0.0), gy = T(0.0);
+    for (int i = 0; i < m.cellNodesCount[c]; ++i) {
+      int f = m.cellFaces[(size_t)c * 8 + i];
+      double nx = m.cellNormals[(size_t)c * 16 + 2 * i], ny = m.cellNormals[(size_t)c * 16 + 2 * i + 1];
+      gx = gx + nx * d.zbFaces[f] * m.faceLengths[f];
+      gy = gy + ny * d.zbFaces[f] * m.faceLengths[f];
+    }
+    d.S0x[c] = -1.0 * (gx / m.cellAreas[c]);                      // S0 = -1.0 * gradient (process_bed_2D.jl:55)
+    d.S0y[c] = -1.0 * (gy / m.cellAreas[c]);
+  }
+  return d;
+}
+
+// zb at cells = mean of node z (fvm_schemes_2D.jl:216-224).
+inline std::vector<double> nodes_to_cells(const Mesh& m, const std::vector<double>& zn) {
+  std::vector<double> zc(m.nCells);
+  for (int c = 0; c < m.nCells; ++c) {
+    double s = 0.0;
+    for (int i = 0; i < m.cellNodesCount[c]; ++i) s += zn[m.cellNodes[(size_t)c * 8 + i]];
+    zc[c] = s / m.cellNodesCount[c];
+  }
+  return zc;
+}
+
+// ---------------------------------------------------------------------------
+// Roe flux (src/fvm/discretization/Riemman_solvers/swe_2D_solvers.jl:4-164).
+// ---------------------------------------------------------------------------
+template <class T>
+inline void roe_flux(T xiL, T hstillL, T hL, T huL, T hvL, T zbL, T xiR, T hstillR, T hR, T huR, T hvR, T zbR,
+                     double g, double nx, double ny, double hmin, T out[3]) {
+  using std::sqrt;
+  if (value(hL) <= hmin && value(hR) <= hmin) {                          // :16-22 both dry
+    out[0] = T(0.0); out[1] = T(0.0); out[2] = T(0.0);
+    return;
+  } else if (value(hL + zbL) < value(zbR + hmin) && value(hR) <= hmin) {   // :23-38 wall: R <- mirrored L (xiR kept)
+    hR = hL; huR = -huL; hvR = -hvL;
+  } else if (value(hR + zbR) < value(zbL + hmin) && value(hL) <= hmin) {   // :39-53 wall: L <- mirrored R (xiL kept)
+    hL = hR; huL = -huR; hvL = -hvR;
+  } else if (value(hL) <= hmin) {                                        // :54-64 left dry: physical flux of R
+    T p = 0.5 * g * smooth_pow2(hR);
+    out[0] = huR * nx + hvR * ny;
+    out[1] = (huR * (huR / hR) + p) * nx + huR * (hvR / hR) * ny;
+    out[2] = (hvR * (huR / hR)) * nx + (hvR * (hvR / hR) + p) * ny;
+    return;
+  } else if (value(hR) <= hmin) {                                        // :65-75 right dry: physical flux of L
+    T p = 0.5 * g * smooth_pow2(hL);
+    out[0] = huL * nx + hvL * ny;
+    out[1] = (huL * (huL / hL) + p) * nx + huL * (hvL / hL) * ny;
+    out[2] = (hvL * (huL / hL)) * nx + (hvL * (hvL / hL) + p) * ny;
+    return;
+  }
+  T uL = huL / hL, vL = hvL / hL, uR = huR / hR, vR = hvR / hR;          // :79-82
+  T sqrt_hL = smooth_sqrt(hL), sqrt_hR = smooth_sqrt(hR);                // :89-90
+  T hRoe = (hL + hR) / 2.0;                                              // :91 arithmetic average
+  T uRoe = (sqrt_hL * uL + sqrt_hR * uR) / (sqrt_hL + sqrt_hR);
+  T vRoe = (sqrt_hL * vL + sqrt_hR * vR) / (sqrt_hL + sqrt_hR);
+  T unRoe = uRoe * nx + vRoe * ny;
+  T cRoe = smooth_sqrt(g * hRoe);
+  T o2c = 0.5 / cRoe;                                                    // one/2.0/cRoe
+  // R, L, |Lambda| (:103-113); absA_dQ = R * (|Lambda| * (L * dQ)) (:118)
+  T R10 = T(ny), R11 = uRoe - cRoe * nx, R12 = uRoe + cRoe * nx;
+  T R20 = T(-nx), R21 = vRoe - cRoe * ny, R22 = vRoe + cRoe * ny;
+  T L00 = -(uRoe * ny - vRoe * nx), L01 = T(ny), L02 = T(-nx);
+  T L10 = unRoe * o2c + 0.5, L11 = -nx * o2c, L12 = -ny * o2c;
+  T L20 = -unRoe * o2c + 0.5, L21 = nx * o2c, L22 = ny * o2c;
+  T a0 = smooth_abs(unRoe), a1 = smooth_abs(unRoe - cRoe), a2 = smooth_abs(unRoe + cRoe);
+  T d0 = xiR - xiL, d1 = huR - huL, d2 = hvR - hvL;                      // :115 dQ uses xi
+  T w0 = L00 * d0 + L01 * d1 + L02 * d2;
+  T w1 = L10 * d0 + L11 * d1 + L12 * d2;
+  T w2 = L20 * d0 + L21 * d1 + L22 * d2;
+  w0 = a0 * w0; w1 = a1 * w1; w2 = a2 * w2;
+  T A0 = w1 + w2;                                                        // row 1 of R is (0 1 1)
+  T A1 = R10 * w0 + R11 * w1 + R12 * w2;
+  T A2 = R20 * w0 + R21 * w1 + R22 * w2;
+  T pL = 0.5 * g * (smooth_pow2(xiL) + 2.0 * xiL * hstillL);           // :122-127 pre-balanced pressure
+  T pR = 0.5 * g * (smooth_pow2(xiR) + 2.0 * xiR * hstillR);
+  T fL0 = huL * nx + hvL * ny;
+  T fL1 = (huL * uL + pL) * nx + huL * vL * ny;
+  T fL2 = (hvL * uL) * nx + (hvL * vL + pL) * ny;
+  T fR0 = huR * nx + hvR * ny;
+  T fR1 = (huR * uR + pR) * nx + huR * vR * ny;
+  T fR2 = (hvR * uR) * nx + (hvR * vR + pR) * ny;
+  out[0] = (fL0 + fR0 - A0) / 2.0;                                       // :131-133
+  out[1] = (fL1 + fR1 - A1) / 2.0;
+  out[2] = (fL2 + fR2 - A2) / 2.0;
+}
+
+// ---------------------------------------------------------------------------
+// The RHS (src/fvm/discretization/semi_discretize_swe_2D.jl:18-277).
+// ---------------------------------------------------------------------------
+struct Consts {
+  double g = 9.81, k_n = 1.0, h_small = 1.0e-3;   // solve_swe_2D.jl:51-107
+};
+
+template <class T>
+struct Params {
+  std::vector<T> manningCells;   // ManningN_cells (process_ManningN_2D.jl:242-269 for zones)
+  std::vector<T> zbCells;        // zb_cells (active parameter replaces it, semi_discretize_swe_2D.jl:114-126)
+  std::vector<T> inletQ;         // inletQ_TotalQ per inlet-Q boundary (:190-199)
+  std::vector<T> exitWSE;        // exitH_WSE per exit-H boundary
+  BedData<T> bed;                // derived from zbCells
+};
+
+struct Case {
+  Mesh mesh;
+  Bcs bcs;
+  Consts k;
+  std::vector<double> hstill;        // wstill - zb (process_ICs_2D.jl:55,84); not recomputed when zb changes
+  std::vector<double> hstillGhost;   // setup_ghost_cells_initial_condition (process_ICs_2D.jl:145-155)
+};
+
+template <class T>
+void set_zb(const Case& cs, Params<T>& p, const std::vector<T>& zb) {
+  p.zbCells = zb;
+  p.bed = update_bed_data<T>(cs.mesh, zb.data());
+}
+
+// Ghost states (bc_2D.jl:575-875).  h, qx, qy are the clamped cell states.
+template <class T>
+void ghost_states(const Case& cs, const Params<T>& p, const std::vector<T>& h, const std::vector<T>& qx,
+                  const std::vector<T>& qy, std::vector<T>& hg, std::vector<T>& qxg, std::vector<T>& qyg) {
+  const Mesh& m = cs.mesh;
+  size_t nG = m.allBoundaryFaces.size();
+  hg.assign(nG, T(0.0)); qxg.assign(nG, T(0.0)); qyg.assign(nG, T(0.0));
+  const double hs = cs.k.h_small;
+  for (size_t b = 0; b < cs.bcs.inletQ.size(); ++b) {                    // :640-730 inlet-Q
+    const BcGroup& G = cs.bcs.inletQ[b];
+    T totalA = T(0.0);
+    std::vector<double> wet(G.faces.size());
+    for (size_t i = 0; i < G.faces.size(); ++i) {
+      int c = G.internals[i];
+      wet[i] = value(h[c]) > hs ? 1.0 : 0.0;
+      totalA = totalA + std::pow(G.lengths[i], 5.0 / 3.0) * h[c] / p.manningCells[c] * wet[i];
+    }
+    if (!(value(totalA) > 1e-10)) throw std::runtime_error("inlet-Q conveyance is not positive (bc_2D.jl:679)");
+    for (size_t i = 0; i < G.faces.size(); ++i) {
+      int c = G.internals[i], gh = G.ghosts[i];
+      T vn = p.inletQ[b] / totalA * std::pow(G.lengths[i], 2.0 / 3.0) / p.manningCells[c];
+      hg[gh] = h[c];
+      qxg[gh] = -h[c] * vn * G.onx[i] * wet[i];
+      qyg[gh] = -h[c] * vn * G.ony[i] * wet[i];
+    }
+  }
+  for (size_t b = 0; b < cs.bcs.exitH.size(); ++b) {                     // :748-773 exit-H
+    const BcGroup& G = cs.bcs.exitH[b];
+    for (size_t i = 0; i < G.faces.size(); ++i) {
+      int c = G.internals[i], gh = G.ghosts[i];
+      T hn = p.exitWSE[b] - p.zbCells[c];
+      hg[gh] = value(hn) > hs ? hn : T(hs);                               // max(h_small, WSE - zb_cell)
+      qxg[gh] = qx[c];
+      qyg[gh] = qy[c];
+    }
+  }
+  for (const BcGroup& G : cs.bcs.wall)                                   // :777-799 wall
+    for (size_t i = 0; i < G.faces.size(); ++i) {
+      int c = G.internals[i], gh = G.ghosts[i];
+      hg[gh] = h[c]; qxg[gh] = -qx[c]; qyg[gh] = -qy[c];
+    }
+  for (const BcGroup& G : cs.bcs.symm)                                   // :803-834 symmetry
+    for (size_t i = 0; i < G.faces.size(); ++i) {
+      int c = G.internals[i], gh = G.ghosts[i];
+      T vdn = qx[c] * G.onx[i] + qy[c] * G.ony[i];
+      hg[gh] = h[c];
+      qxg[gh] = qx[c] - 2.0 * vdn * G.onx[i];
+      qyg[gh] = qy[c] - 2.0 * vdn * G.ony[i];
+    }
+}
+
+// Manning friction (semi_discretize_swe_2D.jl:544-547).
+template <class T>
+inline T friction_factor(double g, double k_n, double h_small, const T& n, const T& h, const T& qx, const T& qy) {
+  using std::pow;
+  return g * (n * n) / (k_n * k_n) / pow(h + h_small, 7.0 / 3.0) * smooth_sqrt(qx * qx + qy * qy);
+}
+
+// dQ = swe_2d_rhs(Q) with Q = [xi; qx; qy] (semi_discretize_swe_2D.jl:18-277).
+template <class T>
+void rhs(const Case& cs, const Params<T>& p, const T* Q, T* dQ, int nthreads = 1) {
+  const Mesh& m = cs.mesh;
+  const int N = m.nCells;
+  const double hs = cs.k.h_small, g = cs.k.g;
+  std::vector<T> h(N), qx(N), qy(N);
+  for (int i = 0; i < N; ++i) {                                         // :101-106 clamp
+    T hh = Q[i] + cs.hstill[i];
+    bool dry = value(hh) <= hs;
+    h[i] = dry ? T(hs) : hh;
+    qx[i] = dry ? T(0.0) : Q[N + i];
+    qy[i] = dry ? T(0.0) : Q[2 * N + i];
+  }
+  std::vector<T> hg, qxg, qyg;
+  ghost_states(cs, p, h, qx, qy, hg, qxg, qyg);                          // :215-217
+  std::vector<T> xig(hg.size());
+  for (size_t k = 0; k < hg.size(); ++k) xig[k] = hg[k] - cs.hstillGhost[k];   // :220
+  (void)nthreads;
+#pragma omp parallel for schedule(static) num_threads(nthreads > 0 ? nthreads : 1) if (nthreads > 1)
+  for (int c = 0; c < N; ++c) {                                          // compute_inviscid_fluxes :286-419
+    T fs0 = T(0.0), fs1 = T(0.0), fs2 = T(0.0);
+    for (int i = 0; i < m.cellNodesCount[c]; ++i) {
+      int f = m.cellFaces[(size_t)c * 8 + i];
+      int r = m.cellNeighbors[(size_t)c * 8 + i];
+      double nx = m.cellNormals[(size_t)c * 16 + 2 * i], ny = m.cellNormals[(size_t)c * 16 + 2 * i + 1];
+      T xiR, hstR, hR, huR, hvR, zbR;
+      if (!m.faceIsBoundary[f]) {
+        xiR = Q[r]; hstR = T(cs.hstill[r]); hR = h[r]; huR = qx[r]; hvR = qy[r]; zbR = p.zbCells[r];
+      } else {
+        xiR = xig[r]; hstR = T(cs.hstillGhost[r]); hR = hg[r]; huR = qxg[r]; hvR = qyg[r]; zbR = p.bed.zbGhost[r];
+      }
+      T F[3];
+      roe_flux<T>(Q[c], T(cs.hstill[c]), h[c], qx[c], qy[c], p.zbCells[c], xiR, hstR, hR, huR, hvR, zbR, g, nx, ny,
+                  hs, F);
+      double L = m.faceLengths[f];
+      fs0 = fs0 + F[0] * L;                                              // :387
+      fs1 = fs1 + F[1] * L;
+      fs2 = fs2 + F[2] * L;
+    }
+    double A = m.cellAreas[c];
+    T inv0 = -fs0 / A, inv1 = -fs1 / A, inv2 = -fs2 / A;                // :415
+    // compute_source_terms (:449-505) + compute_friction_terms (:508-559)
+    T fr = friction_factor<T>(g, cs.k.k_n, hs, p.manningCells[c], h[c], qx[c], qy[c]);
+    T frx = fr * qx[c], fry = fr * qy[c];
+    bool above = value(h[c]) > hs;
+    T sx = above ? (g * Q[c] * p.bed.S0x[c] - frx) : T(0.0);
+    T sy = above ? (g * Q[c] * p.bed.S0y[c] - fry) : T(0.0);
+    dQ[c] = inv0 + 0.0;                                                  // continuity source is zero (:478)
+    dQ[N + c] = inv1 + sx;                                               // :264
+    dQ[2 * N + c] = inv2 + sy;
+  }
+}
+
+// Wet/dry diagnostic flags (src/fvm/discretization/process_dry_wet.jl:2-35).
+// Recomputed by the reference each RHS call but never consumed by fluxes or
+// sources; kept here as a diagnostic only.
+inline void dry_wet_flags(const Mesh& m, const std::vector<double>& h, const std::vector<double>& zb, double h_small,
+                          std::vector<char>& wet, std::vector<char>& adjDry, std::vector<char>& adjHighDry) {
+  int N = m.nCells;
+  wet.assign(N, 0); adjDry.assign(N, 0); adjHighDry.assign(N, 0);
+  for (int c = 0; c < N; ++c) wet[c] = h[c] > h_small;
+  for (int c = 0; c < N; ++c)
+    for (int i = 0; i < m.cellNodesCount[c]; ++i) {
+      int f = m.cellFaces[(size_t)c * 8 + i], nb = m.cellNeighbors[(size_t)c * 8 + i];
+      bool bnd = m.faceIsBoundary[f];
+      if (bnd || !wet[nb]) adjDry[c] = 1;
+      if (bnd || (!wet[nb] && (h[c] + zb[c]) < zb[nb])) adjHighDry[c] = 1;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Time stepping.
+// ---------------------------------------------------------------------------
+// Forward Euler with the reference's clamp (custom_ODE_solvers.jl:5-33): the
+// first state block is compared with h_small as if it were h.
+template <class T>
+void euler_step_reference(const Case& cs, const Params<T>& p, std::vector<T>& Q, double dt, int nthreads = 1) {
+  const int N = cs.mesh.nCells;
+  std::vector<T> dQ(3 * (size_t)N);
+  rhs<T>(cs, p, Q.data(), dQ.data(), nthreads);
+  for (size_t k = 0; k < Q.size(); ++k) Q[k] = Q[k] + dt * dQ[k];
+  for (int i = 0; i < N; ++i)
+    if (value(Q[i]) < cs.k.h_small) { Q[i] = T(cs.k.h_small); Q[N + i] = T(0.0); Q[2 * N + i] = T(0.0); }
+}
+
+// Depth-positivity clamp applied after each explicit stage: where
+// h = xi + hstill < h_small, set h = h_small (xi = h_small - hstill) and q = 0.
+// With hstill = 0 this is exactly custom_ODE_update_cells' clamp
+// (custom_ODE_solvers.jl:18-26); for hstill != 0 it clamps the depth, not xi.
+template <class T>
+inline void clamp_stage(const Case& cs, T* Q) {
+  const int N = cs.mesh.nCells;
+  for (int i = 0; i < N; ++i)
+    if (value(Q[i]) + cs.hstill[i] < cs.k.h_small) {
+      Q[i] = T(cs.k.h_small - cs.hstill[i]);
+      Q[N + i] = T(0.0);
+      Q[2 * N + i] = T(0.0);
+    }
+}
+
+// CFL time step from the state Q: dt = CFL * min_c A_c / sum_f L_f (|u.n_f| + sqrt(g h)),
+// with the clamped h, u = qx/h, v = qy/h of cell c and its outward normals.
+// (The reference stores CFL = 0.4 but never uses it, solve_swe_2D.jl:86.)
+inline double cfl_dt(const Case& cs, const double* Q, double cfl) {
+  const Mesh& m = cs.mesh;
+  const int N = m.nCells;
+  double best = INFINITY;
+  for (int c = 0; c < N; ++c) {
+    double h = Q[c] + cs.hstill[c];
+    double qx = Q[N + c], qy = Q[2 * N + c];
+    if (h <= cs.k.h_small) { h = cs.k.h_small; qx = 0.0; qy = 0.0; }
+    double u = qx / h, v = qy / h, a = std::sqrt(cs.k.g * h);
+    double s = 0.0;
+    for (int i = 0; i < m.cellNodesCount[c]; ++i) {
+      double nx = m.cellNormals[(size_t)c * 16 + 2 * i], ny = m.cellNormals[(size_t)c * 16 + 2 * i + 1];
+      s += m.faceLengths[m.cellFaces[(size_t)c * 8 + i]] * (std::fabs(u * nx + v * ny) + a);
+    }
+    double r = m.cellAreas[c] / s;
+    if (r < best) best = r;
+  }
+  return cfl * best;
+}
+
+// One SSP-RK2 (Heun) step: Q1 = C(Q0 + dt R(Q0)); Q2 = C(0.5*(Q0 + (Q1 + dt R(Q1)))).
+template <class T>
+void rk2_step(const Case& cs, const Params<T>& p, std::vector<T>& Q, double dt, int nthreads = 1) {
+  const size_t n3 = Q.size();
+  std::vector<T> R(n3), Q1(n3);
+  rhs<T>(cs, p, Q.data(), R.data(), nthreads);
+  for (size_t k = 0; k < n3; ++k) Q1[k] = Q[k] + dt * R[k];
+  clamp_stage<T>(cs, Q1.data());
+  rhs<T>(cs, p, Q1.data(), R.data(), nthreads);
+  for (size_t k = 0; k < n3; ++k) Q[k] = 0.5 * (Q[k] + (Q1[k] + dt * R[k]));
+  clamp_stage<T>(cs, Q.data());
+}
+
+}  // namespace hgo
