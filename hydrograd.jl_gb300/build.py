@@ -1,0 +1,66 @@
+"""Build libhydrograd_gb.so in-tree (hydrograd.jl_gb300/build/) for sm_103a.
+
+CUDA sources go through nvcc with one -gencode (compute_103a -> sm_103a);
+host C++ sources through g++ with -ffp-contract=off, so that mesh geometry
+and bed slopes are computed with exactly the reference's rounding on x86_64
+and aarch64 alike.  Translation units compile in parallel.
+"""
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+CSRC = os.path.join(HERE, "csrc")
+OUT = os.path.join(HERE, "build")
+LIB = os.path.join(OUT, "libhydrograd_gb.so")
+INCLUDE = os.path.join(ROOT, "include")
+
+CUDA_SOURCES = ["hg_forward.cu", "hg_adjoint_kernels.cu"]
+CXX_SOURCES = ["hg_mesh.cpp", "hg_capi.cpp", "hg_adjoint.cpp"]
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def _cuda_home():
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    return os.path.dirname(os.path.dirname(os.path.realpath(nvcc))), nvcc
+
+
+def _run(cmd):
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("build failed:\n" + " ".join(cmd) + "\n" + r.stdout + r.stderr)
+    return r.stdout + r.stderr
+
+
+def build(verbose=False):
+    cuda_home, nvcc = _cuda_home()
+    os.makedirs(OUT, exist_ok=True)
+    jobs = []
+    objs = []
+    for src in CUDA_SOURCES:
+        if not os.path.exists(os.path.join(CSRC, src)):
+            continue
+        obj = os.path.join(OUT, src + ".o")
+        objs.append(obj)
+        jobs.append([nvcc, "-std=c++17", "-O3", *ARCH, "-lineinfo", "-Xcompiler", "-fPIC", "-I", INCLUDE,
+                     "-c", os.path.join(CSRC, src), "-o", obj])
+    for src in CXX_SOURCES:
+        obj = os.path.join(OUT, src + ".o")
+        objs.append(obj)
+        jobs.append(["g++", "-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-Wall", "-I", INCLUDE,
+                     "-I", os.path.join(cuda_home, "include"), "-c", os.path.join(CSRC, src), "-o", obj])
+    with ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
+        logs = list(ex.map(_run, jobs))
+    if verbose:
+        for log in logs:
+            if log.strip():
+                print(log)
+    _run([nvcc, "-shared", *ARCH, "-o", LIB, *objs, "-lcudart_static", "-lrt", "-lpthread", "-ldl"])
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(verbose="-v" in sys.argv))

@@ -1,0 +1,783 @@
+// C ABI implementation: context lifecycle, parameter upload, host<->device
+// state transfer, and the step sequences (graph-captured on request).
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <new>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "hg_adjoint.hpp"
+#include "hg_ctx.hpp"
+#include "hg_mesh.hpp"
+#include "hg_state.hpp"
+#include "hydrograd_gb.h"
+
+using namespace hg;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(hg_ctx* ctx, int code, const std::string& msg) {
+  if (ctx) ctx->err = msg;
+  else g_err = msg;
+  return code;
+}
+
+#define HG_CUDA(ctx, call)                                                                        \
+  do {                                                                                            \
+    cudaError_t e_ = (call);                                                                      \
+    if (e_ != cudaSuccess)                                                                        \
+      return fail((ctx), HG_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));        \
+  } while (0)
+
+template <class T>
+cudaError_t dalloc(hg_ctx* c, T** p, size_t count) {
+  void* q = nullptr;
+  cudaError_t e = cudaMalloc(&q, count * sizeof(T) + 16);
+  if (e == cudaSuccess) {
+    c->allocs.push_back(q);
+    *p = static_cast<T*>(q);
+  }
+  return e;
+}
+
+template <class T>
+cudaError_t upload(hg_ctx* c, T* d, const std::vector<T>& h) {
+  if (h.empty()) return cudaSuccess;
+  return cudaMemcpyAsync(d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, c->stream);
+}
+
+std::vector<float> to_float(const std::vector<double>& v) {
+  std::vector<float> r(v.size());
+  for (size_t i = 0; i < v.size(); ++i) r[i] = (float)v[i];
+  return r;
+}
+
+// Bed data from zb at cells (process_bed_2D.jl:46-66; fvm_schemes_2D.jl:197-213,253-275),
+// in the reference's operation order.  Outputs in the caller's cell order.
+void compute_bed(const HostMesh& m, const std::vector<double>& zb, std::vector<double>& s0x, std::vector<double>& s0y) {
+  std::vector<double> zf(m.nFaces);
+  for (int f = 0; f < m.nFaces; ++f)
+    zf[f] = m.faceC1[f] >= 0 ? (zb[m.faceC0[f]] + zb[m.faceC1[f]]) / 2.0 : zb[m.faceC0[f]];
+  s0x.assign(m.nCells, 0.0);
+  s0y.assign(m.nCells, 0.0);
+  for (int c = 0; c < m.nCells; ++c) {
+    double gx = 0.0, gy = 0.0;
+    for (int i = 0; i < m.ncf[c]; ++i) {
+      const int f = m.cf[(size_t)c * 8 + i];
+      gx = gx + m.snx[(size_t)c * 8 + i] * zf[f] * m.faceLen[f];
+      gy = gy + m.sny[(size_t)c * 8 + i] * zf[f] * m.faceLen[f];
+    }
+    s0x[c] = -1.0 * (gx / m.area[c]);
+    s0y[c] = -1.0 * (gy / m.area[c]);
+  }
+}
+
+template <class T>
+std::vector<T> to_device_order(const hg_ctx* c, const T* user) {
+  std::vector<T> r(c->n);
+  for (int i = 0; i < c->n; ++i) r[i] = user[c->perm[i]];
+  return r;
+}
+
+int upload_cells(hg_ctx* c) {
+  // FP64 and FP32 copies of the per-cell parameters, in device order.
+  std::vector<double> hst = to_device_order(c, c->hstill.data());
+  std::vector<double> zb = to_device_order(c, c->zbCell.data());
+  std::vector<double> man = to_device_order(c, c->manning.data());
+  std::vector<double> s0x = to_device_order(c, c->s0x.data());
+  std::vector<double> s0y = to_device_order(c, c->s0y.data());
+  HG_CUDA(c, upload(c, c->d_hst, hst));
+  HG_CUDA(c, upload(c, c->d_zb, zb));
+  HG_CUDA(c, upload(c, c->d_man, man));
+  HG_CUDA(c, upload(c, c->d_s0x, s0x));
+  HG_CUDA(c, upload(c, c->d_s0y, s0y));
+  std::vector<float> hhi(c->n), hlo(c->n);
+  for (int i = 0; i < c->n; ++i) {
+    hhi[i] = (float)hst[i];
+    hlo[i] = (float)(hst[i] - (double)hhi[i]);
+  }
+  c->h_hsthi = hhi;
+  c->h_hstlo = hlo;
+  HG_CUDA(c, upload(c, c->d_hsthi, hhi));
+  HG_CUDA(c, upload(c, c->d_hstlo, hlo));
+  c->h_zbf = to_float(zb);
+  c->h_manf = to_float(man);
+  c->h_s0xf = to_float(s0x);
+  c->h_s0yf = to_float(s0y);
+  HG_CUDA(c, upload(c, c->d_zbf, c->h_zbf));
+  HG_CUDA(c, upload(c, c->d_manf, c->h_manf));
+  HG_CUDA(c, upload(c, c->d_s0xf, c->h_s0xf));
+  HG_CUDA(c, upload(c, c->d_s0yf, c->h_s0yf));
+  HG_CUDA(c, cudaStreamSynchronize(c->stream));
+  return HG_OK;
+}
+
+int upload_boundary_values(hg_ctx* c) {
+  HG_CUDA(c, upload(c, c->d_inletQ, c->inletQ));
+  HG_CUDA(c, upload(c, c->d_exitWse, c->exitWse));
+  HG_CUDA(c, cudaStreamSynchronize(c->stream));
+  return HG_OK;
+}
+
+int check_flags(hg_ctx* c) {
+  int32_t f = 0;
+  HG_CUDA(c, cudaMemcpyAsync(&f, c->ds.flags, sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream));
+  HG_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (f & 2) return fail(c, HG_ERR_INLET, "inlet-Q total conveyance is not positive (all inlet cells dry?)");
+  if (f & 1) return fail(c, HG_ERR_STATE, "non-finite value in the state");
+  return HG_OK;
+}
+
+int ensure_dt_capacity(hg_ctx* c, int32_t steps) {
+  if (steps <= c->ds.dtCap) return HG_OK;
+  int32_t cap = std::max(steps, 2 * c->ds.dtCap);
+  double* p = nullptr;
+  HG_CUDA(c, cudaMalloc(&p, (size_t)cap * sizeof(double)));
+  if (c->ds.dtHist) cudaFree(c->ds.dtHist);
+  c->ds.dtHist = p;
+  c->ds.dtCap = cap;
+  c->graphValid = false;   // the captured scalars struct holds the old pointer
+  return HG_OK;
+}
+
+StateF32 xa(hg_ctx* c) { return StateF32{c->XAhi, c->XAlo}; }
+StateF32 xb(hg_ctx* c) { return StateF32{c->XBhi, c->XBlo}; }
+
+// Enqueue the state upload from a host buffer (caller order).
+int enqueue_upload(hg_ctx* c, const double* Q) {
+  HG_CUDA(c, cudaMemcpyAsync(c->Quser, Q, (size_t)3 * c->n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  if (c->precision == HG_FP64) launch_gather_state_f64(c->n, c->d_perm, c->Quser, c->QA, c->stream);
+  else launch_gather_state_f32(c->n, c->d_perm, c->Quser, xa(c), c->stream);
+  c->launches += 1;
+  return HG_OK;
+}
+
+int enqueue_download(hg_ctx* c, double* Q) {
+  if (c->precision == HG_FP64) launch_scatter_state_f64(c->n, c->d_perm, c->QA, c->Quser, c->stream);
+  else launch_scatter_state_f32(c->n, c->d_perm, xa(c), c->Quser, c->stream);
+  c->launches += 1;
+  HG_CUDA(c, cudaMemcpyAsync(Q, c->Quser, (size_t)3 * c->n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  return HG_OK;
+}
+
+// One SSP-RK2 step on the resident state (QA / XA).  Kernels per step:
+// step_begin, [inlet], stage1, [inlet], stage2.
+void enqueue_rk2_step(hg_ctx* c, bool cflMode, double cfl) {
+  launch_step_begin(c->ds, cflMode, cfl, c->stream);
+  if (c->precision == HG_FP64) {
+    launch_inlet_total_f64(c->dm, c->ds, c->QA, c->stream);
+    launch_stage_f64(c->dm, c->ds, kModeStage1, c->QA, nullptr, c->QB, false, c->stream);
+    launch_inlet_total_f64(c->dm, c->ds, c->QB, c->stream);
+    launch_stage_f64(c->dm, c->ds, kModeStage2, c->QB, c->QA, c->QA, cflMode, c->stream);
+  } else {
+    launch_inlet_total_f32(c->dm, c->ds, xa(c), c->stream);
+    launch_stage_f32(c->dm, c->ds, kModeStage1, xa(c), StateF32{}, xb(c), nullptr, false, c->stream);
+    launch_inlet_total_f32(c->dm, c->ds, xb(c), c->stream);
+    launch_stage_f32(c->dm, c->ds, kModeStage2, xb(c), xa(c), xa(c), nullptr, cflMode, c->stream);
+  }
+  c->launches += 3 + (c->dm.nInlet > 0 ? 2 : 0);
+}
+
+void enqueue_euler_step(hg_ctx* c, bool cflMode, double cfl) {
+  launch_step_begin(c->ds, cflMode, cfl, c->stream);
+  if (c->precision == HG_FP64) {
+    launch_inlet_total_f64(c->dm, c->ds, c->QA, c->stream);
+    launch_stage_f64(c->dm, c->ds, kModeEulerRef, c->QA, nullptr, c->QB, false, c->stream);
+    if (cflMode) launch_cfl_f64(c->dm, c->ds, c->QB, c->stream);
+    std::swap(c->QA, c->QB);
+  } else {
+    launch_inlet_total_f32(c->dm, c->ds, xa(c), c->stream);
+    launch_stage_f32(c->dm, c->ds, kModeEulerRef, xa(c), StateF32{}, xb(c), nullptr, false, c->stream);
+    if (cflMode) launch_cfl_f32(c->dm, c->ds, xb(c), c->stream);
+    std::swap(c->XAhi, c->XBhi);
+    std::swap(c->XAlo, c->XBlo);
+  }
+  c->launches += 2 + (c->dm.nInlet > 0 ? 1 : 0) + (cflMode ? 1 : 0);
+}
+
+void enqueue_cfl_prime(hg_ctx* c) {
+  if (c->precision == HG_FP64) launch_cfl_f64(c->dm, c->ds, c->QA, c->stream);
+  else launch_cfl_f32(c->dm, c->ds, xa(c), c->stream);
+  c->launches += 1;
+}
+
+int set_fixed_dt(hg_ctx* c, double dt) {
+  float dtf = (float)dt;
+  HG_CUDA(c, cudaMemcpyAsync(c->ds.dt, &dt, sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  HG_CUDA(c, cudaMemcpyAsync(c->ds.dtf, &dtf, sizeof(float), cudaMemcpyHostToDevice, c->stream));
+  HG_CUDA(c, cudaStreamSynchronize(c->stream));
+  return HG_OK;
+}
+
+}  // namespace
+
+hg_ctx::~hg_ctx() {
+  if (graphExec) cudaGraphExecDestroy(graphExec);
+  if (stream) cudaStreamSynchronize(stream);
+  for (void* p : allocs) cudaFree(p);
+  if (ds.dtHist) cudaFree(ds.dtHist);
+  adjoint_release(this);
+  if (stream) cudaStreamDestroy(stream);
+}
+
+extern "C" {
+
+int hg_abi_version(void) { return HG_ABI_VERSION; }
+
+int hg_last_error(const hg_ctx* ctx, char* buf, int32_t len) {
+  if (!buf || len <= 0) return HG_ERR_ARG;
+  const std::string& s = ctx ? ctx->err : g_err;
+  std::snprintf(buf, (size_t)len, "%s", s.c_str());
+  return HG_OK;
+}
+
+int hg_mesh_build(const hg_mesh_desc* desc, hg_mesh** out) {
+  if (!desc || !out) return fail(nullptr, HG_ERR_ARG, "hg_mesh_build: null argument");
+  *out = nullptr;
+  try {
+    auto m = std::make_unique<hg_mesh>();
+    std::string err;
+    int rc = build_host_mesh(*desc, m->m, err);
+    if (rc != HG_OK) return fail(nullptr, rc, err);
+    *out = m.release();
+    return HG_OK;
+  } catch (const std::bad_alloc&) {
+    return fail(nullptr, HG_ERR_ARG, "hg_mesh_build: out of host memory");
+  }
+}
+
+int hg_mesh_free(hg_mesh* mesh) {
+  delete mesh;
+  return HG_OK;
+}
+
+static int sizes_of(const HostMesh& m, int32_t* s) {
+  s[0] = m.nCells; s[1] = m.nFaces; s[2] = m.nGhost;
+  s[3] = (int32_t)m.inletGroups.size(); s[4] = (int32_t)m.exitGroups.size();
+  s[5] = (int32_t)m.wallGroups.size(); s[6] = (int32_t)m.symmGroups.size();
+  s[7] = m.maxCellFaces;
+  return HG_OK;
+}
+
+int hg_mesh_sizes(const hg_mesh* mesh, int32_t* sizes8) {
+  if (!mesh || !sizes8) return fail(nullptr, HG_ERR_ARG, "hg_mesh_sizes: null argument");
+  return sizes_of(mesh->m, sizes8);
+}
+
+int hg_mesh_cell_faces(const hg_mesh* mesh, int32_t* nbr8, double* normals16, double* lengths8, double* areas,
+                       double* centroids2) {
+  if (!mesh) return fail(nullptr, HG_ERR_ARG, "hg_mesh_cell_faces: null mesh");
+  const HostMesh& m = mesh->m;
+  for (int c = 0; c < m.nCells; ++c) {
+    for (int i = 0; i < 8; ++i) {
+      const bool has = i < m.ncf[c];
+      const size_t k = (size_t)c * 8 + i;
+      if (nbr8) nbr8[k] = has ? m.nbr[k] : -2;
+      if (normals16) {
+        normals16[2 * k] = has ? m.snx[k] : 0.0;
+        normals16[2 * k + 1] = has ? m.sny[k] : 0.0;
+      }
+      if (lengths8) lengths8[k] = has ? m.faceLen[m.cf[k]] : 0.0;
+    }
+    if (areas) areas[c] = m.area[c];
+    if (centroids2) { centroids2[2 * c] = m.cx[c]; centroids2[2 * c + 1] = m.cy[c]; }
+  }
+  return HG_OK;
+}
+
+int hg_mesh_order(const hg_mesh* mesh, int32_t order, int32_t* perm) {
+  if (!mesh || !perm) return fail(nullptr, HG_ERR_ARG, "hg_mesh_order: null argument");
+  std::vector<int> p = order_cells(mesh->m, order);
+  std::memcpy(perm, p.data(), p.size() * sizeof(int32_t));
+  return HG_OK;
+}
+
+int hg_create(const hg_mesh_desc* desc, const hg_consts* consts, int32_t precision, int32_t device, hg_ctx** out) {
+  if (!desc || !consts || !out) return fail(nullptr, HG_ERR_ARG, "hg_create: null argument");
+  *out = nullptr;
+  if (precision != HG_FP64 && precision != HG_FP32C) return fail(nullptr, HG_ERR_ARG, "hg_create: bad precision");
+  if (consts->riemann != HG_ROE)
+    return fail(nullptr, HG_ERR_UNSUPPORTED, "hg_create: only the Roe solver exists (semi_discretize_swe_2D.jl:352-362)");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0)
+    return fail(nullptr, HG_ERR_NO_DEVICE, "hg_create: no CUDA device (this library has no CPU fallback)");
+  if (device < 0 || device >= ndev) return fail(nullptr, HG_ERR_ARG, "hg_create: bad device index");
+  std::unique_ptr<hg_ctx> c(new (std::nothrow) hg_ctx());
+  if (!c) return fail(nullptr, HG_ERR_ARG, "hg_create: out of host memory");
+  std::string err;
+  int rc = build_host_mesh(*desc, c->hm, err);
+  if (rc != HG_OK) return fail(nullptr, rc, err);
+  c->k = *consts;
+  c->precision = precision;
+  c->device = device;
+  if (cudaSetDevice(device) != cudaSuccess) return fail(nullptr, HG_ERR_CUDA, "hg_create: cudaSetDevice failed");
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess)
+    return fail(nullptr, HG_ERR_CUDA, "hg_create: cudaStreamCreate failed");
+  rc = ctx_setup_device(c.get());
+  if (rc != HG_OK) {
+    std::string msg = c->err;
+    return fail(nullptr, rc, msg);
+  }
+  *out = c.release();
+  return HG_OK;
+}
+
+int hg_destroy(hg_ctx* ctx) {
+  if (ctx) cudaSetDevice(ctx->device);
+  delete ctx;
+  return HG_OK;
+}
+
+int hg_sizes(const hg_ctx* ctx, int32_t* sizes8) {
+  if (!ctx || !sizes8) return fail(nullptr, HG_ERR_ARG, "hg_sizes: null argument");
+  return sizes_of(ctx->hm, sizes8);
+}
+
+int hg_set_still_water(hg_ctx* ctx, const double* wstill) {
+  if (!ctx || !wstill) return fail(ctx, HG_ERR_ARG, "hg_set_still_water: null argument");
+  cudaSetDevice(ctx->device);
+  for (int i = 0; i < ctx->n; ++i) ctx->hstill[i] = wstill[i] - ctx->zbCell[i];   // process_ICs_2D.jl:55
+  return upload_cells(ctx);
+}
+
+int hg_set_manning_zones(hg_ctx* ctx, const int32_t* mat_id, int32_t n_zones, const double* n_zone) {
+  if (!ctx || !mat_id || !n_zone || n_zones <= 0) return fail(ctx, HG_ERR_ARG, "hg_set_manning_zones: bad argument");
+  for (int i = 0; i < ctx->n; ++i) {
+    if (mat_id[i] < 0 || mat_id[i] >= n_zones)
+      return fail(ctx, HG_ERR_ARG, "hg_set_manning_zones: cell " + std::to_string(i) + " has zone " +
+                                       std::to_string(mat_id[i]) + " outside [0, n_zones)");
+  }
+  cudaSetDevice(ctx->device);
+  for (int i = 0; i < ctx->n; ++i) ctx->manning[i] = n_zone[mat_id[i]];   // process_ManningN_2D.jl:259
+  return upload_cells(ctx);
+}
+
+int hg_set_manning_cells(hg_ctx* ctx, const double* n) {
+  if (!ctx || !n) return fail(ctx, HG_ERR_ARG, "hg_set_manning_cells: null argument");
+  cudaSetDevice(ctx->device);
+  ctx->manning.assign(n, n + ctx->n);
+  return upload_cells(ctx);
+}
+
+int hg_set_zb_cells(hg_ctx* ctx, const double* zb) {
+  if (!ctx || !zb) return fail(ctx, HG_ERR_ARG, "hg_set_zb_cells: null argument");
+  cudaSetDevice(ctx->device);
+  ctx->zbCell.assign(zb, zb + ctx->n);
+  compute_bed(ctx->hm, ctx->zbCell, ctx->s0x, ctx->s0y);
+  return upload_cells(ctx);
+}
+
+int hg_set_inlet_q(hg_ctx* ctx, const double* q, int32_t n) {
+  if (!ctx || (n > 0 && !q) || n != (int32_t)ctx->inletQ.size())
+    return fail(ctx, HG_ERR_ARG, "hg_set_inlet_q: expected one value per inlet-Q boundary");
+  cudaSetDevice(ctx->device);
+  ctx->inletQ.assign(q, q + n);
+  return upload_boundary_values(ctx);
+}
+
+int hg_set_exit_wse(hg_ctx* ctx, const double* w, int32_t n) {
+  if (!ctx || (n > 0 && !w) || n != (int32_t)ctx->exitWse.size())
+    return fail(ctx, HG_ERR_ARG, "hg_set_exit_wse: expected one value per exit-H boundary");
+  cudaSetDevice(ctx->device);
+  ctx->exitWse.assign(w, w + n);
+  return upload_boundary_values(ctx);
+}
+
+int hg_get_bed(hg_ctx* ctx, double* zb, double* S0, double* man, double* hstill) {
+  if (!ctx) return fail(ctx, HG_ERR_ARG, "hg_get_bed: null context");
+  for (int i = 0; i < ctx->n; ++i) {
+    if (zb) zb[i] = ctx->zbCell[i];
+    if (S0) { S0[2 * i] = ctx->s0x[i]; S0[2 * i + 1] = ctx->s0y[i]; }
+    if (man) man[i] = ctx->manning[i];
+    if (hstill) hstill[i] = ctx->hstill[i];
+  }
+  return HG_OK;
+}
+
+int hg_check_initial_state(hg_ctx* ctx, const double* Q) {
+  if (!ctx || !Q) return fail(ctx, HG_ERR_ARG, "hg_check_initial_state: null argument");
+  for (int i = 0; i < ctx->n; ++i) {
+    const double h = Q[i] + ctx->hstill[i];
+    if (!std::isfinite(Q[i]) || !std::isfinite(Q[ctx->n + i]) || !std::isfinite(Q[2 * ctx->n + i]))
+      return fail(ctx, HG_ERR_STATE, "initial state is not finite at cell " + std::to_string(i));
+    if (h < ctx->k.h_small)
+      return fail(ctx, HG_ERR_STATE, "initial depth " + std::to_string(h) + " at cell " + std::to_string(i) +
+                                         " is below h_small (process_ICs_2D.jl:97-99)");
+  }
+  return HG_OK;
+}
+
+int hg_rhs(hg_ctx* ctx, const double* Q, double /*t*/, double* dQ) {
+  if (!ctx || !Q || !dQ) return fail(ctx, HG_ERR_ARG, "hg_rhs: null argument");
+  cudaSetDevice(ctx->device);
+  launch_reset_scalars(ctx->ds, ctx->stream);
+  int rc = enqueue_upload(ctx, Q);
+  if (rc) return rc;
+  if (ctx->precision == HG_FP64) {
+    launch_inlet_total_f64(ctx->dm, ctx->ds, ctx->QA, ctx->stream);
+    launch_stage_f64(ctx->dm, ctx->ds, kModeRhs, ctx->QA, nullptr, ctx->QB, false, ctx->stream);
+    launch_scatter_state_f64(ctx->n, ctx->d_perm, ctx->QB, ctx->Quser, ctx->stream);
+  } else {
+    launch_inlet_total_f32(ctx->dm, ctx->ds, xa(ctx), ctx->stream);
+    launch_stage_f32(ctx->dm, ctx->ds, kModeRhs, xa(ctx), StateF32{}, StateF32{}, ctx->QB, false, ctx->stream);
+    launch_scatter_state_f64(ctx->n, ctx->d_perm, ctx->QB, ctx->Quser, ctx->stream);
+  }
+  ctx->launches += 4;
+  HG_CUDA(ctx, cudaMemcpyAsync(dQ, ctx->Quser, (size_t)3 * ctx->n * sizeof(double), cudaMemcpyDeviceToHost,
+                               ctx->stream));
+  HG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  HG_CUDA(ctx, cudaGetLastError());
+  return check_flags(ctx);
+}
+
+int hg_integrate(hg_ctx* ctx, double* Q, double /*t0*/, int32_t nsteps, int32_t method, double dt, double cfl,
+                 int32_t save_every, double* saves, double* dts_out) {
+  if (!ctx || !Q || nsteps < 0) return fail(ctx, HG_ERR_ARG, "hg_integrate: bad argument");
+  if (method != 0 && method != 1) return fail(ctx, HG_ERR_ARG, "hg_integrate: method must be 0 (SSP-RK2) or 1 (Euler)");
+  if (save_every > 0 && !saves) return fail(ctx, HG_ERR_ARG, "hg_integrate: saves is NULL");
+  if (dt <= 0 && !(cfl > 0)) return fail(ctx, HG_ERR_ARG, "hg_integrate: need dt > 0 or cfl > 0");
+  cudaSetDevice(ctx->device);
+  int rc = ensure_dt_capacity(ctx, nsteps);
+  if (rc) return rc;
+  launch_reset_scalars(ctx->ds, ctx->stream);
+  rc = enqueue_upload(ctx, Q);
+  if (rc) return rc;
+  const bool cflMode = dt <= 0;
+  if (!cflMode) {
+    rc = set_fixed_dt(ctx, dt);
+    if (rc) return rc;
+  } else {
+    enqueue_cfl_prime(ctx);
+  }
+  int saved = 0;
+  for (int s = 0; s < nsteps; ++s) {
+    if (method == 0) enqueue_rk2_step(ctx, cflMode, cfl);
+    else enqueue_euler_step(ctx, cflMode, cfl);
+    if (save_every > 0 && (s + 1) % save_every == 0) {
+      rc = enqueue_download(ctx, saves + (size_t)saved * 3 * ctx->n);
+      if (rc) return rc;
+      ++saved;
+    }
+  }
+  ctx->cflPrimed = cflMode;
+  rc = enqueue_download(ctx, Q);
+  if (rc) return rc;
+  if (dts_out && nsteps > 0)
+    HG_CUDA(ctx, cudaMemcpyAsync(dts_out, ctx->ds.dtHist, (size_t)nsteps * sizeof(double), cudaMemcpyDeviceToHost,
+                                 ctx->stream));
+  HG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  HG_CUDA(ctx, cudaGetLastError());
+  return check_flags(ctx);
+}
+
+int hg_state_upload(hg_ctx* ctx, const double* Q) {
+  if (!ctx || !Q) return fail(ctx, HG_ERR_ARG, "hg_state_upload: null argument");
+  cudaSetDevice(ctx->device);
+  launch_reset_scalars(ctx->ds, ctx->stream);
+  int rc = enqueue_upload(ctx, Q);
+  if (rc) return rc;
+  ctx->cflPrimed = false;
+  HG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return HG_OK;
+}
+
+int hg_state_download(hg_ctx* ctx, double* Q) {
+  if (!ctx || !Q) return fail(ctx, HG_ERR_ARG, "hg_state_download: null argument");
+  cudaSetDevice(ctx->device);
+  int rc = enqueue_download(ctx, Q);
+  if (rc) return rc;
+  HG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return check_flags(ctx);
+}
+
+int hg_advance(hg_ctx* ctx, int32_t nsteps, double dt, double cfl, int32_t graph) {
+  if (!ctx || nsteps < 0) return fail(ctx, HG_ERR_ARG, "hg_advance: bad argument");
+  if (dt <= 0 && !(cfl > 0)) return fail(ctx, HG_ERR_ARG, "hg_advance: need dt > 0 or cfl > 0");
+  cudaSetDevice(ctx->device);
+  const bool cflMode = dt <= 0;
+  if (!cflMode) {
+    int rc = set_fixed_dt(ctx, dt);
+    if (rc) return rc;
+  } else if (!ctx->cflPrimed) {
+    enqueue_cfl_prime(ctx);
+  }
+  int done = 0;
+  if (graph) {
+    const int K = kGraphSteps;
+    if (nsteps >= K) {
+      if (!ctx->graphValid || ctx->graphCflMode != cflMode || ctx->graphCfl != cfl) {
+        if (ctx->graphExec) {
+          cudaGraphExecDestroy(ctx->graphExec);
+          ctx->graphExec = nullptr;
+        }
+        cudaGraph_t g;
+        HG_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+        int64_t before = ctx->launches;
+        for (int s = 0; s < K; ++s) enqueue_rk2_step(ctx, cflMode, cfl);
+        ctx->graphLaunches = ctx->launches - before;
+        ctx->launches = before;
+        HG_CUDA(ctx, cudaStreamEndCapture(ctx->stream, &g));
+        cudaError_t e = cudaGraphInstantiate(&ctx->graphExec, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return fail(ctx, HG_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+        ctx->graphValid = true;
+        ctx->graphCflMode = cflMode;
+        ctx->graphCfl = cfl;
+      }
+      for (; done + K <= nsteps; done += K) {
+        HG_CUDA(ctx, cudaGraphLaunch(ctx->graphExec, ctx->stream));
+        ctx->launches += ctx->graphLaunches;
+      }
+    }
+  }
+  for (; done < nsteps; ++done) enqueue_rk2_step(ctx, cflMode, cfl);
+  ctx->cflPrimed = cflMode;
+  HG_CUDA(ctx, cudaGetLastError());
+  return HG_OK;
+}
+
+int hg_synchronize(hg_ctx* ctx) {
+  if (!ctx) return fail(ctx, HG_ERR_ARG, "hg_synchronize: null context");
+  cudaSetDevice(ctx->device);
+  HG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return check_flags(ctx);
+}
+
+int hg_elapsed_time(hg_ctx* ctx, double* t) {
+  if (!ctx || !t) return fail(ctx, HG_ERR_ARG, "hg_elapsed_time: null argument");
+  cudaSetDevice(ctx->device);
+  HG_CUDA(ctx, cudaMemcpyAsync(t, ctx->ds.tSum, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  HG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return HG_OK;
+}
+
+int hg_launch_count(const hg_ctx* ctx, int64_t* count) {
+  if (!ctx || !count) return fail(nullptr, HG_ERR_ARG, "hg_launch_count: null argument");
+  *count = ctx->launches;
+  return HG_OK;
+}
+
+int hg_flush_l2(hg_ctx* ctx) {
+  if (!ctx) return fail(ctx, HG_ERR_ARG, "hg_flush_l2: null context");
+  cudaSetDevice(ctx->device);
+  launch_flush(ctx->flushBuf, ctx->flushBytes, ctx->stream);
+  ctx->launches += 1;
+  HG_CUDA(ctx, cudaGetLastError());
+  return HG_OK;
+}
+
+int hg_time_stage_kernel(hg_ctx* ctx, int32_t n, int32_t flush_l2, double* avg_ms) {
+  if (!ctx || n <= 0 || !avg_ms) return fail(ctx, HG_ERR_ARG, "hg_time_stage_kernel: bad argument");
+  cudaSetDevice(ctx->device);
+  cudaEvent_t a, b;
+  HG_CUDA(ctx, cudaEventCreate(&a));
+  HG_CUDA(ctx, cudaEventCreate(&b));
+  double total = 0.0;
+  for (int i = 0; i < n; ++i) {
+    if (flush_l2) launch_flush(ctx->flushBuf, ctx->flushBytes, ctx->stream);
+    cudaEventRecord(a, ctx->stream);
+    if (ctx->precision == HG_FP64)
+      launch_stage_f64(ctx->dm, ctx->ds, kModeStage1, ctx->QA, nullptr, ctx->QB, false, ctx->stream);
+    else
+      launch_stage_f32(ctx->dm, ctx->ds, kModeStage1, xa(ctx), StateF32{}, xb(ctx), nullptr, false, ctx->stream);
+    cudaEventRecord(b, ctx->stream);
+    cudaEventSynchronize(b);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    total += ms;
+    ctx->launches += flush_l2 ? 2 : 1;
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  *avg_ms = total / n;
+  HG_CUDA(ctx, cudaGetLastError());
+  return HG_OK;
+}
+
+int hg_loss_and_grad(hg_ctx* ctx, const double* Q0, int32_t nsteps, double dt, int32_t ckpt_every,
+                     const int32_t* probe_cells, const double* obs, int32_t n_probe, double* loss,
+                     double* g_manning_cells, double* g_zb, double* g_inletq, double* Q_final) {
+  if (!ctx || !Q0 || nsteps <= 0 || !(dt > 0) || n_probe < 0 || (n_probe > 0 && (!probe_cells || !obs)) || !loss)
+    return fail(ctx, HG_ERR_ARG, "hg_loss_and_grad: bad argument");
+  for (int i = 0; i < n_probe; ++i)
+    if (probe_cells[i] < 0 || probe_cells[i] >= ctx->n) return fail(ctx, HG_ERR_ARG, "hg_loss_and_grad: bad probe id");
+  cudaSetDevice(ctx->device);
+  return adjoint_loss_and_grad(ctx, Q0, nsteps, dt, ckpt_every, probe_cells, obs, n_probe, loss, g_manning_cells, g_zb,
+                               g_inletq, Q_final);
+}
+
+int hg_pinned_alloc(int64_t bytes, void** out) {
+  if (!out || bytes <= 0) return fail(nullptr, HG_ERR_ARG, "hg_pinned_alloc: bad argument");
+  if (cudaMallocHost(out, (size_t)bytes) != cudaSuccess) return fail(nullptr, HG_ERR_CUDA, "cudaMallocHost failed");
+  return HG_OK;
+}
+
+int hg_pinned_free(void* p) {
+  if (p) cudaFreeHost(p);
+  return HG_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Device setup (called by hg_create)
+// ---------------------------------------------------------------------------
+int ctx_setup_device(hg_ctx* c) {
+  const HostMesh& m = c->hm;
+  const int N = m.nCells;
+  c->n = N;
+  c->perm = order_cells(m, c->k.order);
+  c->inv.assign(N, 0);
+  for (int i = 0; i < N; ++i) c->inv[c->perm[i]] = i;
+  // Boundary faces, numbered by face id.
+  std::vector<int> bfOf(m.nFaces, -1);
+  int nbf = 0;
+  for (int f = 0; f < m.nFaces; ++f)
+    if (m.faceC1[f] < 0) bfOf[f] = nbf++;
+  std::vector<int> groupOf(m.bnd.size(), 0);
+  for (size_t g = 0; g < m.inletGroups.size(); ++g) groupOf[m.inletGroups[g]] = (int)g;
+  for (size_t g = 0; g < m.exitGroups.size(); ++g) groupOf[m.exitGroups[g]] = (int)g;
+  std::vector<int32_t> bfInfo(nbf, 0);
+  std::vector<double> bfLp23(nbf, 0.0);
+  for (int f = 0; f < m.nFaces; ++f) {
+    if (bfOf[f] < 0) continue;
+    const int bi = m.faceBnd[f];
+    const int type = m.bnd[bi].bc;
+    bfInfo[bfOf[f]] = type | (groupOf[bi] << 2);
+    if (type == HG_BC_INLETQ) bfLp23[bfOf[f]] = std::pow(m.faceLen[f], 2.0 / 3.0);
+  }
+  const int S = m.maxCellFaces;
+  std::vector<int32_t> nb((size_t)S * N, INT32_MIN);
+  std::vector<double> snx((size_t)S * N, 0.0), sny((size_t)S * N, 0.0), slen((size_t)S * N, 0.0);
+  for (int c2 = 0; c2 < N; ++c2) {
+    const int o = c->perm[c2];
+    for (int k = 0; k < m.ncf[o]; ++k) {
+      const size_t src = (size_t)o * 8 + k, dst = (size_t)k * N + c2;
+      const int f = m.cf[src];
+      nb[dst] = m.nbr[src] >= 0 ? c->inv[m.nbr[src]] : -1 - bfOf[f];
+      snx[dst] = m.snx[src];
+      sny[dst] = m.sny[src];
+      slen[dst] = m.faceLen[f];
+    }
+  }
+  std::vector<int32_t> inletOff(1, 0), inletCell;
+  std::vector<double> inletLp53;
+  for (int g : m.inletGroups) {
+    for (int f : m.bnd[g].faces) {
+      inletCell.push_back(c->inv[m.faceC0[f]]);
+      inletLp53.push_back(std::pow(m.faceLen[f], 5.0 / 3.0));
+    }
+    inletOff.push_back((int32_t)inletCell.size());
+  }
+  std::vector<double> area = to_device_order(c, m.area.data());
+
+  // Parameters with their defaults: zb from the nodes, hstill 0 until set,
+  // Manning n 0.03 until set, boundary values 0 until set.
+  c->zbCell = m.zbCell;
+  compute_bed(m, c->zbCell, c->s0x, c->s0y);
+  c->hstill.assign(N, 0.0);
+  c->manning.assign(N, 0.03);
+  c->inletQ.assign(m.inletGroups.size(), 0.0);
+  c->exitWse.assign(m.exitGroups.size(), 0.0);
+
+  int32_t* d_nb; double *d_snx, *d_sny, *d_slen, *d_area, *d_lp23, *d_lp53; float *d_snxf, *d_snyf, *d_slenf, *d_areaf,
+      *d_lp23f; int32_t *d_bfInfo, *d_inletOff, *d_inletCell;
+  HG_CUDA(c, dalloc(c, &d_nb, nb.size()));
+  HG_CUDA(c, dalloc(c, &d_snx, snx.size()));
+  HG_CUDA(c, dalloc(c, &d_sny, sny.size()));
+  HG_CUDA(c, dalloc(c, &d_slen, slen.size()));
+  HG_CUDA(c, dalloc(c, &d_snxf, snx.size()));
+  HG_CUDA(c, dalloc(c, &d_snyf, sny.size()));
+  HG_CUDA(c, dalloc(c, &d_slenf, slen.size()));
+  HG_CUDA(c, dalloc(c, &d_area, (size_t)N));
+  HG_CUDA(c, dalloc(c, &d_areaf, (size_t)N));
+  HG_CUDA(c, dalloc(c, &d_bfInfo, (size_t)std::max(nbf, 1)));
+  HG_CUDA(c, dalloc(c, &d_lp23, (size_t)std::max(nbf, 1)));
+  HG_CUDA(c, dalloc(c, &d_lp23f, (size_t)std::max(nbf, 1)));
+  HG_CUDA(c, dalloc(c, &d_inletOff, inletOff.size()));
+  HG_CUDA(c, dalloc(c, &d_inletCell, std::max<size_t>(inletCell.size(), 1)));
+  HG_CUDA(c, dalloc(c, &d_lp53, std::max<size_t>(inletLp53.size(), 1)));
+  for (double** p : {&c->d_hst, &c->d_zb, &c->d_man, &c->d_s0x, &c->d_s0y}) HG_CUDA(c, dalloc(c, p, (size_t)N));
+  for (float** p : {&c->d_hsthi, &c->d_hstlo, &c->d_zbf, &c->d_manf, &c->d_s0xf, &c->d_s0yf})
+    HG_CUDA(c, dalloc(c, p, (size_t)N));
+  HG_CUDA(c, dalloc(c, &c->d_inletQ, std::max<size_t>(c->inletQ.size(), 1)));
+  HG_CUDA(c, dalloc(c, &c->d_exitWse, std::max<size_t>(c->exitWse.size(), 1)));
+  HG_CUDA(c, dalloc(c, &c->d_totalA, std::max<size_t>(c->inletQ.size(), 1)));
+  HG_CUDA(c, dalloc(c, &c->d_perm, (size_t)N));
+  HG_CUDA(c, dalloc(c, &c->Quser, (size_t)3 * N));
+  HG_CUDA(c, dalloc(c, &c->QB, (size_t)3 * N));   // FP64 stage buffer; also the FP32 path's RHS output
+  if (c->precision == HG_FP64) {
+    HG_CUDA(c, dalloc(c, &c->QA, (size_t)3 * N));
+  } else {
+    for (float** p : {&c->XAhi, &c->XAlo, &c->XBhi, &c->XBlo}) HG_CUDA(c, dalloc(c, p, (size_t)3 * N));
+  }
+  // Scalars
+  HG_CUDA(c, dalloc(c, &c->ds.dt, 1));
+  HG_CUDA(c, dalloc(c, &c->ds.dtf, 1));
+  HG_CUDA(c, dalloc(c, &c->ds.cflMin, 1));
+  HG_CUDA(c, dalloc(c, &c->ds.cflMinF, 1));
+  HG_CUDA(c, dalloc(c, &c->ds.stepIdx, 1));
+  HG_CUDA(c, dalloc(c, &c->ds.tSum, 1));
+  HG_CUDA(c, dalloc(c, &c->ds.flags, 1));
+  {
+    int rc = ensure_dt_capacity(c, 1024);
+    if (rc) return rc;
+  }
+  // L2 flush buffer (larger than the 126 MB L2).
+  c->flushBytes = (size_t)256 << 20;
+  HG_CUDA(c, dalloc(c, reinterpret_cast<char**>(&c->flushBuf), c->flushBytes));
+
+  HG_CUDA(c, upload(c, d_nb, nb));
+  HG_CUDA(c, upload(c, d_snx, snx));
+  HG_CUDA(c, upload(c, d_sny, sny));
+  HG_CUDA(c, upload(c, d_slen, slen));
+  std::vector<float> snxf = to_float(snx), snyf = to_float(sny), slenf = to_float(slen), areaf = to_float(area),
+                     lp23f = to_float(bfLp23);
+  HG_CUDA(c, upload(c, d_snxf, snxf));
+  HG_CUDA(c, upload(c, d_snyf, snyf));
+  HG_CUDA(c, upload(c, d_slenf, slenf));
+  HG_CUDA(c, upload(c, d_area, area));
+  HG_CUDA(c, upload(c, d_areaf, areaf));
+  HG_CUDA(c, upload(c, d_bfInfo, bfInfo));
+  HG_CUDA(c, upload(c, d_lp23, bfLp23));
+  HG_CUDA(c, upload(c, d_lp23f, lp23f));
+  HG_CUDA(c, upload(c, d_inletOff, inletOff));
+  HG_CUDA(c, upload(c, d_inletCell, inletCell));
+  HG_CUDA(c, upload(c, d_lp53, inletLp53));
+  std::vector<int32_t> permv(c->perm.begin(), c->perm.end());
+  HG_CUDA(c, upload(c, c->d_perm, permv));
+  // Keep host copies alive until the async copies finish.
+  HG_CUDA(c, cudaStreamSynchronize(c->stream));
+
+  DevMesh& dm = c->dm;
+  dm.n = N;
+  dm.nslot = S;
+  dm.nbf = nbf;
+  dm.nInlet = (int32_t)m.inletGroups.size();
+  dm.nExit = (int32_t)m.exitGroups.size();
+  dm.nb = d_nb; dm.snx = d_snx; dm.sny = d_sny; dm.slen = d_slen;
+  dm.snxf = d_snxf; dm.snyf = d_snyf; dm.slenf = d_slenf;
+  dm.bfInfo = d_bfInfo; dm.bfLp23 = d_lp23; dm.bfLp23f = d_lp23f;
+  dm.inletOff = d_inletOff; dm.inletCell = d_inletCell; dm.inletLp53 = d_lp53;
+  dm.area = d_area; dm.hst = c->d_hst; dm.zb = c->d_zb; dm.man = c->d_man; dm.s0x = c->d_s0x; dm.s0y = c->d_s0y;
+  dm.areaf = d_areaf; dm.hsthi = c->d_hsthi; dm.hstlo = c->d_hstlo; dm.zbf = c->d_zbf; dm.manf = c->d_manf;
+  dm.s0xf = c->d_s0xf; dm.s0yf = c->d_s0yf;
+  dm.exitWse = c->d_exitWse; dm.inletQ = c->d_inletQ; dm.totalA = c->d_totalA;
+  dm.g = c->k.g; dm.kn2 = c->k.k_n * c->k.k_n; dm.hsm = c->k.h_small;
+  c->slotNb = d_nb;
+  int rc = upload_cells(c);
+  if (rc) return rc;
+  rc = upload_boundary_values(c);
+  if (rc) return rc;
+  launch_reset_scalars(c->ds, c->stream);
+  HG_CUDA(c, cudaStreamSynchronize(c->stream));
+  HG_CUDA(c, cudaGetLastError());
+  return HG_OK;
+}

@@ -1,0 +1,57 @@
+// The context behind the opaque hg_ctx handle.
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "hg_mesh.hpp"
+#include "hg_state.hpp"
+#include "hydrograd_gb.h"
+
+namespace hg {
+constexpr int kGraphSteps = 50;   // steps per captured CUDA graph
+struct AdjointBuffers;
+}  // namespace hg
+
+struct hg_ctx {
+  hg::HostMesh hm;
+  hg_consts k{};
+  int32_t precision = HG_FP64;
+  int32_t device = 0;
+  int32_t n = 0;
+  std::vector<int> perm, inv;   // perm[device id] = caller id
+  cudaStream_t stream = nullptr;
+  std::vector<void*> allocs;
+  hg::DevMesh dm;
+  hg::DevScalars ds;
+  // Parameters (caller order, FP64 host copies)
+  std::vector<double> zbCell, hstill, manning, s0x, s0y, inletQ, exitWse;
+  // FP32 host copies (device order) kept alive across async uploads
+  std::vector<float> h_hsthi, h_hstlo, h_zbf, h_manf, h_s0xf, h_s0yf;
+  // Writable device parameter arrays
+  double *d_hst = nullptr, *d_zb = nullptr, *d_man = nullptr, *d_s0x = nullptr, *d_s0y = nullptr;
+  float *d_hsthi = nullptr, *d_hstlo = nullptr, *d_zbf = nullptr, *d_manf = nullptr, *d_s0xf = nullptr,
+        *d_s0yf = nullptr;
+  double *d_inletQ = nullptr, *d_exitWse = nullptr, *d_totalA = nullptr;
+  int32_t* d_perm = nullptr;
+  const int32_t* slotNb = nullptr;
+  // State
+  double *QA = nullptr, *QB = nullptr, *Quser = nullptr;
+  float *XAhi = nullptr, *XAlo = nullptr, *XBhi = nullptr, *XBlo = nullptr;
+  void* flushBuf = nullptr;
+  size_t flushBytes = 0;
+  bool cflPrimed = false;
+  // Captured graph of kGraphSteps steps
+  cudaGraphExec_t graphExec = nullptr;
+  bool graphValid = false, graphCflMode = false;
+  double graphCfl = 0.0;
+  int64_t graphLaunches = 0;
+  int64_t launches = 0;
+  hg::AdjointBuffers* adj = nullptr;
+  std::string err;
+  ~hg_ctx();
+};
+
+int ctx_setup_device(hg_ctx* c);

@@ -1,0 +1,143 @@
+// Device-side arithmetic of the shallow-water RHS, templated on the scalar
+// (double for the FP64 path, float for the FP32-compensated path).
+//
+// Follows src/fvm/discretization/Riemman_solvers/swe_2D_solvers.jl:4-164 (Roe
+// flux with its dry/wet branches), src/utilities/smooth_functions.jl:4-52,
+// src/fvm/boundary_conditions/bc_2D.jl:640-834 (ghost states) and
+// src/fvm/discretization/semi_discretize_swe_2D.jl:449-559 (sources).
+#pragma once
+#include <cstdint>
+
+namespace hgd {
+
+// eps(Float64) from the smooth_* helpers.  The FP32 path keeps the FP64
+// constant (as an FP32 literal): eps(Float32) would floor |u.n| near 3.4e-4.
+template <class T> __device__ __forceinline__ T eps_c() { return T(2.220446049250313e-16); }
+
+template <class T> __device__ __forceinline__ T smooth_abs(T x) { return sqrt(x * x + eps_c<T>()); }
+template <class T> __device__ __forceinline__ T smooth_sqrt(T x) { return sqrt(x + eps_c<T>()); }
+template <class T> __device__ __forceinline__ T smooth_pow2(T x) { T y = x + eps_c<T>(); return y * y; }
+
+// Boundary face encoding in the slot neighbour table.
+constexpr int32_t kNoFace = INT32_MIN;
+__device__ __forceinline__ bool is_boundary(int32_t nb) { return nb < 0; }
+__device__ __forceinline__ int32_t boundary_index(int32_t nb) { return -1 - nb; }
+
+enum : int32_t { kBcWall = 0, kBcSymm = 1, kBcInletQ = 2, kBcExitH = 3 };
+
+// One side of a face as the Roe solver sees it.
+// `dry` is the reference's clamp decision h <= h_small (semi_discretize_swe_2D.jl:101-106).
+// A clamped side has h == h_small and an unclamped side h > h_small, so the
+// solver's `h <= hmin` tests are exactly `dry`; carrying the flag lets the FP32
+// path take these decisions from its FP64-exact depth.
+template <class T>
+struct Side {
+  T xi, hst, h, hu, hv, zb;
+  bool dry;
+};
+
+// Roe flux through a face with unit normal (nx, ny) pointing from L to R.
+// dxi = xiR - xiL is passed in so that the FP32 path can form it from its
+// hi/lo state pairs without cancellation.
+template <class T>
+__device__ __forceinline__ void roe_flux(Side<T> L, Side<T> R, T dxi, T g, T nx, T ny, T hmin, T F[3]) {
+  if (L.dry && R.dry) {                                   // both dry
+    F[0] = T(0); F[1] = T(0); F[2] = T(0);
+    return;
+  } else if ((L.h + L.zb) < (R.zb + hmin) && R.dry) {     // wall: R <- mirrored L (xiR kept)
+    R.h = L.h; R.hu = -L.hu; R.hv = -L.hv;
+  } else if ((R.h + R.zb) < (L.zb + hmin) && L.dry) {     // wall: L <- mirrored R (xiL kept)
+    L.h = R.h; L.hu = -R.hu; L.hv = -R.hv;
+  } else if (L.dry) {                                     // left dry: physical flux of R, h-based pressure
+    T p = T(0.5) * g * smooth_pow2(R.h);
+    F[0] = R.hu * nx + R.hv * ny;
+    F[1] = (R.hu * (R.hu / R.h) + p) * nx + R.hu * (R.hv / R.h) * ny;
+    F[2] = (R.hv * (R.hu / R.h)) * nx + (R.hv * (R.hv / R.h) + p) * ny;
+    return;
+  } else if (R.dry) {                                     // right dry: physical flux of L
+    T p = T(0.5) * g * smooth_pow2(L.h);
+    F[0] = L.hu * nx + L.hv * ny;
+    F[1] = (L.hu * (L.hu / L.h) + p) * nx + L.hu * (L.hv / L.h) * ny;
+    F[2] = (L.hv * (L.hu / L.h)) * nx + (L.hv * (L.hv / L.h) + p) * ny;
+    return;
+  }
+  const T uL = L.hu / L.h, vL = L.hv / L.h, uR = R.hu / R.h, vR = R.hv / R.h;
+  const T sL = smooth_sqrt(L.h), sR = smooth_sqrt(R.h);
+  const T hRoe = (L.h + R.h) / T(2);
+  const T uRoe = (sL * uL + sR * uR) / (sL + sR);
+  const T vRoe = (sL * vL + sR * vR) / (sL + sR);
+  const T unRoe = uRoe * nx + vRoe * ny;
+  const T cRoe = smooth_sqrt(g * hRoe);
+  const T o2c = T(0.5) / cRoe;
+  const T d1 = R.hu - L.hu, d2 = R.hv - L.hv;
+  // w = |Lambda| (Lmat dQ), absA_dQ = Rmat w  (swe_2D_solvers.jl:103-118)
+  T w0 = -(uRoe * ny - vRoe * nx) * dxi + ny * d1 + (-nx) * d2;
+  T w1 = (unRoe * o2c + T(0.5)) * dxi + (-nx * o2c) * d1 + (-ny * o2c) * d2;
+  T w2 = (-unRoe * o2c + T(0.5)) * dxi + (nx * o2c) * d1 + (ny * o2c) * d2;
+  w0 *= smooth_abs(unRoe);
+  w1 *= smooth_abs(unRoe - cRoe);
+  w2 *= smooth_abs(unRoe + cRoe);
+  const T A0 = w1 + w2;
+  const T A1 = ny * w0 + (uRoe - cRoe * nx) * w1 + (uRoe + cRoe * nx) * w2;
+  const T A2 = (-nx) * w0 + (vRoe - cRoe * ny) * w1 + (vRoe + cRoe * ny) * w2;
+  // pre-balanced pressure 0.5 g (xi^2 + 2 xi hstill)  (swe_2D_solvers.jl:122-127)
+  const T pL = T(0.5) * g * (smooth_pow2(L.xi) + T(2) * L.xi * L.hst);
+  const T pR = T(0.5) * g * (smooth_pow2(R.xi) + T(2) * R.xi * R.hst);
+  const T fL0 = L.hu * nx + L.hv * ny;
+  const T fL1 = (L.hu * uL + pL) * nx + L.hu * vL * ny;
+  const T fL2 = (L.hv * uL) * nx + (L.hv * vL + pL) * ny;
+  const T fR0 = R.hu * nx + R.hv * ny;
+  const T fR1 = (R.hu * uR + pR) * nx + R.hu * vR * ny;
+  const T fR2 = (R.hv * uR) * nx + (R.hv * vR + pR) * ny;
+  F[0] = (fL0 + fR0 - A0) / T(2);
+  F[1] = (fL1 + fR1 - A1) / T(2);
+  F[2] = (fL2 + fR2 - A2) / T(2);
+}
+
+// Ghost state of a boundary face (bc_2D.jl:640-834) from the clamped state of
+// its internal cell L, the outward normal (nx, ny), and the boundary data.
+// Returns R with R.xi = R.h - hstill (semi_discretize_swe_2D.jl:220), R.hst =
+// hstill and R.zb = zb of the internal cell (update_ghost_cells_scalar).
+template <class T>
+__device__ __forceinline__ Side<T> ghost_state(const Side<T>& L, int32_t type, T nx, T ny, T hmin, T exitWse,
+                                               T inletQ, T totalA, T lp23, T manning) {
+  Side<T> R;
+  R.hst = L.hst;
+  R.zb = L.zb;
+  R.h = L.h;
+  R.dry = L.dry;
+  if (type == kBcWall) {                       // (h, -qx, -qy)
+    R.hu = -L.hu;
+    R.hv = -L.hv;
+  } else if (type == kBcSymm) {                // mirror the normal momentum
+    T vdn = L.hu * nx + L.hv * ny;
+    R.hu = L.hu - T(2) * vdn * nx;
+    R.hv = L.hv - T(2) * vdn * ny;
+  } else if (type == kBcExitH) {               // h = max(h_small, WSE - zb), q copied
+    T hn = exitWse - L.zb;
+    R.dry = !(hn > hmin);
+    R.h = R.dry ? hmin : hn;
+    R.hu = L.hu;
+    R.hv = L.hv;
+  } else {                                     // inlet-Q: q = -h v_n n_out wet, v_n = Q/total_A L^(2/3)/n
+    T wet = L.dry ? T(0) : T(1);
+    T vn = inletQ / totalA * lp23 / manning;
+    R.hu = -L.h * vn * nx * wet;
+    R.hv = -L.h * vn * ny * wet;
+  }
+  R.xi = R.h - R.hst;
+  return R;
+}
+
+// Manning friction coefficient g n^2/k_n^2/(h+h_small)^(7/3) * smooth_sqrt(qx^2+qy^2)
+// (semi_discretize_swe_2D.jl:544-547).
+__device__ __forceinline__ double friction_coef(double g, double kn2, double hsm, double n, double h, double qx,
+                                                double qy) {
+  return g * (n * n) / kn2 / pow(h + hsm, 7.0 / 3.0) * smooth_sqrt(qx * qx + qy * qy);
+}
+__device__ __forceinline__ float friction_coef(float g, float kn2, float hsm, float n, float h, float qx, float qy) {
+  // (h + h_small)^(-7/3) = exp2(-7/3 log2(h + h_small))
+  return g * (n * n) / kn2 * exp2f(-2.3333333333333335f * log2f(h + hsm)) * smooth_sqrt(qx * qx + qy * qy);
+}
+
+}  // namespace hgd

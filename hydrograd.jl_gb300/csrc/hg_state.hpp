@@ -1,0 +1,95 @@
+// Device-side data of a context and the launch wrappers shared by the host
+// code (hg_capi.cpp) and the kernels (hg_forward.cu, hg_adjoint.cu).
+#pragma once
+#include <cstddef>
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+namespace hg {
+
+// Mesh and parameters in device memory, cells in the device (renumbered) order.
+// Slot-major face tables: entry [k * n + c] is edge slot k of cell c.
+struct DevMesh {
+  int32_t n = 0;        // cells
+  int32_t nslot = 0;    // max faces per cell
+  int32_t nbf = 0;      // boundary faces
+  int32_t nInlet = 0, nExit = 0;
+  const int32_t* nb = nullptr;       // [nslot*n] neighbour (>=0), -1-bf (boundary face bf), INT32_MIN (none)
+  const double* snx = nullptr;       // [nslot*n] outward unit normal x
+  const double* sny = nullptr;
+  const double* slen = nullptr;      // [nslot*n] edge length
+  const float* snxf = nullptr;       // FP32 copies
+  const float* snyf = nullptr;
+  const float* slenf = nullptr;
+  const int32_t* bfInfo = nullptr;   // [nbf] type | group << 2
+  const double* bfLp23 = nullptr;    // [nbf] L^(2/3) (inlet-Q faces)
+  const float* bfLp23f = nullptr;
+  const int32_t* inletOff = nullptr; // [nInlet+1] CSR over inlet faces in NodeString order
+  const int32_t* inletCell = nullptr;
+  const double* inletLp53 = nullptr; // L^(5/3)
+  // FP64 per-cell data
+  const double* area = nullptr;
+  const double* hst = nullptr;       // hstill
+  const double* zb = nullptr;
+  const double* man = nullptr;       // Manning n
+  const double* s0x = nullptr;
+  const double* s0y = nullptr;
+  // FP32 per-cell data (hstill as an exact hi+lo pair)
+  const float* areaf = nullptr;
+  const float* hsthi = nullptr;
+  const float* hstlo = nullptr;
+  const float* zbf = nullptr;
+  const float* manf = nullptr;
+  const float* s0xf = nullptr;
+  const float* s0yf = nullptr;
+  // Boundary values
+  const double* exitWse = nullptr;   // [nExit]
+  const double* inletQ = nullptr;    // [nInlet]
+  double* totalA = nullptr;          // [nInlet] conveyance of the current stage input
+  double g = 9.81, kn2 = 1.0, hsm = 1e-3;
+};
+
+// Scalars that live on the device so that steps can be captured in a graph.
+struct DevScalars {
+  double* dt = nullptr;                   // current step size
+  float* dtf = nullptr;                   // the same, as float (FP32 path)
+  unsigned long long* cflMin = nullptr;   // min over cells of A / sum L(|u.n|+c), as ordered bits
+  unsigned int* cflMinF = nullptr;        // the same from the FP32 path
+  double* dtHist = nullptr;               // [capacity] step sizes taken
+  int32_t* stepIdx = nullptr;             // steps taken since the last reset
+  double* tSum = nullptr;                 // sum of the steps taken
+  int32_t* flags = nullptr;               // bit 0: non-finite state, bit 1: inlet conveyance <= 1e-10
+  int32_t dtCap = 0;
+};
+
+enum StageMode : int32_t { kModeRhs = 0, kModeStage1 = 1, kModeStage2 = 2, kModeEulerRef = 3 };
+
+// FP64 state: Q blocks [xi | qx | qy] of n doubles.
+void launch_inlet_total_f64(const DevMesh& m, const DevScalars& s, const double* Q, cudaStream_t st);
+void launch_stage_f64(const DevMesh& m, const DevScalars& s, int mode, const double* Qin, const double* Qbase,
+                      double* Qout, bool cfl, cudaStream_t st);
+void launch_cfl_f64(const DevMesh& m, const DevScalars& s, const double* Q, cudaStream_t st);
+
+// FP32-compensated state: hi and lo float arrays, each [xi | qx | qy].
+struct StateF32 {
+  float* hi = nullptr;
+  float* lo = nullptr;
+};
+void launch_inlet_total_f32(const DevMesh& m, const DevScalars& s, StateF32 X, cudaStream_t st);
+void launch_stage_f32(const DevMesh& m, const DevScalars& s, int mode, StateF32 Xin, StateF32 Xbase, StateF32 Xout,
+                      double* Rout, bool cfl, cudaStream_t st);
+void launch_cfl_f32(const DevMesh& m, const DevScalars& s, StateF32 X, cudaStream_t st);
+
+// Step bookkeeping: when cflMode, dt = cfl * min; records dt and resets the min.
+void launch_step_begin(const DevScalars& s, bool cflMode, double cfl, cudaStream_t st);
+void launch_reset_scalars(const DevScalars& s, cudaStream_t st);
+
+// Renumbering between the caller's order (user) and the device order.
+void launch_gather_state_f64(int32_t n, const int32_t* perm, const double* user, double* dev, cudaStream_t st);
+void launch_scatter_state_f64(int32_t n, const int32_t* perm, const double* dev, double* user, cudaStream_t st);
+void launch_gather_state_f32(int32_t n, const int32_t* perm, const double* user, StateF32 dev, cudaStream_t st);
+void launch_scatter_state_f32(int32_t n, const int32_t* perm, StateF32 dev, double* user, cudaStream_t st);
+void launch_flush(void* buf, size_t bytes, cudaStream_t st);
+
+}  // namespace hg

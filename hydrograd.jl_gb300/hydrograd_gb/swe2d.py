@@ -1,0 +1,297 @@
+"""Host-side mirror of Hydrograd.jl's ODE-RHS / parameter interface over the C ABI.
+
+Hydrograd builds ``ODEFunction((u, p, t) -> swe_2d_rhs(du, u, p, t, swe_extra_params))``
+(src/applications/solve_swe_2D.jl:281-307) and hands it to SciML or to its own
+Euler loop.  This module gives the same shapes over libhydrograd_gb.so:
+
+* :class:`SWE2D` -- one device context: mesh, boundary conditions, parameters
+  and state buffers (what ``SWE2D_Extra_Parameters`` holds,
+  src/applications/application_commons.jl:7-44).
+* :func:`swe_2d_rhs` -- ``swe_2d_rhs(dQdt, Q, params_vector, t, p_extra)`` with
+  the reference's active-parameter injection (semi_discretize_swe_2D.jl:112-199).
+* :func:`custom_ODE_solve` -- the reference's forward-Euler loop
+  (src/ode_solvers/custom_ODE_solvers.jl:36-95).
+
+Every call goes to the CUDA library; a missing library raises (no fallback).
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import HgConsts, HgMeshDesc, check, lib
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int32)
+
+PRECISIONS = {"fp64": _lib.HG_FP64, "fp32c": _lib.HG_FP32C}
+ORDERS = {"none": _lib.HG_ORDER_NONE, "rcm": _lib.HG_ORDER_RCM, "hilbert": _lib.HG_ORDER_HILBERT}
+
+
+def _d(a):
+    return None if a is None else a.ctypes.data_as(_dp)
+
+
+def _i(a):
+    return None if a is None else a.ctypes.data_as(_ip)
+
+
+class MeshDesc:
+    """hg_mesh_desc over numpy arrays kept alive by this object.
+
+    ``case`` holds node_xyz [n,3], cell_nodes [n,8] (0-based, -1 padded),
+    cell_node_count [n], string_ids, string_offsets, string_nodes, string_bc.
+    """
+
+    def __init__(self, case):
+        xyz = np.asarray(case["node_xyz"], dtype=np.float64)
+        self.x = np.ascontiguousarray(xyz[:, 0])
+        self.y = np.ascontiguousarray(xyz[:, 1])
+        self.z = np.ascontiguousarray(xyz[:, 2])
+        self.cnt = np.ascontiguousarray(case["cell_node_count"], dtype=np.int32)
+        self.cn = np.ascontiguousarray(case["cell_nodes"], dtype=np.int32)
+        self.sid = np.ascontiguousarray(case.get("string_ids", np.zeros(0)), dtype=np.int32)
+        self.soff = np.ascontiguousarray(case.get("string_offsets", np.zeros(1)), dtype=np.int32)
+        self.snod = np.ascontiguousarray(case.get("string_nodes", np.zeros(0)), dtype=np.int32)
+        self.sbc = np.ascontiguousarray(case.get("string_bc", np.zeros(0)), dtype=np.int32)
+        if self.cn.shape != (len(self.cnt), 8):
+            raise ValueError("cell_nodes must be [n_cells, 8]")
+        self.desc = HgMeshDesc(len(self.x), _d(self.x), _d(self.y), _d(self.z), len(self.cnt), _i(self.cnt),
+                               _i(self.cn), len(self.sid), _i(self.sid), _i(self.soff), _i(self.snod), _i(self.sbc))
+
+
+class HostMesh:
+    """Host-only mesh topology (hg_mesh_build): no device needed."""
+
+    def __init__(self, case):
+        self._desc = MeshDesc(case)
+        h = ctypes.c_void_p()
+        check(lib().hg_mesh_build(ctypes.byref(self._desc.desc), ctypes.byref(h)))
+        self.h = h
+        s = np.zeros(8, np.int32)
+        check(lib().hg_mesh_sizes(self.h, _i(s)))
+        (self.n_cells, self.n_faces, self.n_ghosts, self.n_inletq, self.n_exith, self.n_wall, self.n_symm,
+         self.max_cell_faces) = map(int, s)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().hg_mesh_free(self.h)
+            self.h = None
+
+    def cell_faces(self):
+        N = self.n_cells
+        nbr = np.zeros(N * 8, np.int32)
+        nrm = np.zeros(N * 16)
+        ln = np.zeros(N * 8)
+        ar = np.zeros(N)
+        ce = np.zeros(N * 2)
+        check(lib().hg_mesh_cell_faces(self.h, _i(nbr), _d(nrm), _d(ln), _d(ar), _d(ce)))
+        return dict(nbr=nbr.reshape(N, 8), normals=nrm.reshape(N, 8, 2), lengths=ln.reshape(N, 8), areas=ar,
+                    centroids=ce.reshape(N, 2))
+
+    def order(self, order="hilbert"):
+        p = np.zeros(self.n_cells, np.int32)
+        check(lib().hg_mesh_order(self.h, ORDERS[order], _i(p)))
+        return p
+
+
+class SWE2D:
+    """A device context: the compiled RHS with its mesh, BCs, parameters and state."""
+
+    def __init__(self, case, precision="fp64", order="hilbert", g=9.81, k_n=1.0, h_small=1.0e-3, device=0):
+        self._desc = MeshDesc(case)
+        k = HgConsts(g, k_n, h_small, 0, ORDERS[order])
+        h = ctypes.c_void_p()
+        check(lib().hg_create(ctypes.byref(self._desc.desc), ctypes.byref(k), PRECISIONS[precision], device,
+                              ctypes.byref(h)))
+        self.h = h
+        self.precision = precision
+        s = np.zeros(8, np.int32)
+        check(lib().hg_sizes(self.h, _i(s)), self.h)
+        (self.n_cells, self.n_faces, self.n_ghosts, self.n_inletq, self.n_exith, self.n_wall, self.n_symm,
+         self.max_cell_faces) = map(int, s)
+        self.h_small = h_small
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().hg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def _chk(self, rc):
+        return check(rc, self.h)
+
+    # -- parameters ------------------------------------------------------------
+    def set_still_water(self, wstill):
+        w = np.ascontiguousarray(np.broadcast_to(np.asarray(wstill, np.float64), (self.n_cells,)))
+        self._chk(lib().hg_set_still_water(self.h, _d(w)))
+
+    def set_manning_zones(self, mat_id, n_zone):
+        m = np.ascontiguousarray(mat_id, dtype=np.int32)
+        z = np.ascontiguousarray(n_zone, dtype=np.float64)
+        self._chk(lib().hg_set_manning_zones(self.h, _i(m), len(z), _d(z)))
+
+    def set_manning_cells(self, n):
+        self._chk(lib().hg_set_manning_cells(self.h, _d(np.ascontiguousarray(n, dtype=np.float64))))
+
+    def set_zb_cells(self, zb):
+        self._chk(lib().hg_set_zb_cells(self.h, _d(np.ascontiguousarray(zb, dtype=np.float64))))
+
+    def set_inlet_q(self, q):
+        q = np.ascontiguousarray(np.atleast_1d(q), dtype=np.float64)
+        self._chk(lib().hg_set_inlet_q(self.h, _d(q), len(q)))
+
+    def set_exit_wse(self, w):
+        w = np.ascontiguousarray(np.atleast_1d(w), dtype=np.float64)
+        self._chk(lib().hg_set_exit_wse(self.h, _d(w), len(w)))
+
+    def bed(self):
+        N = self.n_cells
+        zb, S0, man, hst = np.zeros(N), np.zeros(2 * N), np.zeros(N), np.zeros(N)
+        self._chk(lib().hg_get_bed(self.h, _d(zb), _d(S0), _d(man), _d(hst)))
+        return dict(zb=zb, S0=S0.reshape(N, 2), manning=man, hstill=hst)
+
+    # -- forward -----------------------------------------------------------------
+    def check_initial_state(self, Q):
+        self._chk(lib().hg_check_initial_state(self.h, _d(np.ascontiguousarray(Q, dtype=np.float64))))
+
+    def rhs(self, Q, t=0.0, out=None):
+        Q = np.ascontiguousarray(Q, dtype=np.float64)
+        if out is None:
+            out = np.empty_like(Q)
+        self._chk(lib().hg_rhs(self.h, _d(Q), float(t), _d(out)))
+        return out
+
+    def integrate(self, Q, nsteps, method="rk2", dt=None, cfl=0.4, save_every=0):
+        """nsteps explicit steps from Q; returns (Q, dts[, saves])."""
+        Q = np.array(Q, dtype=np.float64)
+        dts = np.zeros(max(nsteps, 1))
+        saves = np.zeros((nsteps // save_every, Q.size)) if save_every > 0 else None
+        m = {"rk2": 0, "euler": 1}[method]
+        self._chk(lib().hg_integrate(self.h, _d(Q), 0.0, int(nsteps), m, float(dt) if dt else -1.0, float(cfl),
+                                     int(save_every), _d(saves), _d(dts)))
+        if saves is not None:
+            return Q, dts[:nsteps], saves
+        return Q, dts[:nsteps]
+
+    def upload(self, Q):
+        self._chk(lib().hg_state_upload(self.h, _d(np.ascontiguousarray(Q, dtype=np.float64))))
+
+    def download(self, out=None):
+        if out is None:
+            out = np.empty(3 * self.n_cells)
+        self._chk(lib().hg_state_download(self.h, _d(out)))
+        return out
+
+    def advance(self, nsteps, dt=None, cfl=0.4, graph=True):
+        self._chk(lib().hg_advance(self.h, int(nsteps), float(dt) if dt else -1.0, float(cfl), 1 if graph else 0))
+
+    def synchronize(self):
+        self._chk(lib().hg_synchronize(self.h))
+
+    def elapsed_time(self):
+        t = np.zeros(1)
+        self._chk(lib().hg_elapsed_time(self.h, _d(t)))
+        return float(t[0])
+
+    def launch_count(self):
+        c = ctypes.c_int64()
+        self._chk(lib().hg_launch_count(self.h, ctypes.byref(c)))
+        return int(c.value)
+
+    def time_stage_kernel(self, n=10, flush_l2=True):
+        ms = np.zeros(1)
+        self._chk(lib().hg_time_stage_kernel(self.h, int(n), 1 if flush_l2 else 0, _d(ms)))
+        return float(ms[0])
+
+    def flush_l2(self):
+        self._chk(lib().hg_flush_l2(self.h))
+
+    # -- gradient ----------------------------------------------------------------
+    def loss_and_grad(self, Q0, nsteps, dt, probes, obs, ckpt_every=50, want=("manning", "zb", "inletq")):
+        N = self.n_cells
+        Q0 = np.ascontiguousarray(Q0, dtype=np.float64)
+        probes = np.ascontiguousarray(probes, dtype=np.int32)
+        obs = np.ascontiguousarray(obs, dtype=np.float64)
+        loss = np.zeros(1)
+        gn = np.zeros(N) if "manning" in want else None
+        gz = np.zeros(N) if "zb" in want else None
+        gq = np.zeros(max(self.n_inletq, 1)) if "inletq" in want else None
+        Qf = np.zeros(3 * N)
+        self._chk(lib().hg_loss_and_grad(self.h, _d(Q0), int(nsteps), float(dt), int(ckpt_every), _i(probes),
+                                         _d(obs), len(probes), _d(loss), _d(gn), _d(gz), _d(gq), _d(Qf)))
+        return dict(loss=float(loss[0]), g_manning=gn, g_zb=gz, g_inletq=None if gq is None else gq[:self.n_inletq],
+                    Q=Qf)
+
+
+class PinnedBuffer:
+    """Page-locked host array (float64) for timed host<->device copies."""
+
+    def __init__(self, n):
+        p = ctypes.c_void_p()
+        check(lib().hg_pinned_alloc(int(n) * 8, ctypes.byref(p)))
+        self.p = p
+        self.array = np.ctypeslib.as_array(ctypes.cast(p, _dp), shape=(int(n),))
+
+    def __del__(self):
+        if getattr(self, "p", None):
+            lib().hg_pinned_free(self.p)
+            self.p = None
+
+
+# ---------------------------------------------------------------------------
+# The reference's interface
+# ---------------------------------------------------------------------------
+class SWE2DExtraParameters:
+    """The fields of SWE2D_Extra_Parameters (application_commons.jl:7-44) that
+    the RHS reads at run time: the active parameter name and how a parameter
+    vector maps onto the model."""
+
+    def __init__(self, ctx, active_param_name="none", mat_id=None, bInPlaceODE=False):
+        if active_param_name not in ("none", "ManningN", "zb", "Q"):
+            raise ValueError("active_param_name must be one of none, ManningN, zb, Q "
+                             "(process_model_parameters_2D.jl:2-168)")
+        self.ctx = ctx
+        self.active_param_name = active_param_name
+        self.mat_id = None if mat_id is None else np.ascontiguousarray(mat_id, dtype=np.int32)
+        self.bInPlaceODE = bInPlaceODE
+        self._last = None
+
+    def apply(self, params_vector):
+        """Inject the active parameter (semi_discretize_swe_2D.jl:112-199)."""
+        if self.active_param_name == "none" or params_vector is None:
+            return
+        p = np.asarray(params_vector, dtype=np.float64)
+        if self._last is not None and self._last.shape == p.shape and np.array_equal(self._last, p):
+            return
+        if self.active_param_name == "ManningN":
+            self.ctx.set_manning_zones(self.mat_id, p)      # ManningN_cells = p[matID + 1] (1-based)
+        elif self.active_param_name == "zb":
+            self.ctx.set_zb_cells(p)                        # update_bed_data (process_bed_2D.jl:46-66)
+        elif self.active_param_name == "Q":
+            self.ctx.set_inlet_q(p)                         # inletQ_TotalQ = params_vector
+        self._last = p.copy()
+
+
+def swe_2d_rhs(dQdt, Q, params_vector, t, p_extra):
+    """dQ/dt of Q = [xi; q_x; q_y] (semi_discretize_swe_2D.jl:18-277).
+
+    In-place (fills and returns ``dQdt``) when ``p_extra.bInPlaceODE``, else
+    returns a new array, as the reference's two ODEFunction forms do."""
+    p_extra.apply(params_vector)
+    if p_extra.bInPlaceODE:
+        p_extra.ctx.rhs(Q, t, out=dQdt)
+        return dQdt
+    return p_extra.ctx.rhs(Q, t)
+
+
+def custom_ODE_solve(Q0, params_vector, p_extra, tspan, dt):
+    """The reference's forward-Euler loop (custom_ODE_solvers.jl:36-95): one
+    step per element of ``t_start:dt:t_end`` with its clamp; returns the saved
+    states as columns, [3N, nsteps]."""
+    p_extra.apply(params_vector)
+    nsteps = len(np.arange(tspan[0], tspan[1] + dt * 1e-9, dt))
+    _, _, saves = p_extra.ctx.integrate(Q0, nsteps, method="euler", dt=dt, save_every=1)
+    return saves.T

@@ -1,0 +1,204 @@
+"""Seeded synthetic workloads (meshes, parameters, initial states).
+
+The reference ships meshes of at most 1,306 cells and publishes no benchmark
+data set, so the workloads below are generated: structured grids stored as
+unstructured cell lists, with a project-written splitmix64 stream so every
+harness (tests, benchmark, oracle) sees the same inputs for the same seed.
+
+* :func:`dam_break`      200x40 quads over 100 m x 20 m, walls, h = 1.0 / 0.5 m.
+* :func:`river_triangles` n x n grid split into 2 triangles per quad, nodes
+  jittered by +-0.2 dx over 2 km x 2 km; bed = 1e-3 slope + 20 Gaussian bumps;
+  5 Voronoi Manning zones; inlet-Q on the west edge, exit-H on the east edge,
+  walls elsewhere; dry except a 1.5 m pool that touches the inlet.
+
+A case is a dict with the mesh arrays of ``hg_mesh_desc`` plus parameters:
+mat_id, manning_zones, inlet_q, exit_wse, wstill (per cell) and Q0.
+"""
+import numpy as np
+
+H_SMALL = 1.0e-3
+_GOLD = np.uint64(0x9E3779B97F4A7C15)
+
+
+def splitmix64(seed, n):
+    """n uniform doubles in [0, 1) from the splitmix64 stream of ``seed``."""
+    with np.errstate(over="ignore"):
+        x = np.uint64(seed) + (np.arange(1, n + 1, dtype=np.uint64) * _GOLD)
+        z = x
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        z = z ^ (z >> np.uint64(31))
+    return (z >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0)
+
+
+class Stream:
+    """Sequential draws from one seed."""
+
+    def __init__(self, seed):
+        self.seed = np.uint64(seed)
+        self.pos = 0
+
+    def uniform(self, n, lo=0.0, hi=1.0):
+        with np.errstate(over="ignore"):
+            start = np.uint64(self.seed + np.uint64(self.pos) * _GOLD)
+        u = splitmix64(start, n) if n > 0 else np.zeros(0)
+        self.pos += n
+        return lo + (hi - lo) * u
+
+
+def _grid_nodes(nx, ny, Lx, Ly):
+    xs = np.linspace(0.0, Lx, nx + 1)
+    ys = np.linspace(0.0, Ly, ny + 1)
+    X, Y = np.meshgrid(xs, ys, indexing="xy")      # node (i, j) -> j*(nx+1) + i
+    return X.ravel(), Y.ravel()
+
+
+def _nid(i, j, nx):
+    return j * (nx + 1) + i
+
+
+def _string(nodes):
+    return np.asarray(nodes, dtype=np.int32)
+
+
+def _pack_strings(strings):
+    ids = np.array([s[0] for s in strings], dtype=np.int32)
+    bcs = np.array([s[1] for s in strings], dtype=np.int32)
+    offs = np.cumsum([0] + [len(s[2]) for s in strings]).astype(np.int32)
+    nodes = np.concatenate([s[2] for s in strings]).astype(np.int32) if strings else np.zeros(0, np.int32)
+    return ids, offs, nodes, bcs
+
+
+def initial_xi(h, wstill, zb):
+    """xi = h - hstill with hstill = wstill - zb, nudged up by ulps where
+    rounding would put xi + hstill below the intended depth (so a cell set to
+    h_small is not rejected by the initial-depth check, process_ICs_2D.jl:97-99)."""
+    hst = wstill - zb
+    xi = h - hst
+    for _ in range(8):
+        bad = xi + hst < h
+        if not bad.any():
+            break
+        xi[bad] = np.nextafter(xi[bad], np.inf)
+    return xi
+
+
+def cell_centroids(case):
+    """Polygon centroids (same formula as the mesh builder)."""
+    xyz = case["node_xyz"]
+    cn, cnt = case["cell_nodes"], case["cell_node_count"]
+    N = len(cnt)
+    cx = np.zeros(N)
+    cy = np.zeros(N)
+    a = np.zeros(N)
+    for k in range(cn.shape[1]):
+        has = k < cnt
+        if not has.any():
+            break
+        p = cn[:, k]
+        q = np.where(k + 1 < cnt, cn[:, (k + 1) % 8], cn[:, 0])
+        x1, y1 = xyz[p, 0], xyz[p, 1]
+        x2, y2 = xyz[q, 0], xyz[q, 1]
+        cr = np.where(has, x1 * y2 - x2 * y1, 0.0)
+        cx += np.where(has, (x1 + x2) * cr, 0.0)
+        cy += np.where(has, (y1 + y2) * cr, 0.0)
+        a += cr
+    a = np.abs(a) / 2
+    return cx / (6 * a), cy / (6 * a)
+
+
+def dam_break(nx=200, ny=40, Lx=100.0, Ly=20.0, n=0.03, h_left=1.0, h_right=0.5, x_gate=50.0):
+    """Flat-bed dam break, all boundaries walls (the default wall boundary)."""
+    X, Y = _grid_nodes(nx, ny, Lx, Ly)
+    xyz = np.stack([X, Y, np.zeros_like(X)], axis=1)
+    i, j = np.meshgrid(np.arange(nx), np.arange(ny), indexing="xy")
+    i, j = i.ravel(), j.ravel()
+    cells = np.full((nx * ny, 8), -1, dtype=np.int32)
+    cells[:, 0] = _nid(i, j, nx)
+    cells[:, 1] = _nid(i + 1, j, nx)
+    cells[:, 2] = _nid(i + 1, j + 1, nx)
+    cells[:, 3] = _nid(i, j + 1, nx)
+    case = dict(node_xyz=xyz, cell_nodes=cells, cell_node_count=np.full(nx * ny, 4, np.int32),
+                string_ids=np.zeros(0, np.int32), string_offsets=np.zeros(1, np.int32),
+                string_nodes=np.zeros(0, np.int32), string_bc=np.zeros(0, np.int32))
+    N = nx * ny
+    cx, _ = cell_centroids(case)
+    h = np.where(cx < x_gate, h_left, h_right)
+    case.update(mat_id=np.zeros(N, np.int32), manning_zones=np.array([n]), inlet_q=np.zeros(0), exit_wse=np.zeros(0),
+                wstill=np.zeros(N), Q0=np.concatenate([h, np.zeros(N), np.zeros(N)]),
+                name=f"dam_break_{nx}x{ny}")
+    return case
+
+
+def river_triangles(n=708, L=2000.0, seed=0, inlet_q=500.0, exit_wse=2.0, wstill=2.0, pool_h=1.5,
+                    pool_center=(300.0, 1000.0), pool_radius=350.0, n_bumps=20, n_zones=5, jitter=0.2):
+    """Triangulated 2 km reach with moving wet/dry fronts (2 n^2 cells)."""
+    rs = Stream(seed)
+    dx = L / n
+    X, Y = _grid_nodes(n, n, L, L)
+    nn = X.size
+    jx = rs.uniform(nn, -jitter, jitter) * dx
+    jy = rs.uniform(nn, -jitter, jitter) * dx
+    ii = np.tile(np.arange(n + 1), n + 1)
+    jj = np.repeat(np.arange(n + 1), n + 1)
+    interior_x = (ii > 0) & (ii < n)
+    interior_y = (jj > 0) & (jj < n)
+    X = X + np.where(interior_x, jx, 0.0)      # boundary nodes stay on their edge
+    Y = Y + np.where(interior_y, jy, 0.0)
+    # Bed: linear slope 1e-3 falling to the east plus Gaussian bumps.
+    A = rs.uniform(n_bumps, 0.5, 3.0)
+    S = rs.uniform(n_bumps, 20.0, 150.0)
+    BX = rs.uniform(n_bumps, 0.0, L)
+    BY = rs.uniform(n_bumps, 0.0, L)
+    Z = 1e-3 * (L - X)
+    for k in range(n_bumps):
+        Z = Z + A[k] * np.exp(-((X - BX[k]) ** 2 + (Y - BY[k]) ** 2) / (2 * S[k] ** 2))
+    xyz = np.stack([X, Y, Z], axis=1)
+    i, j = np.meshgrid(np.arange(n), np.arange(n), indexing="xy")
+    i, j = i.ravel(), j.ravel()
+    n00, n10, n11, n01 = _nid(i, j, n), _nid(i + 1, j, n), _nid(i + 1, j + 1, n), _nid(i, j + 1, n)
+    cells = np.full((2 * n * n, 8), -1, dtype=np.int32)
+    cells[0::2, 0], cells[0::2, 1], cells[0::2, 2] = n00, n10, n11
+    cells[1::2, 0], cells[1::2, 1], cells[1::2, 2] = n00, n11, n01
+    N = 2 * n * n
+    west = [_nid(0, jj_, n) for jj_ in range(n, -1, -1)]          # north -> south along x = 0
+    east = [_nid(n, jj_, n) for jj_ in range(0, n + 1)]           # south -> north along x = L
+    ids, offs, snodes, bcs = _pack_strings([(1, 2, _string(west)), (2, 3, _string(east))])
+    case = dict(node_xyz=xyz, cell_nodes=cells, cell_node_count=np.full(N, 3, np.int32), string_ids=ids,
+                string_offsets=offs, string_nodes=snodes, string_bc=bcs)
+    cx, cy = cell_centroids(case)
+    # Orientation check: every triangle counter-clockwise.
+    p, q, r = cells[:, 0], cells[:, 1], cells[:, 2]
+    area2 = (X[q] - X[p]) * (Y[r] - Y[p]) - (X[r] - X[p]) * (Y[q] - Y[p])
+    if not (area2 > 0).all():
+        raise RuntimeError("jittered mesh has an inverted triangle; lower the jitter")
+    # Manning zones: nearest of n_zones Voronoi seeds.
+    SX = rs.uniform(n_zones, 0.0, L)
+    SY = rs.uniform(n_zones, 0.0, L)
+    zones_n = rs.uniform(n_zones, 0.02, 0.06)
+    d2 = (cx[:, None] - SX[None, :]) ** 2 + (cy[:, None] - SY[None, :]) ** 2
+    mat = np.argmin(d2, axis=1).astype(np.int32)
+    zb = ((Z[cells[:, 0]] + Z[cells[:, 1]]) + Z[cells[:, 2]]) / 3    # mean of node z, in the mesh builder's order
+    pool = (cx - pool_center[0]) ** 2 + (cy - pool_center[1]) ** 2 < pool_radius ** 2
+    h = np.where(pool, pool_h, H_SMALL)
+    xi = initial_xi(h, np.full(N, wstill), zb)
+    case.update(mat_id=mat, manning_zones=zones_n, inlet_q=np.array([inlet_q]), exit_wse=np.array([exit_wse]),
+                wstill=np.full(N, wstill), Q0=np.concatenate([xi, np.zeros(N), np.zeros(N)]),
+                zb_cells=zb, name=f"river_tri_{n}x{n}x2")
+    return case
+
+
+def probes_and_perturbation(case, n_probe=64, seed=1, zb_sigma=0.05):
+    """Seeded probe cells (wet at t = 0, so the loss sees the flow) and a
+    per-cell bed perturbation drawn in FP32 with standard deviation zb_sigma."""
+    rs = Stream(seed)
+    N = len(case["cell_node_count"])
+    Q0 = case["Q0"]
+    wet = np.nonzero(Q0[:N] + case["wstill"] - case["zb_cells"] > 2 * H_SMALL)[0]
+    pick = np.unique((rs.uniform(4 * n_probe) * len(wet)).astype(np.int64))[:n_probe]
+    probes = wet[np.sort(pick)].astype(np.int32)
+    # Box-Muller from two uniform draws, rounded to float32.
+    u1 = np.maximum(rs.uniform(N), 1e-300)
+    u2 = rs.uniform(N)
+    dz = (zb_sigma * np.sqrt(-2.0 * np.log(u1)) * np.cos(2 * np.pi * u2)).astype(np.float32)
+    return probes, dz.astype(np.float64)

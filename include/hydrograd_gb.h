@@ -1,0 +1,196 @@
+/*
+ * hydrograd_gb.h -- C ABI of the GB300 (sm_103a) shallow-water RHS / time-stepping library.
+ *
+ * The library replaces the hot path of Hydrograd.jl: the ODE right-hand side
+ * swe_2d_rhs (src/fvm/discretization/semi_discretize_swe_2D.jl:18-277), its
+ * time integration (src/ode_solvers/custom_ODE_solvers.jl:5-95 and the SciML
+ * ODEProblem call sites, src/applications/forward_simulation/
+ * swe_2D_forward_simulation.jl:24-53), and the reverse-mode gradient that
+ * SciMLSensitivity/Zygote compute through it (src/applications/inversion/
+ * swe_2D_inversion.jl:247-483).  Julia binds these entry points with ccall;
+ * nothing here takes or returns a Julia, PyTorch or CUDA type.
+ *
+ * Conventions
+ *  - Every entry point returns an int status: HG_OK (0) or an HG_ERR_* code;
+ *    hg_last_error() gives a message.  No C++ exception crosses this ABI.
+ *  - All ids are 0-based.  Node ids index node_x/y/z; cell ids index the cell
+ *    arrays in the caller's order (the library renumbers internally and maps
+ *    back at this boundary).
+ *  - The state is the reference's Q = [xi; q_x; q_y] (3 blocks of n_cells
+ *    doubles), xi = wse - wstill (semi_discretize_swe_2D.jl:93-95,
+ *    process_ICs_2D.jl:53-57).
+ *  - Host buffers are owned by the caller and only read/written during the
+ *    call.  Device memory is owned by the context and never exposed.
+ *  - One context per host thread; each context runs on its own CUDA stream.
+ *  - There is no CPU fallback: hg_create fails with HG_ERR_NO_DEVICE when no
+ *    CUDA device is present.
+ */
+#ifndef HYDROGRAD_GB_H
+#define HYDROGRAD_GB_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HG_ABI_VERSION 1
+
+enum hg_status {
+  HG_OK = 0,
+  HG_ERR_ARG = 1,        /* bad argument (size, null pointer, id out of range) */
+  HG_ERR_MESH = 2,       /* mesh topology/geometry error (clockwise cell, open NodeString, ...) */
+  HG_ERR_CUDA = 3,       /* a CUDA call failed */
+  HG_ERR_NO_DEVICE = 4,  /* no CUDA device: there is no CPU fallback */
+  HG_ERR_STATE = 5,      /* invalid state (initial depth below h_small, NaN/Inf in the result) */
+  HG_ERR_INLET = 6,      /* inlet-Q conveyance not positive (bc_2D.jl:679) */
+  HG_ERR_UNSUPPORTED = 7 /* option not available in this build */
+};
+
+/* Boundary types of a NodeString (src/fvm/boundary_conditions/bc_2D.jl:154-260). */
+enum hg_bc { HG_BC_NONE = -1, HG_BC_WALL = 0, HG_BC_SYMM = 1, HG_BC_INLETQ = 2, HG_BC_EXITH = 3 };
+
+/* Arithmetic of the device path. */
+enum hg_precision {
+  HG_FP64 = 0,  /* plain FP64 everywhere (parity path, within 1e-12 of the FP64 oracle) */
+  HG_FP32C = 1  /* FP32 flux/source arithmetic, compensated (hi+lo FP32) state update,
+                   FP64-exact wet/dry and positivity decisions, FP64 accumulators */
+};
+
+/* Cell renumbering used on the device. */
+enum hg_order { HG_ORDER_NONE = 0, HG_ORDER_RCM = 1, HG_ORDER_HILBERT = 2 };
+
+/* Riemann solver (semi_discretize_swe_2D.jl:352-362: the reference has Roe only). */
+enum hg_riemann { HG_ROE = 0 };
+
+/*
+ * Mesh as an SRH-2D geometry holds it (src/utilities/SRH_2D/SRH_2D_SRHGeom.jl:14-46):
+ * nodes, cells as counter-clockwise node lists (<= 8 nodes, rows of 8, unused
+ * slots ignored), and NodeStrings.  A NodeString with string_bc = HG_BC_NONE is
+ * not a boundary (monitoring line).  Boundary edges on no NodeString form a
+ * default wall boundary (SRH_2D_SRHGeom.jl:344-349).  Bed elevation at cells is
+ * the mean of node_z (src/fvm/discretization/fvm_schemes_2D.jl:216-224).
+ */
+typedef struct hg_mesh_desc {
+  int32_t n_nodes;
+  const double* node_x;
+  const double* node_y;
+  const double* node_z;
+  int32_t n_cells;
+  const int32_t* cell_node_count; /* [n_cells] */
+  const int32_t* cell_nodes;      /* [n_cells * 8] */
+  int32_t n_strings;
+  const int32_t* string_ids;      /* [n_strings] NodeString ids (boundary ids) */
+  const int32_t* string_offsets;  /* [n_strings + 1] into string_nodes */
+  const int32_t* string_nodes;    /* node ids along each NodeString */
+  const int32_t* string_bc;       /* [n_strings] hg_bc */
+} hg_mesh_desc;
+
+/* Problem constants (src/constants/swe_2D_constants.jl:4-17; solve_swe_2D.jl:51-107). */
+typedef struct hg_consts {
+  double g;        /* 9.81 (SI) or 32.2 (EN) */
+  double k_n;      /* 1.0 (SI) or 1.486 (EN) */
+  double h_small;  /* dry threshold, 1e-3 */
+  int32_t riemann; /* hg_riemann */
+  int32_t order;   /* hg_order (device renumbering) */
+} hg_consts;
+
+typedef struct hg_ctx hg_ctx;
+typedef struct hg_mesh hg_mesh;
+
+/* ---- diagnostics -------------------------------------------------------- */
+/* Message of the last failing call on ctx (ctx may be NULL for hg_create / hg_mesh_build failures). */
+int hg_last_error(const hg_ctx* ctx, char* buf, int32_t len);
+int hg_abi_version(void);
+
+/* ---- host-only mesh topology (no device needed) -------------------------- */
+/* Topology + geometry exactly as initialize_mesh_2D builds it (src/meshes/mesh_2D.jl:75-453). */
+int hg_mesh_build(const hg_mesh_desc* desc, hg_mesh** out);
+int hg_mesh_free(hg_mesh* mesh);
+/* sizes: [n_cells, n_faces, n_ghosts, n_inletq, n_exith, n_wall, n_symm, max_cell_faces] */
+int hg_mesh_sizes(const hg_mesh* mesh, int32_t* sizes8);
+/* Per cell, per local face slot i (edge node i -> node i+1), in the caller's cell order:
+ * neighbour cell id or -1 on a boundary, outward normal, edge length; plus cell areas
+ * and centroids (mesh_2D.jl:456-652).  Any output may be NULL. */
+int hg_mesh_cell_faces(const hg_mesh* mesh, int32_t* nbr8, double* normals16, double* lengths8, double* areas,
+                       double* centroids2);
+/* Cell permutation used on the device: perm[new] = old. */
+int hg_mesh_order(const hg_mesh* mesh, int32_t order, int32_t* perm);
+
+/* ---- context lifecycle (replaces building SWE2D_Extra_Parameters, application_commons.jl:7-44) */
+int hg_create(const hg_mesh_desc* desc, const hg_consts* consts, int32_t precision, int32_t device, hg_ctx** out);
+int hg_destroy(hg_ctx* ctx);
+int hg_sizes(const hg_ctx* ctx, int32_t* sizes8); /* as hg_mesh_sizes */
+
+/* ---- parameters (semi_discretize_swe_2D.jl:112-199; process_ManningN_2D.jl:242-269) */
+/* hstill = wstill - zb_cells; hstill is fixed from here on, as in the reference
+ * (it is not recomputed when zb changes, process_ICs_2D.jl:55,84). */
+int hg_set_still_water(hg_ctx* ctx, const double* wstill_cells);
+/* ManningN_cells[i] = n_zone[mat_id[i]] (mat_id 0 = default zone). */
+int hg_set_manning_zones(hg_ctx* ctx, const int32_t* mat_id, int32_t n_zones, const double* n_zone);
+int hg_set_manning_cells(hg_ctx* ctx, const double* n_cells);
+/* Active zb parameter: replaces zb_cells and recomputes zb ghost/face values and
+ * the bed slope S0 on the device (process_bed_2D.jl:46-66). */
+int hg_set_zb_cells(hg_ctx* ctx, const double* zb_cells);
+int hg_set_inlet_q(hg_ctx* ctx, const double* q, int32_t n_inletq);   /* inletQ_TotalQ */
+int hg_set_exit_wse(hg_ctx* ctx, const double* wse, int32_t n_exith); /* exitH_WSE */
+/* Read back derived data: zb_cells [n], S0 [2n] (x,y interleaved), ManningN_cells [n], hstill [n]. */
+int hg_get_bed(hg_ctx* ctx, double* zb_cells, double* S0, double* manning_cells, double* hstill);
+
+/* ---- forward ------------------------------------------------------------- */
+/* dQdt = swe_2d_rhs(Q, p, t) with host buffers (semi_discretize_swe_2D.jl:18-277). */
+int hg_rhs(hg_ctx* ctx, const double* Q, double t, double* dQdt);
+/* Check an initial state the way setup_initial_condition does (process_ICs_2D.jl:89-99). */
+int hg_check_initial_state(hg_ctx* ctx, const double* Q);
+/*
+ * Integrate nsteps explicit steps from Q (host, in/out).
+ *   method: 0 = SSP-RK2 (Heun) with a depth-positivity clamp after each stage,
+ *           1 = forward Euler with the reference's clamp (custom_ODE_solvers.jl:5-33).
+ *   dt > 0: fixed step; dt <= 0: CFL step dt = cfl * min_c A_c / sum_f L_f(|u.n_f| + sqrt(g h))
+ *           recomputed on the device before every step.
+ *   save_every > 0: the state after every save_every-th step is written to saves
+ *           (host, [nsteps/save_every][3n]); may be NULL otherwise.
+ *   dts_out: the step sizes used ([nsteps], host), may be NULL.
+ */
+int hg_integrate(hg_ctx* ctx, double* Q, double t0, int32_t nsteps, int32_t method, double dt, double cfl,
+                 int32_t save_every, double* saves, double* dts_out);
+
+/* ---- device-resident stepping (the state stays in HBM between calls) ------ */
+int hg_state_upload(hg_ctx* ctx, const double* Q);
+int hg_state_download(hg_ctx* ctx, double* Q);
+/* Enqueue nsteps SSP-RK2 steps on the resident state (no host synchronisation;
+ * replays a captured CUDA graph when graph != 0). */
+int hg_advance(hg_ctx* ctx, int32_t nsteps, double dt, double cfl, int32_t graph);
+int hg_synchronize(hg_ctx* ctx);
+/* Sum of the device time steps taken since the last upload. */
+int hg_elapsed_time(hg_ctx* ctx, double* t);
+
+/* ---- gradient (replaces Zygote/SciMLSensitivity through the RHS) ----------- */
+/*
+ * Loss = mean over steps k = 1..nsteps and probes p of (h_p^k - obs[k][p])^2,
+ * h = xi + hstill, for nsteps fixed-dt SSP-RK2 steps from Q0.  Gradients by a
+ * discrete adjoint with checkpoints every ckpt_every steps and recomputation.
+ * g_manning_cells [n] (dL/dn per cell; zone gradients are sums over a zone's
+ * cells), g_zb [n] (dL/dzb_cells through S0, ghost and exit-H values), g_inletq
+ * [n_inletq].  Any gradient output may be NULL.  Q_final (host, 3n) may be NULL.
+ */
+int hg_loss_and_grad(hg_ctx* ctx, const double* Q0, int32_t nsteps, double dt, int32_t ckpt_every,
+                     const int32_t* probe_cells, const double* obs, int32_t n_probe, double* loss,
+                     double* g_manning_cells, double* g_zb, double* g_inletq, double* Q_final);
+
+/* ---- measurement support ---------------------------------------------------- */
+/* Number of kernel launches this context has enqueued (graph replays count their kernels). */
+int hg_launch_count(const hg_ctx* ctx, int64_t* count);
+/* Time n launches of the stage kernel alone with CUDA events on the context's stream,
+ * flushing L2 between launches when flush_l2 != 0; avg_ms receives the mean duration. */
+int hg_time_stage_kernel(hg_ctx* ctx, int32_t n, int32_t flush_l2, double* avg_ms);
+/* Write a device buffer larger than L2 (used between timed iterations). */
+int hg_flush_l2(hg_ctx* ctx);
+/* Page-locked host buffers for fast host<->device copies of states. */
+int hg_pinned_alloc(int64_t bytes, void** out);
+int hg_pinned_free(void* p);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HYDROGRAD_GB_H */
