@@ -1,0 +1,346 @@
+"""Benchmark: cell-updates/s of the SWE-2D RHS + SSP-RK2 stepping at 1M cells.
+
+Workload: the 2 km reach on a 708 x 708 grid split into 1,002,528 jittered
+triangles (hydrograd_gb.workloads.river_triangles, seed 0), 5 Manning zones,
+inlet-Q 500 m^3/s, exit-H, walls; 2,000 CFL-0.4 SSP-RK2 steps.  One "step" is
+one RK2 step of every cell (two fused stage passes); value = cells x steps / s.
+
+Our arm (default): the FP32-compensated path is the headline ``value``; the
+plain FP64 path, FP32C-vs-FP64 error, roofline of the stage kernel, the
+end-to-end number through the C ABI with host buffers, and the CPU baseline
+(the oracle, all host threads, bounded sample) are reported beside it.
+--impl reference: the oracle (the reference's algorithm restated in C++,
+OpenMP over cells) on this machine's host cores, on the same workload and metric.
+
+Multi-GPU: the path does not shard in this build (replicas only): under
+torchrun each rank runs its own replica; value sums the ranks' cell-updates
+over the slowest rank's time.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "hydrograd.jl_gb300"))
+
+import numpy as np  # noqa: E402
+
+METRIC = "cell-updates/s (fwd; fwd+adjoint) at 1M cells: FP32-comp vs FP64, err≤1e-5"
+UNIT = "cell-updates/s"
+# Algorithmic (compulsory) bytes per cell for one stage pass: state read +
+# per-cell parameters + write, plus per-face geometry phi per cell, and per
+# RK2 cell-update (two stages + the stage-2 re-read of Q^n).
+BYTES_STAGE = {"fp32c": (72.0, 20.0), "fp64": (96.0, 32.0)}   # (per cell, per face)
+BYTES_STEP_EXTRA = {"fp32c": 24.0, "fp64": 24.0}
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic(precision):
+    """Per-cell DRAM bytes of the stage kernel from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "stage_kernel_river_tri.md")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        line = line.strip()
+        if line.startswith("{") and '"dram_bytes_per_cell"' in line:
+            d = json.loads(line)
+            if d.get("precision") == precision:
+                return float(d["dram_bytes_per_cell"])
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi SM clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) == 7:
+                self.rows.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[3 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws <= 1:
+        return 0, 1, 0, None
+    import torch
+    import torch.distributed as dist
+    rank, local = int(os.environ["RANK"]), int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist.init_process_group("nccl")
+    return rank, ws, local, dist
+
+
+def barrier(dist):
+    if dist is not None:
+        import torch
+        t = torch.zeros(1, device="cuda")
+        dist.all_reduce(t)
+        torch.cuda.synchronize()
+
+
+def max_over_ranks(dist, v):
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], device="cuda", dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def make_ctx(case, precision, device):
+    from hydrograd_gb import SWE2D
+    ctx = SWE2D(case, precision=precision, order="hilbert", device=device)
+    ctx.set_still_water(case["wstill"])
+    ctx.set_manning_zones(case["mat_id"], case["manning_zones"])
+    ctx.set_inlet_q(case["inlet_q"])
+    ctx.set_exit_wse(case["exit_wse"])
+    return ctx
+
+
+def setup_oracle(case):
+    from oracle.oracle import Oracle
+    o = Oracle(case)
+    o.set_wstill(case["wstill"])
+    o.set_manning_cells(case["manning_zones"][case["mat_id"]])
+    o.set_inlet_q(case["inlet_q"])
+    o.set_exit_wse(case["exit_wse"])
+    return o
+
+
+def cpu_baseline(case, seconds=12.0):
+    """The oracle's SSP-RK2 on all host threads, a bounded sample of steps."""
+    o = setup_oracle(case)
+    N = len(case["cell_node_count"])
+    threads = os.cpu_count() or 1
+    Q = case["Q0"].copy()
+    dt = o.cfl_dt(Q, 0.4)
+    o.rk2(Q, 1, dt=dt, nthreads=threads)            # warm-up (page-in, thread pool)
+    steps, t0 = 0, time.perf_counter()
+    while time.perf_counter() - t0 < seconds:
+        Q = o.rk2(Q, 1, cfl=0.4, nthreads=threads)
+        steps += 1
+    el = time.perf_counter() - t0
+    return {"value": N * steps / el, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{steps} SSP-RK2 CFL steps of the {N}-cell workload in {el:.1f} s"}, o
+
+
+def run_reference(args):
+    rank, ws, _, dist = dist_setup()
+    if rank != 0:
+        return
+    from hydrograd_gb.workloads import river_triangles
+    case = river_triangles(n=args.n)
+    N = len(case["cell_node_count"])
+    o = setup_oracle(case)
+    threads = os.cpu_count() or 1
+    Q = case["Q0"].copy()
+    for _ in range(args.warmup):
+        Q = o.rk2(Q, 1, cfl=0.4, nthreads=threads)
+    t0 = time.perf_counter()
+    Q = o.rk2(Q, args.ref_steps, cfl=0.4, nthreads=threads)
+    el = time.perf_counter() - t0
+    v = N * args.ref_steps / el
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.ref_steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.ref_steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"{case['name']}: {N} triangles, SSP-RK2 CFL 0.4", "cells": N,
+                   "sample": f"{args.ref_steps} steps of the 2,000-step run"},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{args.ref_steps} SSP-RK2 steps on {threads} threads"},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+
+
+def run_ours(args):
+    rank, ws, local, dist = dist_setup()
+    from hydrograd_gb import PinnedBuffer
+    from hydrograd_gb.workloads import river_triangles
+    case = river_triangles(n=args.n)
+    N = len(case["cell_node_count"])
+    nfaces_cell = None
+    out = {}
+    ctxs = {}
+    for prec in ("fp32c", "fp64"):
+        ctx = make_ctx(case, prec, local)
+        ctxs[prec] = ctx
+        nfaces_cell = ctx.n_faces / N
+        steps = args.steps if prec == "fp32c" else args.steps_fp64
+        ctx.upload(case["Q0"])
+        ctx.advance_timed(args.warmup, cfl=0.4, flush_l2=True)
+        ctx.upload(case["Q0"])
+        barrier(dist)
+        l0 = ctx.launch_count()
+        sampler = ClockSampler(local) if prec == "fp32c" else None
+        if sampler:
+            sampler.__enter__()
+        ms = ctx.advance_timed(steps, cfl=0.4, flush_l2=True)
+        if sampler:
+            sampler.__exit__()
+        launches = ctx.launch_count() - l0 - steps   # minus the L2 flushes
+        ms = max_over_ranks(dist, ms)
+        barrier(dist)
+        out[prec] = dict(ms=ms, steps=steps, value=ws * N * steps / (ms * 1e-3), launches=launches,
+                         clocks=sampler.summary() if sampler else None, state=ctx.download(),
+                         sim_time=ctx.elapsed_time())
+        # Continuous run without flushes (L2 kept warm), for reference.
+        ctx.upload(case["Q0"])
+        ctx.advance(args.warmup, cfl=0.4)
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        ctx.advance(steps, cfl=0.4, graph=True)
+        ctx.synchronize()
+        out[prec]["warm_value"] = N * steps / (time.perf_counter() - t0)
+        # Stage kernel alone (roofline).
+        ctx.upload(case["Q0"])
+        out[prec]["stage_ms"] = ctx.time_stage_kernel(20, True)
+    # FP32C error vs the FP64 path over the whole run (same CFL rule; the FP64
+    # path itself is checked against the oracle below and by the GPU tests).
+    a, b = out["fp32c"]["state"], out["fp64"]["state"]
+    err = {}
+    if args.steps == args.steps_fp64:
+        err["fp32c_vs_fp64_state_rel_linf"] = float(max(
+            np.abs(a[k * N:(k + 1) * N] - b[k * N:(k + 1) * N]).max() / max(np.abs(b).max(), 1e-300) for k in range(3)))
+        err["fp32c_vs_fp64_state_rel_l2"] = float(np.linalg.norm(a - b) / np.linalg.norm(b))
+    # End to end through the C ABI with host (pinned) buffers: hg_integrate of
+    # e2e_chunk steps per call, H2D of the state in and D2H of the state out per call.
+    ctx = ctxs["fp32c"]
+    host = PinnedBuffer(3 * N)
+    host.array[:] = case["Q0"]
+    ctx.integrate(host.array, 2, cfl=0.4)
+    calls = max(1, args.steps // args.e2e_chunk)
+    barrier(dist)
+    t0 = time.perf_counter()
+    for _ in range(calls):
+        q, _ = ctx.integrate(host.array, args.e2e_chunk, cfl=0.4)
+        host.array[:] = q
+    el = max_over_ranks(dist, time.perf_counter() - t0)
+    e2e = {"value": ws * N * args.e2e_chunk * calls / el, "unit": UNIT,
+           "h2d_bytes_per_step": 3 * N * 8 / args.e2e_chunk, "d2h_bytes_per_step": 3 * N * 8 / args.e2e_chunk,
+           "calls": calls, "steps_per_call": args.e2e_chunk}
+    if rank != 0:
+        return
+    peak, peak_kind = load_peaks()
+    cell_b, face_b = BYTES_STAGE["fp32c"]
+    bytes_stage = (cell_b + nfaces_cell * face_b) * N
+    achieved = bytes_stage / (out["fp32c"]["stage_ms"] * 1e-3) / 1e9
+    tr = profile_traffic("fp32c")
+    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": None if tr is None else tr * N, "kernel": "k_stage_f32 (one RK2 stage pass)",
+            "algorithmic_bytes_per_launch": bytes_stage, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)"}
+    fp64_bytes = (BYTES_STAGE["fp64"][0] + nfaces_cell * BYTES_STAGE["fp64"][1]) * N
+    cpu = None
+    if not args.no_cpu:
+        cpu, o = cpu_baseline(case, args.cpu_seconds)
+        # FP64 path vs the oracle on the full mesh, a short horizon.
+        ctx64 = ctxs["fp64"]
+        q_gpu, dts = ctx64.integrate(case["Q0"], args.oracle_steps, cfl=0.4)
+        qo = case["Q0"].copy()
+        for d in dts:
+            qo = o.rk2(qo, 1, dt=float(d), nthreads=os.cpu_count() or 1)
+        err["fp64_vs_oracle_state_rel_linf"] = float(max(
+            np.abs(q_gpu[k * N:(k + 1) * N] - qo[k * N:(k + 1) * N]).max() / max(np.abs(qo).max(), 1e-300)
+            for k in range(3)))
+        err["fp64_vs_oracle_steps"] = args.oracle_steps
+    f32 = out["fp32c"]
+    line = {
+        "metric": METRIC, "value": f32["value"], "unit": UNIT, "n_gpus": ws, "steps": f32["steps"],
+        "warmup": args.warmup, "ms_per_step": f32["ms"] / f32["steps"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 (hi+lo compensated state)", "data": "synthetic",
+        "config": {"workload": f"{case['name']}: {N} jittered triangles, 2 km reach, SSP-RK2 CFL 0.4, "
+                               f"{f32['steps']} steps", "cells": N, "faces": ctxs["fp32c"].n_faces,
+                   "l2": "flushed before every timed step (256 MB write, outside the timed events)",
+                   "order": "hilbert", "parallelism": "replicas" if ws > 1 else "single GPU"},
+        "fp64": {"value": out["fp64"]["value"], "ms_per_step": out["fp64"]["ms"] / out["fp64"]["steps"],
+                 "steps": out["fp64"]["steps"], "stage_ms": out["fp64"]["stage_ms"],
+                 "stage_gbs": fp64_bytes / (out["fp64"]["stage_ms"] * 1e-3) / 1e9,
+                 "warm_value": out["fp64"]["warm_value"]},
+        "fp32c_over_fp64_speedup": f32["value"] / out["fp64"]["value"],
+        "warm_value": f32["warm_value"], "simulated_seconds": f32["sim_time"],
+        "error": err,
+        "roofline": roof,
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "gpu_launches": f32["launches"],
+        "clocks": f32["clocks"],
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=708, help="grid size: 2 n^2 triangles")
+    ap.add_argument("--steps-fp64", type=int, default=None)
+    ap.add_argument("--e2e-chunk", type=int, default=100)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--oracle-steps", type=int, default=20)
+    ap.add_argument("--ref-steps", type=int, default=20)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.steps_fp64 is None:
+        args.steps_fp64 = args.steps
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -18,7 +18,8 @@ OUT = os.path.join(HERE, "build")
 LIB = os.path.join(OUT, "libhydrograd_gb.so")
 INCLUDE = os.path.join(ROOT, "include")
 
-CUDA_SOURCES = ["hg_forward.cu", "hg_adjoint_kernels.cu"]
+CUDA_SOURCES = ["hg_forward_f64.cu", "hg_forward_f32.cu", "hg_adjoint_kernels.cu"]
+NO_FMAD = {"hg_forward_f64.cu"}   # FP64 parity path: no fused multiply-add, as in the reference
 CXX_SOURCES = ["hg_mesh.cpp", "hg_capi.cpp", "hg_adjoint.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -45,7 +46,8 @@ def build(verbose=False):
             continue
         obj = os.path.join(OUT, src + ".o")
         objs.append(obj)
-        jobs.append([nvcc, "-std=c++17", "-O3", *ARCH, "-lineinfo", "-Xcompiler", "-fPIC", "-I", INCLUDE,
+        fmad = ["--fmad=false"] if src in NO_FMAD else []
+        jobs.append([nvcc, "-std=c++17", "-O3", *ARCH, *fmad, "-lineinfo", "-Xcompiler", "-fPIC", "-I", INCLUDE,
                      "-c", os.path.join(CSRC, src), "-o", obj])
     for src in CXX_SOURCES:
         obj = os.path.join(OUT, src + ".o")

@@ -573,6 +573,42 @@ int hg_flush_l2(hg_ctx* ctx) {
   return HG_OK;
 }
 
+int hg_advance_timed(hg_ctx* ctx, int32_t nsteps, double dt, double cfl, int32_t flush_l2, double* total_ms) {
+  if (!ctx || nsteps <= 0 || !total_ms) return fail(ctx, HG_ERR_ARG, "hg_advance_timed: bad argument");
+  if (dt <= 0 && !(cfl > 0)) return fail(ctx, HG_ERR_ARG, "hg_advance_timed: need dt > 0 or cfl > 0");
+  cudaSetDevice(ctx->device);
+  const bool cflMode = dt <= 0;
+  if (!cflMode) {
+    int rc = set_fixed_dt(ctx, dt);
+    if (rc) return rc;
+  } else if (!ctx->cflPrimed) {
+    enqueue_cfl_prime(ctx);
+  }
+  std::vector<cudaEvent_t> ev(2 * (size_t)nsteps, nullptr);
+  for (auto& e : ev) HG_CUDA(ctx, cudaEventCreate(&e));
+  for (int s = 0; s < nsteps; ++s) {
+    if (flush_l2) {
+      launch_flush(ctx->flushBuf, ctx->flushBytes, ctx->stream);
+      ctx->launches += 1;
+    }
+    cudaEventRecord(ev[2 * s], ctx->stream);
+    enqueue_rk2_step(ctx, cflMode, cfl);
+    cudaEventRecord(ev[2 * s + 1], ctx->stream);
+  }
+  ctx->cflPrimed = cflMode;
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  double total = 0.0;
+  for (int s = 0; s < nsteps && e == cudaSuccess; ++s) {
+    float ms = 0.f;
+    e = cudaEventElapsedTime(&ms, ev[2 * s], ev[2 * s + 1]);
+    total += ms;
+  }
+  for (auto& x : ev) cudaEventDestroy(x);
+  if (e != cudaSuccess) return fail(ctx, HG_ERR_CUDA, std::string("hg_advance_timed: ") + cudaGetErrorString(e));
+  *total_ms = total;
+  return check_flags(ctx);
+}
+
 int hg_time_stage_kernel(hg_ctx* ctx, int32_t n, int32_t flush_l2, double* avg_ms) {
   if (!ctx || n <= 0 || !avg_ms) return fail(ctx, HG_ERR_ARG, "hg_time_stage_kernel: bad argument");
   cudaSetDevice(ctx->device);

@@ -18,6 +18,21 @@ template <class T> __device__ __forceinline__ T smooth_abs(T x) { return sqrt(x 
 template <class T> __device__ __forceinline__ T smooth_sqrt(T x) { return sqrt(x + eps_c<T>()); }
 template <class T> __device__ __forceinline__ T smooth_pow2(T x) { T y = x + eps_c<T>(); return y * y; }
 
+// xi of a dry cell: the largest xi with xi + hstill <= h_small in FP64, so the
+// RHS sees the cell as dry.  h_small - hstill alone can round one ulp above
+// h_small: a wet film 1e-19 m thick whose Manning friction (h + h_small)^(-7/3)
+// breaks any explicit step.
+__device__ __forceinline__ double prev_double(double x) {   // next representable double toward -inf (finite x)
+  if (x == 0.0) return -4.9406564584124654e-324;
+  const long long b = __double_as_longlong(x);
+  return __longlong_as_double(x > 0.0 ? b - 1 : b + 1);
+}
+__device__ __forceinline__ double dry_xi(double hsm, double hst) {
+  double x = __dsub_rn(hsm, hst);
+  for (int i = 0; i < 4 && __dadd_rn(x, hst) > hsm; ++i) x = prev_double(x);
+  return x;
+}
+
 // Boundary face encoding in the slot neighbour table.
 constexpr int32_t kNoFace = INT32_MIN;
 __device__ __forceinline__ bool is_boundary(int32_t nb) { return nb < 0; }

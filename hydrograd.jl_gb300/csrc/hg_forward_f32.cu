@@ -1,3 +1,5 @@
+// FP32-compensated stage kernels, step bookkeeping and renumbering kernels.
+//
 // Forward kernels: one fused pass per explicit stage.
 //
 // Each thread owns one cell (device order) and gathers its faces in the
@@ -11,6 +13,7 @@
 #include <cmath>
 
 #include "hg_device.cuh"
+#include "hg_reduce.cuh"
 #include "hg_state.hpp"
 
 namespace hg {
@@ -23,180 +26,7 @@ constexpr int kBlock = 256;
 
 inline int blocks_for(int n) { return (n + kBlock - 1) / kBlock; }
 
-// ---------------------------------------------------------------------------
-// Reductions
-// ---------------------------------------------------------------------------
-// Block-wide minimum of non-negative values, published with one atomicMin on
-// the IEEE bit pattern (non-negative doubles order like unsigned integers), so
-// the result does not depend on the order blocks finish in.
-__device__ __forceinline__ void block_min_publish(double v, unsigned long long* out) {
-  __shared__ double sm[32];
-  for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  if (lane == 0) sm[w] = v;
-  __syncthreads();
-  if (w == 0) {
-    v = lane < (int)(blockDim.x >> 5) ? sm[lane] : INFINITY;
-    for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
-    if (lane == 0) atomicMin(out, (unsigned long long)__double_as_longlong(v));
-  }
-}
-
-// FP32 variant: minimum of non-negative floats published on their bit pattern.
-__device__ __forceinline__ void block_min_publish_f(float v, unsigned int* out) {
-  __shared__ float smf[32];
-  for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  if (lane == 0) smf[w] = v;
-  __syncthreads();
-  if (w == 0) {
-    v = lane < (int)(blockDim.x >> 5) ? smf[lane] : INFINITY;
-    for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
-    if (lane == 0) atomicMin(out, __float_as_uint(v));
-  }
-}
-
-// Deterministic block sum (fixed thread -> element mapping, fixed tree).
-__device__ __forceinline__ double block_sum(double v) {
-  __shared__ double sm[32];
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  __syncthreads();
-  if (lane == 0) sm[w] = v;
-  __syncthreads();
-  double r = 0.0;
-  if (w == 0) {
-    r = lane < (int)(blockDim.x >> 5) ? sm[lane] : 0.0;
-    for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
-  }
-  return r;   // valid in thread 0
-}
-
-// ---------------------------------------------------------------------------
-// FP64 path
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ Side<double> load_f64(const DevMesh& m, const double* __restrict__ Q, int j) {
-  Side<double> s;
-  s.xi = Q[j];
-  s.hst = m.hst[j];
-  s.zb = m.zb[j];
-  double h = s.xi + s.hst;          // h = xi + hstill, clamped (semi_discretize_swe_2D.jl:101-106)
-  s.dry = h <= m.hsm;
-  s.h = s.dry ? m.hsm : h;
-  s.hu = s.dry ? 0.0 : Q[m.n + j];
-  s.hv = s.dry ? 0.0 : Q[2 * m.n + j];
-  return s;
-}
-
-// Sum over faces of F * L for cell c (FP64).
-__device__ __forceinline__ void face_sum_f64(const DevMesh& m, const double* __restrict__ Q, int c,
-                                             const Side<double>& L, double& f0, double& f1, double& f2) {
-  f0 = 0.0; f1 = 0.0; f2 = 0.0;
-  for (int k = 0; k < m.nslot; ++k) {
-    const int32_t nb = m.nb[(size_t)k * m.n + c];
-    if (nb == kNoFace) break;
-    const double nx = m.snx[(size_t)k * m.n + c], ny = m.sny[(size_t)k * m.n + c];
-    const double len = m.slen[(size_t)k * m.n + c];
-    Side<double> R;
-    if (nb >= 0) {
-      R = load_f64(m, Q, nb);
-    } else {
-      const int32_t bf = boundary_index(nb);
-      const int32_t info = m.bfInfo[bf], type = info & 3, grp = info >> 2;
-      R = ghost_state<double>(L, type, nx, ny, m.hsm, type == kBcExitH ? m.exitWse[grp] : 0.0,
-                              type == kBcInletQ ? m.inletQ[grp] : 0.0, type == kBcInletQ ? m.totalA[grp] : 1.0,
-                              m.bfLp23[bf], m.man[c]);
-    }
-    double F[3];
-    roe_flux<double>(L, R, R.xi - L.xi, m.g, nx, ny, m.hsm, F);
-    f0 = f0 + F[0] * len;
-    f1 = f1 + F[1] * len;
-    f2 = f2 + F[2] * len;
-  }
-}
-
-// CFL candidate A / sum_f L (|u.n| + sqrt(g h)) of one cell.
-__device__ __forceinline__ double cfl_candidate_f64(const DevMesh& m, int c, double xi, double qx, double qy) {
-  double h = xi + m.hst[c];
-  if (h <= m.hsm) { h = m.hsm; qx = 0.0; qy = 0.0; }
-  const double u = qx / h, v = qy / h, a = sqrt(m.g * h);
-  double s = 0.0;
-  for (int k = 0; k < m.nslot; ++k) {
-    const int32_t nb = m.nb[(size_t)k * m.n + c];
-    if (nb == kNoFace) break;
-    s += m.slen[(size_t)k * m.n + c] * (fabs(u * m.snx[(size_t)k * m.n + c] + v * m.sny[(size_t)k * m.n + c]) + a);
-  }
-  return m.area[c] / s;
-}
-
-__global__ void __launch_bounds__(kBlock) k_stage_f64(DevMesh m, DevScalars s, int mode, const double* __restrict__ Qin,
-                                                      const double* Qbase, double* Qout, int cfl) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  const bool active = c < m.n;
-  double cand = INFINITY;
-  if (active) {
-    const Side<double> L = load_f64(m, Qin, c);
-    double f0, f1, f2;
-    face_sum_f64(m, Qin, c, L, f0, f1, f2);
-    const double A = m.area[c];
-    const double r0 = -f0 / A, r1 = -f1 / A, r2 = -f2 / A;     // :415
-    // Sources (:449-559): (h > h_small) * (g xi S0 - friction), continuity 0.
-    const double fr = friction_coef(m.g, m.kn2, m.hsm, m.man[c], L.h, L.hu, L.hv);
-    const double sx = L.dry ? 0.0 : (m.g * L.xi * m.s0x[c] - fr * L.hu);
-    const double sy = L.dry ? 0.0 : (m.g * L.xi * m.s0y[c] - fr * L.hv);
-    const double d0 = r0 + 0.0, d1 = r1 + sx, d2 = r2 + sy;
-    if (mode == kModeRhs) {
-      Qout[c] = d0; Qout[m.n + c] = d1; Qout[2 * m.n + c] = d2;
-    } else {
-      const double dt = *s.dt;
-      double x0, x1, x2;
-      if (mode == kModeStage2) {
-        x0 = 0.5 * (Qbase[c] + (Qin[c] + dt * d0));
-        x1 = 0.5 * (Qbase[m.n + c] + (Qin[m.n + c] + dt * d1));
-        x2 = 0.5 * (Qbase[2 * m.n + c] + (Qin[2 * m.n + c] + dt * d2));
-      } else {
-        x0 = Qin[c] + dt * d0;
-        x1 = Qin[m.n + c] + dt * d1;
-        x2 = Qin[2 * m.n + c] + dt * d2;
-      }
-      if (mode == kModeEulerRef) {
-        // custom_ODE_update_cells (custom_ODE_solvers.jl:18-26): first block compared as if it were h.
-        if (x0 < m.hsm) { x0 = m.hsm; x1 = 0.0; x2 = 0.0; }
-      } else if (x0 + m.hst[c] < m.hsm) {
-        // depth-positivity clamp: h = h_small, q = 0
-        x0 = m.hsm - m.hst[c]; x1 = 0.0; x2 = 0.0;
-      }
-      if (!(isfinite(x0) && isfinite(x1) && isfinite(x2))) atomicOr(s.flags, 1);
-      Qout[c] = x0; Qout[m.n + c] = x1; Qout[2 * m.n + c] = x2;
-      if (cfl) cand = cfl_candidate_f64(m, c, x0, x1, x2);
-    }
-  }
-  if (cfl) block_min_publish(cand, s.cflMin);
-}
-
-__global__ void __launch_bounds__(kBlock) k_cfl_f64(DevMesh m, DevScalars s, const double* __restrict__ Q) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  double cand = INFINITY;
-  if (c < m.n) cand = cfl_candidate_f64(m, c, Q[c], Q[m.n + c], Q[2 * m.n + c]);
-  block_min_publish(cand, s.cflMin);
-}
-
-// total_A = sum_faces L^(5/3) h / n * wet over one inlet-Q boundary (bc_2D.jl:673-679).
-__global__ void __launch_bounds__(kBlock) k_inlet_total_f64(DevMesh m, DevScalars s, const double* __restrict__ Q) {
-  const int g = blockIdx.x;
-  const int o0 = m.inletOff[g], o1 = m.inletOff[g + 1];
-  double acc = 0.0;
-  for (int i = o0 + threadIdx.x; i < o1; i += blockDim.x) {
-    const int c = m.inletCell[i];
-    const Side<double> L = load_f64(m, Q, c);
-    acc += L.dry ? 0.0 : m.inletLp53[i] * L.h / m.man[c] * 1.0;
-  }
-  const double t = block_sum(acc);
-  if (threadIdx.x == 0) {
-    m.totalA[g] = t;
-    if (!(t > 1e-10)) atomicOr(s.flags, 2);
-  }
-}
+using namespace devred;
 
 // ---------------------------------------------------------------------------
 // FP32-compensated path
@@ -369,7 +199,7 @@ __global__ void __launch_bounds__(kBlock) k_stage_f32(DevMesh m, DevScalars s, i
         clamp = dn.dry;   // h <= h_small (within the pair granularity): h = h_small, q = 0
       }
       if (clamp) {
-        const double x0 = (mode == kModeEulerRef) ? m.hsm : m.hsm - ((double)hh + (double)hl);
+        const double x0 = (mode == kModeEulerRef) ? m.hsm : dry_xi(m.hsm, (double)hh + (double)hl);
         xh[0] = (float)x0;
         xl[0] = (float)(x0 - (double)xh[0]);
         xh[1] = xl[1] = xh[2] = xl[2] = 0.0f;
@@ -491,17 +321,6 @@ __global__ void k_flush(uint4* buf, size_t n16) {
 }
 
 }  // namespace
-
-void launch_inlet_total_f64(const DevMesh& m, const DevScalars& s, const double* Q, cudaStream_t st) {
-  if (m.nInlet > 0) k_inlet_total_f64<<<m.nInlet, kBlock, 0, st>>>(m, s, Q);
-}
-void launch_stage_f64(const DevMesh& m, const DevScalars& s, int mode, const double* Qin, const double* Qbase,
-                      double* Qout, bool cfl, cudaStream_t st) {
-  k_stage_f64<<<blocks_for(m.n), kBlock, 0, st>>>(m, s, mode, Qin, Qbase, Qout, cfl ? 1 : 0);
-}
-void launch_cfl_f64(const DevMesh& m, const DevScalars& s, const double* Q, cudaStream_t st) {
-  k_cfl_f64<<<blocks_for(m.n), kBlock, 0, st>>>(m, s, Q);
-}
 void launch_inlet_total_f32(const DevMesh& m, const DevScalars& s, StateF32 X, cudaStream_t st) {
   if (m.nInlet > 0) k_inlet_total_f32<<<m.nInlet, kBlock, 0, st>>>(m, s, X);
 }

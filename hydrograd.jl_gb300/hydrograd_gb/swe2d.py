@@ -188,6 +188,13 @@ class SWE2D:
     def advance(self, nsteps, dt=None, cfl=0.4, graph=True):
         self._chk(lib().hg_advance(self.h, int(nsteps), float(dt) if dt else -1.0, float(cfl), 1 if graph else 0))
 
+    def advance_timed(self, nsteps, dt=None, cfl=0.4, flush_l2=True):
+        """Device time (ms) of nsteps RK2 steps, each timed by CUDA events."""
+        ms = np.zeros(1)
+        self._chk(lib().hg_advance_timed(self.h, int(nsteps), float(dt) if dt else -1.0, float(cfl),
+                                         1 if flush_l2 else 0, _d(ms)))
+        return float(ms[0])
+
     def synchronize(self):
         self._chk(lib().hg_synchronize(self.h))
 

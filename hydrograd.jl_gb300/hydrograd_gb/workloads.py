@@ -70,16 +70,26 @@ def _pack_strings(strings):
 
 
 def initial_xi(h, wstill, zb):
-    """xi = h - hstill with hstill = wstill - zb, nudged up by ulps where
-    rounding would put xi + hstill below the intended depth (so a cell set to
-    h_small is not rejected by the initial-depth check, process_ICs_2D.jl:97-99)."""
+    """xi = h - hstill with hstill = wstill - zb.
+
+    A cell meant to be dry (h == h_small) gets the largest xi whose FP64 depth
+    xi + hstill does not exceed h_small, so the RHS clamps it (h <= h_small,
+    semi_discretize_swe_2D.jl:104).  Rounding alone would leave about half of
+    such cells one ulp above h_small, i.e. a wet film 1e-19 m thick whose
+    Manning friction is stiff enough to break any explicit step."""
     hst = wstill - zb
     xi = h - hst
+    dry = h <= H_SMALL
     for _ in range(8):
-        bad = xi + hst < h
-        if not bad.any():
+        hi = dry & (xi + hst > h)
+        if not hi.any():
             break
-        xi[bad] = np.nextafter(xi[bad], np.inf)
+        xi[hi] = np.nextafter(xi[hi], -np.inf)
+    for _ in range(8):
+        lo = ~dry & (xi + hst < h)
+        if not lo.any():
+            break
+        xi[lo] = np.nextafter(xi[lo], np.inf)
     return xi
 
 
@@ -130,9 +140,23 @@ def dam_break(nx=200, ny=40, Lx=100.0, Ly=20.0, n=0.03, h_left=1.0, h_right=0.5,
     return case
 
 
-def river_triangles(n=708, L=2000.0, seed=0, inlet_q=500.0, exit_wse=2.0, wstill=2.0, pool_h=1.5,
-                    pool_center=(300.0, 1000.0), pool_radius=350.0, n_bumps=20, n_zones=5, jitter=0.2):
-    """Triangulated 2 km reach with moving wet/dry fronts (2 n^2 cells)."""
+def river_triangles(n=708, L=2000.0, seed=0, inlet_q=500.0, exit_wse=None, wstill=None, pool_h=1.5,
+                    pool_center=(300.0, 1000.0), pool_radius=350.0, n_bumps=20, n_zones=5, jitter=0.2,
+                    dry_land=False):
+    """Triangulated reach of 2 n^2 cells.
+
+    dry_land=False (the benchmark state): a lake at rest at wstill (default
+    0.3 m above the highest bed cell, so every cell is wet) with the water
+    surface raised by pool_h inside the pool disk -- the release sends a bore
+    across the reach; exit-H holds the lake level.  dry_land=True: every cell
+    outside the pool is dry (h = h_small) and the pool touches the inlet.
+
+    The reference scheme is not robust on a dry bed: at a dry bank its Roe
+    wall branch keeps the dry side's xi (swe_2D_solvers.jl:23-53) and pumps
+    mass into the wet cell even at rest, and a flooded cell gets the full
+    one-sided pressure as momentum while nearly empty.  Dry-bed states are
+    therefore used for short parity runs, not for the long benchmark runs.
+    """
     rs = Stream(seed)
     dx = L / n
     X, Y = _grid_nodes(n, n, L, L)
@@ -180,11 +204,18 @@ def river_triangles(n=708, L=2000.0, seed=0, inlet_q=500.0, exit_wse=2.0, wstill
     mat = np.argmin(d2, axis=1).astype(np.int32)
     zb = ((Z[cells[:, 0]] + Z[cells[:, 1]]) + Z[cells[:, 2]]) / 3    # mean of node z, in the mesh builder's order
     pool = (cx - pool_center[0]) ** 2 + (cy - pool_center[1]) ** 2 < pool_radius ** 2
-    h = np.where(pool, pool_h, H_SMALL)
+    if wstill is None:
+        wstill = 2.0 if dry_land else float(np.ceil((zb.max() + 0.3) * 10.0) / 10.0)
+    if exit_wse is None:
+        exit_wse = 2.0 if dry_land else wstill
+    if dry_land:
+        h = np.where(pool, pool_h, H_SMALL)
+    else:
+        h = (wstill - zb) + np.where(pool, pool_h, 0.0)
     xi = initial_xi(h, np.full(N, wstill), zb)
     case.update(mat_id=mat, manning_zones=zones_n, inlet_q=np.array([inlet_q]), exit_wse=np.array([exit_wse]),
                 wstill=np.full(N, wstill), Q0=np.concatenate([xi, np.zeros(N), np.zeros(N)]),
-                zb_cells=zb, name=f"river_tri_{n}x{n}x2")
+                zb_cells=zb, name=f"river_tri_{n}x{n}x2" + ("_dry" if dry_land else ""))
     return case
 
 

@@ -186,6 +186,10 @@ int hg_launch_count(const hg_ctx* ctx, int64_t* count);
 int hg_time_stage_kernel(hg_ctx* ctx, int32_t n, int32_t flush_l2, double* avg_ms);
 /* Write a device buffer larger than L2 (used between timed iterations). */
 int hg_flush_l2(hg_ctx* ctx);
+/* nsteps SSP-RK2 steps on the resident state, each bracketed by CUDA events on
+ * the context's stream; when flush_l2 != 0 an L2 flush runs before each step,
+ * outside the events.  total_ms receives the summed device time of the steps. */
+int hg_advance_timed(hg_ctx* ctx, int32_t nsteps, double dt, double cfl, int32_t flush_l2, double* total_ms);
 /* Page-locked host buffers for fast host<->device copies of states. */
 int hg_pinned_alloc(int64_t bytes, void** out);
 int hg_pinned_free(void* p);

@@ -583,16 +583,28 @@ void euler_step_reference(const Case& cs, const Params<T>& p, std::vector<T>& Q,
     if (value(Q[i]) < cs.k.h_small) { Q[i] = T(cs.k.h_small); Q[N + i] = T(0.0); Q[2 * N + i] = T(0.0); }
 }
 
+// xi of a dry cell: the largest xi with xi + hstill <= h_small in FP64, so
+// that the RHS sees the cell as dry (h <= h_small).  h_small - hstill alone can
+// round to a depth one ulp above h_small: a wet film whose Manning friction
+// (h + h_small)^(-7/3) breaks any explicit step.
+inline double dry_xi(double h_small, double hstill) {
+  double x = h_small - hstill;
+  while (x + hstill > h_small) x = std::nextafter(x, -INFINITY);
+  return x;
+}
+
 // Depth-positivity clamp applied after each explicit stage: where
-// h = xi + hstill < h_small, set h = h_small (xi = h_small - hstill) and q = 0.
-// With hstill = 0 this is exactly custom_ODE_update_cells' clamp
-// (custom_ODE_solvers.jl:18-26); for hstill != 0 it clamps the depth, not xi.
+// h = xi + hstill <= h_small the cell is dry: xi = dry_xi (h = h_small) and
+// q = 0.  With hstill = 0 this is custom_ODE_update_cells' clamp
+// (custom_ODE_solvers.jl:18-26), except that it also resets a cell sitting
+// exactly at h_small, whose momentum the RHS ignores (it clamps h <= h_small,
+// semi_discretize_swe_2D.jl:104-106) but which would otherwise accumulate.
 template <class T>
 inline void clamp_stage(const Case& cs, T* Q) {
   const int N = cs.mesh.nCells;
   for (int i = 0; i < N; ++i)
-    if (value(Q[i]) + cs.hstill[i] < cs.k.h_small) {
-      Q[i] = T(cs.k.h_small - cs.hstill[i]);
+    if (value(Q[i]) + cs.hstill[i] <= cs.k.h_small) {
+      Q[i] = T(dry_xi(cs.k.h_small, cs.hstill[i]));
       Q[N + i] = T(0.0);
       Q[2 * N + i] = T(0.0);
     }

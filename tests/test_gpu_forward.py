@@ -1,8 +1,13 @@
 """CUDA forward path vs the oracle, through the C ABI.
 
-Tolerances (normwise, per state block b: max|gpu - oracle| / max|oracle|):
-  FP64 path   1e-12 for one RHS evaluation, 1e-10 after many steps
-  FP32C path  1e-5  (state), per the FP32-compensated contract
+Error measures (normwise relative):
+  RHS:    max|gpu - oracle| / max(max|oracle|, S), S = the flux scale of the
+          state, max_c (g h^2/2 + |q|^2/h) * perimeter_c / area_c: the size of
+          the terms the RHS sums, so that a residual that cancels to ~0 (a
+          near-steady state) is judged against what was summed.
+  State:  per block b, max|gpu_b - oracle_b| / max(max|oracle_b|, 1e-3 max|oracle|).
+Tolerances: FP64 path 1e-12 for one RHS, 1e-10 after many steps;
+            FP32C path 2e-5 for one RHS, 1e-5 for states.
 """
 import numpy as np
 import pytest
@@ -16,12 +21,35 @@ pytestmark = pytest.mark.gpu
 
 
 def block_err(a, b, N):
+    """State error (see module docstring)."""
     out = []
     for k in range(3):
         ref = b[k * N:(k + 1) * N]
         scale = max(np.abs(ref).max(), np.abs(b).max() * 1e-3, 1e-300)
         out.append(np.abs(a[k * N:(k + 1) * N] - ref).max() / scale)
     return max(out)
+
+
+def flux_scale(o, Q, g=9.81, h_small=1e-3):
+    N = o.n_cells
+    m = o.mesh_arrays()
+    lengths = m["face_lengths"][m["cell_faces"].reshape(N, 8)]
+    per = np.where(np.arange(8)[None, :] < o._keep["cell_node_count"][:, None], lengths, 0.0).sum(axis=1)
+    h = np.maximum(Q[:N] + o.hstill(), h_small)
+    q2 = Q[N:2 * N] ** 2 + Q[2 * N:] ** 2
+    return np.max((0.5 * g * h * h + q2 / h) * per / m["areas"])
+
+
+def rhs_err(a, b, o, Q):
+    """RHS error (see module docstring)."""
+    scale = max(np.abs(b).max(), flux_scale(o, Q))
+    return np.abs(a - b).max() / scale
+
+
+def small_river(n=32, L=500.0, dry=False):
+    """A small copy of the benchmark reach (dry=True: dry bed outside the pool)."""
+    return river_triangles(n=n, L=L, inlet_q=500.0 * L / 2000.0, pool_center=(0.15 * L, 0.5 * L),
+                           pool_radius=0.175 * L, dry_land=dry)
 
 
 def setup_pair(case, precision="fp64", order="hilbert", manning=None):
@@ -58,7 +86,7 @@ def test_rhs_fp64_matches_oracle_on_reference_cases(name, order):
     d, states = golden_states(name)
     ctx, o, N = setup_pair(d, order=order)
     for Q in states:
-        assert block_err(ctx.rhs(Q), o.rhs(Q), N) <= 1e-12
+        assert rhs_err(ctx.rhs(Q), o.rhs(Q), o, Q) <= 1e-12
 
 
 def test_bed_slope_on_device_context_matches_reference_truth():
@@ -68,14 +96,16 @@ def test_bed_slope_on_device_context_matches_reference_truth():
     assert np.array_equal(ctx.bed()["S0"], S0t)
 
 
-def test_rhs_fp64_dam_break_and_wet_dry_fronts():
-    for case in (dam_break(), river_triangles(n=32, L=500.0, pool_center=(75.0, 250.0), pool_radius=90.0)):
-        ctx, o, N = setup_pair(case)
-        Q = case["Q0"]
-        assert block_err(ctx.rhs(Q), o.rhs(Q), N) <= 1e-12
-        # advance the oracle so that fronts, dry cells and inlet/exit ghosts are exercised
-        Qm = o.rk2(Q, 40, cfl=0.4, nthreads=4)
-        assert block_err(ctx.rhs(Qm), o.rhs(Qm), N) <= 1e-12
+@pytest.mark.parametrize("which", ["dam_break", "river_wet", "river_dry"])
+def test_rhs_fp64_dam_break_and_wet_dry_fronts(which):
+    case = {"dam_break": dam_break, "river_wet": small_river, "river_dry": lambda: small_river(dry=True)}[which]()
+    ctx, o, N = setup_pair(case)
+    Q = case["Q0"]
+    assert rhs_err(ctx.rhs(Q), o.rhs(Q), o, Q) <= 1e-12
+    # advance the oracle so that fronts, dry cells and inlet/exit ghosts are exercised
+    # (a dry bed only briefly: the reference scheme floods dry cells unstably)
+    Qm = o.rk2(Q, 8 if which == "river_dry" else 40, cfl=0.4, nthreads=4)
+    assert rhs_err(ctx.rhs(Qm), o.rhs(Qm), o, Qm) <= 1e-12
 
 
 def test_rk2_dam_break_1000_steps_fp64():
@@ -89,7 +119,7 @@ def test_rk2_dam_break_1000_steps_fp64():
 
 
 def test_rk2_cfl_river_fp64_follows_oracle():
-    case = river_triangles(n=32, L=500.0, pool_center=(75.0, 250.0), pool_radius=90.0)
+    case = small_river()
     ctx, o, N = setup_pair(case)
     Q, dts = ctx.integrate(case["Q0"], 300, method="rk2", cfl=0.4)
     assert abs(dts[0] - o.cfl_dt(case["Q0"], 0.4)) <= 1e-14 * dts[0]
@@ -124,23 +154,23 @@ def test_active_parameter_injection_matches_oracle():
     pz = np.array([0.021, 0.034, 0.027])
     pe = SWE2DExtraParameters(ctx, "ManningN", mat_id=d["mat_id"])
     o2.set_manning_cells(pz[d["mat_id"]])
-    assert block_err(swe_2d_rhs(None, Q, pz, 0.0, pe), o2.rhs(Q), N) <= 1e-12
+    assert rhs_err(swe_2d_rhs(None, Q, pz, 0.0, pe), o2.rhs(Q), o2, Q) <= 1e-12
     # zb (hstill kept)
     zb = o2.bed()[0] + 0.01 * np.sin(np.arange(N))
     pe = SWE2DExtraParameters(ctx, "zb")
     o2.set_zb_cells(zb)
-    assert block_err(swe_2d_rhs(None, Q, zb, 0.0, pe), o2.rhs(Q), N) <= 1e-12
+    assert rhs_err(swe_2d_rhs(None, Q, zb, 0.0, pe), o2.rhs(Q), o2, Q) <= 1e-12
     # inlet Q, in-place form
     pe = SWE2DExtraParameters(ctx, "Q", bInPlaceODE=True)
     o2.set_inlet_q([0.25])
     out = np.zeros(3 * N)
     r = swe_2d_rhs(out, Q, np.array([0.25]), 0.0, pe)
     assert r is out
-    assert block_err(out, o2.rhs(Q), N) <= 1e-12
+    assert rhs_err(out, o2.rhs(Q), o2, Q) <= 1e-12
 
 
 def test_runs_are_bitwise_deterministic():
-    case = river_triangles(n=24, L=400.0, pool_center=(60.0, 200.0), pool_radius=80.0)
+    case = small_river(24, 400.0)
     ctx, _, _ = setup_pair(case)
     a, _ = ctx.integrate(case["Q0"], 100, cfl=0.4)
     b, _ = ctx.integrate(case["Q0"], 100, cfl=0.4)
@@ -148,7 +178,7 @@ def test_runs_are_bitwise_deterministic():
 
 
 def test_device_resident_graph_path_equals_integrate():
-    case = river_triangles(n=24, L=400.0, pool_center=(60.0, 200.0), pool_radius=80.0)
+    case = small_river(24, 400.0)
     ctx, _, _ = setup_pair(case)
     a, dts = ctx.integrate(case["Q0"], 120, cfl=0.4)
     ctx.upload(case["Q0"])
@@ -160,15 +190,20 @@ def test_device_resident_graph_path_equals_integrate():
 
 @pytest.mark.parametrize("order", ["none", "hilbert"])
 def test_rhs_fp32c_within_tolerance(order):
-    case = river_triangles(n=32, L=500.0, pool_center=(75.0, 250.0), pool_radius=90.0)
+    case = small_river()
     ctx, o, N = setup_pair(case, precision="fp32c", order=order)
     Qm = o.rk2(case["Q0"], 40, cfl=0.4, nthreads=4)
+    dry = small_river(dry=True)
     for Q in (case["Q0"], Qm):
-        assert block_err(ctx.rhs(Q), o.rhs(Q), N) <= 2e-5
+        assert rhs_err(ctx.rhs(Q), o.rhs(Q), o, Q) <= 2e-5
+    ctx, o, N = setup_pair(dry, precision="fp32c", order=order)
+    Qd = o.rk2(dry["Q0"], 8, cfl=0.4, nthreads=4)
+    for Q in (dry["Q0"], Qd):
+        assert rhs_err(ctx.rhs(Q), o.rhs(Q), o, Q) <= 2e-5
 
 
 def test_rk2_fp32c_state_error_vs_fp64_oracle():
-    case = river_triangles(n=32, L=500.0, pool_center=(75.0, 250.0), pool_radius=90.0)
+    case = small_river()
     ctx, o, N = setup_pair(case, precision="fp32c")
     Q, dts = ctx.integrate(case["Q0"], 300, cfl=0.4)
     Qr = case["Q0"].copy()
@@ -178,7 +213,7 @@ def test_rk2_fp32c_state_error_vs_fp64_oracle():
 
 
 def test_dry_inlet_is_reported():
-    case = river_triangles(n=16, L=400.0, pool_center=(300.0, 300.0), pool_radius=40.0)
+    case = river_triangles(n=16, L=400.0, pool_center=(300.0, 300.0), pool_radius=40.0, dry_land=True)
     ctx, _, _ = setup_pair(case)
     with pytest.raises(HgError) as e:
         ctx.rhs(case["Q0"])
