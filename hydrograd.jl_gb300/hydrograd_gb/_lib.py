@@ -68,6 +68,7 @@ SIGNATURES = {
     "hg_time_stage_kernel": [_vp, ctypes.c_int32, ctypes.c_int32, _dp],
     "hg_flush_l2": [_vp],
     "hg_advance_timed": [_vp, ctypes.c_int32, ctypes.c_double, ctypes.c_double, ctypes.c_int32, _dp],
+    "hg_rhs_device_noalloc": [_vp, _vp, _vp, _vp, _vp],
     "hg_pinned_alloc": [ctypes.c_int64, ctypes.POINTER(_vp)],
     "hg_pinned_free": [_vp],
 }

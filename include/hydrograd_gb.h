@@ -190,6 +190,28 @@ int hg_flush_l2(hg_ctx* ctx);
  * the context's stream; when flush_l2 != 0 an L2 flush runs before each step,
  * outside the events.  total_ms receives the summed device time of the steps. */
 int hg_advance_timed(hg_ctx* ctx, int32_t nsteps, double dt, double cfl, int32_t flush_l2, double* total_ms);
+/* ---- no-allocation RHS ----------------------------------------------------- */
+/*
+ * No counterpart in the reference.  dQdt = RHS(Q) of an FP64 context for a
+ * state that is already in device memory, for callers that cannot allocate
+ * device memory once their time loop runs (an integrator inside CUDA.jl's
+ * memory pool, or a step being recorded into a CUDA graph, where allocation
+ * and device synchronisation are not allowed).  It calls no cudaMalloc or
+ * cudaFree: the scratch it needs (inlet-Q conveyance totals and an error-flag
+ * word) is a static device array sized for HG_NOALLOC_MAX_INLETQ inlet-Q
+ * boundaries; a context with more is rejected with HG_ERR_ARG.
+ *   d_Q, d_dQ: device pointers to 3 n doubles in the device cell order
+ *              (perm[device id] = caller id from hg_mesh_order with consts.order).
+ *   d_flags:   device int32 that receives the error flags (bit 1: inlet-Q
+ *              conveyance not positive), or NULL.  Nothing is checked on the host.
+ *   stream:    cudaStream_t to run on, or NULL for the context's stream.
+ * The call is asynchronous.  Its first call on a device looks up the scratch
+ * array's device address; make that first call before any stream capture.
+ * All calls share the scratch array: calls that overlap on the GPU race.
+ */
+#define HG_NOALLOC_MAX_INLETQ 64
+int hg_rhs_device_noalloc(hg_ctx* ctx, const double* d_Q, double* d_dQ, int32_t* d_flags, void* stream);
+
 /* Page-locked host buffers for fast host<->device copies of states. */
 int hg_pinned_alloc(int64_t bytes, void** out);
 int hg_pinned_free(void* p);
