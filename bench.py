@@ -270,6 +270,37 @@ def run_ours(args):
     e2e = {"value": ws * N * args.e2e_chunk * calls / el, "unit": UNIT,
            "h2d_bytes_per_step": 3 * N * 8 / args.e2e_chunk, "d2h_bytes_per_step": 3 * N * 8 / args.e2e_chunk,
            "calls": calls, "steps_per_call": args.e2e_chunk}
+    # Forward + adjoint: hg_loss_and_grad over adj_steps fixed-dt steps (the CFL
+    # step of the initial state), checkpoints every 50 steps, 64 probes.
+    adj = {}
+    if args.adj_steps > 0:
+        from hydrograd_gb.workloads import probes_and_perturbation
+        probes, _ = probes_and_perturbation(case, 64)
+        dt_adj = 0.5 * ctxs["fp64"].integrate(case["Q0"], 1, cfl=0.4)[1][0]
+        hs = ctxs["fp64"].bed()["hstill"]
+        obs = np.tile(case["Q0"][probes] + hs[probes] + 0.01, (args.adj_steps, 1))
+        grads = {}
+        for prec in ("fp32c", "fp64"):
+            ctx = ctxs[prec]
+            ctx.loss_and_grad(case["Q0"], 4, dt_adj, probes, obs[:4], ckpt_every=2)       # warm-up / allocation
+            barrier(dist)
+            t0 = time.perf_counter()
+            r = ctx.loss_and_grad(case["Q0"], args.adj_steps, dt_adj, probes, obs, ckpt_every=50)
+            el = max_over_ranks(dist, time.perf_counter() - t0)
+            grads[prec] = r
+            adj[prec] = {"value": ws * N * args.adj_steps / el, "seconds": el, "steps": args.adj_steps}
+        g32, g64 = grads["fp32c"], grads["fp64"]
+        zones = case["mat_id"]
+        gz32 = np.array([g32["g_manning"][zones == z].sum() for z in range(len(case["manning_zones"]))])
+        gz64 = np.array([g64["g_manning"][zones == z].sum() for z in range(len(case["manning_zones"]))])
+        adj["fp32c_over_fp64_speedup"] = adj["fp32c"]["value"] / adj["fp64"]["value"]
+        adj["error_fp32c_vs_fp64"] = {
+            "grad_zone_n_rel": float(np.abs(gz32 - gz64).max() / np.abs(gz64).max()),
+            "grad_inlet_q_rel": float(abs(g32["g_inletq"][0] - g64["g_inletq"][0]) / abs(g64["g_inletq"][0])),
+            "grad_zb_field_rel_linf": float(np.abs(g32["g_zb"] - g64["g_zb"]).max() / np.abs(g64["g_zb"]).max()),
+            "loss_rel": float(abs(g32["loss"] - g64["loss"]) / abs(g64["loss"])),
+        }
+        adj["config"] = f"{args.adj_steps} fixed-dt steps (dt = half the initial CFL step), checkpoints every 50, 64 probes"
     if rank != 0:
         return
     peak, peak_kind = load_peaks()
@@ -308,6 +339,7 @@ def run_ours(args):
                  "stage_gbs": fp64_bytes / (out["fp64"]["stage_ms"] * 1e-3) / 1e9,
                  "warm_value": out["fp64"]["warm_value"]},
         "fp32c_over_fp64_speedup": f32["value"] / out["fp64"]["value"],
+        "fwd_adjoint": adj,
         "warm_value": f32["warm_value"], "simulated_seconds": f32["sim_time"],
         "error": err,
         "roofline": roof,
@@ -332,6 +364,7 @@ def main():
     ap.add_argument("--oracle-steps", type=int, default=20)
     ap.add_argument("--ref-steps", type=int, default=20)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--adj-steps", type=int, default=100, help="steps of the forward+adjoint measurement (0: skip)")
     args = ap.parse_args()
     if args.steps_fp64 is None:
         args.steps_fp64 = args.steps

@@ -1,16 +1,349 @@
-// Host driver of the discrete adjoint (checkpointed SSP-RK2).
+// Host driver of the discrete adjoint of SSP-RK2 with checkpointing.
+//
+// Forward step (fixed dt), C the depth-positivity clamp:
+//   Q1 = C(Q0 + dt R(Q0)),   Q2 = C(0.5 (Q0 + (Q1 + dt R(Q1))))
+// Loss = mean over steps k and probes p of (h_p^k - obs_kp)^2, h = xi + hstill
+// (the probe-depth misfit; cf. the WSE loss of swe_2D_inversion.jl:404-416).
+// Reverse step, with mu2 = dL/dQ2 masked by the stage-2 clamp:
+//   mu1 = M1 (0.5 mu2 + 0.5 dt J(Q1)^T mu2)
+//   mu2' = M0 (0.5 mu2 + mu1 + dt J(Q0)^T mu1)
+//   dL/dtheta += 0.5 dt (dR/dtheta)(Q1)^T mu2 + dt (dR/dtheta)(Q0)^T mu1
+// The forward pass stores the state every ckpt_every steps; the reverse sweep
+// recomputes one segment at a time, keeping that segment's stage states.
+// Loss and parameter gradients accumulate in FP64.
 #include "hg_adjoint.hpp"
 
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "hg_adjoint_state.hpp"
 #include "hg_ctx.hpp"
 
 namespace hg {
 
-struct AdjointBuffers {};
+struct AdjointBuffers {
+  AdjDev dev;
+  std::vector<void*> fixed;   // allocations sized by the mesh
+  double* ckpt = nullptr;
+  size_t ckptStates = 0;
+  double* seg = nullptr;
+  size_t segStates = 0;
+  double *mu1 = nullptr, *mu2 = nullptr, *gzb = nullptr;
+  int32_t* probes = nullptr;
+  double* obs = nullptr;
+  size_t probeCap = 0, obsCap = 0;
+  ~AdjointBuffers() {
+    for (void* p : fixed) cudaFree(p);
+    cudaFree(ckpt);
+    cudaFree(seg);
+    cudaFree(probes);
+    cudaFree(obs);
+  }
+};
 
-int adjoint_loss_and_grad(hg_ctx* ctx, const double*, int32_t, double, int32_t, const int32_t*, const double*, int32_t,
-                          double*, double*, double*, double*, double*) {
-  ctx->err = "hg_loss_and_grad: not available in this build";
-  return HG_ERR_UNSUPPORTED;
+namespace {
+
+int fail(hg_ctx* c, int code, const std::string& m) {
+  c->err = m;
+  return code;
+}
+
+#define ADJ_CUDA(c, call)                                                                        \
+  do {                                                                                           \
+    cudaError_t e_ = (call);                                                                     \
+    if (e_ != cudaSuccess) return fail((c), HG_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+template <class T>
+cudaError_t falloc(AdjointBuffers* b, T** p, size_t count) {
+  void* q = nullptr;
+  cudaError_t e = cudaMalloc(&q, std::max<size_t>(count, 1) * sizeof(T));
+  if (e == cudaSuccess) {
+    b->fixed.push_back(q);
+    *p = static_cast<T*>(q);
+  }
+  return e;
+}
+
+int setup(hg_ctx* c) {
+  if (c->adj) return HG_OK;
+  auto* b = new AdjointBuffers();
+  c->adj = b;
+  const HostMesh& m = c->hm;
+  const int N = c->n;
+  AdjDev& a = b->dev;
+  ADJ_CUDA(c, falloc(b, &a.gN, N));
+  ADJ_CUDA(c, falloc(b, &a.gS0x, N));
+  ADJ_CUDA(c, falloc(b, &a.gS0y, N));
+  ADJ_CUDA(c, falloc(b, &a.gZb, N));
+  ADJ_CUDA(c, falloc(b, &a.bfGradQ, c->dm.nbf));
+  ADJ_CUDA(c, falloc(b, &a.bfGradTA, c->dm.nbf));
+  ADJ_CUDA(c, falloc(b, &a.gQ, c->dm.nInlet));
+  ADJ_CUDA(c, falloc(b, &a.loss, 1));
+  ADJ_CUDA(c, falloc(b, &b->mu1, (size_t)3 * N));
+  ADJ_CUDA(c, falloc(b, &b->mu2, (size_t)3 * N));
+  ADJ_CUDA(c, falloc(b, &b->gzb, N));
+  // Inlet tables: boundary-face index of each inlet CSR entry (faces numbered
+  // by face id, as the forward tables), and per group the distinct cells with
+  // the sum of L^(5/3) over their faces in the group.
+  std::vector<int> bfOf(m.nFaces, -1);
+  int nbf = 0;
+  for (int f = 0; f < m.nFaces; ++f)
+    if (m.faceC1[f] < 0) bfOf[f] = nbf++;
+  std::vector<int32_t> inletBf, uOff(1, 0), uCell;
+  std::vector<double> uCoef;
+  for (int g : m.inletGroups) {
+    std::map<int, double> coef;   // caller cell id -> sum L^(5/3)
+    std::vector<int> order;
+    for (int f : m.bnd[g].faces) {
+      inletBf.push_back(bfOf[f]);
+      const int cell = m.faceC0[f];
+      if (!coef.count(cell)) order.push_back(cell);
+      coef[cell] += std::pow(m.faceLen[f], 5.0 / 3.0);
+    }
+    for (int cell : order) {
+      uCell.push_back(c->inv[cell]);
+      uCoef.push_back(coef[cell]);
+    }
+    uOff.push_back((int32_t)uCell.size());
+  }
+  int32_t *dBf, *dUOff, *dUCell;
+  double* dUCoef;
+  ADJ_CUDA(c, falloc(b, &dBf, inletBf.size()));
+  ADJ_CUDA(c, falloc(b, &dUOff, uOff.size()));
+  ADJ_CUDA(c, falloc(b, &dUCell, uCell.size()));
+  ADJ_CUDA(c, falloc(b, &dUCoef, uCoef.size()));
+  if (!inletBf.empty()) ADJ_CUDA(c, cudaMemcpy(dBf, inletBf.data(), inletBf.size() * 4, cudaMemcpyHostToDevice));
+  ADJ_CUDA(c, cudaMemcpy(dUOff, uOff.data(), uOff.size() * 4, cudaMemcpyHostToDevice));
+  if (!uCell.empty()) {
+    ADJ_CUDA(c, cudaMemcpy(dUCell, uCell.data(), uCell.size() * 4, cudaMemcpyHostToDevice));
+    ADJ_CUDA(c, cudaMemcpy(dUCoef, uCoef.data(), uCoef.size() * 8, cudaMemcpyHostToDevice));
+  }
+  a.inletBf = dBf;
+  a.inletUOff = dUOff;
+  a.inletUCell = dUCell;
+  a.inletUCoef = dUCoef;
+  return HG_OK;
+}
+
+int reserve(hg_ctx* c, double** p, size_t* have, size_t states) {
+  if (states <= *have) return HG_OK;
+  cudaFree(*p);
+  *p = nullptr;
+  *have = 0;
+  ADJ_CUDA(c, cudaMalloc(p, states * 3 * (size_t)c->n * sizeof(double)));
+  *have = states;
+  return HG_OK;
+}
+
+}  // namespace
+
+namespace {
+
+// FP32-compensated state buffer of `states` states: [states][n] float4 then [states][n] float2.
+struct F32States {
+  float4* x = nullptr;
+  float2* q = nullptr;
+  StateF32 at(size_t i, int n) const { return StateF32{x + i * (size_t)n, q + i * (size_t)n}; }
+};
+
+F32States f32_view(double* base, size_t states, int n) {
+  F32States v;
+  v.x = reinterpret_cast<float4*>(base);
+  v.q = reinterpret_cast<float2*>(reinterpret_cast<char*>(base) + states * (size_t)n * sizeof(float4));
+  return v;
+}
+
+}  // namespace
+
+int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int32_t C, const int32_t* probeCells,
+                          const double* obs, int32_t P, double* loss, double* gManning, double* gZb, double* gInlet,
+                          double* Qfinal) {
+  int rc = setup(c);
+  if (rc) return rc;
+  AdjointBuffers* b = c->adj;
+  AdjDev& a = b->dev;
+  const int N = c->n;
+  const size_t n3 = (size_t)3 * N;
+  const bool f64 = c->precision == HG_FP64;
+  if (C <= 0) C = K;
+  C = std::min(C, K);
+  const int nck = (K + C - 1) / C;
+  // A double-sized state slot holds one FP32-compensated state too (24 B per cell either way).
+  rc = reserve(c, &b->ckpt, &b->ckptStates, (size_t)nck);
+  if (rc) return rc;
+  rc = reserve(c, &b->seg, &b->segStates, (size_t)(2 * C + 1));
+  if (rc) return rc;
+  cudaStream_t st = c->stream;
+  // Probes (device order) and observations.
+  if ((size_t)std::max(P, 1) > b->probeCap) {
+    cudaFree(b->probes);
+    b->probes = nullptr;
+    ADJ_CUDA(c, cudaMalloc(&b->probes, std::max(P, 1) * sizeof(int32_t)));
+    b->probeCap = std::max(P, 1);
+  }
+  const size_t nobs = (size_t)K * std::max(P, 0);
+  if (std::max<size_t>(nobs, 1) > b->obsCap) {
+    cudaFree(b->obs);
+    b->obs = nullptr;
+    ADJ_CUDA(c, cudaMalloc(&b->obs, std::max<size_t>(nobs, 1) * sizeof(double)));
+    b->obsCap = std::max<size_t>(nobs, 1);
+  }
+  std::vector<int32_t> pdev(std::max(P, 0));
+  for (int p = 0; p < P; ++p) pdev[p] = c->inv[probeCells[p]];
+  if (P > 0) {
+    ADJ_CUDA(c, cudaMemcpyAsync(b->probes, pdev.data(), P * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+    ADJ_CUDA(c, cudaMemcpyAsync(b->obs, obs, nobs * sizeof(double), cudaMemcpyHostToDevice, st));
+  }
+  // Accumulators and dt.
+  ADJ_CUDA(c, cudaMemsetAsync(a.gN, 0, N * sizeof(double), st));
+  ADJ_CUDA(c, cudaMemsetAsync(a.gS0x, 0, N * sizeof(double), st));
+  ADJ_CUDA(c, cudaMemsetAsync(a.gS0y, 0, N * sizeof(double), st));
+  ADJ_CUDA(c, cudaMemsetAsync(a.gZb, 0, N * sizeof(double), st));
+  ADJ_CUDA(c, cudaMemsetAsync(a.gQ, 0, std::max(c->dm.nInlet, 1) * sizeof(double), st));
+  ADJ_CUDA(c, cudaMemsetAsync(a.loss, 0, sizeof(double), st));
+  ADJ_CUDA(c, cudaMemsetAsync(c->ds.flags, 0, sizeof(int32_t), st));
+  const float dtf = (float)dt;
+  ADJ_CUDA(c, cudaMemcpyAsync(c->ds.dt, &dt, sizeof(double), cudaMemcpyHostToDevice, st));
+  ADJ_CUDA(c, cudaMemcpyAsync(c->ds.dtf, &dtf, sizeof(float), cudaMemcpyHostToDevice, st));
+  ADJ_CUDA(c, cudaMemcpyAsync(c->Quser, Q0, n3 * sizeof(double), cudaMemcpyHostToDevice, st));
+  const double scale = (P > 0) ? 1.0 / ((double)K * P) : 0.0;
+  const DevMesh& dm = c->dm;
+  const DevScalars& ds = c->ds;
+  const int extraPerStep = 2 * dm.nInlet;
+
+  if (f64) {
+    launch_gather_state_f64(N, c->d_perm, c->Quser, c->QA, st);
+    // Forward pass with checkpoints.
+    for (int s = 0; s < K; ++s) {
+      if (s % C == 0)
+        ADJ_CUDA(c, cudaMemcpyAsync(b->ckpt + (size_t)(s / C) * n3, c->QA, n3 * sizeof(double),
+                                    cudaMemcpyDeviceToDevice, st));
+      launch_inlet_total_f64(dm, ds, c->QA, st);
+      launch_stage_f64(dm, ds, kModeStage1, c->QA, nullptr, c->QB, false, st);
+      launch_inlet_total_f64(dm, ds, c->QB, st);
+      launch_stage_f64(dm, ds, kModeStage2, c->QB, c->QA, c->QA, false, st);
+      launch_probe_loss_f64(dm, a, c->QA, b->probes, b->obs + (size_t)s * P, P, st);
+      c->launches += 3 + extraPerStep;
+    }
+    if (Qfinal) {
+      launch_scatter_state_f64(N, c->d_perm, c->QA, c->Quser, st);
+      ADJ_CUDA(c, cudaMemcpyAsync(Qfinal, c->Quser, n3 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    }
+    // Reverse sweep.
+    ADJ_CUDA(c, cudaMemsetAsync(b->mu2, 0, n3 * sizeof(double), st));
+    launch_probe_adjoint_f64(dm, c->QA, b->mu2, b->probes, b->obs + (size_t)(K - 1) * P, P, scale, st);
+    for (int seg = nck - 1; seg >= 0; --seg) {
+      const int s0 = seg * C, s1 = std::min(K, s0 + C);
+      double* Q0s = b->seg;                          // Q0 of step s0 + i at Q0s + i n3 (i = 0..C)
+      double* Q1s = b->seg + (size_t)(C + 1) * n3;   // Q1 of step s0 + i
+      ADJ_CUDA(c, cudaMemcpyAsync(Q0s, b->ckpt + (size_t)seg * n3, n3 * sizeof(double), cudaMemcpyDeviceToDevice,
+                                  st));
+      for (int s = s0; s < s1; ++s) {
+        const size_t i = (size_t)(s - s0);
+        launch_inlet_total_f64(dm, ds, Q0s + i * n3, st);
+        launch_stage_f64(dm, ds, kModeStage1, Q0s + i * n3, nullptr, Q1s + i * n3, false, st);
+        launch_inlet_total_f64(dm, ds, Q1s + i * n3, st);
+        launch_stage_f64(dm, ds, kModeStage2, Q1s + i * n3, Q0s + i * n3, Q0s + (i + 1) * n3, false, st);
+        c->launches += 2 + extraPerStep;
+      }
+      for (int s = s1 - 1; s >= s0; --s) {
+        const size_t i = (size_t)(s - s0);
+        const double* q0 = Q0s + i * n3;
+        const double* q1 = Q1s + i * n3;
+        launch_inlet_total_f64(dm, ds, q1, st);
+        launch_vjp_f64(dm, a, q1, b->mu2, nullptr, b->mu1, 0.5, 0.0, 0.5 * dt, st);
+        launch_inlet_adjoint_f64(dm, a, q1, b->mu1, 0.5 * dt, st);
+        launch_inlet_total_f64(dm, ds, q0, st);
+        launch_vjp_f64(dm, a, q0, b->mu1, b->mu2, b->mu2, 1.0, 0.5, dt, st);
+        launch_inlet_adjoint_f64(dm, a, q0, b->mu2, dt, st);
+        if (s >= 1) launch_probe_adjoint_f64(dm, q0, b->mu2, b->probes, b->obs + (size_t)(s - 1) * P, P, scale, st);
+        c->launches += 2 + 2 * extraPerStep + (s >= 1 && P > 0 ? 1 : 0);
+      }
+    }
+  } else {
+    const int n = N;
+    const F32States ck = f32_view(b->ckpt, (size_t)nck, n);
+    const F32States sg = f32_view(b->seg, (size_t)(2 * C + 1), n);
+    float* mu1 = reinterpret_cast<float*>(b->mu1);
+    float* mu2 = reinterpret_cast<float*>(b->mu2);
+    const StateF32 XA{c->XA, c->XQA}, XB{c->XB, c->XQB};
+    launch_gather_state_f32(N, c->d_perm, c->Quser, XA, st);
+    auto copy_state = [&](StateF32 dst, StateF32 src) -> cudaError_t {
+      cudaError_t e = cudaMemcpyAsync(dst.x, src.x, (size_t)n * sizeof(float4), cudaMemcpyDeviceToDevice, st);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(dst.q, src.q, (size_t)n * sizeof(float2), cudaMemcpyDeviceToDevice, st);
+      return e;
+    };
+    for (int s = 0; s < K; ++s) {
+      if (s % C == 0) ADJ_CUDA(c, copy_state(ck.at(s / C, n), XA));
+      launch_inlet_total_f32(dm, ds, XA, st);
+      launch_stage_f32(dm, ds, kModeStage1, XA, StateF32{}, XB, nullptr, false, st);
+      launch_inlet_total_f32(dm, ds, XB, st);
+      launch_stage_f32(dm, ds, kModeStage2, XB, XA, XA, nullptr, false, st);
+      launch_probe_loss_f32(dm, a, XA, b->probes, b->obs + (size_t)s * P, P, st);
+      c->launches += 3 + extraPerStep;
+    }
+    if (Qfinal) {
+      launch_scatter_state_f32(N, c->d_perm, XA, c->Quser, st);
+      ADJ_CUDA(c, cudaMemcpyAsync(Qfinal, c->Quser, n3 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    }
+    ADJ_CUDA(c, cudaMemsetAsync(mu2, 0, n3 * sizeof(float), st));
+    launch_probe_adjoint_f32(dm, XA, mu2, b->probes, b->obs + (size_t)(K - 1) * P, P, scale, st);
+    for (int seg = nck - 1; seg >= 0; --seg) {
+      const int s0 = seg * C, s1 = std::min(K, s0 + C);
+      ADJ_CUDA(c, copy_state(sg.at(0, n), ck.at(seg, n)));
+      for (int s = s0; s < s1; ++s) {
+        const size_t i = (size_t)(s - s0);
+        const StateF32 q0 = sg.at(i, n), q1 = sg.at(C + 1 + i, n), q2 = sg.at(i + 1, n);
+        launch_inlet_total_f32(dm, ds, q0, st);
+        launch_stage_f32(dm, ds, kModeStage1, q0, StateF32{}, q1, nullptr, false, st);
+        launch_inlet_total_f32(dm, ds, q1, st);
+        launch_stage_f32(dm, ds, kModeStage2, q1, q0, q2, nullptr, false, st);
+        c->launches += 2 + extraPerStep;
+      }
+      for (int s = s1 - 1; s >= s0; --s) {
+        const size_t i = (size_t)(s - s0);
+        const StateF32 q0 = sg.at(i, n), q1 = sg.at(C + 1 + i, n);
+        launch_inlet_total_f32(dm, ds, q1, st);
+        launch_vjp_f32(dm, a, q1, mu2, nullptr, mu1, 0.5f, 0.0f, 0.5f * dtf, st);
+        launch_inlet_adjoint_f32(dm, a, q1, mu1, 0.5 * dt, st);
+        launch_inlet_total_f32(dm, ds, q0, st);
+        launch_vjp_f32(dm, a, q0, mu1, mu2, mu2, 1.0f, 0.5f, dtf, st);
+        launch_inlet_adjoint_f32(dm, a, q0, mu2, dt, st);
+        if (s >= 1) launch_probe_adjoint_f32(dm, q0, mu2, b->probes, b->obs + (size_t)(s - 1) * P, P, scale, st);
+        c->launches += 2 + 2 * extraPerStep + (s >= 1 && P > 0 ? 1 : 0);
+      }
+    }
+  }
+  launch_zb_gradient(dm, a, b->gzb, st);
+  c->launches += 1;
+  ADJ_CUDA(c, cudaGetLastError());
+  // Results, mapped back to the caller's cell order.
+  std::vector<double> hN(N), hZ(N), hQ(std::max(dm.nInlet, 1));
+  double hl = 0.0;
+  ADJ_CUDA(c, cudaMemcpyAsync(&hl, a.loss, sizeof(double), cudaMemcpyDeviceToHost, st));
+  ADJ_CUDA(c, cudaMemcpyAsync(hN.data(), a.gN, N * sizeof(double), cudaMemcpyDeviceToHost, st));
+  ADJ_CUDA(c, cudaMemcpyAsync(hZ.data(), b->gzb, N * sizeof(double), cudaMemcpyDeviceToHost, st));
+  if (dm.nInlet > 0)
+    ADJ_CUDA(c, cudaMemcpyAsync(hQ.data(), a.gQ, dm.nInlet * sizeof(double), cudaMemcpyDeviceToHost, st));
+  int32_t flags = 0;
+  ADJ_CUDA(c, cudaMemcpyAsync(&flags, ds.flags, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  ADJ_CUDA(c, cudaStreamSynchronize(st));
+  if (flags & 2) return fail(c, HG_ERR_INLET, "inlet-Q total conveyance is not positive during the run");
+  if (flags & 1) return fail(c, HG_ERR_STATE, "non-finite value in the state during the run");
+  *loss = hl * scale;
+  for (int i = 0; i < N; ++i) {
+    const int o = c->perm[i];
+    if (gManning) gManning[o] = hN[i];
+    if (gZb) gZb[o] = hZ[i];
+  }
+  if (gInlet)
+    for (int g = 0; g < dm.nInlet; ++g) gInlet[g] = hQ[g];
+  return HG_OK;
 }
 
 void adjoint_release(hg_ctx* ctx) {

@@ -1,0 +1,213 @@
+// Adjoint (vector-Jacobian product) kernels of the FP32-compensated path.
+//
+// Same gather-form VJP as hg_adjoint_f64.cu (see there for the formulas), on
+// the packed FP32 records (hg_f32.cuh), with the FP32 path's own wet/dry
+// decisions (FP64-exact near h_small) so that every branch is the forward
+// pass's.  Cotangents are FP32; parameter gradients accumulate in FP64.
+// Compiled with the same fast-math options as the FP32 forward kernels.
+#include <cfloat>
+#include <cmath>
+
+#include "hg_adjoint_state.hpp"
+#include "hg_device.cuh"
+#include "hg_dual.cuh"
+#include "hg_f32.cuh"
+#include "hg_reduce.cuh"
+
+namespace hg {
+
+using namespace hgd;
+using namespace devred;
+
+namespace {
+
+constexpr int kBlock = 128;
+inline int blocks_for(int n) { return (n + kBlock - 1) / kBlock; }
+
+using F3 = Dn<float, 3>;
+using F7 = Dn<float, 7>;
+
+template <class D>
+__device__ __forceinline__ Side<D> seeded(const Side<float>& s, int kzb) {
+  Side<D> r;
+  r.xi = D::seed(s.xi, 0);
+  r.hst = D(s.hst);
+  r.zb = D::seed(s.zb, kzb);
+  r.dry = s.dry;
+  r.h = s.dry ? D(s.h) : D::seed(s.h, 0);
+  r.hu = s.dry ? D(0.0f) : D::seed(s.hu, 1);
+  r.hv = s.dry ? D(0.0f) : D::seed(s.hv, 2);
+  return r;
+}
+
+template <class D>
+__device__ __forceinline__ Side<D> constant(const Side<float>& s) {
+  Side<D> r;
+  r.xi = D(s.xi); r.hst = D(s.hst); r.zb = D(s.zb); r.dry = s.dry;
+  r.h = D(s.h); r.hu = D(s.hu); r.hv = D(s.hv);
+  return r;
+}
+
+template <int NS>
+__global__ void __launch_bounds__(kBlock) k_vjp_f32(DevMesh m, AdjDev a, StateF32 Q, const float* __restrict__ mu,
+                                                    const float* __restrict__ extra, float* out, float cSelf,
+                                                    float cExtra, float beta) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= m.n) return;
+  const int n = m.n;
+  const float4 cp = __ldg(&m.CP[j]);
+  const float4 cs = __ldg(&m.CS[j]);
+  const SideF32 L = make_side_f32(__ldg(&Q.x[j]), cp, m.hsmf, m.hsm);
+  const float Aj = cs.z;
+  const float mj0 = mu[j], mj1 = mu[n + j], mj2 = mu[2 * n + j];
+  float g0 = 0.0f, g1 = 0.0f, g2 = 0.0f, gn = 0.0f, gzb = 0.0f;
+  const Side<F3> L3 = seeded<F3>(L.s, -1);
+#pragma unroll
+  for (int k = 0; k < NS; ++k) {
+    const float4 sl = __ldg(&m.SL[(size_t)k * n + j]);
+    const int32_t nb = slot_nb(sl);
+    if (nb == kNoFace) continue;
+    const float nx = sl.x, ny = sl.y, len = sl.z;
+    if (nb >= 0) {
+      const SideF32 R = make_side_f32(__ldg(&Q.x[nb]), __ldg(&m.CP[nb]), m.hsmf, m.hsm);
+      const float An = __ldg(&m.CS[nb]).z;
+      const float w0 = len * (mu[nb] / An - mj0 / Aj);
+      const float w1 = len * (mu[n + nb] / An - mj1 / Aj);
+      const float w2 = len * (mu[2 * n + nb] / An - mj2 / Aj);
+      const Side<F3> R3 = constant<F3>(R.s);
+      const F3 dxi = (R3.xi - L3.xi) + F3(R.xlo - L.xlo);
+      F3 F[3];
+      roe_flux<F3>(L3, R3, dxi, F3(m.gf), F3(nx), F3(ny), F3(m.hsmf), F);
+      g0 += w0 * F[0].d[0] + w1 * F[1].d[0] + w2 * F[2].d[0];
+      g1 += w0 * F[0].d[1] + w1 * F[1].d[1] + w2 * F[2].d[1];
+      g2 += w0 * F[0].d[2] + w1 * F[1].d[2] + w2 * F[2].d[2];
+    } else {
+      const int32_t bf = boundary_index(nb);
+      const int32_t info = m.bfInfo[bf], type = info & 3, grp = info >> 2;
+      const float w0 = -len * mj0 / Aj, w1 = -len * mj1 / Aj, w2 = -len * mj2 / Aj;
+      const Side<F7> L7 = seeded<F7>(L.s, 4);
+      const F7 man = F7::seed(cp.w, 3);
+      const F7 qin = F7::seed(type == kBcInletQ ? (float)m.inletQ[grp] : 0.0f, 5);
+      const F7 ta = F7::seed(type == kBcInletQ ? (float)m.totalA[grp] : 1.0f, 6);
+      const Side<F7> R7 = ghost_state<F7>(L7, type, F7(nx), F7(ny), F7(m.hsmf),
+                                          F7(type == kBcExitH ? (float)m.exitWse[grp] : 0.0f), qin, ta,
+                                          F7(m.bfLp23f[bf]), man);
+      F7 ex(L.excess);
+      if (L.s.dry) ex.d[0] = -1.0f;   // excess = h_small - (xi + hstill) for a dry cell
+      const F7 dxi = (R7.h - L7.h) + ex;
+      F7 F[3];
+      roe_flux<F7>(L7, R7, dxi, F7(m.gf), F7(nx), F7(ny), F7(m.hsmf), F);
+      float c[7];
+#pragma unroll
+      for (int d = 0; d < 7; ++d) c[d] = w0 * F[0].d[d] + w1 * F[1].d[d] + w2 * F[2].d[d];
+      g0 += c[0]; g1 += c[1]; g2 += c[2];
+      gn += c[3];
+      gzb += c[4];
+      a.bfGradQ[bf] = (double)c[5];
+      a.bfGradTA[bf] = (double)c[6];
+    }
+  }
+  if (!L.s.dry) {
+    const float hu = L.s.hu, hv = L.s.hv, man = cp.w;
+    const float s2 = hu * hu + hv * hv + eps_c<float>();
+    const float hp = L.s.h + m.hsmf;
+    const float k = friction_coef(m.gf, m.kn2f, m.hsmf, man, L.s.h, hu, hv);
+    const float dkdh = -(7.0f / 3.0f) * k / hp;
+    const float dkdqx = k * hu / s2, dkdqy = k * hv / s2;
+    const float dkdn = 2.0f * k / man;
+    g0 += mj1 * (m.gf * cs.x - hu * dkdh) + mj2 * (m.gf * cs.y - hv * dkdh);
+    g1 += mj1 * (-k - hu * dkdqx) + mj2 * (-hv * dkdqx);
+    g2 += mj1 * (-hu * dkdqy) + mj2 * (-k - hv * dkdqy);
+    gn += -(mj1 * hu + mj2 * hv) * dkdn;
+    a.gS0x[j] += (double)beta * (double)(mj1 * m.gf * L.s.xi);
+    a.gS0y[j] += (double)beta * (double)(mj2 * m.gf * L.s.xi);
+  }
+  a.gN[j] += (double)beta * (double)gn;
+  a.gZb[j] += (double)beta * (double)gzb;
+  const float mask = L.s.dry ? 0.0f : 1.0f;
+  const float e0 = extra ? extra[j] : 0.0f, e1 = extra ? extra[n + j] : 0.0f, e2 = extra ? extra[2 * n + j] : 0.0f;
+  out[j] = mask * (cSelf * mj0 + cExtra * e0 + beta * g0);
+  out[n + j] = mask * (cSelf * mj1 + cExtra * e1 + beta * g1);
+  out[2 * n + j] = mask * (cSelf * mj2 + cExtra * e2 + beta * g2);
+}
+
+__global__ void __launch_bounds__(256) k_inlet_adjoint_f32(DevMesh m, AdjDev a, StateF32 Q, float* out, double beta,
+                                                           int g) {
+  const int o0 = m.inletOff[g], o1 = m.inletOff[g + 1];
+  double sTA = 0.0, sQ = 0.0;
+  for (int i = o0 + threadIdx.x; i < o1; i += blockDim.x) {
+    const int bf = a.inletBf[i];
+    sTA += a.bfGradTA[bf];
+    sQ += a.bfGradQ[bf];
+  }
+  __shared__ double tot;
+  const double t1 = block_sum(sTA);
+  if (threadIdx.x == 0) tot = t1;
+  const double t2 = block_sum(sQ);
+  if (threadIdx.x == 0) a.gQ[g] += beta * t2;
+  __syncthreads();
+  const double gTA = tot;
+  const int u0 = a.inletUOff[g], u1 = a.inletUOff[g + 1];
+  for (int i = u0 + threadIdx.x; i < u1; i += blockDim.x) {
+    const int c = a.inletUCell[i];
+    const float4 cp = m.CP[c];
+    const SideF32 L = make_side_f32(Q.x[c], cp, m.hsmf, m.hsm);
+    if (L.s.dry) continue;
+    const double coef = a.inletUCoef[i], n = cp.w;
+    out[c] += (float)(beta * gTA * coef / n);
+    a.gN[c] += beta * gTA * (-coef * (double)L.s.h / (n * n));
+  }
+}
+
+__device__ __forceinline__ double depth_f64(const DevMesh& m, StateF32 Q, int c) {
+  const float4 x = Q.x[c];
+  const float4 cp = m.CP[c];
+  return ((double)x.x + (double)x.y) + ((double)cp.x + (double)cp.y);
+}
+
+__global__ void __launch_bounds__(256) k_probe_loss_f32(DevMesh m, AdjDev a, StateF32 Q,
+                                                        const int32_t* __restrict__ probes,
+                                                        const double* __restrict__ obs, int np) {
+  double s = 0.0;
+  for (int p = threadIdx.x; p < np; p += blockDim.x) {
+    const double e = depth_f64(m, Q, probes[p]) - obs[p];
+    s += e * e;
+  }
+  const double t = block_sum(s);
+  if (threadIdx.x == 0) a.loss[0] += t;
+}
+
+__global__ void k_probe_adjoint_f32(DevMesh m, StateF32 Q, float* mu, const int32_t* __restrict__ probes,
+                                    const double* __restrict__ obs, int np, double scale) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  for (int p = 0; p < np; ++p) {
+    const int c = probes[p];
+    const float4 cp = m.CP[c];
+    const SideF32 L = make_side_f32(Q.x[c], cp, m.hsmf, m.hsm);
+    if (L.s.dry) continue;
+    mu[c] += (float)(scale * 2.0 * (depth_f64(m, Q, c) - obs[p]));
+  }
+}
+
+}  // namespace
+
+void launch_vjp_f32(const DevMesh& m, const AdjDev& a, StateF32 Q, const float* mu, const float* extra, float* out,
+                    float cSelf, float cExtra, float beta, cudaStream_t st) {
+  if (m.nslot <= 3) k_vjp_f32<3><<<blocks_for(m.n), kBlock, 0, st>>>(m, a, Q, mu, extra, out, cSelf, cExtra, beta);
+  else if (m.nslot <= 4) k_vjp_f32<4><<<blocks_for(m.n), kBlock, 0, st>>>(m, a, Q, mu, extra, out, cSelf, cExtra, beta);
+  else k_vjp_f32<8><<<blocks_for(m.n), kBlock, 0, st>>>(m, a, Q, mu, extra, out, cSelf, cExtra, beta);
+}
+void launch_inlet_adjoint_f32(const DevMesh& m, const AdjDev& a, StateF32 Q, float* out, double beta,
+                              cudaStream_t st) {
+  for (int g = 0; g < m.nInlet; ++g) k_inlet_adjoint_f32<<<1, 256, 0, st>>>(m, a, Q, out, beta, g);
+}
+void launch_probe_loss_f32(const DevMesh& m, const AdjDev& a, StateF32 Q, const int32_t* probes, const double* obs,
+                           int32_t nprobe, cudaStream_t st) {
+  if (nprobe > 0) k_probe_loss_f32<<<1, 256, 0, st>>>(m, a, Q, probes, obs, nprobe);
+}
+void launch_probe_adjoint_f32(const DevMesh& m, StateF32 Q, float* mu, const int32_t* probes, const double* obs,
+                              int32_t nprobe, double scale, cudaStream_t st) {
+  if (nprobe > 0) k_probe_adjoint_f32<<<1, 32, 0, st>>>(m, Q, mu, probes, obs, nprobe, scale);
+}
+
+}  // namespace hg

@@ -1,0 +1,51 @@
+// Device buffers and launch wrappers of the discrete adjoint.
+#pragma once
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+#include "hg_state.hpp"
+
+namespace hg {
+
+// Adjoint accumulators and tables, device order.
+struct AdjDev {
+  double* gN = nullptr;        // [n] dL/dn per cell, accumulated over all stages
+  double* gS0x = nullptr;      // [n] dL/dS0x per cell (S0 is linear in zb; mapped to zb at the end)
+  double* gS0y = nullptr;
+  double* gZb = nullptr;       // [n] dL/dzb through the exit-H ghost depth
+  double* bfGradQ = nullptr;   // [nbf] per boundary face: sum_k w_k dF_k/dQ_inlet of the current stage
+  double* bfGradTA = nullptr;  // [nbf] the same for the inlet conveyance total_A
+  double* gQ = nullptr;        // [nInlet] dL/dQ_inlet, accumulated
+  const int32_t* inletBf = nullptr;    // inlet CSR entry -> boundary face index
+  const int32_t* inletUOff = nullptr;  // [nInlet+1] unique inlet cells per group
+  const int32_t* inletUCell = nullptr;
+  const double* inletUCoef = nullptr;  // sum over the cell's faces in the group of L^(5/3)
+  double* loss = nullptr;              // [1] sum over steps and probes of (h - obs)^2
+};
+
+// out_j = M(Q_j) (cSelf mu_j + cExtra extra_j + beta (J(Q)^T mu)_j), parameter
+// gradients += beta (dR/dtheta)^T mu; M(Q_j) = 1 when cell j of Q is wet.
+void launch_vjp_f64(const DevMesh& m, const AdjDev& a, const double* Q, const double* mu, const double* extra,
+                    double* out, double cSelf, double cExtra, double beta, cudaStream_t st);
+// Inlet-Q conveyance terms of the same VJP (total_A couples all cells of a group).
+void launch_inlet_adjoint_f64(const DevMesh& m, const AdjDev& a, const double* Q, double* out, double beta,
+                              cudaStream_t st);
+// Loss terms: forward (accumulate), adjoint (mu_xi[p] += M scale 2 (h - obs)).
+void launch_probe_loss_f64(const DevMesh& m, const AdjDev& a, const double* Q, const int32_t* probes,
+                           const double* obs, int32_t nprobe, cudaStream_t st);
+void launch_probe_adjoint_f64(const DevMesh& m, const double* Q, double* mu, const int32_t* probes,
+                              const double* obs, int32_t nprobe, double scale, cudaStream_t st);
+// FP32-compensated path: the same with packed FP32 states and FP32 cotangents.
+void launch_vjp_f32(const DevMesh& m, const AdjDev& a, StateF32 Q, const float* mu, const float* extra, float* out,
+                    float cSelf, float cExtra, float beta, cudaStream_t st);
+void launch_inlet_adjoint_f32(const DevMesh& m, const AdjDev& a, StateF32 Q, float* out, double beta,
+                              cudaStream_t st);
+void launch_probe_loss_f32(const DevMesh& m, const AdjDev& a, StateF32 Q, const int32_t* probes, const double* obs,
+                           int32_t nprobe, cudaStream_t st);
+void launch_probe_adjoint_f32(const DevMesh& m, StateF32 Q, float* mu, const int32_t* probes, const double* obs,
+                              int32_t nprobe, double scale, cudaStream_t st);
+// dL/dzb = S0 transpose (Green-Gauss of face averages) applied to dL/dS0, plus the direct term.
+void launch_zb_gradient(const DevMesh& m, const AdjDev& a, double* gzb, cudaStream_t st);
+
+}  // namespace hg

@@ -98,23 +98,16 @@ int upload_cells(hg_ctx* c) {
   HG_CUDA(c, upload(c, c->d_man, man));
   HG_CUDA(c, upload(c, c->d_s0x, s0x));
   HG_CUDA(c, upload(c, c->d_s0y, s0y));
-  std::vector<float> hhi(c->n), hlo(c->n);
+  // FP32 records: CP {hstill_hi, hstill_lo, zb, n}, CS {S0x, S0y, area, 0}.
+  c->h_CP.resize(c->n);
+  c->h_CS.resize(c->n);
   for (int i = 0; i < c->n; ++i) {
-    hhi[i] = (float)hst[i];
-    hlo[i] = (float)(hst[i] - (double)hhi[i]);
+    const float hh = (float)hst[i];
+    c->h_CP[i] = make_float4(hh, (float)(hst[i] - (double)hh), (float)zb[i], (float)man[i]);
+    c->h_CS[i] = make_float4((float)s0x[i], (float)s0y[i], c->h_area[i], 0.0f);
   }
-  c->h_hsthi = hhi;
-  c->h_hstlo = hlo;
-  HG_CUDA(c, upload(c, c->d_hsthi, hhi));
-  HG_CUDA(c, upload(c, c->d_hstlo, hlo));
-  c->h_zbf = to_float(zb);
-  c->h_manf = to_float(man);
-  c->h_s0xf = to_float(s0x);
-  c->h_s0yf = to_float(s0y);
-  HG_CUDA(c, upload(c, c->d_zbf, c->h_zbf));
-  HG_CUDA(c, upload(c, c->d_manf, c->h_manf));
-  HG_CUDA(c, upload(c, c->d_s0xf, c->h_s0xf));
-  HG_CUDA(c, upload(c, c->d_s0yf, c->h_s0yf));
+  HG_CUDA(c, upload(c, c->d_CP, c->h_CP));
+  HG_CUDA(c, upload(c, c->d_CS, c->h_CS));
   HG_CUDA(c, cudaStreamSynchronize(c->stream));
   return HG_OK;
 }
@@ -147,8 +140,8 @@ int ensure_dt_capacity(hg_ctx* c, int32_t steps) {
   return HG_OK;
 }
 
-StateF32 xa(hg_ctx* c) { return StateF32{c->XAhi, c->XAlo}; }
-StateF32 xb(hg_ctx* c) { return StateF32{c->XBhi, c->XBlo}; }
+StateF32 xa(hg_ctx* c) { return StateF32{c->XA, c->XQA}; }
+StateF32 xb(hg_ctx* c) { return StateF32{c->XB, c->XQB}; }
 
 // Enqueue the state upload from a host buffer (caller order).
 int enqueue_upload(hg_ctx* c, const double* Q) {
@@ -196,8 +189,8 @@ void enqueue_euler_step(hg_ctx* c, bool cflMode, double cfl) {
     launch_inlet_total_f32(c->dm, c->ds, xa(c), c->stream);
     launch_stage_f32(c->dm, c->ds, kModeEulerRef, xa(c), StateF32{}, xb(c), nullptr, false, c->stream);
     if (cflMode) launch_cfl_f32(c->dm, c->ds, xb(c), c->stream);
-    std::swap(c->XAhi, c->XBhi);
-    std::swap(c->XAlo, c->XBlo);
+    std::swap(c->XA, c->XB);
+    std::swap(c->XQA, c->XQB);
   }
   c->launches += 2 + (c->dm.nInlet > 0 ? 1 : 0) + (cflMode ? 1 : 0);
 }
@@ -723,17 +716,14 @@ int ctx_setup_device(hg_ctx* c) {
   c->inletQ.assign(m.inletGroups.size(), 0.0);
   c->exitWse.assign(m.exitGroups.size(), 0.0);
 
-  int32_t* d_nb; double *d_snx, *d_sny, *d_slen, *d_area, *d_lp23, *d_lp53; float *d_snxf, *d_snyf, *d_slenf, *d_areaf,
-      *d_lp23f; int32_t *d_bfInfo, *d_inletOff, *d_inletCell;
+  int32_t* d_nb; double *d_snx, *d_sny, *d_slen, *d_area, *d_lp23, *d_lp53; float* d_lp23f; float4* d_SL;
+  int32_t *d_bfInfo, *d_inletOff, *d_inletCell;
   HG_CUDA(c, dalloc(c, &d_nb, nb.size()));
   HG_CUDA(c, dalloc(c, &d_snx, snx.size()));
   HG_CUDA(c, dalloc(c, &d_sny, sny.size()));
   HG_CUDA(c, dalloc(c, &d_slen, slen.size()));
-  HG_CUDA(c, dalloc(c, &d_snxf, snx.size()));
-  HG_CUDA(c, dalloc(c, &d_snyf, sny.size()));
-  HG_CUDA(c, dalloc(c, &d_slenf, slen.size()));
+  HG_CUDA(c, dalloc(c, &d_SL, nb.size()));
   HG_CUDA(c, dalloc(c, &d_area, (size_t)N));
-  HG_CUDA(c, dalloc(c, &d_areaf, (size_t)N));
   HG_CUDA(c, dalloc(c, &d_bfInfo, (size_t)std::max(nbf, 1)));
   HG_CUDA(c, dalloc(c, &d_lp23, (size_t)std::max(nbf, 1)));
   HG_CUDA(c, dalloc(c, &d_lp23f, (size_t)std::max(nbf, 1)));
@@ -741,8 +731,8 @@ int ctx_setup_device(hg_ctx* c) {
   HG_CUDA(c, dalloc(c, &d_inletCell, std::max<size_t>(inletCell.size(), 1)));
   HG_CUDA(c, dalloc(c, &d_lp53, std::max<size_t>(inletLp53.size(), 1)));
   for (double** p : {&c->d_hst, &c->d_zb, &c->d_man, &c->d_s0x, &c->d_s0y}) HG_CUDA(c, dalloc(c, p, (size_t)N));
-  for (float** p : {&c->d_hsthi, &c->d_hstlo, &c->d_zbf, &c->d_manf, &c->d_s0xf, &c->d_s0yf})
-    HG_CUDA(c, dalloc(c, p, (size_t)N));
+  HG_CUDA(c, dalloc(c, &c->d_CP, (size_t)N));
+  HG_CUDA(c, dalloc(c, &c->d_CS, (size_t)N));
   HG_CUDA(c, dalloc(c, &c->d_inletQ, std::max<size_t>(c->inletQ.size(), 1)));
   HG_CUDA(c, dalloc(c, &c->d_exitWse, std::max<size_t>(c->exitWse.size(), 1)));
   HG_CUDA(c, dalloc(c, &c->d_totalA, std::max<size_t>(c->inletQ.size(), 1)));
@@ -752,7 +742,10 @@ int ctx_setup_device(hg_ctx* c) {
   if (c->precision == HG_FP64) {
     HG_CUDA(c, dalloc(c, &c->QA, (size_t)3 * N));
   } else {
-    for (float** p : {&c->XAhi, &c->XAlo, &c->XBhi, &c->XBlo}) HG_CUDA(c, dalloc(c, p, (size_t)3 * N));
+    HG_CUDA(c, dalloc(c, &c->XA, (size_t)N));
+    HG_CUDA(c, dalloc(c, &c->XB, (size_t)N));
+    HG_CUDA(c, dalloc(c, &c->XQA, (size_t)N));
+    HG_CUDA(c, dalloc(c, &c->XQB, (size_t)N));
   }
   // Scalars
   HG_CUDA(c, dalloc(c, &c->ds.dt, 1));
@@ -770,17 +763,24 @@ int ctx_setup_device(hg_ctx* c) {
   c->flushBytes = (size_t)256 << 20;
   HG_CUDA(c, dalloc(c, reinterpret_cast<char**>(&c->flushBuf), c->flushBytes));
 
+  // FP32 slot records {nx, ny, L, nb as bits}
+  std::vector<float4> SL(nb.size());
+  for (size_t i = 0; i < nb.size(); ++i) {
+    float4 r;
+    r.x = (float)snx[i];
+    r.y = (float)sny[i];
+    r.z = (float)slen[i];
+    std::memcpy(&r.w, &nb[i], sizeof(float));
+    SL[i] = r;
+  }
+  c->h_area = to_float(area);
   HG_CUDA(c, upload(c, d_nb, nb));
   HG_CUDA(c, upload(c, d_snx, snx));
   HG_CUDA(c, upload(c, d_sny, sny));
   HG_CUDA(c, upload(c, d_slen, slen));
-  std::vector<float> snxf = to_float(snx), snyf = to_float(sny), slenf = to_float(slen), areaf = to_float(area),
-                     lp23f = to_float(bfLp23);
-  HG_CUDA(c, upload(c, d_snxf, snxf));
-  HG_CUDA(c, upload(c, d_snyf, snyf));
-  HG_CUDA(c, upload(c, d_slenf, slenf));
+  HG_CUDA(c, upload(c, d_SL, SL));
+  std::vector<float> lp23f = to_float(bfLp23);
   HG_CUDA(c, upload(c, d_area, area));
-  HG_CUDA(c, upload(c, d_areaf, areaf));
   HG_CUDA(c, upload(c, d_bfInfo, bfInfo));
   HG_CUDA(c, upload(c, d_lp23, bfLp23));
   HG_CUDA(c, upload(c, d_lp23f, lp23f));
@@ -799,14 +799,14 @@ int ctx_setup_device(hg_ctx* c) {
   dm.nInlet = (int32_t)m.inletGroups.size();
   dm.nExit = (int32_t)m.exitGroups.size();
   dm.nb = d_nb; dm.snx = d_snx; dm.sny = d_sny; dm.slen = d_slen;
-  dm.snxf = d_snxf; dm.snyf = d_snyf; dm.slenf = d_slenf;
+  dm.SL = d_SL;
   dm.bfInfo = d_bfInfo; dm.bfLp23 = d_lp23; dm.bfLp23f = d_lp23f;
   dm.inletOff = d_inletOff; dm.inletCell = d_inletCell; dm.inletLp53 = d_lp53;
   dm.area = d_area; dm.hst = c->d_hst; dm.zb = c->d_zb; dm.man = c->d_man; dm.s0x = c->d_s0x; dm.s0y = c->d_s0y;
-  dm.areaf = d_areaf; dm.hsthi = c->d_hsthi; dm.hstlo = c->d_hstlo; dm.zbf = c->d_zbf; dm.manf = c->d_manf;
-  dm.s0xf = c->d_s0xf; dm.s0yf = c->d_s0yf;
+  dm.CP = c->d_CP; dm.CS = c->d_CS;
   dm.exitWse = c->d_exitWse; dm.inletQ = c->d_inletQ; dm.totalA = c->d_totalA;
   dm.g = c->k.g; dm.kn2 = c->k.k_n * c->k.k_n; dm.hsm = c->k.h_small;
+  dm.gf = (float)c->k.g; dm.kn2f = (float)(c->k.k_n * c->k.k_n); dm.hsmf = (float)c->k.h_small;
   c->slotNb = d_nb;
   int rc = upload_cells(c);
   if (rc) return rc;

@@ -28,18 +28,19 @@ struct hg_ctx {
   hg::DevScalars ds;
   // Parameters (caller order, FP64 host copies)
   std::vector<double> zbCell, hstill, manning, s0x, s0y, inletQ, exitWse;
-  // FP32 host copies (device order) kept alive across async uploads
-  std::vector<float> h_hsthi, h_hstlo, h_zbf, h_manf, h_s0xf, h_s0yf;
+  // FP32 packed cell records (device order), host copies kept alive across async uploads
+  std::vector<float4> h_CP, h_CS;
+  std::vector<float> h_area;   // device order
   // Writable device parameter arrays
   double *d_hst = nullptr, *d_zb = nullptr, *d_man = nullptr, *d_s0x = nullptr, *d_s0y = nullptr;
-  float *d_hsthi = nullptr, *d_hstlo = nullptr, *d_zbf = nullptr, *d_manf = nullptr, *d_s0xf = nullptr,
-        *d_s0yf = nullptr;
+  float4 *d_CP = nullptr, *d_CS = nullptr;
   double *d_inletQ = nullptr, *d_exitWse = nullptr, *d_totalA = nullptr;
   int32_t* d_perm = nullptr;
   const int32_t* slotNb = nullptr;
   // State
   double *QA = nullptr, *QB = nullptr, *Quser = nullptr;
-  float *XAhi = nullptr, *XAlo = nullptr, *XBhi = nullptr, *XBlo = nullptr;
+  float4 *XA = nullptr, *XB = nullptr;   // FP32 path state records
+  float2 *XQA = nullptr, *XQB = nullptr;
   void* flushBuf = nullptr;
   size_t flushBytes = 0;
   bool cflPrimed = false;

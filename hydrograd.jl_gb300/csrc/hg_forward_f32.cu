@@ -1,24 +1,26 @@
 // FP32-compensated stage kernels, step bookkeeping and renumbering kernels.
 //
-// Forward kernels: one fused pass per explicit stage.
-//
-// Each thread owns one cell (device order) and gathers its faces in the
-// reference's local order (compute_inviscid_fluxes,
+// One fused pass per explicit stage.  Each thread owns one cell (device order)
+// and gathers its faces in the reference's local order (compute_inviscid_fluxes,
 // src/fvm/discretization/semi_discretize_swe_2D.jl:286-419): clamp, ghost
 // state, Roe flux, -sum F L / A, Manning friction + bed-slope source, then the
-// stage update and the depth-positivity clamp.  Gather form: no atomics, and
-// the per-cell summation order is the reference's, so the result is
-// deterministic and independent of the launch shape.
+// compensated stage update and the depth-positivity clamp.  Gather form: no
+// atomics; per-cell summation order fixed, so results are bit-reproducible.
+// Cell records are packed (hg_f32.cuh) so that a cell costs a few 16-byte
+// loads, and the slot loop is unrolled to the mesh's maximum cell degree so
+// that all of a cell's slot and neighbour loads are in flight together.
 #include <cfloat>
 #include <cmath>
 
 #include "hg_device.cuh"
+#include "hg_f32.cuh"
 #include "hg_reduce.cuh"
 #include "hg_state.hpp"
 
 namespace hg {
 
 using namespace hgd;
+using namespace devred;
 
 namespace {
 
@@ -26,205 +28,128 @@ constexpr int kBlock = 256;
 
 inline int blocks_for(int n) { return (n + kBlock - 1) / kBlock; }
 
-using namespace devred;
-
-// ---------------------------------------------------------------------------
-// FP32-compensated path
-// ---------------------------------------------------------------------------
-// State components are hi + lo float pairs; hstill is an exact hi + lo pair.
-// Depth h = xi + hstill: the dry decision h <= h_small is taken exactly as the
-// FP64 reference takes it -- from an FP32 estimate when that estimate is
-// farther from h_small than its error bound, else from an FP64 sum -- with a
-// tolerance of a few units of the pair representation (2^-46 relative), the
-// granularity at which a clamped cell's xi = h_small - hstill is stored.
-struct DepthF32 {
-  float h;        // clamped depth
-  float excess;   // (h_clamped - hstill) - xi: 0 when wet, the clamp shift when dry
-  bool dry;
-};
-
-__device__ __forceinline__ DepthF32 depth_f32(float xh, float xl, float hh, float hl, float hsmf, double hsm) {
-  DepthF32 d;
-  const float est = (xh + hh) + (xl + hl);
-  const float mag = fabsf(xh) + fabsf(hh);
-  const float bound = 4.0e-7f * mag + 1.0e-30f;
-  if (fabsf(est - hsmf) > bound + 1.0e-10f) {
-    d.dry = est <= hsmf;
-    d.h = est;
-  } else {
-    const double hd = ((double)xh + (double)xl) + ((double)hh + (double)hl);
-    const double tol = 1.4210854715202004e-14 * (double)mag;   // 2^-46 * magnitude
-    d.dry = hd <= hsm + tol;
-    d.h = (float)hd;
-  }
-  d.excess = d.dry ? (hsmf - est) : 0.0f;
-  if (d.dry) d.h = hsmf;
-  return d;
-}
-
-struct SideF32 {
-  Side<float> s;
-  float xlo;      // lo part of xi
-  float excess;
-};
-
-__device__ __forceinline__ SideF32 load_f32(const DevMesh& m, const float* __restrict__ Xh, const float* __restrict__ Xl,
-                                            int j, float hsmf) {
-  SideF32 r;
-  const float xh = Xh[j], xl = Xl[j];
-  const float hh = m.hsthi[j], hl = m.hstlo[j];
-  const DepthF32 d = depth_f32(xh, xl, hh, hl, hsmf, m.hsm);
-  r.s.xi = xh;
-  r.xlo = xl;
-  r.s.hst = hh;
-  r.s.zb = m.zbf[j];
-  r.s.dry = d.dry;
-  r.s.h = d.h;
-  r.s.hu = d.dry ? 0.0f : Xh[m.n + j];
-  r.s.hv = d.dry ? 0.0f : Xh[2 * m.n + j];
-  r.excess = d.excess;
-  return r;
-}
-
-__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
-  s = a + b;
-  const float bb = s - a;
-  e = (a - (s - bb)) + (b - bb);
-}
-__device__ __forceinline__ void fast_two_sum(float a, float b, float& s, float& e) {
-  s = a + b;
-  e = b - (s - a);
-}
-// (ah + al) + d, renormalised.
-__device__ __forceinline__ void df_add(float ah, float al, float d, float& rh, float& rl) {
-  float s, e;
-  two_sum(ah, d, s, e);
-  e += al;
-  fast_two_sum(s, e, rh, rl);
-}
-// (ah + al) + (bh + bl), renormalised.
-__device__ __forceinline__ void df_add2(float ah, float al, float bh, float bl, float& rh, float& rl) {
-  float s, e;
-  two_sum(ah, bh, s, e);
-  e += al + bl;
-  fast_two_sum(s, e, rh, rl);
-}
-
-__device__ __forceinline__ void face_sum_f32(const DevMesh& m, const float* __restrict__ Xh,
-                                             const float* __restrict__ Xl, int c, const SideF32& L, float hsmf,
-                                             float g, float& f0, float& f1, float& f2) {
+template <int NS>
+__device__ __forceinline__ void face_sum_f32(const DevMesh& m, const float4* __restrict__ X, int c, const SideF32& L,
+                                             float& f0, float& f1, float& f2) {
   f0 = 0.0f; f1 = 0.0f; f2 = 0.0f;
-  for (int k = 0; k < m.nslot; ++k) {
-    const int32_t nb = m.nb[(size_t)k * m.n + c];
-    if (nb == kNoFace) break;
-    const float nx = m.snxf[(size_t)k * m.n + c], ny = m.snyf[(size_t)k * m.n + c];
-    const float len = m.slenf[(size_t)k * m.n + c];
+  float4 sl[NS];
+#pragma unroll
+  for (int k = 0; k < NS; ++k) sl[k] = __ldg(&m.SL[(size_t)k * m.n + c]);
+#pragma unroll
+  for (int k = 0; k < NS; ++k) {
+    const int32_t nb = slot_nb(sl[k]);
+    if (nb == kNoFace) continue;
+    const float nx = sl[k].x, ny = sl[k].y, len = sl[k].z;
     Side<float> R;
     float dxi;
     if (nb >= 0) {
-      const SideF32 r = load_f32(m, Xh, Xl, nb, hsmf);
+      const SideF32 r = make_side_f32(__ldg(&X[nb]), __ldg(&m.CP[nb]), m.hsmf, m.hsm);
       R = r.s;
       dxi = (r.s.xi - L.s.xi) + (r.xlo - L.xlo);
     } else {
       const int32_t bf = boundary_index(nb);
       const int32_t info = m.bfInfo[bf], type = info & 3, grp = info >> 2;
-      R = ghost_state<float>(L.s, type, nx, ny, hsmf, type == kBcExitH ? (float)m.exitWse[grp] : 0.0f,
+      const float man = __ldg(&m.CP[c]).w;
+      R = ghost_state<float>(L.s, type, nx, ny, m.hsmf, type == kBcExitH ? (float)m.exitWse[grp] : 0.0f,
                              type == kBcInletQ ? (float)m.inletQ[grp] : 0.0f,
-                             type == kBcInletQ ? (float)m.totalA[grp] : 1.0f, m.bfLp23f[bf], m.manf[c]);
+                             type == kBcInletQ ? (float)m.totalA[grp] : 1.0f, m.bfLp23f[bf], man);
       // xi_ghost - xi = (h_ghost - h) + ((h - hstill) - xi)
       dxi = (R.h - L.s.h) + L.excess;
     }
     float F[3];
-    roe_flux<float>(L.s, R, dxi, g, nx, ny, hsmf, F);
+    roe_flux<float>(L.s, R, dxi, m.gf, nx, ny, m.hsmf, F);
     f0 = fmaf(F[0], len, f0);
     f1 = fmaf(F[1], len, f1);
     f2 = fmaf(F[2], len, f2);
   }
 }
 
+template <int NS>
 __device__ __forceinline__ float cfl_candidate_f32(const DevMesh& m, int c, float h, float qx, float qy, bool dry,
-                                                   float g) {
+                                                   float area) {
   if (dry) { qx = 0.0f; qy = 0.0f; }
-  const float u = qx / h, v = qy / h, a = sqrtf(g * h);
+  const float u = qx / h, v = qy / h, a = sqrtf(m.gf * h);
   float s = 0.0f;
-  for (int k = 0; k < m.nslot; ++k) {
-    const int32_t nb = m.nb[(size_t)k * m.n + c];
-    if (nb == kNoFace) break;
-    s += m.slenf[(size_t)k * m.n + c] * (fabsf(u * m.snxf[(size_t)k * m.n + c] + v * m.snyf[(size_t)k * m.n + c]) + a);
+#pragma unroll
+  for (int k = 0; k < NS; ++k) {
+    const float4 sl = __ldg(&m.SL[(size_t)k * m.n + c]);
+    if (slot_nb(sl) == kNoFace) continue;
+    s += sl.z * (fabsf(u * sl.x + v * sl.y) + a);
   }
-  return m.areaf[c] / s;
+  return area / s;
 }
 
+template <int NS>
 __global__ void __launch_bounds__(kBlock) k_stage_f32(DevMesh m, DevScalars s, int mode, StateF32 Xin, StateF32 Xbase,
                                                       StateF32 Xout, double* Rout, int cfl) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   const bool active = c < m.n;
-  const float hsmf = (float)m.hsm, g = (float)m.g;
   float cand = INFINITY;
   if (active) {
-    const SideF32 L = load_f32(m, Xin.hi, Xin.lo, c, hsmf);
+    const float4 xin = __ldg(&Xin.x[c]);
+    const float4 cp = __ldg(&m.CP[c]);
+    const float4 cs = __ldg(&m.CS[c]);
+    const SideF32 L = make_side_f32(xin, cp, m.hsmf, m.hsm);
     float f0, f1, f2;
-    face_sum_f32(m, Xin.hi, Xin.lo, c, L, hsmf, g, f0, f1, f2);
-    const float A = m.areaf[c];
+    face_sum_f32<NS>(m, Xin.x, c, L, f0, f1, f2);
+    const float A = cs.z;
     const float r0 = -f0 / A, r1 = -f1 / A, r2 = -f2 / A;
-    const float fr = friction_coef(g, (float)m.kn2, hsmf, m.manf[c], L.s.h, L.s.hu, L.s.hv);
-    const float sx = L.s.dry ? 0.0f : (g * L.s.xi * m.s0xf[c] - fr * L.s.hu);
-    const float sy = L.s.dry ? 0.0f : (g * L.s.xi * m.s0yf[c] - fr * L.s.hv);
+    const float fr = friction_coef(m.gf, m.kn2f, m.hsmf, cp.w, L.s.h, L.s.hu, L.s.hv);
+    const float sx = L.s.dry ? 0.0f : (m.gf * L.s.xi * cs.x - fr * L.s.hu);
+    const float sy = L.s.dry ? 0.0f : (m.gf * L.s.xi * cs.y - fr * L.s.hv);
     const float d0 = r0, d1 = r1 + sx, d2 = r2 + sy;
     if (mode == kModeRhs) {
       Rout[c] = d0; Rout[m.n + c] = d1; Rout[2 * m.n + c] = d2;
     } else {
       const float dt = *s.dtf;
+      const float2 qin = Xin.q[c];
+      const float hi[3] = {xin.x, xin.z, xin.w}, lo[3] = {xin.y, qin.x, qin.y};
       const float inc[3] = {dt * d0, dt * d1, dt * d2};
       float xh[3], xl[3];
+      if (mode == kModeStage2) {
+        const float4 xb = Xbase.x[c];
+        const float2 qb = Xbase.q[c];
+        const float bh[3] = {xb.x, xb.z, xb.w}, bl[3] = {xb.y, qb.x, qb.y};
 #pragma unroll
-      for (int b = 0; b < 3; ++b) {
-        const size_t i = (size_t)b * m.n + c;
-        if (mode == kModeStage2) {
-          float sh, sl;
-          df_add2(Xbase.hi[i], Xbase.lo[i], Xin.hi[i], Xin.lo[i], sh, sl);
-          df_add(sh, sl, inc[b], xh[b], xl[b]);
+        for (int b = 0; b < 3; ++b) {
+          float sh, slo;
+          df_add2(bh[b], bl[b], hi[b], lo[b], sh, slo);
+          df_add(sh, slo, inc[b], xh[b], xl[b]);
           xh[b] *= 0.5f;
           xl[b] *= 0.5f;
-        } else {
-          df_add(Xin.hi[i], Xin.lo[i], inc[b], xh[b], xl[b]);
         }
-      }
-      const float hh = m.hsthi[c], hl = m.hstlo[c];
-      DepthF32 dn = depth_f32(xh[0], xl[0], hh, hl, hsmf, m.hsm);
-      bool clamp;
-      if (mode == kModeEulerRef) {
-        clamp = (double)xh[0] + (double)xl[0] < m.hsm;
       } else {
-        clamp = dn.dry;   // h <= h_small (within the pair granularity): h = h_small, q = 0
+#pragma unroll
+        for (int b = 0; b < 3; ++b) df_add(hi[b], lo[b], inc[b], xh[b], xl[b]);
       }
+      DepthF32 dn = depth_f32(xh[0], xl[0], cp.x, cp.y, m.hsmf, m.hsm);
+      const bool clamp = (mode == kModeEulerRef) ? ((double)xh[0] + (double)xl[0] < m.hsm)
+                                                 : dn.dry;   // h <= h_small (pair granularity): h = h_small, q = 0
       if (clamp) {
-        const double x0 = (mode == kModeEulerRef) ? m.hsm : dry_xi(m.hsm, (double)hh + (double)hl);
+        const double x0 = (mode == kModeEulerRef) ? m.hsm : dry_xi(m.hsm, (double)cp.x + (double)cp.y);
         xh[0] = (float)x0;
         xl[0] = (float)(x0 - (double)xh[0]);
         xh[1] = xl[1] = xh[2] = xl[2] = 0.0f;
         dn.dry = true;
-        dn.h = hsmf;
+        dn.h = m.hsmf;
       }
       if (!(isfinite(xh[0]) && isfinite(xh[1]) && isfinite(xh[2]))) atomicOr(s.flags, 1);
-#pragma unroll
-      for (int b = 0; b < 3; ++b) {
-        Xout.hi[(size_t)b * m.n + c] = xh[b];
-        Xout.lo[(size_t)b * m.n + c] = xl[b];
-      }
-      if (cfl) cand = cfl_candidate_f32(m, c, dn.h, xh[1], xh[2], dn.dry, g);
+      Xout.x[c] = make_float4(xh[0], xl[0], xh[1], xh[2]);
+      Xout.q[c] = make_float2(xl[1], xl[2]);
+      if (cfl) cand = cfl_candidate_f32<NS>(m, c, dn.h, xh[1], xh[2], dn.dry, A);
     }
   }
   if (cfl) block_min_publish_f(cand, s.cflMinF);
 }
 
+template <int NS>
 __global__ void __launch_bounds__(kBlock) k_cfl_f32(DevMesh m, DevScalars s, StateF32 X) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   float cand = INFINITY;
   if (c < m.n) {
-    const float hsmf = (float)m.hsm;
-    const SideF32 L = load_f32(m, X.hi, X.lo, c, hsmf);
-    cand = cfl_candidate_f32(m, c, L.s.h, X.hi[m.n + c], X.hi[2 * m.n + c], L.s.dry, (float)m.g);
+    const float4 x = X.x[c];
+    const SideF32 L = make_side_f32(x, m.CP[c], m.hsmf, m.hsm);
+    cand = cfl_candidate_f32<NS>(m, c, L.s.h, x.z, x.w, L.s.dry, m.CS[c].z);
   }
   block_min_publish_f(cand, s.cflMinF);
 }
@@ -232,12 +157,12 @@ __global__ void __launch_bounds__(kBlock) k_cfl_f32(DevMesh m, DevScalars s, Sta
 __global__ void __launch_bounds__(kBlock) k_inlet_total_f32(DevMesh m, DevScalars s, StateF32 X) {
   const int g = blockIdx.x;
   const int o0 = m.inletOff[g], o1 = m.inletOff[g + 1];
-  const float hsmf = (float)m.hsm;
   double acc = 0.0;
   for (int i = o0 + threadIdx.x; i < o1; i += blockDim.x) {
     const int c = m.inletCell[i];
-    const SideF32 L = load_f32(m, X.hi, X.lo, c, hsmf);
-    acc += L.s.dry ? 0.0 : m.inletLp53[i] * (double)L.s.h / (double)m.manf[c];
+    const float4 cp = m.CP[c];
+    const SideF32 L = make_side_f32(X.x[c], cp, m.hsmf, m.hsm);
+    acc += L.s.dry ? 0.0 : m.inletLp53[i] * (double)L.s.h / (double)cp.w;
   }
   const double t = block_sum(acc);
   if (threadIdx.x == 0) {
@@ -293,26 +218,32 @@ __global__ void k_scatter_f64(int32_t n, const int32_t* __restrict__ perm, const
   user[2 * n + o] = dev[2 * n + i];
 }
 
+__device__ __forceinline__ void split(double v, float& h, float& l) {
+  h = (float)v;
+  l = (float)(v - (double)h);
+}
+
 __global__ void k_gather_f32(int32_t n, const int32_t* __restrict__ perm, const double* __restrict__ user, StateF32 X) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int o = perm[i];
-#pragma unroll
-  for (int b = 0; b < 3; ++b) {
-    const double v = user[(size_t)b * n + o];
-    const float h = (float)v;
-    X.hi[(size_t)b * n + i] = h;
-    X.lo[(size_t)b * n + i] = (float)(v - (double)h);
-  }
+  float xh, xl, uh, ul, vh, vl;
+  split(user[o], xh, xl);
+  split(user[n + o], uh, ul);
+  split(user[2 * n + o], vh, vl);
+  X.x[i] = make_float4(xh, xl, uh, vh);
+  X.q[i] = make_float2(ul, vl);
 }
 
 __global__ void k_scatter_f32(int32_t n, const int32_t* __restrict__ perm, StateF32 X, double* __restrict__ user) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int o = perm[i];
-#pragma unroll
-  for (int b = 0; b < 3; ++b)
-    user[(size_t)b * n + o] = (double)X.hi[(size_t)b * n + i] + (double)X.lo[(size_t)b * n + i];
+  const float4 x = X.x[i];
+  const float2 q = X.q[i];
+  user[o] = (double)x.x + (double)x.y;
+  user[n + o] = (double)x.z + (double)q.x;
+  user[2 * n + o] = (double)x.w + (double)q.y;
 }
 
 __global__ void k_flush(uint4* buf, size_t n16) {
@@ -321,15 +252,21 @@ __global__ void k_flush(uint4* buf, size_t n16) {
 }
 
 }  // namespace
+
 void launch_inlet_total_f32(const DevMesh& m, const DevScalars& s, StateF32 X, cudaStream_t st) {
   if (m.nInlet > 0) k_inlet_total_f32<<<m.nInlet, kBlock, 0, st>>>(m, s, X);
 }
 void launch_stage_f32(const DevMesh& m, const DevScalars& s, int mode, StateF32 Xin, StateF32 Xbase, StateF32 Xout,
                       double* Rout, bool cfl, cudaStream_t st) {
-  k_stage_f32<<<blocks_for(m.n), kBlock, 0, st>>>(m, s, mode, Xin, Xbase, Xout, Rout, cfl ? 1 : 0);
+  const int f = cfl ? 1 : 0;
+  if (m.nslot <= 3) k_stage_f32<3><<<blocks_for(m.n), kBlock, 0, st>>>(m, s, mode, Xin, Xbase, Xout, Rout, f);
+  else if (m.nslot <= 4) k_stage_f32<4><<<blocks_for(m.n), kBlock, 0, st>>>(m, s, mode, Xin, Xbase, Xout, Rout, f);
+  else k_stage_f32<8><<<blocks_for(m.n), kBlock, 0, st>>>(m, s, mode, Xin, Xbase, Xout, Rout, f);
 }
 void launch_cfl_f32(const DevMesh& m, const DevScalars& s, StateF32 X, cudaStream_t st) {
-  k_cfl_f32<<<blocks_for(m.n), kBlock, 0, st>>>(m, s, X);
+  if (m.nslot <= 3) k_cfl_f32<3><<<blocks_for(m.n), kBlock, 0, st>>>(m, s, X);
+  else if (m.nslot <= 4) k_cfl_f32<4><<<blocks_for(m.n), kBlock, 0, st>>>(m, s, X);
+  else k_cfl_f32<8><<<blocks_for(m.n), kBlock, 0, st>>>(m, s, X);
 }
 void launch_step_begin(const DevScalars& s, bool cflMode, double cfl, cudaStream_t st) {
   k_step_begin<<<1, 32, 0, st>>>(s, cflMode ? 1 : 0, cfl);

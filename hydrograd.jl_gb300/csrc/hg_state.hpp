@@ -19,9 +19,7 @@ struct DevMesh {
   const double* snx = nullptr;       // [nslot*n] outward unit normal x
   const double* sny = nullptr;
   const double* slen = nullptr;      // [nslot*n] edge length
-  const float* snxf = nullptr;       // FP32 copies
-  const float* snyf = nullptr;
-  const float* slenf = nullptr;
+  const float4* SL = nullptr;        // FP32 path: [nslot*n] {nx, ny, L, nb as bits} (see hg_f32.cuh)
   const int32_t* bfInfo = nullptr;   // [nbf] type | group << 2
   const double* bfLp23 = nullptr;    // [nbf] L^(2/3) (inlet-Q faces)
   const float* bfLp23f = nullptr;
@@ -35,14 +33,11 @@ struct DevMesh {
   const double* man = nullptr;       // Manning n
   const double* s0x = nullptr;
   const double* s0y = nullptr;
-  // FP32 per-cell data (hstill as an exact hi+lo pair)
-  const float* areaf = nullptr;
-  const float* hsthi = nullptr;
-  const float* hstlo = nullptr;
-  const float* zbf = nullptr;
-  const float* manf = nullptr;
-  const float* s0xf = nullptr;
-  const float* s0yf = nullptr;
+  // FP32 per-cell data: CP {hstill_hi, hstill_lo, zb, n} (hstill as an exact
+  // hi + lo pair), CS {S0x, S0y, area, 0}
+  const float4* CP = nullptr;
+  const float4* CS = nullptr;
+  float hsmf = 1e-3f, gf = 9.81f, kn2f = 1.0f;
   // Boundary values
   const double* exitWse = nullptr;   // [nExit]
   const double* inletQ = nullptr;    // [nInlet]
@@ -71,10 +66,10 @@ void launch_stage_f64(const DevMesh& m, const DevScalars& s, int mode, const dou
                       double* Qout, bool cfl, cudaStream_t st);
 void launch_cfl_f64(const DevMesh& m, const DevScalars& s, const double* Q, cudaStream_t st);
 
-// FP32-compensated state: hi and lo float arrays, each [xi | qx | qy].
+// FP32-compensated state: x[c] {xi_hi, xi_lo, qx_hi, qy_hi}, q[c] {qx_lo, qy_lo}.
 struct StateF32 {
-  float* hi = nullptr;
-  float* lo = nullptr;
+  float4* x = nullptr;
+  float2* q = nullptr;
 };
 void launch_inlet_total_f32(const DevMesh& m, const DevScalars& s, StateF32 X, cudaStream_t st);
 void launch_stage_f32(const DevMesh& m, const DevScalars& s, int mode, StateF32 Xin, StateF32 Xbase, StateF32 Xout,
