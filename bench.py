@@ -276,9 +276,18 @@ def run_ours(args):
     if args.adj_steps > 0:
         from hydrograd_gb.workloads import probes_and_perturbation
         probes, _ = probes_and_perturbation(case, 64)
-        dt_adj = 0.5 * ctxs["fp64"].integrate(case["Q0"], 1, cfl=0.4)[1][0]
-        hs = ctxs["fp64"].bed()["hstill"]
-        obs = np.tile(case["Q0"][probes] + hs[probes] + 0.01, (args.adj_steps, 1))
+        c64 = ctxs["fp64"]
+        dt_adj = 0.5 * c64.integrate(case["Q0"], 1, cfl=0.4)[1][0]
+        hs = c64.bed()["hstill"]
+        # Observations: probe depths of an FP64 run with hidden zone values.
+        nz = len(case["manning_zones"])
+        c64.set_manning_zones(case["mat_id"], case["manning_zones"] * (1.0 + 0.2 * np.sin(np.arange(nz) + 1.0)))
+        obs = np.zeros((args.adj_steps, len(probes)))
+        q = case["Q0"].copy()
+        for k in range(args.adj_steps):
+            q = c64.integrate(q, 1, dt=dt_adj)[0]
+            obs[k] = q[probes] + hs[probes]
+        c64.set_manning_zones(case["mat_id"], case["manning_zones"])
         grads = {}
         for prec in ("fp32c", "fp64"):
             ctx = ctxs[prec]
@@ -300,7 +309,8 @@ def run_ours(args):
             "grad_zb_field_rel_linf": float(np.abs(g32["g_zb"] - g64["g_zb"]).max() / np.abs(g64["g_zb"]).max()),
             "loss_rel": float(abs(g32["loss"] - g64["loss"]) / abs(g64["loss"])),
         }
-        adj["config"] = f"{args.adj_steps} fixed-dt steps (dt = half the initial CFL step), checkpoints every 50, 64 probes"
+        adj["config"] = (f"{args.adj_steps} fixed-dt steps (dt = half the initial CFL step), checkpoints every 50, "
+                         f"{len(probes)} probes on the pool rim, observations from an FP64 run with perturbed zone n")
     if rank != 0:
         return
     peak, peak_kind = load_peaks()

@@ -160,9 +160,53 @@ int enqueue_download(hg_ctx* c, double* Q) {
   return HG_OK;
 }
 
-// One SSP-RK2 step on the resident state (QA / XA).  Kernels per step:
+// The FP32 path steps with two fused launches when the inlet groups fit.
+bool fused(const hg_ctx* c) { return c->precision == HG_FP32C && c->dm.nInlet <= kMaxFusedInlets; }
+
+// Before a run of fused steps: conveyance totals of the resident state and, in
+// CFL mode, its CFL minimum in buffer 0 (the fixed dt is already on the device).
+void enqueue_fused_prime(hg_ctx* c, bool cflMode) {
+  DevMesh m = c->dm;
+  m.totalA = c->d_tot;
+  launch_inlet_total_f32(m, c->ds, xa(c), c->stream);
+  c->parity = 0;
+  if (cflMode) {
+    launch_reset_cfl(c->ds, 0, c->stream);
+    launch_cfl_f32(c->dm, c->ds, xa(c), c->stream);
+  }
+  c->launches += (c->dm.nInlet > 0 ? 1 : 0) + (cflMode ? 2 : 0);
+}
+
+// One fused SSP-RK2 step: stage 1 (records the step, totals of Q1), stage 2
+// (totals of Q2 and the CFL minimum of Q2 for the next step).
+void enqueue_rk2_step_fused(hg_ctx* c, bool cflMode, double cfl) {
+  StageFuse f;
+  f.partials = c->d_partials;
+  f.ticket = c->d_ticket;
+  f.blockSlot = c->d_blockSlot;
+  f.nSlots = c->nSlots;
+  f.cflMode = cflMode ? 1 : 0;
+  f.cfl = cfl;
+  f.parity = c->parity;
+  f.record = 1;
+  f.totalIn = c->d_tot;
+  f.totalOut = c->d_tot + kMaxFusedInlets;
+  launch_stage_f32_fused(c->dm, c->ds, kModeStage1, xa(c), StateF32{}, xb(c), f, c->stream);
+  f.record = 0;
+  f.totalIn = c->d_tot + kMaxFusedInlets;
+  f.totalOut = c->d_tot;
+  launch_stage_f32_fused(c->dm, c->ds, kModeStage2, xb(c), xa(c), xa(c), f, c->stream);
+  c->parity ^= 1;
+  c->launches += 2;
+}
+
+// One SSP-RK2 step on the resident state (QA / XA).  Unfused kernels per step:
 // step_begin, [inlet], stage1, [inlet], stage2.
 void enqueue_rk2_step(hg_ctx* c, bool cflMode, double cfl) {
+  if (fused(c)) {
+    enqueue_rk2_step_fused(c, cflMode, cfl);
+    return;
+  }
   launch_step_begin(c->ds, cflMode, cfl, c->stream);
   if (c->precision == HG_FP64) {
     launch_inlet_total_f64(c->dm, c->ds, c->QA, c->stream);
@@ -206,6 +250,21 @@ int set_fixed_dt(hg_ctx* c, double dt) {
   HG_CUDA(c, cudaMemcpyAsync(c->ds.dt, &dt, sizeof(double), cudaMemcpyHostToDevice, c->stream));
   HG_CUDA(c, cudaMemcpyAsync(c->ds.dtf, &dtf, sizeof(float), cudaMemcpyHostToDevice, c->stream));
   HG_CUDA(c, cudaStreamSynchronize(c->stream));
+  return HG_OK;
+}
+
+// Set-up before a run of RK2 steps (rk2 = false: reference Euler steps).
+int begin_steps(hg_ctx* c, bool rk2, double dt, double cfl) {
+  const bool cflMode = dt <= 0;
+  if (!cflMode) {
+    int rc = set_fixed_dt(c, dt);
+    if (rc) return rc;
+  }
+  if (rk2 && fused(c)) {
+    enqueue_fused_prime(c, cflMode);
+  } else if (cflMode && !c->cflPrimed) {
+    enqueue_cfl_prime(c);
+  }
   return HG_OK;
 }
 
@@ -443,12 +502,9 @@ int hg_integrate(hg_ctx* ctx, double* Q, double /*t0*/, int32_t nsteps, int32_t 
   rc = enqueue_upload(ctx, Q);
   if (rc) return rc;
   const bool cflMode = dt <= 0;
-  if (!cflMode) {
-    rc = set_fixed_dt(ctx, dt);
-    if (rc) return rc;
-  } else {
-    enqueue_cfl_prime(ctx);
-  }
+  ctx->cflPrimed = false;
+  rc = begin_steps(ctx, method == 0, dt, cfl);
+  if (rc) return rc;
   int saved = 0;
   for (int s = 0; s < nsteps; ++s) {
     if (method == 0) enqueue_rk2_step(ctx, cflMode, cfl);
@@ -495,22 +551,24 @@ int hg_advance(hg_ctx* ctx, int32_t nsteps, double dt, double cfl, int32_t graph
   if (dt <= 0 && !(cfl > 0)) return fail(ctx, HG_ERR_ARG, "hg_advance: need dt > 0 or cfl > 0");
   cudaSetDevice(ctx->device);
   const bool cflMode = dt <= 0;
-  if (!cflMode) {
-    int rc = set_fixed_dt(ctx, dt);
-    if (rc) return rc;
-  } else if (!ctx->cflPrimed) {
-    enqueue_cfl_prime(ctx);
-  }
+  int rc0 = begin_steps(ctx, true, dt, cfl);
+  if (rc0) return rc0;
   int done = 0;
   if (graph) {
     const int K = kGraphSteps;
-    if (nsteps >= K) {
-      if (!ctx->graphValid || ctx->graphCflMode != cflMode || ctx->graphCfl != cfl) {
+    if (fused(ctx) && ctx->graphValid && ctx->parity != ctx->graphParity && nsteps > K) {
+      enqueue_rk2_step(ctx, cflMode, cfl);   // bring the CFL-buffer parity to the graph's
+      ++done;
+    }
+    if (nsteps - done >= K) {
+      if (!ctx->graphValid || ctx->graphCflMode != cflMode || ctx->graphCfl != cfl ||
+          (fused(ctx) && ctx->parity != ctx->graphParity)) {
         if (ctx->graphExec) {
           cudaGraphExecDestroy(ctx->graphExec);
           ctx->graphExec = nullptr;
         }
         cudaGraph_t g;
+        ctx->graphParity = ctx->parity;
         HG_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
         int64_t before = ctx->launches;
         for (int s = 0; s < K; ++s) enqueue_rk2_step(ctx, cflMode, cfl);
@@ -528,6 +586,7 @@ int hg_advance(hg_ctx* ctx, int32_t nsteps, double dt, double cfl, int32_t graph
         HG_CUDA(ctx, cudaGraphLaunch(ctx->graphExec, ctx->stream));
         ctx->launches += ctx->graphLaunches;
       }
+      ctx->parity = ctx->graphParity;   // K is even: a graph ends on the parity it starts with
     }
   }
   for (; done < nsteps; ++done) enqueue_rk2_step(ctx, cflMode, cfl);
@@ -571,12 +630,8 @@ int hg_advance_timed(hg_ctx* ctx, int32_t nsteps, double dt, double cfl, int32_t
   if (dt <= 0 && !(cfl > 0)) return fail(ctx, HG_ERR_ARG, "hg_advance_timed: need dt > 0 or cfl > 0");
   cudaSetDevice(ctx->device);
   const bool cflMode = dt <= 0;
-  if (!cflMode) {
-    int rc = set_fixed_dt(ctx, dt);
-    if (rc) return rc;
-  } else if (!ctx->cflPrimed) {
-    enqueue_cfl_prime(ctx);
-  }
+  int rc0 = begin_steps(ctx, true, dt, cfl);
+  if (rc0) return rc0;
   std::vector<cudaEvent_t> ev(2 * (size_t)nsteps, nullptr);
   for (auto& e : ev) HG_CUDA(ctx, cudaEventCreate(&e));
   for (int s = 0; s < nsteps; ++s) {
@@ -674,13 +729,16 @@ int ctx_setup_device(hg_ctx* c) {
   for (size_t g = 0; g < m.inletGroups.size(); ++g) groupOf[m.inletGroups[g]] = (int)g;
   for (size_t g = 0; g < m.exitGroups.size(); ++g) groupOf[m.exitGroups[g]] = (int)g;
   std::vector<int32_t> bfInfo(nbf, 0);
-  std::vector<double> bfLp23(nbf, 0.0);
+  std::vector<double> bfLp23(nbf, 0.0), bfLp53(nbf, 0.0);
   for (int f = 0; f < m.nFaces; ++f) {
     if (bfOf[f] < 0) continue;
     const int bi = m.faceBnd[f];
     const int type = m.bnd[bi].bc;
     bfInfo[bfOf[f]] = type | (groupOf[bi] << 2);
-    if (type == HG_BC_INLETQ) bfLp23[bfOf[f]] = std::pow(m.faceLen[f], 2.0 / 3.0);
+    if (type == HG_BC_INLETQ) {
+      bfLp23[bfOf[f]] = std::pow(m.faceLen[f], 2.0 / 3.0);
+      bfLp53[bfOf[f]] = std::pow(m.faceLen[f], 5.0 / 3.0);
+    }
   }
   const int S = m.maxCellFaces;
   std::vector<int32_t> nb((size_t)S * N, INT32_MIN);
@@ -716,7 +774,7 @@ int ctx_setup_device(hg_ctx* c) {
   c->inletQ.assign(m.inletGroups.size(), 0.0);
   c->exitWse.assign(m.exitGroups.size(), 0.0);
 
-  int32_t* d_nb; double *d_snx, *d_sny, *d_slen, *d_area, *d_lp23, *d_lp53; float* d_lp23f; float4* d_SL;
+  int32_t* d_nb; double *d_snx, *d_sny, *d_slen, *d_area, *d_lp23, *d_lp53, *d_bflp53; float* d_lp23f; float4* d_SL;
   int32_t *d_bfInfo, *d_inletOff, *d_inletCell;
   HG_CUDA(c, dalloc(c, &d_nb, nb.size()));
   HG_CUDA(c, dalloc(c, &d_snx, snx.size()));
@@ -727,6 +785,7 @@ int ctx_setup_device(hg_ctx* c) {
   HG_CUDA(c, dalloc(c, &d_bfInfo, (size_t)std::max(nbf, 1)));
   HG_CUDA(c, dalloc(c, &d_lp23, (size_t)std::max(nbf, 1)));
   HG_CUDA(c, dalloc(c, &d_lp23f, (size_t)std::max(nbf, 1)));
+  HG_CUDA(c, dalloc(c, &d_bflp53, (size_t)std::max(nbf, 1)));
   HG_CUDA(c, dalloc(c, &d_inletOff, inletOff.size()));
   HG_CUDA(c, dalloc(c, &d_inletCell, std::max<size_t>(inletCell.size(), 1)));
   HG_CUDA(c, dalloc(c, &d_lp53, std::max<size_t>(inletLp53.size(), 1)));
@@ -750,11 +809,28 @@ int ctx_setup_device(hg_ctx* c) {
   // Scalars
   HG_CUDA(c, dalloc(c, &c->ds.dt, 1));
   HG_CUDA(c, dalloc(c, &c->ds.dtf, 1));
-  HG_CUDA(c, dalloc(c, &c->ds.cflMin, 1));
-  HG_CUDA(c, dalloc(c, &c->ds.cflMinF, 1));
+  HG_CUDA(c, dalloc(c, &c->ds.cflMin, 2));
+  HG_CUDA(c, dalloc(c, &c->ds.cflMinF, 2));
   HG_CUDA(c, dalloc(c, &c->ds.stepIdx, 1));
   HG_CUDA(c, dalloc(c, &c->ds.tSum, 1));
   HG_CUDA(c, dalloc(c, &c->ds.flags, 1));
+  HG_CUDA(c, dalloc(c, &c->d_tot, (size_t)2 * kMaxFusedInlets));
+  // Fused FP32 stepping: the stage blocks holding inlet-Q cells, numbered in block order.
+  std::vector<int32_t> blockSlot;
+  {
+    DevMesh sized;
+    sized.n = N;
+    const int nBlocks = std::max(stage_blocks_f32(sized), 1);
+    blockSlot.assign(nBlocks, -1);
+    for (int32_t cell : inletCell) blockSlot[cell / kStageBlockF32] = 0;
+    c->nSlots = 0;
+    for (int b = 0; b < nBlocks; ++b)
+      if (blockSlot[b] == 0) blockSlot[b] = c->nSlots++;
+    HG_CUDA(c, dalloc(c, &c->d_partials, (size_t)kMaxFusedInlets * std::max(c->nSlots, 1)));
+    HG_CUDA(c, dalloc(c, &c->d_blockSlot, blockSlot.size()));
+  }
+  HG_CUDA(c, dalloc(c, &c->d_ticket, 1));
+  HG_CUDA(c, cudaMemsetAsync(c->d_ticket, 0, sizeof(unsigned int), c->stream));
   {
     int rc = ensure_dt_capacity(c, 1024);
     if (rc) return rc;
@@ -775,6 +851,7 @@ int ctx_setup_device(hg_ctx* c) {
   }
   c->h_area = to_float(area);
   HG_CUDA(c, upload(c, d_nb, nb));
+  HG_CUDA(c, upload(c, c->d_blockSlot, blockSlot));
   HG_CUDA(c, upload(c, d_snx, snx));
   HG_CUDA(c, upload(c, d_sny, sny));
   HG_CUDA(c, upload(c, d_slen, slen));
@@ -784,6 +861,7 @@ int ctx_setup_device(hg_ctx* c) {
   HG_CUDA(c, upload(c, d_bfInfo, bfInfo));
   HG_CUDA(c, upload(c, d_lp23, bfLp23));
   HG_CUDA(c, upload(c, d_lp23f, lp23f));
+  HG_CUDA(c, upload(c, d_bflp53, bfLp53));
   HG_CUDA(c, upload(c, d_inletOff, inletOff));
   HG_CUDA(c, upload(c, d_inletCell, inletCell));
   HG_CUDA(c, upload(c, d_lp53, inletLp53));
@@ -800,7 +878,7 @@ int ctx_setup_device(hg_ctx* c) {
   dm.nExit = (int32_t)m.exitGroups.size();
   dm.nb = d_nb; dm.snx = d_snx; dm.sny = d_sny; dm.slen = d_slen;
   dm.SL = d_SL;
-  dm.bfInfo = d_bfInfo; dm.bfLp23 = d_lp23; dm.bfLp23f = d_lp23f;
+  dm.bfInfo = d_bfInfo; dm.bfLp23 = d_lp23; dm.bfLp23f = d_lp23f; dm.bfLp53 = d_bflp53;
   dm.inletOff = d_inletOff; dm.inletCell = d_inletCell; dm.inletLp53 = d_lp53;
   dm.area = d_area; dm.hst = c->d_hst; dm.zb = c->d_zb; dm.man = c->d_man; dm.s0x = c->d_s0x; dm.s0y = c->d_s0y;
   dm.CP = c->d_CP; dm.CS = c->d_CS;

@@ -44,6 +44,15 @@ struct hg_ctx {
   void* flushBuf = nullptr;
   size_t flushBytes = 0;
   bool cflPrimed = false;
+  // Fused FP32 stepping: conveyance totals of the resident state (tot) and of
+  // the stage buffer (tot + kMaxFusedInlets), per-block partials, last-block ticket.
+  double* d_tot = nullptr;
+  double* d_partials = nullptr;
+  unsigned int* d_ticket = nullptr;
+  int32_t* d_blockSlot = nullptr;   // slot of each stage block that holds inlet cells, else -1
+  int32_t nSlots = 0;
+  int parity = 0;                   // CFL-minimum buffer the next fused step reads
+  int graphParity = 0;              // parity the captured graph starts (and ends) with
   // Captured graph of kGraphSteps steps
   cudaGraphExec_t graphExec = nullptr;
   bool graphValid = false, graphCflMode = false;

@@ -24,17 +24,15 @@ using namespace devred;
 
 namespace {
 
-constexpr int kBlock = 256;
+constexpr int kBlock = kStageBlockF32;
 
 inline int blocks_for(int n) { return (n + kBlock - 1) / kBlock; }
 
 template <int NS>
 __device__ __forceinline__ void face_sum_f32(const DevMesh& m, const float4* __restrict__ X, int c, const SideF32& L,
-                                             float& f0, float& f1, float& f2) {
+                                             const float4 (&sl)[NS], const double* __restrict__ totalA, float man,
+                                             int32_t* flags, float& f0, float& f1, float& f2) {
   f0 = 0.0f; f1 = 0.0f; f2 = 0.0f;
-  float4 sl[NS];
-#pragma unroll
-  for (int k = 0; k < NS; ++k) sl[k] = __ldg(&m.SL[(size_t)k * m.n + c]);
 #pragma unroll
   for (int k = 0; k < NS; ++k) {
     const int32_t nb = slot_nb(sl[k]);
@@ -49,10 +47,10 @@ __device__ __forceinline__ void face_sum_f32(const DevMesh& m, const float4* __r
     } else {
       const int32_t bf = boundary_index(nb);
       const int32_t info = m.bfInfo[bf], type = info & 3, grp = info >> 2;
-      const float man = __ldg(&m.CP[c]).w;
+      if (type == kBcInletQ && !(totalA[grp] > 1e-10)) atomicOr(flags, 2);   // bc_2D.jl:679
       R = ghost_state<float>(L.s, type, nx, ny, m.hsmf, type == kBcExitH ? (float)m.exitWse[grp] : 0.0f,
                              type == kBcInletQ ? (float)m.inletQ[grp] : 0.0f,
-                             type == kBcInletQ ? (float)m.totalA[grp] : 1.0f, m.bfLp23f[bf], man);
+                             type == kBcInletQ ? (float)totalA[grp] : 1.0f, m.bfLp23f[bf], man);
       // xi_ghost - xi = (h_ghost - h) + ((h - hstill) - xi)
       dxi = (R.h - L.s.h) + L.excess;
     }
@@ -65,33 +63,79 @@ __device__ __forceinline__ void face_sum_f32(const DevMesh& m, const float4* __r
 }
 
 template <int NS>
-__device__ __forceinline__ float cfl_candidate_f32(const DevMesh& m, int c, float h, float qx, float qy, bool dry,
-                                                   float area) {
+__device__ __forceinline__ float cfl_candidate_f32(const DevMesh& m, const float4 (&sl)[NS], float h, float qx,
+                                                   float qy, bool dry, float area) {
   if (dry) { qx = 0.0f; qy = 0.0f; }
   const float u = qx / h, v = qy / h, a = sqrtf(m.gf * h);
   float s = 0.0f;
 #pragma unroll
   for (int k = 0; k < NS; ++k) {
-    const float4 sl = __ldg(&m.SL[(size_t)k * m.n + c]);
-    if (slot_nb(sl) == kNoFace) continue;
-    s += sl.z * (fabsf(u * sl.x + v * sl.y) + a);
+    if (slot_nb(sl[k]) == kNoFace) continue;
+    s += sl[k].z * (fabsf(u * sl[k].x + v * sl[k].y) + a);
   }
   return area / s;
 }
 
 template <int NS>
+__device__ __forceinline__ void load_slots(const DevMesh& m, int c, float4 (&sl)[NS]) {
+#pragma unroll
+  for (int k = 0; k < NS; ++k) sl[k] = __ldg(&m.SL[(size_t)k * m.n + c]);
+}
+
+// Inlet-Q conveyance totals of a fused stage's output state: the blocks that
+// hold inlet cells write partial sums; the last of them adds the partials in
+// slot order.
+__device__ __forceinline__ void fused_inlet_totals(const DevMesh& m, const StageFuse& f,
+                                                   const double (&contrib)[kMaxFusedInlets]) {
+  const int slot = f.blockSlot[blockIdx.x];
+  if (slot < 0) return;   // uniform over the block
+  __shared__ int isLast;
+  const int ng = m.nInlet;
+  for (int g = 0; g < ng; ++g) {
+    const double t = block_sum(contrib[g]);
+    if (threadIdx.x == 0) f.partials[(size_t)g * f.nSlots + slot] = t;
+  }
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const unsigned int t = atomicAdd(f.ticket, 1u);
+    isLast = (t == (unsigned int)f.nSlots - 1u);
+  }
+  __syncthreads();
+  if (!isLast) return;
+  __threadfence();
+  for (int g = 0; g < ng; ++g) {
+    double acc = 0.0;
+    for (int b = threadIdx.x; b < f.nSlots; b += blockDim.x) acc += __ldcg(&f.partials[(size_t)g * f.nSlots + b]);
+    const double t = block_sum(acc);
+    if (threadIdx.x == 0) f.totalOut[g] = t;
+  }
+  if (threadIdx.x == 0) *f.ticket = 0u;
+}
+
+// dt of a fused step: from the published CFL minimum (CFL mode) or the fixed dt.
+__device__ __forceinline__ double fused_dt(const DevScalars& s, const StageFuse& f) {
+  if (!f.cflMode) return *s.dt;
+  const double mn = fmin(__longlong_as_double((long long)s.cflMin[f.parity]),
+                         (double)__uint_as_float(s.cflMinF[f.parity]));
+  return f.cfl * mn;
+}
+
+template <int NS, bool FUSED>
 __global__ void __launch_bounds__(kBlock) k_stage_f32(DevMesh m, DevScalars s, int mode, StateF32 Xin, StateF32 Xbase,
-                                                      StateF32 Xout, double* Rout, int cfl) {
+                                                      StateF32 Xout, double* Rout, int cfl, StageFuse f) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   const bool active = c < m.n;
   float cand = INFINITY;
+  double contrib[kMaxFusedInlets] = {0.0, 0.0, 0.0, 0.0};
   if (active) {
+    float4 sl[NS];
+    load_slots<NS>(m, c, sl);
     const float4 xin = __ldg(&Xin.x[c]);
     const float4 cp = __ldg(&m.CP[c]);
     const float4 cs = __ldg(&m.CS[c]);
     const SideF32 L = make_side_f32(xin, cp, m.hsmf, m.hsm);
     float f0, f1, f2;
-    face_sum_f32<NS>(m, Xin.x, c, L, f0, f1, f2);
+    face_sum_f32<NS>(m, Xin.x, c, L, sl, FUSED ? f.totalIn : m.totalA, cp.w, s.flags, f0, f1, f2);
     const float A = cs.z;
     const float r0 = -f0 / A, r1 = -f1 / A, r2 = -f2 / A;
     const float fr = friction_coef(m.gf, m.kn2f, m.hsmf, cp.w, L.s.h, L.s.hu, L.s.hv);
@@ -101,7 +145,7 @@ __global__ void __launch_bounds__(kBlock) k_stage_f32(DevMesh m, DevScalars s, i
     if (mode == kModeRhs) {
       Rout[c] = d0; Rout[m.n + c] = d1; Rout[2 * m.n + c] = d2;
     } else {
-      const float dt = *s.dtf;
+      const float dt = FUSED ? (float)fused_dt(s, f) : *s.dtf;
       const float2 qin = Xin.q[c];
       const float hi[3] = {xin.x, xin.z, xin.w}, lo[3] = {xin.y, qin.x, qin.y};
       const float inc[3] = {dt * d0, dt * d1, dt * d2};
@@ -136,10 +180,38 @@ __global__ void __launch_bounds__(kBlock) k_stage_f32(DevMesh m, DevScalars s, i
       if (!(isfinite(xh[0]) && isfinite(xh[1]) && isfinite(xh[2]))) atomicOr(s.flags, 1);
       Xout.x[c] = make_float4(xh[0], xl[0], xh[1], xh[2]);
       Xout.q[c] = make_float2(xl[1], xl[2]);
-      if (cfl) cand = cfl_candidate_f32<NS>(m, c, dn.h, xh[1], xh[2], dn.dry, A);
+      if (cfl) cand = cfl_candidate_f32<NS>(m, sl, dn.h, xh[1], xh[2], dn.dry, A);
+      if (FUSED && !dn.dry) {
+        // inlet-Q conveyance of the output state (bc_2D.jl:673-676)
+#pragma unroll
+        for (int k = 0; k < NS; ++k) {
+          const int32_t nb = slot_nb(sl[k]);
+          if (nb >= 0 || nb == kNoFace) continue;
+          const int32_t bf = boundary_index(nb);
+          const int32_t info = m.bfInfo[bf];
+          if ((info & 3) != kBcInletQ) continue;
+          const int32_t g = info >> 2;
+#pragma unroll
+          for (int q = 0; q < kMaxFusedInlets; ++q)
+            if (q == g) contrib[q] += m.bfLp53[bf] * (double)dn.h / (double)cp.w;
+        }
+      }
     }
   }
-  if (cfl) block_min_publish_f(cand, s.cflMinF);
+  if (FUSED && f.record && blockIdx.x == 0 && threadIdx.x == 0) {
+    // step bookkeeping, and clear the CFL buffer stage 2 publishes into
+    const double dt = fused_dt(s, f);
+    const int k = *s.stepIdx;
+    if (k < s.dtCap) s.dtHist[k] = dt;
+    *s.stepIdx = k + 1;
+    *s.tSum += dt;
+    *s.dt = dt;
+    *s.dtf = (float)dt;
+    s.cflMin[1 - f.parity] = (unsigned long long)__double_as_longlong(INFINITY);
+    s.cflMinF[1 - f.parity] = __float_as_uint(INFINITY);
+  }
+  if (cfl) block_min_publish_f(cand, FUSED ? s.cflMinF + (1 - f.parity) : s.cflMinF);
+  if (FUSED && m.nInlet > 0) fused_inlet_totals(m, f, contrib);
 }
 
 template <int NS>
@@ -148,8 +220,10 @@ __global__ void __launch_bounds__(kBlock) k_cfl_f32(DevMesh m, DevScalars s, Sta
   float cand = INFINITY;
   if (c < m.n) {
     const float4 x = X.x[c];
+    float4 sl[NS];
+    load_slots<NS>(m, c, sl);
     const SideF32 L = make_side_f32(x, m.CP[c], m.hsmf, m.hsm);
-    cand = cfl_candidate_f32<NS>(m, c, L.s.h, x.z, x.w, L.s.dry, m.CS[c].z);
+    cand = cfl_candidate_f32<NS>(m, sl, L.s.h, x.z, x.w, L.s.dry, m.CS[c].z);
   }
   block_min_publish_f(cand, s.cflMinF);
 }
@@ -189,10 +263,16 @@ __global__ void k_step_begin(DevScalars s, int cflMode, double cfl) {
   *s.tSum += *s.dt;
 }
 
+__global__ void k_reset_cfl(DevScalars s, int p) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  s.cflMin[p] = (unsigned long long)__double_as_longlong(INFINITY);
+  s.cflMinF[p] = __float_as_uint(INFINITY);
+}
+
 __global__ void k_reset_scalars(DevScalars s) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  *s.cflMin = (unsigned long long)__double_as_longlong(INFINITY);
-  *s.cflMinF = __float_as_uint(INFINITY);
+  s.cflMin[0] = s.cflMin[1] = (unsigned long long)__double_as_longlong(INFINITY);
+  s.cflMinF[0] = s.cflMinF[1] = __float_as_uint(INFINITY);
   *s.stepIdx = 0;
   *s.tSum = 0.0;
   *s.flags = 0;
@@ -259,10 +339,20 @@ void launch_inlet_total_f32(const DevMesh& m, const DevScalars& s, StateF32 X, c
 void launch_stage_f32(const DevMesh& m, const DevScalars& s, int mode, StateF32 Xin, StateF32 Xbase, StateF32 Xout,
                       double* Rout, bool cfl, cudaStream_t st) {
   const int f = cfl ? 1 : 0;
-  if (m.nslot <= 3) k_stage_f32<3><<<blocks_for(m.n), kBlock, 0, st>>>(m, s, mode, Xin, Xbase, Xout, Rout, f);
-  else if (m.nslot <= 4) k_stage_f32<4><<<blocks_for(m.n), kBlock, 0, st>>>(m, s, mode, Xin, Xbase, Xout, Rout, f);
-  else k_stage_f32<8><<<blocks_for(m.n), kBlock, 0, st>>>(m, s, mode, Xin, Xbase, Xout, Rout, f);
+  const StageFuse nf{};
+  if (m.nslot <= 3) k_stage_f32<3, false><<<blocks_for(m.n), kBlock, 0, st>>>(m, s, mode, Xin, Xbase, Xout, Rout, f, nf);
+  else if (m.nslot <= 4) k_stage_f32<4, false><<<blocks_for(m.n), kBlock, 0, st>>>(m, s, mode, Xin, Xbase, Xout, Rout, f, nf);
+  else k_stage_f32<8, false><<<blocks_for(m.n), kBlock, 0, st>>>(m, s, mode, Xin, Xbase, Xout, Rout, f, nf);
 }
+void launch_stage_f32_fused(const DevMesh& m, const DevScalars& s, int mode, StateF32 Xin, StateF32 Xbase,
+                            StateF32 Xout, const StageFuse& fu, cudaStream_t st) {
+  const int f = (!fu.record && fu.cflMode) ? 1 : 0;   // stage 2 publishes the next CFL minimum
+  if (m.nslot <= 3) k_stage_f32<3, true><<<blocks_for(m.n), kBlock, 0, st>>>(m, s, mode, Xin, Xbase, Xout, nullptr, f, fu);
+  else if (m.nslot <= 4) k_stage_f32<4, true><<<blocks_for(m.n), kBlock, 0, st>>>(m, s, mode, Xin, Xbase, Xout, nullptr, f, fu);
+  else k_stage_f32<8, true><<<blocks_for(m.n), kBlock, 0, st>>>(m, s, mode, Xin, Xbase, Xout, nullptr, f, fu);
+}
+int stage_blocks_f32(const DevMesh& m) { return blocks_for(m.n); }
+void launch_reset_cfl(const DevScalars& s, int parity, cudaStream_t st) { k_reset_cfl<<<1, 32, 0, st>>>(s, parity); }
 void launch_cfl_f32(const DevMesh& m, const DevScalars& s, StateF32 X, cudaStream_t st) {
   if (m.nslot <= 3) k_cfl_f32<3><<<blocks_for(m.n), kBlock, 0, st>>>(m, s, X);
   else if (m.nslot <= 4) k_cfl_f32<4><<<blocks_for(m.n), kBlock, 0, st>>>(m, s, X);

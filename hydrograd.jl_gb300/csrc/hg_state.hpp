@@ -22,6 +22,7 @@ struct DevMesh {
   const float4* SL = nullptr;        // FP32 path: [nslot*n] {nx, ny, L, nb as bits} (see hg_f32.cuh)
   const int32_t* bfInfo = nullptr;   // [nbf] type | group << 2
   const double* bfLp23 = nullptr;    // [nbf] L^(2/3) (inlet-Q faces)
+  const double* bfLp53 = nullptr;    // [nbf] L^(5/3) (inlet-Q faces)
   const float* bfLp23f = nullptr;
   const int32_t* inletOff = nullptr; // [nInlet+1] CSR over inlet faces in NodeString order
   const int32_t* inletCell = nullptr;
@@ -49,8 +50,8 @@ struct DevMesh {
 struct DevScalars {
   double* dt = nullptr;                   // current step size
   float* dtf = nullptr;                   // the same, as float (FP32 path)
-  unsigned long long* cflMin = nullptr;   // min over cells of A / sum L(|u.n|+c), as ordered bits
-  unsigned int* cflMinF = nullptr;        // the same from the FP32 path
+  unsigned long long* cflMin = nullptr;   // [2] min over cells of A / sum L(|u.n|+c), as ordered bits
+  unsigned int* cflMinF = nullptr;        // [2] the same from the FP32 path (index 1: fused stepping only)
   double* dtHist = nullptr;               // [capacity] step sizes taken
   int32_t* stepIdx = nullptr;             // steps taken since the last reset
   double* tSum = nullptr;                 // sum of the steps taken
@@ -59,6 +60,29 @@ struct DevScalars {
 };
 
 enum StageMode : int32_t { kModeRhs = 0, kModeStage1 = 1, kModeStage2 = 2, kModeEulerRef = 3 };
+
+// Fused FP32 stepping: one RK2 step is two launches.
+//  * dt: in CFL mode every thread computes dt = cfl * min from the minimum the
+//    previous step published into cflMin[parity] / cflMinF[parity]; stage 2
+//    publishes into the other buffer, and stage 1 of a step clears it (block 0),
+//    which nobody reads during stage 1.  Stage 1's block 0 records the step.
+//  * inlet-Q conveyance totals of a stage's output state (read by the next
+//    stage's inlet ghosts): only the blocks holding inlet cells (blockSlot >= 0)
+//    take part; each writes its partial sums, and the last of them to finish
+//    (atomic ticket) adds them in slot order -- deterministic -- and resets the ticket.
+constexpr int kMaxFusedInlets = 4;
+struct StageFuse {
+  const double* totalIn = nullptr;   // conveyance totals of the input state (replaces DevMesh::totalA)
+  double* totalOut = nullptr;        // totals of the output state
+  double* partials = nullptr;        // [kMaxFusedInlets][nSlots]
+  unsigned int* ticket = nullptr;
+  const int32_t* blockSlot = nullptr;   // [blocks] slot of a block holding inlet cells, else -1
+  int32_t nSlots = 0;
+  int32_t record = 0;                // stage 1: block 0 records the step and clears the other CFL buffer
+  int32_t cflMode = 0;
+  int32_t parity = 0;
+  double cfl = 0.0;
+};
 
 // FP64 state: Q blocks [xi | qx | qy] of n doubles.
 void launch_inlet_total_f64(const DevMesh& m, const DevScalars& s, const double* Q, cudaStream_t st);
@@ -74,6 +98,14 @@ struct StateF32 {
 void launch_inlet_total_f32(const DevMesh& m, const DevScalars& s, StateF32 X, cudaStream_t st);
 void launch_stage_f32(const DevMesh& m, const DevScalars& s, int mode, StateF32 Xin, StateF32 Xbase, StateF32 Xout,
                       double* Rout, bool cfl, cudaStream_t st);
+// Stage with the fused work of StageFuse (requires nInlet <= kMaxFusedInlets).
+void launch_stage_f32_fused(const DevMesh& m, const DevScalars& s, int mode, StateF32 Xin, StateF32 Xbase,
+                            StateF32 Xout, const StageFuse& f, cudaStream_t st);
+// Blocks of an FP32 stage launch; block b holds cells [b * kStageBlockF32, (b + 1) * kStageBlockF32).
+constexpr int kStageBlockF32 = 256;
+int stage_blocks_f32(const DevMesh& m);
+// Clear CFL-minimum buffer `parity` (fused stepping keeps two).
+void launch_reset_cfl(const DevScalars& s, int parity, cudaStream_t st);
 void launch_cfl_f32(const DevMesh& m, const DevScalars& s, StateF32 X, cudaStream_t st);
 
 // Step bookkeeping: when cflMode, dt = cfl * min; records dt and resets the min.

@@ -215,19 +215,32 @@ def river_triangles(n=708, L=2000.0, seed=0, inlet_q=500.0, exit_wse=None, wstil
     xi = initial_xi(h, np.full(N, wstill), zb)
     case.update(mat_id=mat, manning_zones=zones_n, inlet_q=np.array([inlet_q]), exit_wse=np.array([exit_wse]),
                 wstill=np.full(N, wstill), Q0=np.concatenate([xi, np.zeros(N), np.zeros(N)]),
-                zb_cells=zb, name=f"river_tri_{n}x{n}x2" + ("_dry" if dry_land else ""))
+                zb_cells=zb, pool_center=tuple(pool_center), pool_radius=float(pool_radius),
+                name=f"river_tri_{n}x{n}x2" + ("_dry" if dry_land else ""))
     return case
 
 
-def probes_and_perturbation(case, n_probe=64, seed=1, zb_sigma=0.05):
-    """Seeded probe cells (wet at t = 0, so the loss sees the flow) and a
-    per-cell bed perturbation drawn in FP32 with standard deviation zb_sigma."""
+def probes_and_perturbation(case, n_probe=64, seed=1, zb_sigma=0.05, rim_width=None):
+    """Seeded probe cells and a per-cell bed perturbation drawn in FP32 with
+    standard deviation zb_sigma.  The probes are wet cells within rim_width
+    (default: 4 mean cell sizes) of the pool's rim, where the released bore
+    passes in the first steps, so that a short run's loss sees the flow."""
     rs = Stream(seed)
     N = len(case["cell_node_count"])
     Q0 = case["Q0"]
-    wet = np.nonzero(Q0[:N] + case["wstill"] - case["zb_cells"] > 2 * H_SMALL)[0]
-    pick = np.unique((rs.uniform(4 * n_probe) * len(wet)).astype(np.int64))[:n_probe]
-    probes = wet[np.sort(pick)].astype(np.int32)
+    wet = Q0[:N] + case["wstill"] - case["zb_cells"] > 2 * H_SMALL
+    cand = np.nonzero(wet)[0]
+    if "pool_center" in case:
+        cx, cy = cell_centroids(case)
+        xyz = case["node_xyz"]
+        cell = np.sqrt((np.ptp(xyz[:, 0]) * np.ptp(xyz[:, 1])) / N)
+        w = 4.0 * cell if rim_width is None else rim_width
+        r = np.hypot(cx - case["pool_center"][0], cy - case["pool_center"][1])
+        rim = np.nonzero(wet & (np.abs(r - case["pool_radius"]) < w))[0]
+        if len(rim) >= n_probe:
+            cand = rim
+    pick = np.unique((rs.uniform(4 * n_probe) * len(cand)).astype(np.int64))[:n_probe]
+    probes = cand[np.sort(pick)].astype(np.int32)
     # Box-Muller from two uniform draws, rounded to float32.
     u1 = np.maximum(rs.uniform(N), 1e-300)
     u2 = rs.uniform(N)

@@ -52,14 +52,19 @@ def observations(case, Q0, K, dt, probes, hidden_zones):
     return obs
 
 
-def setup_problem(case, K, nprobe=16, seed=3, near_inlet=False):
+def setup_problem(case, K, nprobe=16, seed=3, near_inlet=False, near_pool=False):
     N = len(case["cell_node_count"])
     Q0 = case["Q0"] if "Q0" in case else initial_state(case, N)
     ctx, o, _ = make_pair(case)
     dt = 0.5 * o.cfl_dt(Q0, 0.4)
-    if near_inlet:   # the cells closest to the west (inlet) edge
-        cx = o.mesh_arrays()["centroids"].reshape(N, 2)[:, 0]
-        probes = np.sort(np.argsort(cx)[:nprobe]).astype(np.int32)
+    cxy = o.mesh_arrays()["centroids"].reshape(N, 2)
+    if near_inlet and near_pool:   # half at the west (inlet) edge, half around the pool's rim
+        west = np.argsort(cxy[:, 0])[:nprobe // 2]
+        r = np.hypot(cxy[:, 0] - case["pool_center"][0], cxy[:, 1] - case["pool_center"][1])
+        rim = np.argsort(np.abs(r - case["pool_radius"]))[:nprobe - nprobe // 2]
+        probes = np.unique(np.concatenate([west, rim])).astype(np.int32)
+    elif near_inlet:   # the cells closest to the west (inlet) edge
+        probes = np.sort(np.argsort(cxy[:, 0])[:nprobe]).astype(np.int32)
     else:
         probes = np.unique((Stream(seed).uniform(4 * nprobe) * N).astype(np.int32))[:nprobe]
     hidden = case["manning_zones"] * (1.0 + 0.2 * np.sin(np.arange(len(case["manning_zones"])) + 1.0))
@@ -149,7 +154,7 @@ def test_fp32c_adjoint_error_vs_fp64():
     (normwise) of the FP64 adjoint, itself checked against the oracle above."""
     case = river()
     K = 40
-    ctx, o, N, Q0, dt, probes, obs = setup_problem(case, K)
+    ctx, o, N, Q0, dt, probes, obs = setup_problem(case, K, near_inlet=True, near_pool=True)
     c32 = SWE2D(case, precision="fp32c")
     c32.set_still_water(case["wstill"])
     c32.set_manning_zones(case["mat_id"], case["manning_zones"])
@@ -164,6 +169,7 @@ def test_fp32c_adjoint_error_vs_fp64():
     g_zone = np.array([r32["g_manning"][case["mat_id"] == z].sum() for z in range(nz)])
     assert rel(g_zone, dl_n).max() <= 1e-5
     assert abs(r32["g_inletq"][0] - dl_q[0]) <= 1e-5 * abs(dl_q[0])
+    assert np.abs(r64["g_zb"]).max() > 1e-8 * np.abs(r64["g_manning"]).max()   # the probes see the bed
     assert np.abs(r32["g_zb"] - r64["g_zb"]).max() <= 1e-4 * np.abs(r64["g_zb"]).max()
     # state after the run
     for b in range(3):

@@ -169,17 +169,19 @@ def test_active_parameter_injection_matches_oracle():
     assert rhs_err(out, o2.rhs(Q), o2, Q) <= 1e-12
 
 
-def test_runs_are_bitwise_deterministic():
+@pytest.mark.parametrize("precision", ["fp64", "fp32c"])
+def test_runs_are_bitwise_deterministic(precision):
     case = small_river(24, 400.0)
-    ctx, _, _ = setup_pair(case)
+    ctx, _, _ = setup_pair(case, precision=precision)
     a, _ = ctx.integrate(case["Q0"], 100, cfl=0.4)
     b, _ = ctx.integrate(case["Q0"], 100, cfl=0.4)
     assert np.array_equal(a, b)
 
 
-def test_device_resident_graph_path_equals_integrate():
+@pytest.mark.parametrize("precision", ["fp64", "fp32c"])
+def test_device_resident_graph_path_equals_integrate(precision):
     case = small_river(24, 400.0)
-    ctx, _, _ = setup_pair(case)
+    ctx, _, _ = setup_pair(case, precision=precision)
     a, dts = ctx.integrate(case["Q0"], 120, cfl=0.4)
     ctx.upload(case["Q0"])
     ctx.advance(120, cfl=0.4, graph=True)
