@@ -375,14 +375,31 @@ def main():
     ap.add_argument("--ref-steps", type=int, default=20)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--adj-steps", type=int, default=100, help="steps of the forward+adjoint measurement (0: skip)")
+    ap.add_argument("--profile-stage", default=None, choices=["fp32c", "fp64"],
+                    help="only run the stage kernel a few times (a small case for ncu captures)")
     args = ap.parse_args()
     if args.steps_fp64 is None:
         args.steps_fp64 = args.steps
     args.warmup = max(args.warmup, 3)
-    if args.impl == "reference":
+    if args.profile_stage:
+        profile_stage(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)
+
+
+def profile_stage(args):
+    """Workload state after `warmup` CFL steps, then 3 stage-kernel launches
+    (each after an L2 flush): launches 1-2 of k_stage_* are warm-up, 3 is the one to capture."""
+    from hydrograd_gb.workloads import river_triangles
+    case = river_triangles(n=args.n)
+    ctx = make_ctx(case, args.profile_stage, 0)
+    ctx.upload(case["Q0"])
+    ctx.advance(args.warmup, cfl=0.4, graph=False)
+    ctx.synchronize()
+    ms = ctx.time_stage_kernel(3, True)
+    print(json.dumps({"precision": args.profile_stage, "cells": len(case["cell_node_count"]), "stage_ms": ms}))
 
 
 if __name__ == "__main__":

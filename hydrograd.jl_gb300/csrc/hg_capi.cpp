@@ -664,13 +664,30 @@ int hg_time_stage_kernel(hg_ctx* ctx, int32_t n, int32_t flush_l2, double* avg_m
   HG_CUDA(ctx, cudaEventCreate(&a));
   HG_CUDA(ctx, cudaEventCreate(&b));
   double total = 0.0;
+  if (fused(ctx)) {   // conveyance totals of the resident state
+    DevMesh m = ctx->dm;
+    m.totalA = ctx->d_tot;
+    launch_inlet_total_f32(m, ctx->ds, xa(ctx), ctx->stream);
+    ctx->launches += ctx->dm.nInlet > 0 ? 1 : 0;
+  }
   for (int i = 0; i < n; ++i) {
     if (flush_l2) launch_flush(ctx->flushBuf, ctx->flushBytes, ctx->stream);
     cudaEventRecord(a, ctx->stream);
-    if (ctx->precision == HG_FP64)
+    if (ctx->precision == HG_FP64) {
       launch_stage_f64(ctx->dm, ctx->ds, kModeStage1, ctx->QA, nullptr, ctx->QB, false, ctx->stream);
-    else
+    } else if (fused(ctx)) {
+      // the stage-1 launch of a fused step at the current dt, without the step bookkeeping
+      StageFuse f;
+      f.partials = ctx->d_partials;
+      f.ticket = ctx->d_ticket;
+      f.blockSlot = ctx->d_blockSlot;
+      f.nSlots = ctx->nSlots;
+      f.totalIn = ctx->d_tot;
+      f.totalOut = ctx->d_tot + kMaxFusedInlets;
+      launch_stage_f32_fused(ctx->dm, ctx->ds, kModeStage1, xa(ctx), StateF32{}, xb(ctx), f, ctx->stream);
+    } else {
       launch_stage_f32(ctx->dm, ctx->ds, kModeStage1, xa(ctx), StateF32{}, xb(ctx), nullptr, false, ctx->stream);
+    }
     cudaEventRecord(b, ctx->stream);
     cudaEventSynchronize(b);
     float ms = 0.f;
