@@ -52,6 +52,8 @@ def build(verbose=False):
         fmad = ["--fmad=false"] if src in NO_FMAD else []
         if src in FAST_MATH and os.environ.get("HG_FAST_MATH", "1") == "1":
             fmad = ["--use_fast_math"]
+        if src == "hg_forward_f32.cu" and os.environ.get("HG_STAGE_MIN_BLOCKS"):
+            fmad = fmad + ["-DHG_STAGE_MIN_BLOCKS=%d" % int(os.environ["HG_STAGE_MIN_BLOCKS"])]
         jobs.append([nvcc, "-std=c++17", "-O3", *ARCH, *fmad, "-lineinfo", "-Xcompiler", "-fPIC", "-I", INCLUDE,
                      "-c", os.path.join(CSRC, src), "-o", obj])
     for src in CXX_SOURCES:

@@ -82,17 +82,27 @@ __device__ __forceinline__ void load_slots(const DevMesh& m, int c, float4 (&sl)
   for (int k = 0; k < NS; ++k) sl[k] = __ldg(&m.SL[(size_t)k * m.n + c]);
 }
 
-// Inlet-Q conveyance totals of a fused stage's output state: the blocks that
-// hold inlet cells write partial sums; the last of them adds the partials in
-// slot order.
-__device__ __forceinline__ void fused_inlet_totals(const DevMesh& m, const StageFuse& f,
-                                                   const double (&contrib)[kMaxFusedInlets]) {
+// Inlet-Q conveyance totals of a fused stage's output state (bc_2D.jl:673-676):
+// the blocks that hold inlet cells write partial sums; the last of them adds
+// the partials in slot order.  Only those few blocks reload the slot records,
+// so the other blocks carry no extra registers for it.
+template <int NS>
+__device__ __forceinline__ void fused_inlet_totals(const DevMesh& m, const StageFuse& f, int c, float hOut, bool wetOut) {
   const int slot = f.blockSlot[blockIdx.x];
   if (slot < 0) return;   // uniform over the block
   __shared__ int isLast;
   const int ng = m.nInlet;
   for (int g = 0; g < ng; ++g) {
-    const double t = block_sum(contrib[g]);
+    double contrib = 0.0;
+    if (wetOut) {
+      for (int k = 0; k < NS; ++k) {
+        const int32_t nb = slot_nb(m.SL[(size_t)k * m.n + c]);
+        if (nb >= 0 || nb == kNoFace) continue;
+        const int32_t bf = boundary_index(nb);
+        if (m.bfInfo[bf] == (kBcInletQ | (g << 2))) contrib += m.bfLp53[bf] * (double)hOut / (double)m.CP[c].w;
+      }
+    }
+    const double t = block_sum(contrib);
     if (threadIdx.x == 0) f.partials[(size_t)g * f.nSlots + slot] = t;
   }
   if (threadIdx.x == 0) {
@@ -120,13 +130,24 @@ __device__ __forceinline__ double fused_dt(const DevScalars& s, const StageFuse&
   return f.cfl * mn;
 }
 
+// The stage kernel is latency-bound (neighbour gathers): for meshes of degree
+// <= 4 it is held to the register budget of HG_STAGE_MIN_BLOCKS resident
+// blocks per SM (4: 64 registers, no spills; 50% occupancy).
+#ifndef HG_STAGE_MIN_BLOCKS
+#define HG_STAGE_MIN_BLOCKS 4
+#endif
+template <int NS>
+constexpr int stage_min_blocks() { return NS <= 4 ? HG_STAGE_MIN_BLOCKS : 1; }
+
 template <int NS, bool FUSED>
-__global__ void __launch_bounds__(kBlock) k_stage_f32(DevMesh m, DevScalars s, int mode, StateF32 Xin, StateF32 Xbase,
-                                                      StateF32 Xout, double* Rout, int cfl, StageFuse f) {
+__global__ void __launch_bounds__(kBlock, stage_min_blocks<NS>())
+    k_stage_f32(DevMesh m, DevScalars s, int mode, StateF32 Xin, StateF32 Xbase, StateF32 Xout, double* Rout, int cfl,
+                StageFuse f) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   const bool active = c < m.n;
   float cand = INFINITY;
-  double contrib[kMaxFusedInlets] = {0.0, 0.0, 0.0, 0.0};
+  float hOut = 0.0f;      // output depth, and whether the output cell is wet (fused inlet totals)
+  bool wetOut = false;
   if (active) {
     float4 sl[NS];
     load_slots<NS>(m, c, sl);
@@ -181,21 +202,8 @@ __global__ void __launch_bounds__(kBlock) k_stage_f32(DevMesh m, DevScalars s, i
       Xout.x[c] = make_float4(xh[0], xl[0], xh[1], xh[2]);
       Xout.q[c] = make_float2(xl[1], xl[2]);
       if (cfl) cand = cfl_candidate_f32<NS>(m, sl, dn.h, xh[1], xh[2], dn.dry, A);
-      if (FUSED && !dn.dry) {
-        // inlet-Q conveyance of the output state (bc_2D.jl:673-676)
-#pragma unroll
-        for (int k = 0; k < NS; ++k) {
-          const int32_t nb = slot_nb(sl[k]);
-          if (nb >= 0 || nb == kNoFace) continue;
-          const int32_t bf = boundary_index(nb);
-          const int32_t info = m.bfInfo[bf];
-          if ((info & 3) != kBcInletQ) continue;
-          const int32_t g = info >> 2;
-#pragma unroll
-          for (int q = 0; q < kMaxFusedInlets; ++q)
-            if (q == g) contrib[q] += m.bfLp53[bf] * (double)dn.h / (double)cp.w;
-        }
-      }
+      hOut = dn.h;
+      wetOut = !dn.dry;
     }
   }
   if (FUSED && f.record && blockIdx.x == 0 && threadIdx.x == 0) {
@@ -211,7 +219,7 @@ __global__ void __launch_bounds__(kBlock) k_stage_f32(DevMesh m, DevScalars s, i
     s.cflMinF[1 - f.parity] = __float_as_uint(INFINITY);
   }
   if (cfl) block_min_publish_f(cand, FUSED ? s.cflMinF + (1 - f.parity) : s.cflMinF);
-  if (FUSED && m.nInlet > 0) fused_inlet_totals(m, f, contrib);
+  if (FUSED && m.nInlet > 0) fused_inlet_totals<NS>(m, f, c, hOut, wetOut);
 }
 
 template <int NS>
