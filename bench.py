@@ -229,7 +229,7 @@ def run_ours(args):
         ms = ctx.advance_timed(steps, cfl=0.4, flush_l2=True)
         if sampler:
             sampler.__exit__()
-        launches = ctx.launch_count() - l0 - steps   # minus the L2 flushes
+        launches = ctx.launch_count() - l0 - 2 * steps   # minus the L2 flushes (write + read kernel)
         ms = max_over_ranks(dist, ms)
         barrier(dist)
         out[prec] = dict(ms=ms, steps=steps, value=ws * N * steps / (ms * 1e-3), launches=launches,
@@ -342,7 +342,8 @@ def run_ours(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 (hi+lo compensated state)", "data": "synthetic",
         "config": {"workload": f"{case['name']}: {N} jittered triangles, 2 km reach, SSP-RK2 CFL 0.4, "
                                f"{f32['steps']} steps", "cells": N, "faces": ctxs["fp32c"].n_faces,
-                   "l2": "flushed before every timed step (256 MB write, outside the timed events)",
+                   "l2": "flushed before every timed step: 256 MB written, then a different 256 MB read "
+                         "(L2 left with clean lines only), outside the timed events",
                    "order": "hilbert", "parallelism": "replicas" if ws > 1 else "single GPU"},
         "fp64": {"value": out["fp64"]["value"], "ms_per_step": out["fp64"]["ms"] / out["fp64"]["steps"],
                  "steps": out["fp64"]["steps"], "stage_ms": out["fp64"]["stage_ms"],

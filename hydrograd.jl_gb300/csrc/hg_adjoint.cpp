@@ -80,6 +80,7 @@ int setup(hg_ctx* c) {
   ADJ_CUDA(c, falloc(b, &a.gS0x, N));
   ADJ_CUDA(c, falloc(b, &a.gS0y, N));
   ADJ_CUDA(c, falloc(b, &a.gZb, N));
+  if (c->precision == HG_FP32C) ADJ_CUDA(c, falloc(b, &a.accF, (size_t)4 * N));
   ADJ_CUDA(c, falloc(b, &a.bfGradQ, c->dm.nbf));
   ADJ_CUDA(c, falloc(b, &a.bfGradTA, c->dm.nbf));
   ADJ_CUDA(c, falloc(b, &a.gQ, c->dm.nInlet));
@@ -204,6 +205,7 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
   ADJ_CUDA(c, cudaMemsetAsync(a.gS0x, 0, N * sizeof(double), st));
   ADJ_CUDA(c, cudaMemsetAsync(a.gS0y, 0, N * sizeof(double), st));
   ADJ_CUDA(c, cudaMemsetAsync(a.gZb, 0, N * sizeof(double), st));
+  if (a.accF) ADJ_CUDA(c, cudaMemsetAsync(a.accF, 0, (size_t)4 * N * sizeof(float2), st));
   ADJ_CUDA(c, cudaMemsetAsync(a.gQ, 0, std::max(c->dm.nInlet, 1) * sizeof(double), st));
   ADJ_CUDA(c, cudaMemsetAsync(a.loss, 0, sizeof(double), st));
   ADJ_CUDA(c, cudaMemsetAsync(c->ds.flags, 0, sizeof(int32_t), st));
@@ -318,6 +320,10 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
         c->launches += 2 + 2 * extraPerStep + (s >= 1 && P > 0 ? 1 : 0);
       }
     }
+  }
+  if (a.accF) {
+    launch_fold_accumulators_f32(dm, a, st);
+    c->launches += 1;
   }
   launch_zb_gradient(dm, a, b->gzb, st);
   c->launches += 1;

@@ -2,8 +2,9 @@
 //
 // Same gather-form VJP as hg_adjoint_f64.cu (see there for the formulas), on
 // the packed FP32 records (hg_f32.cuh), with the FP32 path's own wet/dry
-// decisions (FP64-exact near h_small) so that every branch is the forward
-// pass's.  Cotangents are FP32; parameter gradients accumulate in FP64.
+// decisions (depth_f32) so that every branch is the forward pass's.  Cotangents are FP32; per-cell parameter gradients accumulate as
+// compensated FP32 pairs (GB300's FP64 rate is a small fraction of its FP32
+// rate) and are folded into FP64 once, after the reverse sweep.
 // Compiled with the same fast-math options as the FP32 forward kernels.
 #include <cfloat>
 #include <cmath>
@@ -48,6 +49,19 @@ __device__ __forceinline__ Side<D> constant(const Side<float>& s) {
   return r;
 }
 
+// acc += b * g with the product exact (fma residual) and the sum compensated:
+// FP32 instructions only, about 2^-44 relative over thousands of terms.
+__device__ __forceinline__ void acc_add(float2* p, float b, float g) {
+  const float prod = b * g;
+  const float perr = fmaf(b, g, -prod);
+  float2 a = *p;
+  float s, e;
+  two_sum(a.x, prod, s, e);
+  e += a.y + perr;
+  fast_two_sum(s, e, a.x, a.y);
+  *p = a;
+}
+
 template <int NS>
 __global__ void __launch_bounds__(kBlock) k_vjp_f32(DevMesh m, AdjDev a, StateF32 Q, const float* __restrict__ mu,
                                                     const float* __restrict__ extra, float* out, float cSelf,
@@ -57,7 +71,7 @@ __global__ void __launch_bounds__(kBlock) k_vjp_f32(DevMesh m, AdjDev a, StateF3
   const int n = m.n;
   const float4 cp = __ldg(&m.CP[j]);
   const float4 cs = __ldg(&m.CS[j]);
-  const SideF32 L = make_side_f32(__ldg(&Q.x[j]), cp, m.hsmf, m.hsm);
+  const SideF32 L = make_side_f32(__ldg(&Q.x[j]), cp, m.hsmf, m.hsmLo);
   const float Aj = cs.z;
   const float mj0 = mu[j], mj1 = mu[n + j], mj2 = mu[2 * n + j];
   float g0 = 0.0f, g1 = 0.0f, g2 = 0.0f, gn = 0.0f, gzb = 0.0f;
@@ -69,7 +83,7 @@ __global__ void __launch_bounds__(kBlock) k_vjp_f32(DevMesh m, AdjDev a, StateF3
     if (nb == kNoFace) continue;
     const float nx = sl.x, ny = sl.y, len = sl.z;
     if (nb >= 0) {
-      const SideF32 R = make_side_f32(__ldg(&Q.x[nb]), __ldg(&m.CP[nb]), m.hsmf, m.hsm);
+      const SideF32 R = make_side_f32(__ldg(&Q.x[nb]), __ldg(&m.CP[nb]), m.hsmf, m.hsmLo);
       const float An = __ldg(&m.CS[nb]).z;
       const float w0 = len * (mu[nb] / An - mj0 / Aj);
       const float w1 = len * (mu[n + nb] / An - mj1 / Aj);
@@ -119,11 +133,11 @@ __global__ void __launch_bounds__(kBlock) k_vjp_f32(DevMesh m, AdjDev a, StateF3
     g1 += mj1 * (-k - hu * dkdqx) + mj2 * (-hv * dkdqx);
     g2 += mj1 * (-hu * dkdqy) + mj2 * (-k - hv * dkdqy);
     gn += -(mj1 * hu + mj2 * hv) * dkdn;
-    a.gS0x[j] += (double)beta * (double)(mj1 * m.gf * L.s.xi);
-    a.gS0y[j] += (double)beta * (double)(mj2 * m.gf * L.s.xi);
+    acc_add(&a.accF[(size_t)n + j], beta, mj1 * m.gf * L.s.xi);
+    acc_add(&a.accF[(size_t)2 * n + j], beta, mj2 * m.gf * L.s.xi);
   }
-  a.gN[j] += (double)beta * (double)gn;
-  a.gZb[j] += (double)beta * (double)gzb;
+  if (gn != 0.0f) acc_add(&a.accF[j], beta, gn);
+  if (gzb != 0.0f) acc_add(&a.accF[(size_t)3 * n + j], beta, gzb);   // exit-H cells only
   const float mask = L.s.dry ? 0.0f : 1.0f;
   const float e0 = extra ? extra[j] : 0.0f, e1 = extra ? extra[n + j] : 0.0f, e2 = extra ? extra[2 * n + j] : 0.0f;
   out[j] = mask * (cSelf * mj0 + cExtra * e0 + beta * g0);
@@ -151,7 +165,7 @@ __global__ void __launch_bounds__(256) k_inlet_adjoint_f32(DevMesh m, AdjDev a, 
   for (int i = u0 + threadIdx.x; i < u1; i += blockDim.x) {
     const int c = a.inletUCell[i];
     const float4 cp = m.CP[c];
-    const SideF32 L = make_side_f32(Q.x[c], cp, m.hsmf, m.hsm);
+    const SideF32 L = make_side_f32(Q.x[c], cp, m.hsmf, m.hsmLo);
     if (L.s.dry) continue;
     const double coef = a.inletUCoef[i], n = cp.w;
     out[c] += (float)(beta * gTA * coef / n);
@@ -183,9 +197,20 @@ __global__ void k_probe_adjoint_f32(DevMesh m, StateF32 Q, float* mu, const int3
   for (int p = 0; p < np; ++p) {
     const int c = probes[p];
     const float4 cp = m.CP[c];
-    const SideF32 L = make_side_f32(Q.x[c], cp, m.hsmf, m.hsm);
+    const SideF32 L = make_side_f32(Q.x[c], cp, m.hsmf, m.hsmLo);
     if (L.s.dry) continue;
     mu[c] += (float)(scale * 2.0 * (depth_f64(m, Q, c) - obs[p]));
+  }
+}
+
+__global__ void k_fold_accumulators_f32(DevMesh m, AdjDev a) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= m.n) return;
+  double* dst[4] = {a.gN, a.gS0x, a.gS0y, a.gZb};
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const float2 v = a.accF[(size_t)k * m.n + j];
+    dst[k][j] += (double)v.x + (double)v.y;
   }
 }
 
@@ -208,6 +233,9 @@ void launch_probe_loss_f32(const DevMesh& m, const AdjDev& a, StateF32 Q, const 
 void launch_probe_adjoint_f32(const DevMesh& m, StateF32 Q, float* mu, const int32_t* probes, const double* obs,
                               int32_t nprobe, double scale, cudaStream_t st) {
   if (nprobe > 0) k_probe_adjoint_f32<<<1, 32, 0, st>>>(m, Q, mu, probes, obs, nprobe, scale);
+}
+void launch_fold_accumulators_f32(const DevMesh& m, const AdjDev& a, cudaStream_t st) {
+  k_fold_accumulators_f32<<<blocks_for(m.n), kBlock, 0, st>>>(m, a);
 }
 
 }  // namespace hg

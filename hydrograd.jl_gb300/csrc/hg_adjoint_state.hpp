@@ -22,6 +22,9 @@ struct AdjDev {
   const int32_t* inletUCell = nullptr;
   const double* inletUCoef = nullptr;  // sum over the cell's faces in the group of L^(5/3)
   double* loss = nullptr;              // [1] sum over steps and probes of (h - obs)^2
+  // FP32-compensated path: per-cell sums of gN, gS0x, gS0y, gZb ([4][n]) as
+  // unevaluated float pairs {hi, lo}, folded into the FP64 arrays at the end.
+  float2* accF = nullptr;
 };
 
 // out_j = M(Q_j) (cSelf mu_j + cExtra extra_j + beta (J(Q)^T mu)_j), parameter
@@ -45,6 +48,8 @@ void launch_probe_loss_f32(const DevMesh& m, const AdjDev& a, StateF32 Q, const 
                            int32_t nprobe, cudaStream_t st);
 void launch_probe_adjoint_f32(const DevMesh& m, StateF32 Q, float* mu, const int32_t* probes, const double* obs,
                               int32_t nprobe, double scale, cudaStream_t st);
+// gN, gS0x, gS0y, gZb += the FP32 pair accumulators (accF).
+void launch_fold_accumulators_f32(const DevMesh& m, const AdjDev& a, cudaStream_t st);
 // dL/dzb = S0 transpose (Green-Gauss of face averages) applied to dL/dS0, plus the direct term.
 void launch_zb_gradient(const DevMesh& m, const AdjDev& a, double* gzb, cudaStream_t st);
 

@@ -619,8 +619,7 @@ int hg_launch_count(const hg_ctx* ctx, int64_t* count) {
 int hg_flush_l2(hg_ctx* ctx) {
   if (!ctx) return fail(ctx, HG_ERR_ARG, "hg_flush_l2: null context");
   cudaSetDevice(ctx->device);
-  launch_flush(ctx->flushBuf, ctx->flushBytes, ctx->stream);
-  ctx->launches += 1;
+  ctx->launches += launch_flush(ctx->flushBuf, ctx->flushBytes, ctx->stream);
   HG_CUDA(ctx, cudaGetLastError());
   return HG_OK;
 }
@@ -635,10 +634,7 @@ int hg_advance_timed(hg_ctx* ctx, int32_t nsteps, double dt, double cfl, int32_t
   std::vector<cudaEvent_t> ev(2 * (size_t)nsteps, nullptr);
   for (auto& e : ev) HG_CUDA(ctx, cudaEventCreate(&e));
   for (int s = 0; s < nsteps; ++s) {
-    if (flush_l2) {
-      launch_flush(ctx->flushBuf, ctx->flushBytes, ctx->stream);
-      ctx->launches += 1;
-    }
+    if (flush_l2) ctx->launches += launch_flush(ctx->flushBuf, ctx->flushBytes, ctx->stream);
     cudaEventRecord(ev[2 * s], ctx->stream);
     enqueue_rk2_step(ctx, cflMode, cfl);
     cudaEventRecord(ev[2 * s + 1], ctx->stream);
@@ -671,7 +667,7 @@ int hg_time_stage_kernel(hg_ctx* ctx, int32_t n, int32_t flush_l2, double* avg_m
     ctx->launches += ctx->dm.nInlet > 0 ? 1 : 0;
   }
   for (int i = 0; i < n; ++i) {
-    if (flush_l2) launch_flush(ctx->flushBuf, ctx->flushBytes, ctx->stream);
+    if (flush_l2) ctx->launches += launch_flush(ctx->flushBuf, ctx->flushBytes, ctx->stream);
     cudaEventRecord(a, ctx->stream);
     if (ctx->precision == HG_FP64) {
       launch_stage_f64(ctx->dm, ctx->ds, kModeStage1, ctx->QA, nullptr, ctx->QB, false, ctx->stream);
@@ -693,7 +689,7 @@ int hg_time_stage_kernel(hg_ctx* ctx, int32_t n, int32_t flush_l2, double* avg_m
     float ms = 0.f;
     cudaEventElapsedTime(&ms, a, b);
     total += ms;
-    ctx->launches += flush_l2 ? 2 : 1;
+    ctx->launches += 1;
   }
   cudaEventDestroy(a);
   cudaEventDestroy(b);
@@ -852,8 +848,8 @@ int ctx_setup_device(hg_ctx* c) {
     int rc = ensure_dt_capacity(c, 1024);
     if (rc) return rc;
   }
-  // L2 flush buffer (larger than the 126 MB L2).
-  c->flushBytes = (size_t)256 << 20;
+  // L2 flush buffer: 256 MB written, then a different 256 MB read (each larger than the 126 MB L2).
+  c->flushBytes = (size_t)512 << 20;
   HG_CUDA(c, dalloc(c, reinterpret_cast<char**>(&c->flushBuf), c->flushBytes));
 
   // FP32 slot records {nx, ny, L, nb as bits}
@@ -902,6 +898,7 @@ int ctx_setup_device(hg_ctx* c) {
   dm.exitWse = c->d_exitWse; dm.inletQ = c->d_inletQ; dm.totalA = c->d_totalA;
   dm.g = c->k.g; dm.kn2 = c->k.k_n * c->k.k_n; dm.hsm = c->k.h_small;
   dm.gf = (float)c->k.g; dm.kn2f = (float)(c->k.k_n * c->k.k_n); dm.hsmf = (float)c->k.h_small;
+  dm.hsmLo = (float)(c->k.h_small - (double)dm.hsmf);
   c->slotNb = d_nb;
   int rc = upload_cells(c);
   if (rc) return rc;

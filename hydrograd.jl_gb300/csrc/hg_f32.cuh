@@ -15,33 +15,40 @@
 
 namespace hgd {
 
-// Depth h = xi + hstill with the reference's dry decision h <= h_small taken
-// as the FP64 reference takes it: from an FP32 estimate when that estimate is
-// farther from h_small than its error bound, else from an FP64 sum, with a
-// tolerance of 2^-46 relative -- the granularity at which the hi + lo pair
-// stores a clamped cell's xi.
 struct DepthF32 {
   float h;        // clamped depth
   float excess;   // (h_clamped - hstill) - xi: 0 when wet, the clamp shift when dry
   bool dry;
 };
 
-__device__ __forceinline__ DepthF32 depth_f32(float xh, float xl, float hh, float hl, float hsmf, double hsm) {
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+
+// Depth h = xi + hstill with the reference's dry decision h <= h_small, from
+// the hi + lo pairs of xi and hstill and h_small = hsmf + hsmLo, in FP32
+// only (GB300 issues FP64 at a small fraction of the FP32 rate):
+// xh + hh - hsmf is formed exactly by two error-free sums, the lo terms are
+// added to it, and the decision takes a tolerance of 2^-46 |xh| + |hh| -- the
+// granularity at which the pairs store a clamped cell's xi (dry_xi), so a
+// clamped cell stays dry.  The arithmetic error of the difference is below
+// 2^-47 of that magnitude, so the decision is the exact one outside the
+// tolerance band.
+__device__ __forceinline__ DepthF32 depth_f32(float xh, float xl, float hh, float hl, float hsmf, float hsmLo) {
   DepthF32 d;
-  const float est = (xh + hh) + (xl + hl);
+  float s, e;
+  two_sum(xh, hh, s, e);                 // s + e = xh + hh exactly
+  const float low = (e + xl) + hl;
+  const float est = s + low;             // depth estimate
+  float t, te;
+  two_sum(s, -hsmf, t, te);              // t + te = s - hsmf exactly
+  const float diff = t + ((te + low) - hsmLo);
   const float mag = fabsf(xh) + fabsf(hh);
-  const float bound = 4.0e-7f * mag + 1.0e-30f;
-  if (fabsf(est - hsmf) > bound + 1.0e-10f) {
-    d.dry = est <= hsmf;
-    d.h = est;
-  } else {
-    const double hd = ((double)xh + (double)xl) + ((double)hh + (double)hl);
-    const double tol = 1.4210854715202004e-14 * (double)mag;   // 2^-46 * magnitude
-    d.dry = hd <= hsm + tol;
-    d.h = (float)hd;
-  }
+  d.dry = diff <= 1.4210854715202004e-14f * mag;
   d.excess = d.dry ? (hsmf - est) : 0.0f;
-  if (d.dry) d.h = hsmf;
+  d.h = d.dry ? hsmf : est;
   return d;
 }
 
@@ -51,9 +58,9 @@ struct SideF32 {
   float excess;   // see DepthF32
 };
 
-__device__ __forceinline__ SideF32 make_side_f32(float4 x, float4 p, float hsmf, double hsm) {
+__device__ __forceinline__ SideF32 make_side_f32(float4 x, float4 p, float hsmf, float hsmLo) {
   SideF32 r;
-  const DepthF32 d = depth_f32(x.x, x.y, p.x, p.y, hsmf, hsm);
+  const DepthF32 d = depth_f32(x.x, x.y, p.x, p.y, hsmf, hsmLo);
   r.s.xi = x.x;
   r.xlo = x.y;
   r.s.hst = p.x;
@@ -66,11 +73,6 @@ __device__ __forceinline__ SideF32 make_side_f32(float4 x, float4 p, float hsmf,
   return r;
 }
 
-__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
-  s = a + b;
-  const float bb = s - a;
-  e = (a - (s - bb)) + (b - bb);
-}
 __device__ __forceinline__ void fast_two_sum(float a, float b, float& s, float& e) {
   s = a + b;
   e = b - (s - a);

@@ -39,6 +39,7 @@ struct DevMesh {
   const float4* CP = nullptr;
   const float4* CS = nullptr;
   float hsmf = 1e-3f, gf = 9.81f, kn2f = 1.0f;
+  float hsmLo = 0.0f;                // h_small - hsmf, so that hsmf + hsmLo is h_small to 2^-48
   // Boundary values
   const double* exitWse = nullptr;   // [nExit]
   const double* inletQ = nullptr;    // [nInlet]
@@ -62,8 +63,9 @@ struct DevScalars {
 enum StageMode : int32_t { kModeRhs = 0, kModeStage1 = 1, kModeStage2 = 2, kModeEulerRef = 3 };
 
 // Fused FP32 stepping: one RK2 step is two launches.
-//  * dt: in CFL mode every thread computes dt = cfl * min from the minimum the
-//    previous step published into cflMin[parity] / cflMinF[parity]; stage 2
+//  * dt: in CFL mode thread 0 of every block forms dt = cfl * min from the
+//    minimum the previous step published into cflMin[parity] / cflMinF[parity]
+//    and shares it through shared memory; stage 2
 //    publishes into the other buffer, and stage 1 of a step clears it (block 0),
 //    which nobody reads during stage 1.  Stage 1's block 0 records the step.
 //  * inlet-Q conveyance totals of a stage's output state (read by the next
@@ -117,6 +119,7 @@ void launch_gather_state_f64(int32_t n, const int32_t* perm, const double* user,
 void launch_scatter_state_f64(int32_t n, const int32_t* perm, const double* dev, double* user, cudaStream_t st);
 void launch_gather_state_f32(int32_t n, const int32_t* perm, const double* user, StateF32 dev, cudaStream_t st);
 void launch_scatter_state_f32(int32_t n, const int32_t* perm, StateF32 dev, double* user, cudaStream_t st);
-void launch_flush(void* buf, size_t bytes, cudaStream_t st);
+// L2 flush over a buffer of `bytes` (> 2x L2): returns the launches made.
+int launch_flush(void* buf, size_t bytes, cudaStream_t st);
 
 }  // namespace hg
