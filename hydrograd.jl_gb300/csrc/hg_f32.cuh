@@ -94,4 +94,58 @@ __device__ __forceinline__ void df_add2(float ah, float al, float bh, float bl, 
 
 __device__ __forceinline__ int32_t slot_nb(float4 s) { return __float_as_int(s.w); }
 
+// Quantities of a wet cell that the Roe flux uses on every one of its faces,
+// formed once per cell: velocity, sqrt(h), pre-balanced pressure and the
+// physical flux tensor [[hu u + p, hu v], [hv u, hv v + p]].
+struct OwnF32 {
+  float u, v, s, p;
+  float fxx, fxy, fyx, fyy;
+};
+
+__device__ __forceinline__ OwnF32 own_f32(const Side<float>& L, float g) {
+  OwnF32 o;
+  const float r = 1.0f / L.h;
+  o.u = L.hu * r;
+  o.v = L.hv * r;
+  o.s = smooth_sqrt(L.h);
+  o.p = 0.5f * g * (smooth_pow2(L.xi) + 2.0f * L.xi * L.hst);
+  o.fxx = L.hu * o.u + o.p;
+  o.fxy = L.hu * o.v;
+  o.fyx = L.hv * o.u;
+  o.fyy = L.hv * o.v + o.p;
+  return o;
+}
+
+// Roe flux of a face whose two sides are both wet -- the case in which the
+// reference solver (swe_2D_solvers.jl:79-164) takes none of its dry or wall
+// branches -- with the own cell's quantities from own_f32.  The algebra is
+// the reference's, regrouped: w1 + w2 = dxi exactly, so w1 = dxi/2 + t and
+// w2 = dxi/2 - t with t = (un dxi - nx d1 - ny d2) / (2c), and the rows of
+// R |Lambda| w are collected around w1 + w2 and w2 - w1.
+__device__ __forceinline__ void roe_flux_wet_f32(const Side<float>& L, const OwnF32& o, const Side<float>& R,
+                                                 float dxi, float g, float nx, float ny, float F[3]) {
+  const float rR = 1.0f / R.h;
+  const float uR = R.hu * rR, vR = R.hv * rR;
+  const float sR = smooth_sqrt(R.h);
+  const float rs = 1.0f / (o.s + sR);
+  const float uRoe = (o.s * o.u + sR * uR) * rs;
+  const float vRoe = (o.s * o.v + sR * vR) * rs;
+  const float unRoe = uRoe * nx + vRoe * ny;
+  const float cRoe = smooth_sqrt(g * ((L.h + R.h) * 0.5f));
+  const float d1 = R.hu - L.hu, d2 = R.hv - L.hv;
+  const float t = (unRoe * dxi - nx * d1 - ny * d2) * (0.5f / cRoe);
+  const float w0 = (ny * d1 - nx * d2 - (uRoe * ny - vRoe * nx) * dxi) * smooth_abs(unRoe);
+  const float w1 = (0.5f * dxi + t) * smooth_abs(unRoe - cRoe);
+  const float w2 = (0.5f * dxi - t) * smooth_abs(unRoe + cRoe);
+  const float sum = w1 + w2, dif = cRoe * (w2 - w1);
+  const float A0 = sum;
+  const float A1 = ny * w0 + uRoe * sum + nx * dif;
+  const float A2 = -nx * w0 + vRoe * sum + ny * dif;
+  const float pR = 0.5f * g * (smooth_pow2(R.xi) + 2.0f * R.xi * R.hst);
+  const float fR1x = R.hu * uR + pR, fR2y = R.hv * vR + pR;
+  F[0] = 0.5f * ((L.hu * nx + L.hv * ny) + (R.hu * nx + R.hv * ny) - A0);
+  F[1] = 0.5f * ((o.fxx * nx + o.fxy * ny) + (fR1x * nx + R.hu * vR * ny) - A1);
+  F[2] = 0.5f * ((o.fyx * nx + o.fyy * ny) + (R.hv * uR * nx + fR2y * ny) - A2);
+}
+
 }  // namespace hgd

@@ -29,9 +29,11 @@ constexpr int kBlock = kStageBlockF32;
 inline int blocks_for(int n) { return (n + kBlock - 1) / kBlock; }
 
 template <int NS>
-__device__ __forceinline__ void face_sum_f32(const DevMesh& m, const float4* __restrict__ X, int c, const SideF32& L,
-                                             const float4 (&sl)[NS], const double* __restrict__ totalA, float man,
-                                             int32_t* flags, float& f0, float& f1, float& f2) {
+__device__ __forceinline__ void face_sum_f32(const DevMesh& m, const float4* __restrict__ X, const float4* sX,
+                                             const float4* sP, int base, int c, const SideF32& L,
+                                             const OwnF32& own, const float4 (&sl)[NS],
+                                             const double* __restrict__ totalA, float man, int32_t* flags, float& f0,
+                                             float& f1, float& f2) {
   f0 = 0.0f; f1 = 0.0f; f2 = 0.0f;
 #pragma unroll
   for (int k = 0; k < NS; ++k) {
@@ -41,7 +43,16 @@ __device__ __forceinline__ void face_sum_f32(const DevMesh& m, const float4* __r
     Side<float> R;
     float dxi;
     if (nb >= 0) {
-      const SideF32 r = make_side_f32(__ldg(&X[nb]), __ldg(&m.CP[nb]), m.hsmf, m.hsmLo);
+      const unsigned int ln = (unsigned int)(nb - base);   // in-block neighbour: staged record
+      float4 xr, pr;
+      if (ln < (unsigned int)kBlock) {
+        xr = sX[ln];
+        pr = sP[ln];
+      } else {
+        xr = __ldg(&X[nb]);
+        pr = __ldg(&m.CP[nb]);
+      }
+      const SideF32 r = make_side_f32(xr, pr, m.hsmf, m.hsmLo);
       R = r.s;
       dxi = (r.s.xi - L.s.xi) + (r.xlo - L.xlo);
     } else {
@@ -55,7 +66,8 @@ __device__ __forceinline__ void face_sum_f32(const DevMesh& m, const float4* __r
       dxi = (R.h - L.s.h) + L.excess;
     }
     float F[3];
-    roe_flux<float>(L.s, R, dxi, m.gf, nx, ny, m.hsmf, F);
+    if (!L.s.dry && !R.dry) roe_flux_wet_f32(L.s, own, R, dxi, m.gf, nx, ny, F);
+    else roe_flux<float>(L.s, R, dxi, m.gf, nx, ny, m.hsmf, F);
     f0 = fmaf(F[0], len, f0);
     f1 = fmaf(F[1], len, f1);
     f2 = fmaf(F[2], len, f2);
@@ -147,25 +159,36 @@ template <int NS, bool FUSED, int MODE>
 __global__ void __launch_bounds__(kBlock, stage_min_blocks<NS>())
     k_stage_f32(DevMesh m, DevScalars s, StateF32 Xin, StateF32 Xbase, StateF32 Xout, double* Rout, int cfl,
                 StageFuse f) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  const int base = blockIdx.x * kBlock;
+  const int c = base + threadIdx.x;
   const bool active = c < m.n;
   float cand = INFINITY;
   float hOut = 0.0f;      // output depth, and whether the output cell is wet (fused inlet totals)
   bool wetOut = false;
+  // The block's own state and parameter records, staged for the neighbours in
+  // the block (most of them, in Hilbert order): every global load of the block
+  // is issued before the barrier, and in-block neighbour reads skip a second
+  // round trip to L2/DRAM.
+  __shared__ float4 sX[kBlock], sP[kBlock];
   __shared__ float dtShared;
+  float4 sl[NS], xin, cp, cs;
+  if (active) {
+    load_slots<NS>(m, c, sl);
+    xin = __ldg(&Xin.x[c]);
+    cp = __ldg(&m.CP[c]);
+    cs = __ldg(&m.CS[c]);
+    sX[threadIdx.x] = xin;
+    sP[threadIdx.x] = cp;
+  }
   if constexpr (FUSED) {
     if (threadIdx.x == 0) dtShared = (float)fused_dt(s, f);
-    __syncthreads();
   }
+  __syncthreads();
   if (active) {
-    float4 sl[NS];
-    load_slots<NS>(m, c, sl);
-    const float4 xin = __ldg(&Xin.x[c]);
-    const float4 cp = __ldg(&m.CP[c]);
-    const float4 cs = __ldg(&m.CS[c]);
     const SideF32 L = make_side_f32(xin, cp, m.hsmf, m.hsmLo);
+    const OwnF32 own = own_f32(L.s, m.gf);
     float f0, f1, f2;
-    face_sum_f32<NS>(m, Xin.x, c, L, sl, FUSED ? f.totalIn : m.totalA, cp.w, s.flags, f0, f1, f2);
+    face_sum_f32<NS>(m, Xin.x, sX, sP, base, c, L, own, sl, FUSED ? f.totalIn : m.totalA, cp.w, s.flags, f0, f1, f2);
     const float A = cs.z;
     const float r0 = -f0 / A, r1 = -f1 / A, r2 = -f2 / A;
     const float fr = friction_coef(m.gf, m.kn2f, m.hsmf, cp.w, L.s.h, L.s.hu, L.s.hv);
