@@ -378,12 +378,16 @@ def main():
     ap.add_argument("--adj-steps", type=int, default=100, help="steps of the forward+adjoint measurement (0: skip)")
     ap.add_argument("--profile-stage", default=None, choices=["fp32c", "fp64"],
                     help="only run the stage kernel a few times (a small case for ncu captures)")
+    ap.add_argument("--profile-adjoint", default=None, choices=["fp32c", "fp64"],
+                    help="only run one short forward+adjoint (a small case for ncu captures)")
     args = ap.parse_args()
     if args.steps_fp64 is None:
         args.steps_fp64 = args.steps
     args.warmup = max(args.warmup, 3)
     if args.profile_stage:
         profile_stage(args)
+    elif args.profile_adjoint:
+        profile_adjoint(args)
     elif args.impl == "reference":
         run_reference(args)
     else:
@@ -401,6 +405,21 @@ def profile_stage(args):
     ctx.synchronize()
     ms = ctx.time_stage_kernel(3, True)
     print(json.dumps({"precision": args.profile_stage, "cells": len(case["cell_node_count"]), "stage_ms": ms}))
+
+
+def profile_adjoint(args):
+    """One forward+adjoint of 4 fixed-dt steps (checkpoints every 2) on the
+    workload: 8 VJP launches, after the 4 + 4 forward stage pairs."""
+    from hydrograd_gb.workloads import probes_and_perturbation, river_triangles
+    case = river_triangles(n=args.n)
+    ctx = make_ctx(case, args.profile_adjoint, 0)
+    probes, _ = probes_and_perturbation(case, 64)
+    dt = 0.5 * ctx.integrate(case["Q0"], 1, cfl=0.4)[1][0]
+    obs = np.tile(case["Q0"][probes], (4, 1))
+    t0 = time.perf_counter()
+    r = ctx.loss_and_grad(case["Q0"], 4, dt, probes, obs, ckpt_every=2)
+    print(json.dumps({"precision": args.profile_adjoint, "cells": len(case["cell_node_count"]), "loss": r["loss"],
+                      "seconds": time.perf_counter() - t0}))
 
 
 if __name__ == "__main__":

@@ -128,6 +128,21 @@ int setup(hg_ctx* c) {
   a.inletUOff = dUOff;
   a.inletUCell = dUCell;
   a.inletUCoef = dUCoef;
+  // Cells with a boundary face, in device order.
+  std::vector<int32_t> bnd;
+  for (int i = 0; i < N; ++i) {
+    const int o = c->perm[i];
+    for (int k = 0; k < m.ncf[o]; ++k)
+      if (m.nbr[(size_t)o * 8 + k] < 0) {
+        bnd.push_back(i);
+        break;
+      }
+  }
+  int32_t* dBnd;
+  ADJ_CUDA(c, falloc(b, &dBnd, bnd.size()));
+  if (!bnd.empty()) ADJ_CUDA(c, cudaMemcpy(dBnd, bnd.data(), bnd.size() * 4, cudaMemcpyHostToDevice));
+  a.bndCells = dBnd;
+  a.nBndCells = (int32_t)bnd.size();
   return HG_OK;
 }
 
@@ -311,13 +326,13 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
         const size_t i = (size_t)(s - s0);
         const StateF32 q0 = sg.at(i, n), q1 = sg.at(C + 1 + i, n);
         launch_inlet_total_f32(dm, ds, q1, st);
-        launch_vjp_f32(dm, a, q1, mu2, nullptr, mu1, 0.5f, 0.0f, 0.5f * dtf, st);
+        c->launches += launch_vjp_f32(dm, a, q1, mu2, nullptr, mu1, 0.5f, 0.0f, 0.5f * dtf, st);
         launch_inlet_adjoint_f32(dm, a, q1, mu1, 0.5 * dt, st);
         launch_inlet_total_f32(dm, ds, q0, st);
-        launch_vjp_f32(dm, a, q0, mu1, mu2, mu2, 1.0f, 0.5f, dtf, st);
+        c->launches += launch_vjp_f32(dm, a, q0, mu1, mu2, mu2, 1.0f, 0.5f, dtf, st);
         launch_inlet_adjoint_f32(dm, a, q0, mu2, dt, st);
         if (s >= 1) launch_probe_adjoint_f32(dm, q0, mu2, b->probes, b->obs + (size_t)(s - 1) * P, P, scale, st);
-        c->launches += 2 + 2 * extraPerStep + (s >= 1 && P > 0 ? 1 : 0);
+        c->launches += 2 * extraPerStep + (s >= 1 && P > 0 ? 1 : 0);
       }
     }
   }

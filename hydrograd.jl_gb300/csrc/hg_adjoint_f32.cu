@@ -2,9 +2,10 @@
 //
 // Same gather-form VJP as hg_adjoint_f64.cu (see there for the formulas), on
 // the packed FP32 records (hg_f32.cuh), with the FP32 path's own wet/dry
-// decisions (depth_f32) so that every branch is the forward pass's.  Cotangents are FP32; per-cell parameter gradients accumulate as
-// compensated FP32 pairs (GB300's FP64 rate is a small fraction of its FP32
-// rate) and are folded into FP64 once, after the reverse sweep.
+// decisions (depth_f32) so that every branch is the forward pass's.
+// Cotangents are FP32; per-cell parameter gradients accumulate as compensated
+// FP32 pairs (GB300's FP64 rate is a small fraction of its FP32 rate) and are
+// folded into FP64 once, after the reverse sweep.
 // Compiled with the same fast-math options as the FP32 forward kernels.
 #include <cfloat>
 #include <cmath>
@@ -62,8 +63,16 @@ __device__ __forceinline__ void acc_add(float2* p, float b, float g) {
   *p = a;
 }
 
+// Interior faces (3-direction duals: d/d own xi, hu, hv) and the source
+// terms.  Boundary faces, whose ghost states also depend on n, zb, Q and
+// total_A (7-direction duals), are added afterwards by k_vjp_bnd_f32, so that
+// this kernel -- the one over every cell -- carries only the registers of the
+// 3-direction flux.
 template <int NS>
-__global__ void __launch_bounds__(kBlock) k_vjp_f32(DevMesh m, AdjDev a, StateF32 Q, const float* __restrict__ mu,
+constexpr int vjp_min_blocks() { return NS <= 4 ? 5 : 1; }   // <= 96 registers, no spills
+
+template <int NS>
+__global__ void __launch_bounds__(kBlock, vjp_min_blocks<NS>()) k_vjp_f32(DevMesh m, AdjDev a, StateF32 Q, const float* __restrict__ mu,
                                                     const float* __restrict__ extra, float* out, float cSelf,
                                                     float cExtra, float beta) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -74,52 +83,26 @@ __global__ void __launch_bounds__(kBlock) k_vjp_f32(DevMesh m, AdjDev a, StateF3
   const SideF32 L = make_side_f32(__ldg(&Q.x[j]), cp, m.hsmf, m.hsmLo);
   const float Aj = cs.z;
   const float mj0 = mu[j], mj1 = mu[n + j], mj2 = mu[2 * n + j];
-  float g0 = 0.0f, g1 = 0.0f, g2 = 0.0f, gn = 0.0f, gzb = 0.0f;
+  float g0 = 0.0f, g1 = 0.0f, g2 = 0.0f, gn = 0.0f;
   const Side<F3> L3 = seeded<F3>(L.s, -1);
 #pragma unroll
   for (int k = 0; k < NS; ++k) {
     const float4 sl = __ldg(&m.SL[(size_t)k * n + j]);
     const int32_t nb = slot_nb(sl);
-    if (nb == kNoFace) continue;
+    if (nb < 0) continue;   // no face, or a boundary face (k_vjp_bnd_f32)
     const float nx = sl.x, ny = sl.y, len = sl.z;
-    if (nb >= 0) {
-      const SideF32 R = make_side_f32(__ldg(&Q.x[nb]), __ldg(&m.CP[nb]), m.hsmf, m.hsmLo);
-      const float An = __ldg(&m.CS[nb]).z;
-      const float w0 = len * (mu[nb] / An - mj0 / Aj);
-      const float w1 = len * (mu[n + nb] / An - mj1 / Aj);
-      const float w2 = len * (mu[2 * n + nb] / An - mj2 / Aj);
-      const Side<F3> R3 = constant<F3>(R.s);
-      const F3 dxi = (R3.xi - L3.xi) + F3(R.xlo - L.xlo);
-      F3 F[3];
-      roe_flux<F3>(L3, R3, dxi, F3(m.gf), F3(nx), F3(ny), F3(m.hsmf), F);
-      g0 += w0 * F[0].d[0] + w1 * F[1].d[0] + w2 * F[2].d[0];
-      g1 += w0 * F[0].d[1] + w1 * F[1].d[1] + w2 * F[2].d[1];
-      g2 += w0 * F[0].d[2] + w1 * F[1].d[2] + w2 * F[2].d[2];
-    } else {
-      const int32_t bf = boundary_index(nb);
-      const int32_t info = m.bfInfo[bf], type = info & 3, grp = info >> 2;
-      const float w0 = -len * mj0 / Aj, w1 = -len * mj1 / Aj, w2 = -len * mj2 / Aj;
-      const Side<F7> L7 = seeded<F7>(L.s, 4);
-      const F7 man = F7::seed(cp.w, 3);
-      const F7 qin = F7::seed(type == kBcInletQ ? (float)m.inletQ[grp] : 0.0f, 5);
-      const F7 ta = F7::seed(type == kBcInletQ ? (float)m.totalA[grp] : 1.0f, 6);
-      const Side<F7> R7 = ghost_state<F7>(L7, type, F7(nx), F7(ny), F7(m.hsmf),
-                                          F7(type == kBcExitH ? (float)m.exitWse[grp] : 0.0f), qin, ta,
-                                          F7(m.bfLp23f[bf]), man);
-      F7 ex(L.excess);
-      if (L.s.dry) ex.d[0] = -1.0f;   // excess = h_small - (xi + hstill) for a dry cell
-      const F7 dxi = (R7.h - L7.h) + ex;
-      F7 F[3];
-      roe_flux<F7>(L7, R7, dxi, F7(m.gf), F7(nx), F7(ny), F7(m.hsmf), F);
-      float c[7];
-#pragma unroll
-      for (int d = 0; d < 7; ++d) c[d] = w0 * F[0].d[d] + w1 * F[1].d[d] + w2 * F[2].d[d];
-      g0 += c[0]; g1 += c[1]; g2 += c[2];
-      gn += c[3];
-      gzb += c[4];
-      a.bfGradQ[bf] = (double)c[5];
-      a.bfGradTA[bf] = (double)c[6];
-    }
+    const SideF32 R = make_side_f32(__ldg(&Q.x[nb]), __ldg(&m.CP[nb]), m.hsmf, m.hsmLo);
+    const float An = __ldg(&m.CS[nb]).z;
+    const float w0 = len * (mu[nb] / An - mj0 / Aj);
+    const float w1 = len * (mu[n + nb] / An - mj1 / Aj);
+    const float w2 = len * (mu[2 * n + nb] / An - mj2 / Aj);
+    const Side<F3> R3 = constant<F3>(R.s);
+    const F3 dxi = (R3.xi - L3.xi) + F3(R.xlo - L.xlo);
+    F3 F[3];
+    roe_flux<F3>(L3, R3, dxi, F3(m.gf), F3(nx), F3(ny), F3(m.hsmf), F);
+    g0 += w0 * F[0].d[0] + w1 * F[1].d[0] + w2 * F[2].d[0];
+    g1 += w0 * F[0].d[1] + w1 * F[1].d[1] + w2 * F[2].d[1];
+    g2 += w0 * F[0].d[2] + w1 * F[1].d[2] + w2 * F[2].d[2];
   }
   if (!L.s.dry) {
     const float hu = L.s.hu, hv = L.s.hv, man = cp.w;
@@ -137,12 +120,66 @@ __global__ void __launch_bounds__(kBlock) k_vjp_f32(DevMesh m, AdjDev a, StateF3
     acc_add(&a.accF[(size_t)2 * n + j], beta, mj2 * m.gf * L.s.xi);
   }
   if (gn != 0.0f) acc_add(&a.accF[j], beta, gn);
-  if (gzb != 0.0f) acc_add(&a.accF[(size_t)3 * n + j], beta, gzb);   // exit-H cells only
   const float mask = L.s.dry ? 0.0f : 1.0f;
   const float e0 = extra ? extra[j] : 0.0f, e1 = extra ? extra[n + j] : 0.0f, e2 = extra ? extra[2 * n + j] : 0.0f;
   out[j] = mask * (cSelf * mj0 + cExtra * e0 + beta * g0);
   out[n + j] = mask * (cSelf * mj1 + cExtra * e1 + beta * g1);
   out[2 * n + j] = mask * (cSelf * mj2 + cExtra * e2 + beta * g2);
+}
+
+// Boundary faces of the cells that have any (one thread per such cell, after
+// k_vjp_f32 on the same stream): ghost-state duals in the own state, n, zb, Q
+// and total_A; adds to out[j] and the n / zb accumulators, and leaves the
+// Q / total_A cotangents per boundary face for k_inlet_adjoint_f32.
+template <int NS>
+__global__ void __launch_bounds__(64) k_vjp_bnd_f32(DevMesh m, AdjDev a, StateF32 Q, const float* __restrict__ mu,
+                                                    float* out, float beta) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.nBndCells) return;
+  const int j = a.bndCells[i];
+  const int n = m.n;
+  const float4 cp = __ldg(&m.CP[j]);
+  const SideF32 L = make_side_f32(__ldg(&Q.x[j]), cp, m.hsmf, m.hsmLo);
+  const float Aj = __ldg(&m.CS[j]).z;
+  const float mj0 = mu[j], mj1 = mu[n + j], mj2 = mu[2 * n + j];
+  float g0 = 0.0f, g1 = 0.0f, g2 = 0.0f, gn = 0.0f, gzb = 0.0f;
+#pragma unroll
+  for (int k = 0; k < NS; ++k) {
+    const float4 sl = __ldg(&m.SL[(size_t)k * n + j]);
+    const int32_t nb = slot_nb(sl);
+    if (nb >= 0 || nb == kNoFace) continue;
+    const float nx = sl.x, ny = sl.y, len = sl.z;
+    const int32_t bf = boundary_index(nb);
+    const int32_t info = m.bfInfo[bf], type = info & 3, grp = info >> 2;
+    const float w0 = -len * mj0 / Aj, w1 = -len * mj1 / Aj, w2 = -len * mj2 / Aj;
+    const Side<F7> L7 = seeded<F7>(L.s, 4);
+    const F7 man = F7::seed(cp.w, 3);
+    const F7 qin = F7::seed(type == kBcInletQ ? (float)m.inletQ[grp] : 0.0f, 5);
+    const F7 ta = F7::seed(type == kBcInletQ ? (float)m.totalA[grp] : 1.0f, 6);
+    const Side<F7> R7 = ghost_state<F7>(L7, type, F7(nx), F7(ny), F7(m.hsmf),
+                                        F7(type == kBcExitH ? (float)m.exitWse[grp] : 0.0f), qin, ta,
+                                        F7(m.bfLp23f[bf]), man);
+    F7 ex(L.excess);
+    if (L.s.dry) ex.d[0] = -1.0f;   // excess = h_small - (xi + hstill) for a dry cell
+    const F7 dxi = (R7.h - L7.h) + ex;
+    F7 F[3];
+    roe_flux<F7>(L7, R7, dxi, F7(m.gf), F7(nx), F7(ny), F7(m.hsmf), F);
+    float c[7];
+#pragma unroll
+    for (int d = 0; d < 7; ++d) c[d] = w0 * F[0].d[d] + w1 * F[1].d[d] + w2 * F[2].d[d];
+    g0 += c[0]; g1 += c[1]; g2 += c[2];
+    gn += c[3];
+    gzb += c[4];
+    a.bfGradQ[bf] = (double)c[5];
+    a.bfGradTA[bf] = (double)c[6];
+  }
+  if (gn != 0.0f) acc_add(&a.accF[j], beta, gn);
+  if (gzb != 0.0f) acc_add(&a.accF[(size_t)3 * n + j], beta, gzb);
+  if (!L.s.dry) {
+    out[j] += beta * g0;
+    out[n + j] += beta * g1;
+    out[2 * n + j] += beta * g2;
+  }
 }
 
 __global__ void __launch_bounds__(256) k_inlet_adjoint_f32(DevMesh m, AdjDev a, StateF32 Q, float* out, double beta,
@@ -216,11 +253,20 @@ __global__ void k_fold_accumulators_f32(DevMesh m, AdjDev a) {
 
 }  // namespace
 
-void launch_vjp_f32(const DevMesh& m, const AdjDev& a, StateF32 Q, const float* mu, const float* extra, float* out,
-                    float cSelf, float cExtra, float beta, cudaStream_t st) {
-  if (m.nslot <= 3) k_vjp_f32<3><<<blocks_for(m.n), kBlock, 0, st>>>(m, a, Q, mu, extra, out, cSelf, cExtra, beta);
-  else if (m.nslot <= 4) k_vjp_f32<4><<<blocks_for(m.n), kBlock, 0, st>>>(m, a, Q, mu, extra, out, cSelf, cExtra, beta);
-  else k_vjp_f32<8><<<blocks_for(m.n), kBlock, 0, st>>>(m, a, Q, mu, extra, out, cSelf, cExtra, beta);
+int launch_vjp_f32(const DevMesh& m, const AdjDev& a, StateF32 Q, const float* mu, const float* extra, float* out,
+                   float cSelf, float cExtra, float beta, cudaStream_t st) {
+  const int nbb = (a.nBndCells + 63) / 64;
+  if (m.nslot <= 3) {
+    k_vjp_f32<3><<<blocks_for(m.n), kBlock, 0, st>>>(m, a, Q, mu, extra, out, cSelf, cExtra, beta);
+    if (nbb) k_vjp_bnd_f32<3><<<nbb, 64, 0, st>>>(m, a, Q, mu, out, beta);
+  } else if (m.nslot <= 4) {
+    k_vjp_f32<4><<<blocks_for(m.n), kBlock, 0, st>>>(m, a, Q, mu, extra, out, cSelf, cExtra, beta);
+    if (nbb) k_vjp_bnd_f32<4><<<nbb, 64, 0, st>>>(m, a, Q, mu, out, beta);
+  } else {
+    k_vjp_f32<8><<<blocks_for(m.n), kBlock, 0, st>>>(m, a, Q, mu, extra, out, cSelf, cExtra, beta);
+    if (nbb) k_vjp_bnd_f32<8><<<nbb, 64, 0, st>>>(m, a, Q, mu, out, beta);
+  }
+  return nbb ? 2 : 1;
 }
 void launch_inlet_adjoint_f32(const DevMesh& m, const AdjDev& a, StateF32 Q, float* out, double beta,
                               cudaStream_t st) {

@@ -25,6 +25,9 @@ struct AdjDev {
   // FP32-compensated path: per-cell sums of gN, gS0x, gS0y, gZb ([4][n]) as
   // unevaluated float pairs {hi, lo}, folded into the FP64 arrays at the end.
   float2* accF = nullptr;
+  // Cells with at least one boundary face, device order (FP32C boundary VJP).
+  const int32_t* bndCells = nullptr;
+  int32_t nBndCells = 0;
 };
 
 // out_j = M(Q_j) (cSelf mu_j + cExtra extra_j + beta (J(Q)^T mu)_j), parameter
@@ -40,8 +43,9 @@ void launch_probe_loss_f64(const DevMesh& m, const AdjDev& a, const double* Q, c
 void launch_probe_adjoint_f64(const DevMesh& m, const double* Q, double* mu, const int32_t* probes,
                               const double* obs, int32_t nprobe, double scale, cudaStream_t st);
 // FP32-compensated path: the same with packed FP32 states and FP32 cotangents.
-void launch_vjp_f32(const DevMesh& m, const AdjDev& a, StateF32 Q, const float* mu, const float* extra, float* out,
-                    float cSelf, float cExtra, float beta, cudaStream_t st);
+// Returns the launches made (interior kernel, and the boundary-cell kernel).
+int launch_vjp_f32(const DevMesh& m, const AdjDev& a, StateF32 Q, const float* mu, const float* extra, float* out,
+                   float cSelf, float cExtra, float beta, cudaStream_t st);
 void launch_inlet_adjoint_f32(const DevMesh& m, const AdjDev& a, StateF32 Q, float* out, double beta,
                               cudaStream_t st);
 void launch_probe_loss_f32(const DevMesh& m, const AdjDev& a, StateF32 Q, const int32_t* probes, const double* obs,

@@ -1,5 +1,6 @@
-// FP32-compensated path: packed cell records, the FP64-exact dry decision and
-// double-float (hi + lo) arithmetic, shared by the forward and adjoint kernels.
+// FP32-compensated path: packed cell records, the dry decision from the hi + lo
+// pairs, double-float (hi + lo) arithmetic and the wet-wet Roe fast path,
+// shared by the forward and adjoint kernels.
 //
 // Layout (device cell order):
 //   X[c]  float4 {xi_hi, xi_lo, qx_hi, qy_hi}   the part of the state a neighbour reads
