@@ -34,14 +34,19 @@ struct AdjointBuffers {
   size_t segStates = 0;
   double *mu1 = nullptr, *mu2 = nullptr, *gzb = nullptr;
   int32_t* probes = nullptr;
+  int32_t* probeCsr = nullptr;   // FP32C: probes grouped by cell (ProbeCsr), <= 3 P + 1 entries
   double* obs = nullptr;
   size_t probeCap = 0, obsCap = 0;
+  double* segTot = nullptr;      // FP32C: inlet totals of a segment's states
+  size_t segTotCap = 0;
   ~AdjointBuffers() {
     for (void* p : fixed) cudaFree(p);
     cudaFree(ckpt);
     cudaFree(seg);
     cudaFree(probes);
+    cudaFree(probeCsr);
     cudaFree(obs);
+    cudaFree(segTot);
   }
 };
 
@@ -198,8 +203,11 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
   // Probes (device order) and observations.
   if ((size_t)std::max(P, 1) > b->probeCap) {
     cudaFree(b->probes);
+    cudaFree(b->probeCsr);
     b->probes = nullptr;
+    b->probeCsr = nullptr;
     ADJ_CUDA(c, cudaMalloc(&b->probes, std::max(P, 1) * sizeof(int32_t)));
+    ADJ_CUDA(c, cudaMalloc(&b->probeCsr, (3 * (size_t)std::max(P, 1) + 1) * sizeof(int32_t)));
     b->probeCap = std::max(P, 1);
   }
   const size_t nobs = (size_t)K * std::max(P, 0);
@@ -211,8 +219,32 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
   }
   std::vector<int32_t> pdev(std::max(P, 0));
   for (int p = 0; p < P; ++p) pdev[p] = c->inv[probeCells[p]];
+  // The same probes grouped by cell (distinct cells in order of first
+  // appearance, each with its probe indices in increasing order).
+  std::vector<int32_t> csr;
+  ProbeCsr pc;
+  {
+    std::vector<int32_t> cells, off(1, 0), idx;
+    std::map<int32_t, std::vector<int32_t>> at;
+    for (int p = 0; p < P; ++p) {
+      if (!at.count(pdev[p])) cells.push_back(pdev[p]);
+      at[pdev[p]].push_back(p);
+    }
+    for (int32_t cell : cells) {
+      for (int32_t p : at[cell]) idx.push_back(p);
+      off.push_back((int32_t)idx.size());
+    }
+    csr = cells;
+    csr.insert(csr.end(), off.begin(), off.end());
+    csr.insert(csr.end(), idx.begin(), idx.end());
+    pc.cell = b->probeCsr;
+    pc.off = b->probeCsr + cells.size();
+    pc.idx = b->probeCsr + 2 * cells.size() + 1;
+    pc.nCells = (int32_t)cells.size();
+  }
   if (P > 0) {
     ADJ_CUDA(c, cudaMemcpyAsync(b->probes, pdev.data(), P * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+    ADJ_CUDA(c, cudaMemcpyAsync(b->probeCsr, csr.data(), csr.size() * sizeof(int32_t), cudaMemcpyHostToDevice, st));
     ADJ_CUDA(c, cudaMemcpyAsync(b->obs, obs, nobs * sizeof(double), cudaMemcpyHostToDevice, st));
   }
   // Accumulators and dt.
@@ -289,50 +321,99 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
     float* mu1 = reinterpret_cast<float*>(b->mu1);
     float* mu2 = reinterpret_cast<float*>(b->mu2);
     const StateF32 XA{c->XA, c->XQA}, XB{c->XB, c->XQB};
+    // Inlet conveyance totals of every state a VJP or a stage reads, kept
+    // instead of recomputed: T0[i] of Q0s[i] (i = 0..C) and T1[i] of Q1s[i].
+    // When the inlet groups fit the fused stage kernels, those kernels produce
+    // the totals of their output states; otherwise k_inlet_total does.
+    const bool fz = dm.nInlet <= kMaxFusedInlets;
+    const size_t stride = (size_t)std::max(dm.nInlet, kMaxFusedInlets);
+    const size_t totNeed = (size_t)(2 * C + 1) * stride;
+    if (totNeed > b->segTotCap) {
+      cudaFree(b->segTot);
+      b->segTot = nullptr;
+      ADJ_CUDA(c, cudaMalloc(&b->segTot, totNeed * sizeof(double)));
+      b->segTotCap = totNeed;
+    }
+    double* T0 = b->segTot;
+    double* T1 = b->segTot + (size_t)(C + 1) * stride;
+    auto totals = [&](StateF32 q, double* t) {   // totals of q into t
+      if (dm.nInlet == 0) return;
+      DevMesh mm = dm;
+      mm.totalA = t;
+      launch_inlet_total_f32(mm, ds, q, st);
+      c->launches += 1;
+    };
+    // One SSP-RK2 step q0 -> (q1) -> q2 at the fixed dt, with the totals t0 of q0
+    // on entry and those of q1 and q2 on exit.
+    auto step = [&](StateF32 q0, StateF32 q1, StateF32 q2, double* t0, double* t1, double* t2) {
+      if (fz) {
+        StageFuse f;
+        f.partials = c->d_partials;
+        f.ticket = c->d_ticket;
+        f.blockSlot = c->d_blockSlot;
+        f.nSlots = c->nSlots;
+        f.totalIn = t0;
+        f.totalOut = t1;
+        launch_stage_f32_fused(dm, ds, kModeStage1, q0, StateF32{}, q1, f, st);
+        f.totalIn = t1;
+        f.totalOut = t2;
+        launch_stage_f32_fused(dm, ds, kModeStage2, q1, q0, q2, f, st);
+        c->launches += 2;
+      } else {
+        DevMesh mm = dm;
+        mm.totalA = t0;
+        launch_stage_f32(mm, ds, kModeStage1, q0, StateF32{}, q1, nullptr, false, st);
+        totals(q1, t1);
+        mm.totalA = t1;
+        launch_stage_f32(mm, ds, kModeStage2, q1, q0, q2, nullptr, false, st);
+        totals(q2, t2);
+        c->launches += 2;
+      }
+    };
     launch_gather_state_f32(N, c->d_perm, c->Quser, XA, st);
     auto copy_state = [&](StateF32 dst, StateF32 src) -> cudaError_t {
       cudaError_t e = cudaMemcpyAsync(dst.x, src.x, (size_t)n * sizeof(float4), cudaMemcpyDeviceToDevice, st);
       if (e == cudaSuccess) e = cudaMemcpyAsync(dst.q, src.q, (size_t)n * sizeof(float2), cudaMemcpyDeviceToDevice, st);
       return e;
     };
+    // Forward pass with checkpoints (totals ping-pong in T0[0] / T0[1]).
+    totals(XA, T0);
     for (int s = 0; s < K; ++s) {
       if (s % C == 0) ADJ_CUDA(c, copy_state(ck.at(s / C, n), XA));
-      launch_inlet_total_f32(dm, ds, XA, st);
-      launch_stage_f32(dm, ds, kModeStage1, XA, StateF32{}, XB, nullptr, false, st);
-      launch_inlet_total_f32(dm, ds, XB, st);
-      launch_stage_f32(dm, ds, kModeStage2, XB, XA, XA, nullptr, false, st);
+      step(XA, XB, XA, T0, T0 + stride, T0);
       launch_probe_loss_f32(dm, a, XA, b->probes, b->obs + (size_t)s * P, P, st);
-      c->launches += 3 + extraPerStep;
+      c->launches += P > 0 ? 1 : 0;
     }
     if (Qfinal) {
       launch_scatter_state_f32(N, c->d_perm, XA, c->Quser, st);
       ADJ_CUDA(c, cudaMemcpyAsync(Qfinal, c->Quser, n3 * sizeof(double), cudaMemcpyDeviceToHost, st));
     }
     ADJ_CUDA(c, cudaMemsetAsync(mu2, 0, n3 * sizeof(float), st));
-    launch_probe_adjoint_f32(dm, XA, mu2, b->probes, b->obs + (size_t)(K - 1) * P, P, scale, st);
+    launch_probe_adjoint_f32(dm, XA, mu2, pc, b->obs + (size_t)(K - 1) * P, scale, st);
     for (int seg = nck - 1; seg >= 0; --seg) {
       const int s0 = seg * C, s1 = std::min(K, s0 + C);
       ADJ_CUDA(c, copy_state(sg.at(0, n), ck.at(seg, n)));
+      totals(sg.at(0, n), T0);
       for (int s = s0; s < s1; ++s) {
         const size_t i = (size_t)(s - s0);
-        const StateF32 q0 = sg.at(i, n), q1 = sg.at(C + 1 + i, n), q2 = sg.at(i + 1, n);
-        launch_inlet_total_f32(dm, ds, q0, st);
-        launch_stage_f32(dm, ds, kModeStage1, q0, StateF32{}, q1, nullptr, false, st);
-        launch_inlet_total_f32(dm, ds, q1, st);
-        launch_stage_f32(dm, ds, kModeStage2, q1, q0, q2, nullptr, false, st);
-        c->launches += 2 + extraPerStep;
+        step(sg.at(i, n), sg.at(C + 1 + i, n), sg.at(i + 1, n), T0 + i * stride, T1 + i * stride,
+             T0 + (i + 1) * stride);
       }
       for (int s = s1 - 1; s >= s0; --s) {
         const size_t i = (size_t)(s - s0);
         const StateF32 q0 = sg.at(i, n), q1 = sg.at(C + 1 + i, n);
-        launch_inlet_total_f32(dm, ds, q1, st);
-        c->launches += launch_vjp_f32(dm, a, q1, mu2, nullptr, mu1, 0.5f, 0.0f, 0.5f * dtf, st);
-        launch_inlet_adjoint_f32(dm, a, q1, mu1, 0.5 * dt, st);
-        launch_inlet_total_f32(dm, ds, q0, st);
-        c->launches += launch_vjp_f32(dm, a, q0, mu1, mu2, mu2, 1.0f, 0.5f, dtf, st);
-        launch_inlet_adjoint_f32(dm, a, q0, mu2, dt, st);
-        if (s >= 1) launch_probe_adjoint_f32(dm, q0, mu2, b->probes, b->obs + (size_t)(s - 1) * P, P, scale, st);
-        c->launches += 2 * extraPerStep + (s >= 1 && P > 0 ? 1 : 0);
+        DevMesh m1 = dm, m0 = dm;
+        m1.totalA = T1 + i * stride;
+        m0.totalA = T0 + i * stride;
+        c->launches += launch_vjp_f32(m1, a, q1, mu2, nullptr, mu1, 0.5f, 0.0f, 0.5f * dtf, st);
+        launch_inlet_adjoint_f32(m1, a, q1, mu1, 0.5 * dt, st);
+        c->launches += launch_vjp_f32(m0, a, q0, mu1, mu2, mu2, 1.0f, 0.5f, dtf, st);
+        launch_inlet_adjoint_f32(m0, a, q0, mu2, dt, st);
+        c->launches += 2 * dm.nInlet;
+        if (s >= 1 && P > 0) {
+          launch_probe_adjoint_f32(dm, q0, mu2, pc, b->obs + (size_t)(s - 1) * P, scale, st);
+          c->launches += 1;
+        }
       }
     }
   }
@@ -341,7 +422,7 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
     c->launches += 1;
   }
   launch_zb_gradient(dm, a, b->gzb, st);
-  c->launches += 1;
+  c->launches += 2;
   ADJ_CUDA(c, cudaGetLastError());
   // Results, mapped back to the caller's cell order.
   std::vector<double> hN(N), hZ(N), hQ(std::max(dm.nInlet, 1));

@@ -182,7 +182,7 @@ __global__ void __launch_bounds__(64) k_vjp_bnd_f32(DevMesh m, AdjDev a, StateF3
   }
 }
 
-__global__ void __launch_bounds__(256) k_inlet_adjoint_f32(DevMesh m, AdjDev a, StateF32 Q, float* out, double beta,
+__global__ void __launch_bounds__(1024) k_inlet_adjoint_f32(DevMesh m, AdjDev a, StateF32 Q, float* out, double beta,
                                                            int g) {
   const int o0 = m.inletOff[g], o1 = m.inletOff[g + 1];
   double sTA = 0.0, sQ = 0.0;
@@ -228,16 +228,20 @@ __global__ void __launch_bounds__(256) k_probe_loss_f32(DevMesh m, AdjDev a, Sta
   if (threadIdx.x == 0) a.loss[0] += t;
 }
 
-__global__ void k_probe_adjoint_f32(DevMesh m, StateF32 Q, float* mu, const int32_t* __restrict__ probes,
-                                    const double* __restrict__ obs, int np, double scale) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  for (int p = 0; p < np; ++p) {
-    const int c = probes[p];
-    const float4 cp = m.CP[c];
-    const SideF32 L = make_side_f32(Q.x[c], cp, m.hsmf, m.hsmLo);
-    if (L.s.dry) continue;
-    mu[c] += (float)(scale * 2.0 * (depth_f64(m, Q, c) - obs[p]));
-  }
+// One thread per distinct probe cell u: mu_xi[c] += sum over the probes p at
+// c (in probe order) of scale 2 (h - obs_p), when c is wet.
+__global__ void k_probe_adjoint_f32(DevMesh m, StateF32 Q, float* mu, ProbeCsr pc, const double* __restrict__ obs,
+                                    double scale) {
+  const int u = blockIdx.x * blockDim.x + threadIdx.x;
+  if (u >= pc.nCells) return;
+  const int c = pc.cell[u];
+  const float4 cp = m.CP[c];
+  const SideF32 L = make_side_f32(Q.x[c], cp, m.hsmf, m.hsmLo);
+  if (L.s.dry) return;
+  const double h = depth_f64(m, Q, c);
+  double acc = 0.0;
+  for (int i = pc.off[u]; i < pc.off[u + 1]; ++i) acc += scale * 2.0 * (h - obs[pc.idx[i]]);
+  mu[c] += (float)acc;
 }
 
 __global__ void k_fold_accumulators_f32(DevMesh m, AdjDev a) {
@@ -270,15 +274,15 @@ int launch_vjp_f32(const DevMesh& m, const AdjDev& a, StateF32 Q, const float* m
 }
 void launch_inlet_adjoint_f32(const DevMesh& m, const AdjDev& a, StateF32 Q, float* out, double beta,
                               cudaStream_t st) {
-  for (int g = 0; g < m.nInlet; ++g) k_inlet_adjoint_f32<<<1, 256, 0, st>>>(m, a, Q, out, beta, g);
+  for (int g = 0; g < m.nInlet; ++g) k_inlet_adjoint_f32<<<1, 1024, 0, st>>>(m, a, Q, out, beta, g);
 }
 void launch_probe_loss_f32(const DevMesh& m, const AdjDev& a, StateF32 Q, const int32_t* probes, const double* obs,
                            int32_t nprobe, cudaStream_t st) {
   if (nprobe > 0) k_probe_loss_f32<<<1, 256, 0, st>>>(m, a, Q, probes, obs, nprobe);
 }
-void launch_probe_adjoint_f32(const DevMesh& m, StateF32 Q, float* mu, const int32_t* probes, const double* obs,
-                              int32_t nprobe, double scale, cudaStream_t st) {
-  if (nprobe > 0) k_probe_adjoint_f32<<<1, 32, 0, st>>>(m, Q, mu, probes, obs, nprobe, scale);
+void launch_probe_adjoint_f32(const DevMesh& m, StateF32 Q, float* mu, const ProbeCsr& pc, const double* obs,
+                              double scale, cudaStream_t st) {
+  if (pc.nCells > 0) k_probe_adjoint_f32<<<(pc.nCells + 127) / 128, 128, 0, st>>>(m, Q, mu, pc, obs, scale);
 }
 void launch_fold_accumulators_f32(const DevMesh& m, const AdjDev& a, cudaStream_t st) {
   k_fold_accumulators_f32<<<blocks_for(m.n), kBlock, 0, st>>>(m, a);

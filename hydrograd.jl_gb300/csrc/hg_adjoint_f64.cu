@@ -203,11 +203,20 @@ __global__ void k_probe_adjoint_f64(DevMesh m, const double* __restrict__ Q, dou
 
 // dL/dzb_j = sum_f of the transposed S0 = -GreenGauss(zb_faces) map
 // (process_bed_2D.jl:46-66; fvm_schemes_2D.jl:197-213,253-275) + the direct term.
+// dL/dS0 / A per cell, in place (the gradient w.r.t. S0 is not needed after
+// this), so that k_zb_gradient divides once per cell rather than once per face.
+__global__ void __launch_bounds__(256) k_zb_scale(DevMesh m, AdjDev a) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= m.n) return;
+  a.gS0x[j] = a.gS0x[j] / m.area[j];
+  a.gS0y[j] = a.gS0y[j] / m.area[j];
+}
+
 __global__ void __launch_bounds__(256) k_zb_gradient(DevMesh m, AdjDev a, double* gzb) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= m.n) return;
   const int n = m.n;
-  const double gxj = a.gS0x[j] / m.area[j], gyj = a.gS0y[j] / m.area[j];
+  const double gxj = a.gS0x[j], gyj = a.gS0y[j];
   double acc = a.gZb[j];
   for (int k = 0; k < m.nslot; ++k) {
     const int32_t nb = m.nb[(size_t)k * n + j];
@@ -215,7 +224,7 @@ __global__ void __launch_bounds__(256) k_zb_gradient(DevMesh m, AdjDev a, double
     const double nx = m.snx[(size_t)k * n + j], ny = m.sny[(size_t)k * n + j];
     const double len = m.slen[(size_t)k * n + j];
     if (nb >= 0) {
-      const double gxn = a.gS0x[nb] / m.area[nb], gyn = a.gS0y[nb] / m.area[nb];
+      const double gxn = a.gS0x[nb], gyn = a.gS0y[nb];
       acc += -0.5 * len * ((gxj - gxn) * nx + (gyj - gyn) * ny);
     } else {
       acc += -len * (gxj * nx + gyj * ny);
@@ -243,6 +252,7 @@ void launch_probe_adjoint_f64(const DevMesh& m, const double* Q, double* mu, con
   if (nprobe > 0) k_probe_adjoint_f64<<<1, 32, 0, st>>>(m, Q, mu, probes, obs, nprobe, scale);
 }
 void launch_zb_gradient(const DevMesh& m, const AdjDev& a, double* gzb, cudaStream_t st) {
+  k_zb_scale<<<(m.n + 255) / 256, 256, 0, st>>>(m, a);
   k_zb_gradient<<<(m.n + 255) / 256, 256, 0, st>>>(m, a, gzb);
 }
 

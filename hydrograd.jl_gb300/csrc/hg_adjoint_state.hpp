@@ -50,8 +50,15 @@ void launch_inlet_adjoint_f32(const DevMesh& m, const AdjDev& a, StateF32 Q, flo
                               cudaStream_t st);
 void launch_probe_loss_f32(const DevMesh& m, const AdjDev& a, StateF32 Q, const int32_t* probes, const double* obs,
                            int32_t nprobe, cudaStream_t st);
-void launch_probe_adjoint_f32(const DevMesh& m, StateF32 Q, float* mu, const int32_t* probes, const double* obs,
-                              int32_t nprobe, double scale, cudaStream_t st);
+// Probes grouped by cell: cell[u] (distinct, device order) holds probes idx[off[u] .. off[u+1]).
+struct ProbeCsr {
+  const int32_t* cell = nullptr;
+  const int32_t* off = nullptr;
+  const int32_t* idx = nullptr;
+  int32_t nCells = 0;
+};
+void launch_probe_adjoint_f32(const DevMesh& m, StateF32 Q, float* mu, const ProbeCsr& pc, const double* obs,
+                              double scale, cudaStream_t st);
 // gN, gS0x, gS0y, gZb += the FP32 pair accumulators (accF).
 void launch_fold_accumulators_f32(const DevMesh& m, const AdjDev& a, cudaStream_t st);
 // dL/dzb = S0 transpose (Green-Gauss of face averages) applied to dL/dS0, plus the direct term.
