@@ -84,27 +84,41 @@ __global__ void __launch_bounds__(kBlock, vjp_min_blocks<NS>()) k_vjp_f32(DevMes
   const float Aj = cs.z;
   const float mj0 = mu[j], mj1 = mu[n + j], mj2 = mu[2 * n + j];
   float g0 = 0.0f, g1 = 0.0f, g2 = 0.0f, gn = 0.0f;
-  const Side<F3> L3 = seeded<F3>(L.s, -1);
+  if (!L.s.dry) {   // a dry cell's output is masked to zero, and its faces add to nothing else
+    // Wet-wet faces in reverse mode (roe_wet_vjp_f32, the own quantities'
+    // adjoints summed over the faces and taken back once); faces with a dry
+    // neighbour through 3-direction duals of the reference solver.
+    const OwnF32 o = own_f32(L.s, m.gf);
+    OwnAdjF32 b;
 #pragma unroll
-  for (int k = 0; k < NS; ++k) {
-    const float4 sl = __ldg(&m.SL[(size_t)k * n + j]);
-    const int32_t nb = slot_nb(sl);
-    if (nb < 0) continue;   // no face, or a boundary face (k_vjp_bnd_f32)
-    const float nx = sl.x, ny = sl.y, len = sl.z;
-    const SideF32 R = make_side_f32(__ldg(&Q.x[nb]), __ldg(&m.CP[nb]), m.hsmf, m.hsmLo);
-    const float An = __ldg(&m.CS[nb]).z;
-    const float w0 = len * (mu[nb] / An - mj0 / Aj);
-    const float w1 = len * (mu[n + nb] / An - mj1 / Aj);
-    const float w2 = len * (mu[2 * n + nb] / An - mj2 / Aj);
-    const Side<F3> R3 = constant<F3>(R.s);
-    const F3 dxi = (R3.xi - L3.xi) + F3(R.xlo - L.xlo);
-    F3 F[3];
-    roe_flux<F3>(L3, R3, dxi, F3(m.gf), F3(nx), F3(ny), F3(m.hsmf), F);
-    g0 += w0 * F[0].d[0] + w1 * F[1].d[0] + w2 * F[2].d[0];
-    g1 += w0 * F[0].d[1] + w1 * F[1].d[1] + w2 * F[2].d[1];
-    g2 += w0 * F[0].d[2] + w1 * F[1].d[2] + w2 * F[2].d[2];
-  }
-  if (!L.s.dry) {
+    for (int k = 0; k < NS; ++k) {
+      const float4 sl = __ldg(&m.SL[(size_t)k * n + j]);
+      const int32_t nb = slot_nb(sl);
+      if (nb < 0) continue;   // no face, or a boundary face (k_vjp_bnd_f32)
+      const float nx = sl.x, ny = sl.y, len = sl.z;
+      const SideF32 R = make_side_f32(__ldg(&Q.x[nb]), __ldg(&m.CP[nb]), m.hsmf, m.hsmLo);
+      const float An = __ldg(&m.CS[nb]).z;
+      const float w0 = len * (mu[nb] / An - mj0 / Aj);
+      const float w1 = len * (mu[n + nb] / An - mj1 / Aj);
+      const float w2 = len * (mu[2 * n + nb] / An - mj2 / Aj);
+      if (!R.s.dry) {
+        roe_wet_vjp_f32(L.s, o, R.s, (R.s.xi - L.s.xi) + (R.xlo - L.xlo), m.gf, nx, ny, w0, w1, w2, b);
+      } else {
+        const Side<F3> L3 = seeded<F3>(L.s, -1);
+        const Side<F3> R3 = constant<F3>(R.s);
+        const F3 dxi = (R3.xi - L3.xi) + F3(R.xlo - L.xlo);
+        F3 F[3];
+        roe_flux<F3>(L3, R3, dxi, F3(m.gf), F3(nx), F3(ny), F3(m.hsmf), F);
+        g0 += w0 * F[0].d[0] + w1 * F[1].d[0] + w2 * F[2].d[0];
+        g1 += w0 * F[0].d[1] + w1 * F[1].d[1] + w2 * F[2].d[1];
+        g2 += w0 * F[0].d[2] + w1 * F[1].d[2] + w2 * F[2].d[2];
+      }
+    }
+    float gx, gu, gv;
+    own_vjp_f32(L.s, o, m.gf, b, gx, gu, gv);
+    g0 += gx;
+    g1 += gu;
+    g2 += gv;
     const float hu = L.s.hu, hv = L.s.hv, man = cp.w;
     const float s2 = hu * hu + hv * hv + eps_c<float>();
     const float hp = L.s.h + m.hsmf;
