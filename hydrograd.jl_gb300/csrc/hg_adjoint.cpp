@@ -39,7 +39,12 @@ struct AdjointBuffers {
   size_t probeCap = 0, obsCap = 0;
   double* segTot = nullptr;      // FP32C: inlet totals of a segment's states
   size_t segTotCap = 0;
+  cudaStream_t side = nullptr;   // FP32C: the boundary VJP beside the interior one
+  cudaEvent_t evFork = nullptr, evJoin = nullptr;
   ~AdjointBuffers() {
+    if (evFork) cudaEventDestroy(evFork);
+    if (evJoin) cudaEventDestroy(evJoin);
+    if (side) cudaStreamDestroy(side);
     for (void* p : fixed) cudaFree(p);
     cudaFree(ckpt);
     cudaFree(seg);
@@ -133,21 +138,52 @@ int setup(hg_ctx* c) {
   a.inletUOff = dUOff;
   a.inletUCell = dUCell;
   a.inletUCoef = dUCoef;
-  // Cells with a boundary face, in device order.
-  std::vector<int32_t> bnd;
+  // Cells with a boundary face, in device order, with the inlet (group,
+  // sum L^(5/3)) pairs of each.
+  std::map<int, std::vector<std::pair<int32_t, double>>> inletOf;   // device cell -> pairs
+  for (size_t g = 0; g + 1 < uOff.size(); ++g)
+    for (int32_t u = uOff[g]; u < uOff[g + 1]; ++u) inletOf[uCell[u]].push_back({(int32_t)g, uCoef[u]});
+  std::vector<int32_t> bnd, bOff(1, 0), bGrp;
+  std::vector<double> bCoef;
   for (int i = 0; i < N; ++i) {
     const int o = c->perm[i];
     for (int k = 0; k < m.ncf[o]; ++k)
       if (m.nbr[(size_t)o * 8 + k] < 0) {
         bnd.push_back(i);
+        auto it = inletOf.find(i);
+        if (it != inletOf.end())
+          for (auto& pr : it->second) {
+            bGrp.push_back(pr.first);
+            bCoef.push_back(pr.second);
+          }
+        bOff.push_back((int32_t)bGrp.size());
         break;
       }
   }
-  int32_t* dBnd;
+  int32_t *dBnd, *dBOff, *dBGrp;
+  double* dBCoef;
   ADJ_CUDA(c, falloc(b, &dBnd, bnd.size()));
+  ADJ_CUDA(c, falloc(b, &dBOff, bOff.size()));
+  ADJ_CUDA(c, falloc(b, &dBGrp, bGrp.size()));
+  ADJ_CUDA(c, falloc(b, &dBCoef, bCoef.size()));
   if (!bnd.empty()) ADJ_CUDA(c, cudaMemcpy(dBnd, bnd.data(), bnd.size() * 4, cudaMemcpyHostToDevice));
+  ADJ_CUDA(c, cudaMemcpy(dBOff, bOff.data(), bOff.size() * 4, cudaMemcpyHostToDevice));
+  if (!bGrp.empty()) {
+    ADJ_CUDA(c, cudaMemcpy(dBGrp, bGrp.data(), bGrp.size() * 4, cudaMemcpyHostToDevice));
+    ADJ_CUDA(c, cudaMemcpy(dBCoef, bCoef.data(), bCoef.size() * 8, cudaMemcpyHostToDevice));
+  }
   a.bndCells = dBnd;
   a.nBndCells = (int32_t)bnd.size();
+  a.bndInOff = dBOff;
+  a.bndInGrp = dBGrp;
+  a.bndInCoef = dBCoef;
+  ADJ_CUDA(c, falloc(b, &a.bndG, (size_t)5 * bnd.size()));
+  ADJ_CUDA(c, falloc(b, &a.grpTA, (size_t)c->dm.nInlet));
+  ADJ_CUDA(c, falloc(b, &a.bndTicket, 1));
+  ADJ_CUDA(c, cudaMemset(a.bndTicket, 0, sizeof(unsigned int)));
+  ADJ_CUDA(c, cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking));
+  ADJ_CUDA(c, cudaEventCreateWithFlags(&b->evFork, cudaEventDisableTiming));
+  ADJ_CUDA(c, cudaEventCreateWithFlags(&b->evJoin, cudaEventDisableTiming));
   return HG_OK;
 }
 
@@ -405,11 +441,9 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
         DevMesh m1 = dm, m0 = dm;
         m1.totalA = T1 + i * stride;
         m0.totalA = T0 + i * stride;
-        c->launches += launch_vjp_f32(m1, a, q1, mu2, nullptr, mu1, 0.5f, 0.0f, 0.5f * dtf, st);
-        launch_inlet_adjoint_f32(m1, a, q1, mu1, 0.5 * dt, st);
-        c->launches += launch_vjp_f32(m0, a, q0, mu1, mu2, mu2, 1.0f, 0.5f, dtf, st);
-        launch_inlet_adjoint_f32(m0, a, q0, mu2, dt, st);
-        c->launches += 2 * dm.nInlet;
+        c->launches += launch_vjp_f32(m1, a, q1, mu2, nullptr, mu1, 0.5f, 0.0f, 0.5 * dt, st, b->side, b->evFork,
+                                      b->evJoin);
+        c->launches += launch_vjp_f32(m0, a, q0, mu1, mu2, mu2, 1.0f, 0.5f, dt, st, b->side, b->evFork, b->evJoin);
         if (s >= 1 && P > 0) {
           launch_probe_adjoint_f32(dm, q0, mu2, pc, b->obs + (size_t)(s - 1) * P, scale, st);
           c->launches += 1;

@@ -141,86 +141,104 @@ __global__ void __launch_bounds__(kBlock, vjp_min_blocks<NS>()) k_vjp_f32(DevMes
   out[2 * n + j] = mask * (cSelf * mj2 + cExtra * e2 + beta * g2);
 }
 
-// Boundary faces of the cells that have any (one thread per such cell, after
-// k_vjp_f32 on the same stream): ghost-state duals in the own state, n, zb, Q
-// and total_A; adds to out[j] and the n / zb accumulators, and leaves the
-// Q / total_A cotangents per boundary face for k_inlet_adjoint_f32.
+// Boundary faces of the cells that have any (one thread per such cell; runs
+// beside k_vjp_f32, which reads none of what it writes): ghost-state duals in
+// the own state, n, zb, Q and total_A.  Leaves the cell's terms in bndG and
+// the Q / total_A cotangents per boundary face; the last block to finish sums
+// the latter per inlet group (gQ += beta sum, grpTA = sum) in face order.
 template <int NS>
 __global__ void __launch_bounds__(64) k_vjp_bnd_f32(DevMesh m, AdjDev a, StateF32 Q, const float* __restrict__ mu,
-                                                    float* out, float beta) {
+                                                    double betaD) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < a.nBndCells) {
+    const int j = a.bndCells[i];
+    const int n = m.n;
+    const float4 cp = __ldg(&m.CP[j]);
+    const SideF32 L = make_side_f32(__ldg(&Q.x[j]), cp, m.hsmf, m.hsmLo);
+    const float Aj = __ldg(&m.CS[j]).z;
+    const float mj0 = mu[j], mj1 = mu[n + j], mj2 = mu[2 * n + j];
+    float g0 = 0.0f, g1 = 0.0f, g2 = 0.0f, gn = 0.0f, gzb = 0.0f;
+#pragma unroll
+    for (int k = 0; k < NS; ++k) {
+      const float4 sl = __ldg(&m.SL[(size_t)k * n + j]);
+      const int32_t nb = slot_nb(sl);
+      if (nb >= 0 || nb == kNoFace) continue;
+      const float nx = sl.x, ny = sl.y, len = sl.z;
+      const int32_t bf = boundary_index(nb);
+      const int32_t info = m.bfInfo[bf], type = info & 3, grp = info >> 2;
+      const float w0 = -len * mj0 / Aj, w1 = -len * mj1 / Aj, w2 = -len * mj2 / Aj;
+      const Side<F7> L7 = seeded<F7>(L.s, 4);
+      const F7 man = F7::seed(cp.w, 3);
+      const F7 qin = F7::seed(type == kBcInletQ ? (float)m.inletQ[grp] : 0.0f, 5);
+      const F7 ta = F7::seed(type == kBcInletQ ? (float)m.totalA[grp] : 1.0f, 6);
+      const Side<F7> R7 = ghost_state<F7>(L7, type, F7(nx), F7(ny), F7(m.hsmf),
+                                          F7(type == kBcExitH ? (float)m.exitWse[grp] : 0.0f), qin, ta,
+                                          F7(m.bfLp23f[bf]), man);
+      F7 ex(L.excess);
+      if (L.s.dry) ex.d[0] = -1.0f;   // excess = h_small - (xi + hstill) for a dry cell
+      const F7 dxi = (R7.h - L7.h) + ex;
+      F7 F[3];
+      roe_flux<F7>(L7, R7, dxi, F7(m.gf), F7(nx), F7(ny), F7(m.hsmf), F);
+      float c[7];
+#pragma unroll
+      for (int d = 0; d < 7; ++d) c[d] = w0 * F[0].d[d] + w1 * F[1].d[d] + w2 * F[2].d[d];
+      g0 += c[0]; g1 += c[1]; g2 += c[2];
+      gn += c[3];
+      gzb += c[4];
+      a.bfGradQ[bf] = (double)c[5];
+      a.bfGradTA[bf] = (double)c[6];
+    }
+    float* o = a.bndG + (size_t)5 * i;
+    o[0] = g0; o[1] = g1; o[2] = g2; o[3] = gn; o[4] = gzb;
+  }
+  if (m.nInlet == 0) return;
+  __shared__ int isLast;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) isLast = (atomicAdd(a.bndTicket, 1u) == gridDim.x - 1);
+  __syncthreads();
+  if (!isLast) return;
+  __threadfence();
+  for (int g = 0; g < m.nInlet; ++g) {
+    double sTA = 0.0, sQ = 0.0;
+    for (int e = m.inletOff[g] + threadIdx.x; e < m.inletOff[g + 1]; e += blockDim.x) {
+      const int bf = a.inletBf[e];
+      sTA += __ldcg(&a.bfGradTA[bf]);
+      sQ += __ldcg(&a.bfGradQ[bf]);
+    }
+    const double tTA = block_sum(sTA);
+    const double tQ = block_sum(sQ);
+    if (threadIdx.x == 0) {
+      a.grpTA[g] = tTA;
+      a.gQ[g] += betaD * tQ;
+    }
+  }
+  if (threadIdx.x == 0) *a.bndTicket = 0u;
+}
+
+// After both VJP kernels: each boundary cell's terms into out (when wet) and
+// the n / zb accumulators, then its inlet total_A terms (bc_2D.jl:673-676:
+// total_A = sum L^(5/3) h / n over the group's wet cells) into out and gN.
+__global__ void __launch_bounds__(128) k_vjp_combine_f32(DevMesh m, AdjDev a, StateF32 Q, float* out, float beta,
+                                                         double betaD) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.nBndCells) return;
   const int j = a.bndCells[i];
   const int n = m.n;
-  const float4 cp = __ldg(&m.CP[j]);
-  const SideF32 L = make_side_f32(__ldg(&Q.x[j]), cp, m.hsmf, m.hsmLo);
-  const float Aj = __ldg(&m.CS[j]).z;
-  const float mj0 = mu[j], mj1 = mu[n + j], mj2 = mu[2 * n + j];
-  float g0 = 0.0f, g1 = 0.0f, g2 = 0.0f, gn = 0.0f, gzb = 0.0f;
-#pragma unroll
-  for (int k = 0; k < NS; ++k) {
-    const float4 sl = __ldg(&m.SL[(size_t)k * n + j]);
-    const int32_t nb = slot_nb(sl);
-    if (nb >= 0 || nb == kNoFace) continue;
-    const float nx = sl.x, ny = sl.y, len = sl.z;
-    const int32_t bf = boundary_index(nb);
-    const int32_t info = m.bfInfo[bf], type = info & 3, grp = info >> 2;
-    const float w0 = -len * mj0 / Aj, w1 = -len * mj1 / Aj, w2 = -len * mj2 / Aj;
-    const Side<F7> L7 = seeded<F7>(L.s, 4);
-    const F7 man = F7::seed(cp.w, 3);
-    const F7 qin = F7::seed(type == kBcInletQ ? (float)m.inletQ[grp] : 0.0f, 5);
-    const F7 ta = F7::seed(type == kBcInletQ ? (float)m.totalA[grp] : 1.0f, 6);
-    const Side<F7> R7 = ghost_state<F7>(L7, type, F7(nx), F7(ny), F7(m.hsmf),
-                                        F7(type == kBcExitH ? (float)m.exitWse[grp] : 0.0f), qin, ta,
-                                        F7(m.bfLp23f[bf]), man);
-    F7 ex(L.excess);
-    if (L.s.dry) ex.d[0] = -1.0f;   // excess = h_small - (xi + hstill) for a dry cell
-    const F7 dxi = (R7.h - L7.h) + ex;
-    F7 F[3];
-    roe_flux<F7>(L7, R7, dxi, F7(m.gf), F7(nx), F7(ny), F7(m.hsmf), F);
-    float c[7];
-#pragma unroll
-    for (int d = 0; d < 7; ++d) c[d] = w0 * F[0].d[d] + w1 * F[1].d[d] + w2 * F[2].d[d];
-    g0 += c[0]; g1 += c[1]; g2 += c[2];
-    gn += c[3];
-    gzb += c[4];
-    a.bfGradQ[bf] = (double)c[5];
-    a.bfGradTA[bf] = (double)c[6];
-  }
-  if (gn != 0.0f) acc_add(&a.accF[j], beta, gn);
-  if (gzb != 0.0f) acc_add(&a.accF[(size_t)3 * n + j], beta, gzb);
-  if (!L.s.dry) {
-    out[j] += beta * g0;
-    out[n + j] += beta * g1;
-    out[2 * n + j] += beta * g2;
-  }
-}
-
-__global__ void __launch_bounds__(1024) k_inlet_adjoint_f32(DevMesh m, AdjDev a, StateF32 Q, float* out, double beta,
-                                                           int g) {
-  const int o0 = m.inletOff[g], o1 = m.inletOff[g + 1];
-  double sTA = 0.0, sQ = 0.0;
-  for (int i = o0 + threadIdx.x; i < o1; i += blockDim.x) {
-    const int bf = a.inletBf[i];
-    sTA += a.bfGradTA[bf];
-    sQ += a.bfGradQ[bf];
-  }
-  __shared__ double tot;
-  const double t1 = block_sum(sTA);
-  if (threadIdx.x == 0) tot = t1;
-  const double t2 = block_sum(sQ);
-  if (threadIdx.x == 0) a.gQ[g] += beta * t2;
-  __syncthreads();
-  const double gTA = tot;
-  const int u0 = a.inletUOff[g], u1 = a.inletUOff[g + 1];
-  for (int i = u0 + threadIdx.x; i < u1; i += blockDim.x) {
-    const int c = a.inletUCell[i];
-    const float4 cp = m.CP[c];
-    const SideF32 L = make_side_f32(Q.x[c], cp, m.hsmf, m.hsmLo);
-    if (L.s.dry) continue;
-    const double coef = a.inletUCoef[i], n = cp.w;
-    out[c] += (float)(beta * gTA * coef / n);
-    a.gN[c] += beta * gTA * (-coef * (double)L.s.h / (n * n));
+  const float4 cp = m.CP[j];
+  const SideF32 L = make_side_f32(Q.x[j], cp, m.hsmf, m.hsmLo);
+  const float* g = a.bndG + (size_t)5 * i;
+  if (g[3] != 0.0f) acc_add(&a.accF[j], beta, g[3]);
+  if (g[4] != 0.0f) acc_add(&a.accF[(size_t)3 * n + j], beta, g[4]);
+  if (L.s.dry) return;
+  out[j] += beta * g[0];
+  out[n + j] += beta * g[1];
+  out[2 * n + j] += beta * g[2];
+  for (int p = a.bndInOff[i]; p < a.bndInOff[i + 1]; ++p) {
+    const double gTA = a.grpTA[a.bndInGrp[p]];
+    const double coef = a.bndInCoef[p], nm = cp.w;
+    out[j] += (float)(betaD * gTA * coef / nm);
+    a.gN[j] += betaD * gTA * (-coef * (double)L.s.h / (nm * nm));
   }
 }
 
@@ -271,24 +289,33 @@ __global__ void k_fold_accumulators_f32(DevMesh m, AdjDev a) {
 
 }  // namespace
 
-int launch_vjp_f32(const DevMesh& m, const AdjDev& a, StateF32 Q, const float* mu, const float* extra, float* out,
-                   float cSelf, float cExtra, float beta, cudaStream_t st) {
+namespace {
+template <int NS>
+int launch_vjp_ns(const DevMesh& m, const AdjDev& a, StateF32 Q, const float* mu, const float* extra, float* out,
+                  float cSelf, float cExtra, double betaD, cudaStream_t st, cudaStream_t side, cudaEvent_t evFork,
+                  cudaEvent_t evJoin) {
+  const float beta = (float)betaD;
   const int nbb = (a.nBndCells + 63) / 64;
-  if (m.nslot <= 3) {
-    k_vjp_f32<3><<<blocks_for(m.n), kBlock, 0, st>>>(m, a, Q, mu, extra, out, cSelf, cExtra, beta);
-    if (nbb) k_vjp_bnd_f32<3><<<nbb, 64, 0, st>>>(m, a, Q, mu, out, beta);
-  } else if (m.nslot <= 4) {
-    k_vjp_f32<4><<<blocks_for(m.n), kBlock, 0, st>>>(m, a, Q, mu, extra, out, cSelf, cExtra, beta);
-    if (nbb) k_vjp_bnd_f32<4><<<nbb, 64, 0, st>>>(m, a, Q, mu, out, beta);
-  } else {
-    k_vjp_f32<8><<<blocks_for(m.n), kBlock, 0, st>>>(m, a, Q, mu, extra, out, cSelf, cExtra, beta);
-    if (nbb) k_vjp_bnd_f32<8><<<nbb, 64, 0, st>>>(m, a, Q, mu, out, beta);
+  if (nbb) {
+    cudaEventRecord(evFork, st);
+    cudaStreamWaitEvent(side, evFork, 0);
+    k_vjp_bnd_f32<NS><<<nbb, 64, 0, side>>>(m, a, Q, mu, betaD);
+    cudaEventRecord(evJoin, side);
   }
-  return nbb ? 2 : 1;
+  k_vjp_f32<NS><<<blocks_for(m.n), kBlock, 0, st>>>(m, a, Q, mu, extra, out, cSelf, cExtra, beta);
+  if (!nbb) return 1;
+  cudaStreamWaitEvent(st, evJoin, 0);
+  k_vjp_combine_f32<<<(a.nBndCells + 127) / 128, 128, 0, st>>>(m, a, Q, out, beta, betaD);
+  return 3;
 }
-void launch_inlet_adjoint_f32(const DevMesh& m, const AdjDev& a, StateF32 Q, float* out, double beta,
-                              cudaStream_t st) {
-  for (int g = 0; g < m.nInlet; ++g) k_inlet_adjoint_f32<<<1, 1024, 0, st>>>(m, a, Q, out, beta, g);
+}  // namespace
+
+int launch_vjp_f32(const DevMesh& m, const AdjDev& a, StateF32 Q, const float* mu, const float* extra, float* out,
+                   float cSelf, float cExtra, double betaD, cudaStream_t st, cudaStream_t side, cudaEvent_t evFork,
+                   cudaEvent_t evJoin) {
+  if (m.nslot <= 3) return launch_vjp_ns<3>(m, a, Q, mu, extra, out, cSelf, cExtra, betaD, st, side, evFork, evJoin);
+  if (m.nslot <= 4) return launch_vjp_ns<4>(m, a, Q, mu, extra, out, cSelf, cExtra, betaD, st, side, evFork, evJoin);
+  return launch_vjp_ns<8>(m, a, Q, mu, extra, out, cSelf, cExtra, betaD, st, side, evFork, evJoin);
 }
 void launch_probe_loss_f32(const DevMesh& m, const AdjDev& a, StateF32 Q, const int32_t* probes, const double* obs,
                            int32_t nprobe, cudaStream_t st) {

@@ -25,9 +25,19 @@ struct AdjDev {
   // FP32-compensated path: per-cell sums of gN, gS0x, gS0y, gZb ([4][n]) as
   // unevaluated float pairs {hi, lo}, folded into the FP64 arrays at the end.
   float2* accF = nullptr;
-  // Cells with at least one boundary face, device order (FP32C boundary VJP).
+  // FP32C boundary VJP (k_vjp_bnd_f32 beside the interior VJP, then
+  // k_vjp_combine_f32): cells with at least one boundary face (device order),
+  // their boundary-face terms of the current VJP {g_xi, g_hu, g_hv, g_n, g_zb},
+  // the inlet (group, sum L^(5/3)) pairs of each (CSR), the per-group sums of
+  // the total_A cotangent, and the last-block ticket.
   const int32_t* bndCells = nullptr;
   int32_t nBndCells = 0;
+  float* bndG = nullptr;
+  const int32_t* bndInOff = nullptr;
+  const int32_t* bndInGrp = nullptr;
+  const double* bndInCoef = nullptr;
+  double* grpTA = nullptr;
+  unsigned int* bndTicket = nullptr;
 };
 
 // out_j = M(Q_j) (cSelf mu_j + cExtra extra_j + beta (J(Q)^T mu)_j), parameter
@@ -43,11 +53,13 @@ void launch_probe_loss_f64(const DevMesh& m, const AdjDev& a, const double* Q, c
 void launch_probe_adjoint_f64(const DevMesh& m, const double* Q, double* mu, const int32_t* probes,
                               const double* obs, int32_t nprobe, double scale, cudaStream_t st);
 // FP32-compensated path: the same with packed FP32 states and FP32 cotangents.
-// Returns the launches made (interior kernel, and the boundary-cell kernel).
+// The whole VJP of one stage, inlet-Q terms included: the interior kernel on
+// st, the boundary-face kernel on `side` at the same time (fork / join through
+// the two events), then the combine kernel on st.  beta = betaD as FP32.
+// Returns the launches made.
 int launch_vjp_f32(const DevMesh& m, const AdjDev& a, StateF32 Q, const float* mu, const float* extra, float* out,
-                   float cSelf, float cExtra, float beta, cudaStream_t st);
-void launch_inlet_adjoint_f32(const DevMesh& m, const AdjDev& a, StateF32 Q, float* out, double beta,
-                              cudaStream_t st);
+                   float cSelf, float cExtra, double betaD, cudaStream_t st, cudaStream_t side, cudaEvent_t evFork,
+                   cudaEvent_t evJoin);
 void launch_probe_loss_f32(const DevMesh& m, const AdjDev& a, StateF32 Q, const int32_t* probes, const double* obs,
                            int32_t nprobe, cudaStream_t st);
 // Probes grouped by cell: cell[u] (distinct, device order) holds probes idx[off[u] .. off[u+1]).
