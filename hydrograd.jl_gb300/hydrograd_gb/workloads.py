@@ -9,7 +9,8 @@ harness (tests, benchmark, oracle) sees the same inputs for the same seed.
 * :func:`river_triangles` n x n grid split into 2 triangles per quad, nodes
   jittered by +-0.2 dx over 2 km x 2 km; bed = 1e-3 slope + 20 Gaussian bumps;
   5 Voronoi Manning zones; inlet-Q on the west edge, exit-H on the east edge,
-  walls elsewhere; dry except a 1.5 m pool that touches the inlet.
+  walls elsewhere; a lake at rest with its surface raised 1.5 m in a pool disk
+  (dry_land=True: dry except the pool).
 
 A case is a dict with the mesh arrays of ``hg_mesh_desc`` plus parameters:
 mat_id, manning_zones, inlet_q, exit_wse, wstill (per cell) and Q0.
@@ -220,27 +221,36 @@ def river_triangles(n=708, L=2000.0, seed=0, inlet_q=500.0, exit_wse=None, wstil
     return case
 
 
-def probes_and_perturbation(case, n_probe=64, seed=1, zb_sigma=0.05, rim_width=None):
+def probes_and_perturbation(case, n_probe=64, seed=1, zb_sigma=0.05, rim_width=None, inlet_share=0.0):
     """Seeded probe cells and a per-cell bed perturbation drawn in FP32 with
     standard deviation zb_sigma.  The probes are wet cells within rim_width
     (default: 4 mean cell sizes) of the pool's rim, where the released bore
-    passes in the first steps, so that a short run's loss sees the flow."""
+    passes in the first steps, so that a short run's loss sees the flow; a
+    fraction inlet_share of them is taken instead from the wet cells within
+    rim_width of the west edge (the inlet-Q boundary of river_triangles)."""
     rs = Stream(seed)
     N = len(case["cell_node_count"])
     Q0 = case["Q0"]
     wet = Q0[:N] + case["wstill"] - case["zb_cells"] > 2 * H_SMALL
     cand = np.nonzero(wet)[0]
+    cx, cy = cell_centroids(case)
+    xyz = case["node_xyz"]
+    cell = np.sqrt((np.ptp(xyz[:, 0]) * np.ptp(xyz[:, 1])) / N)
+    w = 4.0 * cell if rim_width is None else rim_width
+    n_inlet = int(round(n_probe * inlet_share))
+    inlet = np.zeros(0, np.int64)
+    if n_inlet > 0:
+        west = np.nonzero(wet & (cx < xyz[:, 0].min() + w))[0]
+        pick = np.unique((rs.uniform(4 * n_inlet) * len(west)).astype(np.int64))[:n_inlet]
+        inlet = west[np.sort(pick)]
+        n_probe -= len(inlet)
     if "pool_center" in case:
-        cx, cy = cell_centroids(case)
-        xyz = case["node_xyz"]
-        cell = np.sqrt((np.ptp(xyz[:, 0]) * np.ptp(xyz[:, 1])) / N)
-        w = 4.0 * cell if rim_width is None else rim_width
         r = np.hypot(cx - case["pool_center"][0], cy - case["pool_center"][1])
         rim = np.nonzero(wet & (np.abs(r - case["pool_radius"]) < w))[0]
         if len(rim) >= n_probe:
             cand = rim
     pick = np.unique((rs.uniform(4 * n_probe) * len(cand)).astype(np.int64))[:n_probe]
-    probes = cand[np.sort(pick)].astype(np.int32)
+    probes = np.unique(np.concatenate([inlet, cand[np.sort(pick)]])).astype(np.int32)
     # Box-Muller from two uniform draws, rounded to float32.
     u1 = np.maximum(rs.uniform(N), 1e-300)
     u2 = rs.uniform(N)
