@@ -176,7 +176,8 @@ __global__ void __launch_bounds__(64) k_vjp_bnd_f32(DevMesh m, AdjDev a, StateF3
                                           F7(m.bfLp23f[bf]), man);
       F7 ex(L.excess);
       if (L.s.dry) ex.d[0] = -1.0f;   // excess = h_small - (xi + hstill) for a dry cell
-      const F7 dxi = (R7.h - L7.h) + ex;
+      F7 dxi = (R7.h - L7.h) + ex;
+      if (type == kBcExitH && !R7.dry) dxi.v = m.bfExitRel[bf] - (L.s.xi + L.xlo);   // as the forward pass
       F7 F[3];
       roe_flux<F7>(L7, R7, dxi, F7(m.gf), F7(nx), F7(ny), F7(m.hsmf), F);
       float c[7];

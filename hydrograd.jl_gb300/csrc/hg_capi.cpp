@@ -86,6 +86,21 @@ std::vector<T> to_device_order(const hg_ctx* c, const T* user) {
   return r;
 }
 
+// The FP32 path's exit-H surface offset xi_ghost = (WSE - zb) - hstill per
+// exit face, in FP64 (bc_2D.jl exit-H ghost depth; hstill as the RHS sees it).
+// Formed in FP32 from a rounded WSE and zb it would carry an error of a few
+// 1e-7 m, which the Roe dissipation turns into a spurious outflow.
+int upload_exit_rel(hg_ctx* c) {
+  if (!c->d_bfExitRel) return HG_OK;
+  for (size_t e = 0; e < c->exitBf.size(); ++e) {
+    const int cell = c->exitCell[e];
+    c->h_bfExitRel[c->exitBf[e]] = (float)((c->exitWse[c->exitGrp[e]] - c->zbCell[cell]) - c->hstill[cell]);
+  }
+  HG_CUDA(c, upload(c, c->d_bfExitRel, c->h_bfExitRel));
+  HG_CUDA(c, cudaStreamSynchronize(c->stream));
+  return HG_OK;
+}
+
 int upload_cells(hg_ctx* c) {
   // FP64 and FP32 copies of the per-cell parameters, in device order.
   std::vector<double> hst = to_device_order(c, c->hstill.data());
@@ -109,14 +124,14 @@ int upload_cells(hg_ctx* c) {
   HG_CUDA(c, upload(c, c->d_CP, c->h_CP));
   HG_CUDA(c, upload(c, c->d_CS, c->h_CS));
   HG_CUDA(c, cudaStreamSynchronize(c->stream));
-  return HG_OK;
+  return upload_exit_rel(c);
 }
 
 int upload_boundary_values(hg_ctx* c) {
   HG_CUDA(c, upload(c, c->d_inletQ, c->inletQ));
   HG_CUDA(c, upload(c, c->d_exitWse, c->exitWse));
   HG_CUDA(c, cudaStreamSynchronize(c->stream));
-  return HG_OK;
+  return upload_exit_rel(c);
 }
 
 int check_flags(hg_ctx* c) {
@@ -748,6 +763,11 @@ int ctx_setup_device(hg_ctx* c) {
     const int bi = m.faceBnd[f];
     const int type = m.bnd[bi].bc;
     bfInfo[bfOf[f]] = type | (groupOf[bi] << 2);
+    if (type == HG_BC_EXITH) {
+      c->exitBf.push_back(bfOf[f]);
+      c->exitCell.push_back(m.faceC0[f]);
+      c->exitGrp.push_back(groupOf[bi]);
+    }
     if (type == HG_BC_INLETQ) {
       bfLp23[bfOf[f]] = std::pow(m.faceLen[f], 2.0 / 3.0);
       bfLp53[bfOf[f]] = std::pow(m.faceLen[f], 5.0 / 3.0);
@@ -796,6 +816,8 @@ int ctx_setup_device(hg_ctx* c) {
   HG_CUDA(c, dalloc(c, &d_SL, nb.size()));
   HG_CUDA(c, dalloc(c, &d_area, (size_t)N));
   HG_CUDA(c, dalloc(c, &d_bfInfo, (size_t)std::max(nbf, 1)));
+  HG_CUDA(c, dalloc(c, &c->d_bfExitRel, (size_t)std::max(nbf, 1)));
+  c->h_bfExitRel.assign(std::max(nbf, 1), 0.0f);
   HG_CUDA(c, dalloc(c, &d_lp23, (size_t)std::max(nbf, 1)));
   HG_CUDA(c, dalloc(c, &d_lp23f, (size_t)std::max(nbf, 1)));
   HG_CUDA(c, dalloc(c, &d_bflp53, (size_t)std::max(nbf, 1)));
@@ -892,6 +914,7 @@ int ctx_setup_device(hg_ctx* c) {
   dm.nb = d_nb; dm.snx = d_snx; dm.sny = d_sny; dm.slen = d_slen;
   dm.SL = d_SL;
   dm.bfInfo = d_bfInfo; dm.bfLp23 = d_lp23; dm.bfLp23f = d_lp23f; dm.bfLp53 = d_bflp53;
+  dm.bfExitRel = c->d_bfExitRel;
   dm.inletOff = d_inletOff; dm.inletCell = d_inletCell; dm.inletLp53 = d_lp53;
   dm.area = d_area; dm.hst = c->d_hst; dm.zb = c->d_zb; dm.man = c->d_man; dm.s0x = c->d_s0x; dm.s0y = c->d_s0y;
   dm.CP = c->d_CP; dm.CS = c->d_CS;

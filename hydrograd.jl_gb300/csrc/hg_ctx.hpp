@@ -31,6 +31,11 @@ struct hg_ctx {
   // FP32 packed cell records (device order), host copies kept alive across async uploads
   std::vector<float4> h_CP, h_CS;
   std::vector<float> h_area;   // device order
+  // Exit-H boundary faces: boundary-face index, caller cell id, group; and the
+  // FP32 path's (WSE - zb) - hstill per boundary face, formed in FP64.
+  std::vector<int32_t> exitBf, exitCell, exitGrp;
+  std::vector<float> h_bfExitRel;
+  float* d_bfExitRel = nullptr;
   // Writable device parameter arrays
   double *d_hst = nullptr, *d_zb = nullptr, *d_man = nullptr, *d_s0x = nullptr, *d_s0y = nullptr;
   float4 *d_CP = nullptr, *d_CS = nullptr;

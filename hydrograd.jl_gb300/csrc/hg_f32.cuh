@@ -96,8 +96,9 @@ __device__ __forceinline__ void df_add2(float ah, float al, float bh, float bl, 
 __device__ __forceinline__ int32_t slot_nb(float4 s) { return __float_as_int(s.w); }
 
 // Quantities of a wet cell that the Roe flux uses on every one of its faces,
-// formed once per cell: velocity, sqrt(h), pre-balanced pressure and the
-// physical flux tensor [[hu u + p, hu v], [hv u, hv v + p]].
+// formed once per cell: velocity, sqrt(h), pre-balanced pressure
+// p = g/2 (smooth_pow2(xi) + 2 xi hstill) and the advective flux tensor
+// [[hu u, hu v], [hv u, hv v]].
 struct OwnF32 {
   float u, v, s, p;
   float fxx, fxy, fyx, fyy;
@@ -110,21 +111,38 @@ __device__ __forceinline__ OwnF32 own_f32(const Side<float>& L, float g) {
   o.v = L.hv * r;
   o.s = smooth_sqrt(L.h);
   o.p = 0.5f * g * (smooth_pow2(L.xi) + 2.0f * L.xi * L.hst);
-  o.fxx = L.hu * o.u + o.p;
+  o.fxx = L.hu * o.u;
   o.fxy = L.hu * o.v;
   o.fyx = L.hv * o.u;
-  o.fyy = L.hv * o.v + o.p;
+  o.fyy = L.hv * o.v;
   return o;
+}
+
+// Well-balancing in FP32.  A cell's RHS is -sum_k F_k L_k / A, and the sum of
+// its faces' n_k L_k is zero, so subtracting the own pressure p_L n_k from
+// every face's momentum flux leaves the RHS unchanged -- but it removes the
+// large own-pressure terms (p ~ g xi hstill) whose sum cancels only to the
+// FP32 rounding of the normals and lengths, about 1e-7 of p per cell: in a
+// raised pool over a sloping bed that residual drives a spurious flow that
+// grows linearly in time.  The wet-wet flux then carries p_R - p_L, formed
+// from the exact differences of the hi + lo pairs (pressure_jump_f32); every
+// other face subtracts p_L n after the reference solver.
+__device__ __forceinline__ float pressure_jump_f32(float g, float xiL, float xiR, float dxi, float hstR,
+                                                   float dhst) {
+  // (xiR + e)^2 - (xiL + e)^2 + 2 (xiR hstR - xiL hstL)
+  //   = dxi (xiR + xiL + 2 e + 2 hstR) + 2 xiL (hstR - hstL)
+  return 0.5f * g * (dxi * ((xiR + xiL) + 2.0f * eps_c<float>() + 2.0f * hstR) + 2.0f * xiL * dhst);
 }
 
 // Roe flux of a face whose two sides are both wet -- the case in which the
 // reference solver (swe_2D_solvers.jl:79-164) takes none of its dry or wall
-// branches -- with the own cell's quantities from own_f32.  The algebra is
-// the reference's, regrouped: w1 + w2 = dxi exactly, so w1 = dxi/2 + t and
-// w2 = dxi/2 - t with t = (un dxi - nx d1 - ny d2) / (2c), and the rows of
-// R |Lambda| w are collected around w1 + w2 and w2 - w1.
+// branches -- with the own cell's quantities from own_f32, minus p_L n in the
+// momentum rows (see pressure_jump_f32; dhst = hstill_R - hstill_L).  The
+// algebra is the reference's, regrouped: w1 + w2 = dxi exactly, so
+// w1 = dxi/2 + t and w2 = dxi/2 - t with t = (un dxi - nx d1 - ny d2) / (2c),
+// and the rows of R |Lambda| w are collected around w1 + w2 and w2 - w1.
 __device__ __forceinline__ void roe_flux_wet_f32(const Side<float>& L, const OwnF32& o, const Side<float>& R,
-                                                 float dxi, float g, float nx, float ny, float F[3]) {
+                                                 float dxi, float dhst, float g, float nx, float ny, float F[3]) {
   const float rR = 1.0f / R.h;
   const float uR = R.hu * rR, vR = R.hv * rR;
   const float sR = smooth_sqrt(R.h);
@@ -142,8 +160,8 @@ __device__ __forceinline__ void roe_flux_wet_f32(const Side<float>& L, const Own
   const float A0 = sum;
   const float A1 = ny * w0 + uRoe * sum + nx * dif;
   const float A2 = -nx * w0 + vRoe * sum + ny * dif;
-  const float pR = 0.5f * g * (smooth_pow2(R.xi) + 2.0f * R.xi * R.hst);
-  const float fR1x = R.hu * uR + pR, fR2y = R.hv * vR + pR;
+  const float dp = pressure_jump_f32(g, L.xi, R.xi, dxi, R.hst, dhst);   // p_R - p_L
+  const float fR1x = R.hu * uR + dp, fR2y = R.hv * vR + dp;
   F[0] = 0.5f * ((L.hu * nx + L.hv * ny) + (R.hu * nx + R.hv * ny) - A0);
   F[1] = 0.5f * ((o.fxx * nx + o.fxy * ny) + (fR1x * nx + R.hu * vR * ny) - A1);
   F[2] = 0.5f * ((o.fyx * nx + o.fyy * ny) + (R.hv * uR * nx + fR2y * ny) - A2);
@@ -236,7 +254,9 @@ __device__ __forceinline__ void roe_wet_vjp_f32(const Side<float>& L, const OwnF
 // own state: returns d/d(xi, hu, hv).
 __device__ __forceinline__ void own_vjp_f32(const Side<float>& L, const OwnF32& o, float g, OwnAdjF32 b, float& gxi,
                                             float& ghu, float& ghv) {
-  // fxx = hu u + p, fxy = hu v, fyx = hv u, fyy = hv v + p
+  // Derivative of the reference flux, with the own pressure in the tensor:
+  // fxx = hu u + p, fxy = hu v, fyx = hv u, fyy = hv v + p.  (The forward
+  // pass's p_L n shift sums to zero over the cell's faces.)
   b.hu += o.u * b.fxx + o.v * b.fxy;
   b.hv += o.u * b.fyx + o.v * b.fyy;
   b.u += L.hu * b.fxx + L.hv * b.fyx;

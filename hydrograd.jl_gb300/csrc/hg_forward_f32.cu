@@ -31,7 +31,7 @@ inline int blocks_for(int n) { return (n + kBlock - 1) / kBlock; }
 template <int NS>
 __device__ __forceinline__ void face_sum_f32(const DevMesh& m, const float4* __restrict__ X, const float4* sX,
                                              const float4* sP, int base, int c, const SideF32& L,
-                                             const OwnF32& own, const float4 (&sl)[NS],
+                                             const OwnF32& own, float2 hstPair, const float4 (&sl)[NS],
                                              const double* __restrict__ totalA, float man, int32_t* flags, float& f0,
                                              float& f1, float& f2) {
   f0 = 0.0f; f1 = 0.0f; f2 = 0.0f;
@@ -41,7 +41,7 @@ __device__ __forceinline__ void face_sum_f32(const DevMesh& m, const float4* __r
     if (nb == kNoFace) continue;
     const float nx = sl[k].x, ny = sl[k].y, len = sl[k].z;
     Side<float> R;
-    float dxi;
+    float dxi, dhst = 0.0f;
     if (nb >= 0) {
       const unsigned int ln = (unsigned int)(nb - base);   // in-block neighbour: staged record
       float4 xr, pr;
@@ -55,6 +55,7 @@ __device__ __forceinline__ void face_sum_f32(const DevMesh& m, const float4* __r
       const SideF32 r = make_side_f32(xr, pr, m.hsmf, m.hsmLo);
       R = r.s;
       dxi = (r.s.xi - L.s.xi) + (r.xlo - L.xlo);
+      dhst = (pr.x - hstPair.x) + (pr.y - hstPair.y);   // hstill_R - hstill_L from the pairs
     } else {
       const int32_t bf = boundary_index(nb);
       const int32_t info = m.bfInfo[bf], type = info & 3, grp = info >> 2;
@@ -62,12 +63,19 @@ __device__ __forceinline__ void face_sum_f32(const DevMesh& m, const float4* __r
       R = ghost_state<float>(L.s, type, nx, ny, m.hsmf, type == kBcExitH ? (float)m.exitWse[grp] : 0.0f,
                              type == kBcInletQ ? (float)m.inletQ[grp] : 0.0f,
                              type == kBcInletQ ? (float)totalA[grp] : 1.0f, m.bfLp23f[bf], man);
-      // xi_ghost - xi = (h_ghost - h) + ((h - hstill) - xi)
+      // xi_ghost - xi = (h_ghost - h) + ((h - hstill) - xi); for a wet exit-H
+      // ghost, from (WSE - zb) - hstill formed in FP64
       dxi = (R.h - L.s.h) + L.excess;
+      if (type == kBcExitH && !R.dry) dxi = m.bfExitRel[bf] - (L.s.xi + L.xlo);
     }
     float F[3];
-    if (!L.s.dry && !R.dry) roe_flux_wet_f32(L.s, own, R, dxi, m.gf, nx, ny, F);
-    else roe_flux<float>(L.s, R, dxi, m.gf, nx, ny, m.hsmf, F);
+    if (!L.s.dry && !R.dry) {
+      roe_flux_wet_f32(L.s, own, R, dxi, dhst, m.gf, nx, ny, F);
+    } else {
+      roe_flux<float>(L.s, R, dxi, m.gf, nx, ny, m.hsmf, F);
+      F[1] -= own.p * nx;   // the own pressure shift (pressure_jump_f32)
+      F[2] -= own.p * ny;
+    }
     f0 = fmaf(F[0], len, f0);
     f1 = fmaf(F[1], len, f1);
     f2 = fmaf(F[2], len, f2);
@@ -188,7 +196,8 @@ __global__ void __launch_bounds__(kBlock, stage_min_blocks<NS>())
     const SideF32 L = make_side_f32(xin, cp, m.hsmf, m.hsmLo);
     const OwnF32 own = own_f32(L.s, m.gf);
     float f0, f1, f2;
-    face_sum_f32<NS>(m, Xin.x, sX, sP, base, c, L, own, sl, FUSED ? f.totalIn : m.totalA, cp.w, s.flags, f0, f1, f2);
+    face_sum_f32<NS>(m, Xin.x, sX, sP, base, c, L, own, make_float2(cp.x, cp.y), sl, FUSED ? f.totalIn : m.totalA,
+                     cp.w, s.flags, f0, f1, f2);
     const float A = cs.z;
     const float r0 = -f0 / A, r1 = -f1 / A, r2 = -f2 / A;
     const float fr = friction_coef(m.gf, m.kn2f, m.hsmf, cp.w, L.s.h, L.s.hu, L.s.hv);

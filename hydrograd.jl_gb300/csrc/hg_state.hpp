@@ -24,6 +24,7 @@ struct DevMesh {
   const double* bfLp23 = nullptr;    // [nbf] L^(2/3) (inlet-Q faces)
   const double* bfLp53 = nullptr;    // [nbf] L^(5/3) (inlet-Q faces)
   const float* bfLp23f = nullptr;
+  const float* bfExitRel = nullptr;  // [nbf] exit-H faces: (WSE - zb) - hstill of the face's cell, formed in FP64
   const int32_t* inletOff = nullptr; // [nInlet+1] CSR over inlet faces in NodeString order
   const int32_t* inletCell = nullptr;
   const double* inletLp53 = nullptr; // L^(5/3)
