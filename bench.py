@@ -111,33 +111,48 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.rows)}
 
 
-def dist_setup():
+def dist_setup(backend=None):
+    """(rank, world size, local rank, torch.distributed or None) of a torchrun
+    launch; NCCL on the GPUs, or the backend named (gloo: CPU tensors)."""
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     if ws <= 1:
         return 0, 1, 0, None
     import torch
     import torch.distributed as dist
     rank, local = int(os.environ["RANK"]), int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(local)
-    dist.init_process_group("nccl")
+    backend = backend or os.environ.get("HG_DIST_BACKEND", "nccl")
+    if backend == "nccl":
+        torch.cuda.set_device(local)
+    dist.init_process_group(backend)
     return rank, ws, local, dist
+
+
+def _on_gpu(dist):
+    return dist.get_backend() == "nccl"
 
 
 def barrier(dist):
     if dist is not None:
         import torch
-        t = torch.zeros(1, device="cuda")
+        t = torch.zeros(1, device="cuda" if _on_gpu(dist) else "cpu")
         dist.all_reduce(t)
-        torch.cuda.synchronize()
+        if _on_gpu(dist):
+            torch.cuda.synchronize()
 
 
 def max_over_ranks(dist, v):
     if dist is None:
         return v
     import torch
-    t = torch.tensor([v], device="cuda", dtype=torch.float64)
+    t = torch.tensor([v], device="cuda" if _on_gpu(dist) else "cpu", dtype=torch.float64)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def replica_value(ws, units_per_rank, seconds):
+    """Whole-job throughput of ws replicas: every rank processes units_per_rank
+    in its own time; the job's time is the slowest rank's (max over ranks)."""
+    return ws * units_per_rank / seconds
 
 
 def make_ctx(case, precision, device):
@@ -233,7 +248,7 @@ def run_ours(args):
         launches = ctx.launch_count() - l0 - 2 * steps   # minus the L2 flushes (write + read kernel)
         ms = max_over_ranks(dist, ms)
         barrier(dist)
-        out[prec] = dict(ms=ms, steps=steps, value=ws * N * steps / (ms * 1e-3), launches=launches,
+        out[prec] = dict(ms=ms, steps=steps, value=replica_value(ws, N * steps, ms * 1e-3), launches=launches,
                          clocks=sampler.summary() if sampler else None, state=ctx.download(),
                          sim_time=ctx.elapsed_time())
         # Continuous run without flushes (L2 kept warm), for reference.
@@ -268,7 +283,7 @@ def run_ours(args):
         q, _ = ctx.integrate(host.array, args.e2e_chunk, cfl=0.4)
         host.array[:] = q
     el = max_over_ranks(dist, time.perf_counter() - t0)
-    e2e = {"value": ws * N * args.e2e_chunk * calls / el, "unit": UNIT,
+    e2e = {"value": replica_value(ws, N * args.e2e_chunk * calls, el), "unit": UNIT,
            "h2d_bytes_per_step": 3 * N * 8 / args.e2e_chunk, "d2h_bytes_per_step": 3 * N * 8 / args.e2e_chunk,
            "calls": calls, "steps_per_call": args.e2e_chunk}
     # Forward + adjoint: hg_loss_and_grad over adj_steps fixed-dt steps (the CFL
@@ -293,7 +308,7 @@ def run_ours(args):
             r = ctx.loss_and_grad(case["Q0"], args.adj_steps, dt_adj, probes, obs, ckpt_every=50)
             el = max_over_ranks(dist, time.perf_counter() - t0)
             grads[prec] = r
-            adj[prec] = {"value": ws * N * args.adj_steps / el, "seconds": el, "steps": args.adj_steps}
+            adj[prec] = {"value": replica_value(ws, N * args.adj_steps, el), "seconds": el, "steps": args.adj_steps}
         g32, g64 = grads["fp32c"], grads["fp64"]
         zones = case["mat_id"]
         gz32 = np.array([g32["g_manning"][zones == z].sum() for z in range(len(case["manning_zones"]))])
