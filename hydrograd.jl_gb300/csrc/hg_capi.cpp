@@ -366,33 +366,99 @@ int hg_mesh_order(const hg_mesh* mesh, int32_t order, int32_t* perm) {
   return HG_OK;
 }
 
-int hg_create(const hg_mesh_desc* desc, const hg_consts* consts, int32_t precision, int32_t device, hg_ctx** out) {
-  if (!desc || !consts || !out) return fail(nullptr, HG_ERR_ARG, "hg_create: null argument");
-  *out = nullptr;
-  if (precision != HG_FP64 && precision != HG_FP32C) return fail(nullptr, HG_ERR_ARG, "hg_create: bad precision");
+namespace {
+// Checks shared by hg_create and hg_ensemble_create.
+int check_create_args(const hg_consts* consts, int32_t precision, int32_t device, const char* who) {
+  if (precision != HG_FP64 && precision != HG_FP32C) return fail(nullptr, HG_ERR_ARG, std::string(who) + ": bad precision");
   if (consts->riemann != HG_ROE)
-    return fail(nullptr, HG_ERR_UNSUPPORTED, "hg_create: only the Roe solver exists (semi_discretize_swe_2D.jl:352-362)");
+    return fail(nullptr, HG_ERR_UNSUPPORTED,
+                std::string(who) + ": only the Roe solver exists (semi_discretize_swe_2D.jl:352-362)");
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0)
-    return fail(nullptr, HG_ERR_NO_DEVICE, "hg_create: no CUDA device (this library has no CPU fallback)");
-  if (device < 0 || device >= ndev) return fail(nullptr, HG_ERR_ARG, "hg_create: bad device index");
-  std::unique_ptr<hg_ctx> c(new (std::nothrow) hg_ctx());
-  if (!c) return fail(nullptr, HG_ERR_ARG, "hg_create: out of host memory");
-  std::string err;
-  int rc = build_host_mesh(*desc, c->hm, err);
-  if (rc != HG_OK) return fail(nullptr, rc, err);
+    return fail(nullptr, HG_ERR_NO_DEVICE, std::string(who) + ": no CUDA device (this library has no CPU fallback)");
+  if (device < 0 || device >= ndev) return fail(nullptr, HG_ERR_ARG, std::string(who) + ": bad device index");
+  return HG_OK;
+}
+
+// Device set-up of a context whose host mesh is built.
+int finish_create(std::unique_ptr<hg_ctx>& c, const hg_consts* consts, int32_t precision, int32_t device,
+                  hg_ctx** out) {
   c->k = *consts;
   c->precision = precision;
   c->device = device;
   if (cudaSetDevice(device) != cudaSuccess) return fail(nullptr, HG_ERR_CUDA, "hg_create: cudaSetDevice failed");
   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess)
     return fail(nullptr, HG_ERR_CUDA, "hg_create: cudaStreamCreate failed");
-  rc = ctx_setup_device(c.get());
+  int rc = ctx_setup_device(c.get());
   if (rc != HG_OK) {
     std::string msg = c->err;
     return fail(nullptr, rc, msg);
   }
   *out = c.release();
+  return HG_OK;
+}
+}  // namespace
+
+int hg_create(const hg_mesh_desc* desc, const hg_consts* consts, int32_t precision, int32_t device, hg_ctx** out) {
+  if (!desc || !consts || !out) return fail(nullptr, HG_ERR_ARG, "hg_create: null argument");
+  *out = nullptr;
+  int rc = check_create_args(consts, precision, device, "hg_create");
+  if (rc) return rc;
+  std::unique_ptr<hg_ctx> c(new (std::nothrow) hg_ctx());
+  if (!c) return fail(nullptr, HG_ERR_ARG, "hg_create: out of host memory");
+  std::string err;
+  rc = build_host_mesh(*desc, c->hm, err);
+  if (rc != HG_OK) return fail(nullptr, rc, err);
+  return finish_create(c, consts, precision, device, out);
+}
+
+int hg_ensemble_create(const hg_ensemble_desc* e, const hg_consts* consts, int32_t precision, int32_t device,
+                       hg_ctx** out) {
+  if (!e || !consts || !out || !e->meshes || !e->member_mesh || e->n_meshes <= 0 || e->n_members <= 0)
+    return fail(nullptr, HG_ERR_ARG, "hg_ensemble_create: bad argument");
+  *out = nullptr;
+  for (int i = 0; i < e->n_members; ++i)
+    if (e->member_mesh[i] < 0 || e->member_mesh[i] >= e->n_meshes)
+      return fail(nullptr, HG_ERR_ARG, "hg_ensemble_create: member_mesh out of range");
+  int rc = check_create_args(consts, precision, device, "hg_ensemble_create");
+  if (rc) return rc;
+  std::vector<HostMesh> meshes(e->n_meshes);
+  for (int i = 0; i < e->n_meshes; ++i) {
+    std::string err;
+    rc = build_host_mesh(e->meshes[i], meshes[i], err);
+    if (rc != HG_OK) return fail(nullptr, rc, "hg_ensemble_create: mesh " + std::to_string(i) + ": " + err);
+  }
+  int64_t cells = 0;
+  for (int i = 0; i < e->n_members; ++i) cells += meshes[e->member_mesh[i]].nCells;
+  if (cells >= (int64_t)1 << 30) return fail(nullptr, HG_ERR_ARG, "hg_ensemble_create: more than 2^30 cells");
+  std::unique_ptr<hg_ctx> c(new (std::nothrow) hg_ctx());
+  if (!c) return fail(nullptr, HG_ERR_ARG, "hg_ensemble_create: out of host memory");
+  std::vector<const HostMesh*> parts;
+  c->memberCellOff.assign(1, 0);
+  c->memberInletOff.assign(1, 0);
+  c->memberExitOff.assign(1, 0);
+  for (int i = 0; i < e->n_members; ++i) {
+    const HostMesh& m = meshes[e->member_mesh[i]];
+    parts.push_back(&m);
+    c->memberCellOff.push_back(c->memberCellOff.back() + m.nCells);
+    c->memberInletOff.push_back(c->memberInletOff.back() + (int32_t)m.inletGroups.size());
+    c->memberExitOff.push_back(c->memberExitOff.back() + (int32_t)m.exitGroups.size());
+  }
+  concat_host_meshes(parts, c->hm);
+  return finish_create(c, consts, precision, device, out);
+}
+
+int hg_ensemble_layout(const hg_ctx* ctx, int32_t* n_members, int32_t* cell_offset, int32_t* inlet_offset,
+                       int32_t* exit_offset) {
+  if (!ctx || !n_members) return fail(nullptr, HG_ERR_ARG, "hg_ensemble_layout: null argument");
+  const bool ens = !ctx->memberCellOff.empty();
+  const int M = ens ? (int)ctx->memberCellOff.size() - 1 : 1;
+  *n_members = M;
+  for (int i = 0; i <= M; ++i) {
+    if (cell_offset) cell_offset[i] = ens ? ctx->memberCellOff[i] : (i ? ctx->n : 0);
+    if (inlet_offset) inlet_offset[i] = ens ? ctx->memberInletOff[i] : (i ? ctx->dm.nInlet : 0);
+    if (exit_offset) exit_offset[i] = ens ? ctx->memberExitOff[i] : (i ? ctx->dm.nExit : 0);
+  }
   return HG_OK;
 }
 
@@ -745,7 +811,8 @@ int ctx_setup_device(hg_ctx* c) {
   const HostMesh& m = c->hm;
   const int N = m.nCells;
   c->n = N;
-  c->perm = order_cells(m, c->k.order);
+  c->perm = c->memberCellOff.size() > 2 ? order_cells_ranges(m, c->k.order, c->memberCellOff)
+                                        : order_cells(m, c->k.order);
   c->inv.assign(N, 0);
   for (int i = 0; i < N; ++i) c->inv[c->perm[i]] = i;
   // Boundary faces, numbered by face id.

@@ -22,6 +22,9 @@ struct hg_ctx {
   int32_t device = 0;
   int32_t n = 0;
   std::vector<int> perm, inv;   // perm[device id] = caller id
+  // Ensemble members (hg_ensemble_create): cell, inlet-Q and exit-H boundary
+  // offsets per member in the caller's order ([n_members + 1]; empty otherwise).
+  std::vector<int32_t> memberCellOff, memberInletOff, memberExitOff;
   cudaStream_t stream = nullptr;
   std::vector<void*> allocs;
   hg::DevMesh dm;

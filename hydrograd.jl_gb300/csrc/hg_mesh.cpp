@@ -349,23 +349,28 @@ uint64_t hilbert_index(uint32_t x, uint32_t y) {
   return d;
 }
 
-std::vector<int> order_hilbert(const HostMesh& m) {
-  const int N = m.nCells;
+// Hilbert order of the cells [a, b), appended to order.
+void hilbert_range(const HostMesh& m, int a, int b, std::vector<int>& order) {
   double x0 = 1e300, x1 = -1e300, y0 = 1e300, y1 = -1e300;
-  for (int c = 0; c < N; ++c) {
+  for (int c = a; c < b; ++c) {
     x0 = std::min(x0, m.cx[c]); x1 = std::max(x1, m.cx[c]);
     y0 = std::min(y0, m.cy[c]); y1 = std::max(y1, m.cy[c]);
   }
   double sc = 65535.0 / std::max(std::max(x1 - x0, y1 - y0), 1e-300);
-  std::vector<std::pair<uint64_t, int>> key(N);
-  for (int c = 0; c < N; ++c) {
+  std::vector<std::pair<uint64_t, int>> key(b - a);
+  for (int c = a; c < b; ++c) {
     uint32_t ix = (uint32_t)std::min(65535.0, std::max(0.0, (m.cx[c] - x0) * sc));
     uint32_t iy = (uint32_t)std::min(65535.0, std::max(0.0, (m.cy[c] - y0) * sc));
-    key[c] = {hilbert_index(ix, iy), c};
+    key[c - a] = {hilbert_index(ix, iy), c};
   }
   std::sort(key.begin(), key.end());
-  std::vector<int> order(N);
-  for (int i = 0; i < N; ++i) order[i] = key[i].second;
+  for (const auto& k : key) order.push_back(k.second);
+}
+
+std::vector<int> order_hilbert(const HostMesh& m) {
+  std::vector<int> order;
+  order.reserve(m.nCells);
+  hilbert_range(m, 0, m.nCells, order);
   return order;
 }
 
@@ -377,6 +382,75 @@ std::vector<int> order_cells(const HostMesh& m, int order) {
   std::vector<int> id(m.nCells);
   std::iota(id.begin(), id.end(), 0);
   return id;
+}
+
+std::vector<int> order_cells_ranges(const HostMesh& m, int order, const std::vector<int>& start) {
+  if (order != HG_ORDER_HILBERT) return order_cells(m, order);   // RCM visits components in cell order
+  std::vector<int> out;
+  out.reserve(m.nCells);
+  for (size_t r = 0; r + 1 < start.size(); ++r) hilbert_range(m, start[r], start[r + 1], out);
+  return out;
+}
+
+void concat_host_meshes(const std::vector<const HostMesh*>& parts, HostMesh& o) {
+  o = HostMesh();
+  size_t C = 0, V = 0, F = 0;
+  for (const HostMesh* p : parts) {
+    C += p->nCells;
+    V += p->nNodes;
+    F += p->nFaces;
+  }
+  for (auto* v : {&o.x, &o.y, &o.z}) v->reserve(V);
+  o.cellNodes.reserve(C * 8);
+  o.cf.reserve(C * 8);
+  o.nbr.reserve(C * 8);
+  o.faceC0.reserve(F);
+  o.faceC1.reserve(F);
+  int cOff = 0, vOff = 0, fOff = 0, bOff = 0;
+  auto shift = [](int v, int off) { return v >= 0 ? v + off : v; };
+  for (const HostMesh* p : parts) {
+    const HostMesh& m = *p;
+    o.maxCellFaces = std::max(o.maxCellFaces, m.maxCellFaces);
+    o.nGhost += m.nGhost;
+    o.x.insert(o.x.end(), m.x.begin(), m.x.end());
+    o.y.insert(o.y.end(), m.y.begin(), m.y.end());
+    o.z.insert(o.z.end(), m.z.begin(), m.z.end());
+    o.ncf.insert(o.ncf.end(), m.ncf.begin(), m.ncf.end());
+    for (int v : m.cellNodes) o.cellNodes.push_back(shift(v, vOff));
+    for (int c = 0; c < m.nCells; ++c)
+      for (int i = 0; i < kMaxCellFaces; ++i) {
+        const size_t k = (size_t)c * 8 + i;
+        o.cf.push_back(i < m.ncf[c] ? m.cf[k] + fOff : m.cf[k]);
+        o.nbr.push_back(shift(m.nbr[k], cOff));
+      }
+    o.cfs.insert(o.cfs.end(), m.cfs.begin(), m.cfs.end());
+    for (int v : m.faceA) o.faceA.push_back(v + vOff);
+    for (int v : m.faceB) o.faceB.push_back(v + vOff);
+    for (int v : m.faceC0) o.faceC0.push_back(v + cOff);
+    for (int v : m.faceC1) o.faceC1.push_back(shift(v, cOff));
+    for (const Boundary& b : m.bnd) {
+      Boundary nb = b;
+      nb.id = (int)o.bnd.size() + 1;
+      for (int& f : nb.faces) f += fOff;
+      o.bnd.push_back(std::move(nb));
+    }
+    for (int v : m.faceBnd) o.faceBnd.push_back(shift(v, bOff));
+    for (auto pr : {std::make_pair(&o.area, &m.area), std::make_pair(&o.cx, &m.cx), std::make_pair(&o.cy, &m.cy),
+                    std::make_pair(&o.snx, &m.snx), std::make_pair(&o.sny, &m.sny),
+                    std::make_pair(&o.faceLen, &m.faceLen), std::make_pair(&o.zbCell, &m.zbCell)})
+      pr.first->insert(pr.first->end(), pr.second->begin(), pr.second->end());
+    for (int g : m.inletGroups) o.inletGroups.push_back(g + bOff);
+    for (int g : m.exitGroups) o.exitGroups.push_back(g + bOff);
+    for (int g : m.wallGroups) o.wallGroups.push_back(g + bOff);
+    for (int g : m.symmGroups) o.symmGroups.push_back(g + bOff);
+    cOff += m.nCells;
+    vOff += m.nNodes;
+    fOff += m.nFaces;
+    bOff += (int)m.bnd.size();
+  }
+  o.nCells = cOff;
+  o.nNodes = vOff;
+  o.nFaces = fOff;
 }
 
 }  // namespace hg

@@ -51,6 +51,16 @@ int build_host_mesh(const hg_mesh_desc& d, HostMesh& m, std::string& err);
 
 // Cell permutations perm[new] = old.
 std::vector<int> order_cells(const HostMesh& m, int order);
+// The same within each cell range [start[r], start[r+1]) (an ensemble's
+// members, each a separate component): ranges stay in order, cells stay in
+// their range.
+std::vector<int> order_cells_ranges(const HostMesh& m, int order, const std::vector<int>& start);
+
+// Disjoint union of meshes (an ensemble): cells, nodes, faces and boundaries of
+// part p follow those of parts 0..p-1, with every id offset accordingly;
+// boundary ids are renumbered 1, 2, ... in that order, so each type's groups
+// are part-major and, within a part, in the part's own order.
+void concat_host_meshes(const std::vector<const HostMesh*>& parts, HostMesh& out);
 
 }  // namespace hg
 

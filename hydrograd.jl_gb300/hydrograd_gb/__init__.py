@@ -6,5 +6,6 @@ mirror of the reference's ODE-RHS / parameter interface plus the synthetic
 workload generators used by the tests and the benchmark.
 """
 from ._lib import HgError, lib  # noqa: F401
-from .swe2d import (HostMesh, MeshDesc, PinnedBuffer, SWE2D, SWE2DExtraParameters, custom_ODE_solve,  # noqa: F401
+from .swe2d import (HostMesh, MeshDesc, PinnedBuffer, SWE2D, SWE2DEnsemble, SWE2DExtraParameters,  # noqa: F401
+                    custom_ODE_solve,
                     swe_2d_rhs)

@@ -28,6 +28,11 @@ class HgMeshDesc(ctypes.Structure):
                 ("string_nodes", _ip), ("string_bc", _ip)]
 
 
+class HgEnsembleDesc(ctypes.Structure):
+    _fields_ = [("n_meshes", ctypes.c_int32), ("meshes", ctypes.POINTER(HgMeshDesc)),
+                ("n_members", ctypes.c_int32), ("member_mesh", _ip)]
+
+
 class HgConsts(ctypes.Structure):
     _fields_ = [("g", ctypes.c_double), ("k_n", ctypes.c_double), ("h_small", ctypes.c_double),
                 ("riemann", ctypes.c_int32), ("order", ctypes.c_int32)]
@@ -44,6 +49,9 @@ SIGNATURES = {
     "hg_mesh_order": [_vp, ctypes.c_int32, _ip],
     "hg_create": [ctypes.POINTER(HgMeshDesc), ctypes.POINTER(HgConsts), ctypes.c_int32, ctypes.c_int32,
                   ctypes.POINTER(_vp)],
+    "hg_ensemble_create": [ctypes.POINTER(HgEnsembleDesc), ctypes.POINTER(HgConsts), ctypes.c_int32, ctypes.c_int32,
+                           ctypes.POINTER(_vp)],
+    "hg_ensemble_layout": [_vp, _ip, _ip, _ip, _ip],
     "hg_destroy": [_vp],
     "hg_sizes": [_vp, _ip],
     "hg_set_still_water": [_vp, _dp],

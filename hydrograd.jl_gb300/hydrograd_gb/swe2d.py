@@ -19,7 +19,7 @@ import ctypes
 import numpy as np
 
 from . import _lib
-from ._lib import HgConsts, HgMeshDesc, check, lib
+from ._lib import HgConsts, HgEnsembleDesc, HgMeshDesc, check, lib
 
 _dp = ctypes.POINTER(ctypes.c_double)
 _ip = ctypes.POINTER(ctypes.c_int32)
@@ -104,6 +104,9 @@ class SWE2D:
         h = ctypes.c_void_p()
         check(lib().hg_create(ctypes.byref(self._desc.desc), ctypes.byref(k), PRECISIONS[precision], device,
                               ctypes.byref(h)))
+        self._init_handle(h, precision, h_small)
+
+    def _init_handle(self, h, precision, h_small):
         self.h = h
         self.precision = precision
         s = np.zeros(8, np.int32)
@@ -251,6 +254,56 @@ class PinnedBuffer:
 # ---------------------------------------------------------------------------
 # The reference's interface
 # ---------------------------------------------------------------------------
+class SWE2DEnsemble(SWE2D):
+    """Many independent problems stepped together (hg_ensemble_create).
+
+    ``cases`` are mesh cases (as for :class:`SWE2D`); member m runs on
+    ``cases[member_mesh[m]]``.  The members' cells, inlet-Q and exit-H
+    boundaries are concatenated in member order (``cell_offset``,
+    ``inlet_offset``, ``exit_offset``), and every :class:`SWE2D` call applies to
+    the concatenation; :meth:`concat` and :meth:`split` convert between
+    per-member arrays and the concatenated ones.
+    """
+
+    def __init__(self, cases, member_mesh, precision="fp64", order="hilbert", g=9.81, k_n=1.0, h_small=1.0e-3,
+                 device=0):
+        self._descs = [MeshDesc(c) for c in cases]
+        arr = (HgMeshDesc * len(self._descs))(*[d.desc for d in self._descs])
+        self._mm = np.ascontiguousarray(member_mesh, dtype=np.int32)
+        e = HgEnsembleDesc(len(self._descs), arr, len(self._mm), _i(self._mm))
+        self._arr = arr
+        k = HgConsts(g, k_n, h_small, 0, ORDERS[order])
+        h = ctypes.c_void_p()
+        check(lib().hg_ensemble_create(ctypes.byref(e), ctypes.byref(k), PRECISIONS[precision], device,
+                                       ctypes.byref(h)))
+        self._init_handle(h, precision, h_small)
+        nm = ctypes.c_int32()
+        check(lib().hg_ensemble_layout(self.h, ctypes.byref(nm), None, None, None), self.h)
+        self.n_members = nm.value
+        self.cell_offset = np.zeros(self.n_members + 1, np.int32)
+        self.inlet_offset = np.zeros(self.n_members + 1, np.int32)
+        self.exit_offset = np.zeros(self.n_members + 1, np.int32)
+        check(lib().hg_ensemble_layout(self.h, ctypes.byref(nm), _i(self.cell_offset), _i(self.inlet_offset),
+                                       _i(self.exit_offset)), self.h)
+
+    def concat(self, per_member, kind="cell"):
+        """Concatenate per-member arrays (kind: cell, inlet, exit, state)."""
+        if kind == "state":   # Q = [xi; qx; qy] per member -> the concatenated state's three blocks
+            ns = np.diff(self.cell_offset)
+            return np.concatenate([np.concatenate([np.asarray(q)[b * n:(b + 1) * n] for q, n in zip(per_member, ns)])
+                                   for b in range(3)])
+        return np.concatenate([np.asarray(a, dtype=np.float64).ravel() for a in per_member])
+
+    def split(self, arr, kind="cell"):
+        """Per-member views of a concatenated array (kind: cell, inlet, exit, state)."""
+        if kind == "state":
+            N = int(self.cell_offset[-1])
+            return [np.concatenate([arr[b * N + a:b * N + z] for b in range(3)])
+                    for a, z in zip(self.cell_offset[:-1], self.cell_offset[1:])]
+        off = {"cell": self.cell_offset, "inlet": self.inlet_offset, "exit": self.exit_offset}[kind]
+        return [arr[a:z] for a, z in zip(off[:-1], off[1:])]
+
+
 class SWE2DExtraParameters:
     """The fields of SWE2D_Extra_Parameters (application_commons.jl:7-44) that
     the RHS reads at run time: the active parameter name and how a parameter

@@ -119,6 +119,31 @@ int hg_mesh_order(const hg_mesh* mesh, int32_t order, int32_t* perm);
 
 /* ---- context lifecycle (replaces building SWE2D_Extra_Parameters, application_commons.jl:7-44) */
 int hg_create(const hg_mesh_desc* desc, const hg_consts* consts, int32_t precision, int32_t device, hg_ctx** out);
+/* Ensembles: many independent problems ("members"), each on one of a set of
+ * meshes, stepped together in one context -- one launch per stage over every
+ * member's cells.  No counterpart in the reference, which solves one problem
+ * per call.  The members' cells are concatenated in member order: member m
+ * holds cells [cell_offset[m], cell_offset[m+1]) of every per-cell array and
+ * of each of Q's three blocks, and its inlet-Q / exit-H boundaries are
+ * [inlet_offset[m], inlet_offset[m+1]) / [exit_offset[m], ...) of the values
+ * of hg_set_inlet_q / hg_set_exit_wse and of the inlet-Q gradient.  Every
+ * other call (hg_set_*, hg_rhs, hg_integrate, hg_advance, hg_loss_and_grad)
+ * applies unchanged to the concatenation.  All members take the same step: a
+ * fixed dt, or the smallest of the members' CFL steps; the loss of
+ * hg_loss_and_grad is the mean over all members' probes. */
+typedef struct hg_ensemble_desc {
+  int32_t n_meshes;
+  const hg_mesh_desc* meshes;   /* [n_meshes] */
+  int32_t n_members;
+  const int32_t* member_mesh;   /* [n_members] index into meshes */
+} hg_ensemble_desc;
+int hg_ensemble_create(const hg_ensemble_desc* ensemble, const hg_consts* consts, int32_t precision,
+                       int32_t device, hg_ctx** out);
+/* n_members; then, where not NULL, the [n_members + 1] offsets (a context made
+ * by hg_create is one member). */
+int hg_ensemble_layout(const hg_ctx* ctx, int32_t* n_members, int32_t* cell_offset, int32_t* inlet_offset,
+                       int32_t* exit_offset);
+
 int hg_destroy(hg_ctx* ctx);
 int hg_sizes(const hg_ctx* ctx, int32_t* sizes8); /* as hg_mesh_sizes */
 
