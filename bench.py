@@ -220,6 +220,59 @@ def run_reference(args):
     }))
 
 
+# Configuration 4: reach meshes of about these many cells, 32 members each.
+ENSEMBLE_SIZES = (5000, 10000, 20000, 40000, 60000, 100000, 150000, 200000)
+
+
+def run_ensemble(args, device):
+    """hg_ensemble_create over 8 meshes x 32 members (about 18.7 M member-cells):
+    per member zone n ~ U[0.02, 0.06] and inlet Q ~ U[100, 800]; all members
+    share the CFL step (the smallest member's).  FP32C forward steps, then one
+    forward+adjoint with 8 probes per member."""
+    from hydrograd_gb import SWE2DEnsemble
+    from hydrograd_gb.workloads import Stream, probes_and_perturbation, river_triangles
+    meshes = [river_triangles(n=int(round((s / 2) ** 0.5))) for s in ENSEMBLE_SIZES]
+    member_mesh = np.repeat(np.arange(len(meshes)), args.ens_members)
+    rs = Stream(7)
+    t0 = time.perf_counter()
+    e = SWE2DEnsemble(meshes, member_mesh, precision="fp32c", device=device)
+    setup_s = time.perf_counter() - t0
+    cases = [meshes[m] for m in member_mesh]
+    e.set_still_water(e.concat([c["wstill"] for c in cases]))
+    mat, zones, base = [], [], 0
+    for c in cases:
+        mat.append(c["mat_id"] + base)
+        zones.append(rs.uniform(len(c["manning_zones"]), 0.02, 0.06))
+        base += len(c["manning_zones"])
+    e.set_manning_zones(np.concatenate(mat).astype(np.int32), np.concatenate(zones))
+    e.set_inlet_q(rs.uniform(len(cases), 100.0, 800.0))
+    e.set_exit_wse(e.concat([c["exit_wse"] for c in cases], "exit"))
+    Q0 = e.concat([c["Q0"] for c in cases], "state")
+    N = e.n_cells
+    e.upload(Q0)
+    e.advance_timed(args.warmup, cfl=0.4, flush_l2=True)
+    e.upload(Q0)
+    ms = e.advance_timed(args.ens_steps, cfl=0.4, flush_l2=True)
+    out = {"members": int(e.n_members), "meshes": [len(m["cell_node_count"]) for m in meshes], "member_cells": N,
+           "setup_seconds": setup_s,
+           "fwd": {"value": N * args.ens_steps / (ms * 1e-3), "steps": args.ens_steps, "ms_per_step": ms / args.ens_steps,
+                   "simulated_seconds": e.elapsed_time()}}
+    if args.ens_adj_steps > 0:
+        dt = 0.5 * e.integrate(Q0, 1, cfl=0.4)[1][0]
+        per_mesh = [probes_and_perturbation(m, 8, inlet_share=0.5)[0] for m in meshes]
+        probes = np.concatenate([per_mesh[m] + e.cell_offset[i] for i, m in enumerate(member_mesh)]).astype(np.int32)
+        h_rest = np.concatenate([c["wstill"] - c["zb_cells"] for c in cases])
+        obs = np.tile(h_rest[probes], (args.ens_adj_steps, 1))
+        e.loss_and_grad(Q0, 4, dt, probes, obs[:4], ckpt_every=2)   # warm-up / allocation
+        t0 = time.perf_counter()
+        e.loss_and_grad(Q0, args.ens_adj_steps, dt, probes, obs, ckpt_every=args.ens_ckpt)
+        el = time.perf_counter() - t0
+        out["fwd_adjoint"] = {"value": N * args.ens_adj_steps / el, "steps": args.ens_adj_steps, "seconds": el,
+                              "checkpoint_every": args.ens_ckpt, "probes": int(len(probes))}
+    e.close()
+    return out
+
+
 def run_ours(args):
     rank, ws, local, dist = dist_setup()
     from hydrograd_gb import PinnedBuffer
@@ -323,6 +376,11 @@ def run_ours(args):
         adj["config"] = (f"{args.adj_steps} fixed-dt steps (dt = half the initial CFL step), checkpoints every 50, "
                          f"{len(probes)} probes (half on the pool rim, half at the inlet), loss = mean squared "
                          "departure of the probe depths from the lake at rest")
+    ens = None
+    if args.ens_steps > 0:
+        ens = run_ensemble(args, local)
+        ens["config"] = ("configuration 4: 8 reach meshes x %d members, per-member zone n and inlet Q, "
+                         "FP32C, shared CFL 0.4 step, L2 flushed before every timed step" % args.ens_members)
     if rank != 0:
         return
     peak, peak_kind = load_peaks()
@@ -363,6 +421,7 @@ def run_ours(args):
                  "warm_value": out["fp64"]["warm_value"]},
         "fp32c_over_fp64_speedup": f32["value"] / out["fp64"]["value"],
         "fwd_adjoint": adj,
+        "ensemble": ens,
         "warm_value": f32["warm_value"], "simulated_seconds": f32["sim_time"],
         "error": err,
         "roofline": roof,
@@ -388,6 +447,10 @@ def main():
     ap.add_argument("--ref-steps", type=int, default=20)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--adj-steps", type=int, default=100, help="steps of the forward+adjoint measurement (0: skip)")
+    ap.add_argument("--ens-steps", type=int, default=1000, help="ensemble (configuration 4) forward steps (0: skip)")
+    ap.add_argument("--ens-adj-steps", type=int, default=200, help="ensemble forward+adjoint steps (0: skip)")
+    ap.add_argument("--ens-ckpt", type=int, default=25)
+    ap.add_argument("--ens-members", type=int, default=32, help="members per mesh")
     ap.add_argument("--profile-stage", default=None, choices=["fp32c", "fp64"],
                     help="only run the stage kernel a few times (a small case for ncu captures)")
     ap.add_argument("--profile-adjoint", default=None, choices=["fp32c", "fp64"],

@@ -179,8 +179,6 @@ int setup(hg_ctx* c) {
   a.bndInCoef = dBCoef;
   ADJ_CUDA(c, falloc(b, &a.bndG, (size_t)5 * bnd.size()));
   ADJ_CUDA(c, falloc(b, &a.grpTA, (size_t)c->dm.nInlet));
-  ADJ_CUDA(c, falloc(b, &a.bndTicket, 1));
-  ADJ_CUDA(c, cudaMemset(a.bndTicket, 0, sizeof(unsigned int)));
   ADJ_CUDA(c, cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking));
   ADJ_CUDA(c, cudaEventCreateWithFlags(&b->evFork, cudaEventDisableTiming));
   ADJ_CUDA(c, cudaEventCreateWithFlags(&b->evJoin, cudaEventDisableTiming));

@@ -144,8 +144,7 @@ __global__ void __launch_bounds__(kBlock, vjp_min_blocks<NS>()) k_vjp_f32(DevMes
 // Boundary faces of the cells that have any (one thread per such cell; runs
 // beside k_vjp_f32, which reads none of what it writes): ghost-state duals in
 // the own state, n, zb, Q and total_A.  Leaves the cell's terms in bndG and
-// the Q / total_A cotangents per boundary face; the last block to finish sums
-// the latter per inlet group (gQ += beta sum, grpTA = sum) in face order.
+// the Q / total_A cotangents per boundary face (k_inlet_group_sums_f32).
 template <int NS>
 __global__ void __launch_bounds__(64) k_vjp_bnd_f32(DevMesh m, AdjDev a, StateF32 Q, const float* __restrict__ mu,
                                                     double betaD) {
@@ -192,29 +191,29 @@ __global__ void __launch_bounds__(64) k_vjp_bnd_f32(DevMesh m, AdjDev a, StateF3
     float* o = a.bndG + (size_t)5 * i;
     o[0] = g0; o[1] = g1; o[2] = g2; o[3] = gn; o[4] = gzb;
   }
-  if (m.nInlet == 0) return;
-  __shared__ int isLast;
-  __threadfence();
-  __syncthreads();
-  if (threadIdx.x == 0) isLast = (atomicAdd(a.bndTicket, 1u) == gridDim.x - 1);
-  __syncthreads();
-  if (!isLast) return;
-  __threadfence();
-  for (int g = 0; g < m.nInlet; ++g) {
-    double sTA = 0.0, sQ = 0.0;
-    for (int e = m.inletOff[g] + threadIdx.x; e < m.inletOff[g + 1]; e += blockDim.x) {
-      const int bf = a.inletBf[e];
-      sTA += __ldcg(&a.bfGradTA[bf]);
-      sQ += __ldcg(&a.bfGradQ[bf]);
-    }
-    const double tTA = block_sum(sTA);
-    const double tQ = block_sum(sQ);
-    if (threadIdx.x == 0) {
-      a.grpTA[g] = tTA;
-      a.gQ[g] += betaD * tQ;
-    }
+}
+
+// Per inlet-Q group (one warp each, after k_vjp_bnd_f32 on the side stream):
+// grpTA = sum over the group's faces of the total_A cotangent, gQ += beta sum
+// of the Q cotangent -- lanes stride over the faces, a fixed shuffle tree
+// adds them (deterministic).
+__global__ void __launch_bounds__(128) k_inlet_group_sums_f32(DevMesh m, AdjDev a, double betaD) {
+  const int g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (g >= m.nInlet) return;
+  double sTA = 0.0, sQ = 0.0;
+  for (int e = m.inletOff[g] + lane; e < m.inletOff[g + 1]; e += 32) {
+    const int bf = a.inletBf[e];
+    sTA += a.bfGradTA[bf];
+    sQ += a.bfGradQ[bf];
   }
-  if (threadIdx.x == 0) *a.bndTicket = 0u;
+  for (int o = 16; o > 0; o >>= 1) {
+    sTA += __shfl_xor_sync(0xffffffffu, sTA, o);
+    sQ += __shfl_xor_sync(0xffffffffu, sQ, o);
+  }
+  if (lane == 0) {
+    a.grpTA[g] = sTA;
+    a.gQ[g] += betaD * sQ;
+  }
 }
 
 // After both VJP kernels: each boundary cell's terms into out (when wet) and
@@ -301,13 +300,14 @@ int launch_vjp_ns(const DevMesh& m, const AdjDev& a, StateF32 Q, const float* mu
     cudaEventRecord(evFork, st);
     cudaStreamWaitEvent(side, evFork, 0);
     k_vjp_bnd_f32<NS><<<nbb, 64, 0, side>>>(m, a, Q, mu, betaD);
+    if (m.nInlet > 0) k_inlet_group_sums_f32<<<(m.nInlet + 3) / 4, 128, 0, side>>>(m, a, betaD);
     cudaEventRecord(evJoin, side);
   }
   k_vjp_f32<NS><<<blocks_for(m.n), kBlock, 0, st>>>(m, a, Q, mu, extra, out, cSelf, cExtra, beta);
   if (!nbb) return 1;
   cudaStreamWaitEvent(st, evJoin, 0);
   k_vjp_combine_f32<<<(a.nBndCells + 127) / 128, 128, 0, st>>>(m, a, Q, out, beta, betaD);
-  return 3;
+  return m.nInlet > 0 ? 4 : 3;
 }
 }  // namespace
 

@@ -28,8 +28,8 @@ struct AdjDev {
   // FP32C boundary VJP (k_vjp_bnd_f32 beside the interior VJP, then
   // k_vjp_combine_f32): cells with at least one boundary face (device order),
   // their boundary-face terms of the current VJP {g_xi, g_hu, g_hv, g_n, g_zb},
-  // the inlet (group, sum L^(5/3)) pairs of each (CSR), the per-group sums of
-  // the total_A cotangent, and the last-block ticket.
+  // the inlet (group, sum L^(5/3)) pairs of each (CSR), and the per-group sums
+  // of the total_A cotangent.
   const int32_t* bndCells = nullptr;
   int32_t nBndCells = 0;
   float* bndG = nullptr;
@@ -37,7 +37,6 @@ struct AdjDev {
   const int32_t* bndInGrp = nullptr;
   const double* bndInCoef = nullptr;
   double* grpTA = nullptr;
-  unsigned int* bndTicket = nullptr;
 };
 
 // out_j = M(Q_j) (cSelf mu_j + cExtra extra_j + beta (J(Q)^T mu)_j), parameter
