@@ -163,10 +163,6 @@ __device__ __forceinline__ double fused_dt(const DevScalars& s, const StageFuse&
 template <int NS>
 constexpr int stage_min_blocks() { return NS <= 4 ? HG_STAGE_MIN_BLOCKS : 1; }
 
-// GB300 issues FP64 at a small fraction of the FP32 rate, so the per-cell path
-// holds no FP64 arithmetic: the stage mode is a template parameter (the FP64
-// comparison of the reference Euler clamp exists only in that instance), and
-// the fused step's dt is formed once per block.
 // One cell of a stage: clamp, faces, sources, compensated update and clamp of
 // the output, CFL candidate.  sX / sP hold the records of cells [base, base +
 // kBlock) for in-block neighbours.  The input state's lo parts and (stage 2)
