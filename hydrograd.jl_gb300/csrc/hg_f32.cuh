@@ -104,12 +104,22 @@ struct OwnF32 {
   float fxx, fxy, fyx, fyy;
 };
 
+// FP32 forms of the smooth_* helpers on the wet path.  smooth_abs(x) =
+// sqrt(x^2 + eps) is |x| to FP32 precision once |x| > 1e-4 (eps / x^2 < 2.3e-8
+// < 2^-24); sqrt(h + eps) and 1/h of a wet cell (h > h_small) come from one
+// reciprocal square root: sqrt(h) = h r, 1/h = r^2 with r = rsqrt(h).
+__device__ __forceinline__ float smooth_abs_f32(float x) {
+  const float a = fabsf(x);
+  return a > 1.0e-4f ? a : sqrtf(fmaf(x, x, eps_c<float>()));
+}
+
 __device__ __forceinline__ OwnF32 own_f32(const Side<float>& L, float g) {
   OwnF32 o;
-  const float r = 1.0f / L.h;
+  const float rq = rsqrtf(L.h);
+  const float r = rq * rq;
   o.u = L.hu * r;
   o.v = L.hv * r;
-  o.s = smooth_sqrt(L.h);
+  o.s = L.h * rq;
   o.p = 0.5f * g * (smooth_pow2(L.xi) + 2.0f * L.xi * L.hst);
   o.fxx = L.hu * o.u;
   o.fxy = L.hu * o.v;
@@ -143,19 +153,22 @@ __device__ __forceinline__ float pressure_jump_f32(float g, float xiL, float xiR
 // and the rows of R |Lambda| w are collected around w1 + w2 and w2 - w1.
 __device__ __forceinline__ void roe_flux_wet_f32(const Side<float>& L, const OwnF32& o, const Side<float>& R,
                                                  float dxi, float dhst, float g, float nx, float ny, float F[3]) {
-  const float rR = 1.0f / R.h;
+  const float rq = rsqrtf(R.h);
+  const float rR = rq * rq;
   const float uR = R.hu * rR, vR = R.hv * rR;
-  const float sR = smooth_sqrt(R.h);
+  const float sR = R.h * rq;
   const float rs = 1.0f / (o.s + sR);
   const float uRoe = (o.s * o.u + sR * uR) * rs;
   const float vRoe = (o.s * o.v + sR * vR) * rs;
   const float unRoe = uRoe * nx + vRoe * ny;
-  const float cRoe = smooth_sqrt(g * ((L.h + R.h) * 0.5f));
+  const float gh = g * ((L.h + R.h) * 0.5f);
+  const float rc = rsqrtf(gh);
+  const float cRoe = gh * rc;   // sqrt(g hRoe)
   const float d1 = R.hu - L.hu, d2 = R.hv - L.hv;
-  const float t = (unRoe * dxi - nx * d1 - ny * d2) * (0.5f / cRoe);
-  const float w0 = (ny * d1 - nx * d2 - (uRoe * ny - vRoe * nx) * dxi) * smooth_abs(unRoe);
-  const float w1 = (0.5f * dxi + t) * smooth_abs(unRoe - cRoe);
-  const float w2 = (0.5f * dxi - t) * smooth_abs(unRoe + cRoe);
+  const float t = (unRoe * dxi - nx * d1 - ny * d2) * (0.5f * rc);
+  const float w0 = (ny * d1 - nx * d2 - (uRoe * ny - vRoe * nx) * dxi) * smooth_abs_f32(unRoe);
+  const float w1 = (0.5f * dxi + t) * smooth_abs_f32(unRoe - cRoe);
+  const float w2 = (0.5f * dxi - t) * smooth_abs_f32(unRoe + cRoe);
   const float sum = w1 + w2, dif = cRoe * (w2 - w1);
   const float A0 = sum;
   const float A1 = ny * w0 + uRoe * sum + nx * dif;
@@ -183,20 +196,23 @@ __device__ __forceinline__ void roe_wet_vjp_f32(const Side<float>& L, const OwnF
                                                 float dxi, float g, float nx, float ny, float w0, float w1, float w2,
                                                 OwnAdjF32& b) {
   // forward
-  const float rR = 1.0f / R.h;
+  const float rq = rsqrtf(R.h);
+  const float rR = rq * rq;
   const float uR = R.hu * rR, vR = R.hv * rR;
-  const float sR = smooth_sqrt(R.h);
+  const float sR = R.h * rq;
   const float rs = 1.0f / (o.s + sR);
   const float numu = o.s * o.u + sR * uR, numv = o.s * o.v + sR * vR;
   const float uRoe = numu * rs, vRoe = numv * rs;
   const float un = uRoe * nx + vRoe * ny;
-  const float c = smooth_sqrt(g * ((L.h + R.h) * 0.5f));
-  const float q = 0.5f / c;
+  const float gh = g * ((L.h + R.h) * 0.5f);
+  const float rc = rsqrtf(gh);
+  const float c = gh * rc;
+  const float q = 0.5f * rc;
   const float d1 = R.hu - L.hu, d2 = R.hv - L.hv;
   const float T = un * dxi - nx * d1 - ny * d2;
   const float t = T * q;
   const float w0r = ny * d1 - nx * d2 - (uRoe * ny - vRoe * nx) * dxi;
-  const float a0 = smooth_abs(un), a1 = smooth_abs(un - c), a2 = smooth_abs(un + c);
+  const float a0 = smooth_abs_f32(un), a1 = smooth_abs_f32(un - c), a2 = smooth_abs_f32(un + c);
   const float e1 = 0.5f * dxi + t, e2 = 0.5f * dxi - t;
   const float W1 = e1 * a1, W2 = e2 * a2;
   const float sum = W1 + W2;
