@@ -146,9 +146,13 @@ __device__ __forceinline__ Side<T> ghost_state(const Side<T>& L, int32_t type, T
 
 // Manning friction coefficient g n^2/k_n^2/(h+h_small)^(7/3) * smooth_sqrt(qx^2+qy^2)
 // (semi_discretize_swe_2D.jl:544-547).
+// FP64: (h + h_small)^(7/3) as x^2 cbrt(x) -- within a few 1e-16 of pow(x, 7/3)
+// (the reference's ^(7/3)) for a fraction of pow's FP64 instructions, which GB300
+// issues at 1/64 of its FP32 rate.
 __device__ __forceinline__ double friction_coef(double g, double kn2, double hsm, double n, double h, double qx,
                                                 double qy) {
-  return g * (n * n) / kn2 / pow(h + hsm, 7.0 / 3.0) * smooth_sqrt(qx * qx + qy * qy);
+  const double x = h + hsm;
+  return g * (n * n) / kn2 / (x * x * cbrt(x)) * smooth_sqrt(qx * qx + qy * qy);
 }
 __device__ __forceinline__ float friction_coef(float g, float kn2, float hsm, float n, float h, float qx, float qy) {
   // (h + h_small)^(-7/3) = exp2(-7/3 log2(h + h_small))

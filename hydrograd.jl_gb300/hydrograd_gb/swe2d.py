@@ -167,9 +167,15 @@ class SWE2D:
         self._chk(lib().hg_rhs(self.h, _d(Q), float(t), _d(out)))
         return out
 
-    def integrate(self, Q, nsteps, method="rk2", dt=None, cfl=0.4, save_every=0):
-        """nsteps explicit steps from Q; returns (Q, dts[, saves])."""
-        Q = np.array(Q, dtype=np.float64)
+    def integrate(self, Q, nsteps, method="rk2", dt=None, cfl=0.4, save_every=0, inplace=False):
+        """nsteps explicit steps from Q; returns (Q, dts[, saves]).  With
+        inplace=True a C-contiguous float64 Q (e.g. a PinnedBuffer's array) is
+        advanced where it lies, as hg_integrate does with its host buffer."""
+        if inplace:
+            if not (isinstance(Q, np.ndarray) and Q.dtype == np.float64 and Q.flags.c_contiguous and Q.flags.writeable):
+                raise ValueError("inplace needs a writable C-contiguous float64 array")
+        else:
+            Q = np.array(Q, dtype=np.float64)
         dts = np.zeros(max(nsteps, 1))
         saves = np.zeros((nsteps // save_every, Q.size)) if save_every > 0 else None
         m = {"rk2": 0, "euler": 1}[method]
@@ -251,9 +257,6 @@ class PinnedBuffer:
             self.p = None
 
 
-# ---------------------------------------------------------------------------
-# The reference's interface
-# ---------------------------------------------------------------------------
 class SWE2DEnsemble(SWE2D):
     """Many independent problems stepped together (hg_ensemble_create).
 
@@ -304,6 +307,9 @@ class SWE2DEnsemble(SWE2D):
         return [arr[a:z] for a, z in zip(off[:-1], off[1:])]
 
 
+# ---------------------------------------------------------------------------
+# The reference's interface
+# ---------------------------------------------------------------------------
 class SWE2DExtraParameters:
     """The fields of SWE2D_Extra_Parameters (application_commons.jl:7-44) that
     the RHS reads at run time: the active parameter name and how a parameter
