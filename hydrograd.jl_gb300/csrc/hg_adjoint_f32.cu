@@ -15,6 +15,7 @@
 #include "hg_dual.cuh"
 #include "hg_f32.cuh"
 #include "hg_reduce.cuh"
+#include "hg_wet_vjp.cuh"
 
 namespace hg {
 
@@ -85,11 +86,11 @@ __global__ void __launch_bounds__(kBlock, vjp_min_blocks<NS>()) k_vjp_f32(DevMes
   const float mj0 = mu[j], mj1 = mu[n + j], mj2 = mu[2 * n + j];
   float g0 = 0.0f, g1 = 0.0f, g2 = 0.0f, gn = 0.0f;
   if (!L.s.dry) {   // a dry cell's output is masked to zero, and its faces add to nothing else
-    // Wet-wet faces in reverse mode (roe_wet_vjp_f32, the own quantities'
+    // Wet-wet faces in reverse mode (roe_wet_vjp, the own quantities'
     // adjoints summed over the faces and taken back once); faces with a dry
     // neighbour through 3-direction duals of the reference solver.
-    const OwnF32 o = own_f32(L.s, m.gf);
-    OwnAdjF32 b;
+    const OwnV<float> o = own_v(L.s);
+    OwnAdj<float> b;
 #pragma unroll
     for (int k = 0; k < NS; ++k) {
       const float4 sl = __ldg(&m.SL[(size_t)k * n + j]);
@@ -102,7 +103,7 @@ __global__ void __launch_bounds__(kBlock, vjp_min_blocks<NS>()) k_vjp_f32(DevMes
       const float w1 = len * (mu[n + nb] / An - mj1 / Aj);
       const float w2 = len * (mu[2 * n + nb] / An - mj2 / Aj);
       if (!R.s.dry) {
-        roe_wet_vjp_f32(L.s, o, R.s, (R.s.xi - L.s.xi) + (R.xlo - L.xlo), m.gf, nx, ny, w0, w1, w2, b);
+        roe_wet_vjp<float>(L.s, o, R.s, (R.s.xi - L.s.xi) + (R.xlo - L.xlo), m.gf, nx, ny, w0, w1, w2, b);
       } else {
         const Side<F3> L3 = seeded<F3>(L.s, -1);
         const Side<F3> R3 = constant<F3>(R.s);
@@ -115,7 +116,7 @@ __global__ void __launch_bounds__(kBlock, vjp_min_blocks<NS>()) k_vjp_f32(DevMes
       }
     }
     float gx, gu, gv;
-    own_vjp_f32(L.s, o, m.gf, b, gx, gu, gv);
+    own_vjp<float>(L.s, o, m.gf, b, gx, gu, gv);
     g0 += gx;
     g1 += gu;
     g2 += gv;

@@ -19,6 +19,7 @@
 #include "hg_device.cuh"
 #include "hg_dual.cuh"
 #include "hg_reduce.cuh"
+#include "hg_wet_vjp.cuh"
 
 namespace hg {
 
@@ -78,6 +79,12 @@ __global__ void __launch_bounds__(kBlock) k_vjp_f64(DevMesh m, AdjDev a, const d
   const double mj0 = mu[j], mj1 = mu[n + j], mj2 = mu[2 * n + j];
   double g0 = 0.0, g1 = 0.0, g2 = 0.0, gn = 0.0, gzb = 0.0;
   const Side<D3> L3 = seeded<D3>(L, -1);
+  // Interior wet-wet faces in reverse mode (hg_wet_vjp.cuh); faces with a dry
+  // side through 3-direction duals of the reference solver.
+  const bool wetL = !L.dry;
+  OwnV<double> own;
+  if (wetL) own = own_v(L);
+  OwnAdj<double> bo;
   for (int k = 0; k < m.nslot; ++k) {
     const int32_t nb = m.nb[(size_t)k * n + j];
     if (nb == kNoFace) break;
@@ -89,6 +96,10 @@ __global__ void __launch_bounds__(kBlock) k_vjp_f64(DevMesh m, AdjDev a, const d
       const double w0 = len * (mu[nb] / An - mj0 / Aj);
       const double w1 = len * (mu[n + nb] / An - mj1 / Aj);
       const double w2 = len * (mu[2 * n + nb] / An - mj2 / Aj);
+      if (wetL && !R.dry) {
+        roe_wet_vjp<double>(L, own, R, R.xi - L.xi, m.g, nx, ny, w0, w1, w2, bo);
+        continue;
+      }
       const Side<D3> R3 = constant<D3>(R);
       D3 F[3];
       roe_flux<D3>(L3, R3, R3.xi - L3.xi, D3(m.g), D3(nx), D3(ny), D3(m.hsm), F);
@@ -119,11 +130,18 @@ __global__ void __launch_bounds__(kBlock) k_vjp_f64(DevMesh m, AdjDev a, const d
       a.bfGradTA[bf] = c[6];
     }
   }
+  if (wetL) {
+    double gx, gu, gv;
+    own_vjp<double>(L, own, m.g, bo, gx, gu, gv);
+    g0 += gx;
+    g1 += gu;
+    g2 += gv;
+  }
   // Sources (semi_discretize_swe_2D.jl:449-559), wet cells only.
   if (!L.dry) {
     const double s = sqrt(L.hu * L.hu + L.hv * L.hv + eps_c<double>());
     const double hp = L.h + m.hsm;
-    const double k = m.g * (m.man[j] * m.man[j]) / m.kn2 / pow(hp, 7.0 / 3.0) * s;
+    const double k = m.g * (m.man[j] * m.man[j]) / m.kn2 / (hp * hp * cbrt(hp)) * s;   // as friction_coef
     const double dkdh = -(7.0 / 3.0) * k / hp;
     const double dkdqx = k * L.hu / (s * s), dkdqy = k * L.hv / (s * s);
     const double dkdn = 2.0 * k / m.man[j];

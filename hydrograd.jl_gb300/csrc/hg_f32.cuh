@@ -180,115 +180,4 @@ __device__ __forceinline__ void roe_flux_wet_f32(const Side<float>& L, const Own
   F[2] = 0.5f * ((o.fyx * nx + o.fyy * ny) + (R.hv * uR * nx + fR2y * ny) - A2);
 }
 
-// Adjoints of the own cell's quantities, accumulated over its wet-wet faces by
-// roe_wet_vjp_f32 and taken back to (xi, hu, hv) once by own_vjp_f32.
-struct OwnAdjF32 {
-  float u = 0.0f, v = 0.0f, s = 0.0f, fxx = 0.0f, fxy = 0.0f, fyx = 0.0f, fyy = 0.0f;
-  float h = 0.0f, hu = 0.0f, hv = 0.0f, xi = 0.0f;
-};
-
-// Reverse mode of roe_flux_wet_f32 in the own (left) side: adds
-// w . dF/d(own quantities) to b, with dxi = (xiR - xiL) + (lo parts).  The
-// forward values are recomputed here; the reverse sweep follows them in
-// reverse order (smooth_abs(x)' = x / smooth_abs(x), smooth_sqrt(x)' =
-// 1 / (2 smooth_sqrt(x))).
-__device__ __forceinline__ void roe_wet_vjp_f32(const Side<float>& L, const OwnF32& o, const Side<float>& R,
-                                                float dxi, float g, float nx, float ny, float w0, float w1, float w2,
-                                                OwnAdjF32& b) {
-  // forward
-  const float rq = rsqrtf(R.h);
-  const float rR = rq * rq;
-  const float uR = R.hu * rR, vR = R.hv * rR;
-  const float sR = R.h * rq;
-  const float rs = 1.0f / (o.s + sR);
-  const float numu = o.s * o.u + sR * uR, numv = o.s * o.v + sR * vR;
-  const float uRoe = numu * rs, vRoe = numv * rs;
-  const float un = uRoe * nx + vRoe * ny;
-  const float gh = g * ((L.h + R.h) * 0.5f);
-  const float rc = rsqrtf(gh);
-  const float c = gh * rc;
-  const float q = 0.5f * rc;
-  const float d1 = R.hu - L.hu, d2 = R.hv - L.hv;
-  const float T = un * dxi - nx * d1 - ny * d2;
-  const float t = T * q;
-  const float w0r = ny * d1 - nx * d2 - (uRoe * ny - vRoe * nx) * dxi;
-  const float a0 = smooth_abs_f32(un), a1 = smooth_abs_f32(un - c), a2 = smooth_abs_f32(un + c);
-  const float e1 = 0.5f * dxi + t, e2 = 0.5f * dxi - t;
-  const float W1 = e1 * a1, W2 = e2 * a2;
-  const float sum = W1 + W2;
-  // reverse: F = (fL + fR - A) / 2
-  const float bA0 = -0.5f * w0, bA1 = -0.5f * w1, bA2 = -0.5f * w2;
-  b.fxx += 0.5f * w1 * nx;
-  b.fxy += 0.5f * w1 * ny;
-  b.fyx += 0.5f * w2 * nx;
-  b.fyy += 0.5f * w2 * ny;
-  b.hu += 0.5f * w0 * nx;
-  b.hv += 0.5f * w0 * ny;
-  // A0 = sum, A1 = ny W0 + uRoe sum + nx dif, A2 = -nx W0 + vRoe sum + ny dif, dif = c (W2 - W1)
-  const float bW0 = ny * bA1 - nx * bA2;
-  const float bsum = bA0 + uRoe * bA1 + vRoe * bA2;
-  const float bdif = nx * bA1 + ny * bA2;
-  float buRoe = sum * bA1, bvRoe = sum * bA2;
-  float bc = (W2 - W1) * bdif;
-  const float bW1 = bsum - c * bdif, bW2 = bsum + c * bdif;
-  // W0 = w0r a0, W1 = e1 a1, W2 = e2 a2
-  const float bw0r = a0 * bW0;
-  const float ba0 = w0r * bW0, ba1 = e1 * bW1, ba2 = e2 * bW2;
-  const float bt = a1 * bW1 - a2 * bW2;
-  float bdxi = 0.5f * (a1 * bW1 + a2 * bW2);
-  const float r0 = un / a0, r1 = (un - c) / a1, r2 = (un + c) / a2;
-  float bun = ba0 * r0 + ba1 * r1 + ba2 * r2;
-  bc += ba2 * r2 - ba1 * r1;
-  // w0r = ny d1 - nx d2 - (uRoe ny - vRoe nx) dxi
-  float bd1 = ny * bw0r, bd2 = -nx * bw0r;
-  buRoe -= ny * dxi * bw0r;
-  bvRoe += nx * dxi * bw0r;
-  bdxi -= (uRoe * ny - vRoe * nx) * bw0r;
-  // t = T q, q = 1 / (2 c), T = un dxi - nx d1 - ny d2
-  const float bT = q * bt;
-  bc -= T * bt * q / c;
-  bun += dxi * bT;
-  bdxi += un * bT;
-  bd1 -= nx * bT;
-  bd2 -= ny * bT;
-  b.hu -= bd1;
-  b.hv -= bd2;
-  // c = smooth_sqrt(g (hL + hR) / 2)
-  b.h += 0.5f * g * q * bc;
-  // un = uRoe nx + vRoe ny; uRoe = numu rs, rs = 1 / (s + sR)
-  buRoe += nx * bun;
-  bvRoe += ny * bun;
-  const float bnumu = rs * buRoe, bnumv = rs * bvRoe;
-  const float brs = numu * buRoe + numv * bvRoe;
-  b.s += o.u * bnumu + o.v * bnumv - rs * rs * brs;
-  b.u += o.s * bnumu;
-  b.v += o.s * bnumv;
-  b.xi -= bdxi;
-}
-
-// Takes the accumulated adjoints of the own quantities (own_f32) back to the
-// own state: returns d/d(xi, hu, hv).
-__device__ __forceinline__ void own_vjp_f32(const Side<float>& L, const OwnF32& o, float g, OwnAdjF32 b, float& gxi,
-                                            float& ghu, float& ghv) {
-  // Derivative of the reference flux, with the own pressure in the tensor:
-  // fxx = hu u + p, fxy = hu v, fyx = hv u, fyy = hv v + p.  (The forward
-  // pass's p_L n shift sums to zero over the cell's faces.)
-  b.hu += o.u * b.fxx + o.v * b.fxy;
-  b.hv += o.u * b.fyx + o.v * b.fyy;
-  b.u += L.hu * b.fxx + L.hv * b.fyx;
-  b.v += L.hu * b.fxy + L.hv * b.fyy;
-  const float bp = b.fxx + b.fyy;
-  // p = g/2 (smooth_pow2(xi) + 2 xi hstill)
-  b.xi += bp * g * ((L.xi + eps_c<float>()) + L.hst);
-  // s = smooth_sqrt(h); u = hu / h, v = hv / h; h = xi + hstill
-  const float rh = 1.0f / L.h;
-  b.h += b.s * 0.5f / o.s;
-  b.hu += b.u * rh;
-  b.hv += b.v * rh;
-  b.h -= (b.u * o.u + b.v * o.v) * rh;
-  gxi = b.xi + b.h;
-  ghu = b.hu;
-  ghv = b.hv;
-}
-
 }  // namespace hgd

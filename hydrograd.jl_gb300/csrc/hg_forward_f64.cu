@@ -43,10 +43,67 @@ __device__ __forceinline__ Side<double> load_f64(const DevMesh& m, const double*
   return s;
 }
 
+// The quantities of a wet own cell that the reference's Roe solver forms on
+// every one of its faces (swe_2D_solvers.jl:79-127), formed once: the same
+// operations in the same order, so the fluxes are bit-identical.
+struct OwnF64 {
+  double uL, vL, sL, pL;
+  double hu_uL_pL, hu_vL, hv_uL, hv_vL_pL;   // L.hu*uL + pL, L.hu*vL, L.hv*uL, L.hv*vL + pL
+};
+
+__device__ __forceinline__ OwnF64 own_f64(const Side<double>& L, double g) {
+  OwnF64 o;
+  o.uL = L.hu / L.h;
+  o.vL = L.hv / L.h;
+  o.sL = smooth_sqrt(L.h);
+  o.pL = 0.5 * g * (smooth_pow2(L.xi) + 2.0 * L.xi * L.hst);
+  o.hu_uL_pL = L.hu * o.uL + o.pL;
+  o.hu_vL = L.hu * o.vL;
+  o.hv_uL = L.hv * o.uL;
+  o.hv_vL_pL = L.hv * o.vL + o.pL;
+  return o;
+}
+
+// roe_flux<double> of a face with both sides wet (the branch-free path), with
+// the own cell's terms from own_f64.
+__device__ __forceinline__ void roe_flux_wet_f64(const Side<double>& L, const OwnF64& o, const Side<double>& R,
+                                                 double dxi, double g, double nx, double ny, double F[3]) {
+  const double uL = o.uL, vL = o.vL, uR = R.hu / R.h, vR = R.hv / R.h;
+  const double sL = o.sL, sR = smooth_sqrt(R.h);
+  const double hRoe = (L.h + R.h) / 2.0;
+  const double uRoe = (sL * uL + sR * uR) / (sL + sR);
+  const double vRoe = (sL * vL + sR * vR) / (sL + sR);
+  const double unRoe = uRoe * nx + vRoe * ny;
+  const double cRoe = smooth_sqrt(g * hRoe);
+  const double o2c = 0.5 / cRoe;
+  const double d1 = R.hu - L.hu, d2 = R.hv - L.hv;
+  double w0 = -(uRoe * ny - vRoe * nx) * dxi + ny * d1 + (-nx) * d2;
+  double w1 = (unRoe * o2c + 0.5) * dxi + (-nx * o2c) * d1 + (-ny * o2c) * d2;
+  double w2 = (-unRoe * o2c + 0.5) * dxi + (nx * o2c) * d1 + (ny * o2c) * d2;
+  w0 *= smooth_abs(unRoe);
+  w1 *= smooth_abs(unRoe - cRoe);
+  w2 *= smooth_abs(unRoe + cRoe);
+  const double A0 = w1 + w2;
+  const double A1 = ny * w0 + (uRoe - cRoe * nx) * w1 + (uRoe + cRoe * nx) * w2;
+  const double A2 = (-nx) * w0 + (vRoe - cRoe * ny) * w1 + (vRoe + cRoe * ny) * w2;
+  const double pR = 0.5 * g * (smooth_pow2(R.xi) + 2.0 * R.xi * R.hst);
+  const double fL0 = L.hu * nx + L.hv * ny;
+  const double fL1 = o.hu_uL_pL * nx + o.hu_vL * ny;
+  const double fL2 = o.hv_uL * nx + o.hv_vL_pL * ny;
+  const double fR0 = R.hu * nx + R.hv * ny;
+  const double fR1 = (R.hu * uR + pR) * nx + R.hu * vR * ny;
+  const double fR2 = (R.hv * uR) * nx + (R.hv * vR + pR) * ny;
+  F[0] = (fL0 + fR0 - A0) / 2.0;
+  F[1] = (fL1 + fR1 - A1) / 2.0;
+  F[2] = (fL2 + fR2 - A2) / 2.0;
+}
+
 // Sum over faces of F * L for cell c (FP64).
 __device__ __forceinline__ void face_sum_f64(const DevMesh& m, const double* __restrict__ Q, int c,
                                              const Side<double>& L, double& f0, double& f1, double& f2) {
   f0 = 0.0; f1 = 0.0; f2 = 0.0;
+  OwnF64 own;
+  if (!L.dry) own = own_f64(L, m.g);
   for (int k = 0; k < m.nslot; ++k) {
     const int32_t nb = m.nb[(size_t)k * m.n + c];
     if (nb == kNoFace) break;
@@ -63,7 +120,8 @@ __device__ __forceinline__ void face_sum_f64(const DevMesh& m, const double* __r
                               m.bfLp23[bf], m.man[c]);
     }
     double F[3];
-    roe_flux<double>(L, R, R.xi - L.xi, m.g, nx, ny, m.hsm, F);
+    if (!L.dry && !R.dry) roe_flux_wet_f64(L, own, R, R.xi - L.xi, m.g, nx, ny, F);
+    else roe_flux<double>(L, R, R.xi - L.xi, m.g, nx, ny, m.hsm, F);
     f0 = f0 + F[0] * len;
     f1 = f1 + F[1] * len;
     f2 = f2 + F[2] * len;
