@@ -26,116 +26,19 @@ import sys
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-BC_CODES = {"wall": 0, "symm": 1, "inlet-q": 2, "exit-h": 3}
+sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(HERE)), "hydrograd.jl_gb300"))
 
-
-def read_srhgeom(path):
-    """Elem / Node / NodeString records (SRH_2D_SRHGeom.jl:150-219)."""
-    elems, nodes, strings = {}, {}, {}
-    cur = None
-    with open(path) as fh:
-        for line in fh:
-            parts = line.split()
-            if not parts:
-                continue
-            if parts[0] == "Elem":
-                elems[int(parts[1])] = [int(p) for p in parts[2:]]
-                cur = None
-            elif parts[0] == "Node":
-                nodes[int(parts[1])] = [float(p) for p in parts[2:5]]
-                cur = None
-            elif parts[0] == "NodeString":
-                cur = int(parts[1])
-                strings[cur] = [int(p) for p in parts[2:]]
-            elif parts[0].lower() in ("name", "gridunit") or "srhgeom" in parts[0].lower():
-                continue
-            elif cur is not None:
-                strings[cur].extend(int(p) for p in parts)
-    n_nodes = max(nodes)
-    xyz = np.zeros((n_nodes, 3))
-    for k, v in nodes.items():
-        xyz[k - 1] = v
-    n_cells = max(elems)
-    cell_nodes = np.full((n_cells, 8), -1, dtype=np.int32)
-    counts = np.zeros(n_cells, dtype=np.int32)
-    for k, v in elems.items():
-        cell_nodes[k - 1, : len(v)] = np.array(v) - 1
-        counts[k - 1] = len(v)
-    return xyz, cell_nodes, counts, strings
-
-
-def read_srhhydro(path):
-    """ManningsN / BC / IQParams / EWSParamsC records (SRH_2D_SRHHydro.jl:25-96)."""
-    out = {"ManningsN": {}, "BC": {}, "IQParams": {}, "EWSParamsC": {}}
-    with open(path) as fh:
-        for line in fh:
-            parts = line.split()
-            if len(parts) <= 1:
-                continue
-            if parts[0] == "ManningsN":
-                out["ManningsN"][int(parts[1])] = float(parts[2])
-            elif parts[0] == "BC" and parts[2] != "MONITORING":
-                out["BC"][int(parts[1])] = parts[2]
-            elif parts[0] == "IQParams":
-                out["IQParams"][int(parts[1])] = float(parts[2])
-            elif parts[0] == "EWSParamsC":
-                out["EWSParamsC"][int(parts[1])] = float(parts[2])
-    return out
-
-
-def read_srhmat(path, n_cells):
-    """Material zones -> matID per cell, 0 = default zone (SRH_2D_SRHMat.jl:30-108;
-    process_SRH_2D_input.jl:136-153)."""
-    zones, cur = {}, 0
-    with open(path) as fh:
-        for line in fh:
-            parts = line.split()
-            if not parts or parts[0] in ("SRHMAT", "NMaterials", "MatName"):
-                continue
-            if parts[0] == "Material":
-                cur = int(parts[1])
-                zones.setdefault(cur, []).extend(int(p) for p in parts[2:])
-            elif cur:
-                zones[cur].extend(int(p) for p in parts)
-    mat = np.zeros(n_cells, dtype=np.int32)
-    for k, cells in zones.items():
-        for c in cells:
-            mat[c - 1] = k
-    return mat
+from hydrograd_gb.srh2d import read_case  # noqa: E402  (the package's SRH-2D reader)
 
 
 def build_case(case_dir, hydro_name=None):
     ctl = json.load(open(os.path.join(case_dir, "run_control.json")))
     hydro_name = hydro_name or ctl["control_variables"]["srhhydro_file_name"]
-    hydro = read_srhhydro(os.path.join(case_dir, hydro_name))
     stem = os.path.splitext(hydro_name)[0]
     geom_file = [f for f in os.listdir(case_dir) if f.endswith(".srhgeom") and f.startswith(stem)]
     geom_file = geom_file[0] if geom_file else [f for f in os.listdir(case_dir) if f.endswith(".srhgeom")][0]
-    xyz, cell_nodes, counts, strings = read_srhgeom(os.path.join(case_dir, geom_file))
-    mat_file = os.path.join(case_dir, os.path.splitext(geom_file)[0] + ".srhmat")
-    mat = read_srhmat(mat_file, len(counts))
-    ids = sorted(strings)
-    # A NodeString is a boundary when the hydro file gives it a BC
-    # (SRH_2D_SRHGeom.jl:306-310); otherwise it is skipped (-1).
-    bc = [BC_CODES.get(hydro["BC"].get(i, "").lower(), -1) for i in ids]
-    offsets = np.cumsum([0] + [len(strings[i]) for i in ids]).astype(np.int32)
-    snodes = np.concatenate([np.array(strings[i], dtype=np.int32) - 1 for i in ids])
-    inlet_ids = [i for i in ids if hydro["BC"].get(i, "").lower() == "inlet-q"]
-    exit_ids = [i for i in ids if hydro["BC"].get(i, "").lower() == "exit-h"]
-    d = dict(
-        node_xyz=xyz,
-        cell_nodes=cell_nodes,
-        cell_node_count=counts,
-        string_ids=np.array(ids, dtype=np.int32),
-        string_offsets=offsets,
-        string_nodes=snodes,
-        string_bc=np.array(bc, dtype=np.int32),
-        inlet_q=np.array([hydro["IQParams"][i] for i in inlet_ids]),
-        exit_wse=np.array([hydro["EWSParamsC"][i] for i in exit_ids]),
-        mat_id=mat,
-        manning_zones=np.array([hydro["ManningsN"][k] for k in sorted(hydro["ManningsN"])]),
-        tspan=np.array(ctl["time_settings"]["tspan"], dtype=float),
-    )
+    d = read_case(os.path.join(case_dir, geom_file), os.path.join(case_dir, hydro_name))
+    d["tspan"] = np.array(ctl["time_settings"]["tspan"], dtype=float)
     return ctl, d
 
 
@@ -178,7 +81,10 @@ def sensitivity_case(ref, rel, out_name):
 
 
 def main():
+    global HERE
     ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) > 2:   # write the fixtures elsewhere (to compare with the committed ones)
+        HERE = sys.argv[2]
     ex = "examples/SWE_2D"
     forward_case(ref, f"{ex}/forward_simulation/oneD_channel_with_bump", "fwd_bump.npz")
     forward_case(ref, f"{ex}/forward_simulation/oneD_channel_uniform_flow", "fwd_uniform.npz")

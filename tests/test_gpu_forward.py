@@ -240,3 +240,23 @@ def test_initial_depth_check():
     Q[5] = 1e-4
     with pytest.raises(HgError):
         ctx.check_initial_state(Q)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32c"])
+@pytest.mark.parametrize("name", ["fwd_bump", "fwd_uniform", "fwd_savannah"])
+def test_shipped_cases_reach_reference_final_state(name, precision):
+    """The reference's example cases (read from their SRH-2D files by
+    hydrograd_gb.srh2d into the fixtures) run on the device with SSP-RK2 to the
+    case's end time, against the final state of the reference's own Tsit5 run
+    (abstol 1e-6, reltol 1e-3), as the oracle is checked: within 2e-3 of scale."""
+    d = load_fixture(name)
+    N = len(d["cell_node_count"])
+    ctx, o, _ = setup_pair(d, precision)
+    Q0 = initial_state(d, N)
+    T = float(d["tspan"][1])
+    nsteps = int(np.ceil(T / (0.8 * o.cfl_dt(Q0, 0.4))))
+    Q, _ = ctx.integrate(Q0, nsteps, dt=T / nsteps)
+    h = d["h_truth"]
+    ref = np.concatenate([d["xi_truth"], d["u_truth"] * (h + 1e-3), d["v_truth"] * (h + 1e-3)])
+    scale = max(np.abs(ref[:N]).max(), np.abs(ref[N:]).max())
+    assert np.abs(Q - ref).max() <= 2e-3 * scale
