@@ -65,6 +65,9 @@ SIGNATURES = {
     "hg_check_initial_state": [_vp, _dp],
     "hg_integrate": [_vp, _dp, ctypes.c_double, ctypes.c_int32, ctypes.c_int32, ctypes.c_double, ctypes.c_double,
                      ctypes.c_int32, _dp, _dp],
+    "hg_integrate_tsit5": [_vp, _dp, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                           ctypes.c_double, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, _dp, _dp, _ip],
+    "hg_tsit5_tableau": [_dp, _dp, _dp, _dp],
     "hg_state_upload": [_vp, _dp],
     "hg_state_download": [_vp, _dp],
     "hg_advance": [_vp, ctypes.c_int32, ctypes.c_double, ctypes.c_double, ctypes.c_int32],

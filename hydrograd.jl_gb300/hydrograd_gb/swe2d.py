@@ -185,6 +185,23 @@ class SWE2D:
             return Q, dts[:nsteps], saves
         return Q, dts[:nsteps]
 
+    def integrate_tsit5(self, Q, t0, t1, abstol=1e-6, reltol=1e-3, dt0=None, adaptive=True, max_steps=0,
+                        saveat=None):
+        """Tsit5 (Tsitouras 5(4)) from t0 to t1 on the device, as
+        solve(prob, Tsit5(); abstol, reltol, saveat) integrates the reference's
+        ODE problem (adaptive=False: fixed steps of dt0).  Returns (Q, stats[,
+        saves]) with stats = (accepted, rejected, RHS evaluations) and saves[i]
+        the state at saveat[i]."""
+        Q = np.array(Q, dtype=np.float64)
+        ts = np.ascontiguousarray(saveat if saveat is not None else [], dtype=np.float64)
+        saves = np.zeros((len(ts), Q.size)) if len(ts) else None
+        st = np.zeros(3, dtype=np.int32)
+        self._chk(lib().hg_integrate_tsit5(self.h, _d(Q), float(t0), float(t1), float(abstol), float(reltol),
+                                           float(dt0) if dt0 else -1.0, 1 if adaptive else 0, int(max_steps), len(ts),
+                                           _d(ts) if len(ts) else None, _d(saves), _i(st)))
+        stats = tuple(int(v) for v in st)
+        return (Q, stats, saves) if saves is not None else (Q, stats)
+
     def upload(self, Q):
         self._chk(lib().hg_state_upload(self.h, _d(np.ascontiguousarray(Q, dtype=np.float64))))
 

@@ -144,6 +144,23 @@ int hg_ensemble_create(const hg_ensemble_desc* ensemble, const hg_consts* consts
 int hg_ensemble_layout(const hg_ctx* ctx, int32_t* n_members, int32_t* cell_offset, int32_t* inlet_offset,
                        int32_t* exit_offset);
 
+/* ---- Tsit5 (the reference's default solver, swe_2D_forward_simulation.jl:37-39)
+ * Adaptive Tsitouras 5(4) steps of the RHS from t0 to t1 on the device, Q in/out
+ * (caller order).  Error control: weighted RMS norm of the embedded error
+ * with scale abstol + reltol max(|Q_old|, |Q_new|), PI step-size controller,
+ * step factor in [0.2, 10] with safety 0.9; dt0 <= 0 picks the starting step
+ * (Hairer-Norsett-Wanner II.4).  adaptive == 0 takes fixed steps of dt0 > 0
+ * with no error control (solve(...; adaptive=false, dt=dt0)).  The n_save
+ * ascending times t_save in (t0, t1] are stepped onto and their states
+ * written to saves[n_save][3N].  max_steps <= 0: no limit.  stats (may be
+ * NULL): accepted steps, rejected steps, RHS evaluations.  No clamp besides
+ * the RHS's own, as in the reference's ODE solve. */
+int hg_integrate_tsit5(hg_ctx* ctx, double* Q, double t0, double t1, double abstol, double reltol, double dt0,
+                       int32_t adaptive, int32_t max_steps, int32_t n_save, const double* t_save, double* saves,
+                       int32_t* stats);
+/* The Butcher tableau in use: c[7], a[7][7] (row-major, lower triangle), b[7], btilde[7] = b - bhat. */
+int hg_tsit5_tableau(double* c7, double* a49, double* b7, double* btilde7);
+
 int hg_destroy(hg_ctx* ctx);
 int hg_sizes(const hg_ctx* ctx, int32_t* sizes8); /* as hg_mesh_sizes */
 

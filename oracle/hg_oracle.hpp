@@ -646,4 +646,108 @@ void rk2_step(const Case& cs, const Params<T>& p, std::vector<T>& Q, double dt, 
   clamp_stage<T>(cs, Q.data());
 }
 
+// Tsitouras 5(4) pair (Ch. Tsitouras, Comput. Math. Appl. 62 (2011)
+// 770-775), restated from the published tableau, with the step control of
+// Hairer, Norsett & Wanner, Solving ODEs I, II.4: weighted RMS norm of the
+// embedded error (scale abstol + reltol max(|Q|, |Qnew|)), PI controller with
+// gains 0.14 / 0.08, safety 0.9, factor in [0.2, 10], the starting step of
+// II.4 when dt0 <= 0, and steps clamped onto t1; adaptive == false takes fixed
+// steps of dt0.  The CPU check of the device integrator (same algorithm);
+// stats: accepted, rejected, RHS evaluations.  Returns false after maxSteps
+// steps.
+struct Tsit5Stats {
+  int accepted = 0, rejected = 0, evals = 0;
+};
+
+inline bool tsit5(const Case& cs, const Params<double>& p, std::vector<double>& Q, double t0, double t1, double abstol,
+                  double reltol, double dt0, bool adaptive, int maxSteps, Tsit5Stats& st, int nthreads = 1) {
+  static const double C[7] = {0.0, 0.161, 0.327, 0.9, 0.9800255409045097, 1.0, 1.0};
+  static const double A[7][6] = {
+      {0, 0, 0, 0, 0, 0},
+      {0.161, 0, 0, 0, 0, 0},
+      {-0.008480655492356989, 0.335480655492357, 0, 0, 0, 0},
+      {2.897153057105493, -6.359448489975075, 4.3622954328695815, 0, 0, 0},
+      {5.325864828439257, -11.748883564062828, 7.4955393428898365, -0.09249506636175525, 0, 0},
+      {5.86145544294642, -12.92096931784711, 8.159367898576159, -0.071584973281401, -0.028269050394068383, 0},
+      {0.09646076681806523, 0.01, 0.4798896504144996, 1.379008574103742, -3.290069515436081, 2.324710524099774}};
+  static const double BT[7] = {-0.00178001105222577714, -0.0008164344596567469, 0.007880878010261995,
+                               -0.1447110071732629, 0.5823571654525552, -0.45808210592918697, 0.015151515151515152};
+  (void)C;
+  const size_t n3 = Q.size();
+  std::vector<std::vector<double>> K(7, std::vector<double>(n3));
+  std::vector<double> Y(n3), Qn(n3);
+  auto norm = [&](const std::vector<double>& ua, const std::vector<double>& ub, const std::vector<double>& e) {
+    double s = 0.0;
+    for (size_t i = 0; i < n3; ++i) {
+      const double r = e[i] / (abstol + reltol * std::max(std::fabs(ua[i]), std::fabs(ub[i])));
+      s += r * r;
+    }
+    return std::sqrt(s / (double)n3);
+  };
+  rhs<double>(cs, p, Q.data(), K[0].data(), nthreads);
+  st.evals = 1;
+  double dt = dt0;
+  if (adaptive && !(dt > 0)) {
+    const double d0 = norm(Q, Q, Q), d1 = norm(Q, Q, K[0]);
+    const double h0 = (d0 < 1e-5 || d1 < 1e-5) ? 1e-6 : 0.01 * d0 / d1;
+    for (size_t i = 0; i < n3; ++i) Y[i] = Q[i] + h0 * K[0][i];
+    rhs<double>(cs, p, Y.data(), K[1].data(), nthreads);
+    ++st.evals;
+    std::vector<double> df(n3);
+    for (size_t i = 0; i < n3; ++i) df[i] = (K[1][i] - K[0][i]) / h0;
+    const double d2 = norm(Q, Q, df);
+    const double m = std::max(d1, d2);
+    const double h1 = m <= 1e-15 ? std::max(1e-6, h0 * 1e-3) : std::pow(0.01 / m, 1.0 / 5.0);
+    dt = std::min(100.0 * h0, h1);
+  }
+  if (adaptive) dt = std::min(dt, t1 - t0);
+  const double beta1 = 7.0 / 50.0, beta2 = 2.0 / 25.0, gamma = 0.9, qmin = 0.2, qmax = 10.0;
+  double errOld = 1e-4, t = t0;
+  std::vector<double> E(n3);
+  while (t1 - t > 1e-14 * std::max(1.0, std::fabs(t1))) {
+    if (st.accepted + st.rejected >= maxSteps) return false;
+    double h = dt;
+    bool hit = false;
+    if (t + h >= t1 - 1e-14 * std::max(1.0, std::fabs(t1))) {
+      h = t1 - t;
+      hit = true;
+    }
+    for (int i = 1; i < 7; ++i) {
+      std::vector<double>& dst = (i == 6) ? Qn : Y;
+      for (size_t k = 0; k < n3; ++k) {
+        double s = 0.0;
+        for (int j = 0; j < i; ++j) s += A[i][j] * K[j][k];
+        dst[k] = Q[k] + h * s;
+      }
+      rhs<double>(cs, p, dst.data(), K[i].data(), nthreads);
+    }
+    st.evals += 6;
+    double eest = 0.0;
+    if (adaptive) {
+      for (size_t k = 0; k < n3; ++k) {
+        double s = 0.0;
+        for (int j = 0; j < 7; ++j) s += BT[j] * K[j][k];
+        E[k] = h * s;
+      }
+      eest = norm(Q, Qn, E);
+    }
+    if (eest <= 1.0) {
+      t = hit ? t1 : t + h;
+      Q.swap(Qn);
+      K[0].swap(K[6]);
+      ++st.accepted;
+      if (!adaptive) continue;
+      const double fac = std::min(qmax, std::max(qmin, gamma * std::pow(std::max(eest, 1e-12), -beta1) *
+                                                            std::pow(errOld, beta2)));
+      errOld = std::max(eest, 1e-4);
+      dt = h * fac;
+    } else {
+      ++st.rejected;
+      dt = h * (std::isfinite(eest) ? std::max(qmin, gamma * std::pow(eest, -beta1)) : qmin);
+      if (dt < 1e-14 * std::max(1.0, std::fabs(t))) return false;
+    }
+  }
+  return true;
+}
+
 }  // namespace hgo

@@ -47,6 +47,8 @@ def _load():
     lib.ho_cfl_dt.restype = ctypes.c_double
     lib.ho_cfl_dt.argtypes = [ctypes.c_void_p, _dp, ctypes.c_double]
     lib.ho_rk2.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int, _dp]
+    lib.ho_tsit5.argtypes = [ctypes.c_void_p, _dp, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                             ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int, _ip]
     lib.ho_euler_reference.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int, ctypes.c_double, ctypes.c_int]
     lib.ho_rk2_tangent.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int, ctypes.c_double, ctypes.c_int, _dp, _dp, _dp,
                                    ctypes.c_int, _ip, _dp, _dp, _dp, _dp, _dp, ctypes.c_int]
@@ -162,6 +164,16 @@ class Oracle:
         if rc != 0:
             raise RuntimeError("oracle: " + self.lib.ho_last_error().decode())
         return (Q, dts[:nsteps]) if return_dts else Q
+
+    def tsit5(self, Q, t0, t1, abstol=1e-6, reltol=1e-3, dt0=0.0, adaptive=True, max_steps=0, nthreads=1):
+        """Tsit5 from t0 to t1 (hgo::tsit5); returns (Q, (accepted, rejected, evals))."""
+        Q = np.array(Q, dtype=np.float64)
+        st = np.zeros(3, dtype=np.int32)
+        rc = self.lib.ho_tsit5(self.h, _d(Q), t0, t1, abstol, reltol, dt0, 1 if adaptive else 0, max_steps, nthreads,
+                               _i(st))
+        if rc != 0:
+            raise RuntimeError("oracle: " + self.lib.ho_last_error().decode())
+        return Q, tuple(int(v) for v in st)
 
     def euler_reference(self, Q, nsteps, dt, nthreads=1):
         Q = np.array(Q, dtype=np.float64)

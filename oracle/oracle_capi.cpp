@@ -251,6 +251,35 @@ int ho_rk2(void* h, double* Q, int nsteps, double dt, double cfl, int nthreads, 
   return 0;
 }
 
+// Tsit5 from t0 to t1 (hgo::tsit5); stats[3] = accepted, rejected, RHS evaluations.
+int ho_tsit5(void* h, double* Q, double t0, double t1, double abstol, double reltol, double dt0, int adaptive,
+             int maxSteps, int nthreads, int* stats) {
+  auto* oc = static_cast<OracleCase*>(h);
+  try {
+    std::vector<double> q(Q, Q + 3 * (size_t)oc->cs.mesh.nCells);
+    Tsit5Stats st;
+    if (!adaptive && !(dt0 > 0)) {
+      g_err = "tsit5: fixed steps need dt0 > 0";
+      return 1;
+    }
+    if (!tsit5(oc->cs, oc->p, q, t0, t1, abstol, reltol, dt0, adaptive != 0, maxSteps > 0 ? maxSteps : 10000000, st,
+               nthreads)) {
+      g_err = "tsit5: step limit or step-size underflow";
+      return 1;
+    }
+    std::memcpy(Q, q.data(), q.size() * sizeof(double));
+    if (stats) {
+      stats[0] = st.accepted;
+      stats[1] = st.rejected;
+      stats[2] = st.evals;
+    }
+  } catch (const std::exception& e) {
+    g_err = e.what();
+    return 1;
+  }
+  return 0;
+}
+
 // Reference forward-Euler loop with its clamp (custom_ODE_solvers.jl:5-33).
 int ho_euler_reference(void* h, double* Q, int nsteps, double dt, int nthreads) {
   auto* oc = static_cast<OracleCase*>(h);
