@@ -175,8 +175,15 @@ int enqueue_download(hg_ctx* c, double* Q) {
   return HG_OK;
 }
 
-// The FP32 path steps with two fused launches when the inlet groups fit.
-bool fused(const hg_ctx* c) { return c->precision == HG_FP32C && c->dm.nInlet <= kMaxFusedInlets; }
+// The FP32 path steps with two fused launches when the inlet groups fit and
+// the resistance does not depend on the state (the fused stage forms the next
+// stage's conveyance totals from its output state with the resident n).
+bool fused(const hg_ctx* c) {
+  return c->precision == HG_FP32C && c->dm.nInlet <= kMaxFusedInlets && c->dm.res.kind == kResConstant;
+}
+
+// Kernels per RHS evaluation besides the stage: resistance, inlet totals.
+int rhs_prep_launches(const hg_ctx* c) { return resistance_launches(c->dm) + (c->dm.nInlet > 0 ? 1 : 0); }
 
 // Before a run of fused steps: conveyance totals of the resident state and, in
 // CFL mode, its CFL minimum in buffer 0 (the fixed dt is already on the device).
@@ -234,7 +241,7 @@ void enqueue_rk2_step(hg_ctx* c, bool cflMode, double cfl) {
     launch_inlet_total_f32(c->dm, c->ds, xb(c), c->stream);
     launch_stage_f32(c->dm, c->ds, kModeStage2, xb(c), xa(c), xa(c), nullptr, cflMode, c->stream);
   }
-  c->launches += 3 + (c->dm.nInlet > 0 ? 2 : 0);
+  c->launches += 3 + 2 * rhs_prep_launches(c);
 }
 
 void enqueue_euler_step(hg_ctx* c, bool cflMode, double cfl) {
@@ -251,7 +258,7 @@ void enqueue_euler_step(hg_ctx* c, bool cflMode, double cfl) {
     std::swap(c->XA, c->XB);
     std::swap(c->XQA, c->XQB);
   }
-  c->launches += 2 + (c->dm.nInlet > 0 ? 1 : 0) + (cflMode ? 1 : 0);
+  c->launches += 2 + rhs_prep_launches(c) + (cflMode ? 1 : 0);
 }
 
 void enqueue_cfl_prime(hg_ctx* c) {
@@ -281,6 +288,52 @@ int begin_steps(hg_ctx* c, bool rk2, double dt, double cfl) {
     enqueue_cfl_prime(c);
   }
   return HG_OK;
+}
+
+// Network parameters a hg_ude_desc can describe (3 inputs, 4 hidden layers of 16).
+constexpr int kResMaxParams = kResMaxInputs * kResMaxWidth + 3 * kResMaxWidth +
+                              (kResMaxLayers - 1) * (kResMaxWidth * kResMaxWidth + 3 * kResMaxWidth) +
+                              kResMaxWidth + 1;
+
+// Puts r in place as the context's resistance: device buffers on first use,
+// ks and the network parameters uploaded, the captured graph dropped (it holds
+// the old DevMesh by value).
+int install_resistance(hg_ctx* c, ResDev r, const double* ksUser, const double* params, int nParams) {
+  if (!c->d_resKs) {
+    HG_CUDA(c, dalloc(c, &c->d_resKs, c->n));
+    HG_CUDA(c, dalloc(c, &c->d_resW, kResMaxParams));
+    HG_CUDA(c, dalloc(c, &c->d_resWf, kResMaxParams));
+    HG_CUDA(c, dalloc(c, &c->d_resStats, 2 * kResMaxLayers));
+    HG_CUDA(c, dalloc(c, &c->d_resPartials, kResPartials));
+    HG_CUDA(c, dalloc(c, &c->d_resTicket, 1));
+    HG_CUDA(c, dalloc(c, &c->d_fres, c->n));
+    HG_CUDA(c, dalloc(c, &c->d_fresF, c->n));
+    HG_CUDA(c, cudaMemsetAsync(c->d_resTicket, 0, sizeof(unsigned int), c->stream));
+  }
+  std::vector<double> ks, w(params, params + nParams);
+  std::vector<float> wf = to_float(w);
+  if (ksUser) ks = to_device_order(c, ksUser);
+  HG_CUDA(c, upload(c, c->d_resKs, ks));
+  HG_CUDA(c, upload(c, c->d_resW, w));
+  HG_CUDA(c, upload(c, c->d_resWf, wf));
+  HG_CUDA(c, cudaStreamSynchronize(c->stream));
+  r.ks = ksUser ? c->d_resKs : nullptr;
+  r.w = c->d_resW;
+  r.wf = c->d_resWf;
+  r.stats = c->d_resStats;
+  r.partials = c->d_resPartials;
+  r.ticket = c->d_resTicket;
+  r.fres = c->d_fres;
+  r.fresF = c->d_fresF;
+  c->dm.res = r;
+  c->graphValid = false;
+  return HG_OK;
+}
+
+bool all_positive(const double* v, int n) {
+  for (int i = 0; i < n; ++i)
+    if (!(v[i] > 0.0)) return false;
+  return true;
 }
 
 }  // namespace
@@ -523,6 +576,81 @@ int hg_set_exit_wse(hg_ctx* ctx, const double* w, int32_t n) {
   return upload_boundary_values(ctx);
 }
 
+int hg_set_manning_function(hg_ctx* ctx, int32_t kind, const double* params, int32_t n_params, const double* ks) {
+  if (!ctx) return fail(ctx, HG_ERR_ARG, "hg_set_manning_function: null context");
+  cudaSetDevice(ctx->device);
+  if (kind == HG_RES_CONSTANT) {   // back to the cells' n
+    ctx->dm.res = ResDev{};
+    ctx->graphValid = false;
+    return upload_cells(ctx);
+  }
+  if (kind < HG_RES_POWER_LAW || kind > HG_RES_H_UMAG_KS)
+    return fail(ctx, HG_ERR_ARG, "hg_set_manning_function: kind must be one of HG_RES_CONSTANT..HG_RES_H_UMAG_KS");
+  ResDev r;
+  r.kind = kind;
+  if (kind == HG_RES_H_UMAG_KS) {
+    if (!ks || !all_positive(ks, ctx->n))
+      return fail(ctx, HG_ERR_ARG, "hg_set_manning_function: h_Umag_ks needs a positive ks per cell");
+  } else {
+    const int need = kind == HG_RES_SIGMOID ? 4 : 3;
+    if (!params || n_params < need)
+      return fail(ctx, HG_ERR_ARG, "hg_set_manning_function: params = {n_lower, n_upper, k[, h_mid]}");
+    // the reference's own checks (process_ManningN_2D.jl:150,165,181-182)
+    if (!(params[2] > 0.0)) return fail(ctx, HG_ERR_ARG, "k must be a positive scaling factor");
+    if (kind == HG_RES_SIGMOID && !(params[3] > 0.0)) return fail(ctx, HG_ERR_ARG, "h_mid must be a positive water depth");
+    for (int i = 0; i < need; ++i) r.p[i] = params[i];
+  }
+  return install_resistance(ctx, r, kind == HG_RES_H_UMAG_KS ? ks : nullptr, nullptr, 0);
+}
+
+int hg_set_ude(hg_ctx* ctx, const hg_ude_desc* u) {
+  if (!ctx || !u) return fail(ctx, HG_ERR_ARG, "hg_set_ude: null argument");
+  if (u->kind < HG_RES_UDE_MANNING_H || u->kind > HG_RES_UDE_FLOW_RESISTANCE)
+    return fail(ctx, HG_ERR_ARG, "hg_set_ude: kind must be one of the HG_RES_UDE_* values");
+  if (u->n_hidden < 0 || u->n_hidden > kResMaxLayers || (u->n_hidden > 0 && (!u->hidden || !u->activation)))
+    return fail(ctx, HG_ERR_ARG, "hg_set_ude: 0 to 4 hidden layers");
+  ResDev r;
+  r.kind = u->kind;
+  r.inDim = u->kind == HG_RES_UDE_MANNING_H ? 1 : u->kind == HG_RES_UDE_MANNING_H_UMAG_KS ? 3 : 2;
+  r.nHidden = u->n_hidden;
+  r.overBatch = u->layernorm_over_batch ? 1 : 0;
+  r.lnEps = (double)1e-5f;   // Lux's LayerNorm default epsilon (Float32)
+  int din = r.inDim, count = 0;
+  for (int l = 0; l < u->n_hidden; ++l) {
+    const int w = u->hidden[l];
+    if (w < 1 || w > kResMaxWidth) return fail(ctx, HG_ERR_ARG, "hg_set_ude: hidden widths must be 1..16");
+    if (u->activation[l] < HG_ACT_RELU || u->activation[l] > HG_ACT_SOFTPLUS)
+      return fail(ctx, HG_ERR_ARG, "hg_set_ude: unknown activation");
+    r.width[l] = w;
+    r.act[l] = u->activation[l];
+    count += w * din + 3 * w;
+    din = w;
+  }
+  count += din + 1;
+  if (!u->params || u->n_params != count)
+    return fail(ctx, HG_ERR_ARG, "hg_set_ude: expected " + std::to_string(count) + " network parameters");
+  const double* b[3] = {u->h_bounds, u->u_bounds, u->ks_bounds};
+  for (int i = 0; i < 3; ++i) {
+    r.lo[i] = b[i][0];
+    r.hi[i] = b[i][1];
+  }
+  if (!(r.hi[0] != r.lo[0]) || (r.inDim > 1 && !(r.hi[1] != r.lo[1])) ||
+      (u->kind == HG_RES_UDE_MANNING_H_UMAG_KS && !(r.hi[2] != r.lo[2])))
+    return fail(ctx, HG_ERR_ARG, "hg_set_ude: empty input bounds");
+  if (u->kind == HG_RES_UDE_FLOW_RESISTANCE && !(r.hi[0] * r.hi[1] != r.lo[0] * r.lo[1]))
+    return fail(ctx, HG_ERR_ARG, "hg_set_ude: empty discharge bounds");
+  if (u->kind == HG_RES_UDE_MANNING_H_UMAG_KS && !u->ks_cells)
+    return fail(ctx, HG_ERR_ARG, "hg_set_ude: ManningN_h_Umag_ks needs ks per cell");
+  r.outLo = u->output_bounds[0];
+  r.outHi = u->output_bounds[1];
+  cudaSetDevice(ctx->device);
+  int rc = install_resistance(ctx, r, u->kind == HG_RES_UDE_MANNING_H_UMAG_KS ? u->ks_cells : nullptr, u->params,
+                              u->n_params);
+  if (rc) return rc;
+  // n returns to the cells' values where the closure replaces only the friction
+  return u->kind == HG_RES_UDE_FLOW_RESISTANCE ? upload_cells(ctx) : HG_OK;
+}
+
 int hg_get_bed(hg_ctx* ctx, double* zb, double* S0, double* man, double* hstill) {
   if (!ctx) return fail(ctx, HG_ERR_ARG, "hg_get_bed: null context");
   for (int i = 0; i < ctx->n; ++i) {
@@ -562,7 +690,7 @@ int hg_rhs(hg_ctx* ctx, const double* Q, double /*t*/, double* dQ) {
     launch_stage_f32(ctx->dm, ctx->ds, kModeRhs, xa(ctx), StateF32{}, StateF32{}, ctx->QB, false, ctx->stream);
     launch_scatter_state_f64(ctx->n, ctx->d_perm, ctx->QB, ctx->Quser, ctx->stream);
   }
-  ctx->launches += 4;
+  ctx->launches += 3 + rhs_prep_launches(ctx);   // reset, stage, scatter; resistance, inlet totals
   HG_CUDA(ctx, cudaMemcpyAsync(dQ, ctx->Quser, (size_t)3 * ctx->n * sizeof(double), cudaMemcpyDeviceToHost,
                                ctx->stream));
   HG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
@@ -786,6 +914,9 @@ int hg_loss_and_grad(hg_ctx* ctx, const double* Q0, int32_t nsteps, double dt, i
     return fail(ctx, HG_ERR_ARG, "hg_loss_and_grad: bad argument");
   for (int i = 0; i < n_probe; ++i)
     if (probe_cells[i] < 0 || probe_cells[i] >= ctx->n) return fail(ctx, HG_ERR_ARG, "hg_loss_and_grad: bad probe id");
+  if (ctx->dm.res.kind != kResConstant)
+    return fail(ctx, HG_ERR_UNSUPPORTED,
+                "hg_loss_and_grad: gradients through a state-dependent Manning n or a UDE closure are not available");
   cudaSetDevice(ctx->device);
   return adjoint_loss_and_grad(ctx, Q0, nsteps, dt, ckpt_every, probe_cells, obs, n_probe, loss, g_manning_cells, g_zb,
                                g_inletq, Q_final);

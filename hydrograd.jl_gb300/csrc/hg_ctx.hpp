@@ -68,6 +68,11 @@ struct hg_ctx {
   int64_t graphLaunches = 0;
   int64_t launches = 0;
   hg::AdjointBuffers* adj = nullptr;
+  // State-dependent resistance (hg_set_manning_function / hg_set_ude): device
+  // buffers, allocated on first use; dm.res points into them.
+  double *d_resKs = nullptr, *d_resW = nullptr, *d_resStats = nullptr, *d_resPartials = nullptr, *d_fres = nullptr;
+  float *d_resWf = nullptr, *d_fresF = nullptr;
+  unsigned int* d_resTicket = nullptr;
   std::string err;
   ~hg_ctx();
 };

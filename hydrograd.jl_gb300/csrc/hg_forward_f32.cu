@@ -181,7 +181,11 @@ __device__ __forceinline__ void stage_cell(const DevMesh& m, const DevScalars& s
   face_sum_f32<NS>(m, X, sX, sP, base, c, L, own, make_float2(cp.x, cp.y), sl, totalIn, cp.w, s.flags, f0, f1, f2);
   const float A = cs.z;
   const float r0 = -f0 / A, r1 = -f1 / A, r2 = -f2 / A;
-  const float fr = friction_coef(m.gf, m.kn2f, m.hsmf, cp.w, L.s.h, L.s.hu, L.s.hv);
+  // Manning friction, or the flow-resistance closure F q / |q|_smooth
+  // (semi_discretize_swe_2D.jl:517-529) with F from the resistance kernels.
+  const float fr = m.res.kind == kResUdeFlowResistance
+                       ? m.res.fresF[c] / smooth_sqrt(L.s.hu * L.s.hu + L.s.hv * L.s.hv)
+                       : friction_coef(m.gf, m.kn2f, m.hsmf, cp.w, L.s.h, L.s.hu, L.s.hv);
   const float sx = L.s.dry ? 0.0f : (m.gf * L.s.xi * cs.x - fr * L.s.hu);
   const float sy = L.s.dry ? 0.0f : (m.gf * L.s.xi * cs.y - fr * L.s.hv);
   const float d0 = r0, d1 = r1 + sx, d2 = r2 + sy;
@@ -537,6 +541,7 @@ __global__ void k_flush_read(uint4* buf, size_t n16) {
 }  // namespace
 
 void launch_inlet_total_f32(const DevMesh& m, const DevScalars& s, StateF32 X, cudaStream_t st) {
+  launch_resistance_f32(m, X, st);
   if (m.nInlet > 0) k_inlet_total_f32<<<m.nInlet, kBlock, 0, st>>>(m, s, X);
 }
 namespace {

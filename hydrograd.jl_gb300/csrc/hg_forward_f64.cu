@@ -154,9 +154,20 @@ __global__ void __launch_bounds__(kBlock) k_stage_f64(DevMesh m, DevScalars s, i
     const double A = m.area[c];
     const double r0 = -f0 / A, r1 = -f1 / A, r2 = -f2 / A;     // :415
     // Sources (:449-559): (h > h_small) * (g xi S0 - friction), continuity 0.
-    const double fr = friction_coef(m.g, m.kn2, m.hsm, m.man[c], L.h, L.hu, L.hv);
-    const double sx = L.dry ? 0.0 : (m.g * L.xi * m.s0x[c] - fr * L.hu);
-    const double sy = L.dry ? 0.0 : (m.g * L.xi * m.s0y[c] - fr * L.hv);
+    // Manning friction, or the flow-resistance closure F q / |q|_smooth
+    // (semi_discretize_swe_2D.jl:517-529) with F from the resistance kernels.
+    double fx, fy;
+    if (m.res.kind == kResUdeFlowResistance) {
+      const double mag = smooth_sqrt(L.hu * L.hu + L.hv * L.hv);
+      fx = m.res.fres[c] * L.hu / mag;
+      fy = m.res.fres[c] * L.hv / mag;
+    } else {
+      const double fr = friction_coef(m.g, m.kn2, m.hsm, m.man[c], L.h, L.hu, L.hv);
+      fx = fr * L.hu;
+      fy = fr * L.hv;
+    }
+    const double sx = L.dry ? 0.0 : (m.g * L.xi * m.s0x[c] - fx);
+    const double sy = L.dry ? 0.0 : (m.g * L.xi * m.s0y[c] - fy);
     const double d0 = r0 + 0.0, d1 = r1 + sx, d2 = r2 + sy;
     if (mode == kModeRhs) {
       Qout[c] = d0; Qout[m.n + c] = d1; Qout[2 * m.n + c] = d2;
@@ -214,6 +225,7 @@ __global__ void __launch_bounds__(kBlock) k_inlet_total_f64(DevMesh m, DevScalar
 }  // namespace
 
 void launch_inlet_total_f64(const DevMesh& m, const DevScalars& s, const double* Q, cudaStream_t st) {
+  launch_resistance_f64(m, Q, st);
   if (m.nInlet > 0) k_inlet_total_f64<<<m.nInlet, kBlock, 0, st>>>(m, s, Q);
 }
 void launch_stage_f64(const DevMesh& m, const DevScalars& s, int mode, const double* Qin, const double* Qbase,

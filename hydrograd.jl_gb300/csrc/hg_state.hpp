@@ -10,6 +10,43 @@ namespace hg {
 
 // Mesh and parameters in device memory, cells in the device (renumbered) order.
 // Slot-major face tables: entry [k * n + c] is edge slot k of cell c.
+// State-dependent flow resistance (hg_resistance.cu).  Kinds: Manning's n as a
+// function of the state (process_ManningN_2D.jl:102-213) and the UDE closures
+// (process_ManningN_2D.jl:216-273: n from a network; process_FlowResistance_UDE.jl:3-45:
+// the friction magnitude from a network).  Before every RHS evaluation the
+// resistance kernels recompute, from that evaluation's input state, the
+// per-cell n (DevMesh::man and CP.w, read by the friction and the inlet-Q
+// conveyance) or the friction magnitude (fres / fresF).
+enum ResKind : int32_t {
+  kResConstant = 0, kResPowerLaw = 1, kResSigmoid = 2, kResInverse = 3, kResHUmagKs = 4,
+  kResUdeManningH = 5, kResUdeManningHUmagKs = 6, kResUdeFlowResistance = 7
+};
+constexpr int kResMaxLayers = 4;     // hidden Dense + LayerNorm layers
+constexpr int kResMaxWidth = 16;     // neurons per hidden layer
+constexpr int kResMaxInputs = 3;
+constexpr int kResPartials = 1024;   // blocks of a LayerNorm statistics pass
+struct ResDev {
+  int32_t kind = kResConstant;
+  double p[4] = {0.0, 0.0, 0.0, 0.0};   // n_lower, n_upper, k, h_mid
+  const double* ks = nullptr;           // [n] roughness height
+  // network (Lux order: per hidden layer Dense weight (out x in, column-major),
+  // bias, LayerNorm scale, bias; then the output Dense weight, bias)
+  int32_t inDim = 0, nHidden = 0, overBatch = 1;
+  int32_t width[kResMaxLayers] = {0, 0, 0, 0};
+  int32_t act[kResMaxLayers] = {0, 0, 0, 0};
+  const double* w = nullptr;
+  const float* wf = nullptr;
+  double outLo = 0.0, outHi = 1.0, lnEps = 1e-5;
+  // input normalisation bounds: [0] h, [1] Umag (or the velocity magnitude of
+  // the flow-resistance closure), [2] ks
+  double lo[kResMaxInputs] = {0.0, 0.0, 0.0}, hi[kResMaxInputs] = {1.0, 1.0, 1.0};
+  double* stats = nullptr;              // [2 * kResMaxLayers] LayerNorm mean, variance over all cells
+  double* partials = nullptr;           // [kResPartials]
+  unsigned int* ticket = nullptr;
+  double* fres = nullptr;               // [n] friction magnitude (flow-resistance closure), FP64 path
+  float* fresF = nullptr;               // the same, FP32 path
+};
+
 struct DevMesh {
   int32_t n = 0;        // cells
   int32_t nslot = 0;    // max faces per cell
@@ -46,6 +83,7 @@ struct DevMesh {
   const double* inletQ = nullptr;    // [nInlet]
   double* totalA = nullptr;          // [nInlet] conveyance of the current stage input
   double g = 9.81, kn2 = 1.0, hsm = 1e-3;
+  ResDev res;
 };
 
 // Scalars that live on the device so that steps can be captured in a graph.
@@ -99,6 +137,12 @@ struct StateF32 {
   float2* q = nullptr;
 };
 void launch_inlet_total_f32(const DevMesh& m, const DevScalars& s, StateF32 X, cudaStream_t st);
+// Resistance of the state (see ResDev); the number of launches it makes.
+// launch_inlet_total_f64 / _f32 call these first, so every RHS evaluation sees
+// the resistance of its own input state.
+int launch_resistance_f64(const DevMesh& m, const double* Q, cudaStream_t st);
+int launch_resistance_f32(const DevMesh& m, StateF32 X, cudaStream_t st);
+int resistance_launches(const DevMesh& m);
 void launch_stage_f32(const DevMesh& m, const DevScalars& s, int mode, StateF32 Xin, StateF32 Xbase, StateF32 Xout,
                       double* Rout, bool cfl, cudaStream_t st);
 // Stage with the fused work of StageFuse (requires nInlet <= kMaxFusedInlets).

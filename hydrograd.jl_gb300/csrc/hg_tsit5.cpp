@@ -140,7 +140,7 @@ int hg_integrate_tsit5(hg_ctx* ctx, double* Q, double t0, double t1, double abst
       launch_stage_f32(ctx->dm, ctx->ds, kModeRhs, xs, StateF32{}, StateF32{}, out, false, st);
       ctx->launches += 1;
     }
-    ctx->launches += 1 + (ctx->dm.nInlet > 0 ? 1 : 0);
+    ctx->launches += 1 + (ctx->dm.nInlet > 0 ? 1 : 0) + resistance_launches(ctx->dm);
   };
   // Weighted RMS norm of sum_j w_j V_j (scale abstol + reltol max(|Ua|, |Ub|)).
   auto wnorm = [&](const double* Ua, const double* Ub, Tsit5Terms terms, double h, double& out) -> int {

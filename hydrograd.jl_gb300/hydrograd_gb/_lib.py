@@ -15,6 +15,11 @@ HG_FP64 = 0
 HG_FP32C = 1
 HG_ORDER_NONE, HG_ORDER_RCM, HG_ORDER_HILBERT = 0, 1, 2
 BC_NONE, BC_WALL, BC_SYMM, BC_INLETQ, BC_EXITH = -1, 0, 1, 2, 3
+# hg_resistance
+RES_CONSTANT, RES_POWER_LAW, RES_SIGMOID, RES_INVERSE, RES_H_UMAG_KS = 0, 1, 2, 3, 4
+RES_UDE_MANNING_H, RES_UDE_MANNING_H_UMAG_KS, RES_UDE_FLOW_RESISTANCE = 5, 6, 7
+# hg_activation
+ACTIVATIONS = {"relu": 0, "leakyrelu": 1, "sigmoid": 2, "tanh": 3, "softplus": 4}
 
 _dp = ctypes.POINTER(ctypes.c_double)
 _ip = ctypes.POINTER(ctypes.c_int32)
@@ -31,6 +36,13 @@ class HgMeshDesc(ctypes.Structure):
 class HgEnsembleDesc(ctypes.Structure):
     _fields_ = [("n_meshes", ctypes.c_int32), ("meshes", ctypes.POINTER(HgMeshDesc)),
                 ("n_members", ctypes.c_int32), ("member_mesh", _ip)]
+
+
+class HgUdeDesc(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int32), ("n_hidden", ctypes.c_int32), ("hidden", _ip), ("activation", _ip),
+                ("params", _dp), ("n_params", ctypes.c_int32), ("output_bounds", ctypes.c_double * 2),
+                ("h_bounds", ctypes.c_double * 2), ("u_bounds", ctypes.c_double * 2),
+                ("ks_bounds", ctypes.c_double * 2), ("ks_cells", _dp), ("layernorm_over_batch", ctypes.c_int32)]
 
 
 class HgConsts(ctypes.Structure):
@@ -58,6 +70,8 @@ SIGNATURES = {
     "hg_set_manning_zones": [_vp, _ip, ctypes.c_int32, _dp],
     "hg_set_manning_cells": [_vp, _dp],
     "hg_set_zb_cells": [_vp, _dp],
+    "hg_set_manning_function": [_vp, ctypes.c_int32, _dp, ctypes.c_int32, _dp],
+    "hg_set_ude": [_vp, ctypes.POINTER(HgUdeDesc)],
     "hg_set_inlet_q": [_vp, _dp, ctypes.c_int32],
     "hg_set_exit_wse": [_vp, _dp, ctypes.c_int32],
     "hg_get_bed": [_vp, _dp, _dp, _dp, _dp],

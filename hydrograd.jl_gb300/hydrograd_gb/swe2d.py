@@ -19,7 +19,7 @@ import ctypes
 import numpy as np
 
 from . import _lib
-from ._lib import HgConsts, HgEnsembleDesc, HgMeshDesc, check, lib
+from ._lib import HgConsts, HgEnsembleDesc, HgMeshDesc, HgUdeDesc, check, lib
 
 _dp = ctypes.POINTER(ctypes.c_double)
 _ip = ctypes.POINTER(ctypes.c_int32)
@@ -141,6 +141,41 @@ class SWE2D:
 
     def set_zb_cells(self, zb):
         self._chk(lib().hg_set_zb_cells(self.h, _d(np.ascontiguousarray(zb, dtype=np.float64))))
+
+    def set_manning_function(self, kind, params=(), ks=None):
+        """Manning's n as a function of the state (ManningN_option "variable",
+        process_ManningN_2D.jl:102-213): kind "power_law" / "sigmoid" / "inverse"
+        with params {n_lower, n_upper, k[, h_mid]}, or "h_Umag_ks" with ks per
+        cell; "constant" returns to the cells' n."""
+        kinds = {"constant": _lib.RES_CONSTANT, "power_law": _lib.RES_POWER_LAW, "sigmoid": _lib.RES_SIGMOID,
+                 "inverse": _lib.RES_INVERSE, "h_Umag_ks": _lib.RES_H_UMAG_KS}
+        k = kinds[kind] if isinstance(kind, str) else int(kind)
+        if isinstance(params, dict):
+            params = [params.get(n, 0.0) for n in ("n_lower", "n_upper", "k", "h_mid")]
+        p = np.ascontiguousarray(params, dtype=np.float64)
+        self._res_ks = None if ks is None else np.ascontiguousarray(ks, dtype=np.float64)
+        self._chk(lib().hg_set_manning_function(self.h, k, _d(p) if len(p) else None, len(p), _d(self._res_ks)))
+
+    def set_ude(self, choice, hidden, activations, params, output_bounds, h_bounds, u_bounds=(0.0, 1.0),
+                ks_bounds=(0.0, 1.0), ks=None, layernorm_over_batch=True):
+        """A UDE closure in the RHS (process_ManningN_2D.jl:216-273,
+        process_FlowResistance_UDE.jl:3-45): choice "ManningN_h",
+        "ManningN_h_Umag_ks" or "FlowResistance"; the network of
+        process_UDE.jl:3-56 with hidden widths, activation names and its
+        parameters in Lux's flattened order (hg_ude_desc)."""
+        kinds = {"ManningN_h": _lib.RES_UDE_MANNING_H, "ManningN_h_Umag_ks": _lib.RES_UDE_MANNING_H_UMAG_KS,
+                 "FlowResistance": _lib.RES_UDE_FLOW_RESISTANCE}
+        hid = np.ascontiguousarray(hidden, dtype=np.int32)
+        act = np.ascontiguousarray([_lib.ACTIVATIONS[a] if isinstance(a, str) else a for a in activations],
+                                   dtype=np.int32)
+        prm = np.ascontiguousarray(params, dtype=np.float64)
+        ks = None if ks is None else np.ascontiguousarray(ks, dtype=np.float64)
+        self._ude_keep = (hid, act, prm, ks)
+        pair = ctypes.c_double * 2
+        d = HgUdeDesc(kinds[choice] if isinstance(choice, str) else int(choice), len(hid), _i(hid), _i(act), _d(prm),
+                      len(prm), pair(*output_bounds), pair(*h_bounds), pair(*u_bounds), pair(*ks_bounds), _d(ks),
+                      1 if layernorm_over_batch else 0)
+        self._chk(lib().hg_set_ude(self.h, ctypes.byref(d)))
 
     def set_inlet_q(self, q):
         q = np.ascontiguousarray(np.atleast_1d(q), dtype=np.float64)

@@ -179,6 +179,56 @@ int hg_set_exit_wse(hg_ctx* ctx, const double* wse, int32_t n_exith); /* exitH_W
 /* Read back derived data: zb_cells [n], S0 [2n] (x,y interleaved), ManningN_cells [n], hstill [n]. */
 int hg_get_bed(hg_ctx* ctx, double* zb_cells, double* S0, double* manning_cells, double* hstill);
 
+/* ---- state-dependent flow resistance
+ * Manning's n as a function of the state, ManningN_option "variable"
+ * (process_ManningN_2D.jl:102-213, applied at semi_discretize_swe_2D.jl:141-149):
+ * every RHS evaluation recomputes n from its own clamped state, with
+ * Umag = |q| / h, and uses it for the friction and the inlet-Q conveyance.
+ *   HG_RES_POWER_LAW  n = n_lower + (n_upper - n_lower) (h + eps)^(-k)
+ *   HG_RES_SIGMOID    n = n_lower + (n_upper - n_lower) / (1 + exp(k (h - h_mid)))
+ *   HG_RES_INVERSE    n = n_lower + (n_upper - n_lower) / (1 + k h)
+ *   HG_RES_H_UMAG_KS  n from Cheng's (2008) friction factor of Re = Umag h / 1e-6 and h / ks
+ * params = {n_lower, n_upper, k[, h_mid]}; ks_cells [n] (caller order) for
+ * HG_RES_H_UMAG_KS.  HG_RES_CONSTANT returns to the cells' n
+ * (hg_set_manning_zones / _cells).  Gradients (hg_loss_and_grad) are not
+ * available while a state-dependent resistance is set: HG_ERR_UNSUPPORTED. */
+enum hg_resistance {
+  HG_RES_CONSTANT = 0, HG_RES_POWER_LAW = 1, HG_RES_SIGMOID = 2, HG_RES_INVERSE = 3, HG_RES_H_UMAG_KS = 4,
+  HG_RES_UDE_MANNING_H = 5,          /* UDE_choice "ManningN_h": n = NN(h) */
+  HG_RES_UDE_MANNING_H_UMAG_KS = 6,  /* "ManningN_h_Umag_ks": n = NN(h, Umag, ks) */
+  HG_RES_UDE_FLOW_RESISTANCE = 7     /* "FlowResistance": friction = NN(h, |q|) q / |q| */
+};
+int hg_set_manning_function(hg_ctx* ctx, int32_t kind, const double* params, int32_t n_params,
+                            const double* ks_cells);
+/* UDE closures (process_ManningN_2D.jl:216-273, process_FlowResistance_UDE.jl:3-45)
+ * with the network of process_UDE.jl:3-56: per hidden layer Dense(in, w, act)
+ * then LayerNorm(w); a linear Dense(w, 1); output lo + (hi - lo) sigmoid(y).
+ * Inputs normalised to [-1, 1] by their bounds: h (h_bounds); Umag (u_bounds)
+ * and ks (ks_bounds) for ManningN_h_Umag_ks; |q| for FlowResistance with the
+ * bounds h_bounds x u_bounds (u_bounds = velocity_magnitude_bounds).
+ * params: Lux's flattened order -- per hidden layer the Dense weight (w x in,
+ * column-major) and bias, the LayerNorm scale and bias; then the output
+ * weight (1 x w) and bias.  LayerNorm: (x - mean) / sqrt(var + 1f-5) * scale +
+ * bias, uncorrected variance; layernorm_over_batch = 1 takes mean and variance
+ * over the whole (width x cells) array, as Lux's LayerNorm with its default
+ * dims = Colon() does; 0 takes them over each cell's features. */
+enum hg_activation { HG_ACT_RELU = 0, HG_ACT_LEAKYRELU = 1, HG_ACT_SIGMOID = 2, HG_ACT_TANH = 3, HG_ACT_SOFTPLUS = 4 };
+typedef struct hg_ude_desc {
+  int32_t kind;                  /* HG_RES_UDE_* */
+  int32_t n_hidden;              /* 0..4 */
+  const int32_t* hidden;         /* [n_hidden] widths, 1..16 */
+  const int32_t* activation;     /* [n_hidden] hg_activation */
+  const double* params;
+  int32_t n_params;
+  double output_bounds[2];
+  double h_bounds[2];
+  double u_bounds[2];
+  double ks_bounds[2];
+  const double* ks_cells;        /* [n] (HG_RES_UDE_MANNING_H_UMAG_KS) */
+  int32_t layernorm_over_batch;
+} hg_ude_desc;
+int hg_set_ude(hg_ctx* ctx, const hg_ude_desc* ude);
+
 /* ---- forward ------------------------------------------------------------- */
 /* dQdt = swe_2d_rhs(Q, p, t) with host buffers (semi_discretize_swe_2D.jl:18-277). */
 int hg_rhs(hg_ctx* ctx, const double* Q, double t, double* dQdt);

@@ -23,6 +23,7 @@
 #include <map>
 #include <stdexcept>
 #include <string>
+#include <type_traits>
 #include <unordered_map>
 #include <vector>
 
@@ -416,8 +417,178 @@ struct Consts {
   double g = 9.81, k_n = 1.0, h_small = 1.0e-3;   // solve_swe_2D.jl:51-107
 };
 
+// ---------------------------------------------------------------------------
+// State-dependent flow resistance.
+// ---------------------------------------------------------------------------
+// Kinds: Manning's n as a function of the state (ManningN_option "variable",
+// process_ManningN_2D.jl:102-213, applied at semi_discretize_swe_2D.jl:141-149),
+// and the UDE closures (process_ManningN_2D.jl:216-273 for n; the flow
+// resistance magnitude of process_FlowResistance_UDE.jl:3-45, applied at
+// semi_discretize_swe_2D.jl:516-533).
+enum ResKind : int {
+  RES_CONSTANT = 0, RES_POWER_LAW = 1, RES_SIGMOID = 2, RES_INVERSE = 3, RES_H_UMAG_KS = 4,
+  RES_UDE_MANNING_H = 5, RES_UDE_MANNING_H_UMAG_KS = 6, RES_UDE_FLOW_RESISTANCE = 7
+};
+enum Act : int { ACT_RELU = 0, ACT_LEAKYRELU = 1, ACT_SIGMOID = 2, ACT_TANH = 3, ACT_SOFTPLUS = 4 };
+
+// NNlib's activations (relu, leakyrelu with a = 0.01, sigmoid, tanh, softplus).
+inline double sigmoid_nn(double x) {
+  const double t = std::exp(-std::fabs(x));
+  return x >= 0 ? 1.0 / (1.0 + t) : t / (1.0 + t);
+}
+inline double activation(int a, double x) {
+  switch (a) {
+    case ACT_RELU: return x > 0 ? x : 0.0;
+    case ACT_LEAKYRELU: return x > 0 ? x : 0.01 * x;
+    case ACT_SIGMOID: return sigmoid_nn(x);
+    case ACT_TANH: return std::tanh(x);
+    default: return std::log1p(std::exp(-std::fabs(x))) + (x > 0 ? x : 0.0);   // softplus
+  }
+}
+
+// The UDE network (process_UDE.jl:3-56): a Lux Chain of [Dense(in, w_l, act_l),
+// LayerNorm(w_l)] per hidden layer, a linear Dense(w_L, 1), and the output
+// bound lo + (hi - lo) sigmoid(y).  params: Lux's flattened order -- per layer,
+// Dense weight (out x in, column-major) then bias; LayerNorm scale then bias.
+// LayerNorm: y = (x - mu) / sqrt(var + eps) * scale + bias with eps = 1f-5 and
+// the uncorrected variance; with overBatch its statistics are taken over the
+// whole (width x cells) array, as Lux's LayerNorm does with its default
+// dims = Colon(), otherwise over each cell's features.
+struct Mlp {
+  int inDim = 1;
+  std::vector<int> hidden, act;
+  std::vector<double> params;
+  double outLo = 0.0, outHi = 1.0;
+  bool overBatch = true;
+  double lnEps = (double)1e-5f;
+  size_t n_params() const {
+    size_t n = 0;
+    int in = inDim;
+    for (int w : hidden) { n += (size_t)w * in + w + 2 * w; in = w; }
+    return n + (size_t)in + 1;
+  }
+};
+
+struct Resistance {
+  int kind = RES_CONSTANT;
+  double nLower = 0.0, nUpper = 0.0, k = 0.0, hMid = 0.0;   // function parameters
+  std::vector<double> ks;                                  // roughness height per cell
+  Mlp mlp;
+  double hB[2] = {0, 1}, uB[2] = {0, 1}, ksB[2] = {0, 1};  // input normalisation bounds
+};
+
+// Manning's n functions of process_ManningN_2D.jl:140-213 at one cell; for
+// h_Umag_ks also h/ks, the friction factor and Re (Cheng 2008, Eq. 17).
+inline double manning_fn(const Resistance& r, double h, double umag, double ks, double* hks = nullptr,
+                         double* ff = nullptr, double* re = nullptr) {
+  switch (r.kind) {
+    case RES_POWER_LAW: return r.nLower + (r.nUpper - r.nLower) * std::pow(h + kEps, -r.k);            // :164-175
+    case RES_SIGMOID: return r.nLower + (r.nUpper - r.nLower) / (1.0 + std::exp(r.k * (h - r.hMid)));  // :180-193
+    case RES_INVERSE: return r.nLower + (r.nUpper - r.nLower) / (1.0 + r.k * h);                        // :149-160
+    default: {                                                                                          // :197-213
+      const double nu = 1.0e-6;
+      const double Re = umag * h / nu;
+      const double h_ks = h / ks;
+      const double alpha = 1.0 / (1.0 + std::pow(Re / 850.0, 9.0));
+      const double rb = Re / (h_ks * 160.0);
+      const double beta = 1.0 / (1.0 + rb * rb);
+      const double part1 = std::pow(Re / 24.0, alpha);
+      const double part2 = std::pow(1.8 * std::log10(Re / 2.1), 2.0 * (1.0 - alpha) * beta);
+      const double part3 = std::pow(2.0 * std::log10(11.8 * h_ks), 2.0 * (1.0 - alpha) * (1.0 - beta));
+      const double f = 1.0 / (part1 * part2 * part3);
+      if (hks) *hks = h_ks;
+      if (ff) *ff = f;
+      if (re) *re = Re;
+      return std::sqrt(f / 8.0) * std::pow(h, 1.0 / 6.0) / std::sqrt(9.81);
+    }
+  }
+}
+
+// Forward pass of the network over all cells: in[c * inDim + j] are the
+// normalised inputs, out[c] the bounded outputs.
+inline void mlp_forward(const Mlp& M, const std::vector<double>& in, size_t nCells, std::vector<double>& out) {
+  std::vector<double> a(in), z;
+  int din = M.inDim;
+  size_t off = 0;
+  const double* P = M.params.data();
+  for (size_t l = 0; l < M.hidden.size(); ++l) {
+    const int w = M.hidden[l];
+    const double *W = P + off, *b = W + (size_t)w * din, *sc = b + w, *bi = sc + w;
+    off += (size_t)w * din + 3 * (size_t)w;
+    z.assign(nCells * w, 0.0);
+    for (size_t c = 0; c < nCells; ++c)
+      for (int o = 0; o < w; ++o) {
+        double s = 0.0;
+        for (int i = 0; i < din; ++i) s += W[o + (size_t)i * w] * a[c * din + i];
+        z[c * w + o] = activation(M.act[l], s + b[o]);
+      }
+    std::vector<double> mu(nCells), var(nCells);
+    if (M.overBatch) {
+      double s = 0.0;
+      for (double v : z) s += v;
+      const double m = s / (double)z.size();
+      double q = 0.0;
+      for (double v : z) q += (v - m) * (v - m);
+      std::fill(mu.begin(), mu.end(), m);
+      std::fill(var.begin(), var.end(), q / (double)z.size());
+    } else {
+      for (size_t c = 0; c < nCells; ++c) {
+        double s = 0.0, q = 0.0;
+        for (int o = 0; o < w; ++o) s += z[c * w + o];
+        mu[c] = s / w;
+        for (int o = 0; o < w; ++o) q += (z[c * w + o] - mu[c]) * (z[c * w + o] - mu[c]);
+        var[c] = q / w;
+      }
+    }
+    a.assign(nCells * w, 0.0);
+    for (size_t c = 0; c < nCells; ++c)
+      for (int o = 0; o < w; ++o)
+        a[c * w + o] = (z[c * w + o] - mu[c]) / std::sqrt(var[c] + M.lnEps) * sc[o] + bi[o];
+    din = w;
+  }
+  const double *W = P + off, *b = W + din;
+  out.assign(nCells, 0.0);
+  for (size_t c = 0; c < nCells; ++c) {
+    double s = 0.0;
+    for (int i = 0; i < din; ++i) s += W[i] * a[c * din + i];
+    out[c] = M.outLo + (M.outHi - M.outLo) * sigmoid_nn(s + b[0]);
+  }
+}
+
+inline double normalise(double x, const double* b) { return 2.0 * (x - b[0]) / (b[1] - b[0]) - 1.0; }
+
+// Per-cell resistance of the clamped state: Manning's n (kinds 1-6) or the
+// flow resistance magnitude (kind 7).  Umag = |q| / h (semi_discretize_swe_2D.jl:143-145).
+inline void resistance_cells(const Resistance& r, const std::vector<double>& h, const std::vector<double>& qx,
+                             const std::vector<double>& qy, std::vector<double>& out) {
+  const size_t N = h.size();
+  out.assign(N, 0.0);
+  if (r.kind >= RES_POWER_LAW && r.kind <= RES_H_UMAG_KS) {
+    for (size_t c = 0; c < N; ++c) {
+      const double u = qx[c] / h[c], v = qy[c] / h[c];
+      out[c] = manning_fn(r, h[c], std::sqrt(u * u + v * v), r.ks.empty() ? 0.0 : r.ks[c]);
+    }
+    return;
+  }
+  const int nin = r.mlp.inDim;
+  std::vector<double> in(N * nin);
+  for (size_t c = 0; c < N; ++c) {
+    in[c * nin] = normalise(h[c], r.hB);
+    if (r.kind == RES_UDE_MANNING_H_UMAG_KS) {
+      const double u = qx[c] / h[c], v = qy[c] / h[c];
+      in[c * nin + 1] = normalise(std::sqrt(u * u + v * v), r.uB);
+      in[c * nin + 2] = normalise(r.ks[c], r.ksB);
+    } else if (r.kind == RES_UDE_FLOW_RESISTANCE) {   // process_FlowResistance_UDE.jl:13-20
+      const double qb[2] = {r.hB[0] * r.uB[0], r.hB[1] * r.uB[1]};
+      in[c * nin + 1] = normalise(smooth_sqrt(qx[c] * qx[c] + qy[c] * qy[c]), qb);
+    }
+  }
+  mlp_forward(r.mlp, in, N, out);
+}
+
 template <class T>
 struct Params {
+  Resistance res;                // state-dependent n / UDE closure (kind RES_CONSTANT: manningCells)
   std::vector<T> manningCells;   // ManningN_cells (process_ManningN_2D.jl:242-269 for zones)
   std::vector<T> zbCells;        // zb_cells (active parameter replaces it, semi_discretize_swe_2D.jl:114-126)
   std::vector<T> inletQ;         // inletQ_TotalQ per inlet-Q boundary (:190-199)
@@ -441,8 +612,9 @@ void set_zb(const Case& cs, Params<T>& p, const std::vector<T>& zb) {
 
 // Ghost states (bc_2D.jl:575-875).  h, qx, qy are the clamped cell states.
 template <class T>
-void ghost_states(const Case& cs, const Params<T>& p, const std::vector<T>& h, const std::vector<T>& qx,
-                  const std::vector<T>& qy, std::vector<T>& hg, std::vector<T>& qxg, std::vector<T>& qyg) {
+void ghost_states(const Case& cs, const Params<T>& p, const std::vector<T>& manning, const std::vector<T>& h,
+                  const std::vector<T>& qx, const std::vector<T>& qy, std::vector<T>& hg, std::vector<T>& qxg,
+                  std::vector<T>& qyg) {
   const Mesh& m = cs.mesh;
   size_t nG = m.allBoundaryFaces.size();
   hg.assign(nG, T(0.0)); qxg.assign(nG, T(0.0)); qyg.assign(nG, T(0.0));
@@ -454,12 +626,12 @@ void ghost_states(const Case& cs, const Params<T>& p, const std::vector<T>& h, c
     for (size_t i = 0; i < G.faces.size(); ++i) {
       int c = G.internals[i];
       wet[i] = value(h[c]) > hs ? 1.0 : 0.0;
-      totalA = totalA + std::pow(G.lengths[i], 5.0 / 3.0) * h[c] / p.manningCells[c] * wet[i];
+      totalA = totalA + std::pow(G.lengths[i], 5.0 / 3.0) * h[c] / manning[c] * wet[i];
     }
     if (!(value(totalA) > 1e-10)) throw std::runtime_error("inlet-Q conveyance is not positive (bc_2D.jl:679)");
     for (size_t i = 0; i < G.faces.size(); ++i) {
       int c = G.internals[i], gh = G.ghosts[i];
-      T vn = p.inletQ[b] / totalA * std::pow(G.lengths[i], 2.0 / 3.0) / p.manningCells[c];
+      T vn = p.inletQ[b] / totalA * std::pow(G.lengths[i], 2.0 / 3.0) / manning[c];
       hg[gh] = h[c];
       qxg[gh] = -h[c] * vn * G.onx[i] * wet[i];
       qyg[gh] = -h[c] * vn * G.ony[i] * wet[i];
@@ -511,8 +683,21 @@ void rhs(const Case& cs, const Params<T>& p, const T* Q, T* dQ, int nthreads = 1
     qx[i] = dry ? T(0.0) : Q[N + i];
     qy[i] = dry ? T(0.0) : Q[2 * N + i];
   }
+  // State-dependent resistance (:141-149, :167-181, :516-533): n replaces
+  // ManningN_cells everywhere it is read (friction and the inlet-Q
+  // conveyance); the flow-resistance closure replaces the friction only.
+  const std::vector<T>* manning = &p.manningCells;
+  std::vector<T> resCells;
+  if (p.res.kind != RES_CONSTANT) {
+    if constexpr (std::is_same_v<T, double>) {
+      resistance_cells(p.res, h, qx, qy, resCells);
+      if (p.res.kind != RES_UDE_FLOW_RESISTANCE) manning = &resCells;
+    } else {
+      throw std::runtime_error("state-dependent resistance: FP64 values only");
+    }
+  }
   std::vector<T> hg, qxg, qyg;
-  ghost_states(cs, p, h, qx, qy, hg, qxg, qyg);                          // :215-217
+  ghost_states(cs, p, *manning, h, qx, qy, hg, qxg, qyg);               // :215-217
   std::vector<T> xig(hg.size());
   for (size_t k = 0; k < hg.size(); ++k) xig[k] = hg[k] - cs.hstillGhost[k];   // :220
   (void)nthreads;
@@ -540,8 +725,16 @@ void rhs(const Case& cs, const Params<T>& p, const T* Q, T* dQ, int nthreads = 1
     double A = m.cellAreas[c];
     T inv0 = -fs0 / A, inv1 = -fs1 / A, inv2 = -fs2 / A;                // :415
     // compute_source_terms (:449-505) + compute_friction_terms (:508-559)
-    T fr = friction_factor<T>(g, cs.k.k_n, hs, p.manningCells[c], h[c], qx[c], qy[c]);
-    T frx = fr * qx[c], fry = fr * qy[c];
+    T frx, fry;
+    if (p.res.kind == RES_UDE_FLOW_RESISTANCE) {                          // :517-529
+      const T mag = smooth_sqrt(qx[c] * qx[c] + qy[c] * qy[c]);
+      frx = resCells[c] * qx[c] / mag;
+      fry = resCells[c] * qy[c] / mag;
+    } else {
+      T fr = friction_factor<T>(g, cs.k.k_n, hs, (*manning)[c], h[c], qx[c], qy[c]);
+      frx = fr * qx[c];
+      fry = fr * qy[c];
+    }
     bool above = value(h[c]) > hs;
     T sx = above ? (g * Q[c] * p.bed.S0x[c] - frx) : T(0.0);
     T sy = above ? (g * Q[c] * p.bed.S0y[c] - fry) : T(0.0);

@@ -49,6 +49,11 @@ def _load():
     lib.ho_rk2.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int, _dp]
     lib.ho_tsit5.argtypes = [ctypes.c_void_p, _dp, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                              ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int, _ip]
+    lib.ho_set_resistance_fn.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp, _dp]
+    lib.ho_set_ude.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, _ip, _ip, _dp, ctypes.c_int,
+                               ctypes.c_double, ctypes.c_double, _dp, _dp, _dp, _dp, ctypes.c_int]
+    lib.ho_resistance_cells.argtypes = [ctypes.c_void_p, _dp, _dp]
+    lib.ho_manning_fn.argtypes = [ctypes.c_int, _dp, ctypes.c_int, _dp, _dp, _dp, _dp, _dp, _dp, _dp]
     lib.ho_euler_reference.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int, ctypes.c_double, ctypes.c_int]
     lib.ho_rk2_tangent.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int, ctypes.c_double, ctypes.c_int, _dp, _dp, _dp,
                                    ctypes.c_int, _ip, _dp, _dp, _dp, _dp, _dp, ctypes.c_int]
@@ -68,6 +73,21 @@ def _i(a):
     if a is None:
         return None
     return np.ascontiguousarray(a, dtype=np.int32).ctypes.data_as(_ip)
+
+
+def manning_fn(kind, params, h, umag=None, ks=None):
+    """The n functions of hg_oracle.hpp (manning_fn) at given h, Umag, ks:
+    returns (n, h_ks, friction factor, Re)."""
+    lib = _load()
+    p = np.zeros(4)
+    p[:len(params)] = params
+    h = np.ascontiguousarray(h, dtype=np.float64)
+    n = len(h)
+    um = None if umag is None else np.ascontiguousarray(umag, dtype=np.float64)
+    ks = None if ks is None else np.ascontiguousarray(ks, dtype=np.float64)
+    out = [np.zeros(n) for _ in range(4)]
+    lib.ho_manning_fn(int(kind), _d(p), n, _d(h), _d(um), _d(ks), *(_d(o) for o in out))
+    return tuple(out)
 
 
 class Oracle:
@@ -174,6 +194,34 @@ class Oracle:
         if rc != 0:
             raise RuntimeError("oracle: " + self.lib.ho_last_error().decode())
         return Q, tuple(int(v) for v in st)
+
+    def set_resistance_fn(self, kind, params=(0.0, 0.0, 0.0, 0.0), ks=None):
+        """Manning's n as a function of the state (RES_* kinds 0-4 of hg_oracle.hpp)."""
+        p = np.zeros(4)
+        p[:len(params)] = params
+        self._res = (p, None if ks is None else np.ascontiguousarray(ks, dtype=np.float64))
+        if self.lib.ho_set_resistance_fn(self.h, int(kind), _d(p), _d(self._res[1])) != 0:
+            raise RuntimeError("oracle: " + self.lib.ho_last_error().decode())
+
+    def set_ude(self, kind, in_dim, hidden, activations, params, output_bounds, h_bounds, u_bounds=(0.0, 1.0),
+                ks_bounds=(0.0, 1.0), ks=None, over_batch=True):
+        """UDE closure (RES_* kinds 5-7) with the network of hgo::Mlp."""
+        hid = np.ascontiguousarray(hidden, dtype=np.int32)
+        act = np.ascontiguousarray(activations, dtype=np.int32)
+        prm = np.ascontiguousarray(params, dtype=np.float64)
+        b = [np.ascontiguousarray(v, dtype=np.float64) for v in (h_bounds, u_bounds, ks_bounds)]
+        ks = None if ks is None else np.ascontiguousarray(ks, dtype=np.float64)
+        rc = self.lib.ho_set_ude(self.h, int(kind), int(in_dim), len(hid), _i(hid), _i(act), _d(prm), len(prm),
+                                 float(output_bounds[0]), float(output_bounds[1]), _d(b[0]), _d(b[1]), _d(b[2]),
+                                 _d(ks), 1 if over_batch else 0)
+        if rc != 0:
+            raise RuntimeError("oracle: " + self.lib.ho_last_error().decode())
+
+    def resistance_cells(self, Q):
+        Q = np.ascontiguousarray(Q, dtype=np.float64)
+        out = np.zeros(self.n_cells)
+        self.lib.ho_resistance_cells(self.h, _d(Q), _d(out))
+        return out
 
     def euler_reference(self, Q, nsteps, dt, nthreads=1):
         Q = np.array(Q, dtype=np.float64)

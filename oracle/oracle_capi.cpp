@@ -218,6 +218,85 @@ int ho_rhs(void* h, const double* Q, double* dQ, int nthreads) {
 }
 
 // Manning friction terms from given h, q (compute_friction_terms, semi_discretize_swe_2D.jl:544-547).
+// Manning's n as a function of the state (process_ManningN_2D.jl:102-213):
+// kind RES_POWER_LAW..RES_H_UMAG_KS, params {n_lower, n_upper, k, h_mid}, ks per
+// cell (h_Umag_ks); kind RES_CONSTANT switches back to the cells' n.
+int ho_set_resistance_fn(void* h, int kind, const double* params, const double* ks) {
+  auto* oc = static_cast<OracleCase*>(h);
+  if (kind < RES_CONSTANT || kind > RES_H_UMAG_KS) {
+    g_err = "ho_set_resistance_fn: bad kind";
+    return 1;
+  }
+  Resistance r;
+  r.kind = kind;
+  if (params) { r.nLower = params[0]; r.nUpper = params[1]; r.k = params[2]; r.hMid = params[3]; }
+  if (ks) r.ks.assign(ks, ks + oc->cs.mesh.nCells);
+  oc->p.res = r;
+  return 0;
+}
+// UDE closures (process_ManningN_2D.jl:216-273, process_FlowResistance_UDE.jl:3-45)
+// with the network of process_UDE.jl:3-56 (hgo::Mlp).
+int ho_set_ude(void* h, int kind, int inDim, int nHidden, const int* hidden, const int* act, const double* params,
+               int nParams, double outLo, double outHi, const double* hB, const double* uB, const double* ksB,
+               const double* ks, int overBatch) {
+  auto* oc = static_cast<OracleCase*>(h);
+  Resistance r;
+  r.kind = kind;
+  r.mlp.inDim = inDim;
+  r.mlp.hidden.assign(hidden, hidden + nHidden);
+  r.mlp.act.assign(act, act + nHidden);
+  r.mlp.params.assign(params, params + nParams);
+  r.mlp.outLo = outLo;
+  r.mlp.outHi = outHi;
+  r.mlp.overBatch = overBatch != 0;
+  if ((size_t)nParams != r.mlp.n_params()) {
+    g_err = "ho_set_ude: parameter count does not match the layer sizes";
+    return 1;
+  }
+  for (int i = 0; i < 2; ++i) {
+    r.hB[i] = hB ? hB[i] : 0.0;
+    r.uB[i] = uB ? uB[i] : 0.0;
+    r.ksB[i] = ksB ? ksB[i] : 0.0;
+  }
+  if (ks) r.ks.assign(ks, ks + oc->cs.mesh.nCells);
+  oc->p.res = r;
+  return 0;
+}
+// The resistance field of the state Q (after the RHS's clamp): n per cell, or
+// the flow-resistance magnitude for the flow-resistance closure.
+int ho_resistance_cells(void* h, const double* Q, double* out) {
+  auto* oc = static_cast<OracleCase*>(h);
+  const int N = oc->cs.mesh.nCells;
+  const double hs = oc->cs.k.h_small;
+  std::vector<double> hh(N), qx(N), qy(N), r;
+  for (int i = 0; i < N; ++i) {
+    const double d = Q[i] + oc->cs.hstill[i];
+    const bool dry = d <= hs;
+    hh[i] = dry ? hs : d;
+    qx[i] = dry ? 0.0 : Q[N + i];
+    qy[i] = dry ? 0.0 : Q[2 * N + i];
+  }
+  if (oc->p.res.kind == RES_CONSTANT) r = oc->p.manningCells;
+  else resistance_cells(oc->p.res, hh, qx, qy, r);
+  std::memcpy(out, r.data(), sizeof(double) * N);
+  return 0;
+}
+// The n functions alone at given (h, Umag, ks), with h/ks, f and Re of h_Umag_ks.
+int ho_manning_fn(int kind, const double* params, int n, const double* hh, const double* umag, const double* ks,
+                  double* nOut, double* hks, double* ff, double* re) {
+  Resistance r;
+  r.kind = kind;
+  r.nLower = params[0]; r.nUpper = params[1]; r.k = params[2]; r.hMid = params[3];
+  for (int i = 0; i < n; ++i) {
+    double a = 0, b = 0, c = 0;
+    nOut[i] = manning_fn(r, hh[i], umag ? umag[i] : 0.0, ks ? ks[i] : 0.0, &a, &b, &c);
+    if (hks) hks[i] = a;
+    if (ff) ff[i] = b;
+    if (re) re[i] = c;
+  }
+  return 0;
+}
+
 void ho_friction(void* h, const double* hh, const double* qx, const double* qy, double* fx, double* fy) {
   auto* oc = static_cast<OracleCase*>(h);
   const auto& k = oc->cs.k;

@@ -14,6 +14,13 @@ reference's own outputs:
                             forward run (swe_2D_forward_simulation.jl:37-39)
 * ``sensitivity``           ForwardDiff Jacobian of the final state w.r.t. the
                             zone Manning n (swe_2D_sensitivity.jl:80-94)
+* cases with a state-dependent Manning n (ManningN_option "variable"):
+  ``res_kind`` / ``res_params`` (the function and its parameters, kinds as in
+  oracle/hg_oracle.hpp), ``ks_cells`` (roughness height per cell,
+  process_SRH_2D_input.jl:158-167), and the truth fields
+  ``ManningN_cells_truth``, ``h_ks_cells_truth``, ``friction_factor_cells_truth``,
+  ``Re_cells_truth`` computed at the truth state
+  (process_forward_simulation_results_2D.jl:26-38)
 
 Usage:  python tests/golden/make_golden.py [reference_root]
 The reference root defaults to /root/reference.  Only this script reads it; the
@@ -34,6 +41,9 @@ from hydrograd_gb.srh2d import read_case  # noqa: E402  (the package's SRH-2D re
 def build_case(case_dir, hydro_name=None):
     ctl = json.load(open(os.path.join(case_dir, "run_control.json")))
     hydro_name = hydro_name or ctl["control_variables"]["srhhydro_file_name"]
+    # run-control files name some cases with a different letter case than the
+    # file on disk (written on case-insensitive file systems): match without case
+    hydro_name = next((f for f in os.listdir(case_dir) if f.lower() == hydro_name.lower()), hydro_name)
     stem = os.path.splitext(hydro_name)[0]
     geom_file = [f for f in os.listdir(case_dir) if f.endswith(".srhgeom") and f.startswith(stem)]
     geom_file = geom_file[0] if geom_file else [f for f in os.listdir(case_dir) if f.endswith(".srhgeom")][0]
@@ -52,16 +62,31 @@ def initial_state(ctl, case_dir, opts_key, ic_key, file_key):
                 ic_qx=np.array(ic["q_x"], float), ic_qy=np.array(ic["q_y"], float))
 
 
+RES_KINDS = {"power_law": 1, "sigmoid": 2, "inverse": 3, "h_Umag_ks": 4}
+
+
 def forward_case(ref, rel, out_name):
     case_dir = os.path.join(ref, rel)
     ctl, d = build_case(case_dir)
+    opts = ctl["forward_simulation_options"]
     d.update(initial_state(ctl, case_dir, "forward_simulation_options",
                            "forward_simulation_initial_condition_options",
                            "forward_simulation_initial_condition_file_name"))
+    d["dt"] = np.array(float(ctl["time_settings"]["dt"]))
     truth = json.load(open(os.path.join(case_dir, "forward_simulation_solution_truth.json")))
     for k in ("xi_truth", "h_truth", "u_truth", "v_truth", "wstill_truth", "hstill_truth", "zb_cell_truth",
               "friction_x_truth", "friction_y_truth", "ManningN_cells_truth"):
         d[k] = np.array(truth[k], dtype=float)
+    if opts.get("forward_simulation_ManningN_option") == "variable":
+        fn = opts["forward_simulation_ManningN_function_type"]
+        prm = opts["forward_simulation_ManningN_function_parameters"]
+        d["res_kind"] = np.array(RES_KINDS[fn], dtype=np.int32)
+        d["res_params"] = np.array([float(prm.get(k, 0.0)) for k in ("n_lower", "n_upper", "k", "h_mid")])
+        if "ks" in prm:   # srhmat_ks_dict[iMat - 1] = ks[iMat]: zone id -> ks
+            d["ks_cells"] = np.array(prm["ks"], dtype=float)[d["mat_id"]]
+        for k in ("h_ks_cells_truth", "friction_factor_cells_truth", "Re_cells_truth"):
+            if k in truth:
+                d[k] = np.array(truth[k], dtype=float)
     d["S0_cells_truth"] = np.array(truth["S0_cells_truth"], dtype=float)
     np.savez_compressed(os.path.join(HERE, out_name), source=np.array(rel), **d)
 
@@ -89,6 +114,8 @@ def main():
     forward_case(ref, f"{ex}/forward_simulation/oneD_channel_with_bump", "fwd_bump.npz")
     forward_case(ref, f"{ex}/forward_simulation/oneD_channel_uniform_flow", "fwd_uniform.npz")
     forward_case(ref, f"{ex}/forward_simulation/Savannah_River", "fwd_savannah.npz")
+    forward_case(ref, f"{ex}/forward_simulation/oneD_channel_with_bump_ManningN_h", "fwd_bump_nh.npz")
+    forward_case(ref, f"{ex}/forward_simulation/Savannah_River_ManningN_ks_h_Umag", "fwd_savannah_nks.npz")
     sensitivity_case(ref, f"{ex}/sensitivity_analysis/ManningN/oneD_channel_with_bump", "sens_bump.npz")
     sensitivity_case(ref, f"{ex}/sensitivity_analysis/ManningN/oneD_channel_uniform_flow", "sens_uniform.npz")
     for f in sorted(os.listdir(HERE)):
