@@ -19,7 +19,7 @@ LIB = os.path.join(OUT, "libhydrograd_gb.so")
 INCLUDE = os.path.join(ROOT, "include")
 
 CUDA_SOURCES = ["hg_forward_f64.cu", "hg_forward_f32.cu", "hg_adjoint_f64.cu", "hg_adjoint_f32.cu", "hg_noalloc.cu",
-                "hg_tsit5.cu", "hg_resistance.cu"]
+                "hg_tsit5.cu", "hg_resistance.cu", "hg_final_loss.cu"]
 # FP64 parity path: no fused multiply-add, as in the reference (and in the
 # Tsit5 stage sums and the resistance functions, which the oracle forms with
 # separate multiplies and adds).

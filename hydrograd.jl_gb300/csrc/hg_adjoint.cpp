@@ -3,7 +3,9 @@
 // Forward step (fixed dt), C the depth-positivity clamp:
 //   Q1 = C(Q0 + dt R(Q0)),   Q2 = C(0.5 (Q0 + (Q1 + dt R(Q1))))
 // Loss = mean over steps k and probes p of (h_p^k - obs_kp)^2, h = xi + hstill
-// (the probe-depth misfit; cf. the WSE loss of swe_2D_inversion.jl:404-416).
+// (the probe-depth misfit), plus optionally the final-state WSE / velocity
+// misfit of swe_2D_inversion.jl:383-431 (hg_final_loss.cu), which seeds the
+// reverse sweep at the last state.
 // Reverse step, with mu2 = dL/dQ2 masked by the stage-2 clamp:
 //   mu1 = M1 (0.5 mu2 + 0.5 dt J(Q1)^T mu2)
 //   mu2' = M0 (0.5 mu2 + mu1 + dt J(Q0)^T mu1)
@@ -39,6 +41,11 @@ struct AdjointBuffers {
   size_t probeCap = 0, obsCap = 0;
   double* segTot = nullptr;      // FP32C: inlet totals of a segment's states
   size_t segTotCap = 0;
+  // Final-state loss: observations (wse, u, v, zbw; device order), dL/dWSE,
+  // the two loss sums and the reduction scratch.
+  double* fin = nullptr;
+  double* finScratch = nullptr;   // dWse [n], parts [2], partials [2 kFinalLossBlocks]
+  unsigned int* finTicket = nullptr;
   cudaStream_t side = nullptr;   // FP32C: the boundary VJP beside the interior one
   cudaEvent_t evFork = nullptr, evJoin = nullptr;
   ~AdjointBuffers() {
@@ -52,6 +59,9 @@ struct AdjointBuffers {
     cudaFree(probeCsr);
     cudaFree(obs);
     cudaFree(segTot);
+    cudaFree(fin);
+    cudaFree(finScratch);
+    cudaFree(finTicket);
   }
 };
 
@@ -217,7 +227,7 @@ F32States f32_view(double* base, size_t states, int n) {
 
 int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int32_t C, const int32_t* probeCells,
                           const double* obs, int32_t P, double* loss, double* gManning, double* gZb, double* gInlet,
-                          double* Qfinal) {
+                          double* Qfinal, const FinalObs* fo, double* parts) {
   int rc = setup(c);
   if (rc) return rc;
   AdjointBuffers* b = c->adj;
@@ -295,6 +305,46 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
   ADJ_CUDA(c, cudaMemcpyAsync(c->ds.dtf, &dtf, sizeof(float), cudaMemcpyHostToDevice, st));
   ADJ_CUDA(c, cudaMemcpyAsync(c->Quser, Q0, n3 * sizeof(double), cudaMemcpyHostToDevice, st));
   const double scale = (P > 0) ? 1.0 / ((double)K * P) : 0.0;
+  // Final-state loss: its normalisations from the observations, as the
+  // reference takes them (WSE_truth range + sqrt(eps); the largest observed
+  // speed, at least eps), and the observations in device order.
+  FinalLossDev fl;
+  const bool useFinal = fo && (fo->wse || (fo->u && fo->v));
+  if (useFinal) {
+    if (!b->fin) {
+      ADJ_CUDA(c, cudaMalloc(&b->fin, (size_t)4 * N * sizeof(double)));
+      ADJ_CUDA(c, cudaMalloc(&b->finScratch, ((size_t)N + 2 + 2 * kFinalLossBlocks) * sizeof(double)));
+      ADJ_CUDA(c, cudaMalloc(&b->finTicket, sizeof(unsigned int)));
+      ADJ_CUDA(c, cudaMemsetAsync(b->finTicket, 0, sizeof(unsigned int), st));
+    }
+    std::vector<double> dev((size_t)4 * N);
+    auto put = [&](int slot, const double* v) {
+      for (int i = 0; i < N; ++i) dev[(size_t)slot * N + i] = v[c->perm[i]];
+    };
+    fl.invN = 1.0 / (double)N;
+    if (fo->wse) {
+      put(0, fo->wse);
+      const auto mm = std::minmax_element(fo->wse, fo->wse + N);
+      fl.wseDen = (*mm.second - *mm.first) + 1.4901161193847656e-08;
+      fl.wse = b->fin;
+      fl.zbw = fo->zbw ? b->fin + (size_t)3 * N : c->dm.zb;
+      if (fo->zbw) put(3, fo->zbw);
+    }
+    if (fo->u && fo->v) {
+      put(1, fo->u);
+      put(2, fo->v);
+      double vmax = 0.0;
+      for (int i = 0; i < N; ++i) vmax = std::max(vmax, std::sqrt(fo->u[i] * fo->u[i] + fo->v[i] * fo->v[i]));
+      fl.velScale = std::max(vmax, 2.220446049250313e-16);
+      fl.u = b->fin + N;
+      fl.v = b->fin + (size_t)2 * N;
+    }
+    ADJ_CUDA(c, cudaMemcpyAsync(b->fin, dev.data(), dev.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+    fl.dWse = b->finScratch;
+    fl.parts = b->finScratch + N;
+    fl.partials = b->finScratch + N + 2;
+    fl.ticket = b->finTicket;
+  }
   const DevMesh& dm = c->dm;
   const DevScalars& ds = c->ds;
   const int extraPerStep = 2 * dm.nInlet;
@@ -320,6 +370,10 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
     // Reverse sweep.
     ADJ_CUDA(c, cudaMemsetAsync(b->mu2, 0, n3 * sizeof(double), st));
     launch_probe_adjoint_f64(dm, c->QA, b->mu2, b->probes, b->obs + (size_t)(K - 1) * P, P, scale, st);
+    if (useFinal) {
+      launch_final_loss_f64(dm, fl, c->QA, b->mu2, st);
+      c->launches += 1;
+    }
     for (int seg = nck - 1; seg >= 0; --seg) {
       const int s0 = seg * C, s1 = std::min(K, s0 + C);
       double* Q0s = b->seg;                          // Q0 of step s0 + i at Q0s + i n3 (i = 0..C)
@@ -424,6 +478,10 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
     }
     ADJ_CUDA(c, cudaMemsetAsync(mu2, 0, n3 * sizeof(float), st));
     launch_probe_adjoint_f32(dm, XA, mu2, pc, b->obs + (size_t)(K - 1) * P, scale, st);
+    if (useFinal) {
+      launch_final_loss_f32(dm, fl, XA, mu2, st);
+      c->launches += 1;
+    }
     for (int seg = nck - 1; seg >= 0; --seg) {
       const int s0 = seg * C, s1 = std::min(K, s0 + C);
       ADJ_CUDA(c, copy_state(sg.at(0, n), ck.at(seg, n)));
@@ -464,16 +522,26 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
   ADJ_CUDA(c, cudaMemcpyAsync(hZ.data(), b->gzb, N * sizeof(double), cudaMemcpyDeviceToHost, st));
   if (dm.nInlet > 0)
     ADJ_CUDA(c, cudaMemcpyAsync(hQ.data(), a.gQ, dm.nInlet * sizeof(double), cudaMemcpyDeviceToHost, st));
+  double fparts[2] = {0.0, 0.0};
+  const bool direct = useFinal && fl.wse && !fo->zbw;   // WSE_pred = h + (active zb): dL/dzb += dL/dWSE
+  std::vector<double> hW(direct ? N : 0);
+  if (useFinal) ADJ_CUDA(c, cudaMemcpyAsync(fparts, fl.parts, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  if (direct) ADJ_CUDA(c, cudaMemcpyAsync(hW.data(), fl.dWse, N * sizeof(double), cudaMemcpyDeviceToHost, st));
   int32_t flags = 0;
   ADJ_CUDA(c, cudaMemcpyAsync(&flags, ds.flags, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
   ADJ_CUDA(c, cudaStreamSynchronize(st));
   if (flags & 2) return fail(c, HG_ERR_INLET, "inlet-Q total conveyance is not positive during the run");
   if (flags & 1) return fail(c, HG_ERR_STATE, "non-finite value in the state during the run");
-  *loss = hl * scale;
+  *loss = hl * scale + fparts[0] + fparts[1];
+  if (parts) {
+    parts[0] = fparts[0] + fparts[1];
+    parts[1] = fparts[0];
+    parts[2] = fparts[1];
+  }
   for (int i = 0; i < N; ++i) {
     const int o = c->perm[i];
     if (gManning) gManning[o] = hN[i];
-    if (gZb) gZb[o] = hZ[i];
+    if (gZb) gZb[o] = hZ[i] + (direct ? hW[i] : 0.0);
   }
   if (gInlet)
     for (int g = 0; g < dm.nInlet; ++g) gInlet[g] = hQ[g];

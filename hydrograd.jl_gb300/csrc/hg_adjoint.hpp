@@ -7,9 +7,23 @@ struct hg_ctx;
 
 namespace hg {
 
+// Observations of the final-state inversion loss (swe_2D_inversion.jl:383-431),
+// caller order: WSE_truth (or null), u_truth and v_truth (or null), and the zb
+// of WSE_pred = h + zb (null: the context's zb, an active zb parameter whose
+// direct term then enters g_zb).
+struct FinalObs {
+  const double* wse = nullptr;
+  const double* u = nullptr;
+  const double* v = nullptr;
+  const double* zbw = nullptr;
+};
+
+// loss = the probe misfit (mean over steps and probes) + the final-state loss
+// of fo (if given); parts (if given) = {final loss, its WSE term, its uv term}.
 int adjoint_loss_and_grad(hg_ctx* ctx, const double* Q0, int32_t nsteps, double dt, int32_t ckpt_every,
                           const int32_t* probe_cells, const double* obs, int32_t n_probe, double* loss,
-                          double* g_manning_cells, double* g_zb, double* g_inletq, double* Q_final);
+                          double* g_manning_cells, double* g_zb, double* g_inletq, double* Q_final,
+                          const FinalObs* fo = nullptr, double* parts = nullptr);
 void adjoint_release(hg_ctx* ctx);
 
 }  // namespace hg

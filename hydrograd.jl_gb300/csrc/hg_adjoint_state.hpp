@@ -70,6 +70,29 @@ struct ProbeCsr {
 };
 void launch_probe_adjoint_f32(const DevMesh& m, StateF32 Q, float* mu, const ProbeCsr& pc, const double* obs,
                               double scale, cudaStream_t st);
+// Final-state inversion loss (swe_2D_inversion.jl:383-431), device order:
+//   WSE term  sum_c ((h_c + zbw_c - wse_c) / wseDen)^2 / n,  h = xi + hstill
+//   uv term   sum_c ((qx_c / (h_c + eps) - u_c)^2 + (qy_c / (h_c + eps) - v_c)^2) / velScale^2 / n
+// with eps = sqrt(eps(Float64)).  launch_final_loss_* add the loss's gradient
+// w.r.t. the final state to mu (masked by the last stage's clamp, like the
+// probe terms), write dL/dWSE per cell to dWse (the direct term of an active
+// zb parameter) and the two sums to parts[0..1] (deterministic reduction).
+constexpr int kFinalLossBlocks = 1024;
+struct FinalLossDev {
+  const double* wse = nullptr;   // [n] or null: no WSE term
+  const double* u = nullptr;     // [n] u, v or null: no velocity term
+  const double* v = nullptr;
+  const double* zbw = nullptr;   // [n] zb of WSE_pred
+  double wseDen = 1.0;           // WSE_truth range + eps
+  double velScale = 1.0;
+  double invN = 1.0;
+  double* dWse = nullptr;        // [n]
+  double* parts = nullptr;       // [2]
+  double* partials = nullptr;    // [2 * kFinalLossBlocks]
+  unsigned int* ticket = nullptr;
+};
+void launch_final_loss_f64(const DevMesh& m, const FinalLossDev& f, const double* Q, double* mu, cudaStream_t st);
+void launch_final_loss_f32(const DevMesh& m, const FinalLossDev& f, StateF32 Q, float* mu, cudaStream_t st);
 // gN, gS0x, gS0y, gZb += the FP32 pair accumulators (accF).
 void launch_fold_accumulators_f32(const DevMesh& m, const AdjDev& a, cudaStream_t st);
 // dL/dzb = S0 transpose (Green-Gauss of face averages) applied to dL/dS0, plus the direct term.

@@ -651,6 +651,27 @@ int hg_set_ude(hg_ctx* ctx, const hg_ude_desc* u) {
   return u->kind == HG_RES_UDE_FLOW_RESISTANCE ? upload_cells(ctx) : HG_OK;
 }
 
+int hg_final_loss_and_grad(hg_ctx* ctx, const double* Q0, int32_t nsteps, double dt, int32_t ckpt_every,
+                           const hg_final_obs* obs, double* parts, double* g_manning_cells, double* g_zb,
+                           double* g_inletq, double* Q_final) {
+  if (!ctx || !Q0 || nsteps <= 0 || !(dt > 0) || !obs || !parts || (!obs->wse && !(obs->u && obs->v)) ||
+      (!obs->u != !obs->v))
+    return fail(ctx, HG_ERR_ARG, "hg_final_loss_and_grad: bad argument");
+  if (ctx->dm.res.kind != kResConstant)
+    return fail(ctx, HG_ERR_UNSUPPORTED,
+                "hg_final_loss_and_grad: gradients through a state-dependent Manning n or a UDE closure are not "
+                "available");
+  cudaSetDevice(ctx->device);
+  FinalObs fo;
+  fo.wse = obs->wse;
+  fo.u = obs->u;
+  fo.v = obs->v;
+  fo.zbw = obs->zb_wse;
+  double loss = 0.0;
+  return adjoint_loss_and_grad(ctx, Q0, nsteps, dt, ckpt_every, nullptr, nullptr, 0, &loss, g_manning_cells, g_zb,
+                               g_inletq, Q_final, &fo, parts);
+}
+
 int hg_get_bed(hg_ctx* ctx, double* zb, double* S0, double* man, double* hstill) {
   if (!ctx) return fail(ctx, HG_ERR_ARG, "hg_get_bed: null context");
   for (int i = 0; i < ctx->n; ++i) {

@@ -45,6 +45,10 @@ class HgUdeDesc(ctypes.Structure):
                 ("ks_bounds", ctypes.c_double * 2), ("ks_cells", _dp), ("layernorm_over_batch", ctypes.c_int32)]
 
 
+class HgFinalObs(ctypes.Structure):
+    _fields_ = [("wse", _dp), ("u", _dp), ("v", _dp), ("zb_wse", _dp)]
+
+
 class HgConsts(ctypes.Structure):
     _fields_ = [("g", ctypes.c_double), ("k_n", ctypes.c_double), ("h_small", ctypes.c_double),
                 ("riemann", ctypes.c_int32), ("order", ctypes.c_int32)]
@@ -87,6 +91,8 @@ SIGNATURES = {
     "hg_advance": [_vp, ctypes.c_int32, ctypes.c_double, ctypes.c_double, ctypes.c_int32],
     "hg_synchronize": [_vp],
     "hg_elapsed_time": [_vp, _dp],
+    "hg_final_loss_and_grad": [_vp, _dp, ctypes.c_int32, ctypes.c_double, ctypes.c_int32, ctypes.POINTER(HgFinalObs),
+                               _dp, _dp, _dp, _dp, _dp],
     "hg_loss_and_grad": [_vp, _dp, ctypes.c_int32, ctypes.c_double, ctypes.c_int32, _ip, _dp, ctypes.c_int32, _dp,
                          _dp, _dp, _dp, _dp],
     "hg_launch_count": [_vp, ctypes.POINTER(ctypes.c_int64)],

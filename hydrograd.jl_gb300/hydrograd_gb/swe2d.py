@@ -19,7 +19,7 @@ import ctypes
 import numpy as np
 
 from . import _lib
-from ._lib import HgConsts, HgEnsembleDesc, HgMeshDesc, HgUdeDesc, check, lib
+from ._lib import HgConsts, HgEnsembleDesc, HgFinalObs, HgMeshDesc, HgUdeDesc, check, lib
 
 _dp = ctypes.POINTER(ctypes.c_double)
 _ip = ctypes.POINTER(ctypes.c_int32)
@@ -292,6 +292,27 @@ class SWE2D:
                                          _d(obs), len(probes), _d(loss), _d(gn), _d(gz), _d(gq), _d(Qf)))
         return dict(loss=float(loss[0]), g_manning=gn, g_zb=gz, g_inletq=None if gq is None else gq[:self.n_inletq],
                     Q=Qf)
+
+    def final_loss_and_grad(self, Q0, nsteps, dt, wse=None, u=None, v=None, zb_wse=None, ckpt_every=50,
+                            want=("manning", "zb", "inletq")):
+        """The final-state inversion loss of swe_2D_inversion.jl:383-431 (WSE and
+        velocity misfits of the state after nsteps SSP-RK2 steps of dt) and its
+        gradients (hg_final_loss_and_grad).  zb_wse None: WSE_pred = h + the
+        context's zb (an active zb parameter; g_zb then has the direct term)."""
+        N = self.n_cells
+        arr = lambda a: None if a is None else np.ascontiguousarray(a, dtype=np.float64)
+        keep = [arr(a) for a in (wse, u, v, zb_wse)]
+        obs = HgFinalObs(*(_d(a) for a in keep))
+        parts = np.zeros(3)
+        gn = np.zeros(N) if "manning" in want else None
+        gz = np.zeros(N) if "zb" in want else None
+        gq = np.zeros(max(self.n_inletq, 1)) if "inletq" in want else None
+        Qf = np.zeros(3 * N)
+        self._chk(lib().hg_final_loss_and_grad(self.h, _d(np.ascontiguousarray(Q0, dtype=np.float64)), int(nsteps),
+                                               float(dt), int(ckpt_every), ctypes.byref(obs), _d(parts), _d(gn),
+                                               _d(gz), _d(gq), _d(Qf)))
+        return dict(loss=float(parts[0]), loss_wse=float(parts[1]), loss_uv=float(parts[2]), g_manning=gn, g_zb=gz,
+                    g_inletq=None if gq is None else gq[:self.n_inletq], Q=Qf)
 
 
 class PinnedBuffer:

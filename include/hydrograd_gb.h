@@ -269,6 +269,23 @@ int hg_elapsed_time(hg_ctx* ctx, double* t);
 int hg_loss_and_grad(hg_ctx* ctx, const double* Q0, int32_t nsteps, double dt, int32_t ckpt_every,
                      const int32_t* probe_cells, const double* obs, int32_t n_probe, double* loss,
                      double* g_manning_cells, double* g_zb, double* g_inletq, double* Q_final);
+/* The final-state inversion loss of swe_2D_inversion.jl:383-431 and its
+ * gradients, through the same checkpointed adjoint (nsteps SSP-RK2 steps of dt):
+ *   WSE term  sum ((h + zb_wse - wse) / (range(wse) + sqrt(eps)))^2 / n
+ *   uv term   sum ((qx / (h + sqrt(eps)) - u)^2 + (qy / (h + sqrt(eps)) - v)^2) / max|(u, v)|^2 / n
+ * with h = xi + hstill of the final state.  wse may be NULL (no WSE term); u and
+ * v both or neither.  zb_wse NULL: WSE_pred uses the context's zb, as with an
+ * active zb parameter, and g_zb includes the direct term.  parts[3] = {WSE + uv,
+ * WSE, uv}.  The parameter-only regularisers (bound, slope) are the caller's. */
+typedef struct hg_final_obs {
+  const double* wse;     /* [n] WSE_truth */
+  const double* u;       /* [n] u_truth */
+  const double* v;       /* [n] v_truth */
+  const double* zb_wse;  /* [n] zb_cell_truth, or NULL */
+} hg_final_obs;
+int hg_final_loss_and_grad(hg_ctx* ctx, const double* Q0, int32_t nsteps, double dt, int32_t ckpt_every,
+                           const hg_final_obs* obs, double* parts, double* g_manning_cells, double* g_zb,
+                           double* g_inletq, double* Q_final);
 
 /* ---- measurement support ---------------------------------------------------- */
 /* Number of kernel launches this context has enqueued (graph replays count their kernels). */
