@@ -43,6 +43,14 @@ def _run(cmd):
     return r.stdout + r.stderr
 
 
+def _stage_block_define():
+    """HG_STAGE_BLOCK: cells per block of the FP32 stage kernels (default 256),
+    the same in every translation unit (the host builds the fused stepping's
+    per-block tables with it)."""
+    v = os.environ.get("HG_STAGE_BLOCK")
+    return ["-DHG_STAGE_BLOCK=%d" % int(v)] if v else []
+
+
 def build(verbose=False):
     cuda_home, nvcc = _cuda_home()
     os.makedirs(OUT, exist_ok=True)
@@ -58,13 +66,15 @@ def build(verbose=False):
             fmad = ["--use_fast_math"]
         if src == "hg_forward_f32.cu" and os.environ.get("HG_STAGE_MIN_BLOCKS"):
             fmad = fmad + ["-DHG_STAGE_MIN_BLOCKS=%d" % int(os.environ["HG_STAGE_MIN_BLOCKS"])]
+        fmad = fmad + _stage_block_define()
         jobs.append([nvcc, "-std=c++17", "-O3", *ARCH, *fmad, "-lineinfo", "-Xcompiler", "-fPIC", "-I", INCLUDE,
                      "-c", os.path.join(CSRC, src), "-o", obj])
     for src in CXX_SOURCES:
         obj = os.path.join(OUT, src + ".o")
         objs.append(obj)
         jobs.append(["g++", "-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-Wall", "-I", INCLUDE,
-                     "-I", os.path.join(cuda_home, "include"), "-c", os.path.join(CSRC, src), "-o", obj])
+                     "-I", os.path.join(cuda_home, "include"), *_stage_block_define(), "-c", os.path.join(CSRC, src),
+                     "-o", obj])
     with ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
         logs = list(ex.map(_run, jobs))
     if verbose:

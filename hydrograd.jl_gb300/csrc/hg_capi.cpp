@@ -275,11 +275,81 @@ int set_fixed_dt(hg_ctx* c, double dt) {
   return HG_OK;
 }
 
+// Autotuner of the fused FP32 stages: times each stage kernel usable on this
+// mesh (gather, pipe, tma -- all compute the same results) on the resident
+// state, a stage-1 and a stage-2 launch per repetition, each repetition after
+// an L2 flush and the kernels interleaved, and keeps the fastest.  Outputs go
+// to scratch carved from the flush buffer (the flush overwrites it before the
+// next repetition's stage 1 writes it again); the resident state, the step
+// bookkeeping and the error flags are left as they were.
+int autotune_stage(hg_ctx* c, int reps) {
+  if (!fused(c)) return HG_OK;
+  const size_t n = (size_t)c->n;
+  const size_t rec = (n * sizeof(float4) + 255) & ~(size_t)255, lo = (n * sizeof(float2) + 255) & ~(size_t)255;
+  if (2 * (rec + lo) > c->flushBytes) return HG_OK;   // no scratch: keep the default
+  char* base = static_cast<char*>(c->flushBuf);
+  const StateF32 s1{reinterpret_cast<float4*>(base), reinterpret_cast<float2*>(base + rec)};
+  const StateF32 s2{reinterpret_cast<float4*>(base + rec + lo), reinterpret_cast<float2*>(base + 2 * rec + lo)};
+  int32_t flags = 0;
+  HG_CUDA(c, cudaMemcpyAsync(&flags, c->ds.flags, sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream));
+  HG_CUDA(c, cudaStreamSynchronize(c->stream));
+  std::vector<int> cand;
+  for (int k : {(int)kStageGather, (int)kStagePipe, (int)kStageTma})
+    if (stage_kernel_usable(c->dm, k, kModeStage1, xa(c), StateF32{}) &&
+        stage_kernel_usable(c->dm, k, kModeStage2, s1, xa(c)))
+      cand.push_back(k);
+  std::vector<double> total(cand.size(), 0.0);
+  cudaEvent_t a, b;
+  HG_CUDA(c, cudaEventCreate(&a));
+  HG_CUDA(c, cudaEventCreate(&b));
+  StageFuse f;   // fixed dt, no step record, totals into the stage buffer's slots
+  f.partials = c->d_partials;
+  f.ticket = c->d_ticket;
+  f.blockSlot = c->d_blockSlot;
+  f.nSlots = c->nSlots;
+  for (int r = 0; r < reps; ++r)
+    for (size_t i = 0; i < cand.size(); ++i) {
+      DevMesh m = c->dm;
+      m.stageKernel = cand[i];
+      c->launches += launch_flush(c->flushBuf, c->flushBytes, c->stream);
+      cudaEventRecord(a, c->stream);
+      f.totalIn = c->d_tot;
+      f.totalOut = c->d_tot + kMaxFusedInlets;
+      launch_stage_f32_fused(m, c->ds, kModeStage1, xa(c), StateF32{}, s1, f, c->stream);
+      f.totalIn = c->d_tot + kMaxFusedInlets;
+      launch_stage_f32_fused(m, c->ds, kModeStage2, s1, xa(c), s2, f, c->stream);
+      cudaEventRecord(b, c->stream);
+      cudaEventSynchronize(b);
+      float ms = 0.0f;
+      cudaEventElapsedTime(&ms, a, b);
+      total[i] += ms;
+      c->launches += 2;
+    }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  HG_CUDA(c, cudaGetLastError());
+  HG_CUDA(c, cudaMemcpyAsync(c->ds.flags, &flags, sizeof(int32_t), cudaMemcpyHostToDevice, c->stream));
+  HG_CUDA(c, cudaStreamSynchronize(c->stream));
+  size_t best = 0;
+  for (size_t i = 1; i < cand.size(); ++i)
+    if (total[i] < total[best]) best = i;
+  if (!cand.empty() && c->dm.stageKernel != cand[best]) {
+    c->dm.stageKernel = cand[best];
+    c->graphValid = false;
+  }
+  c->stageTuned = true;
+  return HG_OK;
+}
+
 // Set-up before a run of RK2 steps (rk2 = false: reference Euler steps).
 int begin_steps(hg_ctx* c, bool rk2, double dt, double cfl) {
   const bool cflMode = dt <= 0;
   if (!cflMode) {
     int rc = set_fixed_dt(c, dt);
+    if (rc) return rc;
+  }
+  if (rk2 && fused(c) && !c->stageTuned && stage_kernel_forced() < 0) {
+    int rc = autotune_stage(c, 3);
     if (rc) return rc;
   }
   if (rk2 && fused(c)) {
@@ -883,6 +953,15 @@ int hg_advance_timed(hg_ctx* ctx, int32_t nsteps, double dt, double cfl, int32_t
   return check_flags(ctx);
 }
 
+int hg_autotune(hg_ctx* ctx, int32_t reps, int32_t* kernel) {
+  if (!ctx || reps <= 0) return fail(ctx, HG_ERR_ARG, "hg_autotune: bad argument");
+  cudaSetDevice(ctx->device);
+  int rc = autotune_stage(ctx, reps);
+  if (rc) return rc;
+  if (kernel) *kernel = stage_kernel_forced() >= 0 ? stage_kernel_forced() : ctx->dm.stageKernel;
+  return HG_OK;
+}
+
 int hg_time_stage_kernel(hg_ctx* ctx, int32_t n, int32_t flush_l2, double* avg_ms) {
   if (!ctx || n <= 0 || !avg_ms) return fail(ctx, HG_ERR_ARG, "hg_time_stage_kernel: bad argument");
   cudaSetDevice(ctx->device);
@@ -1103,6 +1182,53 @@ int ctx_setup_device(hg_ctx* c) {
     std::memcpy(&r.w, &nb[i], sizeof(float));
     SL[i] = r;
   }
+  // Pipelined stage tables (degree <= 4): per tile of kStageBlockF32 cells, the
+  // out-of-tile neighbours in order of first reference, and the slot records
+  // with tile-local neighbour indices.
+  std::vector<float4> SLp;
+  std::vector<int32_t> halo;
+  if (S <= 4) {
+    const int nTiles = (N + kStageBlockF32 - 1) / kStageBlockF32;
+    SLp = SL;
+    halo.assign((size_t)nTiles * kHaloMax, -1);
+    std::vector<int32_t> seen(N, -1);   // cell -> halo slot in the current tile
+    bool fits = true;
+    for (int t = 0; t < nTiles && fits; ++t) {
+      const int c0 = t * kStageBlockF32, c1 = std::min(N, c0 + kStageBlockF32);
+      int h = 0;
+      for (int cell = c0; cell < c1 && fits; ++cell)
+        for (int k = 0; k < S; ++k) {
+          const size_t i = (size_t)k * N + cell;
+          const int32_t v = nb[i];
+          if (v < 0) continue;
+          int32_t loc;
+          if (v >= c0 && v < c1) {
+            loc = v - c0;
+          } else {
+            if (seen[v] < 0 || halo[(size_t)t * kHaloMax + seen[v]] != v) {
+              if (h == kHaloMax) { fits = false; break; }
+              seen[v] = h;
+              halo[(size_t)t * kHaloMax + h] = v;
+              ++h;
+            }
+            loc = kStageBlockF32 + seen[v];
+          }
+          std::memcpy(&SLp[i].w, &loc, sizeof(float));
+        }
+    }
+    if (!fits) {
+      SLp.clear();
+      halo.clear();
+    }
+  }
+  float4* d_SLp = nullptr;
+  int32_t* d_halo = nullptr;
+  if (!SLp.empty()) {
+    HG_CUDA(c, dalloc(c, &d_SLp, SLp.size()));
+    HG_CUDA(c, dalloc(c, &d_halo, halo.size()));
+    HG_CUDA(c, upload(c, d_SLp, SLp));
+    HG_CUDA(c, upload(c, d_halo, halo));
+  }
   c->h_area = to_float(area);
   HG_CUDA(c, upload(c, d_nb, nb));
   HG_CUDA(c, upload(c, c->d_blockSlot, blockSlot));
@@ -1132,6 +1258,9 @@ int ctx_setup_device(hg_ctx* c) {
   dm.nExit = (int32_t)m.exitGroups.size();
   dm.nb = d_nb; dm.snx = d_snx; dm.sny = d_sny; dm.slen = d_slen;
   dm.SL = d_SL;
+  dm.SLp = d_SLp;
+  dm.halo = d_halo;
+  dm.stageKernel = d_SLp ? kStagePipe : kStageGather;
   dm.bfInfo = d_bfInfo; dm.bfLp23 = d_lp23; dm.bfLp23f = d_lp23f; dm.bfLp53 = d_bflp53;
   dm.bfExitRel = c->d_bfExitRel;
   dm.inletOff = d_inletOff; dm.inletCell = d_inletCell; dm.inletLp53 = d_lp53;

@@ -66,6 +66,7 @@ struct hg_ctx {
   bool graphValid = false, graphCflMode = false;
   double graphCfl = 0.0;
   int64_t graphLaunches = 0;
+  bool stageTuned = false;          // hg_autotune has chosen dm.stageKernel
   int64_t launches = 0;
   hg::AdjointBuffers* adj = nullptr;
   // State-dependent resistance (hg_set_manning_function / hg_set_ude): device

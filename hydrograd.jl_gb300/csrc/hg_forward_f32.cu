@@ -31,9 +31,12 @@ constexpr int kBlock = kStageBlockF32;
 
 inline int blocks_for(int n) { return (n + kBlock - 1) / kBlock; }
 
-template <int NS>
+// LOC: the slot records hold tile-local neighbour indices (DevMesh::SLp): own
+// cells at [0, kBlock) of sX / sP, halo cells at [kBlock, ...) of hX / hP.
+template <int NS, bool LOC>
 __device__ __forceinline__ void face_sum_f32(const DevMesh& m, const float4* __restrict__ X, const float4* sX,
-                                             const float4* sP, int base, int c, const SideF32& L,
+                                             const float4* sP, const float4* hX, const float4* hP, int base, int c,
+                                             const SideF32& L,
                                              const OwnF32& own, float2 hstPair, const float4 (&sl)[NS],
                                              const double* __restrict__ totalA, float man, int32_t* flags, float& f0,
                                              float& f1, float& f2) {
@@ -46,14 +49,24 @@ __device__ __forceinline__ void face_sum_f32(const DevMesh& m, const float4* __r
     Side<float> R;
     float dxi, dhst = 0.0f;
     if (nb >= 0) {
-      const unsigned int ln = (unsigned int)(nb - base);   // in-block neighbour: staged record
       float4 xr, pr;
-      if (ln < (unsigned int)kBlock) {
-        xr = sX[ln];
-        pr = sP[ln];
+      if constexpr (LOC) {
+        if (nb < kBlock) {
+          xr = sX[nb];
+          pr = sP[nb];
+        } else {
+          xr = hX[nb - kBlock];
+          pr = hP[nb - kBlock];
+        }
       } else {
-        xr = __ldg(&X[nb]);
-        pr = __ldg(&m.CP[nb]);
+        const unsigned int ln = (unsigned int)(nb - base);   // in-block neighbour: staged record
+        if (ln < (unsigned int)kBlock) {
+          xr = sX[ln];
+          pr = sP[ln];
+        } else {
+          xr = __ldg(&X[nb]);
+          pr = __ldg(&m.CP[nb]);
+        }
       }
       const SideF32 r = make_side_f32(xr, pr, m.hsmf, m.hsmLo);
       R = r.s;
@@ -156,9 +169,9 @@ __device__ __forceinline__ double fused_dt(const DevScalars& s, const StageFuse&
 
 // The stage kernel is latency-bound (neighbour gathers): for meshes of degree
 // <= 4 it is held to the register budget of HG_STAGE_MIN_BLOCKS resident
-// blocks per SM (4: 64 registers, no spills; 50% occupancy).
+// blocks per SM (by default 64 registers a thread, no spills; 50% occupancy).
 #ifndef HG_STAGE_MIN_BLOCKS
-#define HG_STAGE_MIN_BLOCKS 4
+#define HG_STAGE_MIN_BLOCKS (1024 / kBlock)
 #endif
 template <int NS>
 constexpr int stage_min_blocks() { return NS <= 4 ? HG_STAGE_MIN_BLOCKS : 1; }
@@ -168,9 +181,10 @@ constexpr int stage_min_blocks() { return NS <= 4 ? HG_STAGE_MIN_BLOCKS : 1; }
 // kBlock) for in-block neighbours.  The input state's lo parts and (stage 2)
 // the base state are read at qinP[k], xbP[k], qbP[k] -- global arrays (k = c)
 // or a tile staged in shared memory -- where they are used.
-template <int NS, int MODE>
+template <int NS, int MODE, bool LOC = false>
 __device__ __forceinline__ void stage_cell(const DevMesh& m, const DevScalars& s, const float4* __restrict__ X,
-                                           const float4* sX, const float4* sP, int base, int c,
+                                           const float4* sX, const float4* sP, const float4* hX, const float4* hP,
+                                           int base, int c,
                                            const float4 (&sl)[NS], float4 xin, float4 cp, float4 cs,
                                            const float2* qinP, const float4* xbP, const float2* qbP, int k, float dt,
                                            const double* totalIn, StateF32 Xout, double* Rout, bool cfl,
@@ -178,7 +192,7 @@ __device__ __forceinline__ void stage_cell(const DevMesh& m, const DevScalars& s
   const SideF32 L = make_side_f32(xin, cp, m.hsmf, m.hsmLo);
   const OwnF32 own = own_f32(L.s, m.gf);
   float f0, f1, f2;
-  face_sum_f32<NS>(m, X, sX, sP, base, c, L, own, make_float2(cp.x, cp.y), sl, totalIn, cp.w, s.flags, f0, f1, f2);
+  face_sum_f32<NS, LOC>(m, X, sX, sP, hX, hP, base, c, L, own, make_float2(cp.x, cp.y), sl, totalIn, cp.w, s.flags, f0, f1, f2);
   const float A = cs.z;
   const float r0 = -f0 / A, r1 = -f1 / A, r2 = -f2 / A;
   // Manning friction, or the flow-resistance closure F q / |q|_smooth
@@ -281,8 +295,8 @@ __global__ void __launch_bounds__(kBlock, stage_min_blocks<NS>())
   __syncthreads();
   if (active) {
     const float dt = MODE == kModeRhs ? 0.0f : (FUSED ? dtShared : *s.dtf);
-    stage_cell<NS, MODE>(m, s, Xin.x, sX, sP, base, c, sl, xin, cp, cs, Xin.q, Xbase.x, Xbase.q, c, dt,
-                         FUSED ? f.totalIn : m.totalA, Xout, Rout, cfl, cand, hOut, wetOut);
+    stage_cell<NS, MODE>(m, s, Xin.x, sX, sP, nullptr, nullptr, base, c, sl, xin, cp, cs, Xin.q, Xbase.x, Xbase.q, c,
+                         dt, FUSED ? f.totalIn : m.totalA, Xout, Rout, cfl, cand, hOut, wetOut);
   }
   if (FUSED && f.record && blockIdx.x == 0 && threadIdx.x == 0) fused_record(s, f);
   if (cfl) block_min_publish_f(cand, FUSED ? s.cflMinF + (1 - f.parity) : s.cflMinF);
@@ -400,12 +414,128 @@ __global__ void __launch_bounds__(kBlock, kTmaCtasPerSm)
       float4 sl[NS];
 #pragma unroll
       for (int k = 0; k < NS; ++k) sl[k] = bSL[k * kBlock + tid];
-      stage_cell<NS, MODE>(m, s, Xin.x, bX, bCP, base, c, sl, bX[tid], bCP[tid], bCS[tid], bQ, bXB, bQB, tid, dt,
-                           f.totalIn, Xout, nullptr, cfl, cand, hOut, wetOut);
+      stage_cell<NS, MODE>(m, s, Xin.x, bX, bCP, nullptr, nullptr, base, c, sl, bX[tid], bCP[tid], bCS[tid], bQ, bXB,
+                           bQB, tid, dt, f.totalIn, Xout, nullptr, cfl, cand, hOut, wetOut);
     }
     if (m.nInlet > 0) fused_inlet_totals<NS>(m, f, t, c, hOut, wetOut);
     __syncthreads();   // buffer b is refilled by the copy issued at the top of the iteration after next
   }
+  if (f.record && blockIdx.x == 0 && tid == 0) fused_record(s, f);
+  if (cfl) block_min_publish_f(cand, s.cflMinF + (1 - f.parity));
+}
+
+// ---------------------------------------------------------------------------
+// Pipelined persistent fused stage (the default for meshes of degree <= 4)
+// ---------------------------------------------------------------------------
+// The block-per-tile kernel pays two dependent memory latencies per tile --
+// its own records, then its out-of-tile neighbours from inside the face loop
+// -- and with four resident blocks per SM they leave ~40% of the issue slots
+// empty.  Here each CTA walks tiles t = blockIdx.x, + gridDim.x, ... and,
+// while it computes tile t, asynchronous copies (cp.async, 16 B per record,
+// issued by every thread) bring tile t + gridDim.x into the other of two
+// shared-memory buffers: the tile's slot records (DevMesh::SLp, neighbours as
+// tile-local indices), state, parameter and source records, and its halo --
+// the out-of-tile neighbour records, listed per tile on the host (DevMesh::halo).
+// The halo list of the tile after that is read into a register one iteration
+// ahead, so no copy waits on a load.  The compute phase then reads only shared
+// memory; results equal k_stage_f32's (same stage_cell arithmetic).
+constexpr int kPipeCtasPerSm = 3;
+
+template <int NS, int MODE>
+struct PipeTile {
+  static constexpr uint32_t kRec = kBlock * sizeof(float4);
+  static constexpr uint32_t kLo = kBlock * sizeof(float2);
+  static constexpr uint32_t kHalo = kHaloMax * sizeof(float4);
+  static constexpr uint32_t kSL = 0, kX = NS * kRec, kCP = kX + kRec, kCS = kCP + kRec, kQ = kCS + kRec;
+  static constexpr uint32_t kHX = kQ + kLo, kHP = kHX + kHalo, kXB = kHP + kHalo, kQB = kXB + kRec;
+  static constexpr uint32_t kBuf = (((MODE == kModeStage2) ? kQB + kLo : kXB) + 127u) & ~127u;
+  static constexpr uint32_t kSmem = 2 * kBuf;
+};
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned int a = (unsigned int)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(a), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
+  const unsigned int a = (unsigned int)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(a), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+// Copies of tile t into buffer B: the thread's own cell's records, and halo
+// record hid (-1: none) into halo slot threadIdx.x.
+template <int NS, int MODE>
+__device__ __forceinline__ void pipe_issue(const DevMesh& m, StateF32 Xin, StateF32 Xbase, int t, unsigned char* B,
+                                           int hid) {
+  using T = PipeTile<NS, MODE>;
+  const int tid = threadIdx.x;
+  const int c = t * kBlock + tid;
+  if (c < m.n) {
+#pragma unroll
+    for (int k = 0; k < NS; ++k) cp_async16(B + T::kSL + (k * kBlock + tid) * 16, &m.SLp[(size_t)k * m.n + c]);
+    cp_async16(B + T::kX + tid * 16, &Xin.x[c]);
+    cp_async16(B + T::kCP + tid * 16, &m.CP[c]);
+    cp_async16(B + T::kCS + tid * 16, &m.CS[c]);
+    cp_async8(B + T::kQ + tid * 8, &Xin.q[c]);
+    if constexpr (MODE == kModeStage2) {
+      cp_async16(B + T::kXB + tid * 16, &Xbase.x[c]);
+      cp_async8(B + T::kQB + tid * 8, &Xbase.q[c]);
+    }
+  }
+  if (hid >= 0) {
+    cp_async16(B + T::kHX + tid * 16, &Xin.x[hid]);
+    cp_async16(B + T::kHP + tid * 16, &m.CP[hid]);
+  }
+}
+
+template <int NS, int MODE>
+__global__ void __launch_bounds__(kBlock, kPipeCtasPerSm)
+    k_stage_pipe_f32(DevMesh m, DevScalars s, StateF32 Xin, StateF32 Xbase, StateF32 Xout, int cfl, StageFuse f) {
+  using T = PipeTile<NS, MODE>;
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ float dtShared;
+  const int n = m.n, nTiles = (n + kBlock - 1) / kBlock, tid = threadIdx.x, G = gridDim.x;
+  if (tid == 0) dtShared = (float)fused_dt(s, f);
+  auto halo_id = [&](int t) { return (t < nTiles && tid < kHaloMax) ? m.halo[(size_t)t * kHaloMax + tid] : -1; };
+  int t = blockIdx.x;
+  if (t < nTiles) pipe_issue<NS, MODE>(m, Xin, Xbase, t, smem, halo_id(t));
+  cp_async_commit();
+  int hidNext = halo_id(t + G);
+  float cand = INFINITY;
+  int b = 0;
+  for (; t < nTiles; t += G, b ^= 1) {
+    const int tn = t + G;
+    if (tn < nTiles) pipe_issue<NS, MODE>(m, Xin, Xbase, tn, smem + (b ^ 1) * T::kBuf, hidNext);
+    cp_async_commit();
+    hidNext = halo_id(tn + G);
+    cp_async_wait<1>();   // tile t's copies (all groups but the one just issued) have landed
+    __syncthreads();
+    unsigned char* B = smem + b * T::kBuf;
+    const float4* bSL = reinterpret_cast<const float4*>(B + T::kSL);
+    const float4* bX = reinterpret_cast<const float4*>(B + T::kX);
+    const float4* bCP = reinterpret_cast<const float4*>(B + T::kCP);
+    const float4* bCS = reinterpret_cast<const float4*>(B + T::kCS);
+    const float2* bQ = reinterpret_cast<const float2*>(B + T::kQ);
+    const float4* bHX = reinterpret_cast<const float4*>(B + T::kHX);
+    const float4* bHP = reinterpret_cast<const float4*>(B + T::kHP);
+    const float4* bXB = reinterpret_cast<const float4*>(B + T::kXB);
+    const float2* bQB = reinterpret_cast<const float2*>(B + T::kQB);
+    const int base = t * kBlock, c = base + tid;
+    float hOut = 0.0f;
+    bool wetOut = false;
+    if (c < n) {
+      float4 sl[NS];
+#pragma unroll
+      for (int k = 0; k < NS; ++k) sl[k] = bSL[k * kBlock + tid];
+      stage_cell<NS, MODE, true>(m, s, Xin.x, bX, bCP, bHX, bHP, base, c, sl, bX[tid], bCP[tid], bCS[tid], bQ, bXB,
+                                 bQB, tid, dtShared, f.totalIn, Xout, nullptr, cfl, cand, hOut, wetOut);
+    }
+    if (m.nInlet > 0) fused_inlet_totals<NS>(m, f, t, c, hOut, wetOut);
+    __syncthreads();   // buffer b is refilled at the top of the next iteration
+  }
+  cp_async_wait<0>();
   if (f.record && blockIdx.x == 0 && tid == 0) fused_record(s, f);
   if (cfl) block_min_publish_f(cand, s.cflMinF + (1 - f.parity));
 }
@@ -569,18 +699,21 @@ void launch_stage_f32(const DevMesh& m, const DevScalars& s, int mode, StateF32 
   else launch_stage_ns<8, false>(m, s, mode, Xin, Xbase, Xout, Rout, f, nf, st);
 }
 namespace {
-// HG_STAGE_KERNEL=tma selects the persistent TMA kernel for the fused stages
-// instead of the one-block-per-tile kernel (both compute the same results).
-// Measured on the 1M-cell reach: 38.2 us against 33.1 us per stage -- the
-// prefetch halves the long-scoreboard stalls, but the per-tile barrier and
-// three resident CTAs per SM cost more than that; so the default is the
-// block-per-tile kernel.
-bool use_tma_stage() {
-  static const bool on = [] {
+// Kernel of the fused stages: HG_STAGE_KERNEL = gather / pipe / tma forces
+// one; otherwise DevMesh::stageKernel (hg_autotune's choice).  Measured on the
+// 1M-cell reach (CUDA events, L2 flushed): gather 37.1 us, pipe 37.1 us per
+// stage-1 launch, pipe 3 % faster per step; tma 41 us (its out-of-tile gathers
+// inside the face loop leave barrier stalls at every tile).
+int forced_stage_kernel() {
+  static const int k = [] {
     const char* e = std::getenv("HG_STAGE_KERNEL");
-    return e && std::strcmp(e, "tma") == 0;
+    if (!e) return -1;
+    if (std::strcmp(e, "gather") == 0) return (int)kStageGather;
+    if (std::strcmp(e, "pipe") == 0) return (int)kStagePipe;
+    if (std::strcmp(e, "tma") == 0) return (int)kStageTma;
+    return -1;
   }();
-  return on;
+  return k;
 }
 
 int sm_count() {
@@ -604,6 +737,27 @@ void launch_tma(const DevMesh& m, const DevScalars& s, StateF32 Xin, StateF32 Xb
   k_stage_tma_f32<NS, MODE><<<tiles < grid ? tiles : grid, kBlock, T::kSmem, st>>>(m, s, Xin, Xbase, Xout, cfl, fu);
 }
 
+template <int NS, int MODE>
+void launch_pipe(const DevMesh& m, const DevScalars& s, StateF32 Xin, StateF32 Xbase, StateF32 Xout, int cfl,
+                 const StageFuse& fu, cudaStream_t st) {
+  using T = PipeTile<NS, MODE>;
+  static const bool attr = [] {   // more than 48 KB of dynamic shared memory: opt in once
+    cudaFuncSetAttribute(k_stage_pipe_f32<NS, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T::kSmem);
+    return true;
+  }();
+  (void)attr;
+  static const int grid = sm_count() * kPipeCtasPerSm;
+  const int tiles = blocks_for(m.n);
+  k_stage_pipe_f32<NS, MODE><<<tiles < grid ? tiles : grid, kBlock, T::kSmem, st>>>(m, s, Xin, Xbase, Xout, cfl, fu);
+}
+
+template <int NS>
+void launch_pipe_mode(const DevMesh& m, const DevScalars& s, int mode, StateF32 Xin, StateF32 Xbase, StateF32 Xout,
+                      int cfl, const StageFuse& fu, cudaStream_t st) {
+  if (mode == kModeStage1) launch_pipe<NS, kModeStage1>(m, s, Xin, Xbase, Xout, cfl, fu, st);
+  else launch_pipe<NS, kModeStage2>(m, s, Xin, Xbase, Xout, cfl, fu, st);
+}
+
 template <int NS>
 void launch_tma_mode(const DevMesh& m, const DevScalars& s, int mode, StateF32 Xin, StateF32 Xbase, StateF32 Xout,
                      int cfl, const StageFuse& fu, cudaStream_t st) {
@@ -612,16 +766,33 @@ void launch_tma_mode(const DevMesh& m, const DevScalars& s, int mode, StateF32 X
 }
 }  // namespace
 
+int stage_kernel_forced() { return forced_stage_kernel(); }
+
+bool stage_kernel_usable(const DevMesh& m, int k, int mode, StateF32 Xin, StateF32 Xbase) {
+  auto a16 = [](const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; };
+  auto a8 = [](const void* p) { return (reinterpret_cast<uintptr_t>(p) & 7u) == 0; };
+  if (k == kStageGather) return true;
+  if (m.nslot > 4) return false;
+  if (k == kStagePipe)   // cp.async: 16-byte records 16-byte aligned, the lo parts 8-byte aligned
+    return m.SLp && m.halo && a16(m.SLp) && a16(m.CP) && a16(m.CS) && a16(Xin.x) && a8(Xin.q) &&
+           (mode != kModeStage2 || (a16(Xbase.x) && a8(Xbase.q)));
+  // bulk copies: 16-byte aligned sources (tile offsets are multiples of 2048 B);
+  // a state view whose lo parts start 8 bytes off takes another kernel
+  return a16(m.SL) && a16(m.CP) && a16(m.CS) && a16(Xin.x) && a16(Xin.q) &&
+         (mode != kModeStage2 || (a16(Xbase.x) && a16(Xbase.q)));
+}
+
 void launch_stage_f32_fused(const DevMesh& m, const DevScalars& s, int mode, StateF32 Xin, StateF32 Xbase,
                             StateF32 Xout, const StageFuse& fu, cudaStream_t st) {
   const int f = (!fu.record && fu.cflMode) ? 1 : 0;   // stage 2 publishes the next CFL minimum
-  // Bulk copies need 16-byte aligned sources (tile offsets are multiples of
-  // 2048 B); a state view whose lo parts start 8 bytes off (an odd cell count
-  // at an odd position in a buffer of states) takes the gather kernel.
-  auto a16 = [](const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; };
-  const bool aligned = a16(m.SL) && a16(m.CP) && a16(m.CS) && a16(Xin.x) && a16(Xin.q) &&
-                       (mode != kModeStage2 || (a16(Xbase.x) && a16(Xbase.q)));
-  if (use_tma_stage() && m.nslot <= 4 && aligned) {
+  const int forced = forced_stage_kernel();
+  const int k = forced >= 0 ? forced : m.stageKernel;
+  if (k == kStagePipe && stage_kernel_usable(m, k, mode, Xin, Xbase)) {
+    if (m.nslot <= 3) launch_pipe_mode<3>(m, s, mode, Xin, Xbase, Xout, f, fu, st);
+    else launch_pipe_mode<4>(m, s, mode, Xin, Xbase, Xout, f, fu, st);
+    return;
+  }
+  if (k == kStageTma && stage_kernel_usable(m, k, mode, Xin, Xbase)) {
     if (m.nslot <= 3) launch_tma_mode<3>(m, s, mode, Xin, Xbase, Xout, f, fu, st);
     else launch_tma_mode<4>(m, s, mode, Xin, Xbase, Xout, f, fu, st);
     return;

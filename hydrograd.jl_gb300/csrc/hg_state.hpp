@@ -57,6 +57,16 @@ struct DevMesh {
   const double* sny = nullptr;
   const double* slen = nullptr;      // [nslot*n] edge length
   const float4* SL = nullptr;        // FP32 path: [nslot*n] {nx, ny, L, nb as bits} (see hg_f32.cuh)
+  // Pipelined FP32 stage (meshes of degree <= 4): the slot records with the
+  // neighbour as a tile-local index (own cells [0, kStageBlockF32), halo
+  // cells kStageBlockF32 + j), and each tile's halo: the out-of-tile
+  // neighbour cells, kHaloMax per tile, -1 padded.  Null when some tile has
+  // a larger halo.
+  const float4* SLp = nullptr;
+  const int32_t* halo = nullptr;
+  // Kernel of the fused FP32 stages (hg_autotune): kStageGather,
+  // kStagePipe or kStageTma.  All three compute the same results.
+  int32_t stageKernel = 0;
   const int32_t* bfInfo = nullptr;   // [nbf] type | group << 2
   const double* bfLp23 = nullptr;    // [nbf] L^(2/3) (inlet-Q faces)
   const double* bfLp53 = nullptr;    // [nbf] L^(5/3) (inlet-Q faces)
@@ -149,8 +159,17 @@ void launch_stage_f32(const DevMesh& m, const DevScalars& s, int mode, StateF32 
 void launch_stage_f32_fused(const DevMesh& m, const DevScalars& s, int mode, StateF32 Xin, StateF32 Xbase,
                             StateF32 Xout, const StageFuse& f, cudaStream_t st);
 // Blocks of an FP32 stage launch; block b holds cells [b * kStageBlockF32, (b + 1) * kStageBlockF32).
-constexpr int kStageBlockF32 = 256;
+#ifndef HG_STAGE_BLOCK
+#define HG_STAGE_BLOCK 256
+#endif
+constexpr int kStageBlockF32 = HG_STAGE_BLOCK;
+constexpr int kHaloMax = 128;   // out-of-tile neighbour cells a pipelined stage tile can hold
+enum StageKernel : int32_t { kStageGather = 0, kStagePipe = 1, kStageTma = 2 };
 int stage_blocks_f32(const DevMesh& m);
+// The kernel HG_STAGE_KERNEL forces (gather / pipe / tma), else -1.
+int stage_kernel_forced();
+// Whether kernel k can run the fused stages of this mesh and these states.
+bool stage_kernel_usable(const DevMesh& m, int k, int mode, StateF32 Xin, StateF32 Xbase);
 // Clear CFL-minimum buffer `parity` (fused stepping keeps two).
 void launch_reset_cfl(const DevScalars& s, int parity, cudaStream_t st);
 void launch_cfl_f32(const DevMesh& m, const DevScalars& s, StateF32 X, cudaStream_t st);

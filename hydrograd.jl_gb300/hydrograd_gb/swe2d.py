@@ -269,6 +269,13 @@ class SWE2D:
         self._chk(lib().hg_launch_count(self.h, ctypes.byref(c)))
         return int(c.value)
 
+    def autotune(self, reps=3):
+        """hg_autotune: time the FP32C stage kernels on the resident state and
+        keep the fastest; returns the choice (0 gather, 1 pipe, 2 tma)."""
+        k = np.zeros(1, np.int32)
+        self._chk(lib().hg_autotune(self.h, int(reps), _i(k)))
+        return int(k[0])
+
     def time_stage_kernel(self, n=10, flush_l2=True):
         ms = np.zeros(1)
         self._chk(lib().hg_time_stage_kernel(self.h, int(n), 1 if flush_l2 else 0, _d(ms)))

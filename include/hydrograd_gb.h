@@ -287,6 +287,17 @@ int hg_final_loss_and_grad(hg_ctx* ctx, const double* Q0, int32_t nsteps, double
                            const hg_final_obs* obs, double* parts, double* g_manning_cells, double* g_zb,
                            double* g_inletq, double* Q_final);
 
+/* ---- tuning ------------------------------------------------------------------ */
+/* Choose the kernel of the FP32-compensated fused stages for this mesh: each
+ * kernel that can run it (0 gather: one block per 256-cell tile; 1 pipe:
+ * persistent, the next tile and its halo prefetched by asynchronous copies;
+ * 2 tma: persistent, bulk-copy prefetch of the next tile) is timed on the
+ * resident state, reps times, and the fastest is kept.  All compute the same
+ * results.  The first RK2 steps of a context run it once by themselves;
+ * HG_STAGE_KERNEL=gather|pipe|tma in the environment forces a kernel.
+ * kernel (may be NULL) receives the choice. */
+int hg_autotune(hg_ctx* ctx, int32_t reps, int32_t* kernel);
+
 /* ---- measurement support ---------------------------------------------------- */
 /* Number of kernel launches this context has enqueued (graph replays count their kernels). */
 int hg_launch_count(const hg_ctx* ctx, int64_t* count);
