@@ -48,9 +48,18 @@ def load_peaks():
     return 6800.0, "fallback"
 
 
-def profile_traffic(precision):
+# The FP32C stage kernels hg_autotune chooses among: (name, ncu summary under profiles/)
+STAGE_KERNELS = {0: ("k_stage_f32 (one block per 256-cell tile)", "k_stage_f32_river_tri_1M.md"),
+                 1: ("k_stage_pipe_f32 (persistent; the next tile and its halo prefetched by cp.async)",
+                     "k_stage_pipe_f32_river_tri_1M.md"),
+                 2: ("k_stage_tma_f32 (persistent; the next tile prefetched by bulk copies)", None)}
+
+
+def profile_traffic(precision, kernel=0):
     """Per-cell DRAM bytes of the stage kernel from the committed ncu summary, if any."""
-    name = {"fp32c": "k_stage_f32_river_tri_1M.md", "fp64": "k_stage_f64_river_tri_1M.md"}[precision]
+    name = STAGE_KERNELS[kernel][1] if precision == "fp32c" else "k_stage_f64_river_tri_1M.md"
+    if name is None:
+        return None
     p = os.path.join(ROOT, "profiles", name)
     if not os.path.exists(p):
         return None
@@ -315,6 +324,8 @@ def run_ours(args):
         # Stage kernel alone (roofline).
         ctx.upload(case["Q0"])
         out[prec]["stage_ms"] = ctx.time_stage_kernel(20, True)
+        if prec == "fp32c":
+            out[prec]["stage_kernel"] = ctx.autotune(0)   # the kernel the autotuner chose
     # FP32C error vs the FP64 path over the whole run (same CFL rule; the FP64
     # path itself is checked against the oracle below and by the GPU tests).
     a, b = out["fp32c"]["state"], out["fp64"]["state"]
@@ -386,9 +397,10 @@ def run_ours(args):
     cell_b, face_b = BYTES_STAGE["fp32c"]
     bytes_stage = (cell_b + nfaces_cell * face_b) * N
     achieved = bytes_stage / (out["fp32c"]["stage_ms"] * 1e-3) / 1e9
-    tr = profile_traffic("fp32c")
+    kern = out["fp32c"]["stage_kernel"]
+    tr = profile_traffic("fp32c", kern)
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": None if tr is None else tr * N, "kernel": "k_stage_f32 (one RK2 stage pass)",
+            "traffic": None if tr is None else tr * N, "kernel": STAGE_KERNELS[kern][0] + ", one RK2 stage pass",
             "algorithmic_bytes_per_launch": bytes_stage, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)"}
     fp64_bytes = (BYTES_STAGE["fp64"][0] + nfaces_cell * BYTES_STAGE["fp64"][1]) * N
     cpu = None

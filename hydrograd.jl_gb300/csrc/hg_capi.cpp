@@ -954,10 +954,12 @@ int hg_advance_timed(hg_ctx* ctx, int32_t nsteps, double dt, double cfl, int32_t
 }
 
 int hg_autotune(hg_ctx* ctx, int32_t reps, int32_t* kernel) {
-  if (!ctx || reps <= 0) return fail(ctx, HG_ERR_ARG, "hg_autotune: bad argument");
+  if (!ctx || reps < 0) return fail(ctx, HG_ERR_ARG, "hg_autotune: bad argument");
   cudaSetDevice(ctx->device);
-  int rc = autotune_stage(ctx, reps);
-  if (rc) return rc;
+  if (reps > 0) {
+    int rc = autotune_stage(ctx, reps);
+    if (rc) return rc;
+  }
   if (kernel) *kernel = stage_kernel_forced() >= 0 ? stage_kernel_forced() : ctx->dm.stageKernel;
   return HG_OK;
 }

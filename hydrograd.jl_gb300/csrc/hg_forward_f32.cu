@@ -31,67 +31,79 @@ constexpr int kBlock = kStageBlockF32;
 
 inline int blocks_for(int n) { return (n + kBlock - 1) / kBlock; }
 
-// LOC: the slot records hold tile-local neighbour indices (DevMesh::SLp): own
-// cells at [0, kBlock) of sX / sP, halo cells at [kBlock, ...) of hX / hP.
+// Flux F (times nothing: the caller scales by the face length) of slot sl of
+// the cell with side L, own quantities own.  LOC: the slot's neighbour word
+// holds a tile-local index (bits 0-8: own cells at [0, kBlock) of sX / sP,
+// halo cells at [kBlock, ...) of hX / hP); otherwise a cell id.
+template <bool LOC>
+__device__ __forceinline__ void one_face_f32(const DevMesh& m, const float4* __restrict__ X, const float4* sX,
+                                             const float4* sP, const float4* hX, const float4* hP, int base,
+                                             const SideF32& L, const OwnF32& own, float2 hstPair, float4 sl, int32_t nb,
+                                             const double* __restrict__ totalA, float man, int32_t* flags,
+                                             float F[3]) {
+  const float nx = sl.x, ny = sl.y;
+  Side<float> R;
+  float dxi, dhst = 0.0f;
+  if (nb >= 0) {
+    float4 xr, pr;
+    if constexpr (LOC) {
+      const int li = nb & 511;
+      if (li < kBlock) {
+        xr = sX[li];
+        pr = sP[li];
+      } else {
+        xr = hX[li - kBlock];
+        pr = hP[li - kBlock];
+      }
+    } else {
+      const unsigned int ln = (unsigned int)(nb - base);   // in-block neighbour: staged record
+      if (ln < (unsigned int)kBlock) {
+        xr = sX[ln];
+        pr = sP[ln];
+      } else {
+        xr = __ldg(&X[nb]);
+        pr = __ldg(&m.CP[nb]);
+      }
+    }
+    const SideF32 r = make_side_f32(xr, pr, m.hsmf, m.hsmLo);
+    R = r.s;
+    dxi = (r.s.xi - L.s.xi) + (r.xlo - L.xlo);
+    dhst = (pr.x - hstPair.x) + (pr.y - hstPair.y);   // hstill_R - hstill_L from the pairs
+  } else {
+    const int32_t bf = boundary_index(nb);
+    const int32_t info = m.bfInfo[bf], type = info & 3, grp = info >> 2;
+    if (type == kBcInletQ && !(totalA[grp] > 1e-10)) atomicOr(flags, 2);   // bc_2D.jl:679
+    R = ghost_state<float>(L.s, type, nx, ny, m.hsmf, type == kBcExitH ? (float)m.exitWse[grp] : 0.0f,
+                           type == kBcInletQ ? (float)m.inletQ[grp] : 0.0f,
+                           type == kBcInletQ ? (float)totalA[grp] : 1.0f, m.bfLp23f[bf], man);
+    // xi_ghost - xi = (h_ghost - h) + ((h - hstill) - xi); for a wet exit-H
+    // ghost, from (WSE - zb) - hstill formed in FP64
+    dxi = (R.h - L.s.h) + L.excess;
+    if (type == kBcExitH && !R.dry) dxi = m.bfExitRel[bf] - (L.s.xi + L.xlo);
+  }
+  if (!L.s.dry && !R.dry) {
+    roe_flux_wet_f32(L.s, own, R, dxi, dhst, m.gf, nx, ny, F);
+  } else {
+    roe_flux<float>(L.s, R, dxi, m.gf, nx, ny, m.hsmf, F);
+    F[1] -= own.p * nx;   // the own pressure shift (pressure_jump_f32)
+    F[2] -= own.p * ny;
+  }
+}
+
 template <int NS, bool LOC>
 __device__ __forceinline__ void face_sum_f32(const DevMesh& m, const float4* __restrict__ X, const float4* sX,
                                              const float4* sP, const float4* hX, const float4* hP, int base, int c,
-                                             const SideF32& L,
-                                             const OwnF32& own, float2 hstPair, const float4 (&sl)[NS],
-                                             const double* __restrict__ totalA, float man, int32_t* flags, float& f0,
-                                             float& f1, float& f2) {
+                                             const SideF32& L, const OwnF32& own, float2 hstPair,
+                                             const float4 (&sl)[NS], const double* __restrict__ totalA, float man,
+                                             int32_t* flags, float& f0, float& f1, float& f2) {
   f0 = 0.0f; f1 = 0.0f; f2 = 0.0f;
 #pragma unroll
   for (int k = 0; k < NS; ++k) {
     const int32_t nb = slot_nb(sl[k]);
     if (nb == kNoFace) continue;
-    const float nx = sl[k].x, ny = sl[k].y, len = sl[k].z;
-    Side<float> R;
-    float dxi, dhst = 0.0f;
-    if (nb >= 0) {
-      float4 xr, pr;
-      if constexpr (LOC) {
-        if (nb < kBlock) {
-          xr = sX[nb];
-          pr = sP[nb];
-        } else {
-          xr = hX[nb - kBlock];
-          pr = hP[nb - kBlock];
-        }
-      } else {
-        const unsigned int ln = (unsigned int)(nb - base);   // in-block neighbour: staged record
-        if (ln < (unsigned int)kBlock) {
-          xr = sX[ln];
-          pr = sP[ln];
-        } else {
-          xr = __ldg(&X[nb]);
-          pr = __ldg(&m.CP[nb]);
-        }
-      }
-      const SideF32 r = make_side_f32(xr, pr, m.hsmf, m.hsmLo);
-      R = r.s;
-      dxi = (r.s.xi - L.s.xi) + (r.xlo - L.xlo);
-      dhst = (pr.x - hstPair.x) + (pr.y - hstPair.y);   // hstill_R - hstill_L from the pairs
-    } else {
-      const int32_t bf = boundary_index(nb);
-      const int32_t info = m.bfInfo[bf], type = info & 3, grp = info >> 2;
-      if (type == kBcInletQ && !(totalA[grp] > 1e-10)) atomicOr(flags, 2);   // bc_2D.jl:679
-      R = ghost_state<float>(L.s, type, nx, ny, m.hsmf, type == kBcExitH ? (float)m.exitWse[grp] : 0.0f,
-                             type == kBcInletQ ? (float)m.inletQ[grp] : 0.0f,
-                             type == kBcInletQ ? (float)totalA[grp] : 1.0f, m.bfLp23f[bf], man);
-      // xi_ghost - xi = (h_ghost - h) + ((h - hstill) - xi); for a wet exit-H
-      // ghost, from (WSE - zb) - hstill formed in FP64
-      dxi = (R.h - L.s.h) + L.excess;
-      if (type == kBcExitH && !R.dry) dxi = m.bfExitRel[bf] - (L.s.xi + L.xlo);
-    }
     float F[3];
-    if (!L.s.dry && !R.dry) {
-      roe_flux_wet_f32(L.s, own, R, dxi, dhst, m.gf, nx, ny, F);
-    } else {
-      roe_flux<float>(L.s, R, dxi, m.gf, nx, ny, m.hsmf, F);
-      F[1] -= own.p * nx;   // the own pressure shift (pressure_jump_f32)
-      F[2] -= own.p * ny;
-    }
+    one_face_f32<LOC>(m, X, sX, sP, hX, hP, base, L, own, hstPair, sl[k], nb, totalA, man, flags, F);
+    const float len = sl[k].z;
     f0 = fmaf(F[0], len, f0);
     f1 = fmaf(F[1], len, f1);
     f2 = fmaf(F[2], len, f2);
@@ -176,6 +188,13 @@ __device__ __forceinline__ double fused_dt(const DevScalars& s, const StageFuse&
 template <int NS>
 constexpr int stage_min_blocks() { return NS <= 4 ? HG_STAGE_MIN_BLOCKS : 1; }
 
+template <int NS, int MODE>
+__device__ __forceinline__ void stage_finish(const DevMesh& m, const DevScalars& s, const SideF32& L, float f0,
+                                             float f1, float f2, int c, const float4 (&sl)[NS], float4 xin, float4 cp,
+                                             float4 cs, const float2* qinP, const float4* xbP, const float2* qbP,
+                                             int k, float dt, StateF32 Xout, double* Rout, bool cfl, float& cand,
+                                             float& hOut, bool& wetOut);
+
 // One cell of a stage: clamp, faces, sources, compensated update and clamp of
 // the output, CFL candidate.  sX / sP hold the records of cells [base, base +
 // kBlock) for in-block neighbours.  The input state's lo parts and (stage 2)
@@ -193,6 +212,19 @@ __device__ __forceinline__ void stage_cell(const DevMesh& m, const DevScalars& s
   const OwnF32 own = own_f32(L.s, m.gf);
   float f0, f1, f2;
   face_sum_f32<NS, LOC>(m, X, sX, sP, hX, hP, base, c, L, own, make_float2(cp.x, cp.y), sl, totalIn, cp.w, s.flags, f0, f1, f2);
+  stage_finish<NS, MODE>(m, s, L, f0, f1, f2, c, sl, xin, cp, cs, qinP, xbP, qbP, k, dt, Xout, Rout, cfl, cand, hOut,
+                         wetOut);
+}
+
+// The rest of a cell's stage once its face sums f0..f2 (sum_k F_k L_k) are
+// formed: sources, -sum / A, compensated update, clamp of the output, CFL
+// candidate (or, in RHS mode, the RHS).
+template <int NS, int MODE>
+__device__ __forceinline__ void stage_finish(const DevMesh& m, const DevScalars& s, const SideF32& L, float f0,
+                                             float f1, float f2, int c, const float4 (&sl)[NS], float4 xin, float4 cp,
+                                             float4 cs, const float2* qinP, const float4* xbP, const float2* qbP,
+                                             int k, float dt, StateF32 Xout, double* Rout, bool cfl, float& cand,
+                                             float& hOut, bool& wetOut) {
   const float A = cs.z;
   const float r0 = -f0 / A, r1 = -f1 / A, r2 = -f2 / A;
   // Manning friction, or the flow-resistance closure F q / |q|_smooth
@@ -723,6 +755,15 @@ int sm_count() {
   return sms > 0 ? sms : 1;
 }
 
+// CTAs of a persistent kernel resident per SM (its grid: every CTA resident,
+// so the tiles split evenly).
+template <class Kernel>
+int resident_ctas(Kernel k, uint32_t smem) {
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, kBlock, smem) != cudaSuccess || n < 1) n = 1;
+  return n;
+}
+
 template <int NS, int MODE>
 void launch_tma(const DevMesh& m, const DevScalars& s, StateF32 Xin, StateF32 Xbase, StateF32 Xout, int cfl,
                 const StageFuse& fu, cudaStream_t st) {
@@ -746,7 +787,7 @@ void launch_pipe(const DevMesh& m, const DevScalars& s, StateF32 Xin, StateF32 X
     return true;
   }();
   (void)attr;
-  static const int grid = sm_count() * kPipeCtasPerSm;
+  static const int grid = sm_count() * resident_ctas(k_stage_pipe_f32<NS, MODE>, T::kSmem);
   const int tiles = blocks_for(m.n);
   k_stage_pipe_f32<NS, MODE><<<tiles < grid ? tiles : grid, kBlock, T::kSmem, st>>>(m, s, Xin, Xbase, Xout, cfl, fu);
 }

@@ -64,8 +64,8 @@ struct DevMesh {
   // a larger halo.
   const float4* SLp = nullptr;
   const int32_t* halo = nullptr;
-  // Kernel of the fused FP32 stages (hg_autotune): kStageGather,
-  // kStagePipe or kStageTma.  All three compute the same results.
+  // Kernel of the fused FP32 stages (hg_autotune): kStageGather, kStagePipe or
+  // kStageTma.  All three compute the same results.
   int32_t stageKernel = 0;
   const int32_t* bfInfo = nullptr;   // [nbf] type | group << 2
   const double* bfLp23 = nullptr;    // [nbf] L^(2/3) (inlet-Q faces)

@@ -271,7 +271,8 @@ class SWE2D:
 
     def autotune(self, reps=3):
         """hg_autotune: time the FP32C stage kernels on the resident state and
-        keep the fastest; returns the choice (0 gather, 1 pipe, 2 tma)."""
+        keep the fastest; returns the choice (0 gather, 1 pipe, 2 tma).
+        reps=0 only reports the current choice."""
         k = np.zeros(1, np.int32)
         self._chk(lib().hg_autotune(self.h, int(reps), _i(k)))
         return int(k[0])

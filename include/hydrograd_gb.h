@@ -295,7 +295,7 @@ int hg_final_loss_and_grad(hg_ctx* ctx, const double* Q0, int32_t nsteps, double
  * resident state, reps times, and the fastest is kept.  All compute the same
  * results.  The first RK2 steps of a context run it once by themselves;
  * HG_STAGE_KERNEL=gather|pipe|tma in the environment forces a kernel.
- * kernel (may be NULL) receives the choice. */
+ * kernel (may be NULL) receives the choice; reps = 0 only reports it. */
 int hg_autotune(hg_ctx* ctx, int32_t reps, int32_t* kernel);
 
 /* ---- measurement support ---------------------------------------------------- */
