@@ -229,6 +229,72 @@ def run_reference(args):
     }))
 
 
+def run_config5(args, device):
+    """Configuration 5 (hydrograd_gb.workloads.meander_mixed): 4.0 M mixed
+    cells, a meandering channel, per-cell n, the inlet hydrograph 200 -> 2,000
+    m^3/s over 3,600 s.  FP32C forward over config5_steps CFL-0.4 steps (L2
+    flushed before each); FP32C vs FP64 over config5_err_steps steps; the FP32C
+    checkpointed forward+adjoint w.r.t. the per-cell n over config5_steps fixed
+    steps, and its gradient against the FP64 adjoint's over config5_err_steps."""
+    from hydrograd_gb import SWE2D
+    from hydrograd_gb.workloads import Stream, meander_mixed
+    t0 = time.perf_counter()
+    case = meander_mixed()
+    N = len(case["cell_node_count"])
+
+    def ctx_for(prec):
+        c = SWE2D(case, precision=prec, device=device)
+        c.set_still_water(case["wstill"])
+        c.set_manning_cells(case["manning_cells"])
+        c.set_inlet_q(case["inlet_q"])
+        c.set_exit_wse(case["exit_wse"])
+        c.set_inlet_hydrograph(0, *case["hydrograph"])
+        return c
+    c32 = ctx_for("fp32c")
+    setup_s = time.perf_counter() - t0
+    Q0 = case["Q0"]
+    c32.upload(Q0)
+    c32.advance_timed(args.warmup, cfl=0.4, flush_l2=True)
+    c32.upload(Q0)
+    ms = c32.advance_timed(args.config5_steps, cfl=0.4, flush_l2=True)
+    sim = c32.elapsed_time()
+    out = {"cells": N, "quads": int((case["cell_node_count"] == 4).sum()),
+           "triangles": int((case["cell_node_count"] == 3).sum()), "setup_seconds": setup_s,
+           "fwd": {"value": N * args.config5_steps / (ms * 1e-3), "steps": args.config5_steps,
+                   "ms_per_step": ms / args.config5_steps, "simulated_seconds": sim,
+                   "inlet_q_at_end": float(np.interp(sim, *case["hydrograph"]))}}
+    c64 = ctx_for("fp64")
+    k = args.config5_err_steps
+    a, _ = c64.integrate(Q0, k, cfl=0.4)
+    b, _ = c32.integrate(Q0, k, cfl=0.4)
+    out["error_fp32c_vs_fp64"] = {"steps": k, "state_rel_linf": float(max(
+        np.abs(b[j * N:(j + 1) * N] - a[j * N:(j + 1) * N]).max() / np.abs(a).max() for j in range(3)))}
+    # forward+adjoint w.r.t. the per-cell n: 64 probes in the wet cells, loss =
+    # mean squared departure of their depths from the lake at rest
+    dt = 0.5 * c64.integrate(Q0, 1, cfl=0.4)[1][0]
+    rs = Stream(11)
+    probes = np.unique((rs.uniform(256) * N).astype(np.int64))[:64].astype(np.int32)
+    h_rest = case["wstill"] - case["zb_cells"]
+    obs = np.tile(h_rest[probes], (args.config5_steps, 1))
+    c32.loss_and_grad(Q0, 4, dt, probes, obs[:4], ckpt_every=2)   # allocation
+    t0 = time.perf_counter()
+    r = c32.loss_and_grad(Q0, args.config5_steps, dt, probes, obs, ckpt_every=50, want=("manning",))
+    el = time.perf_counter() - t0
+    out["fwd_adjoint"] = {"value": N * args.config5_steps / el, "steps": args.config5_steps, "seconds": el,
+                          "checkpoint_every": 50, "probes": int(len(probes)), "gradient": "per-cell Manning n"}
+    ra = c64.loss_and_grad(Q0, k, dt, probes, obs[:k], ckpt_every=50, want=("manning",))
+    rb = c32.loss_and_grad(Q0, k, dt, probes, obs[:k], ckpt_every=50, want=("manning",))
+    out["fwd_adjoint"]["error_fp32c_vs_fp64"] = {
+        "steps": k, "grad_n_field_rel_linf": float(np.abs(rb["g_manning"] - ra["g_manning"]).max()
+                                                   / np.abs(ra["g_manning"]).max()),
+        "loss_rel": float(abs(rb["loss"] - ra["loss"]) / abs(ra["loss"]))}
+    out["config"] = ("configuration 5: %d cells (%d quads in a core, %d jittered triangles in a band) over a "
+                     "10 km reach, meandering channel 4 m deep, per-cell n U[0.02, 0.08] smoothed by a 100 m "
+                     "Gaussian, inlet hydrograph 200 -> 2,000 m3/s over 3,600 s, FP32C, CFL 0.4"
+                     % (N, out["quads"], out["triangles"]))
+    return out
+
+
 # Configuration 4: reach meshes of about these many cells, 32 members each.
 ENSEMBLE_SIZES = (5000, 10000, 20000, 40000, 60000, 100000, 150000, 200000)
 
@@ -386,6 +452,7 @@ def run_ours(args):
         adj["config"] = (f"{args.adj_steps} fixed-dt steps (dt = half the initial CFL step), checkpoints every 50, "
                          f"{len(probes)} probes (half on the pool rim, half at the inlet), loss = mean squared "
                          "departure of the probe depths from the lake at rest")
+    cfg5 = run_config5(args, local) if args.config5_steps > 0 else None
     ens = None
     if args.ens_steps > 0:
         ens = run_ensemble(args, local)
@@ -433,6 +500,7 @@ def run_ours(args):
         "fp32c_over_fp64_speedup": f32["value"] / out["fp64"]["value"],
         "fwd_adjoint": adj,
         "ensemble": ens,
+        "config5": cfg5,
         "warm_value": f32["warm_value"], "simulated_seconds": f32["sim_time"],
         "error": err,
         "roofline": roof,
@@ -462,6 +530,10 @@ def main():
     ap.add_argument("--ens-adj-steps", type=int, default=200, help="ensemble forward+adjoint steps (0: skip)")
     ap.add_argument("--ens-ckpt", type=int, default=25)
     ap.add_argument("--ens-members", type=int, default=32, help="members per mesh")
+    ap.add_argument("--config5-steps", type=int, default=5000,
+                    help="configuration 5 (4 M mixed cells, hydrograph) forward and forward+adjoint steps (0: skip)")
+    ap.add_argument("--config5-err-steps", type=int, default=200,
+                    help="configuration 5 steps of the FP32C-vs-FP64 state and gradient comparison")
     ap.add_argument("--profile-stage", default=None, choices=["fp32c", "fp64"],
                     help="only run the stage kernel a few times (a small case for ncu captures)")
     ap.add_argument("--profile-adjoint", default=None, choices=["fp32c", "fp64"],

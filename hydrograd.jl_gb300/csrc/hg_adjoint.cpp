@@ -348,6 +348,10 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
   const DevMesh& dm = c->dm;
   const DevScalars& ds = c->ds;
   const int extraPerStep = 2 * dm.nInlet;
+  // Inlet hydrographs at a stage's time (the run starts at t = 0): stage 1 of
+  // step s at s dt, stage 2 at (s + 1) dt -- in the forward pass, the
+  // recomputation and the VJP of that stage alike.
+  auto hydro = [&](double t) { c->launches += launch_hydrograph(dm, ds, kHydroAt, t, st); };
 
   if (f64) {
     launch_gather_state_f64(N, c->d_perm, c->Quser, c->QA, st);
@@ -356,8 +360,10 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
       if (s % C == 0)
         ADJ_CUDA(c, cudaMemcpyAsync(b->ckpt + (size_t)(s / C) * n3, c->QA, n3 * sizeof(double),
                                     cudaMemcpyDeviceToDevice, st));
+      hydro(s * dt);
       launch_inlet_total_f64(dm, ds, c->QA, st);
       launch_stage_f64(dm, ds, kModeStage1, c->QA, nullptr, c->QB, false, st);
+      hydro((s + 1) * dt);
       launch_inlet_total_f64(dm, ds, c->QB, st);
       launch_stage_f64(dm, ds, kModeStage2, c->QB, c->QA, c->QA, false, st);
       launch_probe_loss_f64(dm, a, c->QA, b->probes, b->obs + (size_t)s * P, P, st);
@@ -382,8 +388,10 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
                                   st));
       for (int s = s0; s < s1; ++s) {
         const size_t i = (size_t)(s - s0);
+        hydro(s * dt);
         launch_inlet_total_f64(dm, ds, Q0s + i * n3, st);
         launch_stage_f64(dm, ds, kModeStage1, Q0s + i * n3, nullptr, Q1s + i * n3, false, st);
+        hydro((s + 1) * dt);
         launch_inlet_total_f64(dm, ds, Q1s + i * n3, st);
         launch_stage_f64(dm, ds, kModeStage2, Q1s + i * n3, Q0s + i * n3, Q0s + (i + 1) * n3, false, st);
         c->launches += 2 + extraPerStep;
@@ -392,9 +400,11 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
         const size_t i = (size_t)(s - s0);
         const double* q0 = Q0s + i * n3;
         const double* q1 = Q1s + i * n3;
+        hydro((s + 1) * dt);
         launch_inlet_total_f64(dm, ds, q1, st);
         launch_vjp_f64(dm, a, q1, b->mu2, nullptr, b->mu1, 0.5, 0.0, 0.5 * dt, st);
         launch_inlet_adjoint_f64(dm, a, q1, b->mu1, 0.5 * dt, st);
+        hydro(s * dt);
         launch_inlet_total_f64(dm, ds, q0, st);
         launch_vjp_f64(dm, a, q0, b->mu1, b->mu2, b->mu2, 1.0, 0.5, dt, st);
         launch_inlet_adjoint_f64(dm, a, q0, b->mu2, dt, st);
@@ -433,7 +443,7 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
     };
     // One SSP-RK2 step q0 -> (q1) -> q2 at the fixed dt, with the totals t0 of q0
     // on entry and those of q1 and q2 on exit.
-    auto step = [&](StateF32 q0, StateF32 q1, StateF32 q2, double* t0, double* t1, double* t2) {
+    auto step = [&](int s, StateF32 q0, StateF32 q1, StateF32 q2, double* t0, double* t1, double* t2) {
       if (fz) {
         StageFuse f;
         f.partials = c->d_partials;
@@ -442,17 +452,21 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
         f.nSlots = c->nSlots;
         f.totalIn = t0;
         f.totalOut = t1;
+        hydro(s * dt);
         launch_stage_f32_fused(dm, ds, kModeStage1, q0, StateF32{}, q1, f, st);
         f.totalIn = t1;
         f.totalOut = t2;
+        hydro((s + 1) * dt);
         launch_stage_f32_fused(dm, ds, kModeStage2, q1, q0, q2, f, st);
         c->launches += 2;
       } else {
         DevMesh mm = dm;
         mm.totalA = t0;
+        hydro(s * dt);
         launch_stage_f32(mm, ds, kModeStage1, q0, StateF32{}, q1, nullptr, false, st);
         totals(q1, t1);
         mm.totalA = t1;
+        hydro((s + 1) * dt);
         launch_stage_f32(mm, ds, kModeStage2, q1, q0, q2, nullptr, false, st);
         totals(q2, t2);
         c->launches += 2;
@@ -468,7 +482,7 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
     totals(XA, T0);
     for (int s = 0; s < K; ++s) {
       if (s % C == 0) ADJ_CUDA(c, copy_state(ck.at(s / C, n), XA));
-      step(XA, XB, XA, T0, T0 + stride, T0);
+      step(s, XA, XB, XA, T0, T0 + stride, T0);
       launch_probe_loss_f32(dm, a, XA, b->probes, b->obs + (size_t)s * P, P, st);
       c->launches += P > 0 ? 1 : 0;
     }
@@ -488,7 +502,7 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
       totals(sg.at(0, n), T0);
       for (int s = s0; s < s1; ++s) {
         const size_t i = (size_t)(s - s0);
-        step(sg.at(i, n), sg.at(C + 1 + i, n), sg.at(i + 1, n), T0 + i * stride, T1 + i * stride,
+        step(s, sg.at(i, n), sg.at(C + 1 + i, n), sg.at(i + 1, n), T0 + i * stride, T1 + i * stride,
              T0 + (i + 1) * stride);
       }
       for (int s = s1 - 1; s >= s0; --s) {
@@ -497,8 +511,10 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
         DevMesh m1 = dm, m0 = dm;
         m1.totalA = T1 + i * stride;
         m0.totalA = T0 + i * stride;
+        hydro((s + 1) * dt);
         c->launches += launch_vjp_f32(m1, a, q1, mu2, nullptr, mu1, 0.5f, 0.0f, 0.5 * dt, st, b->side, b->evFork,
                                       b->evJoin);
+        hydro(s * dt);
         c->launches += launch_vjp_f32(m0, a, q0, mu1, mu2, mu2, 1.0f, 0.5f, dt, st, b->side, b->evFork, b->evJoin);
         if (s >= 1 && P > 0) {
           launch_probe_adjoint_f32(dm, q0, mu2, pc, b->obs + (size_t)(s - 1) * P, scale, st);

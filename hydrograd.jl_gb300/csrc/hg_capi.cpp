@@ -213,13 +213,16 @@ void enqueue_rk2_step_fused(hg_ctx* c, bool cflMode, double cfl) {
   f.record = 1;
   f.totalIn = c->d_tot;
   f.totalOut = c->d_tot + kMaxFusedInlets;
+  // inlet hydrographs: t_n before stage 1, t_n + dt (recorded by stage 1) before stage 2
+  const int hyd = launch_hydrograph(c->dm, c->ds, kHydroNow, 0.0, c->stream);
   launch_stage_f32_fused(c->dm, c->ds, kModeStage1, xa(c), StateF32{}, xb(c), f, c->stream);
   f.record = 0;
   f.totalIn = c->d_tot + kMaxFusedInlets;
   f.totalOut = c->d_tot;
+  launch_hydrograph(c->dm, c->ds, kHydroNow, 0.0, c->stream);
   launch_stage_f32_fused(c->dm, c->ds, kModeStage2, xb(c), xa(c), xa(c), f, c->stream);
   c->parity ^= 1;
-  c->launches += 2;
+  c->launches += 2 + 2 * hyd;
 }
 
 // One SSP-RK2 step on the resident state (QA / XA).  Unfused kernels per step:
@@ -230,22 +233,27 @@ void enqueue_rk2_step(hg_ctx* c, bool cflMode, double cfl) {
     return;
   }
   launch_step_begin(c->ds, cflMode, cfl, c->stream);
+  // inlet hydrographs at each stage's time: t_n, then t_n + dt
+  const int hyd = launch_hydrograph(c->dm, c->ds, kHydroStepStart, 0.0, c->stream);
   if (c->precision == HG_FP64) {
     launch_inlet_total_f64(c->dm, c->ds, c->QA, c->stream);
     launch_stage_f64(c->dm, c->ds, kModeStage1, c->QA, nullptr, c->QB, false, c->stream);
+    launch_hydrograph(c->dm, c->ds, kHydroStepEnd, 0.0, c->stream);
     launch_inlet_total_f64(c->dm, c->ds, c->QB, c->stream);
     launch_stage_f64(c->dm, c->ds, kModeStage2, c->QB, c->QA, c->QA, cflMode, c->stream);
   } else {
     launch_inlet_total_f32(c->dm, c->ds, xa(c), c->stream);
     launch_stage_f32(c->dm, c->ds, kModeStage1, xa(c), StateF32{}, xb(c), nullptr, false, c->stream);
+    launch_hydrograph(c->dm, c->ds, kHydroStepEnd, 0.0, c->stream);
     launch_inlet_total_f32(c->dm, c->ds, xb(c), c->stream);
     launch_stage_f32(c->dm, c->ds, kModeStage2, xb(c), xa(c), xa(c), nullptr, cflMode, c->stream);
   }
-  c->launches += 3 + 2 * rhs_prep_launches(c);
+  c->launches += 3 + 2 * rhs_prep_launches(c) + 2 * hyd;
 }
 
 void enqueue_euler_step(hg_ctx* c, bool cflMode, double cfl) {
   launch_step_begin(c->ds, cflMode, cfl, c->stream);
+  c->launches += launch_hydrograph(c->dm, c->ds, kHydroStepStart, 0.0, c->stream);
   if (c->precision == HG_FP64) {
     launch_inlet_total_f64(c->dm, c->ds, c->QA, c->stream);
     launch_stage_f64(c->dm, c->ds, kModeEulerRef, c->QA, nullptr, c->QB, false, c->stream);
@@ -646,6 +654,47 @@ int hg_set_exit_wse(hg_ctx* ctx, const double* w, int32_t n) {
   return upload_boundary_values(ctx);
 }
 
+int hg_set_inlet_hydrograph(hg_ctx* ctx, int32_t group, int32_t n, const double* t, const double* q) {
+  if (!ctx) return fail(ctx, HG_ERR_ARG, "hg_set_inlet_hydrograph: null context");
+  const int ng = ctx->dm.nInlet;
+  if (group < 0 || group >= ng || n < 0 || (n > 0 && (!t || !q)))
+    return fail(ctx, HG_ERR_ARG, "hg_set_inlet_hydrograph: bad group or points");
+  for (int i = 0; i < n; ++i)
+    if (!std::isfinite(t[i]) || !std::isfinite(q[i]) || (i > 0 && !(t[i] > t[i - 1])))
+      return fail(ctx, HG_ERR_ARG, "hg_set_inlet_hydrograph: times must increase, values be finite");
+  cudaSetDevice(ctx->device);
+  ctx->hydro.resize(ng);
+  ctx->hydro[group].assign(t, t + n);
+  ctx->hydro[group].insert(ctx->hydro[group].end(), q, q + n);
+  std::vector<int32_t> off(ng + 1, 0);
+  std::vector<double> tt, qq;
+  for (int g = 0; g < ng; ++g) {
+    const std::vector<double>& h = ctx->hydro[g];
+    const size_t k = h.size() / 2;
+    tt.insert(tt.end(), h.begin(), h.begin() + k);
+    qq.insert(qq.end(), h.begin() + k, h.end());
+    off[g + 1] = (int32_t)tt.size();
+  }
+  ctx->dm.nHydro = (int32_t)tt.size();
+  if (!tt.empty()) {
+    if (tt.size() > ctx->hydroCap) {
+      HG_CUDA(ctx, dalloc(ctx, &ctx->d_hydroT, tt.size()));
+      HG_CUDA(ctx, dalloc(ctx, &ctx->d_hydroQ, tt.size()));
+      ctx->hydroCap = tt.size();
+    }
+    if (!ctx->d_hydroOff) HG_CUDA(ctx, dalloc(ctx, &ctx->d_hydroOff, (size_t)ng + 1));
+    HG_CUDA(ctx, upload(ctx, ctx->d_hydroOff, off));
+    HG_CUDA(ctx, upload(ctx, ctx->d_hydroT, tt));
+    HG_CUDA(ctx, upload(ctx, ctx->d_hydroQ, qq));
+    HG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    ctx->dm.hydroOff = ctx->d_hydroOff;
+    ctx->dm.hydroT = ctx->d_hydroT;
+    ctx->dm.hydroQ = ctx->d_hydroQ;
+  }
+  ctx->graphValid = false;
+  return upload_boundary_values(ctx);   // groups without a hydrograph: back to their constant discharge
+}
+
 int hg_set_manning_function(hg_ctx* ctx, int32_t kind, const double* params, int32_t n_params, const double* ks) {
   if (!ctx) return fail(ctx, HG_ERR_ARG, "hg_set_manning_function: null context");
   cudaSetDevice(ctx->device);
@@ -766,10 +815,11 @@ int hg_check_initial_state(hg_ctx* ctx, const double* Q) {
   return HG_OK;
 }
 
-int hg_rhs(hg_ctx* ctx, const double* Q, double /*t*/, double* dQ) {
+int hg_rhs(hg_ctx* ctx, const double* Q, double t, double* dQ) {
   if (!ctx || !Q || !dQ) return fail(ctx, HG_ERR_ARG, "hg_rhs: null argument");
   cudaSetDevice(ctx->device);
   launch_reset_scalars(ctx->ds, ctx->stream);
+  ctx->launches += launch_hydrograph(ctx->dm, ctx->ds, kHydroAt, t, ctx->stream);
   int rc = enqueue_upload(ctx, Q);
   if (rc) return rc;
   if (ctx->precision == HG_FP64) {

@@ -74,6 +74,12 @@ struct hg_ctx {
   double *d_resKs = nullptr, *d_resW = nullptr, *d_resStats = nullptr, *d_resPartials = nullptr, *d_fres = nullptr;
   float *d_resWf = nullptr, *d_fresF = nullptr;
   unsigned int* d_resTicket = nullptr;
+  // Inlet-Q hydrographs (hg_set_inlet_hydrograph): per group its times then
+  // its discharges; device copies (dm.hydro*), capacity in points.
+  std::vector<std::vector<double>> hydro;
+  int32_t* d_hydroOff = nullptr;
+  double *d_hydroT = nullptr, *d_hydroQ = nullptr;
+  size_t hydroCap = 0;
   std::string err;
   ~hg_ctx();
 };

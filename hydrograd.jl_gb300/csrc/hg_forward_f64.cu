@@ -224,6 +224,37 @@ __global__ void __launch_bounds__(kBlock) k_inlet_total_f64(DevMesh m, DevScalar
 
 }  // namespace
 
+namespace {
+// Hydrographs: one thread per inlet-Q group (see DevMesh::hydroOff).
+__global__ void k_hydrograph(DevMesh m, DevScalars s, int when, double t) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= m.nInlet) return;
+  const int a = m.hydroOff[g], b = m.hydroOff[g + 1];
+  if (b <= a) return;   // constant discharge
+  if (when == kHydroStepStart) t = *s.tSum - *s.dt;
+  else if (when == kHydroStepEnd || when == kHydroNow) t = *s.tSum;
+  double q;
+  if (t <= m.hydroT[a]) {
+    q = m.hydroQ[a];
+  } else if (t >= m.hydroT[b - 1]) {
+    q = m.hydroQ[b - 1];
+  } else {
+    int k = a;
+    while (k + 1 < b - 1 && m.hydroT[k + 1] <= t) ++k;   // bounded by the group's points
+    const double w = (t - m.hydroT[k]) / (m.hydroT[k + 1] - m.hydroT[k]);
+    q = m.hydroQ[k] + w * (m.hydroQ[k + 1] - m.hydroQ[k]);
+  }
+  const_cast<double*>(m.inletQ)[g] = q;
+}
+
+}  // namespace
+
+int launch_hydrograph(const DevMesh& m, const DevScalars& s, int when, double t, cudaStream_t st) {
+  if (m.nHydro == 0 || m.nInlet == 0) return 0;
+  k_hydrograph<<<(m.nInlet + 31) / 32, 32, 0, st>>>(m, s, when, t);
+  return 1;
+}
+
 void launch_inlet_total_f64(const DevMesh& m, const DevScalars& s, const double* Q, cudaStream_t st) {
   launch_resistance_f64(m, Q, st);
   if (m.nInlet > 0) k_inlet_total_f64<<<m.nInlet, kBlock, 0, st>>>(m, s, Q);

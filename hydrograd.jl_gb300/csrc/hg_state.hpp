@@ -94,6 +94,22 @@ struct DevMesh {
   double* totalA = nullptr;          // [nInlet] conveyance of the current stage input
   double g = 9.81, kn2 = 1.0, hsm = 1e-3;
   ResDev res;
+  // Inlet-Q hydrographs (hg_set_inlet_hydrograph): for each inlet-Q group g
+  // with points, Q(t) interpolates (hydroT, hydroQ)[hydroOff[g] ..
+  // hydroOff[g+1]) linearly (held at the end values outside them) and is
+  // written into inletQ before each RHS evaluation (launch_hydrograph).
+  int32_t nHydro = 0;                // points of all groups (0: constant discharges)
+  const int32_t* hydroOff = nullptr; // [nInlet + 1]
+  const double* hydroT = nullptr;
+  const double* hydroQ = nullptr;
+};
+
+// Times at which launch_hydrograph evaluates the hydrographs.
+enum HydroTime : int32_t {
+  kHydroAt = 0,          // the time passed in
+  kHydroStepStart = 1,   // the step begun by k_step_begin: elapsed time - dt
+  kHydroStepEnd = 2,     // the elapsed time (stage 2 of SSP-RK2)
+  kHydroNow = 3          // the elapsed time (fused stepping: before stage 1, t_n; before stage 2, t_n + dt)
 };
 
 // Scalars that live on the device so that steps can be captured in a graph.
@@ -151,6 +167,9 @@ void launch_inlet_total_f32(const DevMesh& m, const DevScalars& s, StateF32 X, c
 // launch_inlet_total_f64 / _f32 call these first, so every RHS evaluation sees
 // the resistance of its own input state.
 int launch_resistance_f64(const DevMesh& m, const double* Q, cudaStream_t st);
+// inletQ[g] = Q_g(t) for every inlet-Q group with a hydrograph (a no-op
+// without one); the number of launches it made.
+int launch_hydrograph(const DevMesh& m, const DevScalars& s, int when, double t, cudaStream_t st);
 int launch_resistance_f32(const DevMesh& m, StateF32 X, cudaStream_t st);
 int resistance_launches(const DevMesh& m);
 void launch_stage_f32(const DevMesh& m, const DevScalars& s, int mode, StateF32 Xin, StateF32 Xbase, StateF32 Xout,

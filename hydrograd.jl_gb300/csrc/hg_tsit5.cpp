@@ -130,7 +130,8 @@ int hg_integrate_tsit5(hg_ctx* ctx, double* Q, double t0, double t1, double abst
   launch_gather_state_f64(n, ctx->d_perm, ctx->Quser, U, st);
   ctx->launches += 1;
   const StateF32 xs{ctx->XB, ctx->XQB};
-  auto rhs = [&](const double* X, double* out) {
+  auto rhs = [&](const double* X, double* out, double tx) {
+    ctx->launches += launch_hydrograph(ctx->dm, ctx->ds, kHydroAt, tx, st);   // inlet discharges at tx
     if (ctx->precision == HG_FP64) {
       launch_inlet_total_f64(ctx->dm, ctx->ds, X, st);
       launch_stage_f64(ctx->dm, ctx->ds, kModeRhs, X, nullptr, out, false, st);
@@ -159,7 +160,7 @@ int hg_integrate_tsit5(hg_ctx* ctx, double* Q, double t0, double t1, double abst
     t.nk = 1;
     return t;
   };
-  rhs(U, K[0]);
+  rhs(U, K[0], t0);
   double dt = dt0;
   if (adaptive && !(dt > 0)) {   // Hairer, Norsett & Wanner II.4: starting step size
     double d0, d1, d2;
@@ -168,7 +169,7 @@ int hg_integrate_tsit5(hg_ctx* ctx, double* Q, double t0, double t1, double abst
     if (rc) return rc;
     const double h0 = (d0 < 1e-5 || d1 < 1e-5) ? 1e-6 : 0.01 * d0 / d1;
     launch_tsit5_combine(len, U, one(K[0], 1.0), h0, Y, st);
-    rhs(Y, K[1]);
+    rhs(Y, K[1], t0 + h0);
     Tsit5Terms dk{};
     dk.K[0] = K[1];
     dk.K[1] = K[0];
@@ -206,7 +207,7 @@ int hg_integrate_tsit5(hg_ctx* ctx, double* Q, double t0, double t1, double abst
       terms.nk = i;
       double* dst = (i == kTsit5Stages - 1) ? Unew : Y;
       launch_tsit5_combine(len, U, terms, h, dst, st);
-      rhs(dst, K[i]);
+      rhs(dst, K[i], t + tb.c[i] * h);
       ctx->launches += 1;
     }
     evals += kTsit5Stages - 1;

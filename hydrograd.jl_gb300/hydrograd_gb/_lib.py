@@ -74,6 +74,7 @@ SIGNATURES = {
     "hg_set_manning_zones": [_vp, _ip, ctypes.c_int32, _dp],
     "hg_set_manning_cells": [_vp, _dp],
     "hg_set_zb_cells": [_vp, _dp],
+    "hg_set_inlet_hydrograph": [_vp, ctypes.c_int32, ctypes.c_int32, _dp, _dp],
     "hg_set_manning_function": [_vp, ctypes.c_int32, _dp, ctypes.c_int32, _dp],
     "hg_set_ude": [_vp, ctypes.POINTER(HgUdeDesc)],
     "hg_set_inlet_q": [_vp, _dp, ctypes.c_int32],

@@ -142,6 +142,16 @@ class SWE2D:
     def set_zb_cells(self, zb):
         self._chk(lib().hg_set_zb_cells(self.h, _d(np.ascontiguousarray(zb, dtype=np.float64))))
 
+    def set_inlet_hydrograph(self, group, t, q):
+        """Time-varying discharge of inlet-Q boundary `group` (hg_set_inlet_hydrograph);
+        empty t returns it to its set_inlet_q value."""
+        t = np.ascontiguousarray(t, dtype=np.float64)
+        q = np.ascontiguousarray(q, dtype=np.float64)
+        self._hydro = getattr(self, "_hydro", {})
+        self._hydro[group] = (t, q)
+        self._chk(lib().hg_set_inlet_hydrograph(self.h, int(group), len(t), _d(t) if len(t) else None,
+                                                _d(q) if len(q) else None))
+
     def set_manning_function(self, kind, params=(), ks=None):
         """Manning's n as a function of the state (ManningN_option "variable",
         process_ManningN_2D.jl:102-213): kind "power_law" / "sigmoid" / "inverse"

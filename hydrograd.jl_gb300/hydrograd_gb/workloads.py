@@ -11,6 +11,12 @@ harness (tests, benchmark, oracle) sees the same inputs for the same seed.
   5 Voronoi Manning zones; inlet-Q on the west edge, exit-H on the east edge,
   walls elsewhere; a lake at rest with its surface raised 1.5 m in a pool disk
   (dry_land=True: dry except the pool).
+* :func:`meander_mixed`  configuration 5: a 10 km reach on a mixed mesh -- a
+  core of n_core^2 quads inside a band of jittered triangles (1,600^2 quads +
+  1.45 M triangles = 4.0 M cells by default) -- with a meandering channel
+  carved 4 m deep into a floodplain of Gaussian bumps, a per-cell Manning n
+  field U[0.02, 0.08] smoothed by a 100 m Gaussian, and an inlet hydrograph
+  ramping from 200 to 2,000 m^3/s over 3,600 s.
 
 A case is a dict with the mesh arrays of ``hg_mesh_desc`` plus parameters:
 mat_id, manning_zones, inlet_q, exit_wse, wstill (per cell) and Q0.
@@ -256,3 +262,115 @@ def probes_and_perturbation(case, n_probe=64, seed=1, zb_sigma=0.05, rim_width=N
     u2 = rs.uniform(N)
     dz = (zb_sigma * np.sqrt(-2.0 * np.log(u1)) * np.cos(2 * np.pi * u2)).astype(np.float32)
     return probes, dz.astype(np.float64)
+
+
+def _gaussian_smooth(field, sigma_cells):
+    """Separable Gaussian filter (truncated at 4 sigma, reflecting edges) of a 2D array."""
+    r = int(np.ceil(4.0 * sigma_cells))
+    x = np.arange(-r, r + 1, dtype=np.float64)
+    k = np.exp(-0.5 * (x / sigma_cells) ** 2)
+    k /= k.sum()
+    out = field
+    for axis in (0, 1):
+        pad = [(0, 0), (0, 0)]
+        pad[axis] = (r, r)
+        p = np.pad(out, pad, mode="reflect")
+        acc = np.zeros_like(out)
+        for i, w in enumerate(k):
+            sl = [slice(None), slice(None)]
+            sl[axis] = slice(i, i + out.shape[axis])
+            acc += w * p[tuple(sl)]
+        out = acc
+    return out
+
+
+def meander_mixed(n_core=1600, n_band=106, L=10000.0, seed=7, jitter=0.2, n_bumps=40, depth=4.0,
+                  half_width=100.0, q_start=200.0, q_end=2000.0, ramp=3600.0, n_sigma=100.0):
+    """Configuration 5.  An (n_core + 2 n_band)^2 grid over L x L: the inner
+    n_core^2 squares are quads, the others each split into two triangles; the
+    band's interior nodes are jittered by +-jitter dx.  Bed: a 2e-4 slope
+    falling to the east, n_bumps Gaussian bumps (A in U[0.2, 1.5] m, sigma in
+    U[100, 500] m), and a channel of half-width half_width carved depth m deep
+    (cosine profile) along the centreline y = L/2 + a sin(2 pi x / lambda),
+    a in U[200, 600] m, lambda in U[1500, 3000] m.  Manning n per cell: U[0.02,
+    0.08] per grid square, Gaussian-smoothed (sigma n_sigma m).  Inlet-Q on the
+    west edge with the hydrograph (0, q_start), (ramp, q_end); exit-H on the
+    east edge at the lake level; walls elsewhere.  Initial state: a lake at
+    rest 0.3 m above the highest bed cell (every cell wet)."""
+    rs = Stream(seed)
+    nc = n_core + 2 * n_band
+    dx = L / nc
+    X, Y = _grid_nodes(nc, nc, L, L)
+    nn = X.size
+    ii = np.tile(np.arange(nc + 1), nc + 1)
+    jj = np.repeat(np.arange(nc + 1), nc + 1)
+    core_node = (ii >= n_band) & (ii <= n_band + n_core) & (jj >= n_band) & (jj <= n_band + n_core)
+    inner = (ii > 0) & (ii < nc) & (jj > 0) & (jj < nc)
+    jmask = inner & ~core_node
+    jx = rs.uniform(nn, -jitter, jitter) * dx
+    jy = rs.uniform(nn, -jitter, jitter) * dx
+    X = X + np.where(jmask, jx, 0.0)
+    Y = Y + np.where(jmask, jy, 0.0)
+    A = rs.uniform(n_bumps, 0.2, 1.5)
+    S = rs.uniform(n_bumps, 100.0, 500.0)
+    BX = rs.uniform(n_bumps, 0.0, L)
+    BY = rs.uniform(n_bumps, 0.0, L)
+    amp = rs.uniform(1, 200.0, 600.0)[0]
+    lam = rs.uniform(1, 1500.0, 3000.0)[0]
+    Z = 2e-4 * (L - X)
+    for k in range(n_bumps):
+        Z = Z + A[k] * np.exp(-((X - BX[k]) ** 2 + (Y - BY[k]) ** 2) / (2 * S[k] ** 2))
+    d = np.abs(Y - (0.5 * L + amp * np.sin(2 * np.pi * X / lam)))
+    Z = Z - np.where(d < half_width, depth * 0.5 * (1.0 + np.cos(np.pi * d / half_width)), 0.0)
+    xyz = np.stack([X, Y, Z], axis=1)
+    i, j = np.meshgrid(np.arange(nc), np.arange(nc), indexing="xy")
+    i, j = i.ravel(), j.ravel()
+    quad = (i >= n_band) & (i < n_band + n_core) & (j >= n_band) & (j < n_band + n_core)
+    n00, n10, n11, n01 = _nid(i, j, nc), _nid(i + 1, j, nc), _nid(i + 1, j + 1, nc), _nid(i, j + 1, nc)
+    nq = int(quad.sum())
+    nt = 2 * int((~quad).sum())
+    N = nq + nt
+    cells = np.full((N, 8), -1, dtype=np.int32)
+    cnt = np.empty(N, np.int32)
+    sq = np.empty(N, np.int64)   # grid square of each cell (for the n field)
+    # cells in grid-square order: a quad, or the square's two triangles
+    per = np.where(quad, 1, 2)
+    start = np.concatenate([[0], np.cumsum(per)[:-1]])
+    q_idx = start[quad]
+    cells[q_idx, 0], cells[q_idx, 1], cells[q_idx, 2], cells[q_idx, 3] = n00[quad], n10[quad], n11[quad], n01[quad]
+    cnt[q_idx] = 4
+    sq[q_idx] = np.nonzero(quad)[0]
+    t_idx = start[~quad]
+    nb = ~quad
+    cells[t_idx, 0], cells[t_idx, 1], cells[t_idx, 2] = n00[nb], n10[nb], n11[nb]
+    cells[t_idx + 1, 0], cells[t_idx + 1, 1], cells[t_idx + 1, 2] = n00[nb], n11[nb], n01[nb]
+    cnt[t_idx] = 3
+    cnt[t_idx + 1] = 3
+    sq[t_idx] = np.nonzero(nb)[0]
+    sq[t_idx + 1] = np.nonzero(nb)[0]
+    west = [_nid(0, jj_, nc) for jj_ in range(nc, -1, -1)]
+    east = [_nid(nc, jj_, nc) for jj_ in range(0, nc + 1)]
+    ids, offs, snodes, bcs = _pack_strings([(1, 2, _string(west)), (2, 3, _string(east))])
+    case = dict(node_xyz=xyz, cell_nodes=cells, cell_node_count=cnt, string_ids=ids, string_offsets=offs,
+                string_nodes=snodes, string_bc=bcs)
+    # counter-clockwise check (triangles and quads: the first three nodes)
+    p, q, r = cells[:, 0], cells[:, 1], cells[:, 2]
+    area2 = (X[q] - X[p]) * (Y[r] - Y[p]) - (X[r] - X[p]) * (Y[q] - Y[p])
+    if not (area2 > 0).all():
+        raise RuntimeError("jittered mesh has an inverted cell; lower the jitter")
+    nf = rs.uniform(nc * nc, 0.02, 0.08).reshape(nc, nc)
+    n_cells = _gaussian_smooth(nf, n_sigma / dx).ravel()[sq]
+    zsum = Z[cells[:, 0]] + Z[cells[:, 1]]
+    zsum = zsum + Z[cells[:, 2]]
+    zsum = np.where(cnt == 4, zsum + Z[np.maximum(cells[:, 3], 0)], zsum)
+    zb = zsum / cnt
+    wstill = float(np.ceil((zb.max() + 0.3) * 10.0) / 10.0)
+    h = wstill - zb
+    xi = initial_xi(h, np.full(N, wstill), zb)
+    case.update(mat_id=np.zeros(N, np.int32), manning_zones=np.array([0.05]), manning_cells=n_cells,
+                inlet_q=np.array([q_start]), exit_wse=np.array([wstill]), wstill=np.full(N, wstill),
+                Q0=np.concatenate([xi, np.zeros(N), np.zeros(N)]), zb_cells=zb,
+                hydrograph=(np.array([0.0, ramp]), np.array([q_start, q_end])),
+                name=f"meander_mixed_{n_core}q_{n_band}b")
+    return case
+

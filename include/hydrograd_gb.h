@@ -176,6 +176,17 @@ int hg_set_manning_cells(hg_ctx* ctx, const double* n_cells);
 int hg_set_zb_cells(hg_ctx* ctx, const double* zb_cells);
 int hg_set_inlet_q(hg_ctx* ctx, const double* q, int32_t n_inletq);   /* inletQ_TotalQ */
 int hg_set_exit_wse(hg_ctx* ctx, const double* wse, int32_t n_exith); /* exitH_WSE */
+/* Inlet-Q hydrograph (no counterpart in the reference, whose inlet discharges
+ * are constant, bc_2D.jl:192): the discharge of inlet-Q boundary `group`
+ * follows the n points (t[i], q[i]), t increasing, linearly interpolated and
+ * held at the end values outside them, evaluated at the time of each RHS
+ * evaluation: t of hg_rhs; t_n and t_n + dt for the stages of an SSP-RK2 step
+ * (t = the simulated time since the last hg_state_upload or hg_integrate);
+ * the stage times of hg_integrate_tsit5; s dt and (s + 1) dt for step s of
+ * hg_loss_and_grad / hg_final_loss_and_grad, whose inlet-Q gradient is then
+ * the derivative w.r.t. a constant shift of the hydrograph.  n = 0 returns the
+ * group to its hg_set_inlet_q value. */
+int hg_set_inlet_hydrograph(hg_ctx* ctx, int32_t group, int32_t n, const double* t, const double* q);
 /* Read back derived data: zb_cells [n], S0 [2n] (x,y interleaved), ManningN_cells [n], hstill [n]. */
 int hg_get_bed(hg_ctx* ctx, double* zb_cells, double* S0, double* manning_cells, double* hstill);
 

@@ -586,9 +586,27 @@ inline void resistance_cells(const Resistance& r, const std::vector<double>& h, 
   mlp_forward(r.mlp, in, N, out);
 }
 
+// Inlet-Q hydrograph of one group: points (t, q), t increasing; Q(t) is the
+// linear interpolation, held at the end values outside the points.  The
+// reference's inlet discharges are constant (bc_2D.jl:192); this is the
+// time-varying inlet of the long-horizon workload, checked here as the device
+// evaluates it.
+inline double hydro_at(const std::vector<double>& tq, double t) {
+  const size_t n = tq.size() / 2;
+  const double* T = tq.data();
+  const double* Qv = tq.data() + n;
+  if (t <= T[0]) return Qv[0];
+  if (t >= T[n - 1]) return Qv[n - 1];
+  size_t k = 0;
+  while (k + 1 < n - 1 && T[k + 1] <= t) ++k;
+  const double w = (t - T[k]) / (T[k + 1] - T[k]);
+  return Qv[k] + w * (Qv[k + 1] - Qv[k]);
+}
+
 template <class T>
 struct Params {
   Resistance res;                // state-dependent n / UDE closure (kind RES_CONSTANT: manningCells)
+  std::vector<std::vector<double>> hydro;   // per inlet-Q group: times then discharges (empty: constant)
   std::vector<T> manningCells;   // ManningN_cells (process_ManningN_2D.jl:242-269 for zones)
   std::vector<T> zbCells;        // zb_cells (active parameter replaces it, semi_discretize_swe_2D.jl:114-126)
   std::vector<T> inletQ;         // inletQ_TotalQ per inlet-Q boundary (:190-199)
@@ -827,14 +845,28 @@ inline double cfl_dt(const Case& cs, const double* Q, double cfl) {
 }
 
 // One SSP-RK2 (Heun) step: Q1 = C(Q0 + dt R(Q0)); Q2 = C(0.5*(Q0 + (Q1 + dt R(Q1)))).
+// The parameters at time t: inlet discharges from their hydrographs, if any.
 template <class T>
-void rk2_step(const Case& cs, const Params<T>& p, std::vector<T>& Q, double dt, int nthreads = 1) {
+const Params<T>& params_at(const Params<T>& p, Params<T>& scratch, double t) {
+  bool any = false;
+  for (const auto& h : p.hydro) any = any || !h.empty();
+  if (!any) return p;
+  if (scratch.inletQ.size() != p.inletQ.size()) scratch = p;
+  for (size_t g = 0; g < p.hydro.size() && g < scratch.inletQ.size(); ++g)
+    if (!p.hydro[g].empty()) scratch.inletQ[g] = T(hydro_at(p.hydro[g], t));
+  return scratch;
+}
+
+// One SSP-RK2 step from time t (stage 1 at t, stage 2 at t + dt).
+template <class T>
+void rk2_step(const Case& cs, const Params<T>& p, std::vector<T>& Q, double dt, int nthreads = 1, double t = 0.0) {
   const size_t n3 = Q.size();
   std::vector<T> R(n3), Q1(n3);
-  rhs<T>(cs, p, Q.data(), R.data(), nthreads);
+  Params<T> scratch;
+  rhs<T>(cs, params_at(p, scratch, t), Q.data(), R.data(), nthreads);
   for (size_t k = 0; k < n3; ++k) Q1[k] = Q[k] + dt * R[k];
   clamp_stage<T>(cs, Q1.data());
-  rhs<T>(cs, p, Q1.data(), R.data(), nthreads);
+  rhs<T>(cs, params_at(p, scratch, t + dt), Q1.data(), R.data(), nthreads);
   for (size_t k = 0; k < n3; ++k) Q[k] = 0.5 * (Q[k] + (Q1[k] + dt * R[k]));
   clamp_stage<T>(cs, Q.data());
 }
@@ -865,7 +897,6 @@ inline bool tsit5(const Case& cs, const Params<double>& p, std::vector<double>& 
       {0.09646076681806523, 0.01, 0.4798896504144996, 1.379008574103742, -3.290069515436081, 2.324710524099774}};
   static const double BT[7] = {-0.00178001105222577714, -0.0008164344596567469, 0.007880878010261995,
                                -0.1447110071732629, 0.5823571654525552, -0.45808210592918697, 0.015151515151515152};
-  (void)C;
   const size_t n3 = Q.size();
   std::vector<std::vector<double>> K(7, std::vector<double>(n3));
   std::vector<double> Y(n3), Qn(n3);
@@ -877,14 +908,15 @@ inline bool tsit5(const Case& cs, const Params<double>& p, std::vector<double>& 
     }
     return std::sqrt(s / (double)n3);
   };
-  rhs<double>(cs, p, Q.data(), K[0].data(), nthreads);
+  Params<double> scratch;
+  rhs<double>(cs, params_at(p, scratch, t0), Q.data(), K[0].data(), nthreads);
   st.evals = 1;
   double dt = dt0;
   if (adaptive && !(dt > 0)) {
     const double d0 = norm(Q, Q, Q), d1 = norm(Q, Q, K[0]);
     const double h0 = (d0 < 1e-5 || d1 < 1e-5) ? 1e-6 : 0.01 * d0 / d1;
     for (size_t i = 0; i < n3; ++i) Y[i] = Q[i] + h0 * K[0][i];
-    rhs<double>(cs, p, Y.data(), K[1].data(), nthreads);
+    rhs<double>(cs, params_at(p, scratch, t0 + h0), Y.data(), K[1].data(), nthreads);
     ++st.evals;
     std::vector<double> df(n3);
     for (size_t i = 0; i < n3; ++i) df[i] = (K[1][i] - K[0][i]) / h0;
@@ -912,7 +944,7 @@ inline bool tsit5(const Case& cs, const Params<double>& p, std::vector<double>& 
         for (int j = 0; j < i; ++j) s += A[i][j] * K[j][k];
         dst[k] = Q[k] + h * s;
       }
-      rhs<double>(cs, p, dst.data(), K[i].data(), nthreads);
+      rhs<double>(cs, params_at(p, scratch, t + C[i] * h), dst.data(), K[i].data(), nthreads);
     }
     st.evals += 6;
     double eest = 0.0;

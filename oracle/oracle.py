@@ -49,6 +49,7 @@ def _load():
     lib.ho_rk2.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int, _dp]
     lib.ho_tsit5.argtypes = [ctypes.c_void_p, _dp, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                              ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int, _ip]
+    lib.ho_set_hydrograph.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, _dp, _dp]
     lib.ho_set_resistance_fn.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp, _dp]
     lib.ho_set_ude.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, _ip, _ip, _dp, ctypes.c_int,
                                ctypes.c_double, ctypes.c_double, _dp, _dp, _dp, _dp, ctypes.c_int]
@@ -194,6 +195,13 @@ class Oracle:
         if rc != 0:
             raise RuntimeError("oracle: " + self.lib.ho_last_error().decode())
         return Q, tuple(int(v) for v in st)
+
+    def set_hydrograph(self, group, t, q):
+        """Inlet-Q hydrograph of one group (hgo::hydro_at); empty t removes it."""
+        t = np.ascontiguousarray(t, dtype=np.float64)
+        q = np.ascontiguousarray(q, dtype=np.float64)
+        if self.lib.ho_set_hydrograph(self.h, int(group), len(t), _d(t), _d(q)) != 0:
+            raise RuntimeError("oracle: " + self.lib.ho_last_error().decode())
 
     def set_resistance_fn(self, kind, params=(0.0, 0.0, 0.0, 0.0), ks=None):
         """Manning's n as a function of the state (RES_* kinds 0-4 of hg_oracle.hpp)."""

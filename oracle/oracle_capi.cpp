@@ -52,6 +52,7 @@ Params<D<ND>> lift_params(const OracleCase& oc, int nDir, const double* dManning
   }
   q.exitWSE.resize(oc.p.exitWSE.size());
   for (size_t b = 0; b < oc.p.exitWSE.size(); ++b) q.exitWSE[b] = D<ND>(oc.p.exitWSE[b]);
+  q.hydro = oc.p.hydro;
   return q;
 }
 
@@ -67,7 +68,7 @@ int run_tangent(OracleCase& oc, const double* Q0, int nsteps, double dt, int nDi
   for (size_t k = 0; k < Q.size(); ++k) Q[k] = D<ND>(Q0[k]);
   D<ND> L(0.0);
   for (int s = 0; s < nsteps; ++s) {
-    rk2_step<D<ND>>(oc.cs, q, Q, dt, nthreads);
+    rk2_step<D<ND>>(oc.cs, q, Q, dt, nthreads, s * dt);
     for (int pi = 0; pi < nProbe; ++pi) {
       int c = probes[pi];
       D<ND> e = (Q[c] + oc.cs.hstill[c]) - obs[(size_t)s * nProbe + pi];
@@ -218,6 +219,19 @@ int ho_rhs(void* h, const double* Q, double* dQ, int nthreads) {
 }
 
 // Manning friction terms from given h, q (compute_friction_terms, semi_discretize_swe_2D.jl:544-547).
+// Inlet-Q hydrograph of group g (hgo::hydro_at); n = 0 removes it.
+int ho_set_hydrograph(void* h, int g, int n, const double* t, const double* q) {
+  auto* oc = static_cast<OracleCase*>(h);
+  if (g < 0 || g >= (int)oc->p.inletQ.size()) {
+    g_err = "ho_set_hydrograph: bad group";
+    return 1;
+  }
+  oc->p.hydro.resize(oc->p.inletQ.size());
+  oc->p.hydro[g].assign(t, t + n);
+  oc->p.hydro[g].insert(oc->p.hydro[g].end(), q, q + n);
+  return 0;
+}
+
 // Manning's n as a function of the state (process_ManningN_2D.jl:102-213):
 // kind RES_POWER_LAW..RES_H_UMAG_KS, params {n_lower, n_upper, k, h_mid}, ks per
 // cell (h_Umag_ks); kind RES_CONSTANT switches back to the cells' n.
@@ -317,10 +331,12 @@ int ho_rk2(void* h, double* Q, int nsteps, double dt, double cfl, int nthreads, 
   auto* oc = static_cast<OracleCase*>(h);
   try {
     std::vector<double> q(Q, Q + 3 * (size_t)oc->cs.mesh.nCells);
+    double t = 0.0;   // hydrographs: the run starts at t = 0
     for (int s = 0; s < nsteps; ++s) {
       double d = dt > 0 ? dt : cfl_dt(oc->cs, q.data(), cfl);
       if (dtOut) dtOut[s] = d;
-      rk2_step<double>(oc->cs, oc->p, q, d, nthreads);
+      rk2_step<double>(oc->cs, oc->p, q, d, nthreads, t);
+      t += d;
     }
     std::memcpy(Q, q.data(), q.size() * sizeof(double));
   } catch (const std::exception& e) {
@@ -407,7 +423,7 @@ int ho_rk2_loss(void* h, const double* Q0, int nsteps, double dt, int nProbe, co
     std::vector<double> q(Q0, Q0 + 3 * (size_t)N);
     double L = 0.0;
     for (int s = 0; s < nsteps; ++s) {
-      rk2_step<double>(oc->cs, oc->p, q, dt, nthreads);
+      rk2_step<double>(oc->cs, oc->p, q, dt, nthreads, s * dt);
       for (int pi = 0; pi < nProbe; ++pi) {
         int c = probes[pi];
         double e = (q[c] + oc->cs.hstill[c]) - obs[(size_t)s * nProbe + pi];
