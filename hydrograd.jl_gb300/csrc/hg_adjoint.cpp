@@ -10,8 +10,9 @@
 //   mu1 = M1 (0.5 mu2 + 0.5 dt J(Q1)^T mu2)
 //   mu2' = M0 (0.5 mu2 + mu1 + dt J(Q0)^T mu1)
 //   dL/dtheta += 0.5 dt (dR/dtheta)(Q1)^T mu2 + dt (dR/dtheta)(Q0)^T mu1
-// The forward pass stores the state every ckpt_every steps; the reverse sweep
-// recomputes one segment at a time, keeping that segment's stage states.
+// The forward pass stores the state every ckpt_every steps and keeps the last
+// segment's stage states; the reverse sweep recomputes the other segments one
+// at a time, keeping that segment's stage states.
 // Loss and parameter gradients accumulate in FP64.
 #include "hg_adjoint.hpp"
 
@@ -355,20 +356,33 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
 
   if (f64) {
     launch_gather_state_f64(N, c->d_perm, c->Quser, c->QA, st);
-    // Forward pass with checkpoints.
+    // Forward pass with checkpoints.  The last segment's steps write their
+    // stage states straight into the segment buffer, which the reverse sweep
+    // then starts from without recomputing them.
+    const int sLast = (nck - 1) * C;
+    double* Q0s = b->seg;                          // Q0 of step s0 + i at Q0s + i n3 (i = 0..C)
+    double* Q1s = b->seg + (size_t)(C + 1) * n3;   // Q1 of step s0 + i
     for (int s = 0; s < K; ++s) {
-      if (s % C == 0)
+      const bool last = s >= sLast;
+      const size_t i = (size_t)(s - sLast);
+      if (s % C == 0 && !last)
         ADJ_CUDA(c, cudaMemcpyAsync(b->ckpt + (size_t)(s / C) * n3, c->QA, n3 * sizeof(double),
                                     cudaMemcpyDeviceToDevice, st));
+      if (s == sLast) ADJ_CUDA(c, cudaMemcpyAsync(Q0s, c->QA, n3 * sizeof(double), cudaMemcpyDeviceToDevice, st));
+      const double* q0 = last ? Q0s + i * n3 : c->QA;
+      double* q1 = last ? Q1s + i * n3 : c->QB;
+      double* q2 = last ? Q0s + (i + 1) * n3 : c->QA;
       hydro(s * dt);
-      launch_inlet_total_f64(dm, ds, c->QA, st);
-      launch_stage_f64(dm, ds, kModeStage1, c->QA, nullptr, c->QB, false, st);
+      launch_inlet_total_f64(dm, ds, q0, st);
+      launch_stage_f64(dm, ds, kModeStage1, q0, nullptr, q1, false, st);
       hydro((s + 1) * dt);
-      launch_inlet_total_f64(dm, ds, c->QB, st);
-      launch_stage_f64(dm, ds, kModeStage2, c->QB, c->QA, c->QA, false, st);
-      launch_probe_loss_f64(dm, a, c->QA, b->probes, b->obs + (size_t)s * P, P, st);
+      launch_inlet_total_f64(dm, ds, q1, st);
+      launch_stage_f64(dm, ds, kModeStage2, q1, q0, q2, false, st);
+      launch_probe_loss_f64(dm, a, q2, b->probes, b->obs + (size_t)s * P, P, st);
       c->launches += 3 + extraPerStep;
     }
+    ADJ_CUDA(c, cudaMemcpyAsync(c->QA, Q0s + (size_t)(K - sLast) * n3, n3 * sizeof(double),
+                                cudaMemcpyDeviceToDevice, st));   // the final state
     if (Qfinal) {
       launch_scatter_state_f64(N, c->d_perm, c->QA, c->Quser, st);
       ADJ_CUDA(c, cudaMemcpyAsync(Qfinal, c->Quser, n3 * sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -382,11 +396,10 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
     }
     for (int seg = nck - 1; seg >= 0; --seg) {
       const int s0 = seg * C, s1 = std::min(K, s0 + C);
-      double* Q0s = b->seg;                          // Q0 of step s0 + i at Q0s + i n3 (i = 0..C)
-      double* Q1s = b->seg + (size_t)(C + 1) * n3;   // Q1 of step s0 + i
-      ADJ_CUDA(c, cudaMemcpyAsync(Q0s, b->ckpt + (size_t)seg * n3, n3 * sizeof(double), cudaMemcpyDeviceToDevice,
-                                  st));
-      for (int s = s0; s < s1; ++s) {
+      if (seg < nck - 1)   // the last segment's states are in place from the forward pass
+        ADJ_CUDA(c, cudaMemcpyAsync(Q0s, b->ckpt + (size_t)seg * n3, n3 * sizeof(double), cudaMemcpyDeviceToDevice,
+                                    st));
+      for (int s = s0; s < s1 && seg < nck - 1; ++s) {
         const size_t i = (size_t)(s - s0);
         hydro(s * dt);
         launch_inlet_total_f64(dm, ds, Q0s + i * n3, st);
@@ -478,14 +491,26 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
       if (e == cudaSuccess) e = cudaMemcpyAsync(dst.q, src.q, (size_t)n * sizeof(float2), cudaMemcpyDeviceToDevice, st);
       return e;
     };
-    // Forward pass with checkpoints (totals ping-pong in T0[0] / T0[1]).
+    // Forward pass with checkpoints (totals ping-pong in T0[0] / T0[1]).  The
+    // last segment's steps write their stage states and totals straight into
+    // the segment buffers, which the reverse sweep starts from.
+    const int sLast = (nck - 1) * C;
     totals(XA, T0);
     for (int s = 0; s < K; ++s) {
-      if (s % C == 0) ADJ_CUDA(c, copy_state(ck.at(s / C, n), XA));
-      step(s, XA, XB, XA, T0, T0 + stride, T0);
-      launch_probe_loss_f32(dm, a, XA, b->probes, b->obs + (size_t)s * P, P, st);
+      if (s < sLast) {
+        if (s % C == 0) ADJ_CUDA(c, copy_state(ck.at(s / C, n), XA));
+        step(s, XA, XB, XA, T0, T0 + stride, T0);
+        launch_probe_loss_f32(dm, a, XA, b->probes, b->obs + (size_t)s * P, P, st);
+      } else {
+        const size_t i = (size_t)(s - sLast);
+        if (s == sLast) ADJ_CUDA(c, copy_state(sg.at(0, n), XA));   // its totals are in T0 already
+        step(s, sg.at(i, n), sg.at(C + 1 + i, n), sg.at(i + 1, n), T0 + i * stride, T1 + i * stride,
+             T0 + (i + 1) * stride);
+        launch_probe_loss_f32(dm, a, sg.at(i + 1, n), b->probes, b->obs + (size_t)s * P, P, st);
+      }
       c->launches += P > 0 ? 1 : 0;
     }
+    ADJ_CUDA(c, copy_state(XA, sg.at(K - sLast, n)));   // the final state
     if (Qfinal) {
       launch_scatter_state_f32(N, c->d_perm, XA, c->Quser, st);
       ADJ_CUDA(c, cudaMemcpyAsync(Qfinal, c->Quser, n3 * sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -498,12 +523,14 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
     }
     for (int seg = nck - 1; seg >= 0; --seg) {
       const int s0 = seg * C, s1 = std::min(K, s0 + C);
-      ADJ_CUDA(c, copy_state(sg.at(0, n), ck.at(seg, n)));
-      totals(sg.at(0, n), T0);
-      for (int s = s0; s < s1; ++s) {
-        const size_t i = (size_t)(s - s0);
-        step(s, sg.at(i, n), sg.at(C + 1 + i, n), sg.at(i + 1, n), T0 + i * stride, T1 + i * stride,
-             T0 + (i + 1) * stride);
+      if (seg < nck - 1) {   // the last segment's states and totals are in place from the forward pass
+        ADJ_CUDA(c, copy_state(sg.at(0, n), ck.at(seg, n)));
+        totals(sg.at(0, n), T0);
+        for (int s = s0; s < s1; ++s) {
+          const size_t i = (size_t)(s - s0);
+          step(s, sg.at(i, n), sg.at(C + 1 + i, n), sg.at(i + 1, n), T0 + i * stride, T1 + i * stride,
+               T0 + (i + 1) * stride);
+        }
       }
       for (int s = s1 - 1; s >= s0; --s) {
         const size_t i = (size_t)(s - s0);
