@@ -522,14 +522,17 @@ __device__ __forceinline__ void pipe_issue(const DevMesh& m, StateF32 Xin, State
   }
 }
 
-template <int NS, int MODE>
+// FUSED: the fused step's bookkeeping (StageFuse); otherwise a plain stage of
+// an unfused step (dt and inlet totals from DevScalars / DevMesh), as the
+// ensembles and state-dependent resistance take.
+template <int NS, int MODE, bool FUSED>
 __global__ void __launch_bounds__(kBlock, kPipeCtasPerSm)
     k_stage_pipe_f32(DevMesh m, DevScalars s, StateF32 Xin, StateF32 Xbase, StateF32 Xout, int cfl, StageFuse f) {
   using T = PipeTile<NS, MODE>;
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ float dtShared;
   const int n = m.n, nTiles = (n + kBlock - 1) / kBlock, tid = threadIdx.x, G = gridDim.x;
-  if (tid == 0) dtShared = (float)fused_dt(s, f);
+  if (tid == 0) dtShared = FUSED ? (float)fused_dt(s, f) : *s.dtf;
   auto halo_id = [&](int t) { return (t < nTiles && tid < kHaloMax) ? m.halo[(size_t)t * kHaloMax + tid] : -1; };
   int t = blockIdx.x;
   if (t < nTiles) pipe_issue<NS, MODE>(m, Xin, Xbase, t, smem, halo_id(t));
@@ -562,14 +565,15 @@ __global__ void __launch_bounds__(kBlock, kPipeCtasPerSm)
 #pragma unroll
       for (int k = 0; k < NS; ++k) sl[k] = bSL[k * kBlock + tid];
       stage_cell<NS, MODE, true>(m, s, Xin.x, bX, bCP, bHX, bHP, base, c, sl, bX[tid], bCP[tid], bCS[tid], bQ, bXB,
-                                 bQB, tid, dtShared, f.totalIn, Xout, nullptr, cfl, cand, hOut, wetOut);
+                                 bQB, tid, dtShared, FUSED ? f.totalIn : m.totalA, Xout, nullptr, cfl, cand, hOut,
+                                 wetOut);
     }
-    if (m.nInlet > 0) fused_inlet_totals<NS>(m, f, t, c, hOut, wetOut);
+    if (FUSED && m.nInlet > 0) fused_inlet_totals<NS>(m, f, t, c, hOut, wetOut);
     __syncthreads();   // buffer b is refilled at the top of the next iteration
   }
   cp_async_wait<0>();
-  if (f.record && blockIdx.x == 0 && tid == 0) fused_record(s, f);
-  if (cfl) block_min_publish_f(cand, s.cflMinF + (1 - f.parity));
+  if (FUSED && f.record && blockIdx.x == 0 && tid == 0) fused_record(s, f);
+  if (cfl) block_min_publish_f(cand, FUSED ? s.cflMinF + (1 - f.parity) : s.cflMinF);
 }
 
 template <int NS>
@@ -722,14 +726,6 @@ void launch_stage_ns(const DevMesh& m, const DevScalars& s, int mode, StateF32 X
 }
 }  // namespace
 
-void launch_stage_f32(const DevMesh& m, const DevScalars& s, int mode, StateF32 Xin, StateF32 Xbase, StateF32 Xout,
-                      double* Rout, bool cfl, cudaStream_t st) {
-  const int f = cfl ? 1 : 0;
-  const StageFuse nf{};
-  if (m.nslot <= 3) launch_stage_ns<3, false>(m, s, mode, Xin, Xbase, Xout, Rout, f, nf, st);
-  else if (m.nslot <= 4) launch_stage_ns<4, false>(m, s, mode, Xin, Xbase, Xout, Rout, f, nf, st);
-  else launch_stage_ns<8, false>(m, s, mode, Xin, Xbase, Xout, Rout, f, nf, st);
-}
 namespace {
 // Kernel of the fused stages: HG_STAGE_KERNEL = gather / pipe / tma forces
 // one; otherwise DevMesh::stageKernel (hg_autotune's choice).  Measured on the
@@ -778,25 +774,27 @@ void launch_tma(const DevMesh& m, const DevScalars& s, StateF32 Xin, StateF32 Xb
   k_stage_tma_f32<NS, MODE><<<tiles < grid ? tiles : grid, kBlock, T::kSmem, st>>>(m, s, Xin, Xbase, Xout, cfl, fu);
 }
 
-template <int NS, int MODE>
+template <int NS, int MODE, bool FUSED>
 void launch_pipe(const DevMesh& m, const DevScalars& s, StateF32 Xin, StateF32 Xbase, StateF32 Xout, int cfl,
                  const StageFuse& fu, cudaStream_t st) {
   using T = PipeTile<NS, MODE>;
   static const bool attr = [] {   // more than 48 KB of dynamic shared memory: opt in once
-    cudaFuncSetAttribute(k_stage_pipe_f32<NS, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T::kSmem);
+    cudaFuncSetAttribute(k_stage_pipe_f32<NS, MODE, FUSED>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)T::kSmem);
     return true;
   }();
   (void)attr;
-  static const int grid = sm_count() * resident_ctas(k_stage_pipe_f32<NS, MODE>, T::kSmem);
+  static const int grid = sm_count() * resident_ctas(k_stage_pipe_f32<NS, MODE, FUSED>, T::kSmem);
   const int tiles = blocks_for(m.n);
-  k_stage_pipe_f32<NS, MODE><<<tiles < grid ? tiles : grid, kBlock, T::kSmem, st>>>(m, s, Xin, Xbase, Xout, cfl, fu);
+  k_stage_pipe_f32<NS, MODE, FUSED><<<tiles < grid ? tiles : grid, kBlock, T::kSmem, st>>>(m, s, Xin, Xbase, Xout,
+                                                                                            cfl, fu);
 }
 
-template <int NS>
+template <int NS, bool FUSED = true>
 void launch_pipe_mode(const DevMesh& m, const DevScalars& s, int mode, StateF32 Xin, StateF32 Xbase, StateF32 Xout,
                       int cfl, const StageFuse& fu, cudaStream_t st) {
-  if (mode == kModeStage1) launch_pipe<NS, kModeStage1>(m, s, Xin, Xbase, Xout, cfl, fu, st);
-  else launch_pipe<NS, kModeStage2>(m, s, Xin, Xbase, Xout, cfl, fu, st);
+  if (mode == kModeStage1) launch_pipe<NS, kModeStage1, FUSED>(m, s, Xin, Xbase, Xout, cfl, fu, st);
+  else launch_pipe<NS, kModeStage2, FUSED>(m, s, Xin, Xbase, Xout, cfl, fu, st);
 }
 
 template <int NS>
@@ -821,6 +819,28 @@ bool stage_kernel_usable(const DevMesh& m, int k, int mode, StateF32 Xin, StateF
   // a state view whose lo parts start 8 bytes off takes another kernel
   return a16(m.SL) && a16(m.CP) && a16(m.CS) && a16(Xin.x) && a16(Xin.q) &&
          (mode != kModeStage2 || (a16(Xbase.x) && a16(Xbase.q)));
+}
+
+void launch_stage_f32(const DevMesh& m, const DevScalars& s, int mode, StateF32 Xin, StateF32 Xbase, StateF32 Xout,
+                      double* Rout, bool cfl, cudaStream_t st) {
+  const int f = cfl ? 1 : 0;
+  const StageFuse nf{};
+  // Stages of unfused steps (ensembles, state-dependent resistance) take the
+  // persistent pipelined kernel wherever it can run, whatever the autotuner
+  // chose for fused steps: its unfused instance and the gather kernel's differ
+  // in the last FP32 bit of a few cells (the compiler contracts the same
+  // source differently), so a fixed choice keeps runs reproducible.
+  // HG_STAGE_KERNEL=gather (or tma) selects the gather kernel here.
+  const int forced = stage_kernel_forced();
+  if ((mode == kModeStage1 || mode == kModeStage2) && (forced < 0 || forced == kStagePipe) &&
+      stage_kernel_usable(m, kStagePipe, mode, Xin, Xbase)) {
+    if (m.nslot <= 3) launch_pipe_mode<3, false>(m, s, mode, Xin, Xbase, Xout, f, nf, st);
+    else launch_pipe_mode<4, false>(m, s, mode, Xin, Xbase, Xout, f, nf, st);
+    return;
+  }
+  if (m.nslot <= 3) launch_stage_ns<3, false>(m, s, mode, Xin, Xbase, Xout, Rout, f, nf, st);
+  else if (m.nslot <= 4) launch_stage_ns<4, false>(m, s, mode, Xin, Xbase, Xout, Rout, f, nf, st);
+  else launch_stage_ns<8, false>(m, s, mode, Xin, Xbase, Xout, Rout, f, nf, st);
 }
 
 void launch_stage_f32_fused(const DevMesh& m, const DevScalars& s, int mode, StateF32 Xin, StateF32 Xbase,
