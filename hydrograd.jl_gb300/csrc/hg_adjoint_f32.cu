@@ -9,8 +9,12 @@
 // Compiled with the same fast-math options as the FP32 forward kernels.
 #include <cfloat>
 #include <cmath>
+#include <cstdint>
+#include <cstdlib>
+#include <cstring>
 
 #include "hg_adjoint_state.hpp"
+#include "hg_async.cuh"
 #include "hg_device.cuh"
 #include "hg_dual.cuh"
 #include "hg_f32.cuh"
@@ -72,18 +76,44 @@ __device__ __forceinline__ void acc_add(float2* p, float b, float g) {
 template <int NS>
 constexpr int vjp_min_blocks() { return NS <= 4 ? 5 : 1; }   // <= 96 registers, no spills
 
-template <int NS>
-__global__ void __launch_bounds__(kBlock, vjp_min_blocks<NS>()) k_vjp_f32(DevMesh m, AdjDev a, StateF32 Q, const float* __restrict__ mu,
-                                                    const float* __restrict__ extra, float* out, float cSelf,
-                                                    float cExtra, float beta) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= m.n) return;
+// Where a VJP reads its data: the cell's own records and cotangents, its slot
+// records, and a neighbour's records and cotangents.  GlobalSrc reads device
+// memory (neighbours by cell id); TileSrc a pipelined tile in shared memory
+// (neighbours by tile-local index: own cells, then the tile's halo).
+struct VjpNbr {
+  float4 x, p;
+  float area, m0, m1, m2;
+};
+struct GlobalSrc {
+  const DevMesh& m;
+  StateF32 Q;
+  const float* mu;
+  const float* extra;
+  int j;
+  __device__ float4 x() const { return __ldg(&Q.x[j]); }
+  __device__ float4 cp() const { return __ldg(&m.CP[j]); }
+  __device__ float4 cs() const { return __ldg(&m.CS[j]); }
+  __device__ float mu_own(int b) const { return mu[(size_t)b * m.n + j]; }
+  __device__ float extra_own(int b) const { return extra ? extra[(size_t)b * m.n + j] : 0.0f; }
+  __device__ float4 slot(int k) const { return __ldg(&m.SL[(size_t)k * m.n + j]); }
+  __device__ VjpNbr nbr(int nb) const {
+    return VjpNbr{__ldg(&Q.x[nb]), __ldg(&m.CP[nb]), __ldg(&m.CS[nb]).z, mu[nb], mu[m.n + nb],
+                  mu[2 * (size_t)m.n + nb]};
+  }
+};
+
+// The VJP of one stage at cell j (interior faces: 3-direction duals of the
+// reference solver where a side is dry, reverse mode where both are wet; the
+// sources), written to out[j] and the cell's parameter accumulators.
+template <int NS, class Src>
+__device__ __forceinline__ void vjp_cell(const DevMesh& m, const AdjDev& a, int j, const Src& src, float* out,
+                                         float cSelf, float cExtra, float beta) {
   const int n = m.n;
-  const float4 cp = __ldg(&m.CP[j]);
-  const float4 cs = __ldg(&m.CS[j]);
-  const SideF32 L = make_side_f32(__ldg(&Q.x[j]), cp, m.hsmf, m.hsmLo);
+  const float4 cp = src.cp();
+  const float4 cs = src.cs();
+  const SideF32 L = make_side_f32(src.x(), cp, m.hsmf, m.hsmLo);
   const float Aj = cs.z;
-  const float mj0 = mu[j], mj1 = mu[n + j], mj2 = mu[2 * n + j];
+  const float mj0 = src.mu_own(0), mj1 = src.mu_own(1), mj2 = src.mu_own(2);
   float g0 = 0.0f, g1 = 0.0f, g2 = 0.0f, gn = 0.0f;
   if (!L.s.dry) {   // a dry cell's output is masked to zero, and its faces add to nothing else
     // Wet-wet faces in reverse mode (roe_wet_vjp, the own quantities'
@@ -93,15 +123,16 @@ __global__ void __launch_bounds__(kBlock, vjp_min_blocks<NS>()) k_vjp_f32(DevMes
     OwnAdj<float> b;
 #pragma unroll
     for (int k = 0; k < NS; ++k) {
-      const float4 sl = __ldg(&m.SL[(size_t)k * n + j]);
+      const float4 sl = src.slot(k);
       const int32_t nb = slot_nb(sl);
       if (nb < 0) continue;   // no face, or a boundary face (k_vjp_bnd_f32)
       const float nx = sl.x, ny = sl.y, len = sl.z;
-      const SideF32 R = make_side_f32(__ldg(&Q.x[nb]), __ldg(&m.CP[nb]), m.hsmf, m.hsmLo);
-      const float An = __ldg(&m.CS[nb]).z;
-      const float w0 = len * (mu[nb] / An - mj0 / Aj);
-      const float w1 = len * (mu[n + nb] / An - mj1 / Aj);
-      const float w2 = len * (mu[2 * n + nb] / An - mj2 / Aj);
+      const VjpNbr r = src.nbr(nb);
+      const SideF32 R = make_side_f32(r.x, r.p, m.hsmf, m.hsmLo);
+      const float An = r.area;
+      const float w0 = len * (r.m0 / An - mj0 / Aj);
+      const float w1 = len * (r.m1 / An - mj1 / Aj);
+      const float w2 = len * (r.m2 / An - mj2 / Aj);
       if (!R.s.dry) {
         roe_wet_vjp<float>(L.s, o, R.s, (R.s.xi - L.s.xi) + (R.xlo - L.xlo), m.gf, nx, ny, w0, w1, w2, b);
       } else {
@@ -136,10 +167,115 @@ __global__ void __launch_bounds__(kBlock, vjp_min_blocks<NS>()) k_vjp_f32(DevMes
   }
   if (gn != 0.0f) acc_add(&a.accF[j], beta, gn);
   const float mask = L.s.dry ? 0.0f : 1.0f;
-  const float e0 = extra ? extra[j] : 0.0f, e1 = extra ? extra[n + j] : 0.0f, e2 = extra ? extra[2 * n + j] : 0.0f;
+  const float e0 = src.extra_own(0), e1 = src.extra_own(1), e2 = src.extra_own(2);
   out[j] = mask * (cSelf * mj0 + cExtra * e0 + beta * g0);
   out[n + j] = mask * (cSelf * mj1 + cExtra * e1 + beta * g1);
   out[2 * n + j] = mask * (cSelf * mj2 + cExtra * e2 + beta * g2);
+}
+
+template <int NS>
+__global__ void __launch_bounds__(kBlock, vjp_min_blocks<NS>()) k_vjp_f32(DevMesh m, AdjDev a, StateF32 Q, const float* __restrict__ mu,
+                                                    const float* __restrict__ extra, float* out, float cSelf,
+                                                    float cExtra, float beta) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= m.n) return;
+  vjp_cell<NS>(m, a, j, GlobalSrc{m, Q, mu, extra, j}, out, cSelf, cExtra, beta);
+}
+
+// Pipelined persistent VJP (the stage kernel's k_stage_pipe_f32 scheme): each
+// CTA walks 256-cell tiles; while it computes one, cp.async copies bring the
+// next tile's slot records (DevMesh::SLp, tile-local neighbours), state,
+// parameter, source and cotangent records and its halo's (DevMesh::halo)
+// into the other of two shared-memory buffers.  The arithmetic is vjp_cell's.
+constexpr int kVTile = kStageBlockF32;
+template <int NS>
+struct VjpTile {
+  static constexpr uint32_t kRec = kVTile * sizeof(float4), kF = kVTile * sizeof(float);
+  static constexpr uint32_t kH16 = kHaloMax * sizeof(float4), kH4 = kHaloMax * sizeof(float);
+  static constexpr uint32_t kSL = 0, kX = NS * kRec, kCP = kX + kRec, kCS = kCP + kRec;
+  static constexpr uint32_t kMU = kCS + kRec, kEX = kMU + 3 * kF;
+  static constexpr uint32_t kHX = kEX + 3 * kF, kHP = kHX + kH16, kHA = kHP + kH16, kHM = kHA + kH4;
+  static constexpr uint32_t kBuf = (kHM + 3 * kH4 + 127u) & ~127u;
+  static constexpr uint32_t kSmem = 2 * kBuf;
+};
+template <int NS>
+struct TileSrc {
+  const unsigned char* B;
+  int tid;
+  bool hasExtra;   // no cotangent carried in: the extra slab is not filled
+  __device__ const float4* rec(uint32_t off) const { return reinterpret_cast<const float4*>(B + off); }
+  __device__ const float* flt(uint32_t off) const { return reinterpret_cast<const float*>(B + off); }
+  __device__ float4 x() const { return rec(VjpTile<NS>::kX)[tid]; }
+  __device__ float4 cp() const { return rec(VjpTile<NS>::kCP)[tid]; }
+  __device__ float4 cs() const { return rec(VjpTile<NS>::kCS)[tid]; }
+  __device__ float mu_own(int b) const { return flt(VjpTile<NS>::kMU)[b * kVTile + tid]; }
+  __device__ float extra_own(int b) const { return hasExtra ? flt(VjpTile<NS>::kEX)[b * kVTile + tid] : 0.0f; }
+  __device__ float4 slot(int k) const { return rec(VjpTile<NS>::kSL)[k * kVTile + tid]; }
+  __device__ VjpNbr nbr(int nb) const {
+    const int li = nb & 511;
+    if (li < kVTile)
+      return VjpNbr{rec(VjpTile<NS>::kX)[li], rec(VjpTile<NS>::kCP)[li], rec(VjpTile<NS>::kCS)[li].z,
+                    flt(VjpTile<NS>::kMU)[li], flt(VjpTile<NS>::kMU)[kVTile + li],
+                    flt(VjpTile<NS>::kMU)[2 * kVTile + li]};
+    const int h = li - kVTile;
+    return VjpNbr{rec(VjpTile<NS>::kHX)[h], rec(VjpTile<NS>::kHP)[h], flt(VjpTile<NS>::kHA)[h],
+                  flt(VjpTile<NS>::kHM)[h], flt(VjpTile<NS>::kHM)[kHaloMax + h],
+                  flt(VjpTile<NS>::kHM)[2 * kHaloMax + h]};
+  }
+};
+
+template <int NS>
+__device__ __forceinline__ void vjp_issue(const DevMesh& m, StateF32 Q, const float* mu, const float* extra, int t,
+                                          unsigned char* B, int hid) {
+  using T = VjpTile<NS>;
+  const int tid = threadIdx.x, n = m.n;
+  const int c = t * kVTile + tid;
+  if (c < n) {
+#pragma unroll
+    for (int k = 0; k < NS; ++k) cp_async16(B + T::kSL + (k * kVTile + tid) * 16, &m.SLp[(size_t)k * n + c]);
+    cp_async16(B + T::kX + tid * 16, &Q.x[c]);
+    cp_async16(B + T::kCP + tid * 16, &m.CP[c]);
+    cp_async16(B + T::kCS + tid * 16, &m.CS[c]);
+#pragma unroll
+    for (int b = 0; b < 3; ++b) {
+      cp_async4(B + T::kMU + (b * kVTile + tid) * 4, &mu[(size_t)b * n + c]);
+      if (extra) cp_async4(B + T::kEX + (b * kVTile + tid) * 4, &extra[(size_t)b * n + c]);
+    }
+  }
+  if (hid >= 0) {
+    cp_async16(B + T::kHX + tid * 16, &Q.x[hid]);
+    cp_async16(B + T::kHP + tid * 16, &m.CP[hid]);
+    cp_async4(B + T::kHA + tid * 4, &m.CS[hid].z);
+#pragma unroll
+    for (int b = 0; b < 3; ++b) cp_async4(B + T::kHM + (b * kHaloMax + tid) * 4, &mu[(size_t)b * n + hid]);
+  }
+}
+
+template <int NS>
+__global__ void __launch_bounds__(kVTile, 2) k_vjp_pipe_f32(DevMesh m, AdjDev a, StateF32 Q, const float* mu,
+                                                           const float* extra, float* out, float cSelf, float cExtra,
+                                                           float beta) {
+  using T = VjpTile<NS>;
+  extern __shared__ __align__(128) unsigned char smem[];
+  const int n = m.n, nTiles = (n + kVTile - 1) / kVTile, tid = threadIdx.x, G = gridDim.x;
+  auto halo_id = [&](int t) { return (t < nTiles && tid < kHaloMax) ? m.halo[(size_t)t * kHaloMax + tid] : -1; };
+  int t = blockIdx.x;
+  if (t < nTiles) vjp_issue<NS>(m, Q, mu, extra, t, smem, halo_id(t));
+  cp_async_commit();
+  int hidNext = halo_id(t + G);
+  int b = 0;
+  for (; t < nTiles; t += G, b ^= 1) {
+    const int tn = t + G;
+    if (tn < nTiles) vjp_issue<NS>(m, Q, mu, extra, tn, smem + (b ^ 1) * T::kBuf, hidNext);
+    cp_async_commit();
+    hidNext = halo_id(tn + G);
+    cp_async_wait<1>();
+    __syncthreads();
+    const int j = t * kVTile + tid;
+    if (j < n) vjp_cell<NS>(m, a, j, TileSrc<NS>{smem + b * T::kBuf, tid, extra != nullptr}, out, cSelf, cExtra, beta);
+    __syncthreads();   // buffer b is refilled at the top of the next iteration
+  }
+  cp_async_wait<0>();
 }
 
 // Boundary faces of the cells that have any (one thread per such cell; runs
@@ -291,6 +427,44 @@ __global__ void k_fold_accumulators_f32(DevMesh m, AdjDev a) {
 }  // namespace
 
 namespace {
+// The interior VJP takes the pipelined persistent kernel wherever it can run
+// (degree <= 4, the tile tables built, 16-byte aligned state records) -- a
+// fixed choice, so runs reproduce; HG_VJP_KERNEL=gather forces the
+// block-per-128-cells kernel.
+bool vjp_gather_forced() {
+  static const bool on = [] {
+    const char* e = std::getenv("HG_VJP_KERNEL");
+    return e && std::strcmp(e, "gather") == 0;
+  }();
+  return on;
+}
+
+template <int NS>
+void launch_vjp_interior(const DevMesh& m, const AdjDev& a, StateF32 Q, const float* mu, const float* extra,
+                         float* out, float cSelf, float cExtra, float beta, cudaStream_t st) {
+  auto a16 = [](const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; };
+  if constexpr (NS <= 4) {
+    if (!vjp_gather_forced() && m.SLp && m.halo && a16(m.SLp) && a16(m.CP) && a16(m.CS) && a16(Q.x)) {
+      using T = VjpTile<NS>;
+      static const int grid = [] {
+        cudaFuncSetAttribute(k_vjp_pipe_f32<NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T::kSmem);
+        int dev = 0, sms = 0, per = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_vjp_pipe_f32<NS>, kVTile, T::kSmem) != cudaSuccess ||
+            per < 1)
+          per = 1;
+        return (sms > 0 ? sms : 1) * per;
+      }();
+      const int tiles = (m.n + kVTile - 1) / kVTile;
+      k_vjp_pipe_f32<NS><<<tiles < grid ? tiles : grid, kVTile, T::kSmem, st>>>(m, a, Q, mu, extra, out, cSelf,
+                                                                               cExtra, beta);
+      return;
+    }
+  }
+  k_vjp_f32<NS><<<blocks_for(m.n), kBlock, 0, st>>>(m, a, Q, mu, extra, out, cSelf, cExtra, beta);
+}
+
 template <int NS>
 int launch_vjp_ns(const DevMesh& m, const AdjDev& a, StateF32 Q, const float* mu, const float* extra, float* out,
                   float cSelf, float cExtra, double betaD, cudaStream_t st, cudaStream_t side, cudaEvent_t evFork,
@@ -304,7 +478,7 @@ int launch_vjp_ns(const DevMesh& m, const AdjDev& a, StateF32 Q, const float* mu
     if (m.nInlet > 0) k_inlet_group_sums_f32<<<(m.nInlet + 3) / 4, 128, 0, side>>>(m, a, betaD);
     cudaEventRecord(evJoin, side);
   }
-  k_vjp_f32<NS><<<blocks_for(m.n), kBlock, 0, st>>>(m, a, Q, mu, extra, out, cSelf, cExtra, beta);
+  launch_vjp_interior<NS>(m, a, Q, mu, extra, out, cSelf, cExtra, beta, st);
   if (!nbb) return 1;
   cudaStreamWaitEvent(st, evJoin, 0);
   k_vjp_combine_f32<<<(a.nBndCells + 127) / 128, 128, 0, st>>>(m, a, Q, out, beta, betaD);

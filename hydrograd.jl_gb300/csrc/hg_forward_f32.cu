@@ -14,6 +14,7 @@
 #include <cstdlib>
 #include <cstring>
 
+#include "hg_async.cuh"
 #include "hg_device.cuh"
 #include "hg_f32.cuh"
 #include "hg_reduce.cuh"
@@ -483,18 +484,6 @@ struct PipeTile {
   static constexpr uint32_t kBuf = (((MODE == kModeStage2) ? kQB + kLo : kXB) + 127u) & ~127u;
   static constexpr uint32_t kSmem = 2 * kBuf;
 };
-
-__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
-  const unsigned int a = (unsigned int)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(a), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
-  const unsigned int a = (unsigned int)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(a), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
 // Copies of tile t into buffer B: the thread's own cell's records, and halo
 // record hid (-1: none) into halo slot threadIdx.x.
