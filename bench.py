@@ -276,7 +276,8 @@ def run_config5(args, device):
     probes = np.unique((rs.uniform(256) * N).astype(np.int64))[:64].astype(np.int32)
     h_rest = case["wstill"] - case["zb_cells"]
     obs = np.tile(h_rest[probes], (args.config5_steps, 1))
-    c32.loss_and_grad(Q0, 4, dt, probes, obs[:4], ckpt_every=2)   # allocation
+    # warm-up at the timed size: the stage-state tape is allocated outside the timed call
+    c32.loss_and_grad(Q0, args.config5_steps, dt, probes, obs, ckpt_every=50, want=("manning",))
     t0 = time.perf_counter()
     r = c32.loss_and_grad(Q0, args.config5_steps, dt, probes, obs, ckpt_every=50, want=("manning",))
     el = time.perf_counter() - t0
@@ -338,7 +339,7 @@ def run_ensemble(args, device):
         probes = np.concatenate([per_mesh[m] + e.cell_offset[i] for i, m in enumerate(member_mesh)]).astype(np.int32)
         h_rest = np.concatenate([c["wstill"] - c["zb_cells"] for c in cases])
         obs = np.tile(h_rest[probes], (args.ens_adj_steps, 1))
-        e.loss_and_grad(Q0, 4, dt, probes, obs[:4], ckpt_every=2)   # warm-up / allocation
+        e.loss_and_grad(Q0, args.ens_adj_steps, dt, probes, obs, ckpt_every=args.ens_ckpt)   # warm-up / allocation
         t0 = time.perf_counter()
         e.loss_and_grad(Q0, args.ens_adj_steps, dt, probes, obs, ckpt_every=args.ens_ckpt)
         el = time.perf_counter() - t0
@@ -431,7 +432,7 @@ def run_ours(args):
         grads = {}
         for prec in ("fp32c", "fp64"):
             ctx = ctxs[prec]
-            ctx.loss_and_grad(case["Q0"], 4, dt_adj, probes, obs[:4], ckpt_every=2)       # warm-up / allocation
+            ctx.loss_and_grad(case["Q0"], args.adj_steps, dt_adj, probes, obs, ckpt_every=50)   # warm-up / allocation
             barrier(dist)
             t0 = time.perf_counter()
             r = ctx.loss_and_grad(case["Q0"], args.adj_steps, dt_adj, probes, obs, ckpt_every=50)
@@ -449,7 +450,8 @@ def run_ours(args):
             "grad_zb_field_rel_linf": float(np.abs(g32["g_zb"] - g64["g_zb"]).max() / np.abs(g64["g_zb"]).max()),
             "loss_rel": float(abs(g32["loss"] - g64["loss"]) / abs(g64["loss"])),
         }
-        adj["config"] = (f"{args.adj_steps} fixed-dt steps (dt = half the initial CFL step), checkpoints every 50, "
+        adj["config"] = (f"{args.adj_steps} fixed-dt steps (dt = half the initial CFL step), checkpoint spacing 50 "
+                         "widened by the automatic stage-state tape (all steps kept where they fit in HBM), "
                          f"{len(probes)} probes (half on the pool rim, half at the inlet), loss = mean squared "
                          "departure of the probe depths from the lake at rest")
     cfg5 = run_config5(args, local) if args.config5_steps > 0 else None
@@ -538,6 +540,8 @@ def main():
                     help="only run the stage kernel a few times (a small case for ncu captures)")
     ap.add_argument("--profile-adjoint", default=None, choices=["fp32c", "fp64"],
                     help="only run one short forward+adjoint (a small case for ncu captures)")
+    ap.add_argument("--profile-adj-steps", type=int, default=4, help="steps of the --profile-adjoint run")
+    ap.add_argument("--profile-adj-ckpt", type=int, default=2, help="checkpoint spacing of the --profile-adjoint run")
     args = ap.parse_args()
     if args.steps_fp64 is None:
         args.steps_fp64 = args.steps
@@ -566,16 +570,18 @@ def profile_stage(args):
 
 
 def profile_adjoint(args):
-    """One forward+adjoint of 4 fixed-dt steps (checkpoints every 2) on the
-    workload: 8 VJP launches, after the 4 + 4 forward stage pairs."""
+    """One forward+adjoint of --profile-adj-steps fixed-dt steps (default 4,
+    checkpoints every --profile-adj-ckpt, default 2) on the workload: with the
+    defaults, 8 VJP launches after the 4 + 4 forward stage pairs."""
     from hydrograd_gb.workloads import probes_and_perturbation, river_triangles
     case = river_triangles(n=args.n)
     ctx = make_ctx(case, args.profile_adjoint, 0)
     probes, _ = probes_and_perturbation(case, 64)
     dt = 0.5 * ctx.integrate(case["Q0"], 1, cfl=0.4)[1][0]
-    obs = np.tile(case["Q0"][probes], (4, 1))
+    K = args.profile_adj_steps
+    obs = np.tile(case["Q0"][probes], (K, 1))
     t0 = time.perf_counter()
-    r = ctx.loss_and_grad(case["Q0"], 4, dt, probes, obs, ckpt_every=2)
+    r = ctx.loss_and_grad(case["Q0"], K, dt, probes, obs, ckpt_every=args.profile_adj_ckpt)
     print(json.dumps({"precision": args.profile_adjoint, "cells": len(case["cell_node_count"]), "loss": r["loss"],
                       "seconds": time.perf_counter() - t0}))
 

@@ -10,9 +10,11 @@
 //   mu1 = M1 (0.5 mu2 + 0.5 dt J(Q1)^T mu2)
 //   mu2' = M0 (0.5 mu2 + mu1 + dt J(Q0)^T mu1)
 //   dL/dtheta += 0.5 dt (dR/dtheta)(Q1)^T mu2 + dt (dR/dtheta)(Q0)^T mu1
-// The forward pass stores the state every ckpt_every steps and keeps the last
-// segment's stage states; the reverse sweep recomputes the other segments one
-// at a time, keeping that segment's stage states.
+// The forward pass stores the state at the start of every segment and keeps
+// the last segment's stage states; the reverse sweep recomputes the other
+// segments one at a time, keeping that segment's stage states.  A segment is
+// ckpt_every steps, or as many more as the context's tape budget holds (all of
+// them where it fits: no recomputation); the result is the same either way.
 // Loss and parameter gradients accumulate in FP64.
 #include "hg_adjoint.hpp"
 
@@ -36,6 +38,7 @@ struct AdjointBuffers {
   double* seg = nullptr;
   size_t segStates = 0;
   double *mu1 = nullptr, *mu2 = nullptr, *gzb = nullptr;
+  double* userOut = nullptr;   // [2 n] the n and zb gradients in the caller's cell order
   int32_t* probes = nullptr;
   int32_t* probeCsr = nullptr;   // FP32C: probes grouped by cell (ProbeCsr), <= 3 P + 1 entries
   double* obs = nullptr;
@@ -109,6 +112,7 @@ int setup(hg_ctx* c) {
   ADJ_CUDA(c, falloc(b, &b->mu1, (size_t)3 * N));
   ADJ_CUDA(c, falloc(b, &b->mu2, (size_t)3 * N));
   ADJ_CUDA(c, falloc(b, &b->gzb, N));
+  ADJ_CUDA(c, falloc(b, &b->userOut, (size_t)2 * N));
   // Inlet tables: boundary-face index of each inlet CSR entry (faces numbered
   // by face id, as the forward tables), and per group the distinct cells with
   // the sum of L^(5/3) over their faces in the group.
@@ -196,6 +200,27 @@ int setup(hg_ctx* c) {
   return HG_OK;
 }
 
+// Segment length: at least the caller's spacing C, and as long as the
+// stage-state tape of one segment (2 C + 1 states of 24 bytes per cell) fits
+// in the context's budget -- all K steps where it fits.
+int segment_length(hg_ctx* c, int K, int C) {
+  if (c->adjTapeBytes == 0) return C;
+  const size_t state = (size_t)24 * c->n;
+  size_t budget = (size_t)c->adjTapeBytes;
+  if (c->adjTapeBytes < 0) {
+    size_t fr = 0, tot = 0;
+    if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) {
+      cudaGetLastError();
+      return C;
+    }
+    fr += c->adj->segStates * state;   // a longer tape replaces the present one
+    budget = std::min(fr / 2, tot / 4);
+  }
+  const size_t fit = budget / state;   // states
+  if (fit < 3) return C;
+  return std::max(C, (int)std::min<size_t>((fit - 1) / 2, (size_t)K));
+}
+
 int reserve(hg_ctx* c, double** p, size_t* have, size_t states) {
   if (states <= *have) return HG_OK;
   cudaFree(*p);
@@ -237,7 +262,7 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
   const size_t n3 = (size_t)3 * N;
   const bool f64 = c->precision == HG_FP64;
   if (C <= 0) C = K;
-  C = std::min(C, K);
+  C = segment_length(c, K, std::min(C, K));
   const int nck = (K + C - 1) / C;
   // A double-sized state slot holds one FP32-compensated state too (24 B per cell either way).
   rc = reserve(c, &b->ckpt, &b->ckptStates, (size_t)nck);
@@ -383,10 +408,7 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
     }
     ADJ_CUDA(c, cudaMemcpyAsync(c->QA, Q0s + (size_t)(K - sLast) * n3, n3 * sizeof(double),
                                 cudaMemcpyDeviceToDevice, st));   // the final state
-    if (Qfinal) {
-      launch_scatter_state_f64(N, c->d_perm, c->QA, c->Quser, st);
-      ADJ_CUDA(c, cudaMemcpyAsync(Qfinal, c->Quser, n3 * sizeof(double), cudaMemcpyDeviceToHost, st));
-    }
+    if (Qfinal) launch_scatter_state_f64(N, c->d_perm, c->QA, c->Quser, st);   // copied out at the end
     // Reverse sweep.
     ADJ_CUDA(c, cudaMemsetAsync(b->mu2, 0, n3 * sizeof(double), st));
     launch_probe_adjoint_f64(dm, c->QA, b->mu2, b->probes, b->obs + (size_t)(K - 1) * P, P, scale, st);
@@ -511,10 +533,7 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
       c->launches += P > 0 ? 1 : 0;
     }
     ADJ_CUDA(c, copy_state(XA, sg.at(K - sLast, n)));   // the final state
-    if (Qfinal) {
-      launch_scatter_state_f32(N, c->d_perm, XA, c->Quser, st);
-      ADJ_CUDA(c, cudaMemcpyAsync(Qfinal, c->Quser, n3 * sizeof(double), cudaMemcpyDeviceToHost, st));
-    }
+    if (Qfinal) launch_scatter_state_f32(N, c->d_perm, XA, c->Quser, st);   // copied out at the end
     ADJ_CUDA(c, cudaMemsetAsync(mu2, 0, n3 * sizeof(float), st));
     launch_probe_adjoint_f32(dm, XA, mu2, pc, b->obs + (size_t)(K - 1) * P, scale, st);
     if (useFinal) {
@@ -557,19 +576,21 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
   launch_zb_gradient(dm, a, b->gzb, st);
   c->launches += 2;
   ADJ_CUDA(c, cudaGetLastError());
-  // Results, mapped back to the caller's cell order.
-  std::vector<double> hN(N), hZ(N), hQ(std::max(dm.nInlet, 1));
+  // Results, put in the caller's cell order on the device and copied out
+  // after the last kernel.
+  const bool direct = useFinal && fl.wse && !fo->zbw;   // WSE_pred = h + (active zb): dL/dzb += dL/dWSE
+  if (gManning) launch_scatter_field_f64(N, c->d_perm, a.gN, nullptr, b->userOut, st);
+  if (gZb) launch_scatter_field_f64(N, c->d_perm, b->gzb, direct ? fl.dWse : nullptr, b->userOut + N, st);
+  c->launches += (gManning ? 1 : 0) + (gZb ? 1 : 0);
   double hl = 0.0;
   ADJ_CUDA(c, cudaMemcpyAsync(&hl, a.loss, sizeof(double), cudaMemcpyDeviceToHost, st));
-  ADJ_CUDA(c, cudaMemcpyAsync(hN.data(), a.gN, N * sizeof(double), cudaMemcpyDeviceToHost, st));
-  ADJ_CUDA(c, cudaMemcpyAsync(hZ.data(), b->gzb, N * sizeof(double), cudaMemcpyDeviceToHost, st));
-  if (dm.nInlet > 0)
-    ADJ_CUDA(c, cudaMemcpyAsync(hQ.data(), a.gQ, dm.nInlet * sizeof(double), cudaMemcpyDeviceToHost, st));
+  if (gManning) ADJ_CUDA(c, cudaMemcpyAsync(gManning, b->userOut, N * sizeof(double), cudaMemcpyDeviceToHost, st));
+  if (gZb) ADJ_CUDA(c, cudaMemcpyAsync(gZb, b->userOut + N, N * sizeof(double), cudaMemcpyDeviceToHost, st));
+  if (gInlet && dm.nInlet > 0)
+    ADJ_CUDA(c, cudaMemcpyAsync(gInlet, a.gQ, dm.nInlet * sizeof(double), cudaMemcpyDeviceToHost, st));
+  if (Qfinal) ADJ_CUDA(c, cudaMemcpyAsync(Qfinal, c->Quser, n3 * sizeof(double), cudaMemcpyDeviceToHost, st));
   double fparts[2] = {0.0, 0.0};
-  const bool direct = useFinal && fl.wse && !fo->zbw;   // WSE_pred = h + (active zb): dL/dzb += dL/dWSE
-  std::vector<double> hW(direct ? N : 0);
   if (useFinal) ADJ_CUDA(c, cudaMemcpyAsync(fparts, fl.parts, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
-  if (direct) ADJ_CUDA(c, cudaMemcpyAsync(hW.data(), fl.dWse, N * sizeof(double), cudaMemcpyDeviceToHost, st));
   int32_t flags = 0;
   ADJ_CUDA(c, cudaMemcpyAsync(&flags, ds.flags, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
   ADJ_CUDA(c, cudaStreamSynchronize(st));
@@ -581,13 +602,6 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
     parts[1] = fparts[0];
     parts[2] = fparts[1];
   }
-  for (int i = 0; i < N; ++i) {
-    const int o = c->perm[i];
-    if (gManning) gManning[o] = hN[i];
-    if (gZb) gZb[o] = hZ[i] + (direct ? hW[i] : 0.0);
-  }
-  if (gInlet)
-    for (int g = 0; g < dm.nInlet; ++g) gInlet[g] = hQ[g];
   return HG_OK;
 }
 

@@ -1059,6 +1059,12 @@ int hg_time_stage_kernel(hg_ctx* ctx, int32_t n, int32_t flush_l2, double* avg_m
   return HG_OK;
 }
 
+int hg_set_adjoint_tape(hg_ctx* ctx, int64_t bytes) {
+  if (!ctx) return fail(ctx, HG_ERR_ARG, "hg_set_adjoint_tape: null context");
+  ctx->adjTapeBytes = bytes < 0 ? -1 : bytes;
+  return HG_OK;
+}
+
 int hg_loss_and_grad(hg_ctx* ctx, const double* Q0, int32_t nsteps, double dt, int32_t ckpt_every,
                      const int32_t* probe_cells, const double* obs, int32_t n_probe, double* loss,
                      double* g_manning_cells, double* g_zb, double* g_inletq, double* Q_final) {

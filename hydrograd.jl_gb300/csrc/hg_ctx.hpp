@@ -69,6 +69,9 @@ struct hg_ctx {
   bool stageTuned = false;          // hg_autotune has chosen dm.stageKernel
   int64_t launches = 0;
   hg::AdjointBuffers* adj = nullptr;
+  // Adjoint stage-state tape (hg_set_adjoint_tape): -1 automatic budget, 0 the
+  // caller's checkpoint spacing exactly, > 0 a budget in bytes.
+  int64_t adjTapeBytes = -1;
   // State-dependent resistance (hg_set_manning_function / hg_set_ude): device
   // buffers, allocated on first use; dm.res points into them.
   double *d_resKs = nullptr, *d_resW = nullptr, *d_resStats = nullptr, *d_resPartials = nullptr, *d_fres = nullptr;

@@ -649,6 +649,14 @@ __global__ void k_scatter_f64(int32_t n, const int32_t* __restrict__ perm, const
   user[2 * n + o] = dev[2 * n + i];
 }
 
+// One device-order field to the caller's order: user[perm[i]] = dev[i] (+ add[i]).
+__global__ void k_scatter_field_f64(int32_t n, const int32_t* __restrict__ perm, const double* __restrict__ dev,
+                                    const double* __restrict__ add, double* __restrict__ user) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  user[perm[i]] = add ? dev[i] + add[i] : dev[i];
+}
+
 __device__ __forceinline__ void split(double v, float& h, float& l) {
   h = (float)v;
   l = (float)(v - (double)h);
@@ -867,6 +875,10 @@ void launch_gather_state_f64(int32_t n, const int32_t* perm, const double* user,
 }
 void launch_scatter_state_f64(int32_t n, const int32_t* perm, const double* dev, double* user, cudaStream_t st) {
   k_scatter_f64<<<blocks_for(n), kBlock, 0, st>>>(n, perm, dev, user);
+}
+void launch_scatter_field_f64(int32_t n, const int32_t* perm, const double* dev, const double* add, double* user,
+                              cudaStream_t st) {
+  k_scatter_field_f64<<<blocks_for(n), kBlock, 0, st>>>(n, perm, dev, add, user);
 }
 void launch_gather_state_f32(int32_t n, const int32_t* perm, const double* user, StateF32 dev, cudaStream_t st) {
   k_gather_f32<<<blocks_for(n), kBlock, 0, st>>>(n, perm, user, dev);

@@ -200,6 +200,8 @@ void launch_reset_scalars(const DevScalars& s, cudaStream_t st);
 // Renumbering between the caller's order (user) and the device order.
 void launch_gather_state_f64(int32_t n, const int32_t* perm, const double* user, double* dev, cudaStream_t st);
 void launch_scatter_state_f64(int32_t n, const int32_t* perm, const double* dev, double* user, cudaStream_t st);
+void launch_scatter_field_f64(int32_t n, const int32_t* perm, const double* dev, const double* add, double* user,
+                              cudaStream_t st);
 void launch_gather_state_f32(int32_t n, const int32_t* perm, const double* user, StateF32 dev, cudaStream_t st);
 void launch_scatter_state_f32(int32_t n, const int32_t* perm, StateF32 dev, double* user, cudaStream_t st);
 // L2 flush over a buffer of `bytes` (> 2x L2): returns the launches made.

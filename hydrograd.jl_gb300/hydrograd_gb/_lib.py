@@ -98,6 +98,7 @@ SIGNATURES = {
                          _dp, _dp, _dp, _dp],
     "hg_launch_count": [_vp, ctypes.POINTER(ctypes.c_int64)],
     "hg_autotune": [_vp, ctypes.c_int32, _ip],
+    "hg_set_adjoint_tape": [_vp, ctypes.c_int64],
     "hg_time_stage_kernel": [_vp, ctypes.c_int32, ctypes.c_int32, _dp],
     "hg_flush_l2": [_vp],
     "hg_advance_timed": [_vp, ctypes.c_int32, ctypes.c_double, ctypes.c_double, ctypes.c_int32, _dp],

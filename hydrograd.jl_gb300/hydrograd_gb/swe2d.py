@@ -287,6 +287,14 @@ class SWE2D:
         self._chk(lib().hg_autotune(self.h, int(reps), _i(k)))
         return int(k[0])
 
+    def set_adjoint_tape(self, nbytes=-1):
+        """hg_set_adjoint_tape: memory for the adjoint's stage states.  -1 (the
+        default): segments as long as fit in min(half the free device memory,
+        a quarter of the device's), never shorter than ckpt_every; 0: exactly
+        ckpt_every steps per segment; > 0: a budget in bytes.  The gradients
+        do not depend on it."""
+        self._chk(lib().hg_set_adjoint_tape(self.h, int(nbytes)))
+
     def time_stage_kernel(self, n=10, flush_l2=True):
         ms = np.zeros(1)
         self._chk(lib().hg_time_stage_kernel(self.h, int(n), 1 if flush_l2 else 0, _d(ms)))

@@ -298,6 +298,17 @@ int hg_final_loss_and_grad(hg_ctx* ctx, const double* Q0, int32_t nsteps, double
                            const hg_final_obs* obs, double* parts, double* g_manning_cells, double* g_zb,
                            double* g_inletq, double* Q_final);
 
+/* Memory of the adjoint's stage-state tape.  The forward pass keeps a
+ * checkpoint every ckpt_every steps and the stage states of the last segment;
+ * the reverse sweep recomputes the other segments.  A longer segment means less
+ * recomputation (none when one segment holds all nsteps steps) for 2 states of
+ * 24 bytes per cell per step.  bytes < 0 (the default): segments as long as fit
+ * in min(half the free device memory, a quarter of the device's), never shorter
+ * than ckpt_every; 0: exactly ckpt_every; > 0: as long as fit in that many
+ * bytes, never shorter than ckpt_every.  The gradients do not depend on the
+ * segment length (the recomputation repeats the forward pass's arithmetic). */
+int hg_set_adjoint_tape(hg_ctx* ctx, int64_t bytes);
+
 /* ---- tuning ------------------------------------------------------------------ */
 /* Choose the kernel of the FP32-compensated fused stages for this mesh: each
  * kernel that can run it (0 gather: one block per 256-cell tile; 1 pipe:

@@ -81,6 +81,7 @@ def test_adjoint_matches_dual_numbers_river(ckpt):
     case = river()
     K = 40
     ctx, o, N, Q0, dt, probes, obs = setup_problem(case, K)
+    ctx.set_adjoint_tape(0)   # segments of exactly ckpt steps: the recomputation runs
     r = ctx.loss_and_grad(Q0, K, dt, probes, obs, ckpt_every=ckpt)
     nz = len(case["manning_zones"])
     dman = np.stack([(case["mat_id"] == z).astype(float) for z in range(nz)])
@@ -96,15 +97,29 @@ def test_adjoint_matches_dual_numbers_river(ckpt):
     assert abs(r["g_inletq"][0] - dl_q[0]) <= 1e-8 * abs(dl_q[0])
 
 
-def test_checkpoint_interval_does_not_change_the_gradient():
+@pytest.mark.parametrize("precision", ["fp64", "fp32c"])
+def test_checkpoint_interval_does_not_change_the_gradient(precision):
+    """Segments of 4 and 30 steps (with recomputation), a byte budget of 5
+    stage states (segments of 2, widened to the spacing of 4), and the
+    automatic tape (all 30 steps kept): the same loss, gradients and final
+    state, bit for bit."""
     case = river()
     K = 30
-    ctx, o, N, Q0, dt, probes, obs = setup_problem(case, K)
-    a = ctx.loss_and_grad(Q0, K, dt, probes, obs, ckpt_every=4)
-    b = ctx.loss_and_grad(Q0, K, dt, probes, obs, ckpt_every=30)
-    assert a["loss"] == b["loss"]
-    for k in ("g_manning", "g_zb", "g_inletq"):
-        assert np.array_equal(a[k], b[k])
+    _, o, N, Q0, dt, probes, obs = setup_problem(case, K)
+    ctx = SWE2D(case, precision=precision)
+    ctx.set_still_water(case["wstill"])
+    ctx.set_manning_zones(case["mat_id"], case["manning_zones"])
+    ctx.set_inlet_q(case["inlet_q"])
+    ctx.set_exit_wse(case["exit_wse"])
+    runs = []
+    for tape, ckpt in ((0, 4), (0, 30), (5 * 24 * N, 4), (-1, 4)):
+        ctx.set_adjoint_tape(tape)
+        runs.append(ctx.loss_and_grad(Q0, K, dt, probes, obs, ckpt_every=ckpt))
+    a = runs[0]
+    for b in runs[1:]:
+        assert a["loss"] == b["loss"]
+        for k in ("g_manning", "g_zb", "g_inletq", "Q"):
+            assert np.array_equal(a[k], b[k]), k
 
 
 def test_adjoint_vs_central_differences():
