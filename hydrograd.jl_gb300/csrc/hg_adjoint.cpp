@@ -50,12 +50,7 @@ struct AdjointBuffers {
   double* fin = nullptr;
   double* finScratch = nullptr;   // dWse [n], parts [2], partials [2 kFinalLossBlocks]
   unsigned int* finTicket = nullptr;
-  cudaStream_t side = nullptr;   // FP32C: the boundary VJP beside the interior one
-  cudaEvent_t evFork = nullptr, evJoin = nullptr;
   ~AdjointBuffers() {
-    if (evFork) cudaEventDestroy(evFork);
-    if (evJoin) cudaEventDestroy(evJoin);
-    if (side) cudaStreamDestroy(side);
     for (void* p : fixed) cudaFree(p);
     cudaFree(ckpt);
     cudaFree(seg);
@@ -194,9 +189,8 @@ int setup(hg_ctx* c) {
   a.bndInCoef = dBCoef;
   ADJ_CUDA(c, falloc(b, &a.bndG, (size_t)5 * bnd.size()));
   ADJ_CUDA(c, falloc(b, &a.grpTA, (size_t)c->dm.nInlet));
-  ADJ_CUDA(c, cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking));
-  ADJ_CUDA(c, cudaEventCreateWithFlags(&b->evFork, cudaEventDisableTiming));
-  ADJ_CUDA(c, cudaEventCreateWithFlags(&b->evJoin, cudaEventDisableTiming));
+  ADJ_CUDA(c, falloc(b, &a.tileTicket, 3));
+  ADJ_CUDA(c, cudaMemset(a.tileTicket, 0, 3 * sizeof(unsigned int)));
   return HG_OK;
 }
 
@@ -558,10 +552,9 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
         m1.totalA = T1 + i * stride;
         m0.totalA = T0 + i * stride;
         hydro((s + 1) * dt);
-        c->launches += launch_vjp_f32(m1, a, q1, mu2, nullptr, mu1, 0.5f, 0.0f, 0.5 * dt, st, b->side, b->evFork,
-                                      b->evJoin);
+        c->launches += launch_vjp_f32(m1, a, q1, mu2, nullptr, mu1, 0.5f, 0.0f, 0.5 * dt, st);
         hydro(s * dt);
-        c->launches += launch_vjp_f32(m0, a, q0, mu1, mu2, mu2, 1.0f, 0.5f, dt, st, b->side, b->evFork, b->evJoin);
+        c->launches += launch_vjp_f32(m0, a, q0, mu1, mu2, mu2, 1.0f, 0.5f, dt, st);
         if (s >= 1 && P > 0) {
           launch_probe_adjoint_f32(dm, q0, mu2, pc, b->obs + (size_t)(s - 1) * P, scale, st);
           c->launches += 1;

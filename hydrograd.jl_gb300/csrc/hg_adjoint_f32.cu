@@ -173,13 +173,22 @@ __device__ __forceinline__ void vjp_cell(const DevMesh& m, const AdjDev& a, int 
   out[2 * n + j] = mask * (cSelf * mj2 + cExtra * e2 + beta * g2);
 }
 
+// Programmatic dependent launch (griddepcontrol): the boundary VJP releases
+// the interior VJP as soon as it starts, so the interior's CTAs fill the SMs
+// beside the boundary blocks already resident; the interior waits for the
+// boundary grid (completion and memory) only before it exits, so the kernels
+// after it in the stream see both.  Without a prerequisite grid the wait
+// returns at once.
+__device__ __forceinline__ void pdl_release_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait_prerequisites() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 template <int NS>
 __global__ void __launch_bounds__(kBlock, vjp_min_blocks<NS>()) k_vjp_f32(DevMesh m, AdjDev a, StateF32 Q, const float* __restrict__ mu,
                                                     const float* __restrict__ extra, float* out, float cSelf,
                                                     float cExtra, float beta) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= m.n) return;
-  vjp_cell<NS>(m, a, j, GlobalSrc{m, Q, mu, extra, j}, out, cSelf, cExtra, beta);
+  if (j < m.n) vjp_cell<NS>(m, a, j, GlobalSrc{m, Q, mu, extra, j}, out, cSelf, cExtra, beta);
+  pdl_wait_prerequisites();
 }
 
 // Pipelined persistent VJP (the stage kernel's k_stage_pipe_f32 scheme): each
@@ -251,40 +260,95 @@ __device__ __forceinline__ void vjp_issue(const DevMesh& m, StateF32 Q, const fl
   }
 }
 
+// Tiles 0..G-1 go to the G CTAs in order, the rest to whichever CTA asks next
+// (a.tileTicket[0]): a CTA that starts late -- its SM still busy with the
+// boundary VJP beside it -- takes fewer tiles instead of finishing late.  Each
+// cell is still computed by one thread with the same arithmetic, so the
+// result does not depend on the assignment.
 template <int NS>
 __global__ void __launch_bounds__(kVTile, 2) k_vjp_pipe_f32(DevMesh m, AdjDev a, StateF32 Q, const float* mu,
                                                            const float* extra, float* out, float cSelf, float cExtra,
                                                            float beta) {
   using T = VjpTile<NS>;
   extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ int sNext[2];   // alternate slots: a slot is rewritten two barriers after its last read
   const int n = m.n, nTiles = (n + kVTile - 1) / kVTile, tid = threadIdx.x, G = gridDim.x;
   auto halo_id = [&](int t) { return (t < nTiles && tid < kHaloMax) ? m.halo[(size_t)t * kHaloMax + tid] : -1; };
-  int t = blockIdx.x;
-  if (t < nTiles) vjp_issue<NS>(m, Q, mu, extra, t, smem, halo_id(t));
+  auto take = [&] { return G + (int)atomicAdd(&a.tileTicket[0], 1u); };
+  // Tickets are taken two tiles ahead (thread 0 holds the one after next in
+  // `ahead`), so an atomic's round trip overlaps a tile's arithmetic.
+  int t = blockIdx.x;   // < nTiles: the grid is at most the tile count
+  int ahead = 0;
+  if (tid == 0) {
+    sNext[0] = take();
+    ahead = take();
+  }
+  vjp_issue<NS>(m, Q, mu, extra, t, smem, halo_id(t));
   cp_async_commit();
-  int hidNext = halo_id(t + G);
-  int b = 0;
-  for (; t < nTiles; t += G, b ^= 1) {
-    const int tn = t + G;
+  __syncthreads();
+  int tn = sNext[0];
+  int hidNext = halo_id(tn);
+  int b = 0, slot = 1;
+  while (t < nTiles) {
     if (tn < nTiles) vjp_issue<NS>(m, Q, mu, extra, tn, smem + (b ^ 1) * T::kBuf, hidNext);
     cp_async_commit();
-    hidNext = halo_id(tn + G);
+    if (tid == 0) sNext[slot] = ahead;
     cp_async_wait<1>();
     __syncthreads();
+    const int tnn = sNext[slot];
+    if (tid == 0) ahead = take();
+    hidNext = halo_id(tnn);
     const int j = t * kVTile + tid;
     if (j < n) vjp_cell<NS>(m, a, j, TileSrc<NS>{smem + b * T::kBuf, tid, extra != nullptr}, out, cSelf, cExtra, beta);
     __syncthreads();   // buffer b is refilled at the top of the next iteration
+    t = tn;
+    tn = tnn;
+    b ^= 1;
+    slot ^= 1;
   }
   cp_async_wait<0>();
+  if (tid == 0) {
+    __threadfence();   // this CTA's takes come before its finish count
+    if (atomicAdd(&a.tileTicket[1], 1u) == (unsigned)G - 1) {   // the last CTA out: every take is done
+      atomicExch(&a.tileTicket[0], 0u);
+      atomicExch(&a.tileTicket[1], 0u);
+    }
+  }
+  pdl_wait_prerequisites();
+}
+
+// Per inlet-Q group (one warp each): grpTA = sum over the group's faces of
+// the total_A cotangent, gQ += beta sum of the Q cotangent -- lanes stride
+// over the faces, a fixed shuffle tree adds them (deterministic).
+__device__ void inlet_group_sums(const DevMesh& m, const AdjDev& a, double betaD) {
+  const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  for (int g = threadIdx.x >> 5; g < m.nInlet; g += nw) {
+    double sTA = 0.0, sQ = 0.0;
+    for (int e = m.inletOff[g] + lane; e < m.inletOff[g + 1]; e += 32) {
+      const int bf = a.inletBf[e];
+      sTA += __ldcg(&a.bfGradTA[bf]);
+      sQ += __ldcg(&a.bfGradQ[bf]);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      sTA += __shfl_xor_sync(0xffffffffu, sTA, o);
+      sQ += __shfl_xor_sync(0xffffffffu, sQ, o);
+    }
+    if (lane == 0) {
+      a.grpTA[g] = sTA;
+      a.gQ[g] += betaD * sQ;
+    }
+  }
 }
 
 // Boundary faces of the cells that have any (one thread per such cell; runs
-// beside k_vjp_f32, which reads none of what it writes): ghost-state duals in
-// the own state, n, zb, Q and total_A.  Leaves the cell's terms in bndG and
-// the Q / total_A cotangents per boundary face (k_inlet_group_sums_f32).
+// beside the interior VJP, which reads none of what it writes): ghost-state
+// duals in the own state, n, zb, Q and total_A.  Leaves the cell's terms in
+// bndG and the Q / total_A cotangents per boundary face; the last block to
+// finish sums the latter per inlet group.
 template <int NS>
 __global__ void __launch_bounds__(64) k_vjp_bnd_f32(DevMesh m, AdjDev a, StateF32 Q, const float* __restrict__ mu,
                                                     double betaD) {
+  pdl_release_dependents();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < a.nBndCells) {
     const int j = a.bndCells[i];
@@ -328,28 +392,17 @@ __global__ void __launch_bounds__(64) k_vjp_bnd_f32(DevMesh m, AdjDev a, StateF3
     float* o = a.bndG + (size_t)5 * i;
     o[0] = g0; o[1] = g1; o[2] = g2; o[3] = gn; o[4] = gzb;
   }
-}
-
-// Per inlet-Q group (one warp each, after k_vjp_bnd_f32 on the side stream):
-// grpTA = sum over the group's faces of the total_A cotangent, gQ += beta sum
-// of the Q cotangent -- lanes stride over the faces, a fixed shuffle tree
-// adds them (deterministic).
-__global__ void __launch_bounds__(128) k_inlet_group_sums_f32(DevMesh m, AdjDev a, double betaD) {
-  const int g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-  if (g >= m.nInlet) return;
-  double sTA = 0.0, sQ = 0.0;
-  for (int e = m.inletOff[g] + lane; e < m.inletOff[g + 1]; e += 32) {
-    const int bf = a.inletBf[e];
-    sTA += a.bfGradTA[bf];
-    sQ += a.bfGradQ[bf];
-  }
-  for (int o = 16; o > 0; o >>= 1) {
-    sTA += __shfl_xor_sync(0xffffffffu, sTA, o);
-    sQ += __shfl_xor_sync(0xffffffffu, sQ, o);
-  }
-  if (lane == 0) {
-    a.grpTA[g] = sTA;
-    a.gQ[g] += betaD * sQ;
+  if (m.nInlet > 0) {
+    __shared__ bool last;
+    __threadfence();   // this block's face cotangents before its finish count
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(&a.tileTicket[2], 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (last) {
+      __threadfence();
+      inlet_group_sums(m, a, betaD);
+      if (threadIdx.x == 0) a.tileTicket[2] = 0u;
+    }
   }
 }
 
@@ -439,9 +492,25 @@ bool vjp_gather_forced() {
   return on;
 }
 
+template <int NS, class... Args>
+cudaError_t launch_pdl(bool pdl, void (*k)(Args...), int grid, int block, size_t smem, cudaStream_t st, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = pdl ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, k, args...);
+}
+
+// pdl: launched as the programmatic dependent of the boundary VJP just before it.
 template <int NS>
 void launch_vjp_interior(const DevMesh& m, const AdjDev& a, StateF32 Q, const float* mu, const float* extra,
-                         float* out, float cSelf, float cExtra, float beta, cudaStream_t st) {
+                         float* out, float cSelf, float cExtra, float beta, bool pdl, cudaStream_t st) {
   auto a16 = [](const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; };
   if constexpr (NS <= 4) {
     if (!vjp_gather_forced() && m.SLp && m.halo && a16(m.SLp) && a16(m.CP) && a16(m.CS) && a16(Q.x)) {
@@ -457,41 +526,34 @@ void launch_vjp_interior(const DevMesh& m, const AdjDev& a, StateF32 Q, const fl
         return (sms > 0 ? sms : 1) * per;
       }();
       const int tiles = (m.n + kVTile - 1) / kVTile;
-      k_vjp_pipe_f32<NS><<<tiles < grid ? tiles : grid, kVTile, T::kSmem, st>>>(m, a, Q, mu, extra, out, cSelf,
-                                                                               cExtra, beta);
+      launch_pdl<NS>(pdl, k_vjp_pipe_f32<NS>, tiles < grid ? tiles : grid, kVTile, T::kSmem, st, m, a, Q, mu, extra,
+                     out, cSelf, cExtra, beta);
       return;
     }
   }
-  k_vjp_f32<NS><<<blocks_for(m.n), kBlock, 0, st>>>(m, a, Q, mu, extra, out, cSelf, cExtra, beta);
+  launch_pdl<NS>(pdl, k_vjp_f32<NS>, blocks_for(m.n), kBlock, 0, st, m, a, Q, mu, extra, out, cSelf, cExtra, beta);
 }
 
+// The boundary VJP, then the interior VJP as its programmatic dependent (both
+// on the context's stream, running side by side), then the combine.
 template <int NS>
 int launch_vjp_ns(const DevMesh& m, const AdjDev& a, StateF32 Q, const float* mu, const float* extra, float* out,
-                  float cSelf, float cExtra, double betaD, cudaStream_t st, cudaStream_t side, cudaEvent_t evFork,
-                  cudaEvent_t evJoin) {
+                  float cSelf, float cExtra, double betaD, cudaStream_t st) {
   const float beta = (float)betaD;
   const int nbb = (a.nBndCells + 63) / 64;
-  if (nbb) {
-    cudaEventRecord(evFork, st);
-    cudaStreamWaitEvent(side, evFork, 0);
-    k_vjp_bnd_f32<NS><<<nbb, 64, 0, side>>>(m, a, Q, mu, betaD);
-    if (m.nInlet > 0) k_inlet_group_sums_f32<<<(m.nInlet + 3) / 4, 128, 0, side>>>(m, a, betaD);
-    cudaEventRecord(evJoin, side);
-  }
-  launch_vjp_interior<NS>(m, a, Q, mu, extra, out, cSelf, cExtra, beta, st);
+  if (nbb) k_vjp_bnd_f32<NS><<<nbb, 64, 0, st>>>(m, a, Q, mu, betaD);
+  launch_vjp_interior<NS>(m, a, Q, mu, extra, out, cSelf, cExtra, beta, nbb > 0, st);
   if (!nbb) return 1;
-  cudaStreamWaitEvent(st, evJoin, 0);
   k_vjp_combine_f32<<<(a.nBndCells + 127) / 128, 128, 0, st>>>(m, a, Q, out, beta, betaD);
-  return m.nInlet > 0 ? 4 : 3;
+  return 3;
 }
 }  // namespace
 
 int launch_vjp_f32(const DevMesh& m, const AdjDev& a, StateF32 Q, const float* mu, const float* extra, float* out,
-                   float cSelf, float cExtra, double betaD, cudaStream_t st, cudaStream_t side, cudaEvent_t evFork,
-                   cudaEvent_t evJoin) {
-  if (m.nslot <= 3) return launch_vjp_ns<3>(m, a, Q, mu, extra, out, cSelf, cExtra, betaD, st, side, evFork, evJoin);
-  if (m.nslot <= 4) return launch_vjp_ns<4>(m, a, Q, mu, extra, out, cSelf, cExtra, betaD, st, side, evFork, evJoin);
-  return launch_vjp_ns<8>(m, a, Q, mu, extra, out, cSelf, cExtra, betaD, st, side, evFork, evJoin);
+                   float cSelf, float cExtra, double betaD, cudaStream_t st) {
+  if (m.nslot <= 3) return launch_vjp_ns<3>(m, a, Q, mu, extra, out, cSelf, cExtra, betaD, st);
+  if (m.nslot <= 4) return launch_vjp_ns<4>(m, a, Q, mu, extra, out, cSelf, cExtra, betaD, st);
+  return launch_vjp_ns<8>(m, a, Q, mu, extra, out, cSelf, cExtra, betaD, st);
 }
 void launch_probe_loss_f32(const DevMesh& m, const AdjDev& a, StateF32 Q, const int32_t* probes, const double* obs,
                            int32_t nprobe, cudaStream_t st) {

@@ -37,6 +37,10 @@ struct AdjDev {
   const int32_t* bndInGrp = nullptr;
   const double* bndInCoef = nullptr;
   double* grpTA = nullptr;
+  // {interior VJP tiles handed out past the first wave, interior CTAs
+  // finished, boundary-VJP blocks finished}; zero between launches (the last
+  // CTA or block out resets its counters).
+  unsigned int* tileTicket = nullptr;
 };
 
 // out_j = M(Q_j) (cSelf mu_j + cExtra extra_j + beta (J(Q)^T mu)_j), parameter
@@ -52,13 +56,12 @@ void launch_probe_loss_f64(const DevMesh& m, const AdjDev& a, const double* Q, c
 void launch_probe_adjoint_f64(const DevMesh& m, const double* Q, double* mu, const int32_t* probes,
                               const double* obs, int32_t nprobe, double scale, cudaStream_t st);
 // FP32-compensated path: the same with packed FP32 states and FP32 cotangents.
-// The whole VJP of one stage, inlet-Q terms included: the interior kernel on
-// st, the boundary-face kernel on `side` at the same time (fork / join through
-// the two events), then the combine kernel on st.  beta = betaD as FP32.
+// The whole VJP of one stage, inlet-Q terms included, on st: the
+// boundary-face kernel, the interior kernel beside it (a programmatic
+// dependent launch), then the combine kernel.  beta = betaD as FP32.
 // Returns the launches made.
 int launch_vjp_f32(const DevMesh& m, const AdjDev& a, StateF32 Q, const float* mu, const float* extra, float* out,
-                   float cSelf, float cExtra, double betaD, cudaStream_t st, cudaStream_t side, cudaEvent_t evFork,
-                   cudaEvent_t evJoin);
+                   float cSelf, float cExtra, double betaD, cudaStream_t st);
 void launch_probe_loss_f32(const DevMesh& m, const AdjDev& a, StateF32 Q, const int32_t* probes, const double* obs,
                            int32_t nprobe, cudaStream_t st);
 // Probes grouped by cell: cell[u] (distinct, device order) holds probes idx[off[u] .. off[u+1]).
