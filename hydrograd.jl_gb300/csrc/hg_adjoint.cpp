@@ -257,7 +257,13 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
   const bool f64 = c->precision == HG_FP64;
   if (C <= 0) C = K;
   C = segment_length(c, K, std::min(C, K));
+  // Segments end at step K: the last one, whose stage states the forward
+  // pass keeps, is a full C steps; the first takes the remainder.  Segment g
+  // covers steps [seg_start(g), seg_start(g + 1)).
   const int nck = (K + C - 1) / C;
+  const int segOff = nck * C - K;   // 0 <= segOff < C
+  auto seg_start = [&](int g) { return std::min(K, std::max(0, g * C - segOff)); };
+  auto seg_of = [&](int s) { return (s + segOff) / C; };   // the segment holding step s
   // A double-sized state slot holds one FP32-compensated state too (24 B per cell either way).
   rc = reserve(c, &b->ckpt, &b->ckptStates, (size_t)nck);
   if (rc) return rc;
@@ -378,14 +384,14 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
     // Forward pass with checkpoints.  The last segment's steps write their
     // stage states straight into the segment buffer, which the reverse sweep
     // then starts from without recomputing them.
-    const int sLast = (nck - 1) * C;
+    const int sLast = seg_start(nck - 1);   // = K - C
     double* Q0s = b->seg;                          // Q0 of step s0 + i at Q0s + i n3 (i = 0..C)
     double* Q1s = b->seg + (size_t)(C + 1) * n3;   // Q1 of step s0 + i
     for (int s = 0; s < K; ++s) {
       const bool last = s >= sLast;
       const size_t i = (size_t)(s - sLast);
-      if (s % C == 0 && !last)
-        ADJ_CUDA(c, cudaMemcpyAsync(b->ckpt + (size_t)(s / C) * n3, c->QA, n3 * sizeof(double),
+      if (!last && s == seg_start(seg_of(s)))
+        ADJ_CUDA(c, cudaMemcpyAsync(b->ckpt + (size_t)seg_of(s) * n3, c->QA, n3 * sizeof(double),
                                     cudaMemcpyDeviceToDevice, st));
       if (s == sLast) ADJ_CUDA(c, cudaMemcpyAsync(Q0s, c->QA, n3 * sizeof(double), cudaMemcpyDeviceToDevice, st));
       const double* q0 = last ? Q0s + i * n3 : c->QA;
@@ -411,7 +417,7 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
       c->launches += 1;
     }
     for (int seg = nck - 1; seg >= 0; --seg) {
-      const int s0 = seg * C, s1 = std::min(K, s0 + C);
+      const int s0 = seg_start(seg), s1 = seg_start(seg + 1);
       if (seg < nck - 1)   // the last segment's states are in place from the forward pass
         ADJ_CUDA(c, cudaMemcpyAsync(Q0s, b->ckpt + (size_t)seg * n3, n3 * sizeof(double), cudaMemcpyDeviceToDevice,
                                     st));
@@ -510,11 +516,11 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
     // Forward pass with checkpoints (totals ping-pong in T0[0] / T0[1]).  The
     // last segment's steps write their stage states and totals straight into
     // the segment buffers, which the reverse sweep starts from.
-    const int sLast = (nck - 1) * C;
+    const int sLast = seg_start(nck - 1);   // = K - C
     totals(XA, T0);
     for (int s = 0; s < K; ++s) {
       if (s < sLast) {
-        if (s % C == 0) ADJ_CUDA(c, copy_state(ck.at(s / C, n), XA));
+        if (s == seg_start(seg_of(s))) ADJ_CUDA(c, copy_state(ck.at(seg_of(s), n), XA));
         step(s, XA, XB, XA, T0, T0 + stride, T0);
         launch_probe_loss_f32(dm, a, XA, b->probes, b->obs + (size_t)s * P, P, st);
       } else {
@@ -535,7 +541,7 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
       c->launches += 1;
     }
     for (int seg = nck - 1; seg >= 0; --seg) {
-      const int s0 = seg * C, s1 = std::min(K, s0 + C);
+      const int s0 = seg_start(seg), s1 = seg_start(seg + 1);
       if (seg < nck - 1) {   // the last segment's states and totals are in place from the forward pass
         ADJ_CUDA(c, copy_state(sg.at(0, n), ck.at(seg, n)));
         totals(sg.at(0, n), T0);

@@ -18,6 +18,7 @@
 #include "hg_device.cuh"
 #include "hg_dual.cuh"
 #include "hg_f32.cuh"
+#include "hg_pdl.cuh"
 #include "hg_reduce.cuh"
 #include "hg_wet_vjp.cuh"
 
@@ -173,19 +174,18 @@ __device__ __forceinline__ void vjp_cell(const DevMesh& m, const AdjDev& a, int 
   out[2 * n + j] = mask * (cSelf * mj2 + cExtra * e2 + beta * g2);
 }
 
-// Programmatic dependent launch (griddepcontrol): the boundary VJP releases
-// the interior VJP as soon as it starts, so the interior's CTAs fill the SMs
-// beside the boundary blocks already resident; the interior waits for the
-// boundary grid (completion and memory) only before it exits, so the kernels
-// after it in the stream see both.  Without a prerequisite grid the wait
-// returns at once.
-__device__ __forceinline__ void pdl_release_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
-__device__ __forceinline__ void pdl_wait_prerequisites() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+// The interior VJP runs as the programmatic dependent of the boundary VJP
+// (hg_pdl.cuh): the boundary kernel waits for the kernels before it and then
+// releases the interior one, whose CTAs fill the SMs beside the boundary
+// blocks already resident; the interior waits for the boundary grid only
+// before it exits (it reads nothing the boundary kernel writes), so the
+// kernels after it see both.
 
 template <int NS>
 __global__ void __launch_bounds__(kBlock, vjp_min_blocks<NS>()) k_vjp_f32(DevMesh m, AdjDev a, StateF32 Q, const float* __restrict__ mu,
                                                     const float* __restrict__ extra, float* out, float cSelf,
                                                     float cExtra, float beta) {
+  pdl_release_dependents();
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j < m.n) vjp_cell<NS>(m, a, j, GlobalSrc{m, Q, mu, extra, j}, out, cSelf, cExtra, beta);
   pdl_wait_prerequisites();
@@ -277,6 +277,7 @@ __global__ void __launch_bounds__(kVTile, 2) k_vjp_pipe_f32(DevMesh m, AdjDev a,
   auto take = [&] { return G + (int)atomicAdd(&a.tileTicket[0], 1u); };
   // Tickets are taken two tiles ahead (thread 0 holds the one after next in
   // `ahead`), so an atomic's round trip overlaps a tile's arithmetic.
+  pdl_release_dependents();
   int t = blockIdx.x;   // < nTiles: the grid is at most the tile count
   int ahead = 0;
   if (tid == 0) {
@@ -348,7 +349,7 @@ __device__ void inlet_group_sums(const DevMesh& m, const AdjDev& a, double betaD
 template <int NS>
 __global__ void __launch_bounds__(64) k_vjp_bnd_f32(DevMesh m, AdjDev a, StateF32 Q, const float* __restrict__ mu,
                                                     double betaD) {
-  pdl_release_dependents();
+  pdl_enter();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < a.nBndCells) {
     const int j = a.bndCells[i];
@@ -411,6 +412,7 @@ __global__ void __launch_bounds__(64) k_vjp_bnd_f32(DevMesh m, AdjDev a, StateF3
 // total_A = sum L^(5/3) h / n over the group's wet cells) into out and gN.
 __global__ void __launch_bounds__(128) k_vjp_combine_f32(DevMesh m, AdjDev a, StateF32 Q, float* out, float beta,
                                                          double betaD) {
+  pdl_enter();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.nBndCells) return;
   const int j = a.bndCells[i];
@@ -441,6 +443,7 @@ __device__ __forceinline__ double depth_f64(const DevMesh& m, StateF32 Q, int c)
 __global__ void __launch_bounds__(256) k_probe_loss_f32(DevMesh m, AdjDev a, StateF32 Q,
                                                         const int32_t* __restrict__ probes,
                                                         const double* __restrict__ obs, int np) {
+  pdl_enter();
   double s = 0.0;
   for (int p = threadIdx.x; p < np; p += blockDim.x) {
     const double e = depth_f64(m, Q, probes[p]) - obs[p];
@@ -454,6 +457,7 @@ __global__ void __launch_bounds__(256) k_probe_loss_f32(DevMesh m, AdjDev a, Sta
 // c (in probe order) of scale 2 (h - obs_p), when c is wet.
 __global__ void k_probe_adjoint_f32(DevMesh m, StateF32 Q, float* mu, ProbeCsr pc, const double* __restrict__ obs,
                                     double scale) {
+  pdl_enter();
   const int u = blockIdx.x * blockDim.x + threadIdx.x;
   if (u >= pc.nCells) return;
   const int c = pc.cell[u];
@@ -492,21 +496,6 @@ bool vjp_gather_forced() {
   return on;
 }
 
-template <int NS, class... Args>
-cudaError_t launch_pdl(bool pdl, void (*k)(Args...), int grid, int block, size_t smem, cudaStream_t st, Args... args) {
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(grid);
-  cfg.blockDim = dim3(block);
-  cfg.dynamicSmemBytes = smem;
-  cfg.stream = st;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  attr[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = pdl ? 1 : 0;
-  return cudaLaunchKernelEx(&cfg, k, args...);
-}
-
 // pdl: launched as the programmatic dependent of the boundary VJP just before it.
 template <int NS>
 void launch_vjp_interior(const DevMesh& m, const AdjDev& a, StateF32 Q, const float* mu, const float* extra,
@@ -526,12 +515,12 @@ void launch_vjp_interior(const DevMesh& m, const AdjDev& a, StateF32 Q, const fl
         return (sms > 0 ? sms : 1) * per;
       }();
       const int tiles = (m.n + kVTile - 1) / kVTile;
-      launch_pdl<NS>(pdl, k_vjp_pipe_f32<NS>, tiles < grid ? tiles : grid, kVTile, T::kSmem, st, m, a, Q, mu, extra,
-                     out, cSelf, cExtra, beta);
+      launch_k(pdl, k_vjp_pipe_f32<NS>, tiles < grid ? tiles : grid, kVTile, T::kSmem, st, m, a, Q, mu, extra, out,
+               cSelf, cExtra, beta);
       return;
     }
   }
-  launch_pdl<NS>(pdl, k_vjp_f32<NS>, blocks_for(m.n), kBlock, 0, st, m, a, Q, mu, extra, out, cSelf, cExtra, beta);
+  launch_k(pdl, k_vjp_f32<NS>, blocks_for(m.n), kBlock, 0, st, m, a, Q, mu, extra, out, cSelf, cExtra, beta);
 }
 
 // The boundary VJP, then the interior VJP as its programmatic dependent (both
@@ -541,10 +530,10 @@ int launch_vjp_ns(const DevMesh& m, const AdjDev& a, StateF32 Q, const float* mu
                   float cSelf, float cExtra, double betaD, cudaStream_t st) {
   const float beta = (float)betaD;
   const int nbb = (a.nBndCells + 63) / 64;
-  if (nbb) k_vjp_bnd_f32<NS><<<nbb, 64, 0, st>>>(m, a, Q, mu, betaD);
+  if (nbb) launch_k(true, k_vjp_bnd_f32<NS>, nbb, 64, 0, st, m, a, Q, mu, betaD);
   launch_vjp_interior<NS>(m, a, Q, mu, extra, out, cSelf, cExtra, beta, nbb > 0, st);
   if (!nbb) return 1;
-  k_vjp_combine_f32<<<(a.nBndCells + 127) / 128, 128, 0, st>>>(m, a, Q, out, beta, betaD);
+  launch_k(true, k_vjp_combine_f32, (a.nBndCells + 127) / 128, 128, 0, st, m, a, Q, out, beta, betaD);
   return 3;
 }
 }  // namespace
@@ -557,11 +546,11 @@ int launch_vjp_f32(const DevMesh& m, const AdjDev& a, StateF32 Q, const float* m
 }
 void launch_probe_loss_f32(const DevMesh& m, const AdjDev& a, StateF32 Q, const int32_t* probes, const double* obs,
                            int32_t nprobe, cudaStream_t st) {
-  if (nprobe > 0) k_probe_loss_f32<<<1, 256, 0, st>>>(m, a, Q, probes, obs, nprobe);
+  if (nprobe > 0) launch_k(true, k_probe_loss_f32, 1, 256, 0, st, m, a, Q, probes, obs, nprobe);
 }
 void launch_probe_adjoint_f32(const DevMesh& m, StateF32 Q, float* mu, const ProbeCsr& pc, const double* obs,
                               double scale, cudaStream_t st) {
-  if (pc.nCells > 0) k_probe_adjoint_f32<<<(pc.nCells + 127) / 128, 128, 0, st>>>(m, Q, mu, pc, obs, scale);
+  if (pc.nCells > 0) launch_k(true, k_probe_adjoint_f32, (pc.nCells + 127) / 128, 128, 0, st, m, Q, mu, pc, obs, scale);
 }
 void launch_fold_accumulators_f32(const DevMesh& m, const AdjDev& a, cudaStream_t st) {
   k_fold_accumulators_f32<<<blocks_for(m.n), kBlock, 0, st>>>(m, a);

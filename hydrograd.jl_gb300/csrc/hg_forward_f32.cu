@@ -17,6 +17,7 @@
 #include "hg_async.cuh"
 #include "hg_device.cuh"
 #include "hg_f32.cuh"
+#include "hg_pdl.cuh"
 #include "hg_reduce.cuh"
 #include "hg_state.hpp"
 #include "hg_tma.cuh"
@@ -301,6 +302,7 @@ template <int NS, bool FUSED, int MODE>
 __global__ void __launch_bounds__(kBlock, stage_min_blocks<NS>())
     k_stage_f32(DevMesh m, DevScalars s, StateF32 Xin, StateF32 Xbase, StateF32 Xout, double* Rout, int cfl,
                 StageFuse f) {
+  pdl_enter();
   const int base = blockIdx.x * kBlock;
   const int c = base + threadIdx.x;
   const bool active = c < m.n;
@@ -382,6 +384,7 @@ __device__ __forceinline__ void tma_issue_tile(const DevMesh& m, StateF32 Xin, S
 template <int NS, int MODE>
 __global__ void __launch_bounds__(kBlock, kTmaCtasPerSm)
     k_stage_tma_f32(DevMesh m, DevScalars s, StateF32 Xin, StateF32 Xbase, StateF32 Xout, int cfl, StageFuse f) {
+  pdl_enter();
   using T = TmaTile<NS, MODE>;
   extern __shared__ __align__(128) unsigned char smem[];
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem + 2 * T::kBuf);
@@ -517,6 +520,7 @@ __device__ __forceinline__ void pipe_issue(const DevMesh& m, StateF32 Xin, State
 template <int NS, int MODE, bool FUSED>
 __global__ void __launch_bounds__(kBlock, kPipeCtasPerSm)
     k_stage_pipe_f32(DevMesh m, DevScalars s, StateF32 Xin, StateF32 Xbase, StateF32 Xout, int cfl, StageFuse f) {
+  pdl_enter();
   using T = PipeTile<NS, MODE>;
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ float dtShared;
@@ -713,12 +717,14 @@ void launch_stage_ns(const DevMesh& m, const DevScalars& s, int mode, StateF32 X
                      double* Rout, int cfl, const StageFuse& f, cudaStream_t st) {
   const int nb = blocks_for(m.n);
   if (mode == kModeStage1) {
-    k_stage_f32<NS, FUSED, kModeStage1><<<nb, kBlock, 0, st>>>(m, s, Xin, Xbase, Xout, Rout, cfl, f);
+    launch_k(true, k_stage_f32<NS, FUSED, kModeStage1>, nb, kBlock, 0, st, m, s, Xin, Xbase, Xout, Rout, cfl, f);
   } else if (mode == kModeStage2) {
-    k_stage_f32<NS, FUSED, kModeStage2><<<nb, kBlock, 0, st>>>(m, s, Xin, Xbase, Xout, Rout, cfl, f);
+    launch_k(true, k_stage_f32<NS, FUSED, kModeStage2>, nb, kBlock, 0, st, m, s, Xin, Xbase, Xout, Rout, cfl, f);
   } else if constexpr (!FUSED) {
-    if (mode == kModeRhs) k_stage_f32<NS, false, kModeRhs><<<nb, kBlock, 0, st>>>(m, s, Xin, Xbase, Xout, Rout, cfl, f);
-    else k_stage_f32<NS, false, kModeEulerRef><<<nb, kBlock, 0, st>>>(m, s, Xin, Xbase, Xout, Rout, cfl, f);
+    if (mode == kModeRhs)
+      launch_k(true, k_stage_f32<NS, false, kModeRhs>, nb, kBlock, 0, st, m, s, Xin, Xbase, Xout, Rout, cfl, f);
+    else
+      launch_k(true, k_stage_f32<NS, false, kModeEulerRef>, nb, kBlock, 0, st, m, s, Xin, Xbase, Xout, Rout, cfl, f);
   }
 }
 }  // namespace
@@ -768,7 +774,8 @@ void launch_tma(const DevMesh& m, const DevScalars& s, StateF32 Xin, StateF32 Xb
   (void)attr;
   static const int grid = sm_count() * kTmaCtasPerSm;
   const int tiles = blocks_for(m.n);
-  k_stage_tma_f32<NS, MODE><<<tiles < grid ? tiles : grid, kBlock, T::kSmem, st>>>(m, s, Xin, Xbase, Xout, cfl, fu);
+  launch_k(true, k_stage_tma_f32<NS, MODE>, tiles < grid ? tiles : grid, kBlock, T::kSmem, st, m, s, Xin, Xbase, Xout,
+           cfl, fu);
 }
 
 template <int NS, int MODE, bool FUSED>
@@ -783,8 +790,8 @@ void launch_pipe(const DevMesh& m, const DevScalars& s, StateF32 Xin, StateF32 X
   (void)attr;
   static const int grid = sm_count() * resident_ctas(k_stage_pipe_f32<NS, MODE, FUSED>, T::kSmem);
   const int tiles = blocks_for(m.n);
-  k_stage_pipe_f32<NS, MODE, FUSED><<<tiles < grid ? tiles : grid, kBlock, T::kSmem, st>>>(m, s, Xin, Xbase, Xout,
-                                                                                            cfl, fu);
+  launch_k(true, k_stage_pipe_f32<NS, MODE, FUSED>, tiles < grid ? tiles : grid, kBlock, T::kSmem, st, m, s, Xin,
+           Xbase, Xout, cfl, fu);
 }
 
 template <int NS, bool FUSED = true>
