@@ -529,7 +529,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--adj-steps", type=int, default=100, help="steps of the forward+adjoint measurement (0: skip)")
     ap.add_argument("--ens-steps", type=int, default=1000, help="ensemble (configuration 4) forward steps (0: skip)")
-    ap.add_argument("--ens-adj-steps", type=int, default=200, help="ensemble forward+adjoint steps (0: skip)")
+    ap.add_argument("--ens-adj-steps", type=int, default=1000,
+                    help="ensemble (configuration 4) forward+adjoint steps (0: skip)")
     ap.add_argument("--ens-ckpt", type=int, default=25)
     ap.add_argument("--ens-members", type=int, default=32, help="members per mesh")
     ap.add_argument("--config5-steps", type=int, default=5000,

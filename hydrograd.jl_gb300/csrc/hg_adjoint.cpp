@@ -522,20 +522,20 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
       if (s < sLast) {
         if (s == seg_start(seg_of(s))) ADJ_CUDA(c, copy_state(ck.at(seg_of(s), n), XA));
         step(s, XA, XB, XA, T0, T0 + stride, T0);
-        launch_probe_loss_f32(dm, a, XA, b->probes, b->obs + (size_t)s * P, P, st);
       } else {
         const size_t i = (size_t)(s - sLast);
         if (s == sLast) ADJ_CUDA(c, copy_state(sg.at(0, n), XA));   // its totals are in T0 already
         step(s, sg.at(i, n), sg.at(C + 1 + i, n), sg.at(i + 1, n), T0 + i * stride, T1 + i * stride,
              T0 + (i + 1) * stride);
-        launch_probe_loss_f32(dm, a, sg.at(i + 1, n), b->probes, b->obs + (size_t)s * P, P, st);
       }
-      c->launches += P > 0 ? 1 : 0;
     }
     ADJ_CUDA(c, copy_state(XA, sg.at(K - sLast, n)));   // the final state
     if (Qfinal) launch_scatter_state_f32(N, c->d_perm, XA, c->Quser, st);   // copied out at the end
     ADJ_CUDA(c, cudaMemsetAsync(mu2, 0, n3 * sizeof(float), st));
-    launch_probe_adjoint_f32(dm, XA, mu2, pc, b->obs + (size_t)(K - 1) * P, scale, st);
+    // The probe loss of each state after step s and its seed, in one kernel
+    // in the reverse sweep (the state after the last step first).
+    launch_probe_f32(dm, a, XA, mu2, pc, b->probes, b->obs + (size_t)(K - 1) * P, P, scale, st);
+    c->launches += P > 0 ? 1 : 0;
     if (useFinal) {
       launch_final_loss_f32(dm, fl, XA, mu2, st);
       c->launches += 1;
@@ -562,7 +562,7 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
         hydro(s * dt);
         c->launches += launch_vjp_f32(m0, a, q0, mu1, mu2, mu2, 1.0f, 0.5f, dt, st);
         if (s >= 1 && P > 0) {
-          launch_probe_adjoint_f32(dm, q0, mu2, pc, b->obs + (size_t)(s - 1) * P, scale, st);
+          launch_probe_f32(dm, a, q0, mu2, pc, b->probes, b->obs + (size_t)(s - 1) * P, P, scale, st);
           c->launches += 1;
         }
       }

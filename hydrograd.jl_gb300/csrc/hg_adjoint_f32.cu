@@ -440,10 +440,25 @@ __device__ __forceinline__ double depth_f64(const DevMesh& m, StateF32 Q, int c)
   return ((double)x.x + (double)x.y) + ((double)cp.x + (double)cp.y);
 }
 
-__global__ void __launch_bounds__(256) k_probe_loss_f32(DevMesh m, AdjDev a, StateF32 Q,
-                                                        const int32_t* __restrict__ probes,
-                                                        const double* __restrict__ obs, int np) {
+// The probe terms of a state Q of the run, in the reverse sweep: its loss
+// sum over the probes p of (h - obs_p)^2 into a.loss (one block, a
+// fixed-order reduction), and the seed mu_xi[c] += sum over the probes at c
+// (in probe order) of scale 2 (h - obs_p) at each distinct probe cell c that
+// is wet.
+__global__ void __launch_bounds__(256) k_probe_f32(DevMesh m, AdjDev a, StateF32 Q, float* mu, ProbeCsr pc,
+                                                   const int32_t* __restrict__ probes,
+                                                   const double* __restrict__ obs, int np, double scale) {
   pdl_enter();
+  for (int u = threadIdx.x; u < pc.nCells; u += blockDim.x) {
+    const int c = pc.cell[u];
+    const float4 cp = m.CP[c];
+    const SideF32 L = make_side_f32(Q.x[c], cp, m.hsmf, m.hsmLo);
+    if (L.s.dry) continue;
+    const double h = depth_f64(m, Q, c);
+    double acc = 0.0;
+    for (int i = pc.off[u]; i < pc.off[u + 1]; ++i) acc += scale * 2.0 * (h - obs[pc.idx[i]]);
+    mu[c] += (float)acc;
+  }
   double s = 0.0;
   for (int p = threadIdx.x; p < np; p += blockDim.x) {
     const double e = depth_f64(m, Q, probes[p]) - obs[p];
@@ -451,23 +466,6 @@ __global__ void __launch_bounds__(256) k_probe_loss_f32(DevMesh m, AdjDev a, Sta
   }
   const double t = block_sum(s);
   if (threadIdx.x == 0) a.loss[0] += t;
-}
-
-// One thread per distinct probe cell u: mu_xi[c] += sum over the probes p at
-// c (in probe order) of scale 2 (h - obs_p), when c is wet.
-__global__ void k_probe_adjoint_f32(DevMesh m, StateF32 Q, float* mu, ProbeCsr pc, const double* __restrict__ obs,
-                                    double scale) {
-  pdl_enter();
-  const int u = blockIdx.x * blockDim.x + threadIdx.x;
-  if (u >= pc.nCells) return;
-  const int c = pc.cell[u];
-  const float4 cp = m.CP[c];
-  const SideF32 L = make_side_f32(Q.x[c], cp, m.hsmf, m.hsmLo);
-  if (L.s.dry) return;
-  const double h = depth_f64(m, Q, c);
-  double acc = 0.0;
-  for (int i = pc.off[u]; i < pc.off[u + 1]; ++i) acc += scale * 2.0 * (h - obs[pc.idx[i]]);
-  mu[c] += (float)acc;
 }
 
 __global__ void k_fold_accumulators_f32(DevMesh m, AdjDev a) {
@@ -544,13 +542,9 @@ int launch_vjp_f32(const DevMesh& m, const AdjDev& a, StateF32 Q, const float* m
   if (m.nslot <= 4) return launch_vjp_ns<4>(m, a, Q, mu, extra, out, cSelf, cExtra, betaD, st);
   return launch_vjp_ns<8>(m, a, Q, mu, extra, out, cSelf, cExtra, betaD, st);
 }
-void launch_probe_loss_f32(const DevMesh& m, const AdjDev& a, StateF32 Q, const int32_t* probes, const double* obs,
-                           int32_t nprobe, cudaStream_t st) {
-  if (nprobe > 0) launch_k(true, k_probe_loss_f32, 1, 256, 0, st, m, a, Q, probes, obs, nprobe);
-}
-void launch_probe_adjoint_f32(const DevMesh& m, StateF32 Q, float* mu, const ProbeCsr& pc, const double* obs,
-                              double scale, cudaStream_t st) {
-  if (pc.nCells > 0) launch_k(true, k_probe_adjoint_f32, (pc.nCells + 127) / 128, 128, 0, st, m, Q, mu, pc, obs, scale);
+void launch_probe_f32(const DevMesh& m, const AdjDev& a, StateF32 Q, float* mu, const ProbeCsr& pc,
+                      const int32_t* probes, const double* obs, int32_t nprobe, double scale, cudaStream_t st) {
+  if (nprobe > 0) launch_k(true, k_probe_f32, 1, 256, 0, st, m, a, Q, mu, pc, probes, obs, nprobe, scale);
 }
 void launch_fold_accumulators_f32(const DevMesh& m, const AdjDev& a, cudaStream_t st) {
   k_fold_accumulators_f32<<<blocks_for(m.n), kBlock, 0, st>>>(m, a);

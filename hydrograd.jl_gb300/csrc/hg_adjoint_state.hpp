@@ -62,8 +62,6 @@ void launch_probe_adjoint_f64(const DevMesh& m, const double* Q, double* mu, con
 // Returns the launches made.
 int launch_vjp_f32(const DevMesh& m, const AdjDev& a, StateF32 Q, const float* mu, const float* extra, float* out,
                    float cSelf, float cExtra, double betaD, cudaStream_t st);
-void launch_probe_loss_f32(const DevMesh& m, const AdjDev& a, StateF32 Q, const int32_t* probes, const double* obs,
-                           int32_t nprobe, cudaStream_t st);
 // Probes grouped by cell: cell[u] (distinct, device order) holds probes idx[off[u] .. off[u+1]).
 struct ProbeCsr {
   const int32_t* cell = nullptr;
@@ -71,8 +69,9 @@ struct ProbeCsr {
   const int32_t* idx = nullptr;
   int32_t nCells = 0;
 };
-void launch_probe_adjoint_f32(const DevMesh& m, StateF32 Q, float* mu, const ProbeCsr& pc, const double* obs,
-                              double scale, cudaStream_t st);
+// The probe loss of state Q (into a.loss) and its seed into mu (one kernel).
+void launch_probe_f32(const DevMesh& m, const AdjDev& a, StateF32 Q, float* mu, const ProbeCsr& pc,
+                      const int32_t* probes, const double* obs, int32_t nprobe, double scale, cudaStream_t st);
 // Final-state inversion loss (swe_2D_inversion.jl:383-431), device order:
 //   WSE term  sum_c ((h_c + zbw_c - wse_c) / wseDen)^2 / n,  h = xi + hstill
 //   uv term   sum_c ((qx_c / (h_c + eps) - u_c)^2 + (qy_c / (h_c + eps) - v_c)^2) / velScale^2 / n
