@@ -252,6 +252,8 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
   if (rc) return rc;
   AdjointBuffers* b = c->adj;
   AdjDev& a = b->dev;
+  a.wantN = gManning ? 1 : 0;   // the FP32C VJP skips the accumulators of gradients not asked for
+  a.wantZb = gZb ? 1 : 0;
   const int N = c->n;
   const size_t n3 = (size_t)3 * N;
   const bool f64 = c->precision == HG_FP64;
@@ -572,8 +574,10 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
     launch_fold_accumulators_f32(dm, a, st);
     c->launches += 1;
   }
-  launch_zb_gradient(dm, a, b->gzb, st);
-  c->launches += 2;
+  if (gZb) {
+    launch_zb_gradient(dm, a, b->gzb, st);
+    c->launches += 2;
+  }
   ADJ_CUDA(c, cudaGetLastError());
   // Results, put in the caller's cell order on the device and copied out
   // after the last kernel.

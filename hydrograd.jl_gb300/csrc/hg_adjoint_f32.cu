@@ -163,10 +163,12 @@ __device__ __forceinline__ void vjp_cell(const DevMesh& m, const AdjDev& a, int 
     g1 += mj1 * (-k - hu * dkdqx) + mj2 * (-hv * dkdqx);
     g2 += mj1 * (-hu * dkdqy) + mj2 * (-k - hv * dkdqy);
     gn += -(mj1 * hu + mj2 * hv) * dkdn;
-    acc_add(&a.accF[(size_t)n + j], beta, mj1 * m.gf * L.s.xi);
-    acc_add(&a.accF[(size_t)2 * n + j], beta, mj2 * m.gf * L.s.xi);
+    if (a.wantZb) {
+      acc_add(&a.accF[(size_t)n + j], beta, mj1 * m.gf * L.s.xi);
+      acc_add(&a.accF[(size_t)2 * n + j], beta, mj2 * m.gf * L.s.xi);
+    }
   }
-  if (gn != 0.0f) acc_add(&a.accF[j], beta, gn);
+  if (a.wantN && gn != 0.0f) acc_add(&a.accF[j], beta, gn);
   const float mask = L.s.dry ? 0.0f : 1.0f;
   const float e0 = src.extra_own(0), e1 = src.extra_own(1), e2 = src.extra_own(2);
   out[j] = mask * (cSelf * mj0 + cExtra * e0 + beta * g0);
@@ -420,8 +422,8 @@ __global__ void __launch_bounds__(128) k_vjp_combine_f32(DevMesh m, AdjDev a, St
   const float4 cp = m.CP[j];
   const SideF32 L = make_side_f32(Q.x[j], cp, m.hsmf, m.hsmLo);
   const float* g = a.bndG + (size_t)5 * i;
-  if (g[3] != 0.0f) acc_add(&a.accF[j], beta, g[3]);
-  if (g[4] != 0.0f) acc_add(&a.accF[(size_t)3 * n + j], beta, g[4]);
+  if (a.wantN && g[3] != 0.0f) acc_add(&a.accF[j], beta, g[3]);
+  if (a.wantZb && g[4] != 0.0f) acc_add(&a.accF[(size_t)3 * n + j], beta, g[4]);
   if (L.s.dry) return;
   out[j] += beta * g[0];
   out[n + j] += beta * g[1];
@@ -430,7 +432,7 @@ __global__ void __launch_bounds__(128) k_vjp_combine_f32(DevMesh m, AdjDev a, St
     const double gTA = a.grpTA[a.bndInGrp[p]];
     const double coef = a.bndInCoef[p], nm = cp.w;
     out[j] += (float)(betaD * gTA * coef / nm);
-    a.gN[j] += betaD * gTA * (-coef * (double)L.s.h / (nm * nm));
+    if (a.wantN) a.gN[j] += betaD * gTA * (-coef * (double)L.s.h / (nm * nm));
   }
 }
 

@@ -41,6 +41,9 @@ struct AdjDev {
   // finished, boundary-VJP blocks finished}; zero between launches (the last
   // CTA or block out resets its counters).
   unsigned int* tileTicket = nullptr;
+  // The gradients the caller asked for: the FP32C VJP accumulates the n or
+  // the bed (S0, exit-H) terms only when wanted.
+  int32_t wantN = 1, wantZb = 1;
 };
 
 // out_j = M(Q_j) (cSelf mu_j + cExtra extra_j + beta (J(Q)^T mu)_j), parameter

@@ -174,9 +174,11 @@ class Inversion:
         theta = np.asarray(theta, dtype=np.float64)
         self.apply(theta)
         zb_wse = None if s.active_param == "zb" else o["zb_cell_truth"]
+        want = {"ManningN": ("manning",), "zb": ("zb",), "Q": ("inletq",)}[s.active_param]
         r = self.ctx.final_loss_and_grad(self.Q0, self.nsteps, self.dt, wse=o["WSE_truth"] if s.wse_loss else None,
                                          u=o["u_truth"] if s.uv_loss else None,
-                                         v=o["v_truth"] if s.uv_loss else None, zb_wse=zb_wse, ckpt_every=self.ckpt)
+                                         v=o["v_truth"] if s.uv_loss else None, zb_wse=zb_wse, ckpt_every=self.ckpt,
+                                         want=want)
         if s.active_param == "ManningN":
             g = np.bincount(self.mat_id, r["g_manning"], minlength=len(theta))
         elif s.active_param == "zb":

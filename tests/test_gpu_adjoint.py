@@ -122,6 +122,28 @@ def test_checkpoint_interval_does_not_change_the_gradient(precision):
             assert np.array_equal(a[k], b[k]), k
 
 
+@pytest.mark.parametrize("precision", ["fp64", "fp32c"])
+def test_partial_gradient_requests_match(precision):
+    """Asking for one gradient (the others NULL at the C-ABI) gives that
+    gradient, the loss and the final state bit for bit as asking for all."""
+    case = river()
+    K = 20
+    _, o, N, Q0, dt, probes, obs = setup_problem(case, K)
+    ctx = SWE2D(case, precision=precision)
+    ctx.set_still_water(case["wstill"])
+    ctx.set_manning_zones(case["mat_id"], case["manning_zones"])
+    ctx.set_inlet_q(case["inlet_q"])
+    ctx.set_exit_wse(case["exit_wse"])
+    full = ctx.loss_and_grad(Q0, K, dt, probes, obs, ckpt_every=5)
+    for want, key in ((("manning",), "g_manning"), (("zb",), "g_zb"), (("inletq",), "g_inletq")):
+        r = ctx.loss_and_grad(Q0, K, dt, probes, obs, ckpt_every=5, want=want)
+        assert r["loss"] == full["loss"]
+        assert np.array_equal(r["Q"], full["Q"])
+        assert np.array_equal(r[key], full[key]), key
+        for other in {"g_manning", "g_zb", "g_inletq"} - {key}:
+            assert r[other] is None
+
+
 def test_adjoint_vs_central_differences():
     """Central finite differences of the oracle loss, eps = 1e-6 (FP64)."""
     case = river()
