@@ -229,6 +229,60 @@ def run_reference(args):
     }))
 
 
+def run_config1(args, device, cpu):
+    """Configuration 1 (hydrograd_gb.workloads.dam_break): 200 x 40 quads
+    (8,000 cells) over 100 x 20 m, flat bed, walls, n = 0.03, h = 1.0 / 0.5 m
+    either side of x = 50 m; config1_steps SSP-RK2 steps of dt = 0.01 s.  FP64
+    and FP32C device rates (the steps replayed from captured CUDA graphs: at
+    8,000 cells a step is launch-bound); with cpu (rank 0, unless --no-cpu),
+    the oracle's rate on the host cores (the CPU baseline of this
+    configuration) and both device states against the oracle's after the same
+    steps."""
+    from hydrograd_gb import SWE2D
+    from hydrograd_gb.workloads import dam_break
+    case = dam_break()
+    N = len(case["cell_node_count"])
+    K, dt = args.config1_steps, 0.01
+    out = {"cells": N, "steps": K, "dt": dt}
+    states = {}
+    for prec in ("fp64", "fp32c"):
+        c = SWE2D(case, precision=prec, device=device)
+        c.set_still_water(case["wstill"])
+        c.set_manning_zones(case["mat_id"], case["manning_zones"])
+        c.upload(case["Q0"])
+        c.advance(max(args.warmup, 50), dt=dt)
+        c.upload(case["Q0"])
+        c.synchronize()
+        t0 = time.perf_counter()
+        c.advance(K, dt=dt)
+        c.synchronize()
+        el = time.perf_counter() - t0
+        states[prec] = c.download()
+        out[prec] = {"value": N * K / el, "seconds": el}
+        c.close()
+    if cpu:
+        from oracle.oracle import Oracle
+        o = Oracle(case)
+        o.set_wstill(case["wstill"])
+        o.set_manning_cells(case["manning_zones"][case["mat_id"]])
+        threads = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        ref = o.rk2(case["Q0"], K, dt=dt, nthreads=threads)
+        el = time.perf_counter() - t0
+        out["cpu_oracle"] = {"value": N * K / el, "seconds": el, "cores": threads, "kind": "port"}
+        # max |error| / max |state| over the whole state; and per block (xi, qx, qy) over
+        # max(|block|, 1e-3 |state|) -- the dam break moves along x, so its qy block is
+        # rounding noise and takes the floor
+        for prec in ("fp64", "fp32c"):
+            out[prec + "_vs_oracle_state_rel_linf"] = float(np.abs(states[prec] - ref).max() / np.abs(ref).max())
+            out[prec + "_vs_oracle_block_rel_linf"] = [float(
+                np.abs(states[prec][j * N:(j + 1) * N] - ref[j * N:(j + 1) * N]).max()
+                / max(np.abs(ref[j * N:(j + 1) * N]).max(), 1e-3 * np.abs(ref).max(), 1e-300)) for j in range(3)]
+    out["config"] = ("configuration 1: 200 x 40 quads (8,000 cells), flat bed, walls, n = 0.03, dam break "
+                     "h = 1.0 / 0.5 m at x = 50 m, SSP-RK2 dt = 0.01 s")
+    return out
+
+
 def run_config5(args, device):
     """Configuration 5 (hydrograd_gb.workloads.meander_mixed): 4.0 M mixed
     cells, a meandering channel, per-cell n, the inlet hydrograph 200 -> 2,000
@@ -454,6 +508,7 @@ def run_ours(args):
                          "widened by the automatic stage-state tape (all steps kept where they fit in HBM), "
                          f"{len(probes)} probes (half on the pool rim, half at the inlet), loss = mean squared "
                          "departure of the probe depths from the lake at rest")
+    cfg1 = run_config1(args, local, cpu=not args.no_cpu and rank == 0) if args.config1_steps > 0 else None
     cfg5 = run_config5(args, local) if args.config5_steps > 0 else None
     ens = None
     if args.ens_steps > 0:
@@ -502,6 +557,7 @@ def run_ours(args):
         "fp32c_over_fp64_speedup": f32["value"] / out["fp64"]["value"],
         "fwd_adjoint": adj,
         "ensemble": ens,
+        "config1": cfg1,
         "config5": cfg5,
         "warm_value": f32["warm_value"], "simulated_seconds": f32["sim_time"],
         "error": err,
@@ -533,6 +589,8 @@ def main():
                     help="ensemble (configuration 4) forward+adjoint steps (0: skip)")
     ap.add_argument("--ens-ckpt", type=int, default=25)
     ap.add_argument("--ens-members", type=int, default=32, help="members per mesh")
+    ap.add_argument("--config1-steps", type=int, default=1000,
+                    help="configuration 1 (8,000-cell dam break) steps at dt = 0.01 s (0: skip)")
     ap.add_argument("--config5-steps", type=int, default=5000,
                     help="configuration 5 (4 M mixed cells, hydrograph) forward and forward+adjoint steps (0: skip)")
     ap.add_argument("--config5-err-steps", type=int, default=200,

@@ -255,7 +255,9 @@ __global__ void __launch_bounds__(256) k_zb_gradient(DevMesh m, AdjDev a, double
 
 void launch_vjp_f64(const DevMesh& m, const AdjDev& a, const double* Q, const double* mu, const double* extra,
                     double* out, double cSelf, double cExtra, double beta, cudaStream_t st) {
-  k_vjp_f64<<<blocks_for(m.n), kBlock, 0, st>>>(m, a, Q, mu, extra, out, cSelf, cExtra, beta);
+  // at most the kernel's launch bound; a cell's result does not depend on its block
+  const int bs = stage_block_f64(m.n) < kBlock ? stage_block_f64(m.n) : kBlock;
+  k_vjp_f64<<<(m.n + bs - 1) / bs, bs, 0, st>>>(m, a, Q, mu, extra, out, cSelf, cExtra, beta);
 }
 void launch_inlet_adjoint_f64(const DevMesh& m, const AdjDev& a, const double* Q, double* out, double beta,
                               cudaStream_t st) {

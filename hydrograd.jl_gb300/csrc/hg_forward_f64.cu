@@ -259,9 +259,26 @@ void launch_inlet_total_f64(const DevMesh& m, const DevScalars& s, const double*
   launch_resistance_f64(m, Q, st);
   if (m.nInlet > 0) k_inlet_total_f64<<<m.nInlet, kBlock, 0, st>>>(m, s, Q);
 }
+// Block size of the FP64 stage: 256 threads, halved (down to one warp) while
+// the grid would give fewer than 4 blocks per SM -- on a small mesh the
+// FP64-bound kernel then spreads over every SM instead of a few.  A cell's
+// result does not depend on the block it runs in (the CFL minimum is exact).
+int stage_block_f64(int n) {
+  static const int sms = [] {
+    int dev = 0, v = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    return v > 0 ? v : 1;
+  }();
+  int bs = kBlock;
+  while (bs > 32 && (n + bs - 1) / bs < 4 * sms) bs /= 2;
+  return bs;
+}
+
 void launch_stage_f64(const DevMesh& m, const DevScalars& s, int mode, const double* Qin, const double* Qbase,
                       double* Qout, bool cfl, cudaStream_t st) {
-  k_stage_f64<<<blocks_for(m.n), kBlock, 0, st>>>(m, s, mode, Qin, Qbase, Qout, cfl ? 1 : 0);
+  const int bs = stage_block_f64(m.n);
+  k_stage_f64<<<(m.n + bs - 1) / bs, bs, 0, st>>>(m, s, mode, Qin, Qbase, Qout, cfl ? 1 : 0);
 }
 void launch_cfl_f64(const DevMesh& m, const DevScalars& s, const double* Q, cudaStream_t st) {
   k_cfl_f64<<<blocks_for(m.n), kBlock, 0, st>>>(m, s, Q);

@@ -199,6 +199,8 @@ void launch_reset_scalars(const DevScalars& s, cudaStream_t st);
 
 // Renumbering between the caller's order (user) and the device order.
 void launch_gather_state_f64(int32_t n, const int32_t* perm, const double* user, double* dev, cudaStream_t st);
+// Block size of per-cell FP64 kernels on an n-cell mesh (256, smaller on small meshes).
+int stage_block_f64(int n);
 void launch_scatter_state_f64(int32_t n, const int32_t* perm, const double* dev, double* user, cudaStream_t st);
 void launch_scatter_field_f64(int32_t n, const int32_t* perm, const double* dev, const double* add, double* user,
                               cudaStream_t st);
