@@ -272,10 +272,13 @@ int hg_elapsed_time(hg_ctx* ctx, double* t);
 /*
  * Loss = mean over steps k = 1..nsteps and probes p of (h_p^k - obs[k][p])^2,
  * h = xi + hstill, for nsteps fixed-dt SSP-RK2 steps from Q0.  Gradients by a
- * discrete adjoint with checkpoints every ckpt_every steps and recomputation.
- * g_manning_cells [n] (dL/dn per cell; zone gradients are sums over a zone's
- * cells), g_zb [n] (dL/dzb_cells through S0, ghost and exit-H values), g_inletq
- * [n_inletq].  Any gradient output may be NULL.  Q_final (host, 3n) may be NULL.
+ * discrete adjoint with checkpoints every ckpt_every steps (at least; see
+ * hg_set_adjoint_tape) and recomputation.  g_manning_cells [n] (dL/dn per
+ * cell; zone gradients are sums over a zone's cells), g_zb [n] (dL/dzb_cells
+ * through S0, ghost and exit-H values), g_inletq [n_inletq].  Any gradient
+ * output may be NULL: the FP32-compensated sweep then skips that gradient's
+ * accumulation (the others are unchanged, bit for bit).  Q_final (host, 3n)
+ * may be NULL.
  */
 int hg_loss_and_grad(hg_ctx* ctx, const double* Q0, int32_t nsteps, double dt, int32_t ckpt_every,
                      const int32_t* probe_cells, const double* obs, int32_t n_probe, double* loss,
