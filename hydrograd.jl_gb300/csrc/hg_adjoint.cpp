@@ -608,6 +608,16 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
   return HG_OK;
 }
 
+void adjoint_release_tape(hg_ctx* ctx) {
+  AdjointBuffers* b = ctx->adj;
+  if (!b) return;
+  cudaStreamSynchronize(ctx->stream);
+  cudaFree(b->seg);
+  cudaFree(b->ckpt);
+  b->seg = b->ckpt = nullptr;
+  b->segStates = b->ckptStates = 0;
+}
+
 void adjoint_release(hg_ctx* ctx) {
   delete ctx->adj;
   ctx->adj = nullptr;

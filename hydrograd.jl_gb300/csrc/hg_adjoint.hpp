@@ -25,5 +25,7 @@ int adjoint_loss_and_grad(hg_ctx* ctx, const double* Q0, int32_t nsteps, double 
                           double* g_manning_cells, double* g_zb, double* g_inletq, double* Q_final,
                           const FinalObs* fo = nullptr, double* parts = nullptr);
 void adjoint_release(hg_ctx* ctx);
+// Free the stage-state tape and checkpoint buffers (the next gradient call allocates what it needs).
+void adjoint_release_tape(hg_ctx* ctx);
 
 }  // namespace hg

@@ -1061,7 +1061,9 @@ int hg_time_stage_kernel(hg_ctx* ctx, int32_t n, int32_t flush_l2, double* avg_m
 
 int hg_set_adjoint_tape(hg_ctx* ctx, int64_t bytes) {
   if (!ctx) return fail(ctx, HG_ERR_ARG, "hg_set_adjoint_tape: null context");
+  cudaSetDevice(ctx->device);
   ctx->adjTapeBytes = bytes < 0 ? -1 : bytes;
+  adjoint_release_tape(ctx);
   return HG_OK;
 }
 

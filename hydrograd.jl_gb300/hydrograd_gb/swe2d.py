@@ -292,7 +292,7 @@ class SWE2D:
         default): segments as long as fit in min(half the free device memory,
         a quarter of the device's), never shorter than ckpt_every; 0: exactly
         ckpt_every steps per segment; > 0: a budget in bytes.  The gradients
-        do not depend on it."""
+        do not depend on it.  Also frees the tape this context holds."""
         self._chk(lib().hg_set_adjoint_tape(self.h, int(nbytes)))
 
     def time_stage_kernel(self, n=10, flush_l2=True):

@@ -309,7 +309,9 @@ int hg_final_loss_and_grad(hg_ctx* ctx, const double* Q0, int32_t nsteps, double
  * in min(half the free device memory, a quarter of the device's), never shorter
  * than ckpt_every; 0: exactly ckpt_every; > 0: as long as fit in that many
  * bytes, never shorter than ckpt_every.  The gradients do not depend on the
- * segment length (the recomputation repeats the forward pass's arithmetic). */
+ * segment length (the recomputation repeats the forward pass's arithmetic).
+ * The call also frees the tape the context holds from earlier gradient calls;
+ * the next one allocates what it needs. */
 int hg_set_adjoint_tape(hg_ctx* ctx, int64_t bytes);
 
 /* ---- tuning ------------------------------------------------------------------ */
