@@ -411,10 +411,74 @@ inline void roe_flux(T xiL, T hstillL, T hL, T huL, T hvL, T zbL, T xiR, T hstil
 }
 
 // ---------------------------------------------------------------------------
+// HLL flux -- new: the reference's RiemannSolver "HLL" raises an error
+// (semi_discretize_swe_2D.jl:356-357), so this follows the published scheme:
+// Harten, Lax & van Leer (1983), with Einfeldt's (1988) wave-speed estimates
+// S_L = min(un_L - c_L, un_Roe - c_Roe), S_R = max(un_R + c_R, un_Roe + c_Roe).
+// It works on the same variables as roe_flux -- the pre-balanced pressure
+// 0.5 g (xi^2 + 2 xi hstill) and the xi jump in the continuity component, so a
+// lake at rest (xi = 0, q = 0) has zero flux -- and takes roe_flux's dry, wall
+// and one-side-dry branches unchanged; only the wet-wet flux differs:
+//   F = F_L (S_L >= 0),  F_R (S_R <= 0),
+//   else (S_R F_L - S_L F_R + S_L S_R (U_R - U_L)) / (S_R - S_L).
+// ---------------------------------------------------------------------------
+template <class T>
+inline void hll_flux(T xiL, T hstillL, T hL, T huL, T hvL, T zbL, T xiR, T hstillR, T hR, T huR, T hvR, T zbR,
+                     double g, double nx, double ny, double hmin, T out[3]) {
+  if (value(hL) <= hmin && value(hR) <= hmin) {                          // roe_flux's branches
+    out[0] = T(0.0); out[1] = T(0.0); out[2] = T(0.0);
+    return;
+  } else if (value(hL + zbL) < value(zbR + hmin) && value(hR) <= hmin) {
+    hR = hL; huR = -huL; hvR = -hvL;
+  } else if (value(hR + zbR) < value(zbL + hmin) && value(hL) <= hmin) {
+    hL = hR; huL = -huR; hvL = -hvR;
+  } else if (value(hL) <= hmin) {
+    T p = 0.5 * g * smooth_pow2(hR);
+    out[0] = huR * nx + hvR * ny;
+    out[1] = (huR * (huR / hR) + p) * nx + huR * (hvR / hR) * ny;
+    out[2] = (hvR * (huR / hR)) * nx + (hvR * (hvR / hR) + p) * ny;
+    return;
+  } else if (value(hR) <= hmin) {
+    T p = 0.5 * g * smooth_pow2(hL);
+    out[0] = huL * nx + hvL * ny;
+    out[1] = (huL * (huL / hL) + p) * nx + huL * (hvL / hL) * ny;
+    out[2] = (hvL * (huL / hL)) * nx + (hvL * (hvL / hL) + p) * ny;
+    return;
+  }
+  T uL = huL / hL, vL = hvL / hL, uR = huR / hR, vR = hvR / hR;
+  T sqrt_hL = smooth_sqrt(hL), sqrt_hR = smooth_sqrt(hR);
+  T hRoe = (hL + hR) / 2.0;
+  T uRoe = (sqrt_hL * uL + sqrt_hR * uR) / (sqrt_hL + sqrt_hR);
+  T vRoe = (sqrt_hL * vL + sqrt_hR * vR) / (sqrt_hL + sqrt_hR);
+  T unRoe = uRoe * nx + vRoe * ny;
+  T cRoe = smooth_sqrt(g * hRoe);
+  T unL = uL * nx + vL * ny, unR = uR * nx + vR * ny;
+  T cL = smooth_sqrt(g * hL), cR = smooth_sqrt(g * hR);
+  T sL1 = unL - cL, sL2 = unRoe - cRoe, sR1 = unR + cR, sR2 = unRoe + cRoe;
+  T sL = value(sL1) <= value(sL2) ? sL1 : sL2;
+  T sR = value(sR1) >= value(sR2) ? sR1 : sR2;
+  T pL = 0.5 * g * (smooth_pow2(xiL) + 2.0 * xiL * hstillL);
+  T pR = 0.5 * g * (smooth_pow2(xiR) + 2.0 * xiR * hstillR);
+  T fL[3] = {huL * nx + hvL * ny, (huL * uL + pL) * nx + huL * vL * ny, (hvL * uL) * nx + (hvL * vL + pL) * ny};
+  T fR[3] = {huR * nx + hvR * ny, (huR * uR + pR) * nx + huR * vR * ny, (hvR * uR) * nx + (hvR * vR + pR) * ny};
+  if (value(sL) >= 0.0) {
+    for (int k = 0; k < 3; ++k) out[k] = fL[k];
+  } else if (value(sR) <= 0.0) {
+    for (int k = 0; k < 3; ++k) out[k] = fR[k];
+  } else {
+    T d[3] = {xiR - xiL, huR - huL, hvR - hvL};
+    T den = sR - sL;
+    for (int k = 0; k < 3; ++k) out[k] = (sR * fL[k] - sL * fR[k] + sL * sR * d[k]) / den;
+  }
+}
+
+// ---------------------------------------------------------------------------
 // The RHS (src/fvm/discretization/semi_discretize_swe_2D.jl:18-277).
 // ---------------------------------------------------------------------------
+enum Riemann : int { RIEMANN_ROE = 0, RIEMANN_HLL = 1 };
 struct Consts {
   double g = 9.81, k_n = 1.0, h_small = 1.0e-3;   // solve_swe_2D.jl:51-107
+  int riemann = RIEMANN_ROE;                      // swe_2D_constants.jl:16 RiemannSolver ("Roe"; "HLL" new)
 };
 
 // ---------------------------------------------------------------------------
@@ -733,8 +797,12 @@ void rhs(const Case& cs, const Params<T>& p, const T* Q, T* dQ, int nthreads = 1
         xiR = xig[r]; hstR = T(cs.hstillGhost[r]); hR = hg[r]; huR = qxg[r]; hvR = qyg[r]; zbR = p.bed.zbGhost[r];
       }
       T F[3];
-      roe_flux<T>(Q[c], T(cs.hstill[c]), h[c], qx[c], qy[c], p.zbCells[c], xiR, hstR, hR, huR, hvR, zbR, g, nx, ny,
-                  hs, F);
+      if (cs.k.riemann == RIEMANN_HLL)
+        hll_flux<T>(Q[c], T(cs.hstill[c]), h[c], qx[c], qy[c], p.zbCells[c], xiR, hstR, hR, huR, hvR, zbR, g, nx,
+                    ny, hs, F);
+      else
+        roe_flux<T>(Q[c], T(cs.hstill[c]), h[c], qx[c], qy[c], p.zbCells[c], xiR, hstR, hR, huR, hvR, zbR, g, nx,
+                    ny, hs, F);
       double L = m.faceLengths[f];
       fs0 = fs0 + F[0] * L;                                              // :387
       fs1 = fs1 + F[1] * L;

@@ -50,6 +50,7 @@ def _load():
     lib.ho_tsit5.argtypes = [ctypes.c_void_p, _dp, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                              ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int, _ip]
     lib.ho_set_hydrograph.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, _dp, _dp]
+    lib.ho_set_riemann.argtypes = [ctypes.c_void_p, ctypes.c_int]
     lib.ho_set_resistance_fn.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp, _dp]
     lib.ho_set_ude.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, _ip, _ip, _dp, ctypes.c_int,
                                ctypes.c_double, ctypes.c_double, _dp, _dp, _dp, _dp, ctypes.c_int]
@@ -195,6 +196,14 @@ class Oracle:
         if rc != 0:
             raise RuntimeError("oracle: " + self.lib.ho_last_error().decode())
         return Q, tuple(int(v) for v in st)
+
+    def set_riemann_solver(self, name):
+        """Riemann solver of the faces: "Roe" (the reference's) or "HLL" (hgo::hll_flux)."""
+        kinds = {"Roe": 0, "HLL": 1}
+        if name not in kinds:
+            raise ValueError("Riemann solver: Roe or HLL")
+        if self.lib.ho_set_riemann(self.h, kinds[name]) != 0:
+            raise RuntimeError("oracle: " + self.lib.ho_last_error().decode())
 
     def set_hydrograph(self, group, t, q):
         """Inlet-Q hydrograph of one group (hgo::hydro_at); empty t removes it."""

@@ -218,7 +218,17 @@ int ho_rhs(void* h, const double* Q, double* dQ, int nthreads) {
   return 0;
 }
 
-// Manning friction terms from given h, q (compute_friction_terms, semi_discretize_swe_2D.jl:544-547).
+// Riemann solver of the faces: 0 Roe (swe_2D_solvers.jl:4-164), 1 HLL (hgo::hll_flux).
+int ho_set_riemann(void* h, int kind) {
+  auto* oc = static_cast<OracleCase*>(h);
+  if (kind != RIEMANN_ROE && kind != RIEMANN_HLL) {
+    g_err = "ho_set_riemann: 0 (Roe) or 1 (HLL)";
+    return 1;
+  }
+  oc->cs.k.riemann = kind;
+  return 0;
+}
+
 // Inlet-Q hydrograph of group g (hgo::hydro_at); n = 0 removes it.
 int ho_set_hydrograph(void* h, int g, int n, const double* t, const double* q) {
   auto* oc = static_cast<OracleCase*>(h);
