@@ -134,14 +134,14 @@ __device__ __forceinline__ void vjp_cell(const DevMesh& m, const AdjDev& a, int 
       const float w0 = len * (r.m0 / An - mj0 / Aj);
       const float w1 = len * (r.m1 / An - mj1 / Aj);
       const float w2 = len * (r.m2 / An - mj2 / Aj);
-      if (!R.s.dry) {
+      if (!R.s.dry && m.riemann == kRiemannRoe) {
         roe_wet_vjp<float>(L.s, o, R.s, (R.s.xi - L.s.xi) + (R.xlo - L.xlo), m.gf, nx, ny, w0, w1, w2, b);
       } else {
         const Side<F3> L3 = seeded<F3>(L.s, -1);
         const Side<F3> R3 = constant<F3>(R.s);
         const F3 dxi = (R3.xi - L3.xi) + F3(R.xlo - L.xlo);
         F3 F[3];
-        roe_flux<F3>(L3, R3, dxi, F3(m.gf), F3(nx), F3(ny), F3(m.hsmf), F);
+        riemann_flux<F3>(m.riemann, L3, R3, dxi, F3(m.gf), F3(nx), F3(ny), F3(m.hsmf), F);
         g0 += w0 * F[0].d[0] + w1 * F[1].d[0] + w2 * F[2].d[0];
         g1 += w0 * F[0].d[1] + w1 * F[1].d[1] + w2 * F[2].d[1];
         g2 += w0 * F[0].d[2] + w1 * F[1].d[2] + w2 * F[2].d[2];
@@ -382,7 +382,7 @@ __global__ void __launch_bounds__(64) k_vjp_bnd_f32(DevMesh m, AdjDev a, StateF3
       F7 dxi = (R7.h - L7.h) + ex;
       if (type == kBcExitH && !R7.dry) dxi.v = m.bfExitRel[bf] - (L.s.xi + L.xlo);   // as the forward pass
       F7 F[3];
-      roe_flux<F7>(L7, R7, dxi, F7(m.gf), F7(nx), F7(ny), F7(m.hsmf), F);
+      riemann_flux<F7>(m.riemann, L7, R7, dxi, F7(m.gf), F7(nx), F7(ny), F7(m.hsmf), F);
       float c[7];
 #pragma unroll
       for (int d = 0; d < 7; ++d) c[d] = w0 * F[0].d[d] + w1 * F[1].d[d] + w2 * F[2].d[d];

@@ -96,13 +96,13 @@ __global__ void __launch_bounds__(kBlock) k_vjp_f64(DevMesh m, AdjDev a, const d
       const double w0 = len * (mu[nb] / An - mj0 / Aj);
       const double w1 = len * (mu[n + nb] / An - mj1 / Aj);
       const double w2 = len * (mu[2 * n + nb] / An - mj2 / Aj);
-      if (wetL && !R.dry) {
+      if (wetL && !R.dry && m.riemann == kRiemannRoe) {
         roe_wet_vjp<double>(L, own, R, R.xi - L.xi, m.g, nx, ny, w0, w1, w2, bo);
         continue;
       }
       const Side<D3> R3 = constant<D3>(R);
       D3 F[3];
-      roe_flux<D3>(L3, R3, R3.xi - L3.xi, D3(m.g), D3(nx), D3(ny), D3(m.hsm), F);
+      riemann_flux<D3>(m.riemann, L3, R3, R3.xi - L3.xi, D3(m.g), D3(nx), D3(ny), D3(m.hsm), F);
 #pragma unroll
       for (int d = 0; d < 3; ++d) {
         const double c = w0 * F[0].d[d] + w1 * F[1].d[d] + w2 * F[2].d[d];
@@ -119,7 +119,7 @@ __global__ void __launch_bounds__(kBlock) k_vjp_f64(DevMesh m, AdjDev a, const d
       const Side<D7> R7 = ghost_state<D7>(L7, type, D7(nx), D7(ny), D7(m.hsm),
                                           D7(type == kBcExitH ? m.exitWse[grp] : 0.0), qin, ta, D7(m.bfLp23[bf]), man);
       D7 F[3];
-      roe_flux<D7>(L7, R7, R7.xi - L7.xi, D7(m.g), D7(nx), D7(ny), D7(m.hsm), F);
+      riemann_flux<D7>(m.riemann, L7, R7, R7.xi - L7.xi, D7(m.g), D7(nx), D7(ny), D7(m.hsm), F);
       double c[7];
 #pragma unroll
       for (int d = 0; d < 7; ++d) c[d] = w0 * F[0].d[d] + w1 * F[1].d[d] + w2 * F[2].d[d];

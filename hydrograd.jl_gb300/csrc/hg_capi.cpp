@@ -501,9 +501,11 @@ namespace {
 // Checks shared by hg_create and hg_ensemble_create.
 int check_create_args(const hg_consts* consts, int32_t precision, int32_t device, const char* who) {
   if (precision != HG_FP64 && precision != HG_FP32C) return fail(nullptr, HG_ERR_ARG, std::string(who) + ": bad precision");
-  if (consts->riemann != HG_ROE)
+  if (consts->riemann == HG_HLLC)
     return fail(nullptr, HG_ERR_UNSUPPORTED,
-                std::string(who) + ": only the Roe solver exists (semi_discretize_swe_2D.jl:352-362)");
+                std::string(who) + ": HLLC solver not implemented (as in semi_discretize_swe_2D.jl:358-359)");
+  if (consts->riemann != HG_ROE && consts->riemann != HG_HLL)
+    return fail(nullptr, HG_ERR_ARG, std::string(who) + ": bad Riemann solver");
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0)
     return fail(nullptr, HG_ERR_NO_DEVICE, std::string(who) + ": no CUDA device (this library has no CPU fallback)");
@@ -652,6 +654,18 @@ int hg_set_exit_wse(hg_ctx* ctx, const double* w, int32_t n) {
   cudaSetDevice(ctx->device);
   ctx->exitWse.assign(w, w + n);
   return upload_boundary_values(ctx);
+}
+
+int hg_set_riemann_solver(hg_ctx* ctx, int32_t solver) {
+  if (!ctx) return fail(ctx, HG_ERR_ARG, "hg_set_riemann_solver: null context");
+  if (solver == HG_HLLC)
+    return fail(ctx, HG_ERR_UNSUPPORTED,
+                "hg_set_riemann_solver: HLLC solver not implemented (as in semi_discretize_swe_2D.jl:358-359)");
+  if (solver != HG_ROE && solver != HG_HLL) return fail(ctx, HG_ERR_ARG, "hg_set_riemann_solver: expected HG_ROE or HG_HLL");
+  ctx->k.riemann = solver;
+  ctx->dm.riemann = solver;
+  ctx->graphValid = false;   // captured launches hold the mesh descriptor by value
+  return HG_OK;
 }
 
 int hg_set_inlet_hydrograph(hg_ctx* ctx, int32_t group, int32_t n, const double* t, const double* q) {
@@ -1330,6 +1344,7 @@ int ctx_setup_device(hg_ctx* c) {
   dm.g = c->k.g; dm.kn2 = c->k.k_n * c->k.k_n; dm.hsm = c->k.h_small;
   dm.gf = (float)c->k.g; dm.kn2f = (float)(c->k.k_n * c->k.k_n); dm.hsmf = (float)c->k.h_small;
   dm.hsmLo = (float)(c->k.h_small - (double)dm.hsmf);
+  dm.riemann = c->k.riemann;
   c->slotNb = d_nb;
   int rc = upload_cells(c);
   if (rc) return rc;

@@ -39,6 +39,8 @@ __device__ __forceinline__ bool is_boundary(int32_t nb) { return nb < 0; }
 __device__ __forceinline__ int32_t boundary_index(int32_t nb) { return -1 - nb; }
 
 enum : int32_t { kBcWall = 0, kBcSymm = 1, kBcInletQ = 2, kBcExitH = 3 };
+// Riemann solvers of the faces (DevMesh::riemann, hg_set_riemann_solver).
+enum : int32_t { kRiemannRoe = 0, kRiemannHll = 1 };
 
 // One side of a face as the Roe solver sees it.
 // `dry` is the reference's clamp decision h <= h_small (semi_discretize_swe_2D.jl:101-106).
@@ -107,6 +109,75 @@ __device__ __forceinline__ void roe_flux(Side<T> L, Side<T> R, T dxi, T g, T nx,
   F[0] = (fL0 + fR0 - A0) / T(2);
   F[1] = (fL1 + fR1 - A1) / T(2);
   F[2] = (fL2 + fR2 - A2) / T(2);
+}
+
+// HLL flux -- new: the reference's RiemannSolver "HLL" raises an error
+// (semi_discretize_swe_2D.jl:356-357).  Harten, Lax & van Leer (1983) with
+// Einfeldt's (1988) wave speeds S_L = min(un_L - c_L, un_Roe - c_Roe),
+// S_R = max(un_R + c_R, un_Roe + c_Roe), on roe_flux's variables (the
+// pre-balanced pressure, the xi jump in the continuity row) and its dry, wall
+// and one-side-dry branches; only the wet-wet flux differs:
+//   F_L (S_L >= 0), F_R (S_R <= 0), else (S_R F_L - S_L F_R + S_L S_R dU) / (S_R - S_L).
+template <class T>
+__device__ __forceinline__ void hll_flux(Side<T> L, Side<T> R, T dxi, T g, T nx, T ny, T hmin, T F[3]) {
+  if (L.dry && R.dry) {
+    F[0] = T(0); F[1] = T(0); F[2] = T(0);
+    return;
+  } else if ((L.h + L.zb) < (R.zb + hmin) && R.dry) {
+    R.h = L.h; R.hu = -L.hu; R.hv = -L.hv;
+  } else if ((R.h + R.zb) < (L.zb + hmin) && L.dry) {
+    L.h = R.h; L.hu = -R.hu; L.hv = -R.hv;
+  } else if (L.dry) {
+    T p = T(0.5) * g * smooth_pow2(R.h);
+    F[0] = R.hu * nx + R.hv * ny;
+    F[1] = (R.hu * (R.hu / R.h) + p) * nx + R.hu * (R.hv / R.h) * ny;
+    F[2] = (R.hv * (R.hu / R.h)) * nx + (R.hv * (R.hv / R.h) + p) * ny;
+    return;
+  } else if (R.dry) {
+    T p = T(0.5) * g * smooth_pow2(L.h);
+    F[0] = L.hu * nx + L.hv * ny;
+    F[1] = (L.hu * (L.hu / L.h) + p) * nx + L.hu * (L.hv / L.h) * ny;
+    F[2] = (L.hv * (L.hu / L.h)) * nx + (L.hv * (L.hv / L.h) + p) * ny;
+    return;
+  }
+  const T uL = L.hu / L.h, vL = L.hv / L.h, uR = R.hu / R.h, vR = R.hv / R.h;
+  const T sqL = smooth_sqrt(L.h), sqR = smooth_sqrt(R.h);
+  const T hRoe = (L.h + R.h) / T(2);
+  const T uRoe = (sqL * uL + sqR * uR) / (sqL + sqR);
+  const T vRoe = (sqL * vL + sqR * vR) / (sqL + sqR);
+  const T unRoe = uRoe * nx + vRoe * ny;
+  const T cRoe = smooth_sqrt(g * hRoe);
+  const T unL = uL * nx + vL * ny, unR = uR * nx + vR * ny;
+  const T cL = smooth_sqrt(g * L.h), cR = smooth_sqrt(g * R.h);
+  const T sL1 = unL - cL, sL2 = unRoe - cRoe, sR1 = unR + cR, sR2 = unRoe + cRoe;
+  const T sL = sL1 <= sL2 ? sL1 : sL2;
+  const T sR = sR2 <= sR1 ? sR1 : sR2;
+  const T pL = T(0.5) * g * (smooth_pow2(L.xi) + T(2) * L.xi * L.hst);
+  const T pR = T(0.5) * g * (smooth_pow2(R.xi) + T(2) * R.xi * R.hst);
+  const T fL0 = L.hu * nx + L.hv * ny;
+  const T fL1 = (L.hu * uL + pL) * nx + L.hu * vL * ny;
+  const T fL2 = (L.hv * uL) * nx + (L.hv * vL + pL) * ny;
+  const T fR0 = R.hu * nx + R.hv * ny;
+  const T fR1 = (R.hu * uR + pR) * nx + R.hu * vR * ny;
+  const T fR2 = (R.hv * uR) * nx + (R.hv * vR + pR) * ny;
+  if (!(sL < T(0))) {
+    F[0] = fL0; F[1] = fL1; F[2] = fL2;
+  } else if (sR <= T(0)) {
+    F[0] = fR0; F[1] = fR1; F[2] = fR2;
+  } else {
+    const T den = sR - sL;
+    F[0] = (sR * fL0 - sL * fR0 + sL * sR * dxi) / den;
+    F[1] = (sR * fL1 - sL * fR1 + sL * sR * (R.hu - L.hu)) / den;
+    F[2] = (sR * fL2 - sL * fR2 + sL * sR * (R.hv - L.hv)) / den;
+  }
+}
+
+// The face flux of the context's Riemann solver (DevMesh::riemann).
+template <class T>
+__device__ __forceinline__ void riemann_flux(int solver, const Side<T>& L, const Side<T>& R, T dxi, T g, T nx, T ny,
+                                             T hmin, T F[3]) {
+  if (solver == kRiemannHll) hll_flux<T>(L, R, dxi, g, nx, ny, hmin, F);
+  else roe_flux<T>(L, R, dxi, g, nx, ny, hmin, F);
 }
 
 // Ghost state of a boundary face (bc_2D.jl:640-834) from the clamped state of

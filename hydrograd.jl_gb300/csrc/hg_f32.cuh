@@ -180,4 +180,43 @@ __device__ __forceinline__ void roe_flux_wet_f32(const Side<float>& L, const Own
   F[2] = 0.5f * ((o.fyx * nx + o.fyy * ny) + (R.hv * uR * nx + fR2y * ny) - A2);
 }
 
+// HLL flux of a face whose two sides are both wet (hll_flux's wet-wet case),
+// minus p_L n in the momentum rows as in roe_flux_wet_f32.  With f' a side's
+// advective flux and dp = p_R - p_L from the exact differences of the pairs
+// (pressure_jump_f32):
+//   S_L >= 0:  f'_L;   S_R <= 0:  f'_R + dp n;
+//   else       (S_R f'_L - S_L f'_R - S_L dp n + S_L S_R dU) / (S_R - S_L).
+__device__ __forceinline__ void hll_flux_wet_f32(const Side<float>& L, const OwnF32& o, const Side<float>& R,
+                                                 float dxi, float dhst, float g, float nx, float ny, float F[3]) {
+  const float rq = rsqrtf(R.h);
+  const float rR = rq * rq;
+  const float uR = R.hu * rR, vR = R.hv * rR;
+  const float sqR = R.h * rq;
+  const float rs = 1.0f / (o.s + sqR);
+  const float uRoe = (o.s * o.u + sqR * uR) * rs;
+  const float vRoe = (o.s * o.v + sqR * vR) * rs;
+  const float unRoe = uRoe * nx + vRoe * ny;
+  const float cRoe = sqrtf(g * ((L.h + R.h) * 0.5f));
+  const float unL = o.u * nx + o.v * ny, unR = uR * nx + vR * ny;
+  const float cL = sqrtf(g * L.h), cR = sqrtf(g * R.h);
+  const float sL = fminf(unL - cL, unRoe - cRoe), sR = fmaxf(unR + cR, unRoe + cRoe);
+  const float dp = pressure_jump_f32(g, L.xi, R.xi, dxi, R.hst, dhst);
+  const float fL0 = L.hu * nx + L.hv * ny;
+  const float fL1 = o.fxx * nx + o.fxy * ny;
+  const float fL2 = o.fyx * nx + o.fyy * ny;
+  const float fR0 = R.hu * nx + R.hv * ny;
+  const float fR1 = R.hu * uR * nx + R.hu * vR * ny;
+  const float fR2 = R.hv * uR * nx + R.hv * vR * ny;
+  if (sL >= 0.0f) {
+    F[0] = fL0; F[1] = fL1; F[2] = fL2;
+  } else if (sR <= 0.0f) {
+    F[0] = fR0; F[1] = fR1 + dp * nx; F[2] = fR2 + dp * ny;
+  } else {
+    const float r = 1.0f / (sR - sL), sLR = sL * sR;
+    F[0] = (sR * fL0 - sL * fR0 + sLR * dxi) * r;
+    F[1] = (sR * fL1 - sL * fR1 - sL * dp * nx + sLR * (R.hu - L.hu)) * r;
+    F[2] = (sR * fL2 - sL * fR2 - sL * dp * ny + sLR * (R.hv - L.hv)) * r;
+  }
+}
+
 }  // namespace hgd

@@ -84,9 +84,10 @@ __device__ __forceinline__ void one_face_f32(const DevMesh& m, const float4* __r
     if (type == kBcExitH && !R.dry) dxi = m.bfExitRel[bf] - (L.s.xi + L.xlo);
   }
   if (!L.s.dry && !R.dry) {
-    roe_flux_wet_f32(L.s, own, R, dxi, dhst, m.gf, nx, ny, F);
+    if (m.riemann == kRiemannHll) hll_flux_wet_f32(L.s, own, R, dxi, dhst, m.gf, nx, ny, F);
+    else roe_flux_wet_f32(L.s, own, R, dxi, dhst, m.gf, nx, ny, F);
   } else {
-    roe_flux<float>(L.s, R, dxi, m.gf, nx, ny, m.hsmf, F);
+    riemann_flux<float>(m.riemann, L.s, R, dxi, m.gf, nx, ny, m.hsmf, F);
     F[1] -= own.p * nx;   // the own pressure shift (pressure_jump_f32)
     F[2] -= own.p * ny;
   }

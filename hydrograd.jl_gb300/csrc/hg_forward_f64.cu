@@ -120,7 +120,8 @@ __device__ __forceinline__ void face_sum_f64(const DevMesh& m, const double* __r
                               m.bfLp23[bf], m.man[c]);
     }
     double F[3];
-    if (!L.dry && !R.dry) roe_flux_wet_f64(L, own, R, R.xi - L.xi, m.g, nx, ny, F);
+    if (m.riemann == kRiemannHll) hll_flux<double>(L, R, R.xi - L.xi, m.g, nx, ny, m.hsm, F);
+    else if (!L.dry && !R.dry) roe_flux_wet_f64(L, own, R, R.xi - L.xi, m.g, nx, ny, F);
     else roe_flux<double>(L, R, R.xi - L.xi, m.g, nx, ny, m.hsm, F);
     f0 = f0 + F[0] * len;
     f1 = f1 + F[1] * len;

@@ -52,6 +52,7 @@ struct DevMesh {
   int32_t nslot = 0;    // max faces per cell
   int32_t nbf = 0;      // boundary faces
   int32_t nInlet = 0, nExit = 0;
+  int32_t riemann = 0;  // face Riemann solver: 0 Roe, 1 HLL (hg_set_riemann_solver)
   const int32_t* nb = nullptr;       // [nslot*n] neighbour (>=0), -1-bf (boundary face bf), INT32_MIN (none)
   const double* snx = nullptr;       // [nslot*n] outward unit normal x
   const double* sny = nullptr;

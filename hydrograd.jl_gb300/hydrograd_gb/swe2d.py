@@ -287,6 +287,15 @@ class SWE2D:
         self._chk(lib().hg_autotune(self.h, int(reps), _i(k)))
         return int(k[0])
 
+    def set_riemann_solver(self, name):
+        """hg_set_riemann_solver: "Roe" (the reference's, the default) or
+        "HLL" (Harten-Lax-van Leer with Einfeldt's wave speeds); "HLLC" is
+        refused (HgError), as the reference raises an error for it."""
+        kinds = {"Roe": 0, "HLL": 1, "HLLC": 2}
+        if name not in kinds:
+            raise ValueError("Riemann solver: Roe, HLL or HLLC")
+        self._chk(lib().hg_set_riemann_solver(self.h, kinds[name]))
+
     def set_adjoint_tape(self, nbytes=-1):
         """hg_set_adjoint_tape: memory for the adjoint's stage states.  -1 (the
         default): segments as long as fit in min(half the free device memory,

@@ -60,8 +60,12 @@ enum hg_precision {
 /* Cell renumbering used on the device. */
 enum hg_order { HG_ORDER_NONE = 0, HG_ORDER_RCM = 1, HG_ORDER_HILBERT = 2 };
 
-/* Riemann solver (semi_discretize_swe_2D.jl:352-362: the reference has Roe only). */
-enum hg_riemann { HG_ROE = 0 };
+/* Riemann solver (swe_2D_constants.jl:16 RiemannSolver; semi_discretize_swe_2D.jl:352-362):
+ * Roe (swe_2D_solvers.jl:4-164), the reference's only working one; HLL -- new:
+ * the reference's "HLL" raises an error -- Harten-Lax-van Leer with Einfeldt's
+ * wave speeds on the Roe solver's variables and dry/wet/wall branches; HLLC is
+ * refused with HG_ERR_UNSUPPORTED, as the reference raises an error for it. */
+enum hg_riemann { HG_ROE = 0, HG_HLL = 1, HG_HLLC = 2 };
 
 /*
  * Mesh as an SRH-2D geometry holds it (src/utilities/SRH_2D/SRH_2D_SRHGeom.jl:14-46):
@@ -239,6 +243,10 @@ typedef struct hg_ude_desc {
   int32_t layernorm_over_batch;
 } hg_ude_desc;
 int hg_set_ude(hg_ctx* ctx, const hg_ude_desc* ude);
+
+/* Change the Riemann solver (hg_riemann) of a context after hg_create: it
+ * applies to every integrator, the RHS and the adjoint. */
+int hg_set_riemann_solver(hg_ctx* ctx, int32_t solver);
 
 /* ---- forward ------------------------------------------------------------- */
 /* dQdt = swe_2d_rhs(Q, p, t) with host buffers (semi_discretize_swe_2D.jl:18-277). */
