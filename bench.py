@@ -231,6 +231,32 @@ def run_reference(args):
     }))
 
 
+def run_hll(args, case, device):
+    """The HLL Riemann solver (hg_set_riemann_solver) on the 1M-cell reach:
+    FP32C forward rate over hll_steps CFL steps (L2 flushed before each, as
+    the main leg), and the FP32C state against FP64 HLL's after 200 CFL steps
+    each (as the main leg compares Roe's)."""
+    N = len(case["cell_node_count"])
+    out, final = {}, {}
+    for prec in ("fp32c", "fp64"):
+        c = make_ctx(case, prec, device)
+        c.set_riemann_solver("HLL")
+        if prec == "fp32c":
+            c.upload(case["Q0"])
+            c.advance_timed(args.warmup, cfl=0.4, flush_l2=True)
+            c.upload(case["Q0"])
+            ms = c.advance_timed(args.hll_steps, cfl=0.4, flush_l2=True)
+            out["fwd"] = {"value": N * args.hll_steps / (ms * 1e-3), "steps": args.hll_steps,
+                          "ms_per_step": ms / args.hll_steps}
+        final[prec], _ = c.integrate(case["Q0"], 200, cfl=0.4)
+        c.close()
+    a, b = final["fp32c"], final["fp64"]
+    out["error_fp32c_vs_fp64_state_rel_linf"] = float(np.abs(a - b).max() / np.abs(b).max())
+    out["config"] = ("HLL flux (Harten-Lax-van Leer, Einfeldt wave speeds) on the 1M-cell reach, FP32C, CFL 0.4; "
+                     "state error after 200 CFL steps against FP64 HLL")
+    return out
+
+
 def run_config1(args, device, cpu):
     """Configuration 1 (hydrograd_gb.workloads.dam_break): 200 x 40 quads
     (8,000 cells) over 100 x 20 m, flat bed, walls, n = 0.03, h = 1.0 / 0.5 m
@@ -510,6 +536,7 @@ def run_ours(args):
                          "widened by the automatic stage-state tape (all steps kept where they fit in HBM), "
                          f"{len(probes)} probes (half on the pool rim, half at the inlet), loss = mean squared "
                          "departure of the probe depths from the lake at rest")
+    hll = run_hll(args, case, local) if args.hll_steps > 0 else None
     cfg1 = run_config1(args, local, cpu=not args.no_cpu and rank == 0) if args.config1_steps > 0 else None
     cfg5 = run_config5(args, local) if args.config5_steps > 0 else None
     ens = None
@@ -559,6 +586,7 @@ def run_ours(args):
         "fp32c_over_fp64_speedup": f32["value"] / out["fp64"]["value"],
         "fwd_adjoint": adj,
         "ensemble": ens,
+        "hll": hll,
         "config1": cfg1,
         "config5": cfg5,
         "warm_value": f32["warm_value"], "simulated_seconds": f32["sim_time"],
@@ -590,6 +618,8 @@ def main():
                     help="ensemble (configuration 4) forward+adjoint steps (0: skip)")
     ap.add_argument("--ens-ckpt", type=int, default=25)
     ap.add_argument("--ens-members", type=int, default=32, help="members per mesh")
+    ap.add_argument("--hll-steps", type=int, default=500,
+                    help="FP32C steps of the HLL-solver leg on the 1M-cell reach (0: skip)")
     ap.add_argument("--config1-steps", type=int, default=1000,
                     help="configuration 1 (8,000-cell dam break) steps at dt = 0.01 s (0: skip)")
     ap.add_argument("--config5-steps", type=int, default=5000,
