@@ -36,8 +36,10 @@ inline int blocks_for(int n) { return (n + kBlock - 1) / kBlock; }
 // Flux F (times nothing: the caller scales by the face length) of slot sl of
 // the cell with side L, own quantities own.  LOC: the slot's neighbour word
 // holds a tile-local index (bits 0-8: own cells at [0, kBlock) of sX / sP,
-// halo cells at [kBlock, ...) of hX / hP); otherwise a cell id.
-template <bool LOC>
+// halo cells at [kBlock, ...) of hX / hP); otherwise a cell id.  RS: the
+// Riemann solver fixed at compile time (kRiemannRoe / kRiemannHll), or -1 for
+// the context's at run time (DevMesh::riemann).
+template <bool LOC, int RS>
 __device__ __forceinline__ void one_face_f32(const DevMesh& m, const float4* __restrict__ X, const float4* sX,
                                              const float4* sP, const float4* hX, const float4* hP, int base,
                                              const SideF32& L, const OwnF32& own, float2 hstPair, float4 sl, int32_t nb,
@@ -83,17 +85,18 @@ __device__ __forceinline__ void one_face_f32(const DevMesh& m, const float4* __r
     dxi = (R.h - L.s.h) + L.excess;
     if (type == kBcExitH && !R.dry) dxi = m.bfExitRel[bf] - (L.s.xi + L.xlo);
   }
+  const int rs = RS >= 0 ? RS : m.riemann;
   if (!L.s.dry && !R.dry) {
-    if (m.riemann == kRiemannHll) hll_flux_wet_f32(L.s, own, R, dxi, dhst, m.gf, nx, ny, F);
+    if (rs == kRiemannHll) hll_flux_wet_f32(L.s, own, R, dxi, dhst, m.gf, nx, ny, F);
     else roe_flux_wet_f32(L.s, own, R, dxi, dhst, m.gf, nx, ny, F);
   } else {
-    riemann_flux<float>(m.riemann, L.s, R, dxi, m.gf, nx, ny, m.hsmf, F);
+    riemann_flux<float>(rs, L.s, R, dxi, m.gf, nx, ny, m.hsmf, F);
     F[1] -= own.p * nx;   // the own pressure shift (pressure_jump_f32)
     F[2] -= own.p * ny;
   }
 }
 
-template <int NS, bool LOC>
+template <int NS, bool LOC, int RS>
 __device__ __forceinline__ void face_sum_f32(const DevMesh& m, const float4* __restrict__ X, const float4* sX,
                                              const float4* sP, const float4* hX, const float4* hP, int base, int c,
                                              const SideF32& L, const OwnF32& own, float2 hstPair,
@@ -105,7 +108,7 @@ __device__ __forceinline__ void face_sum_f32(const DevMesh& m, const float4* __r
     const int32_t nb = slot_nb(sl[k]);
     if (nb == kNoFace) continue;
     float F[3];
-    one_face_f32<LOC>(m, X, sX, sP, hX, hP, base, L, own, hstPair, sl[k], nb, totalA, man, flags, F);
+    one_face_f32<LOC, RS>(m, X, sX, sP, hX, hP, base, L, own, hstPair, sl[k], nb, totalA, man, flags, F);
     const float len = sl[k].z;
     f0 = fmaf(F[0], len, f0);
     f1 = fmaf(F[1], len, f1);
@@ -203,7 +206,7 @@ __device__ __forceinline__ void stage_finish(const DevMesh& m, const DevScalars&
 // kBlock) for in-block neighbours.  The input state's lo parts and (stage 2)
 // the base state are read at qinP[k], xbP[k], qbP[k] -- global arrays (k = c)
 // or a tile staged in shared memory -- where they are used.
-template <int NS, int MODE, bool LOC = false>
+template <int NS, int MODE, bool LOC = false, int RS = -1>
 __device__ __forceinline__ void stage_cell(const DevMesh& m, const DevScalars& s, const float4* __restrict__ X,
                                            const float4* sX, const float4* sP, const float4* hX, const float4* hP,
                                            int base, int c,
@@ -214,7 +217,7 @@ __device__ __forceinline__ void stage_cell(const DevMesh& m, const DevScalars& s
   const SideF32 L = make_side_f32(xin, cp, m.hsmf, m.hsmLo);
   const OwnF32 own = own_f32(L.s, m.gf);
   float f0, f1, f2;
-  face_sum_f32<NS, LOC>(m, X, sX, sP, hX, hP, base, c, L, own, make_float2(cp.x, cp.y), sl, totalIn, cp.w, s.flags, f0, f1, f2);
+  face_sum_f32<NS, LOC, RS>(m, X, sX, sP, hX, hP, base, c, L, own, make_float2(cp.x, cp.y), sl, totalIn, cp.w, s.flags, f0, f1, f2);
   stage_finish<NS, MODE>(m, s, L, f0, f1, f2, c, sl, xin, cp, cs, qinP, xbP, qbP, k, dt, Xout, Rout, cfl, cand, hOut,
                          wetOut);
 }
@@ -299,7 +302,7 @@ __device__ __forceinline__ void fused_record(const DevScalars& s, const StageFus
 // holds no FP64 arithmetic: the stage mode is a template parameter (the FP64
 // comparison of the reference Euler clamp exists only in that instance), and
 // the fused step's dt is formed once per block.
-template <int NS, bool FUSED, int MODE>
+template <int NS, bool FUSED, int MODE, int RS = -1>
 __global__ void __launch_bounds__(kBlock, stage_min_blocks<NS>())
     k_stage_f32(DevMesh m, DevScalars s, StateF32 Xin, StateF32 Xbase, StateF32 Xout, double* Rout, int cfl,
                 StageFuse f) {
@@ -331,7 +334,8 @@ __global__ void __launch_bounds__(kBlock, stage_min_blocks<NS>())
   __syncthreads();
   if (active) {
     const float dt = MODE == kModeRhs ? 0.0f : (FUSED ? dtShared : *s.dtf);
-    stage_cell<NS, MODE>(m, s, Xin.x, sX, sP, nullptr, nullptr, base, c, sl, xin, cp, cs, Xin.q, Xbase.x, Xbase.q, c,
+    stage_cell<NS, MODE, false, RS>(m, s, Xin.x, sX, sP, nullptr, nullptr, base, c, sl, xin, cp, cs, Xin.q, Xbase.x,
+                                     Xbase.q, c,
                          dt, FUSED ? f.totalIn : m.totalA, Xout, Rout, cfl, cand, hOut, wetOut);
   }
   if (FUSED && f.record && blockIdx.x == 0 && threadIdx.x == 0) fused_record(s, f);
@@ -382,7 +386,7 @@ __device__ __forceinline__ void tma_issue_tile(const DevMesh& m, StateF32 Xin, S
   }
 }
 
-template <int NS, int MODE>
+template <int NS, int MODE, int RS>
 __global__ void __launch_bounds__(kBlock, kTmaCtasPerSm)
     k_stage_tma_f32(DevMesh m, DevScalars s, StateF32 Xin, StateF32 Xbase, StateF32 Xout, int cfl, StageFuse f) {
   pdl_enter();
@@ -451,7 +455,8 @@ __global__ void __launch_bounds__(kBlock, kTmaCtasPerSm)
       float4 sl[NS];
 #pragma unroll
       for (int k = 0; k < NS; ++k) sl[k] = bSL[k * kBlock + tid];
-      stage_cell<NS, MODE>(m, s, Xin.x, bX, bCP, nullptr, nullptr, base, c, sl, bX[tid], bCP[tid], bCS[tid], bQ, bXB,
+      stage_cell<NS, MODE, false, RS>(m, s, Xin.x, bX, bCP, nullptr, nullptr, base, c, sl, bX[tid], bCP[tid], bCS[tid],
+                                      bQ, bXB,
                            bQB, tid, dt, f.totalIn, Xout, nullptr, cfl, cand, hOut, wetOut);
     }
     if (m.nInlet > 0) fused_inlet_totals<NS>(m, f, t, c, hOut, wetOut);
@@ -518,7 +523,7 @@ __device__ __forceinline__ void pipe_issue(const DevMesh& m, StateF32 Xin, State
 // FUSED: the fused step's bookkeeping (StageFuse); otherwise a plain stage of
 // an unfused step (dt and inlet totals from DevScalars / DevMesh), as the
 // ensembles and state-dependent resistance take.
-template <int NS, int MODE, bool FUSED>
+template <int NS, int MODE, bool FUSED, int RS>
 __global__ void __launch_bounds__(kBlock, kPipeCtasPerSm)
     k_stage_pipe_f32(DevMesh m, DevScalars s, StateF32 Xin, StateF32 Xbase, StateF32 Xout, int cfl, StageFuse f) {
   pdl_enter();
@@ -558,7 +563,7 @@ __global__ void __launch_bounds__(kBlock, kPipeCtasPerSm)
       float4 sl[NS];
 #pragma unroll
       for (int k = 0; k < NS; ++k) sl[k] = bSL[k * kBlock + tid];
-      stage_cell<NS, MODE, true>(m, s, Xin.x, bX, bCP, bHX, bHP, base, c, sl, bX[tid], bCP[tid], bCS[tid], bQ, bXB,
+      stage_cell<NS, MODE, true, RS>(m, s, Xin.x, bX, bCP, bHX, bHP, base, c, sl, bX[tid], bCP[tid], bCS[tid], bQ, bXB,
                                  bQB, tid, dtShared, FUSED ? f.totalIn : m.totalA, Xout, nullptr, cfl, cand, hOut,
                                  wetOut);
     }
@@ -717,11 +722,19 @@ template <int NS, bool FUSED>
 void launch_stage_ns(const DevMesh& m, const DevScalars& s, int mode, StateF32 Xin, StateF32 Xbase, StateF32 Xout,
                      double* Rout, int cfl, const StageFuse& f, cudaStream_t st) {
   const int nb = blocks_for(m.n);
-  if (mode == kModeStage1) {
-    launch_k(true, k_stage_f32<NS, FUSED, kModeStage1>, nb, kBlock, 0, st, m, s, Xin, Xbase, Xout, Rout, cfl, f);
+  if constexpr (FUSED) {   // the fused stages: the solver fixed per instance
+    const bool hll = m.riemann == kRiemannHll;
+    if (mode == kModeStage1)
+      launch_k(true, hll ? k_stage_f32<NS, true, kModeStage1, kRiemannHll> : k_stage_f32<NS, true, kModeStage1, kRiemannRoe>,
+               nb, kBlock, 0, st, m, s, Xin, Xbase, Xout, Rout, cfl, f);
+    else if (mode == kModeStage2)
+      launch_k(true, hll ? k_stage_f32<NS, true, kModeStage2, kRiemannHll> : k_stage_f32<NS, true, kModeStage2, kRiemannRoe>,
+               nb, kBlock, 0, st, m, s, Xin, Xbase, Xout, Rout, cfl, f);
+  } else if (mode == kModeStage1) {
+    launch_k(true, k_stage_f32<NS, false, kModeStage1>, nb, kBlock, 0, st, m, s, Xin, Xbase, Xout, Rout, cfl, f);
   } else if (mode == kModeStage2) {
-    launch_k(true, k_stage_f32<NS, FUSED, kModeStage2>, nb, kBlock, 0, st, m, s, Xin, Xbase, Xout, Rout, cfl, f);
-  } else if constexpr (!FUSED) {
+    launch_k(true, k_stage_f32<NS, false, kModeStage2>, nb, kBlock, 0, st, m, s, Xin, Xbase, Xout, Rout, cfl, f);
+  } else {
     if (mode == kModeRhs)
       launch_k(true, k_stage_f32<NS, false, kModeRhs>, nb, kBlock, 0, st, m, s, Xin, Xbase, Xout, Rout, cfl, f);
     else
@@ -764,35 +777,47 @@ int resident_ctas(Kernel k, uint32_t smem) {
   return n;
 }
 
-template <int NS, int MODE>
-void launch_tma(const DevMesh& m, const DevScalars& s, StateF32 Xin, StateF32 Xbase, StateF32 Xout, int cfl,
-                const StageFuse& fu, cudaStream_t st) {
+template <int NS, int MODE, int RS>
+void launch_tma_rs(const DevMesh& m, const DevScalars& s, StateF32 Xin, StateF32 Xbase, StateF32 Xout, int cfl,
+                   const StageFuse& fu, cudaStream_t st) {
   using T = TmaTile<NS, MODE>;
   static const bool attr = [] {   // more than 48 KB of dynamic shared memory: opt in once
-    cudaFuncSetAttribute(k_stage_tma_f32<NS, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T::kSmem);
+    cudaFuncSetAttribute(k_stage_tma_f32<NS, MODE, RS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T::kSmem);
     return true;
   }();
   (void)attr;
   static const int grid = sm_count() * kTmaCtasPerSm;
   const int tiles = blocks_for(m.n);
-  launch_k(true, k_stage_tma_f32<NS, MODE>, tiles < grid ? tiles : grid, kBlock, T::kSmem, st, m, s, Xin, Xbase, Xout,
-           cfl, fu);
+  launch_k(true, k_stage_tma_f32<NS, MODE, RS>, tiles < grid ? tiles : grid, kBlock, T::kSmem, st, m, s, Xin, Xbase,
+           Xout, cfl, fu);
+}
+template <int NS, int MODE>
+void launch_tma(const DevMesh& m, const DevScalars& s, StateF32 Xin, StateF32 Xbase, StateF32 Xout, int cfl,
+                const StageFuse& fu, cudaStream_t st) {
+  if (m.riemann == kRiemannHll) launch_tma_rs<NS, MODE, kRiemannHll>(m, s, Xin, Xbase, Xout, cfl, fu, st);
+  else launch_tma_rs<NS, MODE, kRiemannRoe>(m, s, Xin, Xbase, Xout, cfl, fu, st);
 }
 
-template <int NS, int MODE, bool FUSED>
-void launch_pipe(const DevMesh& m, const DevScalars& s, StateF32 Xin, StateF32 Xbase, StateF32 Xout, int cfl,
-                 const StageFuse& fu, cudaStream_t st) {
+template <int NS, int MODE, bool FUSED, int RS>
+void launch_pipe_rs(const DevMesh& m, const DevScalars& s, StateF32 Xin, StateF32 Xbase, StateF32 Xout, int cfl,
+                    const StageFuse& fu, cudaStream_t st) {
   using T = PipeTile<NS, MODE>;
   static const bool attr = [] {   // more than 48 KB of dynamic shared memory: opt in once
-    cudaFuncSetAttribute(k_stage_pipe_f32<NS, MODE, FUSED>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaFuncSetAttribute(k_stage_pipe_f32<NS, MODE, FUSED, RS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)T::kSmem);
     return true;
   }();
   (void)attr;
-  static const int grid = sm_count() * resident_ctas(k_stage_pipe_f32<NS, MODE, FUSED>, T::kSmem);
+  static const int grid = sm_count() * resident_ctas(k_stage_pipe_f32<NS, MODE, FUSED, RS>, T::kSmem);
   const int tiles = blocks_for(m.n);
-  launch_k(true, k_stage_pipe_f32<NS, MODE, FUSED>, tiles < grid ? tiles : grid, kBlock, T::kSmem, st, m, s, Xin,
+  launch_k(true, k_stage_pipe_f32<NS, MODE, FUSED, RS>, tiles < grid ? tiles : grid, kBlock, T::kSmem, st, m, s, Xin,
            Xbase, Xout, cfl, fu);
+}
+template <int NS, int MODE, bool FUSED>
+void launch_pipe(const DevMesh& m, const DevScalars& s, StateF32 Xin, StateF32 Xbase, StateF32 Xout, int cfl,
+                 const StageFuse& fu, cudaStream_t st) {
+  if (m.riemann == kRiemannHll) launch_pipe_rs<NS, MODE, FUSED, kRiemannHll>(m, s, Xin, Xbase, Xout, cfl, fu, st);
+  else launch_pipe_rs<NS, MODE, FUSED, kRiemannRoe>(m, s, Xin, Xbase, Xout, cfl, fu, st);
 }
 
 template <int NS, bool FUSED = true>
