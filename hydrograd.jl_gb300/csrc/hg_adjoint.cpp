@@ -48,6 +48,7 @@ struct AdjointBuffers {
   // Final-state loss: observations (wse, u, v, zbw; device order), dL/dWSE,
   // the two loss sums and the reduction scratch.
   double* fin = nullptr;
+  double* lam = nullptr;          // [3n] final-state cotangent (hg_final_vjp), device order
   double* finScratch = nullptr;   // dWse [n], parts [2], partials [2 kFinalLossBlocks]
   unsigned int* finTicket = nullptr;
   ~AdjointBuffers() {
@@ -59,6 +60,7 @@ struct AdjointBuffers {
     cudaFree(obs);
     cudaFree(segTot);
     cudaFree(fin);
+    cudaFree(lam);
     cudaFree(finScratch);
     cudaFree(finTicket);
   }
@@ -337,7 +339,7 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
   // reference takes them (WSE_truth range + sqrt(eps); the largest observed
   // speed, at least eps), and the observations in device order.
   FinalLossDev fl;
-  const bool useFinal = fo && (fo->wse || (fo->u && fo->v));
+  const bool useFinal = fo && (fo->wse || (fo->u && fo->v) || fo->lam);
   if (useFinal) {
     if (!b->fin) {
       ADJ_CUDA(c, cudaMalloc(&b->fin, (size_t)4 * N * sizeof(double)));
@@ -368,6 +370,14 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
       fl.v = b->fin + (size_t)2 * N;
     }
     ADJ_CUDA(c, cudaMemcpyAsync(b->fin, dev.data(), dev.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+    if (fo->lam) {   // the final-state cotangent, in device order
+      if (!b->lam) ADJ_CUDA(c, cudaMalloc(&b->lam, (size_t)3 * N * sizeof(double)));
+      std::vector<double> l((size_t)3 * N);
+      for (int blk = 0; blk < 3; ++blk)
+        for (int i = 0; i < N; ++i) l[(size_t)blk * N + i] = fo->lam[(size_t)blk * N + c->perm[i]];
+      ADJ_CUDA(c, cudaMemcpyAsync(b->lam, l.data(), l.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+      fl.lam = b->lam;
+    }
     fl.dWse = b->finScratch;
     fl.parts = b->finScratch + N;
     fl.partials = b->finScratch + N + 2;

@@ -16,6 +16,7 @@ struct FinalObs {
   const double* u = nullptr;
   const double* v = nullptr;
   const double* zbw = nullptr;
+  const double* lam = nullptr;   // [3n] cotangent of the final state (caller's cell order), added to the seed
 };
 
 // loss = the probe misfit (mean over steps and probes) + the final-state loss

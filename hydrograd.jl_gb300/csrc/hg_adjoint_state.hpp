@@ -88,6 +88,7 @@ struct FinalLossDev {
   const double* u = nullptr;     // [n] u, v or null: no velocity term
   const double* v = nullptr;
   const double* zbw = nullptr;   // [n] zb of WSE_pred
+  const double* lam = nullptr;   // [3n] or null: a cotangent of the final state added to the seed
   double wseDen = 1.0;           // WSE_truth range + eps
   double velScale = 1.0;
   double invN = 1.0;

@@ -805,6 +805,20 @@ int hg_final_loss_and_grad(hg_ctx* ctx, const double* Q0, int32_t nsteps, double
                                g_inletq, Q_final, &fo, parts);
 }
 
+int hg_final_vjp(hg_ctx* ctx, const double* Q0, int32_t nsteps, double dt, int32_t ckpt_every, const double* lambda,
+                 double* g_manning_cells, double* g_zb, double* g_inletq, double* Q_final) {
+  if (!ctx || !Q0 || nsteps <= 0 || !(dt > 0) || !lambda) return fail(ctx, HG_ERR_ARG, "hg_final_vjp: bad argument");
+  if (ctx->dm.res.kind != kResConstant)
+    return fail(ctx, HG_ERR_UNSUPPORTED,
+                "hg_final_vjp: gradients through a state-dependent Manning n or a UDE closure are not available");
+  cudaSetDevice(ctx->device);
+  FinalObs fo;
+  fo.lam = lambda;
+  double loss = 0.0, parts[3];
+  return adjoint_loss_and_grad(ctx, Q0, nsteps, dt, ckpt_every, nullptr, nullptr, 0, &loss, g_manning_cells, g_zb,
+                               g_inletq, Q_final, &fo, parts);
+}
+
 int hg_get_bed(hg_ctx* ctx, double* zb, double* S0, double* man, double* hstill) {
   if (!ctx) return fail(ctx, HG_ERR_ARG, "hg_get_bed: null context");
   for (int i = 0; i < ctx->n; ++i) {

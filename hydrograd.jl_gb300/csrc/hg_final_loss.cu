@@ -55,6 +55,11 @@ __global__ void __launch_bounds__(kBlock) k_final_loss(DevMesh m, FinalLossDev f
       gqy += dv / e;
       gxi -= (du * qx + dv * qy) / (e * e);
     }
+    if (f.lam) {
+      gxi += f.lam[c];
+      gqx += f.lam[m.n + c];
+      gqy += f.lam[2 * m.n + c];
+    }
     if (h > m.hsm) {   // a cell the last stage clamped does not depend on its inputs
       mu[c] += (Mu)gxi;
       mu[m.n + c] += (Mu)gqx;

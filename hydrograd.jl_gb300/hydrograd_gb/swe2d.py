@@ -287,6 +287,21 @@ class SWE2D:
         self._chk(lib().hg_autotune(self.h, int(reps), _i(k)))
         return int(k[0])
 
+    def final_state_vjp(self, Q0, nsteps, dt, lam, ckpt_every=50, want=("manning", "zb", "inletq")):
+        """hg_final_vjp: gradients of lam . Q_K (Q_K the state after nsteps
+        SSP-RK2 steps of dt) w.r.t. the per-cell n, zb and the inlet Q."""
+        N = self.n_cells
+        lam = np.ascontiguousarray(lam, dtype=np.float64)
+        if lam.size != 3 * N:
+            raise ValueError("lam: one value per state entry (3 n)")
+        gn = np.zeros(N) if "manning" in want else None
+        gz = np.zeros(N) if "zb" in want else None
+        gq = np.zeros(max(self.n_inletq, 1)) if "inletq" in want else None
+        Qf = np.zeros(3 * N)
+        self._chk(lib().hg_final_vjp(self.h, _d(np.ascontiguousarray(Q0, dtype=np.float64)), int(nsteps), float(dt),
+                                     int(ckpt_every), _d(lam), _d(gn), _d(gz), _d(gq), _d(Qf)))
+        return dict(g_manning=gn, g_zb=gz, g_inletq=None if gq is None else gq[:self.n_inletq], Q=Qf)
+
     def set_riemann_solver(self, name):
         """hg_set_riemann_solver: "Roe" (the reference's, the default) or
         "HLL" (Harten-Lax-van Leer with Einfeldt's wave speeds); "HLLC" is

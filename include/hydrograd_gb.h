@@ -322,6 +322,17 @@ int hg_final_loss_and_grad(hg_ctx* ctx, const double* Q0, int32_t nsteps, double
  * the next one allocates what it needs. */
 int hg_set_adjoint_tape(hg_ctx* ctx, int64_t bytes);
 
+/* Vector-Jacobian product of the final state: with Q_K the state after nsteps
+ * SSP-RK2 steps of dt from Q0, the gradients of lambda . Q_K (lambda [3n], the
+ * caller's cell order, blocks xi, qx, qy) w.r.t. the per-cell n, zb and the
+ * inlet Q, through the same checkpointed adjoint.  One call per cotangent:
+ * the rows of the Jacobian dQ_K/dparams that the reference's sensitivity
+ * analysis forms with ForwardDiff (swe_2D_sensitivity.jl), or the gradient of
+ * any loss of the final state whose dL/dQ_K the caller forms.  Outputs may be
+ * NULL as in hg_loss_and_grad. */
+int hg_final_vjp(hg_ctx* ctx, const double* Q0, int32_t nsteps, double dt, int32_t ckpt_every, const double* lambda,
+                 double* g_manning_cells, double* g_zb, double* g_inletq, double* Q_final);
+
 /* ---- tuning ------------------------------------------------------------------ */
 /* Choose the kernel of the FP32-compensated fused stages for this mesh: each
  * kernel that can run it (0 gather: one block per 256-cell tile; 1 pipe:
