@@ -41,6 +41,8 @@ class InversionSettings:
     optimizers: list = field(default_factory=lambda: ["Adam"])
     learning_rates: list = field(default_factory=lambda: [0.001])
     max_iterations: list = field(default_factory=lambda: [10])
+    abs_tols: list = field(default_factory=list)   # per optimiser (control_settings_2D.jl:46-47)
+    rel_tols: list = field(default_factory=list)
     save_frequency: int = 1
     save_checkpoint: bool = False
     checkpoint_frequency: int = 10
@@ -59,6 +61,8 @@ class InversionSettings:
                    optimizers=list(opts["inversion_optimizers"]),
                    learning_rates=[float(v) for v in opts["inversion_learning_rates"]],
                    max_iterations=[int(v) for v in opts["inversion_max_iterations"]],
+                   abs_tols=[float(v) for v in opts.get("inversion_abs_tols", [])],
+                   rel_tols=[float(v) for v in opts.get("inversion_rel_tols", [])],
                    save_frequency=int(opts["inversion_save_frequency"]),
                    save_checkpoint=bool(opts["inversion_save_checkpoint"]),
                    checkpoint_frequency=int(opts["inversion_checkpoint_frequency"]))
@@ -138,6 +142,104 @@ class Descent:
         return theta - self.eta * g
 
 
+def backtracking(phi, phi0, dphi0, alpha=1.0, c1=1e-4, rho_hi=0.5, rho_lo=0.1, max_iter=1000):
+    """Backtracking line search with the Armijo condition phi(a) <= phi0 + c1 a
+    dphi0: the first shrink from the quadratic through phi0, dphi0 and phi(a),
+    the later ones from the cubic through the last two trials (Nocedal &
+    Wright, Numerical Optimization, 3.5), each new step kept within
+    [rho_lo, rho_hi] of the last -- the algorithm and defaults of
+    LineSearches.jl's BackTracking (order 3), which the reference's LBFGS takes
+    (swe_2D_inversion.jl:684-685).  Returns (a, phi(a), evaluations)."""
+    a1 = a2 = alpha
+    p0, p1 = phi0, phi(a2)
+    n = 1
+    while p1 > phi0 + c1 * a2 * dphi0 and n < max_iter:
+        if n == 1:
+            at = -(dphi0 * a2 * a2) / (2.0 * (p1 - phi0 - dphi0 * a2))
+        else:
+            div = 1.0 / (a1 * a1 * a2 * a2 * (a2 - a1))
+            r1, r0 = p1 - phi0 - dphi0 * a2, p0 - phi0 - dphi0 * a1
+            a = (a1 * a1 * r1 - a2 * a2 * r0) * div
+            b = (-a1 ** 3 * r1 + a2 ** 3 * r0) * div
+            if abs(a) <= 1e-300:
+                at = dphi0 / (2.0 * b)
+            else:
+                at = (-b + np.sqrt(max(b * b - 3.0 * a * dphi0, 0.0))) / (3.0 * a)
+        a1 = a2
+        a2 = max(min(at, a2 * rho_hi), a2 * rho_lo)
+        p0, p1 = p1, phi(a2)
+        n += 1
+    return a2, p1, n
+
+
+class LBFGS:
+    """Limited-memory BFGS (Nocedal & Wright, 7.2): the two-loop recursion
+    over the last m (s, y) pairs with the initial inverse Hessian (s'y / y'y) I
+    of the newest pair, a backtracking line search from the unit step -- the
+    method and defaults of Optim.jl's LBFGS(linesearch = BackTracking()), the
+    reference's choice (swe_2D_inversion.jl:684-685).  Pairs with s'y <= 0 are
+    not stored.  Converged when max|g| <= g_tol or, with rel_tol, when the loss
+    changes by at most rel_tol of its size.  (Restated from the published
+    method; Optim.jl itself is not available to compare against.)"""
+
+    def __init__(self, m=10, g_tol=1e-8, rel_tol=None):
+        self.m, self.g_tol, self.rel_tol = m, g_tol, rel_tol
+        self.S, self.Y = [], []
+
+    def direction(self, g):
+        q = g.copy()
+        al = []
+        for s, y in zip(reversed(self.S), reversed(self.Y)):
+            rho = 1.0 / (y @ s)
+            a = rho * (s @ q)
+            q -= a * y
+            al.append((rho, a))
+        if self.S:
+            q *= (self.S[-1] @ self.Y[-1]) / (self.Y[-1] @ self.Y[-1])
+        for (s, y), (rho, a) in zip(zip(self.S, self.Y), reversed(al)):
+            q += (a - rho * (y @ q)) * s
+        return -q
+
+    def minimize(self, fg, x0, max_iter, callback=None):
+        """fg(x) -> (f, g); callback(iteration, x, f) after every iteration.
+        Returns (x, f, converged)."""
+        x = np.array(x0, dtype=np.float64)
+        f, g = fg(x)
+        cache = {}
+
+        def phi(a, x=None, d=None):
+            xa = x + a * d
+            fa, ga = fg(xa)
+            cache[a] = (xa, fa, ga)
+            return fa
+        for it in range(1, max_iter + 1):
+            if np.abs(g).max() <= self.g_tol:
+                return x, f, True
+            d = self.direction(g)
+            dphi0 = g @ d
+            if dphi0 >= 0:   # not a descent direction: restart from steepest descent
+                self.S.clear()
+                self.Y.clear()
+                d, dphi0 = -g, -(g @ g)
+            cache.clear()
+            a, fa, _ = backtracking(lambda t: phi(t, x, d), f, dphi0)
+            xn, fn, gn = cache[a]
+            s, y = xn - x, gn - g
+            if s @ y > 0:
+                self.S.append(s)
+                self.Y.append(y)
+                if len(self.S) > self.m:
+                    self.S.pop(0)
+                    self.Y.pop(0)
+            converged = self.rel_tol is not None and abs(fn - f) <= self.rel_tol * abs(f)
+            x, f, g = xn, fn, gn
+            if callback:
+                callback(it, x, f)
+            if converged:
+                return x, f, True
+        return x, f, False
+
+
 class Inversion:
     """One inversion problem on a device context (SWE2D): the forward model
     (Q0, nsteps SSP-RK2 steps of dt), the observations (truth fields), the
@@ -209,19 +311,40 @@ class Inversion:
     def run(self, theta0, verbose=False):
         """The optimiser sequence of optimize_parameters_inversion
         (swe_2D_inversion.jl:484-700): each optimiser runs its max_iterations
-        from where the previous one stopped; max_iterations <= 0 skips it.
-        Returns the final theta and the ITER / LOSS / PARS histories."""
+        from where the previous one stopped; max_iterations <= 0 skips it; an
+        LBFGS stage that converges ends the sequence, as the reference's loop
+        breaks on a successful solve.  Returns the final theta and the ITER /
+        LOSS / PARS histories."""
         theta = np.array(theta0, dtype=np.float64)
         ITER, LOSS, PARS = [], [], []
-        for name, lr, iters in zip(self.s.optimizers, self.s.learning_rates, self.s.max_iterations):
+        for k, (name, lr, iters) in enumerate(zip(self.s.optimizers, self.s.learning_rates, self.s.max_iterations)):
             if iters <= 0:
+                continue
+            if name == "LBFGS":
+                rel = self.s.rel_tols[k] if k < len(self.s.rel_tols) else None
+
+                def fg(x):
+                    parts, g, _ = self.loss_and_grad(x)
+                    return float(parts[0]), g
+
+                def cb(_, x, f):
+                    it = len(LOSS) + 1
+                    ITER.append(it)
+                    LOSS.append(float(f))
+                    PARS.append(x.copy())
+                    if verbose:
+                        print(f"iter_number = {it}, loss_total = {f}")
+                    self._save(it, float(f), x, ITER, LOSS, PARS)
+                theta, _, converged = LBFGS(rel_tol=rel).minimize(fg, theta, iters, callback=cb)
+                if converged:
+                    break
                 continue
             if name == "Adam":
                 opt = Adam(lr)
             elif name == "Descent":
                 opt = Descent(lr)
             else:
-                raise NotImplementedError(f"optimizer {name}: Adam and Descent are available")
+                raise ValueError(f"optimizer {name}: Adam, Descent and LBFGS are available")
             for _ in range(iters):
                 parts, g, _ = self.loss_and_grad(theta)
                 it = len(LOSS) + 1

@@ -168,3 +168,21 @@ def test_driver_total_gradient_and_adam_iterations(case, tmp_path):
     assert np.isclose(cb["loss_total"], res["LOSS"][7])
     ck = json.load(open(os.path.join(tmp_path, "checkpoint_inversion_iter_8.json")))
     assert ck["ITER"] == list(range(1, 9)) and len(ck["PARS"]) == 8
+
+
+def test_lbfgs_stage_after_adam_lowers_the_loss(case, tmp_path):
+    """The reference's optimiser sequence with its LBFGS stage enabled: 4 Adam
+    iterations, then up to 4 LBFGS iterations (backtracking line search on the
+    device's loss and gradient) that lower the loss further, one history
+    entry and callback file per iteration."""
+    d, obs = case
+    ctx, _, N = setup_pair(d, "fp64")
+    Q0 = initial_state(d, N)
+    s = InversionSettings(active_param="ManningN", wse_loss=True, uv_loss=True, optimizers=["Adam", "LBFGS"],
+                          learning_rates=[0.002, 0.0], max_iterations=[4, 4])
+    inv = Inversion(ctx, d, Q0, NSTEPS, DT, obs, s, mat_id=d["mat_id"], case_path=str(tmp_path))
+    res = inv.run(np.full(len(d["manning_zones"]), 0.03))
+    n = len(res["LOSS"])
+    assert 5 <= n <= 8 and res["ITER"] == list(range(1, n + 1))
+    assert res["LOSS"][-1] < res["LOSS"][3]
+    assert os.path.exists(os.path.join(tmp_path, f"inversion_callback_save_iter_{n}.json"))

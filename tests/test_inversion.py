@@ -1,11 +1,13 @@
 """Inversion driver pieces without a GPU: the regularisers and their
 gradients, the cell-gradient operator (pinned to the reference's bed slope),
-the optimisers, and the run-control settings."""
+the optimisers (Adam, Descent, L-BFGS with backtracking), the optimiser
+sequence, and the run-control settings."""
 import numpy as np
 import pytest
 
 from hydrograd_gb import HostMesh
-from hydrograd_gb.inversion import Adam, CellGradient, Descent, InversionSettings, bound_loss, slope_loss
+from hydrograd_gb.inversion import (LBFGS, Adam, CellGradient, Descent, Inversion, InversionSettings, backtracking,
+                                    bound_loss, slope_loss)
 from tests.golden_cases import load_fixture
 
 
@@ -91,3 +93,53 @@ def test_settings_from_run_control():
     s = InversionSettings.from_run_control(opts)
     assert (s.active_param, s.uv_loss, s.bound_loss, s.slope_loss) == ("ManningN", True, True, False)
     assert s.optimizers == ["Adam", "LBFGS"] and s.max_iterations == [300, 0]
+
+
+def test_backtracking_takes_the_quadratic_minimiser_first():
+    """phi(a) = (a - 0.3)^2 from a = 1: Armijo fails, the quadratic through
+    phi(0), phi'(0) and phi(1) has its minimum at 0.3, inside [0.1, 0.5]."""
+    phi = lambda a: (a - 0.3) ** 2
+    a, pa, n = backtracking(phi, phi(0.0), -0.6)
+    assert abs(a - 0.3) <= 1e-15 and pa <= 1e-30 and n == 2
+
+
+def test_backtracking_keeps_steps_within_bounds():
+    """A steep rise: the interpolated step is clamped to 0.1 of the last."""
+    phi = lambda a: -a + 1e6 * a * a
+    a, pa, n = backtracking(phi, 0.0, -1.0)
+    assert pa <= 0.0 + 1e-4 * a * -1.0 and a < 1e-5 and n > 2
+
+
+def test_lbfgs_minimizes_rosenbrock():
+    def fg(x):
+        return (100 * (x[1] - x[0] ** 2) ** 2 + (1 - x[0]) ** 2,
+                np.array([-400 * x[0] * (x[1] - x[0] ** 2) - 2 * (1 - x[0]), 200 * (x[1] - x[0] ** 2)]))
+    opt = LBFGS()
+    x, f, conv = opt.minimize(fg, np.array([-1.2, 1.0]), 200)
+    assert conv and np.abs(x - 1.0).max() <= 1e-8 and len(opt.S) <= 10
+
+
+class QuadraticInversion(Inversion):
+    """The driver's optimiser sequence on loss 0.5 |A theta - b|^2 (no device)."""
+
+    def __init__(self, settings):
+        self.s, self.case_path = settings, None
+        r = np.random.default_rng(3)
+        self.A, self.b = r.normal(size=(8, 4)), r.normal(size=8)
+
+    def loss_and_grad(self, theta):
+        e = self.A @ theta - self.b
+        return (0.5 * e @ e, 0.0, 0.0, 0.0, 0.0, 0.0), self.A.T @ e, None
+
+
+def test_optimiser_sequence_adam_then_lbfgs():
+    """Adam for 5 iterations, then LBFGS to the least-squares solution; the
+    histories hold one entry per iteration and the LBFGS stage converges."""
+    s = InversionSettings(optimizers=["Adam", "LBFGS"], learning_rates=[0.01, 0.0], max_iterations=[5, 100],
+                          rel_tols=[0.0, 1e-14])
+    inv = QuadraticInversion(s)
+    out = inv.run(np.zeros(4))
+    x = np.linalg.lstsq(inv.A, inv.b, rcond=None)[0]
+    assert np.abs(out["theta"] - x).max() <= 1e-6
+    assert out["ITER"] == list(range(1, len(out["LOSS"]) + 1)) and 5 < len(out["LOSS"]) < 105
+    assert out["LOSS"][-1] <= out["LOSS"][4]
