@@ -40,7 +40,8 @@ struct AdjointBuffers {
   double *mu1 = nullptr, *mu2 = nullptr, *gzb = nullptr;
   double* userOut = nullptr;   // [2 n] the n and zb gradients in the caller's cell order
   int32_t* probes = nullptr;
-  int32_t* probeCsr = nullptr;   // FP32C: probes grouped by cell (ProbeCsr), <= 3 P + 1 entries
+  int32_t* probeCsr = nullptr;   // FP32C: probes grouped by cell (ProbeCsr), <= 4 P + 1 entries
+  std::vector<int32_t> bndIndexOf;   // device cell -> its index among the boundary cells, or -1
   double* obs = nullptr;
   size_t probeCap = 0, obsCap = 0;
   double* segTot = nullptr;      // FP32C: inlet totals of a segment's states
@@ -186,6 +187,9 @@ int setup(hg_ctx* c) {
   }
   a.bndCells = dBnd;
   a.nBndCells = (int32_t)bnd.size();
+  b->bndIndexOf.assign(N, -1);
+  for (size_t i = 0; i < bnd.size(); ++i) b->bndIndexOf[bnd[i]] = (int32_t)i;
+  ADJ_CUDA(c, falloc(b, &a.bndProbe, bnd.size()));
   a.bndInOff = dBOff;
   a.bndInGrp = dBGrp;
   a.bndInCoef = dBCoef;
@@ -281,7 +285,7 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
     b->probes = nullptr;
     b->probeCsr = nullptr;
     ADJ_CUDA(c, cudaMalloc(&b->probes, std::max(P, 1) * sizeof(int32_t)));
-    ADJ_CUDA(c, cudaMalloc(&b->probeCsr, (3 * (size_t)std::max(P, 1) + 1) * sizeof(int32_t)));
+    ADJ_CUDA(c, cudaMalloc(&b->probeCsr, (4 * (size_t)std::max(P, 1) + 1) * sizeof(int32_t)));
     b->probeCap = std::max(P, 1);
   }
   const size_t nobs = (size_t)K * std::max(P, 0);
@@ -294,8 +298,9 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
   std::vector<int32_t> pdev(std::max(P, 0));
   for (int p = 0; p < P; ++p) pdev[p] = c->inv[probeCells[p]];
   // The same probes grouped by cell (distinct cells in order of first
-  // appearance, each with its probe indices in increasing order).
-  std::vector<int32_t> csr;
+  // appearance, each with its probe indices in increasing order), whether each
+  // is a boundary cell, and for each boundary cell its probe cell, if any.
+  std::vector<int32_t> csr, bndProbe(a.nBndCells, -1);
   ProbeCsr pc;
   {
     std::vector<int32_t> cells, off(1, 0), idx;
@@ -308,17 +313,30 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
       for (int32_t p : at[cell]) idx.push_back(p);
       off.push_back((int32_t)idx.size());
     }
+    std::vector<int32_t> isBnd(cells.size(), 0);
+    for (size_t u = 0; u < cells.size(); ++u) {
+      const int32_t i = b->bndIndexOf[cells[u]];
+      if (i >= 0) {
+        isBnd[u] = 1;
+        bndProbe[i] = (int32_t)u;
+      }
+    }
     csr = cells;
     csr.insert(csr.end(), off.begin(), off.end());
     csr.insert(csr.end(), idx.begin(), idx.end());
+    csr.insert(csr.end(), isBnd.begin(), isBnd.end());
     pc.cell = b->probeCsr;
     pc.off = b->probeCsr + cells.size();
     pc.idx = b->probeCsr + 2 * cells.size() + 1;
+    pc.isBnd = b->probeCsr + 2 * cells.size() + 1 + P;
     pc.nCells = (int32_t)cells.size();
   }
   if (P > 0) {
     ADJ_CUDA(c, cudaMemcpyAsync(b->probes, pdev.data(), P * sizeof(int32_t), cudaMemcpyHostToDevice, st));
     ADJ_CUDA(c, cudaMemcpyAsync(b->probeCsr, csr.data(), csr.size() * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+    if (a.nBndCells > 0)
+      ADJ_CUDA(c, cudaMemcpyAsync(a.bndProbe, bndProbe.data(), bndProbe.size() * sizeof(int32_t),
+                                  cudaMemcpyHostToDevice, st));
     ADJ_CUDA(c, cudaMemcpyAsync(b->obs, obs, nobs * sizeof(double), cudaMemcpyHostToDevice, st));
   }
   // Accumulators and dt.
@@ -572,11 +590,16 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
         hydro((s + 1) * dt);
         c->launches += launch_vjp_f32(m1, a, q1, mu2, nullptr, mu1, 0.5f, 0.0f, 0.5 * dt, st);
         hydro(s * dt);
-        c->launches += launch_vjp_f32(m0, a, q0, mu1, mu2, mu2, 1.0f, 0.5f, dt, st);
+        // with the probe terms of q0, the state after step s - 1, in the same launches
+        ProbeJob pj;
         if (s >= 1 && P > 0) {
-          launch_probe_f32(dm, a, q0, mu2, pc, b->probes, b->obs + (size_t)(s - 1) * P, P, scale, st);
-          c->launches += 1;
+          pj.pc = pc;
+          pj.probes = b->probes;
+          pj.obs = b->obs + (size_t)(s - 1) * P;
+          pj.np = P;
+          pj.scale = scale;
         }
+        c->launches += launch_vjp_f32(m0, a, q0, mu1, mu2, mu2, 1.0f, 0.5f, dt, st, &pj);
       }
     }
   }

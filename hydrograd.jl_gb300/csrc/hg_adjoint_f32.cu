@@ -412,9 +412,63 @@ __global__ void __launch_bounds__(64) k_vjp_bnd_f32(DevMesh m, AdjDev a, StateF3
 // After both VJP kernels: each boundary cell's terms into out (when wet) and
 // the n / zb accumulators, then its inlet total_A terms (bc_2D.jl:673-676:
 // total_A = sum L^(5/3) h / n over the group's wet cells) into out and gN.
-__global__ void __launch_bounds__(128) k_vjp_combine_f32(DevMesh m, AdjDev a, StateF32 Q, float* out, float beta,
-                                                         double betaD) {
+__device__ __forceinline__ double depth_f64(const DevMesh& m, StateF32 Q, int c) {
+  const float4 x = Q.x[c];
+  const float4 cp = m.CP[c];
+  return ((double)x.x + (double)x.y) + ((double)cp.x + (double)cp.y);
+}
+
+// The seed of distinct probe cell u: mu_xi[c] += sum over the probes at c (in
+// probe order) of scale 2 (h - obs_p), when c is wet.
+__device__ __forceinline__ void probe_seed(const DevMesh& m, StateF32 Q, float* mu, const ProbeCsr& pc,
+                                           const double* __restrict__ obs, double scale, int u) {
+  const int c = pc.cell[u];
+  const float4 cp = m.CP[c];
+  const SideF32 L = make_side_f32(Q.x[c], cp, m.hsmf, m.hsmLo);
+  if (L.s.dry) return;
+  const double h = depth_f64(m, Q, c);
+  double acc = 0.0;
+  for (int i = pc.off[u]; i < pc.off[u + 1]; ++i) acc += scale * 2.0 * (h - obs[pc.idx[i]]);
+  mu[c] += (float)acc;
+}
+
+// The probe terms of a state Q of the run, by one whole block: its loss sum
+// over the probes p of (h - obs_p)^2 into a.loss (a fixed-order reduction) and
+// the seeds of the probe cells (skipBnd: not those that are boundary cells,
+// whose seed the combine adds after its own terms).
+__device__ __forceinline__ void probe_block(const DevMesh& m, const AdjDev& a, StateF32 Q, float* mu,
+                                            const ProbeCsr& pc, const int32_t* __restrict__ probes,
+                                            const double* __restrict__ obs, int np, double scale, bool skipBnd) {
+  for (int u = threadIdx.x; u < pc.nCells; u += blockDim.x)
+    if (!skipBnd || !pc.isBnd[u]) probe_seed(m, Q, mu, pc, obs, scale, u);
+  double s = 0.0;
+  for (int p = threadIdx.x; p < np; p += blockDim.x) {
+    const double e = depth_f64(m, Q, probes[p]) - obs[p];
+    s += e * e;
+  }
+  const double t = block_sum(s);
+  if (threadIdx.x == 0) a.loss[0] += t;
+}
+
+// In the reverse sweep, with no combine to join: the probe terms of the state.
+__global__ void __launch_bounds__(256) k_probe_f32(DevMesh m, AdjDev a, StateF32 Q, float* mu, ProbeCsr pc,
+                                                   const int32_t* __restrict__ probes,
+                                                   const double* __restrict__ obs, int np, double scale) {
   pdl_enter();
+  probe_block(m, a, Q, mu, pc, probes, obs, np, scale, false);
+}
+
+// pj.np > 0 (the stage-1 VJP of a step with probes): the last block does the
+// probe terms of the VJP's state (the seeds of probe cells that are not
+// boundary cells, and the loss), and each boundary cell that is a probe cell
+// adds its seed after its own terms -- the order of two separate kernels.
+__global__ void __launch_bounds__(128) k_vjp_combine_f32(DevMesh m, AdjDev a, StateF32 Q, float* out, float beta,
+                                                         double betaD, ProbeJob pj) {
+  pdl_enter();
+  if (pj.np > 0 && blockIdx.x == gridDim.x - 1) {
+    probe_block(m, a, Q, out, pj.pc, pj.probes, pj.obs, pj.np, pj.scale, true);
+    return;
+  }
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.nBndCells) return;
   const int j = a.bndCells[i];
@@ -434,40 +488,7 @@ __global__ void __launch_bounds__(128) k_vjp_combine_f32(DevMesh m, AdjDev a, St
     out[j] += (float)(betaD * gTA * coef / nm);
     if (a.wantN) a.gN[j] += betaD * gTA * (-coef * (double)L.s.h / (nm * nm));
   }
-}
-
-__device__ __forceinline__ double depth_f64(const DevMesh& m, StateF32 Q, int c) {
-  const float4 x = Q.x[c];
-  const float4 cp = m.CP[c];
-  return ((double)x.x + (double)x.y) + ((double)cp.x + (double)cp.y);
-}
-
-// The probe terms of a state Q of the run, in the reverse sweep: its loss
-// sum over the probes p of (h - obs_p)^2 into a.loss (one block, a
-// fixed-order reduction), and the seed mu_xi[c] += sum over the probes at c
-// (in probe order) of scale 2 (h - obs_p) at each distinct probe cell c that
-// is wet.
-__global__ void __launch_bounds__(256) k_probe_f32(DevMesh m, AdjDev a, StateF32 Q, float* mu, ProbeCsr pc,
-                                                   const int32_t* __restrict__ probes,
-                                                   const double* __restrict__ obs, int np, double scale) {
-  pdl_enter();
-  for (int u = threadIdx.x; u < pc.nCells; u += blockDim.x) {
-    const int c = pc.cell[u];
-    const float4 cp = m.CP[c];
-    const SideF32 L = make_side_f32(Q.x[c], cp, m.hsmf, m.hsmLo);
-    if (L.s.dry) continue;
-    const double h = depth_f64(m, Q, c);
-    double acc = 0.0;
-    for (int i = pc.off[u]; i < pc.off[u + 1]; ++i) acc += scale * 2.0 * (h - obs[pc.idx[i]]);
-    mu[c] += (float)acc;
-  }
-  double s = 0.0;
-  for (int p = threadIdx.x; p < np; p += blockDim.x) {
-    const double e = depth_f64(m, Q, probes[p]) - obs[p];
-    s += e * e;
-  }
-  const double t = block_sum(s);
-  if (threadIdx.x == 0) a.loss[0] += t;
+  if (pj.np > 0 && a.bndProbe[i] >= 0) probe_seed(m, Q, out, pj.pc, pj.obs, pj.scale, a.bndProbe[i]);
 }
 
 __global__ void k_fold_accumulators_f32(DevMesh m, AdjDev a) {
@@ -527,22 +548,29 @@ void launch_vjp_interior(const DevMesh& m, const AdjDev& a, StateF32 Q, const fl
 // on the context's stream, running side by side), then the combine.
 template <int NS>
 int launch_vjp_ns(const DevMesh& m, const AdjDev& a, StateF32 Q, const float* mu, const float* extra, float* out,
-                  float cSelf, float cExtra, double betaD, cudaStream_t st) {
+                  float cSelf, float cExtra, double betaD, cudaStream_t st, const ProbeJob* pj) {
   const float beta = (float)betaD;
   const int nbb = (a.nBndCells + 63) / 64;
+  const bool probes = pj && pj->np > 0;
   if (nbb) launch_k(true, k_vjp_bnd_f32<NS>, nbb, 64, 0, st, m, a, Q, mu, betaD);
   launch_vjp_interior<NS>(m, a, Q, mu, extra, out, cSelf, cExtra, beta, nbb > 0, st);
-  if (!nbb) return 1;
-  launch_k(true, k_vjp_combine_f32, (a.nBndCells + 127) / 128, 128, 0, st, m, a, Q, out, beta, betaD);
+  if (!nbb) {
+    if (probes)
+      launch_k(true, k_probe_f32, 1, 256, 0, st, m, a, Q, out, pj->pc, pj->probes, pj->obs, pj->np, pj->scale);
+    return probes ? 2 : 1;
+  }
+  const ProbeJob none;
+  launch_k(true, k_vjp_combine_f32, (a.nBndCells + 127) / 128 + (probes ? 1 : 0), 128, 0, st, m, a, Q, out, beta,
+           betaD, probes ? *pj : none);
   return 3;
 }
 }  // namespace
 
 int launch_vjp_f32(const DevMesh& m, const AdjDev& a, StateF32 Q, const float* mu, const float* extra, float* out,
-                   float cSelf, float cExtra, double betaD, cudaStream_t st) {
-  if (m.nslot <= 3) return launch_vjp_ns<3>(m, a, Q, mu, extra, out, cSelf, cExtra, betaD, st);
-  if (m.nslot <= 4) return launch_vjp_ns<4>(m, a, Q, mu, extra, out, cSelf, cExtra, betaD, st);
-  return launch_vjp_ns<8>(m, a, Q, mu, extra, out, cSelf, cExtra, betaD, st);
+                   float cSelf, float cExtra, double betaD, cudaStream_t st, const ProbeJob* pj) {
+  if (m.nslot <= 3) return launch_vjp_ns<3>(m, a, Q, mu, extra, out, cSelf, cExtra, betaD, st, pj);
+  if (m.nslot <= 4) return launch_vjp_ns<4>(m, a, Q, mu, extra, out, cSelf, cExtra, betaD, st, pj);
+  return launch_vjp_ns<8>(m, a, Q, mu, extra, out, cSelf, cExtra, betaD, st, pj);
 }
 void launch_probe_f32(const DevMesh& m, const AdjDev& a, StateF32 Q, float* mu, const ProbeCsr& pc,
                       const int32_t* probes, const double* obs, int32_t nprobe, double scale, cudaStream_t st) {

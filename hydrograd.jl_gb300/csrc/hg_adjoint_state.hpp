@@ -41,6 +41,8 @@ struct AdjDev {
   // finished, boundary-VJP blocks finished}; zero between launches (the last
   // CTA or block out resets its counters).
   unsigned int* tileTicket = nullptr;
+  // [nBndCells] the probe cell (ProbeCsr index) each boundary cell is, or -1.
+  int32_t* bndProbe = nullptr;
   // The gradients the caller asked for: the FP32C VJP accumulates the n or
   // the bed (S0, exit-H) terms only when wanted.
   int32_t wantN = 1, wantZb = 1;
@@ -64,13 +66,23 @@ void launch_probe_adjoint_f64(const DevMesh& m, const double* Q, double* mu, con
 // dependent launch), then the combine kernel.  beta = betaD as FP32.
 // Returns the launches made.
 int launch_vjp_f32(const DevMesh& m, const AdjDev& a, StateF32 Q, const float* mu, const float* extra, float* out,
-                   float cSelf, float cExtra, double betaD, cudaStream_t st);
+                   float cSelf, float cExtra, double betaD, cudaStream_t st, const struct ProbeJob* pj = nullptr);
 // Probes grouped by cell: cell[u] (distinct, device order) holds probes idx[off[u] .. off[u+1]).
 struct ProbeCsr {
   const int32_t* cell = nullptr;
   const int32_t* off = nullptr;
   const int32_t* idx = nullptr;
+  const int32_t* isBnd = nullptr;   // [nCells] 1: a boundary cell (its seed comes with the combine)
   int32_t nCells = 0;
+};
+// The probe terms of the VJP's state, done by the stage-1 VJP's combine launch
+// (np = 0: none).
+struct ProbeJob {
+  ProbeCsr pc;
+  const int32_t* probes = nullptr;
+  const double* obs = nullptr;
+  int32_t np = 0;
+  double scale = 0.0;
 };
 // The probe loss of state Q (into a.loss) and its seed into mu (one kernel).
 void launch_probe_f32(const DevMesh& m, const AdjDev& a, StateF32 Q, float* mu, const ProbeCsr& pc,
