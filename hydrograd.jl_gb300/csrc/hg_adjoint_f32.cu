@@ -458,12 +458,15 @@ __global__ void __launch_bounds__(256) k_probe_f32(DevMesh m, AdjDev a, StateF32
   probe_block(m, a, Q, mu, pc, probes, obs, np, scale, false);
 }
 
+// 256-thread blocks: the probe block reduces the loss in the order of the
+// standalone k_probe_f32.
+constexpr int kCombineBlock = 256;
 // pj.np > 0 (the stage-1 VJP of a step with probes): the last block does the
 // probe terms of the VJP's state (the seeds of probe cells that are not
 // boundary cells, and the loss), and each boundary cell that is a probe cell
 // adds its seed after its own terms -- the order of two separate kernels.
-__global__ void __launch_bounds__(128) k_vjp_combine_f32(DevMesh m, AdjDev a, StateF32 Q, float* out, float beta,
-                                                         double betaD, ProbeJob pj) {
+__global__ void __launch_bounds__(kCombineBlock) k_vjp_combine_f32(DevMesh m, AdjDev a, StateF32 Q, float* out,
+                                                                   float beta, double betaD, ProbeJob pj) {
   pdl_enter();
   if (pj.np > 0 && blockIdx.x == gridDim.x - 1) {
     probe_block(m, a, Q, out, pj.pc, pj.probes, pj.obs, pj.np, pj.scale, true);
@@ -560,8 +563,8 @@ int launch_vjp_ns(const DevMesh& m, const AdjDev& a, StateF32 Q, const float* mu
     return probes ? 2 : 1;
   }
   const ProbeJob none;
-  launch_k(true, k_vjp_combine_f32, (a.nBndCells + 127) / 128 + (probes ? 1 : 0), 128, 0, st, m, a, Q, out, beta,
-           betaD, probes ? *pj : none);
+  launch_k(true, k_vjp_combine_f32, (a.nBndCells + kCombineBlock - 1) / kCombineBlock + (probes ? 1 : 0), kCombineBlock,
+           0, st, m, a, Q, out, beta, betaD, probes ? *pj : none);
   return 3;
 }
 }  // namespace
