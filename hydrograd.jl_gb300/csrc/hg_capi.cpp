@@ -23,6 +23,10 @@ namespace {
 
 thread_local std::string g_err;
 
+// Smallest CFL step accepted by default: swe_2D_consts.dt_min, which the
+// reference sets to 0.001 s (solve_swe_2D.jl:83,98) and stores unused.
+constexpr double kDtMinDefault = 0.001;
+
 int fail(hg_ctx* ctx, int code, const std::string& msg) {
   if (ctx) ctx->err = msg;
   else g_err = msg;
@@ -140,6 +144,9 @@ int check_flags(hg_ctx* c) {
   HG_CUDA(c, cudaStreamSynchronize(c->stream));
   if (f & 2) return fail(c, HG_ERR_INLET, "inlet-Q total conveyance is not positive (all inlet cells dry?)");
   if (f & 1) return fail(c, HG_ERR_STATE, "non-finite value in the state");
+  if (f & 8)
+    return fail(c, HG_ERR_STATE, "the CFL time step fell below dt_min (" + std::to_string(c->ds.dtMin) +
+                                     " s; hg_set_dt_min): the state is collapsing");
   return HG_OK;
 }
 
@@ -654,6 +661,14 @@ int hg_set_exit_wse(hg_ctx* ctx, const double* w, int32_t n) {
   cudaSetDevice(ctx->device);
   ctx->exitWse.assign(w, w + n);
   return upload_boundary_values(ctx);
+}
+
+int hg_set_dt_min(hg_ctx* ctx, double dt_min) {
+  if (!ctx) return fail(ctx, HG_ERR_ARG, "hg_set_dt_min: null context");
+  if (!(dt_min >= 0.0) || !std::isfinite(dt_min)) return fail(ctx, HG_ERR_ARG, "hg_set_dt_min: dt_min must be >= 0");
+  ctx->ds.dtMin = dt_min;
+  ctx->graphValid = false;   // captured launches hold the scalars descriptor by value
+  return HG_OK;
 }
 
 int hg_set_riemann_solver(hg_ctx* ctx, int32_t solver) {
@@ -1235,6 +1250,7 @@ int ctx_setup_device(hg_ctx* c) {
   HG_CUDA(c, dalloc(c, &c->ds.stepIdx, 1));
   HG_CUDA(c, dalloc(c, &c->ds.tSum, 1));
   HG_CUDA(c, dalloc(c, &c->ds.flags, 1));
+  c->ds.dtMin = kDtMinDefault;
   HG_CUDA(c, dalloc(c, &c->d_tot, (size_t)2 * kMaxFusedInlets));
   // Fused FP32 stepping: the stage blocks holding inlet-Q cells, numbered in block order.
   std::vector<int32_t> blockSlot;

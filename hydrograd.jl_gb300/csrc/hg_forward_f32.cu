@@ -288,6 +288,7 @@ __device__ __forceinline__ void stage_finish(const DevMesh& m, const DevScalars&
 // the CFL buffer stage 2 publishes into.
 __device__ __forceinline__ void fused_record(const DevScalars& s, const StageFuse& f) {
   const double dt = fused_dt(s, f);
+  if (f.cflMode && !(dt >= s.dtMin)) atomicOr(s.flags, 8);   // the step collapsed (or is NaN)
   const int k = *s.stepIdx;
   if (k < s.dtCap) s.dtHist[k] = dt;
   *s.stepIdx = k + 1;
@@ -614,6 +615,7 @@ __global__ void k_step_begin(DevScalars s, int cflMode, double cfl) {
   if (cflMode) {
     const double m = fmin(__longlong_as_double((long long)*s.cflMin), (double)__uint_as_float(*s.cflMinF));
     *s.dt = cfl * m;
+    if (!(*s.dt >= s.dtMin)) atomicOr(s.flags, 8);   // the step collapsed (or is NaN)
     *s.cflMin = (unsigned long long)__double_as_longlong(INFINITY);
     *s.cflMinF = __float_as_uint(INFINITY);
   }

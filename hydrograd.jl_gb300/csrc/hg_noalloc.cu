@@ -61,6 +61,19 @@ extern "C" int hg_rhs_device_noalloc(hg_ctx* ctx, const double* d_Q, double* d_d
     ctx->err = "hg_rhs_device_noalloc: only FP64 contexts are supported";
     return HG_ERR_UNSUPPORTED;
   }
+  // An inlet hydrograph would need the evaluation time (hg_rhs writes Q(t)
+  // into the context's inlet-Q array first), and a state-dependent resistance
+  // writes the context's own per-cell n and LayerNorm buffers before every
+  // RHS: either would make this call read or write context memory that other
+  // calls on the context's stream use, so both are refused.
+  if (ctx->dm.nHydro > 0) {
+    ctx->err = "hg_rhs_device_noalloc: the context has an inlet hydrograph; use hg_rhs (it takes the time t)";
+    return HG_ERR_UNSUPPORTED;
+  }
+  if (ctx->dm.res.kind != hg::kResConstant) {
+    ctx->err = "hg_rhs_device_noalloc: the context has a state-dependent resistance; use hg_rhs";
+    return HG_ERR_UNSUPPORTED;
+  }
   if (ctx->dm.nInlet > HG_NOALLOC_MAX_INLETQ) {
     ctx->err = "hg_rhs_device_noalloc: the mesh has " + std::to_string(ctx->dm.nInlet) +
                " inlet-Q boundaries; at most " + std::to_string(HG_NOALLOC_MAX_INLETQ) + " are supported";
@@ -70,6 +83,7 @@ extern "C" int hg_rhs_device_noalloc(hg_ctx* ctx, const double* d_Q, double* d_d
     ctx->err = "hg_rhs_device_noalloc: device index out of range";
     return HG_ERR_ARG;
   }
+  (void)cudaGetLastError();   // an error left by earlier, unrelated work is not this call's
   cudaError_t e = cudaSetDevice(ctx->device);
   double* scratch = nullptr;
   if (e == cudaSuccess) e = scratch_address(ctx->device, &scratch);
@@ -94,6 +108,6 @@ extern "C" int hg_rhs_device_noalloc(hg_ctx* ctx, const double* d_Q, double* d_d
     ctx->err = std::string("hg_rhs_device_noalloc: ") + cudaGetErrorString(e);
     return HG_ERR_CUDA;
   }
-  ctx->launches += 1 + (m.nInlet > 0 ? 1 : 0);
+  ctx->launches += 1 + (m.nInlet > 0 ? 1 : 0);   // no resistance kernels: refused above
   return HG_OK;
 }

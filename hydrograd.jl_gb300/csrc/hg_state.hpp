@@ -122,8 +122,10 @@ struct DevScalars {
   double* dtHist = nullptr;               // [capacity] step sizes taken
   int32_t* stepIdx = nullptr;             // steps taken since the last reset
   double* tSum = nullptr;                 // sum of the steps taken
-  int32_t* flags = nullptr;               // bit 0: non-finite state, bit 1: inlet conveyance <= 1e-10
+  int32_t* flags = nullptr;               // bit 0: non-finite state, bit 1: inlet conveyance <= 1e-10,
+                                          // bit 3: a CFL step below dtMin
   int32_t dtCap = 0;
+  double dtMin = 0.0;                     // smallest CFL step accepted (swe_2D_consts.dt_min)
 };
 
 enum StageMode : int32_t { kModeRhs = 0, kModeStage1 = 1, kModeStage2 = 2, kModeEulerRef = 3 };

@@ -311,6 +311,12 @@ class SWE2D:
             raise ValueError("Riemann solver: Roe, HLL or HLLC")
         self._chk(lib().hg_set_riemann_solver(self.h, kinds[name]))
 
+    def set_dt_min(self, dt_min):
+        """hg_set_dt_min: CFL steps below dt_min (default 0.001 s, the
+        reference's swe_2D_consts.dt_min) make the stepping call raise HgError
+        (HG_ERR_STATE); 0 turns the check off."""
+        self._chk(lib().hg_set_dt_min(self.h, float(dt_min)))
+
     def set_adjoint_tape(self, nbytes=-1):
         """hg_set_adjoint_tape: memory for the adjoint's stage states.  -1 (the
         default): segments as long as fit in min(half the free device memory,

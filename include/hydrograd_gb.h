@@ -248,6 +248,14 @@ int hg_set_ude(hg_ctx* ctx, const hg_ude_desc* ude);
  * applies to every integrator, the RHS and the adjoint. */
 int hg_set_riemann_solver(hg_ctx* ctx, int32_t solver);
 
+/* Smallest CFL time step accepted (swe_2D_consts.dt_min, swe_2D_constants.jl:9;
+ * the reference sets 0.001 s, solve_swe_2D.jl:83,98, and never reads it).
+ * A CFL step below it -- a collapsing state, e.g. a dry front the scheme
+ * cannot hold -- makes the stepping call return HG_ERR_STATE (the steps are
+ * still taken; the device sets a flag the host reads after them).  Default
+ * 0.001 s; 0 turns the check off.  Fixed-dt and Tsit5 steps are not checked. */
+int hg_set_dt_min(hg_ctx* ctx, double dt_min);
+
 /* ---- forward ------------------------------------------------------------- */
 /* dQdt = swe_2d_rhs(Q, p, t) with host buffers (semi_discretize_swe_2D.jl:18-277). */
 int hg_rhs(hg_ctx* ctx, const double* Q, double t, double* dQdt);
@@ -365,7 +373,11 @@ int hg_advance_timed(hg_ctx* ctx, int32_t nsteps, double dt, double cfl, int32_t
  * and device synchronisation are not allowed).  It calls no cudaMalloc or
  * cudaFree: the scratch it needs (inlet-Q conveyance totals and an error-flag
  * word) is a static device array sized for HG_NOALLOC_MAX_INLETQ inlet-Q
- * boundaries; a context with more is rejected with HG_ERR_ARG.
+ * boundaries; a context with more is rejected with HG_ERR_ARG.  A context
+ * with an inlet hydrograph (its inlet Q depends on the time, which this call
+ * does not take) or a state-dependent resistance (whose kernels write the
+ * context's own per-cell n before every RHS) is rejected with
+ * HG_ERR_UNSUPPORTED: use hg_rhs for those.
  *   d_Q, d_dQ: device pointers to 3 n doubles in the device cell order
  *              (perm[device id] = caller id from hg_mesh_order with consts.order).
  *   d_flags:   device int32 that receives the error flags (bit 1: inlet-Q

@@ -50,3 +50,11 @@ def test_create_without_device_fails_loudly():
     with pytest.raises(HgError) as e:
         SWE2D(dam_break(8, 4, 4.0, 2.0))
     assert e.value.code == 4
+
+
+def test_setters_reject_a_null_context():
+    """Argument checks on the host, before any device work: a null context is
+    HG_ERR_ARG (1), also for hg_set_dt_min."""
+    L = _lib.lib()
+    assert L.hg_set_dt_min(None, 0.001) == 1
+    assert L.hg_set_riemann_solver(None, 0) == 1

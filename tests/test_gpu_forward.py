@@ -260,3 +260,23 @@ def test_shipped_cases_reach_reference_final_state(name, precision):
     ref = np.concatenate([d["xi_truth"], d["u_truth"] * (h + 1e-3), d["v_truth"] * (h + 1e-3)])
     scale = max(np.abs(ref[:N]).max(), np.abs(ref[N:]).max())
     assert np.abs(Q - ref).max() <= 2e-3 * scale
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32c"])
+def test_collapsing_cfl_step_is_reported(precision):
+    """The dry-bed pool of the reach diverges under SSP-RK2 at CFL 0.4 (a
+    property of the reference scheme, see tests/test_dry_bed.py): its third
+    CFL step is about 6e-6 s, far below the reference's dt_min of 0.001 s
+    (swe_2D_constants.jl:9, solve_swe_2D.jl:83).  The stepping call reports
+    it as HG_ERR_STATE; with the check off (dt_min = 0) the same steps pass."""
+    case = river_triangles(n=32, dry_land=True)
+    ctx, _, _ = setup_pair(case, precision)
+    with pytest.raises(HgError) as e:
+        ctx.integrate(case["Q0"], 3, cfl=0.4)
+    assert e.value.code == 5
+    assert "dt_min" in str(e.value) or "non-finite" in str(e.value)
+    ctx.set_dt_min(0.0)
+    _, dts = ctx.integrate(case["Q0"], 2, cfl=0.4)
+    assert dts.min() > 0.0
+    ctx.set_dt_min(0.001)
+    ctx.integrate(case["Q0"], 1, cfl=0.4)     # the first step is 0.63 s: accepted

@@ -95,3 +95,31 @@ def test_noalloc_rejects_too_many_inlet_boundaries():
     assert rc == 1
     with pytest.raises(HgError, match="at most 64"):
         ctx._chk(rc)
+
+
+def test_noalloc_refuses_hydrograph_and_state_dependent_resistance():
+    """A hydrograph makes the inlet Q depend on the time, which this entry
+    point does not take; a state-dependent resistance writes the context's
+    own per-cell n before every RHS.  Both are refused (HG_ERR_UNSUPPORTED),
+    and the context works again once the option is removed."""
+    case = _river()
+    N = len(case["cell_node_count"])
+    dev = torch.device("cuda:0")
+    q = torch.from_numpy(case["Q0"].copy()).to(dev)
+    out = torch.zeros(3 * N, dtype=torch.float64, device=dev)
+    ctx = _ctx(case)
+    ctx.set_inlet_hydrograph(0, [0.0, 100.0], [50.0, 150.0])
+    rc = _noalloc(ctx, q, out, torch.zeros(1, dtype=torch.int32, device=dev))
+    assert rc == 7
+    with pytest.raises(HgError, match="hydrograph"):
+        ctx._chk(rc)
+    ctx.set_inlet_hydrograph(0, [], [])
+    assert _noalloc(ctx, q, out, torch.zeros(1, dtype=torch.int32, device=dev)) == 0
+    ctx.set_manning_function("sigmoid", {"n_lower": 0.02, "n_upper": 0.05, "k": 4.0, "h_mid": 0.5})
+    rc = _noalloc(ctx, q, out, torch.zeros(1, dtype=torch.int32, device=dev))
+    assert rc == 7
+    with pytest.raises(HgError, match="resistance"):
+        ctx._chk(rc)
+    ctx.set_manning_function("constant")
+    assert _noalloc(ctx, q, out, torch.zeros(1, dtype=torch.int32, device=dev)) == 0
+    torch.cuda.synchronize()
