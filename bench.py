@@ -52,7 +52,9 @@ def load_peaks():
 STAGE_KERNELS = {0: ("k_stage_f32 (one block per 256-cell tile)", "k_stage_f32_river_tri_1M.md"),
                  1: ("k_stage_pipe_f32 (persistent; the next tile and its halo prefetched by cp.async)",
                      "k_stage_pipe_f32_river_tri_1M.md"),
-                 2: ("k_stage_tma_f32 (persistent; the next tile prefetched by bulk copies)", None)}
+                 2: ("k_stage_tma_f32 (persistent; the next tile prefetched by bulk copies)", None),
+                 3: ("k_stage_face_f32 (one block per 256-cell tile; each wet-wet face evaluated once)",
+                     "k_stage_face_f32_river_tri_1M.md")}
 
 
 def profile_traffic(precision, kernel=0):
@@ -259,6 +261,57 @@ def run_hll(args, case, device):
     out["error_fp32c_vs_fp64_state_rel_linf"] = float(np.abs(a - b).max() / np.abs(b).max())
     out["config"] = ("HLL flux (Harten-Lax-van Leer, Einfeldt wave speeds) on the 1M-cell reach, FP32C, CFL 0.4; "
                      "state error after 200 CFL steps against FP64 HLL")
+    return out
+
+
+def run_dry_start(args, device):
+    """Configuration 2 with its written start: the 1M-cell reach dry (h =
+    h_small) except a 1.5 m pool touching the inlet (river_triangles(708,
+    dry_land=True)), so the pool spreads over the dry bed in moving wet/dry
+    fronts.  The reference scheme diverges on a dry bed at any CFL-sized step
+    (a property of its Roe wall branch and friction, pinned by
+    tests/test_dry_bed.py), so the run takes a fixed step: the initial state's
+    CFL step at CFL 0.01.  FP32C rate over dry_steps steps (L2 flushed before
+    each), and FP32C against FP64 after the same steps: whole state and the
+    cells whose wet/dry status changed (the fronts)."""
+    from hydrograd_gb.workloads import river_triangles
+    case = river_triangles(n=args.n, dry_land=True)
+    N = len(case["cell_node_count"])
+    hst = case["wstill"] - case["zb_cells"]
+    K = args.dry_steps
+    out, final = {"cells": N, "steps": K}, {}
+    for prec in ("fp32c", "fp64"):
+        c = make_ctx(case, prec, device)
+        if prec == "fp32c":
+            c.set_dt_min(0.0)   # the CFL-0.01 step of this 1M-cell mesh is below the default dt_min (0.001 s)
+            dt = float(c.integrate(case["Q0"], 1, cfl=0.01)[1][0])   # the initial state's CFL-0.01 step
+            out["dt"] = dt
+            c.upload(case["Q0"])
+            c.advance_timed(args.warmup, dt=dt, flush_l2=True)
+            c.upload(case["Q0"])
+            ms = c.advance_timed(K, dt=dt, flush_l2=True)
+            out["fwd"] = {"value": N * K / (ms * 1e-3), "ms_per_step": ms / K}
+        final[prec], _ = c.integrate(case["Q0"], K, dt=out["dt"])
+        c.close()
+    a, b = final["fp32c"], final["fp64"]
+    wet0 = case["Q0"][:N] + hst > 1.5e-3
+    wet_a, wet_b = a[:N] + hst > 1.5e-3, b[:N] + hst > 1.5e-3
+    front = np.nonzero(wet0 != wet_b)[0]
+    scale = np.abs(b).max()
+    blk = [max(np.abs(b[j * N:(j + 1) * N]).max(), 1e-3 * scale) for j in range(3)]
+    out["wet_cells"] = [int(wet0.sum()), int(wet_b.sum())]
+    out["front_cells"] = int(len(front))
+    out["max_abs_q"] = float(np.abs(b[N:]).max())
+    out["error_fp32c_vs_fp64"] = {
+        "state_rel_linf": float(np.abs(a - b).max() / scale),
+        "block_rel_linf": [float(np.abs(a[j * N:(j + 1) * N] - b[j * N:(j + 1) * N]).max() / blk[j])
+                           for j in range(3)],
+        "front_block_rel_linf": [float(np.abs(a[j * N:(j + 1) * N][front] - b[j * N:(j + 1) * N][front]).max()
+                                       / blk[j]) if len(front) else 0.0 for j in range(3)],
+        "wet_dry_decisions_differing": int((wet_a != wet_b).sum())}
+    out["config"] = ("configuration 2 as written: 1M-cell reach dry except a 1.5 m pool at the inlet, moving "
+                     "wet/dry fronts; fixed dt = the initial CFL-0.01 step (the reference scheme diverges on a dry "
+                     "bed at CFL-sized steps); FP32C vs FP64 after the same steps")
     return out
 
 
@@ -551,6 +604,7 @@ def run_ours(args):
                          f"{len(probes)} probes (half on the pool rim, half at the inlet), loss = mean squared "
                          "departure of the probe depths from the lake at rest")
     hll = run_hll(args, case, local) if args.hll_steps > 0 else None
+    dry = run_dry_start(args, local) if args.dry_steps > 0 else None
     cfg1 = run_config1(args, local, cpu=not args.no_cpu and rank == 0) if args.config1_steps > 0 else None
     cfg5 = run_config5(args, local) if args.config5_steps > 0 else None
     ens = None
@@ -603,6 +657,7 @@ def run_ours(args):
         "fwd_adjoint": adj,
         "ensemble": ens,
         "hll": hll,
+        "dry_start": dry,
         "config1": cfg1,
         "config5": cfg5,
         "warm_value": f32["warm_value"], "simulated_seconds": f32["sim_time"],
@@ -636,6 +691,8 @@ def main():
     ap.add_argument("--ens-members", type=int, default=32, help="members per mesh")
     ap.add_argument("--hll-steps", type=int, default=500,
                     help="FP32C steps of the HLL-solver leg on the 1M-cell reach (0: skip)")
+    ap.add_argument("--dry-steps", type=int, default=2000,
+                    help="steps of the dry-start leg (configuration 2's written dry-pool start; 0: skip)")
     ap.add_argument("--config1-steps", type=int, default=1000,
                     help="configuration 1 (8,000-cell dam break) steps at dt = 0.01 s (0: skip)")
     ap.add_argument("--config5-steps", type=int, default=5000,

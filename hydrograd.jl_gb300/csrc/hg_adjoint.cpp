@@ -402,7 +402,8 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
     fl.ticket = b->finTicket;
   }
   const DevMesh& dm = c->dm;
-  const DevScalars& ds = c->ds;
+  DevScalars ds = c->ds;
+  ds.nMembers = 0;   // the adjoint takes one fixed dt for every member
   const int extraPerStep = 2 * dm.nInlet;
   // Inlet hydrographs at a stage's time (the run starts at t = 0): stage 1 of
   // step s at s dt, stage 2 at (s + 1) dt -- in the forward pass, the

@@ -157,6 +157,12 @@ int ensure_dt_capacity(hg_ctx* c, int32_t steps) {
   HG_CUDA(c, cudaMalloc(&p, (size_t)cap * sizeof(double)));
   if (c->ds.dtHist) cudaFree(c->ds.dtHist);
   c->ds.dtHist = p;
+  if (c->ds.nMembers > 0) {   // each member's steps: [cap][members]
+    double* pm = nullptr;
+    HG_CUDA(c, cudaMalloc(&pm, (size_t)cap * c->ds.nMembers * sizeof(double)));
+    if (c->ds.dtHistM) cudaFree(c->ds.dtHistM);
+    c->ds.dtHistM = pm;
+  }
   c->ds.dtCap = cap;
   c->graphValid = false;   // the captured scalars struct holds the old pointer
   return HG_OK;
@@ -186,7 +192,8 @@ int enqueue_download(hg_ctx* c, double* Q) {
 // the resistance does not depend on the state (the fused stage forms the next
 // stage's conveyance totals from its output state with the resident n).
 bool fused(const hg_ctx* c) {
-  return c->precision == HG_FP32C && c->dm.nInlet <= kMaxFusedInlets && c->dm.res.kind == kResConstant;
+  return c->precision == HG_FP32C && c->dm.nInlet <= kMaxFusedInlets && c->dm.res.kind == kResConstant &&
+         c->ds.nMembers == 0;
 }
 
 // Kernels per RHS evaluation besides the stage: resistance, inlet totals.
@@ -415,6 +422,90 @@ int install_resistance(hg_ctx* c, ResDev r, const double* ksUser, const double* 
   return HG_OK;
 }
 
+// Face-once stage tables (k_stage_face_f32): per tile of kStageBlockF32 cells
+// its faces, each listed once -- interior faces (both cells in the tile, or
+// one a halo cell) oriented from the lower cell id and in the order their
+// lower cell meets them, then the tile's boundary faces -- and per cell the
+// entry (face << 1 | side) of each edge slot.  SLp holds the pipelined
+// kernel's tile-local neighbour indices (halo cells kStageBlockF32 + j).
+// False when the tables do not fit their encodings: a tile with more than
+// kFaceMaxPerTile faces, a boundary-face index of more than 21 bits, or an
+// interior face that only one of its cells lists.
+bool build_face_tables(int N, int S, int nbf, const std::vector<int32_t>& nb, const std::vector<float4>& SL,
+                       const std::vector<float4>& SLp, std::vector<float4>& FL, std::vector<int32_t>& FLoff,
+                       std::vector<uint2>& FR, int32_t& faceMax) {
+  if (S > 4 || nbf >= (1 << 21) || SLp.size() != (size_t)S * N) return false;
+  const int nTiles = (N + kStageBlockF32 - 1) / kStageBlockF32;
+  FL.clear();
+  FLoff.assign((size_t)nTiles + 1, 0);
+  faceMax = 0;
+  std::vector<uint16_t> ref((size_t)N * 4, 0xFFFFu);
+  auto back_slot = [&](int v, int cell) {
+    for (int k = 0; k < S; ++k)
+      if (nb[(size_t)k * N + v] == cell) return k;
+    return -1;
+  };
+  auto with_ids = [](float4 r, int32_t w) {
+    std::memcpy(&r.w, &w, sizeof(float));
+    return r;
+  };
+  std::vector<float4> inner, bnd;
+  std::vector<size_t> bndRef;
+  for (int t = 0; t < nTiles; ++t) {
+    const int c0 = t * kStageBlockF32, c1 = std::min(N, c0 + kStageBlockF32);
+    inner.clear();
+    bnd.clear();
+    bndRef.clear();
+    for (int cell = c0; cell < c1; ++cell)
+      for (int k = 0; k < S; ++k) {
+        const size_t i = (size_t)k * N + cell;
+        const int32_t v = nb[i];
+        if (v == INT32_MIN) continue;
+        const int32_t la = cell - c0;
+        if (v < 0) {   // boundary face -1 - v
+          bnd.push_back(with_ids(SL[i], la | ((-1 - v) << 10) | kFaceBoundary));
+          bndRef.push_back((size_t)cell * 4 + k);
+          continue;
+        }
+        if (v >= c0 && v < c1) {   // both cells in the tile: listed once, by the lower id
+          if (v < cell) continue;
+          const int kb = back_slot(v, cell);
+          if (kb < 0) return false;
+          const uint16_t f = (uint16_t)inner.size();
+          inner.push_back(with_ids(SL[i], la | ((v - c0) << 10) | (1 << 20) | (1 << 21)));
+          ref[(size_t)cell * 4 + k] = (uint16_t)(f << 1);
+          ref[(size_t)v * 4 + kb] = (uint16_t)((f << 1) | 1);
+          continue;
+        }
+        int32_t lh;   // v's tile-local halo index
+        std::memcpy(&lh, &SLp[i].w, sizeof(int32_t));
+        const uint16_t f = (uint16_t)inner.size();
+        if (cell < v) {   // oriented from the own cell (side a)
+          inner.push_back(with_ids(SL[i], la | (lh << 10) | (1 << 20)));
+          ref[(size_t)cell * 4 + k] = (uint16_t)(f << 1);
+        } else {          // oriented from the halo cell: its slot's normal; the own cell is side b
+          const int kb = back_slot(v, cell);
+          if (kb < 0) return false;
+          inner.push_back(with_ids(SL[(size_t)kb * N + v], lh | (la << 10) | (1 << 21)));
+          ref[(size_t)cell * 4 + k] = (uint16_t)((f << 1) | 1);
+        }
+      }
+    const size_t nF = inner.size() + bnd.size();
+    if (nF > (size_t)kFaceMaxPerTile) return false;
+    faceMax = std::max(faceMax, (int32_t)nF);
+    for (size_t j = 0; j < bnd.size(); ++j) ref[bndRef[j]] = (uint16_t)((inner.size() + j) << 1);
+    FL.insert(FL.end(), inner.begin(), inner.end());
+    FL.insert(FL.end(), bnd.begin(), bnd.end());
+    FLoff[(size_t)t + 1] = (int32_t)FL.size();
+  }
+  FR.resize(N);
+  for (int c = 0; c < N; ++c) {
+    const uint16_t* r = &ref[(size_t)c * 4];
+    FR[c] = make_uint2((uint32_t)r[0] | ((uint32_t)r[1] << 16), (uint32_t)r[2] | ((uint32_t)r[3] << 16));
+  }
+  return true;
+}
+
 bool all_positive(const double* v, int n) {
   for (int i = 0; i < n; ++i)
     if (!(v[i] > 0.0)) return false;
@@ -428,6 +519,7 @@ hg_ctx::~hg_ctx() {
   if (stream) cudaStreamSynchronize(stream);
   for (void* p : allocs) cudaFree(p);
   if (ds.dtHist) cudaFree(ds.dtHist);
+  if (ds.dtHistM) cudaFree(ds.dtHistM);
   adjoint_release(this);
   if (stream) cudaStreamDestroy(stream);
 }
@@ -586,6 +678,20 @@ int hg_ensemble_create(const hg_ensemble_desc* e, const hg_consts* consts, int32
   }
   concat_host_meshes(parts, c->hm);
   return finish_create(c, consts, precision, device, out);
+}
+
+int hg_ensemble_steps(hg_ctx* ctx, int32_t nsteps, double* dts, double* t_elapsed) {
+  if (!ctx || nsteps < 0) return fail(ctx, HG_ERR_ARG, "hg_ensemble_steps: bad argument");
+  if (ctx->ds.nMembers == 0) return fail(ctx, HG_ERR_ARG, "hg_ensemble_steps: not an ensemble context");
+  if (nsteps > ctx->ds.dtCap) return fail(ctx, HG_ERR_ARG, "hg_ensemble_steps: more steps than recorded");
+  cudaSetDevice(ctx->device);
+  const size_t M = (size_t)ctx->ds.nMembers;
+  if (dts && nsteps > 0)
+    HG_CUDA(ctx, cudaMemcpyAsync(dts, ctx->ds.dtHistM, (size_t)nsteps * M * sizeof(double), cudaMemcpyDeviceToHost,
+                                 ctx->stream));
+  if (t_elapsed) HG_CUDA(ctx, cudaMemcpyAsync(t_elapsed, ctx->ds.tM, M * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  HG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return HG_OK;
 }
 
 int hg_ensemble_layout(const hg_ctx* ctx, int32_t* n_members, int32_t* cell_offset, int32_t* inlet_offset,
@@ -1251,6 +1357,33 @@ int ctx_setup_device(hg_ctx* c) {
   HG_CUDA(c, dalloc(c, &c->ds.tSum, 1));
   HG_CUDA(c, dalloc(c, &c->ds.flags, 1));
   c->ds.dtMin = kDtMinDefault;
+  // Ensembles: every member takes its own step.  Each member's cells form one
+  // contiguous range in the device order (the orderings keep members apart),
+  // at the member's offset of the caller order.
+  if (c->memberCellOff.size() >= 2) {
+    const int M = (int)c->memberCellOff.size() - 1;
+    for (int mm = 0; mm < M; ++mm)
+      for (int i = c->memberCellOff[mm]; i < c->memberCellOff[mm + 1]; ++i)
+        if (c->perm[i] < c->memberCellOff[mm] || c->perm[i] >= c->memberCellOff[mm + 1])
+          return fail(c, HG_ERR_MESH, "ensemble: a member's cells are not contiguous in the device order");
+    std::vector<int32_t> inletMember(std::max<size_t>(inletCell.empty() ? 0 : m.inletGroups.size(), 1), 0);
+    for (int mm = 0; mm < M; ++mm)
+      for (int g = c->memberInletOff[mm]; g < c->memberInletOff[mm + 1]; ++g) inletMember[g] = mm;
+    int32_t *dOff = nullptr, *dInM = nullptr;
+    HG_CUDA(c, dalloc(c, &dOff, (size_t)M + 1));
+    HG_CUDA(c, dalloc(c, &dInM, inletMember.size()));
+    HG_CUDA(c, upload(c, dOff, c->memberCellOff));
+    HG_CUDA(c, upload(c, dInM, inletMember));
+    HG_CUDA(c, dalloc(c, &c->ds.dtM, (size_t)M));
+    HG_CUDA(c, dalloc(c, &c->ds.dtMf, (size_t)M));
+    HG_CUDA(c, dalloc(c, &c->ds.tM, (size_t)M));
+    HG_CUDA(c, dalloc(c, &c->ds.cflMinM, (size_t)M));
+    HG_CUDA(c, dalloc(c, &c->ds.cflMinMF, (size_t)M));
+    c->ds.memberOff = dOff;
+    c->ds.inletMember = dInM;
+    c->ds.nMembers = M;
+    HG_CUDA(c, cudaStreamSynchronize(c->stream));
+  }
   HG_CUDA(c, dalloc(c, &c->d_tot, (size_t)2 * kMaxFusedInlets));
   // Fused FP32 stepping: the stage blocks holding inlet-Q cells, numbered in block order.
   std::vector<int32_t> blockSlot;
@@ -1333,6 +1466,22 @@ int ctx_setup_device(hg_ctx* c) {
     HG_CUDA(c, upload(c, d_SLp, SLp));
     HG_CUDA(c, upload(c, d_halo, halo));
   }
+  // Face-once stage tables (need the halo tables)
+  std::vector<float4> FL;
+  std::vector<int32_t> FLoff;
+  std::vector<uint2> FR;
+  int32_t faceMax = 0;
+  float4* d_FL = nullptr;
+  int32_t* d_FLoff = nullptr;
+  uint2* d_FR = nullptr;
+  if (!SLp.empty() && build_face_tables(N, S, nbf, nb, SL, SLp, FL, FLoff, FR, faceMax)) {
+    HG_CUDA(c, dalloc(c, &d_FL, FL.size()));
+    HG_CUDA(c, dalloc(c, &d_FLoff, FLoff.size()));
+    HG_CUDA(c, dalloc(c, &d_FR, FR.size()));
+    HG_CUDA(c, upload(c, d_FL, FL));
+    HG_CUDA(c, upload(c, d_FLoff, FLoff));
+    HG_CUDA(c, upload(c, d_FR, FR));
+  }
   c->h_area = to_float(area);
   HG_CUDA(c, upload(c, d_nb, nb));
   HG_CUDA(c, upload(c, c->d_blockSlot, blockSlot));
@@ -1364,6 +1513,10 @@ int ctx_setup_device(hg_ctx* c) {
   dm.SL = d_SL;
   dm.SLp = d_SLp;
   dm.halo = d_halo;
+  dm.FL = d_FL;
+  dm.FLoff = d_FLoff;
+  dm.FR = d_FR;
+  dm.faceMax = d_FL ? faceMax : 0;
   dm.stageKernel = d_SLp ? kStagePipe : kStageGather;
   dm.bfInfo = d_bfInfo; dm.bfLp23 = d_lp23; dm.bfLp23f = d_lp23f; dm.bfLp53 = d_bflp53;
   dm.bfExitRel = c->d_bfExitRel;

@@ -219,4 +219,84 @@ __device__ __forceinline__ void hll_flux_wet_f32(const Side<float>& L, const Own
   }
 }
 
+// ---------------------------------------------------------------------------
+// Face-once form (k_stage_face_f32)
+// ---------------------------------------------------------------------------
+// A face whose two sides are both wet takes the reference solver's wet path
+// (swe_2D_solvers.jl:79-164), which is antisymmetric under (a <-> b, n -> -n):
+// F(b, a, -n) = -F(a, b, n).  With the own pressure shift of
+// pressure_jump_f32 the two cells' terms are then
+//   c_a = F(a, b, n) - p_a n,   c_b = F(b, a, -n) + p_b n = -c_a + (p_b - p_a) n,
+// so the flux is evaluated once per face.  A face with a dry side takes the
+// dry / wall branches, which are not antisymmetric (the wall branch keeps the
+// dry side's xi; the one-side-dry branch uses the h-based pressure): each side
+// is evaluated from its own cell, as the per-cell loop does.
+
+// One side of a face, from the side records the face kernel forms once per
+// cell: the pairs of xi and hstill, the clamped depth, the masked momenta and
+// the velocity and sqrt(h) of own_f32.
+struct FaceSideF32 {
+  float xi, hst, h, hu, hv, u, v, s;
+};
+
+// Wet-wet Roe flux of side a (own pressure shift applied) through the face
+// with unit normal n from a to b; returns dp = p_b - p_a (pressure_jump_f32).
+// The algebra is roe_flux_wet_f32's, with b's velocity and sqrt(h) taken from
+// its side record instead of being formed again.
+__device__ __forceinline__ float roe_face_wet_f32(const FaceSideF32& A, const FaceSideF32& B, float dxi, float dhst,
+                                                  float g, float nx, float ny, float F[3]) {
+  const float rs = 1.0f / (A.s + B.s);
+  const float uRoe = (A.s * A.u + B.s * B.u) * rs;
+  const float vRoe = (A.s * A.v + B.s * B.v) * rs;
+  const float unRoe = uRoe * nx + vRoe * ny;
+  const float gh = g * ((A.h + B.h) * 0.5f);
+  const float rc = rsqrtf(gh);
+  const float cRoe = gh * rc;
+  const float d1 = B.hu - A.hu, d2 = B.hv - A.hv;
+  const float t = (unRoe * dxi - nx * d1 - ny * d2) * (0.5f * rc);
+  const float w0 = (ny * d1 - nx * d2 - (uRoe * ny - vRoe * nx) * dxi) * smooth_abs_f32(unRoe);
+  const float w1 = (0.5f * dxi + t) * smooth_abs_f32(unRoe - cRoe);
+  const float w2 = (0.5f * dxi - t) * smooth_abs_f32(unRoe + cRoe);
+  const float sum = w1 + w2, dif = cRoe * (w2 - w1);
+  const float A1 = ny * w0 + uRoe * sum + nx * dif;
+  const float A2 = -nx * w0 + vRoe * sum + ny * dif;
+  const float dp = pressure_jump_f32(g, A.xi, B.xi, dxi, B.hst, dhst);
+  F[0] = 0.5f * ((A.hu * nx + A.hv * ny) + (B.hu * nx + B.hv * ny) - sum);
+  F[1] = 0.5f * (((A.hu * A.u + B.hu * B.u) + dp) * nx + (A.hu * A.v + B.hu * B.v) * ny - A1);
+  F[2] = 0.5f * ((A.hv * A.u + B.hv * B.u) * nx + ((A.hv * A.v + B.hv * B.v) + dp) * ny - A2);
+  return dp;
+}
+
+// Wet-wet HLL flux of side a (own pressure shift applied), hll_flux_wet_f32's
+// algebra; returns dp = p_b - p_a.
+__device__ __forceinline__ float hll_face_wet_f32(const FaceSideF32& A, const FaceSideF32& B, float dxi, float dhst,
+                                                  float g, float nx, float ny, float F[3]) {
+  const float rs = 1.0f / (A.s + B.s);
+  const float uRoe = (A.s * A.u + B.s * B.u) * rs;
+  const float vRoe = (A.s * A.v + B.s * B.v) * rs;
+  const float unRoe = uRoe * nx + vRoe * ny;
+  const float cRoe = sqrtf(g * ((A.h + B.h) * 0.5f));
+  const float unL = A.u * nx + A.v * ny, unR = B.u * nx + B.v * ny;
+  const float cL = sqrtf(g * A.h), cR = sqrtf(g * B.h);
+  const float sL = fminf(unL - cL, unRoe - cRoe), sR = fmaxf(unR + cR, unRoe + cRoe);
+  const float dp = pressure_jump_f32(g, A.xi, B.xi, dxi, B.hst, dhst);
+  const float fL0 = A.hu * nx + A.hv * ny;
+  const float fL1 = A.hu * A.u * nx + A.hu * A.v * ny;
+  const float fL2 = A.hv * A.u * nx + A.hv * A.v * ny;
+  const float fR0 = B.hu * nx + B.hv * ny;
+  const float fR1 = B.hu * B.u * nx + B.hu * B.v * ny;
+  const float fR2 = B.hv * B.u * nx + B.hv * B.v * ny;
+  if (sL >= 0.0f) {
+    F[0] = fL0; F[1] = fL1; F[2] = fL2;
+  } else if (sR <= 0.0f) {
+    F[0] = fR0; F[1] = fR1 + dp * nx; F[2] = fR2 + dp * ny;
+  } else {
+    const float r = 1.0f / (sR - sL), sLR = sL * sR;
+    F[0] = (sR * fL0 - sL * fR0 + sLR * dxi) * r;
+    F[1] = (sR * fL1 - sL * fR1 - sL * dp * nx + sLR * (B.hu - A.hu)) * r;
+    F[2] = (sR * fL2 - sL * fR2 - sL * dp * ny + sLR * (B.hv - A.hv)) * r;
+  }
+  return dp;
+}
+
 }  // namespace hgd

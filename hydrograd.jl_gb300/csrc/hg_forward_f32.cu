@@ -17,6 +17,7 @@
 #include "hg_async.cuh"
 #include "hg_device.cuh"
 #include "hg_f32.cuh"
+#include "hg_members.cuh"
 #include "hg_pdl.cuh"
 #include "hg_reduce.cuh"
 #include "hg_state.hpp"
@@ -333,14 +334,16 @@ __global__ void __launch_bounds__(kBlock, stage_min_blocks<NS>())
     if (threadIdx.x == 0) dtShared = (float)fused_dt(s, f);
   }
   __syncthreads();
+  const int mem = (!FUSED && s.nMembers > 0 && active) ? member_of(s, c) : -1;   // an ensemble member's own step
   if (active) {
-    const float dt = MODE == kModeRhs ? 0.0f : (FUSED ? dtShared : *s.dtf);
+    const float dt = MODE == kModeRhs ? 0.0f : (FUSED ? dtShared : (mem >= 0 ? s.dtMf[mem] : *s.dtf));
     stage_cell<NS, MODE, false, RS>(m, s, Xin.x, sX, sP, nullptr, nullptr, base, c, sl, xin, cp, cs, Xin.q, Xbase.x,
                                      Xbase.q, c,
                          dt, FUSED ? f.totalIn : m.totalA, Xout, Rout, cfl, cand, hOut, wetOut);
   }
   if (FUSED && f.record && blockIdx.x == 0 && threadIdx.x == 0) fused_record(s, f);
-  if (cfl) block_min_publish_f(cand, FUSED ? s.cflMinF + (1 - f.parity) : s.cflMinF);
+  if (cfl && !FUSED && s.nMembers > 0) member_min_publish_f(s, cand, mem);
+  else if (cfl) block_min_publish_f(cand, FUSED ? s.cflMinF + (1 - f.parity) : s.cflMinF);
   if (FUSED && m.nInlet > 0) fused_inlet_totals<NS>(m, f, blockIdx.x, c, hOut, wetOut);
 }
 
@@ -560,20 +563,205 @@ __global__ void __launch_bounds__(kBlock, kPipeCtasPerSm)
     const int base = t * kBlock, c = base + tid;
     float hOut = 0.0f;
     bool wetOut = false;
+    const int mem = (!FUSED && s.nMembers > 0 && c < n) ? member_of(s, c) : -1;   // an ensemble member's own step
     if (c < n) {
       float4 sl[NS];
 #pragma unroll
       for (int k = 0; k < NS; ++k) sl[k] = bSL[k * kBlock + tid];
       stage_cell<NS, MODE, true, RS>(m, s, Xin.x, bX, bCP, bHX, bHP, base, c, sl, bX[tid], bCP[tid], bCS[tid], bQ, bXB,
-                                 bQB, tid, dtShared, FUSED ? f.totalIn : m.totalA, Xout, nullptr, cfl, cand, hOut,
-                                 wetOut);
+                                 bQB, tid, mem >= 0 ? s.dtMf[mem] : dtShared, FUSED ? f.totalIn : m.totalA, Xout,
+                                 nullptr, cfl, cand, hOut, wetOut);
+    }
+    if (!FUSED && cfl && s.nMembers > 0) {   // members: each tile's candidates into their members' minima
+      member_min_publish_f(s, cand, mem);
+      cand = INFINITY;
     }
     if (FUSED && m.nInlet > 0) fused_inlet_totals<NS>(m, f, t, c, hOut, wetOut);
     __syncthreads();   // buffer b is refilled at the top of the next iteration
   }
   cp_async_wait<0>();
   if (FUSED && f.record && blockIdx.x == 0 && tid == 0) fused_record(s, f);
+  if (cfl && (FUSED || s.nMembers == 0)) block_min_publish_f(cand, FUSED ? s.cflMinF + (1 - f.parity) : s.cflMinF);
+}
+
+// ---------------------------------------------------------------------------
+// Face-once fused stage (meshes of degree <= 4)
+// ---------------------------------------------------------------------------
+// The gather kernels evaluate every interior face twice, once from each side,
+// as the reference's per-cell loop does (semi_discretize_swe_2D.jl:286-419),
+// and the face arithmetic is most of their instructions.  Here one block takes
+// one 256-cell tile in three phases:
+//  1. side records: each own cell and each halo cell (the tile's out-of-tile
+//     neighbours, DevMesh::halo) is clamped once and its side record formed in
+//     shared memory (xi and hstill pairs, clamped depth, masked momenta,
+//     velocity, sqrt(h), pre-balanced pressure, zb, n);
+//  2. faces: one thread per entry of the tile's face list (DevMesh::FL): a
+//     wet-wet face is evaluated once and gives both cells' terms
+//     (roe_face_wet_f32); a face with a dry side is evaluated from each of its
+//     in-tile sides, as the per-cell loop does; a boundary face from its cell;
+//     the terms times the face length go to shared memory;
+//  3. cells: each cell adds its slots' terms in slot order (deterministic, no
+//     atomics) and finishes the stage as the gather kernels do (stage_finish).
+// A face between two tiles is listed in both, oriented from its lower cell id,
+// so both tiles form the same flux bits and the continuity terms of every
+// wet-wet face cancel exactly.
+constexpr int kFaceRec = kBlock + kHaloMax;   // side records per tile: own cells, then halo cells
+
+__device__ __forceinline__ void face_side_record(const DevMesh& m, float4* R0, float4* R1, float4* R2, float4* R3, int i,
+                                                 float4 x, float4 p) {
+  const SideF32 d = make_side_f32(x, p, m.hsmf, m.hsmLo);
+  const OwnF32 o = own_f32(d.s, m.gf);
+  R0[i] = make_float4(x.x, x.y, p.x, p.y);
+  R1[i] = make_float4(d.s.h, d.s.hu, d.s.hv, d.s.dry ? 1.0f : 0.0f);
+  R2[i] = make_float4(o.u, o.v, o.s, o.p);
+  R3[i] = make_float4(p.z, d.excess, p.w, 0.0f);
+}
+
+__device__ __forceinline__ Side<float> face_side(float4 r0, float4 r1, float zb) {
+  Side<float> s;
+  s.xi = r0.x;
+  s.hst = r0.z;
+  s.h = r1.x;
+  s.hu = r1.y;
+  s.hv = r1.z;
+  s.zb = zb;
+  s.dry = r1.w != 0.0f;
+  return s;
+}
+
+// Terms of face entry i (record rec) into C[2 i] (side a) and C[2 i + 1] (side b).
+template <int RS>
+__device__ __forceinline__ void face_terms(const DevMesh& m, const float4* R0, const float4* R1, const float4* R2,
+                                           const float4* R3, float4* C, int i, float4 rec,
+                                           const double* __restrict__ totalA, int32_t* flags) {
+  const int32_t w = __float_as_int(rec.w);
+  const float nx = rec.x, ny = rec.y, len = rec.z;
+  const int rs = RS >= 0 ? RS : m.riemann;
+  float F[3];
+  const int a = w & 1023;
+  const float4 a0 = R0[a], a1 = R1[a];
+  if (w >= 0) {
+    const int b = (w >> 10) & 1023;
+    const bool aOwn = (w >> 20) & 1, bOwn = (w >> 21) & 1;
+    const float4 b0 = R0[b], b1 = R1[b];
+    const float dxi = (b0.x - a0.x) + (b0.y - a0.y);    // xi_b - xi_a from the pairs
+    const float dhst = (b0.z - a0.z) + (b0.w - a0.w);   // hstill_b - hstill_a
+    if (a1.w == 0.0f && b1.w == 0.0f) {                 // wet-wet: once for both cells
+      const float4 a2 = R2[a], b2 = R2[b];
+      const FaceSideF32 A{a0.x, a0.z, a1.x, a1.y, a1.z, a2.x, a2.y, a2.z};
+      const FaceSideF32 B{b0.x, b0.z, b1.x, b1.y, b1.z, b2.x, b2.y, b2.z};
+      const float dp = rs == kRiemannHll ? hll_face_wet_f32(A, B, dxi, dhst, m.gf, nx, ny, F)
+                                         : roe_face_wet_f32(A, B, dxi, dhst, m.gf, nx, ny, F);
+      const float c0 = F[0] * len, c1 = F[1] * len, c2 = F[2] * len;
+      if (aOwn) C[2 * i] = make_float4(c0, c1, c2, 0.0f);
+      if (bOwn) C[2 * i + 1] = make_float4(-c0, dp * nx * len - c1, dp * ny * len - c2, 0.0f);
+    } else {                                            // a dry side: each in-tile side from its own cell
+      const Side<float> sa = face_side(a0, a1, R3[a].x), sb = face_side(b0, b1, R3[b].x);
+      if (aOwn) {
+        const float pa = R2[a].w;
+        riemann_flux<float>(rs, sa, sb, dxi, m.gf, nx, ny, m.hsmf, F);
+        C[2 * i] = make_float4(F[0] * len, (F[1] - pa * nx) * len, (F[2] - pa * ny) * len, 0.0f);
+      }
+      if (bOwn) {
+        const float pb = R2[b].w;
+        riemann_flux<float>(rs, sb, sa, -dxi, m.gf, -nx, -ny, m.hsmf, F);
+        C[2 * i + 1] = make_float4(F[0] * len, (F[1] + pb * nx) * len, (F[2] + pb * ny) * len, 0.0f);
+      }
+    }
+    return;
+  }
+  // boundary face of own cell a: its ghost state (bc_2D.jl:640-834)
+  const int32_t bf = (w >> 10) & 0x1FFFFF;
+  const float4 a2 = R2[a], a3 = R3[a];
+  const Side<float> L = face_side(a0, a1, a3.x);
+  const int32_t info = m.bfInfo[bf], type = info & 3, grp = info >> 2;
+  if (type == kBcInletQ && !(totalA[grp] > 1e-10)) atomicOr(flags, 2);   // bc_2D.jl:679
+  const Side<float> R = ghost_state<float>(L, type, nx, ny, m.hsmf, type == kBcExitH ? (float)m.exitWse[grp] : 0.0f,
+                                           type == kBcInletQ ? (float)m.inletQ[grp] : 0.0f,
+                                           type == kBcInletQ ? (float)totalA[grp] : 1.0f, m.bfLp23f[bf], a3.z);
+  float dxi = (R.h - L.h) + a3.y;
+  if (type == kBcExitH && !R.dry) dxi = m.bfExitRel[bf] - (a0.x + a0.y);
+  if (!L.dry && !R.dry) {
+    OwnF32 o;
+    o.u = a2.x; o.v = a2.y; o.s = a2.z; o.p = a2.w;
+    o.fxx = L.hu * o.u; o.fxy = L.hu * o.v; o.fyx = L.hv * o.u; o.fyy = L.hv * o.v;
+    if (rs == kRiemannHll) hll_flux_wet_f32(L, o, R, dxi, 0.0f, m.gf, nx, ny, F);
+    else roe_flux_wet_f32(L, o, R, dxi, 0.0f, m.gf, nx, ny, F);
+  } else {
+    riemann_flux<float>(rs, L, R, dxi, m.gf, nx, ny, m.hsmf, F);
+    F[1] -= a2.w * nx;
+    F[2] -= a2.w * ny;
+  }
+  C[2 * i] = make_float4(F[0] * len, F[1] * len, F[2] * len, 0.0f);
+}
+
+template <int NS, int MODE, bool FUSED, int RS>
+__global__ void __launch_bounds__(kBlock, 4)
+    k_stage_face_f32(DevMesh m, DevScalars s, StateF32 Xin, StateF32 Xbase, StateF32 Xout, int cfl, StageFuse f) {
+  pdl_enter();
+  extern __shared__ float4 fsm[];
+  float4* R0 = fsm;              // {xi_hi, xi_lo, hstill_hi, hstill_lo}
+  float4* R1 = R0 + kFaceRec;    // {h, hu, hv (clamped, masked), dry ? 1 : 0}
+  float4* R2 = R1 + kFaceRec;    // {u, v, sqrt h, p}
+  float4* R3 = R2 + kFaceRec;    // {zb, excess, n, 0}
+  float4* C = R3 + kFaceRec;     // [2 faceMax] terms F L of side a, side b
+  __shared__ float dtShared;
+  const int tile = blockIdx.x, tid = threadIdx.x;
+  const int base = tile * kBlock, c = base + tid;
+  const bool active = c < m.n;
+  const double* totalIn = FUSED ? f.totalIn : m.totalA;
+  // phase 1: side records of the own cells and the halo
+  float4 xin, cp, cs;
+  uint2 refs;
+  if (active) {
+    xin = __ldg(&Xin.x[c]);
+    cp = __ldg(&m.CP[c]);
+    cs = __ldg(&m.CS[c]);
+    refs = __ldg(&m.FR[c]);
+    face_side_record(m, R0, R1, R2, R3, tid, xin, cp);
+  }
+  if (tid < kHaloMax) {
+    const int hid = __ldg(&m.halo[(size_t)tile * kHaloMax + tid]);
+    if (hid >= 0) face_side_record(m, R0, R1, R2, R3, kBlock + tid, __ldg(&Xin.x[hid]), __ldg(&m.CP[hid]));
+  }
+  if (tid == 0) dtShared = FUSED ? (float)fused_dt(s, f) : *s.dtf;
+  __syncthreads();
+  // phase 2: the tile's faces
+  const int f0 = __ldg(&m.FLoff[tile]), nf = __ldg(&m.FLoff[tile + 1]) - f0;
+  for (int i = tid; i < nf; i += kBlock) face_terms<RS>(m, R0, R1, R2, R3, C, i, __ldg(&m.FL[f0 + i]), totalIn, s.flags);
+  __syncthreads();
+  // phase 3: each cell's terms in slot order, then the stage update
+  float cand = INFINITY, hOut = 0.0f;
+  bool wetOut = false;
+  if (active) {
+    float4 sl[NS];
+    float g0 = 0.0f, g1 = 0.0f, g2 = 0.0f;
+#pragma unroll
+    for (int k = 0; k < NS; ++k) {
+      const unsigned int ref = ((k < 2 ? refs.x : refs.y) >> (16 * (k & 1))) & 0xFFFFu;
+      sl[k] = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(kNoFace));
+      if (ref == 0xFFFFu) continue;
+      const float4 t = C[ref];
+      g0 += t.x;
+      g1 += t.y;
+      g2 += t.z;
+      if (cfl) {   // the slot's geometry for the CFL candidate (|u.n| does not depend on the side)
+        const float4 g = __ldg(&m.FL[f0 + (ref >> 1)]);
+        sl[k] = make_float4(g.x, g.y, g.z, 0.0f);
+      }
+    }
+    const float4 r0 = R0[tid], r1 = R1[tid], r3 = R3[tid];
+    SideF32 L;
+    L.s = face_side(r0, r1, r3.x);
+    L.xlo = r0.y;
+    L.excess = r3.y;
+    const float dt = MODE == kModeRhs ? 0.0f : dtShared;
+    stage_finish<NS, MODE>(m, s, L, g0, g1, g2, c, sl, xin, cp, cs, Xin.q, Xbase.x, Xbase.q, c, dt, Xout, nullptr,
+                           cfl, cand, hOut, wetOut);
+  }
+  if (FUSED && f.record && blockIdx.x == 0 && tid == 0) fused_record(s, f);
   if (cfl) block_min_publish_f(cand, FUSED ? s.cflMinF + (1 - f.parity) : s.cflMinF);
+  if (FUSED && m.nInlet > 0) fused_inlet_totals<NS>(m, f, tile, c, hOut, wetOut);
 }
 
 template <int NS>
@@ -587,7 +775,8 @@ __global__ void __launch_bounds__(kBlock) k_cfl_f32(DevMesh m, DevScalars s, Sta
     const SideF32 L = make_side_f32(x, m.CP[c], m.hsmf, m.hsmLo);
     cand = cfl_candidate_f32<NS>(m, sl, L.s.h, x.z, x.w, L.s.dry, m.CS[c].z);
   }
-  block_min_publish_f(cand, s.cflMinF);
+  if (s.nMembers > 0) member_min_publish_f(s, cand, c < m.n ? member_of(s, c) : -1);
+  else block_min_publish_f(cand, s.cflMinF);
 }
 
 __global__ void __launch_bounds__(kBlock) k_inlet_total_f32(DevMesh m, DevScalars s, StateF32 X) {
@@ -611,6 +800,31 @@ __global__ void __launch_bounds__(kBlock) k_inlet_total_f32(DevMesh m, DevScalar
 // Bookkeeping and renumbering
 // ---------------------------------------------------------------------------
 __global__ void k_step_begin(DevScalars s, int cflMode, double cfl) {
+  if (s.nMembers > 0) {   // an ensemble: each member's own step (one block)
+    const int k = *s.stepIdx;
+    for (int mm = threadIdx.x; mm < s.nMembers; mm += blockDim.x) {
+      double dt = *s.dt;
+      if (cflMode) {
+        dt = cfl * fmin(__longlong_as_double((long long)s.cflMinM[mm]), (double)__uint_as_float(s.cflMinMF[mm]));
+        if (!(dt >= s.dtMin)) atomicOr(s.flags, 8);   // the member's step collapsed (or is NaN)
+        s.cflMinM[mm] = (unsigned long long)__double_as_longlong(INFINITY);
+        s.cflMinMF[mm] = __float_as_uint(INFINITY);
+      }
+      s.dtM[mm] = dt;
+      s.dtMf[mm] = (float)dt;
+      if (k < s.dtCap) s.dtHistM[(size_t)k * s.nMembers + mm] = dt;
+      s.tM[mm] += dt;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {   // the context's own record: member 0's step
+      if (cflMode) *s.dt = s.dtM[0];
+      *s.dtf = (float)*s.dt;
+      if (k < s.dtCap) s.dtHist[k] = *s.dt;
+      *s.stepIdx = k + 1;
+      *s.tSum += *s.dt;
+    }
+    return;
+  }
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   if (cflMode) {
     const double m = fmin(__longlong_as_double((long long)*s.cflMin), (double)__uint_as_float(*s.cflMinF));
@@ -633,6 +847,11 @@ __global__ void k_reset_cfl(DevScalars s, int p) {
 }
 
 __global__ void k_reset_scalars(DevScalars s) {
+  for (int mm = threadIdx.x; mm < s.nMembers; mm += blockDim.x) {
+    s.cflMinM[mm] = (unsigned long long)__double_as_longlong(INFINITY);
+    s.cflMinMF[mm] = __float_as_uint(INFINITY);
+    s.tM[mm] = 0.0;
+  }
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   s.cflMin[0] = s.cflMin[1] = (unsigned long long)__double_as_longlong(INFINITY);
   s.cflMinF[0] = s.cflMinF[1] = __float_as_uint(INFINITY);
@@ -758,6 +977,7 @@ int forced_stage_kernel() {
     if (std::strcmp(e, "gather") == 0) return (int)kStageGather;
     if (std::strcmp(e, "pipe") == 0) return (int)kStagePipe;
     if (std::strcmp(e, "tma") == 0) return (int)kStageTma;
+    if (std::strcmp(e, "face") == 0) return (int)kStageFace;
     return -1;
   }();
   return k;
@@ -822,6 +1042,36 @@ void launch_pipe(const DevMesh& m, const DevScalars& s, StateF32 Xin, StateF32 X
   else launch_pipe_rs<NS, MODE, FUSED, kRiemannRoe>(m, s, Xin, Xbase, Xout, cfl, fu, st);
 }
 
+// Dynamic shared memory of the face kernel on this mesh: the side records and
+// two terms per face of the largest tile.
+uint32_t face_smem(const DevMesh& m) { return (uint32_t)(4 * kFaceRec + 2 * m.faceMax) * (uint32_t)sizeof(float4); }
+constexpr uint32_t kFaceSmemMax = (4 * kFaceRec + 2 * kFaceMaxPerTile) * sizeof(float4);
+
+template <int NS, int MODE, bool FUSED, int RS>
+void launch_face_rs(const DevMesh& m, const DevScalars& s, StateF32 Xin, StateF32 Xbase, StateF32 Xout, int cfl,
+                    const StageFuse& fu, cudaStream_t st) {
+  static const bool attr = [] {   // more than 48 KB of dynamic shared memory: opt in once
+    cudaFuncSetAttribute(k_stage_face_f32<NS, MODE, FUSED, RS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)kFaceSmemMax);
+    return true;
+  }();
+  (void)attr;
+  launch_k(true, k_stage_face_f32<NS, MODE, FUSED, RS>, blocks_for(m.n), kBlock, face_smem(m), st, m, s, Xin, Xbase,
+           Xout, cfl, fu);
+}
+template <int NS, int MODE, bool FUSED>
+void launch_face(const DevMesh& m, const DevScalars& s, StateF32 Xin, StateF32 Xbase, StateF32 Xout, int cfl,
+                 const StageFuse& fu, cudaStream_t st) {
+  if (m.riemann == kRiemannHll) launch_face_rs<NS, MODE, FUSED, kRiemannHll>(m, s, Xin, Xbase, Xout, cfl, fu, st);
+  else launch_face_rs<NS, MODE, FUSED, kRiemannRoe>(m, s, Xin, Xbase, Xout, cfl, fu, st);
+}
+template <int NS, bool FUSED = true>
+void launch_face_mode(const DevMesh& m, const DevScalars& s, int mode, StateF32 Xin, StateF32 Xbase, StateF32 Xout,
+                      int cfl, const StageFuse& fu, cudaStream_t st) {
+  if (mode == kModeStage1) launch_face<NS, kModeStage1, FUSED>(m, s, Xin, Xbase, Xout, cfl, fu, st);
+  else launch_face<NS, kModeStage2, FUSED>(m, s, Xin, Xbase, Xout, cfl, fu, st);
+}
+
 template <int NS, bool FUSED = true>
 void launch_pipe_mode(const DevMesh& m, const DevScalars& s, int mode, StateF32 Xin, StateF32 Xbase, StateF32 Xout,
                       int cfl, const StageFuse& fu, cudaStream_t st) {
@@ -844,6 +1094,7 @@ bool stage_kernel_usable(const DevMesh& m, int k, int mode, StateF32 Xin, StateF
   auto a8 = [](const void* p) { return (reinterpret_cast<uintptr_t>(p) & 7u) == 0; };
   if (k == kStageGather) return true;
   if (m.nslot > 4) return false;
+  if (k == kStageFace) return m.FL && m.FLoff && m.FR && m.halo && m.faceMax <= kFaceMaxPerTile;
   if (k == kStagePipe)   // cp.async: 16-byte records 16-byte aligned, the lo parts 8-byte aligned
     return m.SLp && m.halo && a16(m.SLp) && a16(m.CP) && a16(m.CS) && a16(Xin.x) && a8(Xin.q) &&
            (mode != kModeStage2 || (a16(Xbase.x) && a8(Xbase.q)));
@@ -880,6 +1131,11 @@ void launch_stage_f32_fused(const DevMesh& m, const DevScalars& s, int mode, Sta
   const int f = (!fu.record && fu.cflMode) ? 1 : 0;   // stage 2 publishes the next CFL minimum
   const int forced = forced_stage_kernel();
   const int k = forced >= 0 ? forced : m.stageKernel;
+  if (k == kStageFace && stage_kernel_usable(m, k, mode, Xin, Xbase)) {
+    if (m.nslot <= 3) launch_face_mode<3>(m, s, mode, Xin, Xbase, Xout, f, fu, st);
+    else launch_face_mode<4>(m, s, mode, Xin, Xbase, Xout, f, fu, st);
+    return;
+  }
   if (k == kStagePipe && stage_kernel_usable(m, k, mode, Xin, Xbase)) {
     if (m.nslot <= 3) launch_pipe_mode<3>(m, s, mode, Xin, Xbase, Xout, f, fu, st);
     else launch_pipe_mode<4>(m, s, mode, Xin, Xbase, Xout, f, fu, st);
@@ -902,7 +1158,7 @@ void launch_cfl_f32(const DevMesh& m, const DevScalars& s, StateF32 X, cudaStrea
   else k_cfl_f32<8><<<blocks_for(m.n), kBlock, 0, st>>>(m, s, X);
 }
 void launch_step_begin(const DevScalars& s, bool cflMode, double cfl, cudaStream_t st) {
-  k_step_begin<<<1, 32, 0, st>>>(s, cflMode ? 1 : 0, cfl);
+  k_step_begin<<<1, s.nMembers > 0 ? 256 : 32, 0, st>>>(s, cflMode ? 1 : 0, cfl);
 }
 void launch_reset_scalars(const DevScalars& s, cudaStream_t st) { k_reset_scalars<<<1, 32, 0, st>>>(s); }
 void launch_gather_state_f64(int32_t n, const int32_t* perm, const double* user, double* dev, cudaStream_t st) {

@@ -13,6 +13,7 @@
 #include <cmath>
 
 #include "hg_device.cuh"
+#include "hg_members.cuh"
 #include "hg_reduce.cuh"
 #include "hg_state.hpp"
 
@@ -148,6 +149,7 @@ __global__ void __launch_bounds__(kBlock) k_stage_f64(DevMesh m, DevScalars s, i
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   const bool active = c < m.n;
   double cand = INFINITY;
+  const int mem = (s.nMembers > 0 && active) ? member_of(s, c) : -1;   // an ensemble member's own step
   if (active) {
     const Side<double> L = load_f64(m, Qin, c);
     double f0, f1, f2;
@@ -173,7 +175,7 @@ __global__ void __launch_bounds__(kBlock) k_stage_f64(DevMesh m, DevScalars s, i
     if (mode == kModeRhs) {
       Qout[c] = d0; Qout[m.n + c] = d1; Qout[2 * m.n + c] = d2;
     } else {
-      const double dt = *s.dt;
+      const double dt = mem >= 0 ? s.dtM[mem] : *s.dt;
       double x0, x1, x2;
       if (mode == kModeStage2) {
         x0 = 0.5 * (Qbase[c] + (Qin[c] + dt * d0));
@@ -196,14 +198,16 @@ __global__ void __launch_bounds__(kBlock) k_stage_f64(DevMesh m, DevScalars s, i
       if (cfl) cand = cfl_candidate_f64(m, c, x0, x1, x2);
     }
   }
-  if (cfl) block_min_publish(cand, s.cflMin);
+  if (cfl && s.nMembers > 0) member_min_publish(s, cand, mem);
+  else if (cfl) block_min_publish(cand, s.cflMin);
 }
 
 __global__ void __launch_bounds__(kBlock) k_cfl_f64(DevMesh m, DevScalars s, const double* __restrict__ Q) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   double cand = INFINITY;
   if (c < m.n) cand = cfl_candidate_f64(m, c, Q[c], Q[m.n + c], Q[2 * m.n + c]);
-  block_min_publish(cand, s.cflMin);
+  if (s.nMembers > 0) member_min_publish(s, cand, c < m.n ? member_of(s, c) : -1);
+  else block_min_publish(cand, s.cflMin);
 }
 
 // total_A = sum_faces L^(5/3) h / n * wet over one inlet-Q boundary (bc_2D.jl:673-679).
@@ -232,8 +236,14 @@ __global__ void k_hydrograph(DevMesh m, DevScalars s, int when, double t) {
   if (g >= m.nInlet) return;
   const int a = m.hydroOff[g], b = m.hydroOff[g + 1];
   if (b <= a) return;   // constant discharge
-  if (when == kHydroStepStart) t = *s.tSum - *s.dt;
-  else if (when == kHydroStepEnd || when == kHydroNow) t = *s.tSum;
+  if (s.nMembers > 0 && s.inletMember && when != kHydroAt) {   // an ensemble: the group's member's own time
+    const int mm = s.inletMember[g];
+    t = when == kHydroStepStart ? s.tM[mm] - s.dtM[mm] : s.tM[mm];
+  } else if (when == kHydroStepStart) {
+    t = *s.tSum - *s.dt;
+  } else if (when == kHydroStepEnd || when == kHydroNow) {
+    t = *s.tSum;
+  }
   double q;
   if (t <= m.hydroT[a]) {
     q = m.hydroQ[a];

@@ -65,8 +65,17 @@ struct DevMesh {
   // a larger halo.
   const float4* SLp = nullptr;
   const int32_t* halo = nullptr;
-  // Kernel of the fused FP32 stages (hg_autotune): kStageGather, kStagePipe or
-  // kStageTma.  All three compute the same results.
+  // Face-once FP32 stage (k_stage_face_f32; meshes of degree <= 4 whose
+  // tiles' halos fit): per tile of kStageBlockF32 cells its faces, each listed
+  // once (FL[FLoff[t] .. FLoff[t + 1]): {nx, ny, L of side a, packed ids},
+  // interior faces first, then boundary faces), and per cell the face entries
+  // of its edge slots (FR: four 16-bit refs, face << 1 | side, 0xFFFF none).
+  const float4* FL = nullptr;
+  const int32_t* FLoff = nullptr;
+  const uint2* FR = nullptr;
+  int32_t faceMax = 0;               // most faces in one tile
+  // Kernel of the fused FP32 stages (hg_autotune): kStageGather, kStagePipe,
+  // kStageTma (the same results) or kStageFace (each wet-wet face once).
   int32_t stageKernel = 0;
   const int32_t* bfInfo = nullptr;   // [nbf] type | group << 2
   const double* bfLp23 = nullptr;    // [nbf] L^(2/3) (inlet-Q faces)
@@ -126,6 +135,20 @@ struct DevScalars {
                                           // bit 3: a CFL step below dtMin
   int32_t dtCap = 0;
   double dtMin = 0.0;                     // smallest CFL step accepted (swe_2D_consts.dt_min)
+  // Ensembles (nMembers > 0): every member takes its own step, as if it ran
+  // alone.  Member m owns device cells [memberOff[m], memberOff[m + 1]); the
+  // step bookkeeping forms each member's dt from its own CFL minimum (or the
+  // fixed dt) into dtM / dtMf, the stage kernels read their cell's member's
+  // step, and publish CFL candidates into the member's minimum.
+  int32_t nMembers = 0;
+  const int32_t* memberOff = nullptr;     // [nMembers + 1], device order
+  const int32_t* inletMember = nullptr;   // [nInlet] member of each inlet-Q group (hydrograph times)
+  double* dtM = nullptr;                  // [nMembers] current step
+  float* dtMf = nullptr;
+  double* tM = nullptr;                   // [nMembers] elapsed time
+  unsigned long long* cflMinM = nullptr;  // [nMembers] CFL minimum, as ordered bits (FP64 path)
+  unsigned int* cflMinMF = nullptr;       // [nMembers] the same (FP32 path)
+  double* dtHistM = nullptr;              // [dtCap][nMembers] steps taken
 };
 
 enum StageMode : int32_t { kModeRhs = 0, kModeStage1 = 1, kModeStage2 = 2, kModeEulerRef = 3 };
@@ -186,7 +209,13 @@ void launch_stage_f32_fused(const DevMesh& m, const DevScalars& s, int mode, Sta
 #endif
 constexpr int kStageBlockF32 = HG_STAGE_BLOCK;
 constexpr int kHaloMax = 128;   // out-of-tile neighbour cells a pipelined stage tile can hold
-enum StageKernel : int32_t { kStageGather = 0, kStagePipe = 1, kStageTma = 2 };
+enum StageKernel : int32_t { kStageGather = 0, kStagePipe = 1, kStageTma = 2, kStageFace = 3 };
+// Packed ids of a face-once face record (FL .w as int bits): interior faces
+// a | b << 10 | a-in-tile << 20 | b-in-tile << 21 (tile-local indices: own
+// cells [0, kStageBlockF32), halo cells kStageBlockF32 + j); boundary faces
+// a | bf << 10 | 1 << 31 (bf < 2^21).
+constexpr int32_t kFaceBoundary = INT32_MIN;
+constexpr int kFaceMaxPerTile = 1024;
 int stage_blocks_f32(const DevMesh& m);
 // The kernel HG_STAGE_KERNEL forces (gather / pipe / tma), else -1.
 int stage_kernel_forced();

@@ -68,6 +68,7 @@ SIGNATURES = {
     "hg_ensemble_create": [ctypes.POINTER(HgEnsembleDesc), ctypes.POINTER(HgConsts), ctypes.c_int32, ctypes.c_int32,
                            ctypes.POINTER(_vp)],
     "hg_ensemble_layout": [_vp, _ip, _ip, _ip, _ip],
+    "hg_ensemble_steps": [_vp, ctypes.c_int32, _dp, _dp],
     "hg_destroy": [_vp],
     "hg_sizes": [_vp, _ip],
     "hg_set_still_water": [_vp, _dp],

@@ -418,6 +418,14 @@ class SWE2DEnsemble(SWE2D):
         check(lib().hg_ensemble_layout(self.h, ctypes.byref(nm), _i(self.cell_offset), _i(self.inlet_offset),
                                        _i(self.exit_offset)), self.h)
 
+    def steps(self, nsteps):
+        """(dts [nsteps, n_members], elapsed time [n_members]): every member's
+        own steps since the last upload (hg_ensemble_steps)."""
+        dts = np.zeros((nsteps, self.n_members))
+        t = np.zeros(self.n_members)
+        self._chk(lib().hg_ensemble_steps(self.h, int(nsteps), _d(dts), _d(t)))
+        return dts, t
+
     def concat(self, per_member, kind="cell"):
         """Concatenate per-member arrays (kind: cell, inlet, exit, state)."""
         if kind == "state":   # Q = [xi; qx; qy] per member -> the concatenated state's three blocks

@@ -132,9 +132,15 @@ int hg_create(const hg_mesh_desc* desc, const hg_consts* consts, int32_t precisi
  * [inlet_offset[m], inlet_offset[m+1]) / [exit_offset[m], ...) of the values
  * of hg_set_inlet_q / hg_set_exit_wse and of the inlet-Q gradient.  Every
  * other call (hg_set_*, hg_rhs, hg_integrate, hg_advance, hg_loss_and_grad)
- * applies unchanged to the concatenation.  All members take the same step: a
- * fixed dt, or the smallest of the members' CFL steps; the loss of
- * hg_loss_and_grad is the mean over all members' probes. */
+ * applies unchanged to the concatenation.  In CFL stepping each member takes
+ * its own step, formed from its own cells (each member is its own problem, as
+ * the reference solves one ODEProblem per run,
+ * swe_2D_forward_simulation.jl:24-39), and keeps its own time, so a member's
+ * trajectory is the one it has alone; a fixed dt applies to every member.
+ * hg_integrate's dts_out and hg_elapsed_time report member 0's steps and
+ * time; hg_ensemble_steps gives every member's.  The adjoint
+ * (hg_loss_and_grad) takes one fixed dt; its loss is the mean over all
+ * members' probes. */
 typedef struct hg_ensemble_desc {
   int32_t n_meshes;
   const hg_mesh_desc* meshes;   /* [n_meshes] */
@@ -147,6 +153,10 @@ int hg_ensemble_create(const hg_ensemble_desc* ensemble, const hg_consts* consts
  * by hg_create is one member). */
 int hg_ensemble_layout(const hg_ctx* ctx, int32_t* n_members, int32_t* cell_offset, int32_t* inlet_offset,
                        int32_t* exit_offset);
+/* The steps each member took in the steps since the last state upload
+ * (dts [nsteps][n_members], may be NULL) and each member's elapsed time
+ * (t_elapsed [n_members], may be NULL), of an ensemble context. */
+int hg_ensemble_steps(hg_ctx* ctx, int32_t nsteps, double* dts, double* t_elapsed);
 
 /* ---- Tsit5 (the reference's default solver, swe_2D_forward_simulation.jl:37-39)
  * Adaptive Tsitouras 5(4) steps of the RHS from t0 to t1 on the device, Q in/out

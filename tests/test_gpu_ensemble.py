@@ -1,5 +1,6 @@
 """Ensembles (hg_ensemble_create): members stepped together give each member's
-own single-context result.
+own single-context result, and in CFL stepping every member takes its own
+step.
 
 In FP64 every member's state after K fixed-dt steps is bit-identical to a
 context of its own (gather-form sums in the mesh's slot order, inlet totals in
@@ -94,11 +95,34 @@ def test_members_match_their_own_contexts(precision):
             assert np.abs(q - qs).max() <= 1e-6 * np.abs(qs).max()
 
 
-def test_cfl_step_is_the_smallest_members_step():
-    meshes, params, e = _setup("fp64")
-    own = [_single(meshes[m], p, "fp64").integrate(p["Q0"], 1, cfl=0.4)[1][0] for (m, _, _), p in zip(MEMBERS, params)]
-    _, dts = e.integrate(e.concat([p["Q0"] for p in params], "state"), 1, cfl=0.4)
-    assert dts[0] == min(own)
+@pytest.mark.parametrize("precision", ["fp64", "fp32c"])
+def test_each_member_takes_its_own_cfl_steps(precision):
+    """CFL stepping: every member forms its step from its own cells and keeps
+    its own time (hg_ensemble_steps), so its trajectory is the one it has
+    alone (swe_2D_forward_simulation.jl:24-39 solves one problem per run).
+    FP64: bit for bit, steps and states, with a hydrograph on one member
+    (evaluated at that member's own stage times).  FP32C: the ensemble's
+    unfused stages against the single context's fused ones, within 1e-5."""
+    meshes, params, e = _setup(precision)
+    hydro = (np.array([0.0, 2.0, 5.0]), np.array([100.0, 180.0, 60.0]))
+    e.set_inlet_hydrograph(int(e.inlet_offset[2]), *hydro)      # member 2's inlet (mesh 0)
+    K = 30
+    qe, dts_e = e.integrate(e.concat([p["Q0"] for p in params], "state"), K, cfl=0.4)
+    dts, t = e.steps(K)
+    np.testing.assert_array_equal(dts[:, 0], dts_e)              # the context's own record is member 0's
+    assert len(set(dts[0])) == len(MEMBERS)                      # the members' steps differ
+    for i, (((m, _, _), p), q) in enumerate(zip(zip(MEMBERS, params), e.split(qe, "state"))):
+        c = _single(meshes[m], p, precision)
+        if i == 2:
+            c.set_inlet_hydrograph(0, *hydro)
+        qs, dts_s = c.integrate(p["Q0"], K, cfl=0.4)
+        if precision == "fp64":
+            np.testing.assert_array_equal(dts[:, i], dts_s)
+            np.testing.assert_array_equal(q, qs)
+            assert t[i] == c.elapsed_time()
+        else:
+            assert np.abs(dts[:, i] - dts_s).max() <= 1e-5 * dts_s.max()
+            assert np.abs(q - qs).max() <= 1e-5 * np.abs(qs).max()
 
 
 def test_member_gradients_are_their_own_scaled_by_probe_share():
