@@ -591,15 +591,17 @@ __global__ void __launch_bounds__(kBlock, kPipeCtasPerSm)
 // as the reference's per-cell loop does (semi_discretize_swe_2D.jl:286-419),
 // and the face arithmetic is most of their instructions.  Here one block takes
 // one 256-cell tile in three phases:
-//  1. side records: each own cell and each halo cell (the tile's out-of-tile
-//     neighbours, DevMesh::halo) is clamped once and its side record formed in
-//     shared memory (xi and hstill pairs, clamped depth, masked momenta,
-//     velocity, sqrt(h), pre-balanced pressure, zb, n);
-//  2. faces: one thread per entry of the tile's face list (DevMesh::FL): a
-//     wet-wet face is evaluated once and gives both cells' terms
-//     (roe_face_wet_f32); a face with a dry side is evaluated from each of its
-//     in-tile sides, as the per-cell loop does; a boundary face from its cell;
-//     the terms times the face length go to shared memory;
+//  1. loads and side records: every global load of the tile is issued first --
+//     the own cells' records, the tile's face list (DevMesh::FL) and the inputs
+//     of phase 3 by asynchronous copies into shared memory, the halo (the
+//     tile's out-of-tile neighbours, DevMesh::halo) as soon as its ids arrive;
+//     each own and halo cell is clamped once and its side record formed
+//     (xi and hstill pairs, clamped depth, masked momenta, velocity, sqrt(h));
+//  2. faces: one thread per face-list entry: a wet-wet face is evaluated once
+//     and gives both cells' terms (roe_face_wet_f32); a face with a dry side
+//     is evaluated from each of its in-tile sides, as the per-cell loop does;
+//     a boundary face from its cell; the terms times the face length go to
+//     shared memory;
 //  3. cells: each cell adds its slots' terms in slot order (deterministic, no
 //     atomics) and finishes the stage as the gather kernels do (stage_finish).
 // A face between two tiles is listed in both, oriented from its lower cell id,
@@ -607,17 +609,34 @@ __global__ void __launch_bounds__(kBlock, kPipeCtasPerSm)
 // wet-wet face cancel exactly.
 constexpr int kFaceRec = kBlock + kHaloMax;   // side records per tile: own cells, then halo cells
 
-__device__ __forceinline__ void face_side_record(const DevMesh& m, float4* R0, float4* R1, float4* R2, float4* R3, int i,
-                                                 float4 x, float4 p) {
+// Shared-memory layout of k_stage_face_f32, in 16-byte units: side records
+// R0 {xi_hi, xi_lo, hstill_hi, hstill_lo}, R1 {h, hu, hv, excess}, R2 {u, v,
+// sqrt h, dry ? 1 : 0}, R3 {zb, n} (8 bytes each); two terms per face; the
+// face list; the own cells' CS and lo parts and, in stage 2, the base state.
+struct FaceSmem {
+  static constexpr int kR0 = 0, kR1 = kFaceRec, kR2 = 2 * kFaceRec, kR3 = 3 * kFaceRec;
+  static constexpr int kC = kR3 + kFaceRec / 2;
+  __host__ __device__ static int fl(int faceMax) { return kC + 2 * faceMax; }
+  __host__ __device__ static int cs(int faceMax) { return fl(faceMax) + faceMax; }
+  __host__ __device__ static int q(int faceMax) { return cs(faceMax) + kBlock; }
+  __host__ __device__ static int xb(int faceMax) { return q(faceMax) + kBlock / 2; }
+  __host__ __device__ static int qb(int faceMax) { return xb(faceMax) + kBlock; }
+  __host__ __device__ static uint32_t bytes(int faceMax, int mode) {
+    return (uint32_t)(mode == kModeStage2 ? qb(faceMax) + kBlock / 2 : xb(faceMax)) * 16u;
+  }
+};
+
+__device__ __forceinline__ void face_side_record(const DevMesh& m, float4* R0, float4* R1, float4* R2, float2* R3,
+                                                 int i, float4 x, float4 p) {
   const SideF32 d = make_side_f32(x, p, m.hsmf, m.hsmLo);
   const OwnF32 o = own_f32(d.s, m.gf);
   R0[i] = make_float4(x.x, x.y, p.x, p.y);
-  R1[i] = make_float4(d.s.h, d.s.hu, d.s.hv, d.s.dry ? 1.0f : 0.0f);
-  R2[i] = make_float4(o.u, o.v, o.s, o.p);
-  R3[i] = make_float4(p.z, d.excess, p.w, 0.0f);
+  R1[i] = make_float4(d.s.h, d.s.hu, d.s.hv, d.excess);
+  R2[i] = make_float4(o.u, o.v, o.s, d.s.dry ? 1.0f : 0.0f);
+  R3[i] = make_float2(p.z, p.w);
 }
 
-__device__ __forceinline__ Side<float> face_side(float4 r0, float4 r1, float zb) {
+__device__ __forceinline__ Side<float> face_side(float4 r0, float4 r1, float4 r2, float zb) {
   Side<float> s;
   s.xi = r0.x;
   s.hst = r0.z;
@@ -625,29 +644,33 @@ __device__ __forceinline__ Side<float> face_side(float4 r0, float4 r1, float zb)
   s.hu = r1.y;
   s.hv = r1.z;
   s.zb = zb;
-  s.dry = r1.w != 0.0f;
+  s.dry = r2.w != 0.0f;
   return s;
+}
+
+// Pre-balanced pressure g/2 (smooth_pow2(xi) + 2 xi hstill) of a side (own_f32's p).
+__device__ __forceinline__ float face_pressure(const DevMesh& m, float xi, float hst) {
+  return 0.5f * m.gf * (smooth_pow2(xi) + 2.0f * xi * hst);
 }
 
 // Terms of face entry i (record rec) into C[2 i] (side a) and C[2 i + 1] (side b).
 template <int RS>
 __device__ __forceinline__ void face_terms(const DevMesh& m, const float4* R0, const float4* R1, const float4* R2,
-                                           const float4* R3, float4* C, int i, float4 rec,
+                                           const float2* R3, float4* C, int i, float4 rec,
                                            const double* __restrict__ totalA, int32_t* flags) {
   const int32_t w = __float_as_int(rec.w);
   const float nx = rec.x, ny = rec.y, len = rec.z;
   const int rs = RS >= 0 ? RS : m.riemann;
   float F[3];
   const int a = w & 1023;
-  const float4 a0 = R0[a], a1 = R1[a];
+  const float4 a0 = R0[a], a1 = R1[a], a2 = R2[a];
   if (w >= 0) {
     const int b = (w >> 10) & 1023;
     const bool aOwn = (w >> 20) & 1, bOwn = (w >> 21) & 1;
-    const float4 b0 = R0[b], b1 = R1[b];
+    const float4 b0 = R0[b], b1 = R1[b], b2 = R2[b];
     const float dxi = (b0.x - a0.x) + (b0.y - a0.y);    // xi_b - xi_a from the pairs
     const float dhst = (b0.z - a0.z) + (b0.w - a0.w);   // hstill_b - hstill_a
-    if (a1.w == 0.0f && b1.w == 0.0f) {                 // wet-wet: once for both cells
-      const float4 a2 = R2[a], b2 = R2[b];
+    if (a2.w == 0.0f && b2.w == 0.0f) {                 // wet-wet: once for both cells
       const FaceSideF32 A{a0.x, a0.z, a1.x, a1.y, a1.z, a2.x, a2.y, a2.z};
       const FaceSideF32 B{b0.x, b0.z, b1.x, b1.y, b1.z, b2.x, b2.y, b2.z};
       const float dp = rs == kRiemannHll ? hll_face_wet_f32(A, B, dxi, dhst, m.gf, nx, ny, F)
@@ -656,14 +679,14 @@ __device__ __forceinline__ void face_terms(const DevMesh& m, const float4* R0, c
       if (aOwn) C[2 * i] = make_float4(c0, c1, c2, 0.0f);
       if (bOwn) C[2 * i + 1] = make_float4(-c0, dp * nx * len - c1, dp * ny * len - c2, 0.0f);
     } else {                                            // a dry side: each in-tile side from its own cell
-      const Side<float> sa = face_side(a0, a1, R3[a].x), sb = face_side(b0, b1, R3[b].x);
+      const Side<float> sa = face_side(a0, a1, a2, R3[a].x), sb = face_side(b0, b1, b2, R3[b].x);
       if (aOwn) {
-        const float pa = R2[a].w;
+        const float pa = face_pressure(m, a0.x, a0.z);
         riemann_flux<float>(rs, sa, sb, dxi, m.gf, nx, ny, m.hsmf, F);
         C[2 * i] = make_float4(F[0] * len, (F[1] - pa * nx) * len, (F[2] - pa * ny) * len, 0.0f);
       }
       if (bOwn) {
-        const float pb = R2[b].w;
+        const float pb = face_pressure(m, b0.x, b0.z);
         riemann_flux<float>(rs, sb, sa, -dxi, m.gf, -nx, -ny, m.hsmf, F);
         C[2 * i + 1] = make_float4(F[0] * len, (F[1] + pb * nx) * len, (F[2] + pb * ny) * len, 0.0f);
       }
@@ -672,25 +695,26 @@ __device__ __forceinline__ void face_terms(const DevMesh& m, const float4* R0, c
   }
   // boundary face of own cell a: its ghost state (bc_2D.jl:640-834)
   const int32_t bf = (w >> 10) & 0x1FFFFF;
-  const float4 a2 = R2[a], a3 = R3[a];
-  const Side<float> L = face_side(a0, a1, a3.x);
+  const float2 a3 = R3[a];
+  const Side<float> L = face_side(a0, a1, a2, a3.x);
   const int32_t info = m.bfInfo[bf], type = info & 3, grp = info >> 2;
   if (type == kBcInletQ && !(totalA[grp] > 1e-10)) atomicOr(flags, 2);   // bc_2D.jl:679
   const Side<float> R = ghost_state<float>(L, type, nx, ny, m.hsmf, type == kBcExitH ? (float)m.exitWse[grp] : 0.0f,
                                            type == kBcInletQ ? (float)m.inletQ[grp] : 0.0f,
-                                           type == kBcInletQ ? (float)totalA[grp] : 1.0f, m.bfLp23f[bf], a3.z);
-  float dxi = (R.h - L.h) + a3.y;
+                                           type == kBcInletQ ? (float)totalA[grp] : 1.0f, m.bfLp23f[bf], a3.y);
+  float dxi = (R.h - L.h) + a1.w;
   if (type == kBcExitH && !R.dry) dxi = m.bfExitRel[bf] - (a0.x + a0.y);
+  const float pa = face_pressure(m, a0.x, a0.z);
   if (!L.dry && !R.dry) {
     OwnF32 o;
-    o.u = a2.x; o.v = a2.y; o.s = a2.z; o.p = a2.w;
+    o.u = a2.x; o.v = a2.y; o.s = a2.z; o.p = pa;
     o.fxx = L.hu * o.u; o.fxy = L.hu * o.v; o.fyx = L.hv * o.u; o.fyy = L.hv * o.v;
     if (rs == kRiemannHll) hll_flux_wet_f32(L, o, R, dxi, 0.0f, m.gf, nx, ny, F);
     else roe_flux_wet_f32(L, o, R, dxi, 0.0f, m.gf, nx, ny, F);
   } else {
     riemann_flux<float>(rs, L, R, dxi, m.gf, nx, ny, m.hsmf, F);
-    F[1] -= a2.w * nx;
-    F[2] -= a2.w * ny;
+    F[1] -= pa * nx;
+    F[2] -= pa * ny;
   }
   C[2 * i] = make_float4(F[0] * len, F[1] * len, F[2] * len, 0.0f);
 }
@@ -700,35 +724,52 @@ __global__ void __launch_bounds__(kBlock, 4)
     k_stage_face_f32(DevMesh m, DevScalars s, StateF32 Xin, StateF32 Xbase, StateF32 Xout, int cfl, StageFuse f) {
   pdl_enter();
   extern __shared__ float4 fsm[];
-  float4* R0 = fsm;              // {xi_hi, xi_lo, hstill_hi, hstill_lo}
-  float4* R1 = R0 + kFaceRec;    // {h, hu, hv (clamped, masked), dry ? 1 : 0}
-  float4* R2 = R1 + kFaceRec;    // {u, v, sqrt h, p}
-  float4* R3 = R2 + kFaceRec;    // {zb, excess, n, 0}
-  float4* C = R3 + kFaceRec;     // [2 faceMax] terms F L of side a, side b
+  using L = FaceSmem;
+  float4* R0 = fsm + L::kR0;
+  float4* R1 = fsm + L::kR1;
+  float4* R2 = fsm + L::kR2;
+  float2* R3 = reinterpret_cast<float2*>(fsm + L::kR3);
+  float4* C = fsm + L::kC;
+  float4* sFL = fsm + L::fl(m.faceMax);
+  float4* sCS = fsm + L::cs(m.faceMax);
+  float2* sQ = reinterpret_cast<float2*>(fsm + L::q(m.faceMax));
+  float4* sXB = fsm + L::xb(m.faceMax);
+  float2* sQB = reinterpret_cast<float2*>(fsm + L::qb(m.faceMax));
   __shared__ float dtShared;
   const int tile = blockIdx.x, tid = threadIdx.x;
   const int base = tile * kBlock, c = base + tid;
   const bool active = c < m.n;
   const double* totalIn = FUSED ? f.totalIn : m.totalA;
-  // phase 1: side records of the own cells and the halo
-  float4 xin, cp, cs;
+  // phase 1: every load of the tile, then the side records
+  const int hid = tid < kHaloMax ? __ldg(&m.halo[(size_t)tile * kHaloMax + tid]) : -1;
+  const int f0 = __ldg(&m.FLoff[tile]), nf = __ldg(&m.FLoff[tile + 1]) - f0;
+  float4 xin, cp;
   uint2 refs;
   if (active) {
     xin = __ldg(&Xin.x[c]);
     cp = __ldg(&m.CP[c]);
-    cs = __ldg(&m.CS[c]);
     refs = __ldg(&m.FR[c]);
-    face_side_record(m, R0, R1, R2, R3, tid, xin, cp);
+    cp_async16(&sCS[tid], &m.CS[c]);
+    cp_async8(&sQ[tid], &Xin.q[c]);
+    if constexpr (MODE == kModeStage2) {
+      cp_async16(&sXB[tid], &Xbase.x[c]);
+      cp_async8(&sQB[tid], &Xbase.q[c]);
+    }
   }
-  if (tid < kHaloMax) {
-    const int hid = __ldg(&m.halo[(size_t)tile * kHaloMax + tid]);
-    if (hid >= 0) face_side_record(m, R0, R1, R2, R3, kBlock + tid, __ldg(&Xin.x[hid]), __ldg(&m.CP[hid]));
+  for (int i = tid; i < nf; i += kBlock) cp_async16(&sFL[i], &m.FL[f0 + i]);
+  cp_async_commit();
+  float4 xh, ph;
+  if (hid >= 0) {
+    xh = __ldg(&Xin.x[hid]);
+    ph = __ldg(&m.CP[hid]);
   }
+  if (active) face_side_record(m, R0, R1, R2, R3, tid, xin, cp);
+  if (hid >= 0) face_side_record(m, R0, R1, R2, R3, kBlock + tid, xh, ph);
   if (tid == 0) dtShared = FUSED ? (float)fused_dt(s, f) : *s.dtf;
+  cp_async_wait<0>();
   __syncthreads();
   // phase 2: the tile's faces
-  const int f0 = __ldg(&m.FLoff[tile]), nf = __ldg(&m.FLoff[tile + 1]) - f0;
-  for (int i = tid; i < nf; i += kBlock) face_terms<RS>(m, R0, R1, R2, R3, C, i, __ldg(&m.FL[f0 + i]), totalIn, s.flags);
+  for (int i = tid; i < nf; i += kBlock) face_terms<RS>(m, R0, R1, R2, R3, C, i, sFL[i], totalIn, s.flags);
   __syncthreads();
   // phase 3: each cell's terms in slot order, then the stage update
   float cand = INFINITY, hOut = 0.0f;
@@ -746,17 +787,17 @@ __global__ void __launch_bounds__(kBlock, 4)
       g1 += t.y;
       g2 += t.z;
       if (cfl) {   // the slot's geometry for the CFL candidate (|u.n| does not depend on the side)
-        const float4 g = __ldg(&m.FL[f0 + (ref >> 1)]);
+        const float4 g = sFL[ref >> 1];
         sl[k] = make_float4(g.x, g.y, g.z, 0.0f);
       }
     }
-    const float4 r0 = R0[tid], r1 = R1[tid], r3 = R3[tid];
-    SideF32 L;
-    L.s = face_side(r0, r1, r3.x);
-    L.xlo = r0.y;
-    L.excess = r3.y;
+    const float4 r1 = R1[tid], r2 = R2[tid];
+    SideF32 Ls;
+    Ls.s = face_side(R0[tid], r1, r2, cp.z);
+    Ls.xlo = xin.y;
+    Ls.excess = r1.w;
     const float dt = MODE == kModeRhs ? 0.0f : dtShared;
-    stage_finish<NS, MODE>(m, s, L, g0, g1, g2, c, sl, xin, cp, cs, Xin.q, Xbase.x, Xbase.q, c, dt, Xout, nullptr,
+    stage_finish<NS, MODE>(m, s, Ls, g0, g1, g2, c, sl, xin, cp, sCS[tid], sQ, sXB, sQB, tid, dt, Xout, nullptr,
                            cfl, cand, hOut, wetOut);
   }
   if (FUSED && f.record && blockIdx.x == 0 && tid == 0) fused_record(s, f);
@@ -1042,22 +1083,18 @@ void launch_pipe(const DevMesh& m, const DevScalars& s, StateF32 Xin, StateF32 X
   else launch_pipe_rs<NS, MODE, FUSED, kRiemannRoe>(m, s, Xin, Xbase, Xout, cfl, fu, st);
 }
 
-// Dynamic shared memory of the face kernel on this mesh: the side records and
-// two terms per face of the largest tile.
-uint32_t face_smem(const DevMesh& m) { return (uint32_t)(4 * kFaceRec + 2 * m.faceMax) * (uint32_t)sizeof(float4); }
-constexpr uint32_t kFaceSmemMax = (4 * kFaceRec + 2 * kFaceMaxPerTile) * sizeof(float4);
 
 template <int NS, int MODE, bool FUSED, int RS>
 void launch_face_rs(const DevMesh& m, const DevScalars& s, StateF32 Xin, StateF32 Xbase, StateF32 Xout, int cfl,
                     const StageFuse& fu, cudaStream_t st) {
-  static const bool attr = [] {   // more than 48 KB of dynamic shared memory: opt in once
+  static const bool attr = [] {   // more than 48 KB of dynamic shared memory: opt in once, for the largest tables
     cudaFuncSetAttribute(k_stage_face_f32<NS, MODE, FUSED, RS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)kFaceSmemMax);
+                         (int)FaceSmem::bytes(kFaceMaxPerTile, MODE));
     return true;
   }();
   (void)attr;
-  launch_k(true, k_stage_face_f32<NS, MODE, FUSED, RS>, blocks_for(m.n), kBlock, face_smem(m), st, m, s, Xin, Xbase,
-           Xout, cfl, fu);
+  launch_k(true, k_stage_face_f32<NS, MODE, FUSED, RS>, blocks_for(m.n), kBlock, FaceSmem::bytes(m.faceMax, MODE), st,
+           m, s, Xin, Xbase, Xout, cfl, fu);
 }
 template <int NS, int MODE, bool FUSED>
 void launch_face(const DevMesh& m, const DevScalars& s, StateF32 Xin, StateF32 Xbase, StateF32 Xout, int cfl,
@@ -1094,7 +1131,9 @@ bool stage_kernel_usable(const DevMesh& m, int k, int mode, StateF32 Xin, StateF
   auto a8 = [](const void* p) { return (reinterpret_cast<uintptr_t>(p) & 7u) == 0; };
   if (k == kStageGather) return true;
   if (m.nslot > 4) return false;
-  if (k == kStageFace) return m.FL && m.FLoff && m.FR && m.halo && m.faceMax <= kFaceMaxPerTile;
+  if (k == kStageFace)   // cp.async: 16-byte records 16-byte aligned, the lo parts 8-byte aligned
+    return m.FL && m.FLoff && m.FR && m.halo && m.faceMax <= kFaceMaxPerTile && a16(m.CS) && a16(m.FL) &&
+           a8(Xin.q) && (mode != kModeStage2 || (a16(Xbase.x) && a8(Xbase.q)));
   if (k == kStagePipe)   // cp.async: 16-byte records 16-byte aligned, the lo parts 8-byte aligned
     return m.SLp && m.halo && a16(m.SLp) && a16(m.CP) && a16(m.CS) && a16(Xin.x) && a8(Xin.q) &&
            (mode != kModeStage2 || (a16(Xbase.x) && a8(Xbase.q)));
