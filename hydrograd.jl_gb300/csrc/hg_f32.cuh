@@ -22,6 +22,41 @@ struct DepthF32 {
   bool dry;
 };
 
+// Packed FP32x2 arithmetic (Blackwell's paired FP32 instructions: one issue
+// slot for two lanes of the same operation, each rounded as its scalar form).
+// The stage kernels are bound by instruction issue, and most of their FP32
+// work comes in pairs -- the (qx, qy) rows of the update, (u, v), the momentum
+// rows of a flux -- so the pairs are written with these.
+__device__ __forceinline__ float2 p2(float a, float b) { return make_float2(a, b); }
+__device__ __forceinline__ float2 p2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+
+// two_sum / fast_two_sum / df_add / df_add2 on two lanes at once.
+__device__ __forceinline__ void two_sum2(float2 a, float2 b, float2& s, float2& e) {
+  s = add2(a, b);
+  const float2 bb = sub2(s, a);
+  e = add2(sub2(a, sub2(s, bb)), sub2(b, bb));
+}
+__device__ __forceinline__ void fast_two_sum2(float2 a, float2 b, float2& s, float2& e) {
+  s = add2(a, b);
+  e = sub2(b, sub2(s, a));
+}
+__device__ __forceinline__ void df_add_2(float2 ah, float2 al, float2 d, float2& rh, float2& rl) {
+  float2 s, e;
+  two_sum2(ah, d, s, e);
+  e = add2(e, al);
+  fast_two_sum2(s, e, rh, rl);
+}
+__device__ __forceinline__ void df_add2_2(float2 ah, float2 al, float2 bh, float2 bl, float2& rh, float2& rl) {
+  float2 s, e;
+  two_sum2(ah, bh, s, e);
+  e = add2(e, add2(al, bl));
+  fast_two_sum2(s, e, rh, rl);
+}
+
 __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
   s = a + b;
   const float bb = s - a;
@@ -155,29 +190,31 @@ __device__ __forceinline__ void roe_flux_wet_f32(const Side<float>& L, const Own
                                                  float dxi, float dhst, float g, float nx, float ny, float F[3]) {
   const float rq = rsqrtf(R.h);
   const float rR = rq * rq;
-  const float uR = R.hu * rR, vR = R.hv * rR;
+  const float2 qL = p2(L.hu, L.hv), qR = p2(R.hu, R.hv);
+  const float2 uvR = mul2(qR, p2(rR));   // (uR, vR)
   const float sR = R.h * rq;
   const float rs = 1.0f / (o.s + sR);
-  const float uRoe = (o.s * o.u + sR * uR) * rs;
-  const float vRoe = (o.s * o.v + sR * vR) * rs;
-  const float unRoe = uRoe * nx + vRoe * ny;
+  const float2 uvRoe = mul2(fma2(p2(o.s), p2(o.u, o.v), mul2(p2(sR), uvR)), p2(rs));
+  const float unRoe = uvRoe.x * nx + uvRoe.y * ny;
   const float gh = g * ((L.h + R.h) * 0.5f);
   const float rc = rsqrtf(gh);
   const float cRoe = gh * rc;   // sqrt(g hRoe)
-  const float d1 = R.hu - L.hu, d2 = R.hv - L.hv;
-  const float t = (unRoe * dxi - nx * d1 - ny * d2) * (0.5f * rc);
-  const float w0 = (ny * d1 - nx * d2 - (uRoe * ny - vRoe * nx) * dxi) * smooth_abs_f32(unRoe);
+  const float2 d = sub2(qR, qL);   // (d1, d2)
+  const float t = (unRoe * dxi - nx * d.x - ny * d.y) * (0.5f * rc);
+  const float w0 = (ny * d.x - nx * d.y - (uvRoe.x * ny - uvRoe.y * nx) * dxi) * smooth_abs_f32(unRoe);
   const float w1 = (0.5f * dxi + t) * smooth_abs_f32(unRoe - cRoe);
   const float w2 = (0.5f * dxi - t) * smooth_abs_f32(unRoe + cRoe);
   const float sum = w1 + w2, dif = cRoe * (w2 - w1);
-  const float A0 = sum;
-  const float A1 = ny * w0 + uRoe * sum + nx * dif;
-  const float A2 = -nx * w0 + vRoe * sum + ny * dif;
+  // (A1, A2) = (ny, -nx) w0 + (uRoe, vRoe) sum + (nx, ny) dif
+  const float2 A12 = fma2(p2(ny, -nx), p2(w0), fma2(uvRoe, p2(sum), mul2(p2(nx, ny), p2(dif))));
   const float dp = pressure_jump_f32(g, L.xi, R.xi, dxi, R.hst, dhst);   // p_R - p_L
-  const float fR1x = R.hu * uR + dp, fR2y = R.hv * vR + dp;
-  F[0] = 0.5f * ((L.hu * nx + L.hv * ny) + (R.hu * nx + R.hv * ny) - A0);
-  F[1] = 0.5f * ((o.fxx * nx + o.fxy * ny) + (fR1x * nx + R.hu * vR * ny) - A1);
-  F[2] = 0.5f * ((o.fyx * nx + o.fyy * ny) + (R.hv * uR * nx + fR2y * ny) - A2);
+  // momentum rows: own tensor . n, the other side's tensor . n, plus dp n
+  const float2 fLn = fma2(p2(o.fxx, o.fyx), p2(nx), mul2(p2(o.fxy, o.fyy), p2(ny)));
+  const float2 fRn = fma2(mul2(qR, p2(uvR.x)), p2(nx), fma2(mul2(qR, p2(uvR.y)), p2(ny), mul2(p2(dp), p2(nx, ny))));
+  F[0] = 0.5f * ((L.hu * nx + L.hv * ny) + (R.hu * nx + R.hv * ny) - sum);
+  const float2 F12 = mul2(p2(0.5f), sub2(add2(fLn, fRn), A12));
+  F[1] = F12.x;
+  F[2] = F12.y;
 }
 
 // HLL flux of a face whose two sides are both wet (hll_flux's wet-wet case),
@@ -246,24 +283,29 @@ struct FaceSideF32 {
 __device__ __forceinline__ float roe_face_wet_f32(const FaceSideF32& A, const FaceSideF32& B, float dxi, float dhst,
                                                   float g, float nx, float ny, float F[3]) {
   const float rs = 1.0f / (A.s + B.s);
-  const float uRoe = (A.s * A.u + B.s * B.u) * rs;
-  const float vRoe = (A.s * A.v + B.s * B.v) * rs;
-  const float unRoe = uRoe * nx + vRoe * ny;
+  const float2 uvA = p2(A.u, A.v), uvB = p2(B.u, B.v);
+  const float2 qA = p2(A.hu, A.hv), qB = p2(B.hu, B.hv);
+  const float2 uvRoe = mul2(fma2(p2(A.s), uvA, mul2(p2(B.s), uvB)), p2(rs));
+  const float unRoe = uvRoe.x * nx + uvRoe.y * ny;
   const float gh = g * ((A.h + B.h) * 0.5f);
   const float rc = rsqrtf(gh);
   const float cRoe = gh * rc;
-  const float d1 = B.hu - A.hu, d2 = B.hv - A.hv;
-  const float t = (unRoe * dxi - nx * d1 - ny * d2) * (0.5f * rc);
-  const float w0 = (ny * d1 - nx * d2 - (uRoe * ny - vRoe * nx) * dxi) * smooth_abs_f32(unRoe);
+  const float2 d = sub2(qB, qA);
+  const float t = (unRoe * dxi - nx * d.x - ny * d.y) * (0.5f * rc);
+  const float w0 = (ny * d.x - nx * d.y - (uvRoe.x * ny - uvRoe.y * nx) * dxi) * smooth_abs_f32(unRoe);
   const float w1 = (0.5f * dxi + t) * smooth_abs_f32(unRoe - cRoe);
   const float w2 = (0.5f * dxi - t) * smooth_abs_f32(unRoe + cRoe);
   const float sum = w1 + w2, dif = cRoe * (w2 - w1);
-  const float A1 = ny * w0 + uRoe * sum + nx * dif;
-  const float A2 = -nx * w0 + vRoe * sum + ny * dif;
+  const float2 A12 = fma2(p2(ny, -nx), p2(w0), fma2(uvRoe, p2(sum), mul2(p2(nx, ny), p2(dif))));
   const float dp = pressure_jump_f32(g, A.xi, B.xi, dxi, B.hst, dhst);
+  // (hu u, hv u) and (hu v, hv v) of both sides, dotted with n, plus dp n
+  const float2 fu = fma2(qA, p2(uvA.x), mul2(qB, p2(uvB.x)));
+  const float2 fv = fma2(qA, p2(uvA.y), mul2(qB, p2(uvB.y)));
+  const float2 fn = fma2(fu, p2(nx), fma2(fv, p2(ny), mul2(p2(dp), p2(nx, ny))));
   F[0] = 0.5f * ((A.hu * nx + A.hv * ny) + (B.hu * nx + B.hv * ny) - sum);
-  F[1] = 0.5f * (((A.hu * A.u + B.hu * B.u) + dp) * nx + (A.hu * A.v + B.hu * B.v) * ny - A1);
-  F[2] = 0.5f * ((A.hv * A.u + B.hv * B.u) * nx + ((A.hv * A.v + B.hv * B.v) + dp) * ny - A2);
+  const float2 F12 = mul2(p2(0.5f), sub2(fn, A12));
+  F[1] = F12.x;
+  F[2] = F12.y;
   return dp;
 }
 

@@ -112,8 +112,9 @@ __device__ __forceinline__ void face_sum_f32(const DevMesh& m, const float4* __r
     one_face_f32<LOC, RS>(m, X, sX, sP, hX, hP, base, L, own, hstPair, sl[k], nb, totalA, man, flags, F);
     const float len = sl[k].z;
     f0 = fmaf(F[0], len, f0);
-    f1 = fmaf(F[1], len, f1);
-    f2 = fmaf(F[2], len, f2);
+    const float2 f12 = fma2(p2(F[1], F[2]), p2(len), p2(f1, f2));
+    f1 = f12.x;
+    f2 = f12.y;
   }
 }
 
@@ -233,38 +234,45 @@ __device__ __forceinline__ void stage_finish(const DevMesh& m, const DevScalars&
                                              int k, float dt, StateF32 Xout, double* Rout, bool cfl, float& cand,
                                              float& hOut, bool& wetOut) {
   const float A = cs.z;
-  const float r0 = -f0 / A, r1 = -f1 / A, r2 = -f2 / A;
+  const float rA = -1.0f / A;
+  const float r0 = f0 * rA;
+  const float2 r12 = mul2(p2(f1, f2), p2(rA));
   // Manning friction, or the flow-resistance closure F q / |q|_smooth
   // (semi_discretize_swe_2D.jl:517-529) with F from the resistance kernels.
   const float fr = m.res.kind == kResUdeFlowResistance
                        ? m.res.fresF[c] / smooth_sqrt(L.s.hu * L.s.hu + L.s.hv * L.s.hv)
                        : friction_coef(m.gf, m.kn2f, m.hsmf, cp.w, L.s.h, L.s.hu, L.s.hv);
-  const float sx = L.s.dry ? 0.0f : (m.gf * L.s.xi * cs.x - fr * L.s.hu);
-  const float sy = L.s.dry ? 0.0f : (m.gf * L.s.xi * cs.y - fr * L.s.hv);
-  const float d0 = r0, d1 = r1 + sx, d2 = r2 + sy;
+  // (h > h_small) (g xi S0 - friction q), the momentum rows as one pair
+  const float2 src = L.s.dry ? p2(0.0f) : fma2(p2(m.gf * L.s.xi), p2(cs.x, cs.y), mul2(p2(-fr), p2(L.s.hu, L.s.hv)));
+  const float d0 = r0;
+  const float2 d12 = add2(r12, src);
   if constexpr (MODE == kModeRhs) {
-    Rout[c] = d0; Rout[m.n + c] = d1; Rout[2 * m.n + c] = d2;
+    Rout[c] = d0; Rout[m.n + c] = d12.x; Rout[2 * m.n + c] = d12.y;
   } else {
     const float2 qin = qinP[k];
-    const float hi[3] = {xin.x, xin.z, xin.w}, lo[3] = {xin.y, qin.x, qin.y};
-    const float inc[3] = {dt * d0, dt * d1, dt * d2};
+    const float inc0 = dt * d0;
+    const float2 inc12 = mul2(p2(dt), d12);
     float xh[3], xl[3];
+    float2 qh, ql;
     if constexpr (MODE == kModeStage2) {
       const float4 xb = xbP[k];
       const float2 qb = qbP[k];
-      const float bh[3] = {xb.x, xb.z, xb.w}, bl[3] = {xb.y, qb.x, qb.y};
-#pragma unroll
-      for (int b = 0; b < 3; ++b) {
-        float sh, slo;
-        df_add2(bh[b], bl[b], hi[b], lo[b], sh, slo);
-        df_add(sh, slo, inc[b], xh[b], xl[b]);
-        xh[b] *= 0.5f;
-        xl[b] *= 0.5f;
-      }
+      float sh, slo;
+      df_add2(xb.x, xb.y, xin.x, xin.y, sh, slo);
+      df_add(sh, slo, inc0, xh[0], xl[0]);
+      xh[0] *= 0.5f;
+      xl[0] *= 0.5f;
+      float2 sh2, sl2;
+      df_add2_2(p2(xb.z, xb.w), qb, p2(xin.z, xin.w), qin, sh2, sl2);
+      df_add_2(sh2, sl2, inc12, qh, ql);
+      qh = mul2(qh, p2(0.5f));
+      ql = mul2(ql, p2(0.5f));
     } else {
-#pragma unroll
-      for (int b = 0; b < 3; ++b) df_add(hi[b], lo[b], inc[b], xh[b], xl[b]);
+      df_add(xin.x, xin.y, inc0, xh[0], xl[0]);
+      df_add_2(p2(xin.z, xin.w), qin, inc12, qh, ql);
     }
+    xh[1] = qh.x; xh[2] = qh.y;
+    xl[1] = ql.x; xl[2] = ql.y;
     DepthF32 dn = depth_f32(xh[0], xl[0], cp.x, cp.y, m.hsmf, m.hsmLo);
     bool clamp = dn.dry;   // h <= h_small (pair granularity): h = h_small, q = 0
     if constexpr (MODE == kModeEulerRef) clamp = (double)xh[0] + (double)xl[0] < m.hsm;
@@ -675,9 +683,13 @@ __device__ __forceinline__ void face_terms(const DevMesh& m, const float4* R0, c
       const FaceSideF32 B{b0.x, b0.z, b1.x, b1.y, b1.z, b2.x, b2.y, b2.z};
       const float dp = rs == kRiemannHll ? hll_face_wet_f32(A, B, dxi, dhst, m.gf, nx, ny, F)
                                          : roe_face_wet_f32(A, B, dxi, dhst, m.gf, nx, ny, F);
-      const float c0 = F[0] * len, c1 = F[1] * len, c2 = F[2] * len;
-      if (aOwn) C[2 * i] = make_float4(c0, c1, c2, 0.0f);
-      if (bOwn) C[2 * i + 1] = make_float4(-c0, dp * nx * len - c1, dp * ny * len - c2, 0.0f);
+      const float c0 = F[0] * len;
+      const float2 c12 = mul2(p2(F[1], F[2]), p2(len));
+      if (aOwn) C[2 * i] = make_float4(c0, c12.x, c12.y, 0.0f);
+      if (bOwn) {   // -c_a + dp n L
+        const float2 b12 = fma2(p2(dp * len), p2(nx, ny), p2(-c12.x, -c12.y));
+        C[2 * i + 1] = make_float4(-c0, b12.x, b12.y, 0.0f);
+      }
     } else {                                            // a dry side: each in-tile side from its own cell
       const Side<float> sa = face_side(a0, a1, a2, R3[a].x), sb = face_side(b0, b1, b2, R3[b].x);
       if (aOwn) {
@@ -784,8 +796,9 @@ __global__ void __launch_bounds__(kBlock, 4)
       if (ref == 0xFFFFu) continue;
       const float4 t = C[ref];
       g0 += t.x;
-      g1 += t.y;
-      g2 += t.z;
+      const float2 g12 = add2(p2(g1, g2), p2(t.y, t.z));
+      g1 = g12.x;
+      g2 = g12.y;
       if (cfl) {   // the slot's geometry for the CFL candidate (|u.n| does not depend on the side)
         const float4 g = sFL[ref >> 1];
         sl[k] = make_float4(g.x, g.y, g.z, 0.0f);

@@ -88,3 +88,57 @@ def test_reference_euler_loop_floods_the_dry_bed(dry):
     assert below.sum() > 1000
     # xi clamped to h_small: depth = hstill + h_small, water up to the still-water level
     assert np.allclose(h[below], hst[below] + 1e-3, rtol=0, atol=1e-9)
+
+
+def test_a_film_far_thinner_than_fp32_resolution_switches_on_the_bed_slope_source(dry):
+    """Why FP32 flux arithmetic cannot follow the reference on a dry bed: the
+    RHS jumps at h = h_small.  A cell whose depth exceeds h_small by 1e-12 m
+    is wet, so its momentum source (h > h_small) g xi S0
+    (semi_discretize_swe_2D.jl:463,474-475) is on -- with xi = h - hstill
+    about -hstill, an O(0.1) m^2/s^2 acceleration -- while its dry
+    neighbours' one-sided fluxes carry the h-based pressure
+    (swe_2D_solvers.jl:54-75), which does not balance it.  1e-12 m is 1e-12
+    of the state's scale, far below what FP32 (24-bit) flux arithmetic
+    resolves."""
+    case, o, N, hst = dry
+    Q = case["Q0"].copy()
+    dry0 = Q[:N] + hst <= 1.0001e-3
+    r0 = o.rhs(Q)
+    # dry cells below still water away from the pool: no momentum change
+    cand = np.nonzero(dry0 & (hst > 0.5) & (r0[N:2 * N] == 0.0) & (r0[2 * N:] == 0.0))[0]
+    assert len(cand) > 500
+    acc = []
+    for c in cand[:: max(1, len(cand) // 20)]:
+        Qf = Q.copy()
+        Qf[c] = 1e-3 + 1e-12 - hst[c]                   # a film 1e-12 m above h_small
+        r1 = o.rhs(Qf)
+        acc.append(np.hypot(r1[N + c], r1[2 * N + c]))
+    assert np.median(acc) > 1e-2
+
+
+def test_films_spread_ahead_of_the_front_in_fp64():
+    """The reference's own FP64 run (river_triangles(128, dry_land=True),
+    32,768 cells, fixed dt = the CFL-0.01 step) wets cells far ahead of the
+    pool with films of 1e-13-1e-9 m: after 50 steps (0.14 s, in which the
+    pool's edge moves about half a metre) they reach more than 1 km from the
+    pool's centre, a numerical precursor moving about a cell per step.  The
+    same run with FMA contraction, or with the wet state perturbed by 1e-6,
+    reproduces them to 1e-12, so they are systematic FP64 arithmetic -- of a
+    size that FP32 flux arithmetic does not produce, which is why the FP32C
+    path departs from FP64 at dry fronts (tests/test_gpu_fronts.py)."""
+    from hydrograd_gb.workloads import cell_centroids
+    case = river_triangles(n=128, dry_land=True)
+    N = len(case["cell_node_count"])
+    hst = case["wstill"] - case["zb_cells"]
+    o = Oracle(case)
+    o.set_wstill(case["wstill"])
+    o.set_manning_cells(case["manning_zones"][case["mat_id"]])
+    o.set_inlet_q(case["inlet_q"])
+    o.set_exit_wse(case["exit_wse"])
+    Q = o.rk2(case["Q0"], 50, dt=o.cfl_dt(case["Q0"], 0.01), nthreads=THREADS)
+    h = Q[:N] + hst
+    films = (h > 1e-3) & (h < 1e-3 + 1e-9)
+    thin = (h > 1e-3) & (h < 1e-3 + 1e-5)
+    cx, cy = cell_centroids(case)
+    assert films.sum() >= 10
+    assert np.hypot(cx - 300.0, cy - 1000.0)[thin].max() > 1000.0
