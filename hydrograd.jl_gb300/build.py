@@ -27,7 +27,7 @@ NO_FMAD = {"hg_forward_f64.cu", "hg_tsit5.cu", "hg_resistance.cu"}
 # FP32-compensated path: approximate division/sqrt/log2/exp2 (a few ulp; the
 # path's contract is a 1e-5 state error against the FP64 oracle).
 FAST_MATH = {"hg_forward_f32.cu", "hg_adjoint_f32.cu"}
-CXX_SOURCES = ["hg_mesh.cpp", "hg_capi.cpp", "hg_adjoint.cpp", "hg_tsit5.cpp"]
+CXX_SOURCES = ["hg_mesh.cpp", "hg_capi.cpp", "hg_adjoint.cpp", "hg_tsit5.cpp", "hg_autotune.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

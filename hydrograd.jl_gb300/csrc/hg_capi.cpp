@@ -3,6 +3,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <new>
@@ -12,6 +13,7 @@
 #include <cuda_runtime.h>
 
 #include "hg_adjoint.hpp"
+#include "hg_autotune.hpp"
 #include "hg_ctx.hpp"
 #include "hg_mesh.hpp"
 #include "hg_state.hpp"
@@ -26,6 +28,10 @@ thread_local std::string g_err;
 // Smallest CFL step accepted by default: swe_2D_consts.dt_min, which the
 // reference sets to 0.001 s (solve_swe_2D.jl:83,98) and stores unused.
 constexpr double kDtMinDefault = 0.001;
+// Stage-kernel family of a new context (hg_set_stage_family): 0 gather.  On
+// the 1M-cell reach the face-once kernel ties the gather kernel on stage 1
+// (37.0 against 36.0 us) and loses on stage 2, so it is the opt-in family.
+constexpr int kDefaultFamily = 0;
 
 int fail(hg_ctx* ctx, int code, const std::string& msg) {
   if (ctx) ctx->err = msg;
@@ -297,14 +303,60 @@ int set_fixed_dt(hg_ctx* c, double dt) {
   return HG_OK;
 }
 
-// Autotuner of the fused FP32 stages: times each stage kernel usable on this
-// mesh (gather, pipe, tma -- all compute the same results) on the resident
-// state, a stage-1 and a stage-2 launch per repetition, each repetition after
-// an L2 flush and the kernels interleaved, and keeps the fastest.  Outputs go
-// to scratch carved from the flush buffer (the flush overwrites it before the
-// next repetition's stage 1 writes it again); the resident state, the step
-// bookkeeping and the error flags are left as they were.
-int autotune_stage(hg_ctx* c, int reps) {
+// Autotuner of the fused FP32 stages.  Its candidates are kernels and shapes
+// that compute bit-identical results, so the choice changes speed only:
+//   family 0: the gather kernel with the register budget of 4 or 3 resident
+//             blocks per SM, the pipelined persistent kernel, the bulk-copy
+//             persistent kernel;
+//   family 1: the face-once kernel with the budget of 4 or 3 blocks per SM.
+// (The face-once kernel evaluates each wet-wet face once and so rounds
+// differently from the gather family; which family a context uses is fixed by
+// hg_set_stage_family / HG_STAGE_FAMILY, never by timing.)  The usable
+// candidates are timed on the resident state, a stage-1 and a stage-2 launch
+// per repetition, each repetition after an L2 flush and the candidates
+// interleaved; the fastest is kept and written to the cache file
+// (hg_autotune.hpp) under a key of the GPU, the mesh's face tables, the
+// precision, the Riemann solver and the family, so a later context on the
+// same mesh and GPU takes it without timing.  Outputs go to scratch carved from
+// the flush buffer (the flush overwrites it before the next repetition's
+// stage 1 writes it again); the resident state, the step bookkeeping and the
+// error flags are left as they were.
+std::vector<TuneChoice> stage_candidates(const hg_ctx* c, StateF32 s1) {
+  std::vector<TuneChoice> all;
+  if (c->stageFamily == 1) {
+    all = {TuneChoice{kStageFace, 0}, TuneChoice{kStageFace, 1}};
+  } else {
+    all = {TuneChoice{kStageGather, 0}, TuneChoice{kStageGather, 1}, TuneChoice{kStagePipe, 0},
+           TuneChoice{kStageTma, 0}};
+    if (c->dm.nslot > 4) all = {TuneChoice{kStageGather, 0}};
+  }
+  std::vector<TuneChoice> out;
+  for (const TuneChoice& t : all)
+    if (stage_kernel_usable(c->dm, t.kernel, kModeStage1, StateF32{c->XA, c->XQA}, StateF32{}) &&
+        stage_kernel_usable(c->dm, t.kernel, kModeStage2, s1, StateF32{c->XA, c->XQA}))
+      out.push_back(t);
+  return out;
+}
+
+std::string autotune_key(const hg_ctx* c) {
+  cudaDeviceProp p{};
+  cudaGetDeviceProperties(&p, c->device);
+  char sig[32];
+  std::snprintf(sig, sizeof(sig), "%016llx", (unsigned long long)c->meshSig);
+  return std::string(p.name) + "|sm" + std::to_string(p.major * 10 + p.minor) + "|fp32c|family" +
+         std::to_string(c->stageFamily) + "|rs" + std::to_string(c->dm.riemann) + "|n" + std::to_string(c->n) +
+         "|s" + std::to_string(c->dm.nslot) + "|" + sig;
+}
+
+void set_stage_choice(hg_ctx* c, const TuneChoice& t) {
+  if (c->dm.stageKernel != t.kernel || c->dm.stageVariant != t.variant) c->graphValid = false;
+  c->dm.stageKernel = t.kernel;
+  c->dm.stageVariant = t.variant;
+}
+
+// useCache: take a cached choice instead of timing (the automatic tune of a
+// context's first steps); an explicit hg_autotune times and rewrites it.
+int autotune_stage(hg_ctx* c, int reps, bool useCache) {
   if (!fused(c)) return HG_OK;
   const size_t n = (size_t)c->n;
   const size_t rec = (n * sizeof(float4) + 255) & ~(size_t)255, lo = (n * sizeof(float2) + 255) & ~(size_t)255;
@@ -312,14 +364,24 @@ int autotune_stage(hg_ctx* c, int reps) {
   char* base = static_cast<char*>(c->flushBuf);
   const StateF32 s1{reinterpret_cast<float4*>(base), reinterpret_cast<float2*>(base + rec)};
   const StateF32 s2{reinterpret_cast<float4*>(base + rec + lo), reinterpret_cast<float2*>(base + 2 * rec + lo)};
+  const std::vector<TuneChoice> cand = stage_candidates(c, s1);
+  if (cand.empty()) return HG_OK;
+  const std::string path = autotune_cache_path();
+  const std::string key = autotune_key(c);
+  if (useCache) {
+    TuneChoice t;
+    if (autotune_cache_load(path, key, t))
+      for (const TuneChoice& x : cand)
+        if (x.kernel == t.kernel && x.variant == t.variant) {
+          set_stage_choice(c, t);
+          c->stageTuned = true;
+          c->tuneSource = 2;
+          return HG_OK;
+        }
+  }
   int32_t flags = 0;
   HG_CUDA(c, cudaMemcpyAsync(&flags, c->ds.flags, sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream));
   HG_CUDA(c, cudaStreamSynchronize(c->stream));
-  std::vector<int> cand;
-  for (int k : {(int)kStageGather, (int)kStagePipe, (int)kStageTma})
-    if (stage_kernel_usable(c->dm, k, kModeStage1, xa(c), StateF32{}) &&
-        stage_kernel_usable(c->dm, k, kModeStage2, s1, xa(c)))
-      cand.push_back(k);
   std::vector<double> total(cand.size(), 0.0);
   cudaEvent_t a, b;
   HG_CUDA(c, cudaEventCreate(&a));
@@ -332,7 +394,8 @@ int autotune_stage(hg_ctx* c, int reps) {
   for (int r = 0; r < reps; ++r)
     for (size_t i = 0; i < cand.size(); ++i) {
       DevMesh m = c->dm;
-      m.stageKernel = cand[i];
+      m.stageKernel = cand[i].kernel;
+      m.stageVariant = cand[i].variant;
       c->launches += launch_flush(c->flushBuf, c->flushBytes, c->stream);
       cudaEventRecord(a, c->stream);
       f.totalIn = c->d_tot;
@@ -355,11 +418,10 @@ int autotune_stage(hg_ctx* c, int reps) {
   size_t best = 0;
   for (size_t i = 1; i < cand.size(); ++i)
     if (total[i] < total[best]) best = i;
-  if (!cand.empty() && c->dm.stageKernel != cand[best]) {
-    c->dm.stageKernel = cand[best];
-    c->graphValid = false;
-  }
+  set_stage_choice(c, cand[best]);
   c->stageTuned = true;
+  c->tuneSource = 1;
+  if (reps > 0) autotune_cache_store(path, key, cand[best], total[best] / reps);
   return HG_OK;
 }
 
@@ -371,7 +433,7 @@ int begin_steps(hg_ctx* c, bool rk2, double dt, double cfl) {
     if (rc) return rc;
   }
   if (rk2 && fused(c) && !c->stageTuned && stage_kernel_forced() < 0) {
-    int rc = autotune_stage(c, 3);
+    int rc = autotune_stage(c, 3, true);
     if (rc) return rc;
   }
   if (rk2 && fused(c)) {
@@ -1156,10 +1218,31 @@ int hg_autotune(hg_ctx* ctx, int32_t reps, int32_t* kernel) {
   if (!ctx || reps < 0) return fail(ctx, HG_ERR_ARG, "hg_autotune: bad argument");
   cudaSetDevice(ctx->device);
   if (reps > 0) {
-    int rc = autotune_stage(ctx, reps);
+    int rc = autotune_stage(ctx, reps, false);
     if (rc) return rc;
   }
   if (kernel) *kernel = stage_kernel_forced() >= 0 ? stage_kernel_forced() : ctx->dm.stageKernel;
+  return HG_OK;
+}
+
+int hg_autotune_info(const hg_ctx* ctx, int32_t* kernel, int32_t* variant, int32_t* source) {
+  if (!ctx) return fail(nullptr, HG_ERR_ARG, "hg_autotune_info: null context");
+  const bool forced = stage_kernel_forced() >= 0 || stage_variant_forced() >= 0;
+  if (kernel) *kernel = stage_kernel_forced() >= 0 ? stage_kernel_forced() : ctx->dm.stageKernel;
+  if (variant) *variant = stage_variant_forced() >= 0 ? stage_variant_forced() : ctx->dm.stageVariant;
+  if (source) *source = forced ? 3 : ctx->tuneSource;
+  return HG_OK;
+}
+
+int hg_set_stage_family(hg_ctx* ctx, int32_t family) {
+  if (!ctx) return fail(ctx, HG_ERR_ARG, "hg_set_stage_family: null context");
+  if (family != 0 && family != 1) return fail(ctx, HG_ERR_ARG, "hg_set_stage_family: 0 (gather) or 1 (face)");
+  if (family == 1 && !ctx->dm.FL) return fail(ctx, HG_ERR_UNSUPPORTED, "hg_set_stage_family: no face tables for this mesh");
+  ctx->stageFamily = family;
+  set_stage_choice(ctx, family == 1 ? TuneChoice{kStageFace, 0}
+                                    : TuneChoice{ctx->dm.SLp ? kStagePipe : kStageGather, 0});
+  ctx->stageTuned = false;   // the next RK2 steps tune (or read the cache) within the family
+  ctx->tuneSource = 0;
   return HG_OK;
 }
 
@@ -1518,6 +1601,19 @@ int ctx_setup_device(hg_ctx* c) {
   dm.FR = d_FR;
   dm.faceMax = d_FL ? faceMax : 0;
   dm.stageKernel = d_SLp ? kStagePipe : kStageGather;
+  // The autotuner's family (see autotune_stage): HG_STAGE_FAMILY=gather|face, else kDefaultFamily
+  {
+    const char* e = std::getenv("HG_STAGE_FAMILY");
+    int fam = kDefaultFamily;
+    if (e && std::strcmp(e, "gather") == 0) fam = 0;
+    if (e && std::strcmp(e, "face") == 0) fam = 1;
+    c->stageFamily = (fam == 1 && d_FL) ? 1 : 0;
+    if (c->stageFamily == 1) dm.stageKernel = kStageFace;
+    // the mesh signature of the autotune cache: the device-order face tables
+    uint64_t h = fnv1a(nb.data(), nb.size() * sizeof(int32_t));
+    h = fnv1a(SL.data(), SL.size() * sizeof(float4), h);
+    c->meshSig = h;
+  }
   dm.bfInfo = d_bfInfo; dm.bfLp23 = d_lp23; dm.bfLp23f = d_lp23f; dm.bfLp53 = d_bflp53;
   dm.bfExitRel = c->d_bfExitRel;
   dm.inletOff = d_inletOff; dm.inletCell = d_inletCell; dm.inletLp53 = d_lp53;

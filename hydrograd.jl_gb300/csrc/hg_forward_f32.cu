@@ -312,8 +312,10 @@ __device__ __forceinline__ void fused_record(const DevScalars& s, const StageFus
 // holds no FP64 arithmetic: the stage mode is a template parameter (the FP64
 // comparison of the reference Euler clamp exists only in that instance), and
 // the fused step's dt is formed once per block.
-template <int NS, bool FUSED, int MODE, int RS = -1>
-__global__ void __launch_bounds__(kBlock, stage_min_blocks<NS>())
+// MINB > 0: the register budget of MINB resident blocks per SM (a shape the
+// autotuner chooses among; the arithmetic does not depend on it).
+template <int NS, bool FUSED, int MODE, int RS = -1, int MINB = 0>
+__global__ void __launch_bounds__(kBlock, MINB > 0 ? MINB : stage_min_blocks<NS>())
     k_stage_f32(DevMesh m, DevScalars s, StateF32 Xin, StateF32 Xbase, StateF32 Xout, double* Rout, int cfl,
                 StageFuse f) {
   pdl_enter();
@@ -731,8 +733,8 @@ __device__ __forceinline__ void face_terms(const DevMesh& m, const float4* R0, c
   C[2 * i] = make_float4(F[0] * len, F[1] * len, F[2] * len, 0.0f);
 }
 
-template <int NS, int MODE, bool FUSED, int RS>
-__global__ void __launch_bounds__(kBlock, 4)
+template <int NS, int MODE, bool FUSED, int RS, int MINB = 4>
+__global__ void __launch_bounds__(kBlock, MINB)
     k_stage_face_f32(DevMesh m, DevScalars s, StateF32 Xin, StateF32 Xbase, StateF32 Xout, int cfl, StageFuse f) {
   pdl_enter();
   extern __shared__ float4 fsm[];
@@ -997,14 +999,18 @@ template <int NS, bool FUSED>
 void launch_stage_ns(const DevMesh& m, const DevScalars& s, int mode, StateF32 Xin, StateF32 Xbase, StateF32 Xout,
                      double* Rout, int cfl, const StageFuse& f, cudaStream_t st) {
   const int nb = blocks_for(m.n);
-  if constexpr (FUSED) {   // the fused stages: the solver fixed per instance
+  if constexpr (FUSED) {   // the fused stages: the solver fixed per instance, the register budget by variant
     const bool hll = m.riemann == kRiemannHll;
-    if (mode == kModeStage1)
-      launch_k(true, hll ? k_stage_f32<NS, true, kModeStage1, kRiemannHll> : k_stage_f32<NS, true, kModeStage1, kRiemannRoe>,
-               nb, kBlock, 0, st, m, s, Xin, Xbase, Xout, Rout, cfl, f);
-    else if (mode == kModeStage2)
-      launch_k(true, hll ? k_stage_f32<NS, true, kModeStage2, kRiemannHll> : k_stage_f32<NS, true, kModeStage2, kRiemannRoe>,
-               nb, kBlock, 0, st, m, s, Xin, Xbase, Xout, Rout, cfl, f);
+    const bool v3 = NS <= 4 && m.stageVariant == 1;   // 3 blocks per SM (80 registers) instead of 4
+    if (mode == kModeStage1) {
+      auto k = hll ? (v3 ? k_stage_f32<NS, true, kModeStage1, kRiemannHll, 3> : k_stage_f32<NS, true, kModeStage1, kRiemannHll>)
+                   : (v3 ? k_stage_f32<NS, true, kModeStage1, kRiemannRoe, 3> : k_stage_f32<NS, true, kModeStage1, kRiemannRoe>);
+      launch_k(true, k, nb, kBlock, 0, st, m, s, Xin, Xbase, Xout, Rout, cfl, f);
+    } else if (mode == kModeStage2) {
+      auto k = hll ? (v3 ? k_stage_f32<NS, true, kModeStage2, kRiemannHll, 3> : k_stage_f32<NS, true, kModeStage2, kRiemannHll>)
+                   : (v3 ? k_stage_f32<NS, true, kModeStage2, kRiemannRoe, 3> : k_stage_f32<NS, true, kModeStage2, kRiemannRoe>);
+      launch_k(true, k, nb, kBlock, 0, st, m, s, Xin, Xbase, Xout, Rout, cfl, f);
+    }
   } else if (mode == kModeStage1) {
     launch_k(true, k_stage_f32<NS, false, kModeStage1>, nb, kBlock, 0, st, m, s, Xin, Xbase, Xout, Rout, cfl, f);
   } else if (mode == kModeStage2) {
@@ -1097,17 +1103,24 @@ void launch_pipe(const DevMesh& m, const DevScalars& s, StateF32 Xin, StateF32 X
 }
 
 
-template <int NS, int MODE, bool FUSED, int RS>
-void launch_face_rs(const DevMesh& m, const DevScalars& s, StateF32 Xin, StateF32 Xbase, StateF32 Xout, int cfl,
-                    const StageFuse& fu, cudaStream_t st) {
+template <int NS, int MODE, bool FUSED, int RS, int MINB>
+void launch_face_minb(const DevMesh& m, const DevScalars& s, StateF32 Xin, StateF32 Xbase, StateF32 Xout, int cfl,
+                      const StageFuse& fu, cudaStream_t st) {
   static const bool attr = [] {   // more than 48 KB of dynamic shared memory: opt in once, for the largest tables
-    cudaFuncSetAttribute(k_stage_face_f32<NS, MODE, FUSED, RS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaFuncSetAttribute(k_stage_face_f32<NS, MODE, FUSED, RS, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)FaceSmem::bytes(kFaceMaxPerTile, MODE));
     return true;
   }();
   (void)attr;
-  launch_k(true, k_stage_face_f32<NS, MODE, FUSED, RS>, blocks_for(m.n), kBlock, FaceSmem::bytes(m.faceMax, MODE), st,
-           m, s, Xin, Xbase, Xout, cfl, fu);
+  launch_k(true, k_stage_face_f32<NS, MODE, FUSED, RS, MINB>, blocks_for(m.n), kBlock,
+           FaceSmem::bytes(m.faceMax, MODE), st, m, s, Xin, Xbase, Xout, cfl, fu);
+}
+// The register budget by variant: 4 blocks per SM (64 registers), or 3 (80).
+template <int NS, int MODE, bool FUSED, int RS>
+void launch_face_rs(const DevMesh& m, const DevScalars& s, StateF32 Xin, StateF32 Xbase, StateF32 Xout, int cfl,
+                    const StageFuse& fu, cudaStream_t st) {
+  if (m.stageVariant == 1) launch_face_minb<NS, MODE, FUSED, RS, 3>(m, s, Xin, Xbase, Xout, cfl, fu, st);
+  else launch_face_minb<NS, MODE, FUSED, RS, 4>(m, s, Xin, Xbase, Xout, cfl, fu, st);
 }
 template <int NS, int MODE, bool FUSED>
 void launch_face(const DevMesh& m, const DevScalars& s, StateF32 Xin, StateF32 Xbase, StateF32 Xout, int cfl,
@@ -1138,6 +1151,13 @@ void launch_tma_mode(const DevMesh& m, const DevScalars& s, int mode, StateF32 X
 }  // namespace
 
 int stage_kernel_forced() { return forced_stage_kernel(); }
+int stage_variant_forced() {
+  static const int v = [] {
+    const char* e = std::getenv("HG_STAGE_VARIANT");
+    return (e && (e[0] == '0' || e[0] == '1') && e[1] == 0) ? e[0] - '0' : -1;
+  }();
+  return v;
+}
 
 bool stage_kernel_usable(const DevMesh& m, int k, int mode, StateF32 Xin, StateF32 Xbase) {
   auto a16 = [](const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; };
@@ -1178,10 +1198,12 @@ void launch_stage_f32(const DevMesh& m, const DevScalars& s, int mode, StateF32 
   else launch_stage_ns<8, false>(m, s, mode, Xin, Xbase, Xout, Rout, f, nf, st);
 }
 
-void launch_stage_f32_fused(const DevMesh& m, const DevScalars& s, int mode, StateF32 Xin, StateF32 Xbase,
+void launch_stage_f32_fused(const DevMesh& m0, const DevScalars& s, int mode, StateF32 Xin, StateF32 Xbase,
                             StateF32 Xout, const StageFuse& fu, cudaStream_t st) {
   const int f = (!fu.record && fu.cflMode) ? 1 : 0;   // stage 2 publishes the next CFL minimum
   const int forced = forced_stage_kernel();
+  DevMesh m = m0;
+  if (stage_variant_forced() >= 0) m.stageVariant = stage_variant_forced();
   const int k = forced >= 0 ? forced : m.stageKernel;
   if (k == kStageFace && stage_kernel_usable(m, k, mode, Xin, Xbase)) {
     if (m.nslot <= 3) launch_face_mode<3>(m, s, mode, Xin, Xbase, Xout, f, fu, st);

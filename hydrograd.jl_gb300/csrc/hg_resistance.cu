@@ -22,6 +22,7 @@
 #include "hg_device.cuh"
 #include "hg_f32.cuh"
 #include "hg_reduce.cuh"
+#include "hg_resfn.cuh"
 #include "hg_state.hpp"
 
 namespace hg {
@@ -32,31 +33,6 @@ using namespace devred;
 namespace {
 
 constexpr int kBlock = 256;
-
-template <class S>
-struct RM;
-template <>
-struct RM<double> {
-  static __device__ double exp(double x) { return ::exp(x); }
-  static __device__ double tanh(double x) { return ::tanh(x); }
-  static __device__ double log10(double x) { return ::log10(x); }
-  static __device__ double log1p(double x) { return ::log1p(x); }
-  static __device__ double pow(double x, double y) { return ::pow(x, y); }
-  static __device__ double sqrt(double x) { return ::sqrt(x); }
-  static __device__ double abs(double x) { return ::fabs(x); }
-  static __device__ double w(const ResDev& r, int i) { return r.w[i]; }
-};
-template <>
-struct RM<float> {
-  static __device__ float exp(float x) { return ::expf(x); }
-  static __device__ float tanh(float x) { return ::tanhf(x); }
-  static __device__ float log10(float x) { return ::log10f(x); }
-  static __device__ float log1p(float x) { return ::log1pf(x); }
-  static __device__ float pow(float x, float y) { return ::powf(x, y); }
-  static __device__ float sqrt(float x) { return ::sqrtf(x); }
-  static __device__ float abs(float x) { return ::fabsf(x); }
-  static __device__ float w(const ResDev& r, int i) { return r.wf[i]; }
-};
 
 // NNlib's sigmoid (exp of -|x|, no overflow).
 template <class S>
@@ -73,29 +49,6 @@ __device__ __forceinline__ S activation(int a, S x) {
     case 2: return sigmoid_nn(x);
     case 3: return RM<S>::tanh(x);
     default: return RM<S>::log1p(RM<S>::exp(-RM<S>::abs(x))) + (x > S(0) ? x : S(0));   // softplus
-  }
-}
-
-// Manning's n functions (process_ManningN_2D.jl:149-213).
-template <class S>
-__device__ S manning_fn(const ResDev& r, S h, S umag, S ks) {
-  const S nl = S(r.p[0]), nu = S(r.p[1]), k = S(r.p[2]);
-  switch (r.kind) {
-    case kResPowerLaw: return nl + (nu - nl) * RM<S>::pow(h + S(2.220446049250313e-16), -k);
-    case kResSigmoid: return nl + (nu - nl) / (S(1) + RM<S>::exp(k * (h - S(r.p[3]))));
-    case kResInverse: return nl + (nu - nl) / (S(1) + k * h);
-    default: {   // h_Umag_ks: Cheng (2008) friction factor, Eq. 17
-      const S Re = umag * h / S(1.0e-6);
-      const S h_ks = h / ks;
-      const S alpha = S(1) / (S(1) + RM<S>::pow(Re / S(850.0), S(9.0)));
-      const S rb = Re / (h_ks * S(160.0));
-      const S beta = S(1) / (S(1) + rb * rb);
-      const S part1 = RM<S>::pow(Re / S(24.0), alpha);
-      const S part2 = RM<S>::pow(S(1.8) * RM<S>::log10(Re / S(2.1)), S(2) * (S(1) - alpha) * beta);
-      const S part3 = RM<S>::pow(S(2) * RM<S>::log10(S(11.8) * h_ks), S(2) * (S(1) - alpha) * (S(1) - beta));
-      const S f = S(1) / (part1 * part2 * part3);
-      return RM<S>::sqrt(f / S(8.0)) * RM<S>::pow(h, S(1.0 / 6.0)) / RM<S>::sqrt(S(9.81));
-    }
   }
 }
 

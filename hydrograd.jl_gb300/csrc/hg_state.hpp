@@ -75,8 +75,11 @@ struct DevMesh {
   const uint2* FR = nullptr;
   int32_t faceMax = 0;               // most faces in one tile
   // Kernel of the fused FP32 stages (hg_autotune): kStageGather, kStagePipe,
-  // kStageTma (the same results) or kStageFace (each wet-wet face once).
+  // kStageTma (the same results) or kStageFace (each wet-wet face once); and
+  // its shape: 0 the register budget of 4 resident blocks per SM, 1 of 3
+  // (gather and face kernels; the arithmetic does not depend on it).
   int32_t stageKernel = 0;
+  int32_t stageVariant = 0;
   const int32_t* bfInfo = nullptr;   // [nbf] type | group << 2
   const double* bfLp23 = nullptr;    // [nbf] L^(2/3) (inlet-Q faces)
   const double* bfLp53 = nullptr;    // [nbf] L^(5/3) (inlet-Q faces)
@@ -217,8 +220,10 @@ enum StageKernel : int32_t { kStageGather = 0, kStagePipe = 1, kStageTma = 2, kS
 constexpr int32_t kFaceBoundary = INT32_MIN;
 constexpr int kFaceMaxPerTile = 1024;
 int stage_blocks_f32(const DevMesh& m);
-// The kernel HG_STAGE_KERNEL forces (gather / pipe / tma), else -1.
+// The kernel HG_STAGE_KERNEL forces (gather / pipe / tma / face), else -1;
+// the shape HG_STAGE_VARIANT forces (0 / 1), else -1.
 int stage_kernel_forced();
+int stage_variant_forced();
 // Whether kernel k can run the fused stages of this mesh and these states.
 bool stage_kernel_usable(const DevMesh& m, int k, int mode, StateF32 Xin, StateF32 Xbase);
 // Clear CFL-minimum buffer `parity` (fused stepping keeps two).

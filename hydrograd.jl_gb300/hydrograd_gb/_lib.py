@@ -99,6 +99,8 @@ SIGNATURES = {
                          _dp, _dp, _dp, _dp],
     "hg_launch_count": [_vp, ctypes.POINTER(ctypes.c_int64)],
     "hg_autotune": [_vp, ctypes.c_int32, _ip],
+    "hg_autotune_info": [_vp, _ip, _ip, _ip],
+    "hg_set_stage_family": [_vp, ctypes.c_int32],
     "hg_set_adjoint_tape": [_vp, ctypes.c_int64],
     "hg_set_riemann_solver": [_vp, ctypes.c_int32],
     "hg_set_dt_min": [_vp, ctypes.c_double],

@@ -280,12 +280,23 @@ class SWE2D:
         return int(c.value)
 
     def autotune(self, reps=3):
-        """hg_autotune: time the FP32C stage kernels on the resident state and
-        keep the fastest; returns the choice (0 gather, 1 pipe, 2 tma).
-        reps=0 only reports the current choice."""
+        """hg_autotune: time the FP32C stage kernels of the context's family on
+        the resident state and keep (and cache) the fastest; returns the kernel
+        (0 gather, 1 pipe, 2 tma, 3 face).  reps=0 only reports the current one."""
         k = np.zeros(1, np.int32)
         self._chk(lib().hg_autotune(self.h, int(reps), _i(k)))
         return int(k[0])
+
+    def autotune_info(self):
+        """(kernel, variant, source) of the stage-kernel choice (hg_autotune_info;
+        source 0 default, 1 timed, 2 cache file, 3 forced)."""
+        v = np.zeros(3, np.int32)
+        self._chk(lib().hg_autotune_info(self.h, _i(v[0:1]), _i(v[1:2]), _i(v[2:3])))
+        return tuple(int(x) for x in v)
+
+    def set_stage_family(self, family):
+        """hg_set_stage_family: "gather" (gather / pipe / tma) or "face"."""
+        self._chk(lib().hg_set_stage_family(self.h, {"gather": 0, "face": 1}[family]))
 
     def final_state_vjp(self, Q0, nsteps, dt, lam, ckpt_every=50, want=("manning", "zb", "inletq")):
         """hg_final_vjp: gradients of lam . Q_K (Q_K the state after nsteps

@@ -352,15 +352,37 @@ int hg_final_vjp(hg_ctx* ctx, const double* Q0, int32_t nsteps, double dt, int32
                  double* g_manning_cells, double* g_zb, double* g_inletq, double* Q_final);
 
 /* ---- tuning ------------------------------------------------------------------ */
-/* Choose the kernel of the FP32-compensated fused stages for this mesh: each
- * kernel that can run it (0 gather: one block per 256-cell tile; 1 pipe:
- * persistent, the next tile and its halo prefetched by asynchronous copies;
- * 2 tma: persistent, bulk-copy prefetch of the next tile) is timed on the
- * resident state, reps times, and the fastest is kept.  All compute the same
- * results.  The first RK2 steps of a context run it once by themselves;
- * HG_STAGE_KERNEL=gather|pipe|tma in the environment forces a kernel.
- * kernel (may be NULL) receives the choice; reps = 0 only reports it. */
+/* The autotuner of the FP32-compensated fused stages (no counterpart in the
+ * reference, which has no GPU kernels).  It chooses among kernels and shapes
+ * that compute bit-identical results, in one of two families:
+ *   family 0: kernel 0 gather (one block per 256-cell tile) with the register
+ *             budget of 4 or 3 resident blocks per SM (variant 0 / 1);
+ *             kernel 1 pipe (persistent, the next tile and its halo
+ *             prefetched by asynchronous copies); kernel 2 tma (persistent,
+ *             bulk-copy prefetch of the next tile);
+ *   family 1: kernel 3 face (each wet-wet face evaluated once for both of its
+ *             cells), variant 0 / 1 as above, where the mesh has the face
+ *             tables (degree <= 4).  Family 0 is the default.
+ * The two families round differently (the face kernel forms each face's flux
+ * once); a context's family is fixed (hg_set_stage_family, HG_STAGE_FAMILY=
+ * gather|face), never chosen by timing.  Each usable candidate is timed on the
+ * resident state, reps times, and the fastest is kept and stored in a cache
+ * file (HG_AUTOTUNE_CACHE, else $XDG_CACHE_HOME/hydrograd_gb/autotune.json,
+ * else ~/.cache/hydrograd_gb/autotune.json; HG_AUTOTUNE_CACHE= (empty)
+ * disables it) under a key of the GPU, the mesh's face tables, the Riemann
+ * solver and the family.  The first RK2 steps of a context take the cached
+ * choice, or tune once by themselves and store it.  HG_STAGE_KERNEL=
+ * gather|pipe|tma|face and HG_STAGE_VARIANT=0|1 in the environment force a
+ * candidate.  kernel (may be NULL) receives the kernel; reps = 0 only
+ * reports it. */
 int hg_autotune(hg_ctx* ctx, int32_t reps, int32_t* kernel);
+/* The current choice: kernel, variant, and where it came from (source: 0 the
+ * default, 1 timed, 2 the cache file, 3 forced by the environment).  Any
+ * output may be NULL. */
+int hg_autotune_info(const hg_ctx* ctx, int32_t* kernel, int32_t* variant, int32_t* source);
+/* The autotuner's family: 0 gather / pipe / tma, 1 face (HG_ERR_UNSUPPORTED
+ * when the mesh has no face tables).  The next RK2 steps tune within it. */
+int hg_set_stage_family(hg_ctx* ctx, int32_t family);
 
 /* ---- measurement support ---------------------------------------------------- */
 /* Number of kernel launches this context has enqueued (graph replays count their kernels). */
