@@ -52,6 +52,7 @@ struct AdjointBuffers {
   double* lam = nullptr;          // [3n] final-state cotangent (hg_final_vjp), device order
   double* finScratch = nullptr;   // dWse [n], parts [2], partials [2 kFinalLossBlocks]
   unsigned int* finTicket = nullptr;
+  double* resGrad = nullptr;      // [4] the parameter gradient of a state-dependent n
   ~AdjointBuffers() {
     for (void* p : fixed) cudaFree(p);
     cudaFree(ckpt);
@@ -261,6 +262,15 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
   a.wantN = gManning ? 1 : 0;   // the FP32C VJP skips the accumulators of gradients not asked for
   a.wantZb = gZb ? 1 : 0;
   const int N = c->n;
+  // A state-dependent Manning n (the n functions): dL/dn is chained into the
+  // state and the function's parameters instead of accumulated per cell.
+  a.resChain = (c->dm.res.kind >= kResPowerLaw && c->dm.res.kind <= kResHUmagKs) ? 1 : 0;
+  if (!a.resChain) std::fill(c->resGrad, c->resGrad + 4, 0.0);
+  if (a.resChain && !a.gResP) {
+    ADJ_CUDA(c, falloc(b, &a.gResP, (size_t)4 * N));
+    if (c->precision == HG_FP32C) ADJ_CUDA(c, falloc(b, &a.accRes, (size_t)4 * N));
+    ADJ_CUDA(c, falloc(b, &b->resGrad, 4));
+  }
   const size_t n3 = (size_t)3 * N;
   const bool f64 = c->precision == HG_FP64;
   if (C <= 0) C = K;
@@ -345,6 +355,10 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
   ADJ_CUDA(c, cudaMemsetAsync(a.gS0y, 0, N * sizeof(double), st));
   ADJ_CUDA(c, cudaMemsetAsync(a.gZb, 0, N * sizeof(double), st));
   if (a.accF) ADJ_CUDA(c, cudaMemsetAsync(a.accF, 0, (size_t)4 * N * sizeof(float2), st));
+  if (a.resChain) {
+    ADJ_CUDA(c, cudaMemsetAsync(a.gResP, 0, (size_t)4 * N * sizeof(double), st));
+    if (a.accRes) ADJ_CUDA(c, cudaMemsetAsync(a.accRes, 0, (size_t)4 * N * sizeof(float2), st));
+  }
   ADJ_CUDA(c, cudaMemsetAsync(a.gQ, 0, std::max(c->dm.nInlet, 1) * sizeof(double), st));
   ADJ_CUDA(c, cudaMemsetAsync(a.loss, 0, sizeof(double), st));
   ADJ_CUDA(c, cudaMemsetAsync(c->ds.flags, 0, sizeof(int32_t), st));
@@ -489,7 +503,8 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
     // instead of recomputed: T0[i] of Q0s[i] (i = 0..C) and T1[i] of Q1s[i].
     // When the inlet groups fit the fused stage kernels, those kernels produce
     // the totals of their output states; otherwise k_inlet_total does.
-    const bool fz = dm.nInlet <= kMaxFusedInlets;
+    // (not with a state-dependent n: the fused stages form the totals with the resident n)
+    const bool fz = dm.nInlet <= kMaxFusedInlets && dm.res.kind == kResConstant;
     const size_t stride = (size_t)std::max(dm.nInlet, kMaxFusedInlets);
     const size_t totNeed = (size_t)(2 * C + 1) * stride;
     if (totNeed > b->segTotCap) {
@@ -589,8 +604,10 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
         m1.totalA = T1 + i * stride;
         m0.totalA = T0 + i * stride;
         hydro((s + 1) * dt);
+        if (a.resChain) c->launches += launch_resistance_f32(dm, q1, st);   // n of the VJP's state
         c->launches += launch_vjp_f32(m1, a, q1, mu2, nullptr, mu1, 0.5f, 0.0f, 0.5 * dt, st);
         hydro(s * dt);
+        if (a.resChain) c->launches += launch_resistance_f32(dm, q0, st);
         // with the probe terms of q0, the state after step s - 1, in the same launches
         ProbeJob pj;
         if (s >= 1 && P > 0) {
@@ -611,6 +628,11 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
   if (gZb) {
     launch_zb_gradient(dm, a, b->gzb, st);
     c->launches += 2;
+  }
+  if (a.resChain) {
+    launch_res_param_sum(a, N, b->resGrad, st);
+    c->launches += 1;
+    ADJ_CUDA(c, cudaMemcpyAsync(c->resGrad, b->resGrad, 4 * sizeof(double), cudaMemcpyDeviceToHost, st));
   }
   ADJ_CUDA(c, cudaGetLastError());
   // Results, put in the caller's cell order on the device and copied out

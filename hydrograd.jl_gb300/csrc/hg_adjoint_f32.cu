@@ -20,6 +20,7 @@
 #include "hg_f32.cuh"
 #include "hg_pdl.cuh"
 #include "hg_reduce.cuh"
+#include "hg_resfn.cuh"
 #include "hg_wet_vjp.cuh"
 
 namespace hg {
@@ -168,7 +169,19 @@ __device__ __forceinline__ void vjp_cell(const DevMesh& m, const AdjDev& a, int 
       acc_add(&a.accF[(size_t)2 * n + j], beta, mj2 * m.gf * L.s.xi);
     }
   }
-  if (a.wantN && gn != 0.0f) acc_add(&a.accF[j], beta, gn);
+  if (a.resChain) {   // n = f(state): dL/dn into the state and the function's parameters
+    if (gn != 0.0f) {
+      const ResJac<float> J =
+          manning_jac<float>(m.res, L.s.h, L.s.hu, L.s.hv, m.res.ks ? (float)m.res.ks[j] : 0.0f, L.s.dry);
+      g0 += gn * J.dh;
+      g1 += gn * J.dqx;
+      g2 += gn * J.dqy;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) acc_add(&a.accRes[(size_t)k * n + j], beta, gn * J.dp[k]);
+    }
+  } else if (a.wantN && gn != 0.0f) {
+    acc_add(&a.accF[j], beta, gn);
+  }
   const float mask = L.s.dry ? 0.0f : 1.0f;
   const float e0 = src.extra_own(0), e1 = src.extra_own(1), e2 = src.extra_own(2);
   out[j] = mask * (cSelf * mj0 + cExtra * e0 + beta * g0);
@@ -479,9 +492,12 @@ __global__ void __launch_bounds__(kCombineBlock) k_vjp_combine_f32(DevMesh m, Ad
   const float4 cp = m.CP[j];
   const SideF32 L = make_side_f32(Q.x[j], cp, m.hsmf, m.hsmLo);
   const float* g = a.bndG + (size_t)5 * i;
-  if (a.wantN && g[3] != 0.0f) acc_add(&a.accF[j], beta, g[3]);
+  if (a.wantN && !a.resChain && g[3] != 0.0f) acc_add(&a.accF[j], beta, g[3]);
   if (a.wantZb && g[4] != 0.0f) acc_add(&a.accF[(size_t)3 * n + j], beta, g[4]);
   if (L.s.dry) return;
+  // n = f(state): the boundary faces' and the inlet conveyance's dL/dn of the
+  // cell into its state and the function's parameters
+  double gnRes = a.resChain ? (double)g[3] : 0.0;
   out[j] += beta * g[0];
   out[n + j] += beta * g[1];
   out[2 * n + j] += beta * g[2];
@@ -489,7 +505,17 @@ __global__ void __launch_bounds__(kCombineBlock) k_vjp_combine_f32(DevMesh m, Ad
     const double gTA = a.grpTA[a.bndInGrp[p]];
     const double coef = a.bndInCoef[p], nm = cp.w;
     out[j] += (float)(betaD * gTA * coef / nm);
-    if (a.wantN) a.gN[j] += betaD * gTA * (-coef * (double)L.s.h / (nm * nm));
+    const double gnc = gTA * (-coef * (double)L.s.h / (nm * nm));
+    if (a.resChain) gnRes += gnc;
+    else if (a.wantN) a.gN[j] += betaD * gnc;
+  }
+  if (a.resChain && gnRes != 0.0) {
+    const ResJac<double> J = manning_jac<double>(m.res, (double)L.s.h, (double)L.s.hu, (double)L.s.hv,
+                                                 m.res.ks ? m.res.ks[j] : 0.0, false);
+    out[j] += (float)(betaD * gnRes * J.dh);
+    out[n + j] += (float)(betaD * gnRes * J.dqx);
+    out[2 * n + j] += (float)(betaD * gnRes * J.dqy);
+    for (int k = 0; k < 4; ++k) a.gResP[(size_t)k * n + j] += betaD * gnRes * J.dp[k];
   }
   if (pj.np > 0 && a.bndProbe[i] >= 0) probe_seed(m, Q, out, pj.pc, pj.obs, pj.scale, a.bndProbe[i]);
 }
@@ -502,6 +528,13 @@ __global__ void k_fold_accumulators_f32(DevMesh m, AdjDev a) {
   for (int k = 0; k < 4; ++k) {
     const float2 v = a.accF[(size_t)k * m.n + j];
     dst[k][j] += (double)v.x + (double)v.y;
+  }
+  if (a.resChain) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const float2 v = a.accRes[(size_t)k * m.n + j];
+      a.gResP[(size_t)k * m.n + j] += (double)v.x + (double)v.y;
+    }
   }
 }
 

@@ -19,6 +19,7 @@
 #include "hg_device.cuh"
 #include "hg_dual.cuh"
 #include "hg_reduce.cuh"
+#include "hg_resfn.cuh"
 #include "hg_wet_vjp.cuh"
 
 namespace hg {
@@ -152,7 +153,18 @@ __global__ void __launch_bounds__(kBlock) k_vjp_f64(DevMesh m, AdjDev a, const d
     a.gS0x[j] += beta * mj1 * m.g * L.xi;
     a.gS0y[j] += beta * mj2 * m.g * L.xi;
   }
-  a.gN[j] += beta * gn;
+  if (a.resChain) {   // n = f(state): dL/dn into the state and the function's parameters
+    if (gn != 0.0) {
+      const ResJac<double> J = manning_jac<double>(m.res, L.h, L.hu, L.hv, m.res.ks ? m.res.ks[j] : 0.0, L.dry);
+      g0 += gn * J.dh;
+      g1 += gn * J.dqx;
+      g2 += gn * J.dqy;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) a.gResP[(size_t)k * n + j] += beta * gn * J.dp[k];
+    }
+  } else {
+    a.gN[j] += beta * gn;
+  }
   a.gZb[j] += beta * gzb;
   const double mask = L.dry ? 0.0 : 1.0;   // the stage clamp zeroes the derivative of a dry cell
   const double e0 = extra ? extra[j] : 0.0, e1 = extra ? extra[n + j] : 0.0, e2 = extra ? extra[2 * n + j] : 0.0;
@@ -190,7 +202,17 @@ __global__ void __launch_bounds__(256) k_inlet_adjoint_f64(DevMesh m, AdjDev a, 
     if (L.dry) continue;                      // wet_i = 0, and the clamp zeroes a dry cell's derivative
     const double coef = a.inletUCoef[i], n = m.man[c];
     out[c] += beta * gTA * coef / n;          // d total_A / d xi_c (h = xi + hstill)
-    a.gN[c] += beta * gTA * (-coef * L.h / (n * n));
+    const double gn = gTA * (-coef * L.h / (n * n));
+    if (a.resChain && gn != 0.0) {   // n = f(state): into the state and the function's parameters
+      const ResJac<double> J = manning_jac<double>(m.res, L.h, L.hu, L.hv, m.res.ks ? m.res.ks[c] : 0.0, false);
+      const int N = m.n;
+      out[c] += beta * gn * J.dh;
+      out[N + c] += beta * gn * J.dqx;
+      out[2 * N + c] += beta * gn * J.dqy;
+      for (int k = 0; k < 4; ++k) a.gResP[(size_t)k * N + c] += beta * gn * J.dp[k];
+    } else if (!a.resChain) {
+      a.gN[c] += beta * gn;
+    }
   }
 }
 
@@ -271,6 +293,22 @@ void launch_probe_adjoint_f64(const DevMesh& m, const double* Q, double* mu, con
                               const double* obs, int32_t nprobe, double scale, cudaStream_t st) {
   if (nprobe > 0) k_probe_adjoint_f64<<<1, 32, 0, st>>>(m, Q, mu, probes, obs, nprobe, scale);
 }
+namespace {
+// The gradient w.r.t. the parameters of a state-dependent n: the per-cell
+// sums added over all cells, one block per parameter in a fixed order.
+__global__ void __launch_bounds__(256) k_res_param_sum(AdjDev a, int n, double* out4) {
+  const int k = blockIdx.x;
+  double s = 0.0;
+  for (int j = threadIdx.x; j < n; j += blockDim.x) s += a.gResP[(size_t)k * n + j];
+  const double t = block_sum(s);
+  if (threadIdx.x == 0) out4[k] = t;
+}
+}  // namespace
+
+void launch_res_param_sum(const AdjDev& a, int n, double* out4, cudaStream_t st) {
+  k_res_param_sum<<<4, 256, 0, st>>>(a, n, out4);
+}
+
 void launch_zb_gradient(const DevMesh& m, const AdjDev& a, double* gzb, cudaStream_t st) {
   k_zb_scale<<<(m.n + 255) / 256, 256, 0, st>>>(m, a);
   k_zb_gradient<<<(m.n + 255) / 256, 256, 0, st>>>(m, a, gzb);

@@ -46,6 +46,16 @@ struct AdjDev {
   // The gradients the caller asked for: the FP32C VJP accumulates the n or
   // the bed (S0, exit-H) terms only when wanted.
   int32_t wantN = 1, wantZb = 1;
+  // A state-dependent Manning n (hg_set_manning_function: power law, sigmoid,
+  // inverse, h_Umag_ks): n is then not a parameter but a function of each RHS
+  // evaluation's input state, so each stage's dL/dn of a cell is taken back
+  // into the cell's state cotangent through dn/d(h, qx, qy), and into the
+  // function's parameters {n_lower, n_upper, k, h_mid} (per-cell FP64 sums
+  // gResP [4][n]; the FP32C VJP adds into compensated pairs accRes, folded in
+  // at the end).
+  int32_t resChain = 0;
+  double* gResP = nullptr;
+  float2* accRes = nullptr;
 };
 
 // out_j = M(Q_j) (cSelf mu_j + cExtra extra_j + beta (J(Q)^T mu)_j), parameter
@@ -115,5 +125,7 @@ void launch_final_loss_f32(const DevMesh& m, const FinalLossDev& f, StateF32 Q, 
 void launch_fold_accumulators_f32(const DevMesh& m, const AdjDev& a, cudaStream_t st);
 // dL/dzb = S0 transpose (Green-Gauss of face averages) applied to dL/dS0, plus the direct term.
 void launch_zb_gradient(const DevMesh& m, const AdjDev& a, double* gzb, cudaStream_t st);
+// out4[k] = sum over cells of gResP[k] (a state-dependent n's parameter gradient).
+void launch_res_param_sum(const AdjDev& a, int n, double* out4, cudaStream_t st);
 
 }  // namespace hg

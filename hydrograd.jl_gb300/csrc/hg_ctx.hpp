@@ -70,6 +70,9 @@ struct hg_ctx {
   int32_t stageFamily = 0;          // candidates of the autotuner: 0 gather, pipe, tma; 1 face (see autotune_stage)
   int32_t tuneSource = 0;           // where the choice came from: 0 default, 1 timed, 2 cache, 3 forced
   uint64_t meshSig = 0;             // hash of the device-order face tables (autotune cache key)
+  // The last gradient call's gradient w.r.t. the parameters {n_lower, n_upper,
+  // k, h_mid} of a state-dependent n (hg_resistance_grad).
+  double resGrad[4] = {0.0, 0.0, 0.0, 0.0};
   int64_t launches = 0;
   hg::AdjointBuffers* adj = nullptr;
   // Adjoint stage-state tape (hg_set_adjoint_tape): -1 automatic budget, 0 the

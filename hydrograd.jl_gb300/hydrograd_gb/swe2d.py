@@ -166,6 +166,13 @@ class SWE2D:
         self._res_ks = None if ks is None else np.ascontiguousarray(ks, dtype=np.float64)
         self._chk(lib().hg_set_manning_function(self.h, k, _d(p) if len(p) else None, len(p), _d(self._res_ks)))
 
+    def resistance_grad(self):
+        """dL/d{n_lower, n_upper, k, h_mid} of the state-dependent n function
+        from the last gradient call (hg_resistance_grad)."""
+        g = np.zeros(4)
+        self._chk(lib().hg_resistance_grad(self.h, _d(g)))
+        return g
+
     def set_ude(self, choice, hidden, activations, params, output_bounds, h_bounds, u_bounds=(0.0, 1.0),
                 ks_bounds=(0.0, 1.0), ks=None, layernorm_over_batch=True):
         """A UDE closure in the RHS (process_ManningN_2D.jl:216-273,

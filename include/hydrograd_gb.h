@@ -215,8 +215,13 @@ int hg_get_bed(hg_ctx* ctx, double* zb_cells, double* S0, double* manning_cells,
  *   HG_RES_H_UMAG_KS  n from Cheng's (2008) friction factor of Re = Umag h / 1e-6 and h / ks
  * params = {n_lower, n_upper, k[, h_mid]}; ks_cells [n] (caller order) for
  * HG_RES_H_UMAG_KS.  HG_RES_CONSTANT returns to the cells' n
- * (hg_set_manning_zones / _cells).  Gradients (hg_loss_and_grad) are not
- * available while a state-dependent resistance is set: HG_ERR_UNSUPPORTED. */
+ * (hg_set_manning_zones / _cells).  Gradients (hg_loss_and_grad,
+ * hg_final_loss_and_grad, hg_final_vjp) run through these functions: each
+ * RHS evaluation's dL/dn is taken back into its state through
+ * dn/d(h, qx, qy), so the zb and inlet-Q gradients include it, and into the
+ * function's parameters (hg_resistance_grad); the per-cell n gradient is then
+ * zero, n not being a parameter.  Gradients with a UDE closure (kinds 5-7)
+ * are not available: HG_ERR_UNSUPPORTED. */
 enum hg_resistance {
   HG_RES_CONSTANT = 0, HG_RES_POWER_LAW = 1, HG_RES_SIGMOID = 2, HG_RES_INVERSE = 3, HG_RES_H_UMAG_KS = 4,
   HG_RES_UDE_MANNING_H = 5,          /* UDE_choice "ManningN_h": n = NN(h) */
@@ -225,6 +230,11 @@ enum hg_resistance {
 };
 int hg_set_manning_function(hg_ctx* ctx, int32_t kind, const double* params, int32_t n_params,
                             const double* ks_cells);
+/* The gradient of the last hg_loss_and_grad / hg_final_loss_and_grad /
+ * hg_final_vjp call w.r.t. the parameters {n_lower, n_upper, k, h_mid} of the
+ * state-dependent n function (zeros when none was set; h_mid only for the
+ * sigmoid; HG_RES_H_UMAG_KS has none). */
+int hg_resistance_grad(const hg_ctx* ctx, double* g_params4);
 /* UDE closures (process_ManningN_2D.jl:216-273, process_FlowResistance_UDE.jl:3-45)
  * with the network of process_UDE.jl:3-56: per hidden layer Dense(in, w, act)
  * then LayerNorm(w); a linear Dense(w, 1); output lo + (hi - lo) sigmoid(y).

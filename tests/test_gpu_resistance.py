@@ -87,13 +87,17 @@ def test_ude_rhs_and_steps_match_oracle(choice, kind, in_dim, bounds, over_batch
     Qg, _ = ctx.integrate(Q0, 50, dt=dt)
     Qo = o.rk2(Q0, 50, dt=dt, nthreads=4)
     assert block_err(Qg, Qo, N) <= STATE_TOL[precision]
+    with pytest.raises(HgError) as e:   # no gradients through the network's weights
+        ctx.loss_and_grad(Q0, 5, dt, [0, 1], [0.1, 0.1])
+    assert e.value.code == 7
 
 
 @pytest.mark.parametrize("precision", ["fp64", "fp32c"])
 def test_graph_steps_and_constant_restore(precision):
     """Resident steps (hg_advance, captured in a graph) see the state-dependent
     n like hg_integrate does; switching back to "constant" restores the zones'
-    n; gradients refuse a state-dependent resistance."""
+    n; gradients run through the function (their values are checked in
+    tests/test_gpu_resistance_grad.py)."""
     d = load_fixture("fwd_bump_nh")
     ctx, o, N = setup_pair(d, precision)
     Q0 = initial_state(d, N)
@@ -105,9 +109,8 @@ def test_graph_steps_and_constant_restore(precision):
     ctx.advance(120, dt=dt, graph=True)
     Qa = ctx.download()
     assert block_err(Qa, Qi, N) <= (0.0 if precision == "fp64" else 1e-6)
-    with pytest.raises(HgError) as e:
-        ctx.loss_and_grad(Q0, 5, dt, [0, 1], [0.1, 0.1])
-    assert e.value.code == 7
+    r = ctx.loss_and_grad(Q0, 5, dt, [0, 1], [0.1, 0.1])
+    assert np.isfinite(r["loss"]) and np.isfinite(ctx.resistance_grad()).all()
     ctx.set_manning_function("constant")
     np.testing.assert_array_equal(ctx.rhs(Q0), rhs_const)
 
