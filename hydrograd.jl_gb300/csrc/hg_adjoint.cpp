@@ -53,6 +53,7 @@ struct AdjointBuffers {
   double* finScratch = nullptr;   // dWse [n], parts [2], partials [2 kFinalLossBlocks]
   unsigned int* finTicket = nullptr;
   double* resGrad = nullptr;      // [4] the parameter gradient of a state-dependent n
+  size_t udeCap = 0;              // parameters gTheta and udePart are sized for
   ~AdjointBuffers() {
     for (void* p : fixed) cudaFree(p);
     cudaFree(ckpt);
@@ -65,6 +66,8 @@ struct AdjointBuffers {
     cudaFree(lam);
     cudaFree(finScratch);
     cudaFree(finTicket);
+    cudaFree(dev.gTheta);
+    cudaFree(dev.udePart);
   }
 };
 
@@ -271,6 +274,29 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
     if (c->precision == HG_FP32C) ADJ_CUDA(c, falloc(b, &a.accRes, (size_t)4 * N));
     ADJ_CUDA(c, falloc(b, &b->resGrad, 4));
   }
+  // A UDE closure: the network's VJP after each stage's VJP.
+  const int rk = c->dm.res.kind;
+  a.udeChain = (rk == kResUdeManningH || rk == kResUdeManningHUmagKs) ? 1 : rk == kResUdeFlowResistance ? 2 : 0;
+  a.udeP = a.udeChain ? (int32_t)c->udeParams : 0;
+  c->udeGrad.assign((size_t)a.udeP, 0.0);
+  if (a.udeChain) {
+    if (!a.udeGn) {
+      ADJ_CUDA(c, falloc(b, &a.udeGn, N));
+      ADJ_CUDA(c, falloc(b, &a.udeS, 2 * kResMaxLayers));
+      ADJ_CUDA(c, falloc(b, &a.udeTicket, 1));
+      ADJ_CUDA(c, cudaMemset(a.udeTicket, 0, sizeof(unsigned int)));
+    }
+    const size_t need = (size_t)std::max(a.udeP, 2);
+    if (need > b->udeCap) {
+      cudaFree(a.gTheta);
+      cudaFree(a.udePart);
+      a.gTheta = nullptr;
+      a.udePart = nullptr;
+      ADJ_CUDA(c, cudaMalloc(&a.gTheta, need * sizeof(double)));
+      ADJ_CUDA(c, cudaMalloc(&a.udePart, need * kUdeGrid * sizeof(double)));
+      b->udeCap = need;
+    }
+  }
   const size_t n3 = (size_t)3 * N;
   const bool f64 = c->precision == HG_FP64;
   if (C <= 0) C = K;
@@ -355,6 +381,7 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
   ADJ_CUDA(c, cudaMemsetAsync(a.gS0y, 0, N * sizeof(double), st));
   ADJ_CUDA(c, cudaMemsetAsync(a.gZb, 0, N * sizeof(double), st));
   if (a.accF) ADJ_CUDA(c, cudaMemsetAsync(a.accF, 0, (size_t)4 * N * sizeof(float2), st));
+  if (a.udeChain) ADJ_CUDA(c, cudaMemsetAsync(a.gTheta, 0, (size_t)a.udeP * sizeof(double), st));
   if (a.resChain) {
     ADJ_CUDA(c, cudaMemsetAsync(a.gResP, 0, (size_t)4 * N * sizeof(double), st));
     if (a.accRes) ADJ_CUDA(c, cudaMemsetAsync(a.accRes, 0, (size_t)4 * N * sizeof(float2), st));
@@ -484,10 +511,12 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
         launch_inlet_total_f64(dm, ds, q1, st);
         launch_vjp_f64(dm, a, q1, b->mu2, nullptr, b->mu1, 0.5, 0.0, 0.5 * dt, st);
         launch_inlet_adjoint_f64(dm, a, q1, b->mu1, 0.5 * dt, st);
+        c->launches += launch_ude_vjp_f64(dm, a, q1, b->mu1, st);
         hydro(s * dt);
         launch_inlet_total_f64(dm, ds, q0, st);
         launch_vjp_f64(dm, a, q0, b->mu1, b->mu2, b->mu2, 1.0, 0.5, dt, st);
         launch_inlet_adjoint_f64(dm, a, q0, b->mu2, dt, st);
+        c->launches += launch_ude_vjp_f64(dm, a, q0, b->mu2, st);
         if (s >= 1) launch_probe_adjoint_f64(dm, q0, b->mu2, b->probes, b->obs + (size_t)(s - 1) * P, P, scale, st);
         c->launches += 2 + 2 * extraPerStep + (s >= 1 && P > 0 ? 1 : 0);
       }
@@ -604,10 +633,12 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
         m1.totalA = T1 + i * stride;
         m0.totalA = T0 + i * stride;
         hydro((s + 1) * dt);
-        if (a.resChain) c->launches += launch_resistance_f32(dm, q1, st);   // n of the VJP's state
+        const bool resState = a.resChain || a.udeChain;
+        if (resState) c->launches += launch_resistance_f32(dm, q1, st);   // n (or F) of the VJP's state
         c->launches += launch_vjp_f32(m1, a, q1, mu2, nullptr, mu1, 0.5f, 0.0f, 0.5 * dt, st);
+        c->launches += launch_ude_vjp_f32(dm, a, q1, mu1, st);
         hydro(s * dt);
-        if (a.resChain) c->launches += launch_resistance_f32(dm, q0, st);
+        if (resState) c->launches += launch_resistance_f32(dm, q0, st);
         // with the probe terms of q0, the state after step s - 1, in the same launches
         ProbeJob pj;
         if (s >= 1 && P > 0) {
@@ -618,6 +649,7 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
           pj.scale = scale;
         }
         c->launches += launch_vjp_f32(m0, a, q0, mu1, mu2, mu2, 1.0f, 0.5f, dt, st, &pj);
+        c->launches += launch_ude_vjp_f32(dm, a, q0, mu2, st);
       }
     }
   }
@@ -634,6 +666,9 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
     c->launches += 1;
     ADJ_CUDA(c, cudaMemcpyAsync(c->resGrad, b->resGrad, 4 * sizeof(double), cudaMemcpyDeviceToHost, st));
   }
+  if (a.udeChain && a.udeP > 0)
+    ADJ_CUDA(c, cudaMemcpyAsync(c->udeGrad.data(), a.gTheta, (size_t)a.udeP * sizeof(double), cudaMemcpyDeviceToHost,
+                                st));
   ADJ_CUDA(c, cudaGetLastError());
   // Results, put in the caller's cell order on the device and copied out
   // after the last kernel.

@@ -153,17 +153,28 @@ __device__ __forceinline__ void vjp_cell(const DevMesh& m, const AdjDev& a, int 
     g0 += gx;
     g1 += gu;
     g2 += gv;
+    // friction k q: Manning, or the flow-resistance closure's k = F / |q|
     const float hu = L.s.hu, hv = L.s.hv, man = cp.w;
     const float s2 = hu * hu + hv * hv + eps_c<float>();
-    const float hp = L.s.h + m.hsmf;
-    const float k = friction_coef(m.gf, m.kn2f, m.hsmf, man, L.s.h, hu, hv);
-    const float dkdh = -(7.0f / 3.0f) * k / hp;
-    const float dkdqx = k * hu / s2, dkdqy = k * hv / s2;
-    const float dkdn = 2.0f * k / man;
+    float k, dkdh, dkdqx, dkdqy;
+    if (m.res.kind == kResUdeFlowResistance) {
+      const float s = sqrtf(s2);
+      k = m.res.fresF[j] / s;
+      dkdh = 0.0f;
+      dkdqx = -k * hu / s2;
+      dkdqy = -k * hv / s2;
+      gn = -(mj1 * hu + mj2 * hv) / s;   // dL/dF (no term of the interior faces depends on n)
+    } else {
+      const float hp = L.s.h + m.hsmf;
+      k = friction_coef(m.gf, m.kn2f, m.hsmf, man, L.s.h, hu, hv);
+      dkdh = -(7.0f / 3.0f) * k / hp;
+      dkdqx = k * hu / s2;
+      dkdqy = k * hv / s2;
+      gn += -(mj1 * hu + mj2 * hv) * (2.0f * k / man);
+    }
     g0 += mj1 * (m.gf * cs.x - hu * dkdh) + mj2 * (m.gf * cs.y - hv * dkdh);
     g1 += mj1 * (-k - hu * dkdqx) + mj2 * (-hv * dkdqx);
     g2 += mj1 * (-hu * dkdqy) + mj2 * (-k - hv * dkdqy);
-    gn += -(mj1 * hu + mj2 * hv) * dkdn;
     if (a.wantZb) {
       acc_add(&a.accF[(size_t)n + j], beta, mj1 * m.gf * L.s.xi);
       acc_add(&a.accF[(size_t)2 * n + j], beta, mj2 * m.gf * L.s.xi);
@@ -179,6 +190,8 @@ __device__ __forceinline__ void vjp_cell(const DevMesh& m, const AdjDev& a, int 
 #pragma unroll
       for (int k = 0; k < 4; ++k) acc_add(&a.accRes[(size_t)k * n + j], beta, gn * J.dp[k]);
     }
+  } else if (a.udeChain) {   // the network's VJP takes it on (dL/dn, or dL/dF of the closure)
+    a.udeGn[j] = (double)(beta * gn);
   } else if (a.wantN && gn != 0.0f) {
     acc_add(&a.accF[j], beta, gn);
   }
@@ -492,12 +505,13 @@ __global__ void __launch_bounds__(kCombineBlock) k_vjp_combine_f32(DevMesh m, Ad
   const float4 cp = m.CP[j];
   const SideF32 L = make_side_f32(Q.x[j], cp, m.hsmf, m.hsmLo);
   const float* g = a.bndG + (size_t)5 * i;
-  if (a.wantN && !a.resChain && g[3] != 0.0f) acc_add(&a.accF[j], beta, g[3]);
+  const bool chainN = a.resChain || a.udeChain == 1;   // dL/dn of the cell goes to n's function
+  if (a.wantN && !chainN && g[3] != 0.0f) acc_add(&a.accF[j], beta, g[3]);
   if (a.wantZb && g[4] != 0.0f) acc_add(&a.accF[(size_t)3 * n + j], beta, g[4]);
   if (L.s.dry) return;
   // n = f(state): the boundary faces' and the inlet conveyance's dL/dn of the
   // cell into its state and the function's parameters
-  double gnRes = a.resChain ? (double)g[3] : 0.0;
+  double gnRes = chainN ? (double)g[3] : 0.0;
   out[j] += beta * g[0];
   out[n + j] += beta * g[1];
   out[2 * n + j] += beta * g[2];
@@ -506,9 +520,10 @@ __global__ void __launch_bounds__(kCombineBlock) k_vjp_combine_f32(DevMesh m, Ad
     const double coef = a.bndInCoef[p], nm = cp.w;
     out[j] += (float)(betaD * gTA * coef / nm);
     const double gnc = gTA * (-coef * (double)L.s.h / (nm * nm));
-    if (a.resChain) gnRes += gnc;
+    if (chainN) gnRes += gnc;
     else if (a.wantN) a.gN[j] += betaD * gnc;
   }
+  if (a.udeChain == 1 && gnRes != 0.0) a.udeGn[j] += betaD * gnRes;
   if (a.resChain && gnRes != 0.0) {
     const ResJac<double> J = manning_jac<double>(m.res, (double)L.s.h, (double)L.s.hu, (double)L.s.hv,
                                                  m.res.ks ? m.res.ks[j] : 0.0, false);

@@ -78,7 +78,7 @@ __global__ void __launch_bounds__(kBlock) k_vjp_f64(DevMesh m, AdjDev a, const d
   const Side<double> L = load_side(m, Q, j);
   const double Aj = m.area[j];
   const double mj0 = mu[j], mj1 = mu[n + j], mj2 = mu[2 * n + j];
-  double g0 = 0.0, g1 = 0.0, g2 = 0.0, gn = 0.0, gzb = 0.0;
+  double g0 = 0.0, g1 = 0.0, g2 = 0.0, gn = 0.0, gzb = 0.0, gF = 0.0;
   const Side<D3> L3 = seeded<D3>(L, -1);
   // Interior wet-wet faces in reverse mode (hg_wet_vjp.cuh); faces with a dry
   // side through 3-direction duals of the reference solver.
@@ -140,16 +140,27 @@ __global__ void __launch_bounds__(kBlock) k_vjp_f64(DevMesh m, AdjDev a, const d
   }
   // Sources (semi_discretize_swe_2D.jl:449-559), wet cells only.
   if (!L.dry) {
+    // friction k q: Manning k = g n^2 |q| / (kn^2 hp^(7/3)), or the
+    // flow-resistance closure's k = F / |q| (|q| smoothed as in the RHS)
     const double s = sqrt(L.hu * L.hu + L.hv * L.hv + eps_c<double>());
-    const double hp = L.h + m.hsm;
-    const double k = m.g * (m.man[j] * m.man[j]) / m.kn2 / (hp * hp * cbrt(hp)) * s;   // as friction_coef
-    const double dkdh = -(7.0 / 3.0) * k / hp;
-    const double dkdqx = k * L.hu / (s * s), dkdqy = k * L.hv / (s * s);
-    const double dkdn = 2.0 * k / m.man[j];
+    double k, dkdh, dkdqx, dkdqy;
+    if (m.res.kind == kResUdeFlowResistance) {
+      k = m.res.fres[j] / s;
+      dkdh = 0.0;
+      dkdqx = -k * L.hu / (s * s);
+      dkdqy = -k * L.hv / (s * s);
+      gF = -(mj1 * L.hu + mj2 * L.hv) / s;
+    } else {
+      const double hp = L.h + m.hsm;
+      k = m.g * (m.man[j] * m.man[j]) / m.kn2 / (hp * hp * cbrt(hp)) * s;   // as friction_coef
+      dkdh = -(7.0 / 3.0) * k / hp;
+      dkdqx = k * L.hu / (s * s);
+      dkdqy = k * L.hv / (s * s);
+      gn += -(mj1 * L.hu + mj2 * L.hv) * (2.0 * k / m.man[j]);
+    }
     g0 += mj1 * (m.g * m.s0x[j] - L.hu * dkdh) + mj2 * (m.g * m.s0y[j] - L.hv * dkdh);
     g1 += mj1 * (-k - L.hu * dkdqx) + mj2 * (-L.hv * dkdqx);
     g2 += mj1 * (-L.hu * dkdqy) + mj2 * (-k - L.hv * dkdqy);
-    gn += -(mj1 * L.hu + mj2 * L.hv) * dkdn;
     a.gS0x[j] += beta * mj1 * m.g * L.xi;
     a.gS0y[j] += beta * mj2 * m.g * L.xi;
   }
@@ -162,9 +173,12 @@ __global__ void __launch_bounds__(kBlock) k_vjp_f64(DevMesh m, AdjDev a, const d
 #pragma unroll
       for (int k = 0; k < 4; ++k) a.gResP[(size_t)k * n + j] += beta * gn * J.dp[k];
     }
+  } else if (a.udeChain == 1) {   // n from the network: the network's VJP takes it on
+    a.udeGn[j] = beta * gn;
   } else {
     a.gN[j] += beta * gn;
   }
+  if (a.udeChain == 2) a.udeGn[j] = beta * gF;   // F of the flow-resistance closure
   a.gZb[j] += beta * gzb;
   const double mask = L.dry ? 0.0 : 1.0;   // the stage clamp zeroes the derivative of a dry cell
   const double e0 = extra ? extra[j] : 0.0, e1 = extra ? extra[n + j] : 0.0, e2 = extra ? extra[2 * n + j] : 0.0;
@@ -210,6 +224,8 @@ __global__ void __launch_bounds__(256) k_inlet_adjoint_f64(DevMesh m, AdjDev a, 
       out[N + c] += beta * gn * J.dqx;
       out[2 * N + c] += beta * gn * J.dqy;
       for (int k = 0; k < 4; ++k) a.gResP[(size_t)k * N + c] += beta * gn * J.dp[k];
+    } else if (a.udeChain == 1) {
+      a.udeGn[c] += beta * gn;
     } else if (!a.resChain) {
       a.gN[c] += beta * gn;
     }

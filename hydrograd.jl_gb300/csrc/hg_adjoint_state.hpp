@@ -56,12 +56,38 @@ struct AdjDev {
   int32_t resChain = 0;
   double* gResP = nullptr;
   float2* accRes = nullptr;
+  // A UDE closure (hg_set_ude): udeChain = 1 when the network gives n
+  // (ManningN_h, ManningN_h_Umag_ks; every dL/dn of a cell goes to the
+  // network), 2 when it gives the friction magnitude F of the flow-resistance
+  // closure (the friction term's dL/dF goes to the network; the inlet
+  // conveyance's dL/dn stays a gradient of the cells' n).  The VJP kernels
+  // store each stage's per-cell cotangent beta dL/d(n or F) in udeGn; the
+  // network's VJP (launch_ude_vjp_*) then takes it back into the cells' state
+  // cotangents and into gTheta [udeP], the parameters in hg_set_ude's order.
+  int32_t udeChain = 0;
+  int32_t udeP = 0;
+  double* udeGn = nullptr;      // [n]
+  double* gTheta = nullptr;     // [udeP], accumulated over the stages
+  double* udePart = nullptr;    // [kUdeGrid * udeP] per-block partial sums
+  double* udeS = nullptr;       // [2 kResMaxLayers] LayerNorm backward sums of the stage
+  unsigned int* udeTicket = nullptr;
 };
+
+// Grid of the network VJP (one warp per block, a fixed grid so that the
+// per-block partial sums and their reduction have a fixed order).
+constexpr int kUdeGrid = 1216;
 
 // out_j = M(Q_j) (cSelf mu_j + cExtra extra_j + beta (J(Q)^T mu)_j), parameter
 // gradients += beta (dR/dtheta)^T mu; M(Q_j) = 1 when cell j of Q is wet.
 void launch_vjp_f64(const DevMesh& m, const AdjDev& a, const double* Q, const double* mu, const double* extra,
                     double* out, double cSelf, double cExtra, double beta, cudaStream_t st);
+// The UDE network's VJP of one stage (after that stage's VJP kernels):
+// out += M(Q) (dn/dQ)^T udeGn, gTheta += (dn/dtheta)^T udeGn, the LayerNorm
+// statistics taken over all cells when the network normalises over the batch.
+// Needs the network's forward statistics of Q (launch_resistance_* of Q just
+// before).  Returns the launches.
+int launch_ude_vjp_f64(const DevMesh& m, const AdjDev& a, const double* Q, double* out, cudaStream_t st);
+int launch_ude_vjp_f32(const DevMesh& m, const AdjDev& a, StateF32 Q, float* out, cudaStream_t st);
 // Inlet-Q conveyance terms of the same VJP (total_A couples all cells of a group).
 void launch_inlet_adjoint_f64(const DevMesh& m, const AdjDev& a, const double* Q, double* out, double beta,
                               cudaStream_t st);

@@ -480,6 +480,8 @@ int install_resistance(hg_ctx* c, ResDev r, const double* ksUser, const double* 
   r.fres = c->d_fres;
   r.fresF = c->d_fresF;
   c->dm.res = r;
+  c->udeParams = r.kind >= kResUdeManningH ? nParams : 0;
+  c->udeGrad.clear();
   c->graphValid = false;
   return HG_OK;
 }
@@ -837,6 +839,14 @@ int hg_resistance_grad(const hg_ctx* ctx, double* g_params) {
   return HG_OK;
 }
 
+int hg_ude_grad(const hg_ctx* ctx, double* g_params, int64_t n_params) {
+  if (!ctx || (!g_params && n_params > 0)) return fail(nullptr, HG_ERR_ARG, "hg_ude_grad: null argument");
+  if (n_params != (int64_t)ctx->udeParams)
+    return fail(nullptr, HG_ERR_ARG, "hg_ude_grad: the closure has " + std::to_string(ctx->udeParams) + " parameters");
+  for (int64_t k = 0; k < n_params; ++k) g_params[k] = k < (int64_t)ctx->udeGrad.size() ? ctx->udeGrad[k] : 0.0;
+  return HG_OK;
+}
+
 int hg_set_dt_min(hg_ctx* ctx, double dt_min) {
   if (!ctx) return fail(ctx, HG_ERR_ARG, "hg_set_dt_min: null context");
   if (!(dt_min >= 0.0) || !std::isfinite(dt_min)) return fail(ctx, HG_ERR_ARG, "hg_set_dt_min: dt_min must be >= 0");
@@ -979,8 +989,6 @@ int hg_final_loss_and_grad(hg_ctx* ctx, const double* Q0, int32_t nsteps, double
   if (!ctx || !Q0 || nsteps <= 0 || !(dt > 0) || !obs || !parts || (!obs->wse && !(obs->u && obs->v)) ||
       (!obs->u != !obs->v))
     return fail(ctx, HG_ERR_ARG, "hg_final_loss_and_grad: bad argument");
-  if (ctx->dm.res.kind >= kResUdeManningH)
-    return fail(ctx, HG_ERR_UNSUPPORTED, "hg_final_loss_and_grad: gradients through a UDE closure are not available");
   cudaSetDevice(ctx->device);
   FinalObs fo;
   fo.wse = obs->wse;
@@ -995,8 +1003,6 @@ int hg_final_loss_and_grad(hg_ctx* ctx, const double* Q0, int32_t nsteps, double
 int hg_final_vjp(hg_ctx* ctx, const double* Q0, int32_t nsteps, double dt, int32_t ckpt_every, const double* lambda,
                  double* g_manning_cells, double* g_zb, double* g_inletq, double* Q_final) {
   if (!ctx || !Q0 || nsteps <= 0 || !(dt > 0) || !lambda) return fail(ctx, HG_ERR_ARG, "hg_final_vjp: bad argument");
-  if (ctx->dm.res.kind >= kResUdeManningH)
-    return fail(ctx, HG_ERR_UNSUPPORTED, "hg_final_vjp: gradients through a UDE closure are not available");
   cudaSetDevice(ctx->device);
   FinalObs fo;
   fo.lam = lambda;
@@ -1309,8 +1315,6 @@ int hg_loss_and_grad(hg_ctx* ctx, const double* Q0, int32_t nsteps, double dt, i
     return fail(ctx, HG_ERR_ARG, "hg_loss_and_grad: bad argument");
   for (int i = 0; i < n_probe; ++i)
     if (probe_cells[i] < 0 || probe_cells[i] >= ctx->n) return fail(ctx, HG_ERR_ARG, "hg_loss_and_grad: bad probe id");
-  if (ctx->dm.res.kind >= kResUdeManningH)
-    return fail(ctx, HG_ERR_UNSUPPORTED, "hg_loss_and_grad: gradients through a UDE closure are not available");
   cudaSetDevice(ctx->device);
   return adjoint_loss_and_grad(ctx, Q0, nsteps, dt, ckpt_every, probe_cells, obs, n_probe, loss, g_manning_cells, g_zb,
                                g_inletq, Q_final);

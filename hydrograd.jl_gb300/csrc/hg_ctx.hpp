@@ -73,6 +73,9 @@ struct hg_ctx {
   // The last gradient call's gradient w.r.t. the parameters {n_lower, n_upper,
   // k, h_mid} of a state-dependent n (hg_resistance_grad).
   double resGrad[4] = {0.0, 0.0, 0.0, 0.0};
+  // UDE closure: its parameter count and the last gradient's dL/dtheta
+  int32_t udeParams = 0;
+  std::vector<double> udeGrad;
   int64_t launches = 0;
   hg::AdjointBuffers* adj = nullptr;
   // Adjoint stage-state tape (hg_set_adjoint_tape): -1 automatic budget, 0 the

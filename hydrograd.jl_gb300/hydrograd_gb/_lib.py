@@ -79,6 +79,7 @@ SIGNATURES = {
     "hg_set_manning_function": [_vp, ctypes.c_int32, _dp, ctypes.c_int32, _dp],
     "hg_set_ude": [_vp, ctypes.POINTER(HgUdeDesc)],
     "hg_resistance_grad": [_vp, _dp],
+    "hg_ude_grad": [_vp, _dp, ctypes.c_int64],
     "hg_set_inlet_q": [_vp, _dp, ctypes.c_int32],
     "hg_set_exit_wse": [_vp, _dp, ctypes.c_int32],
     "hg_get_bed": [_vp, _dp, _dp, _dp, _dp],

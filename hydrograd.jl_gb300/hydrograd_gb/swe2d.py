@@ -164,6 +164,7 @@ class SWE2D:
             params = [params.get(n, 0.0) for n in ("n_lower", "n_upper", "k", "h_mid")]
         p = np.ascontiguousarray(params, dtype=np.float64)
         self._res_ks = None if ks is None else np.ascontiguousarray(ks, dtype=np.float64)
+        self._ude_nparams = 0
         self._chk(lib().hg_set_manning_function(self.h, k, _d(p) if len(p) else None, len(p), _d(self._res_ks)))
 
     def resistance_grad(self):
@@ -171,6 +172,13 @@ class SWE2D:
         from the last gradient call (hg_resistance_grad)."""
         g = np.zeros(4)
         self._chk(lib().hg_resistance_grad(self.h, _d(g)))
+        return g
+
+    def ude_grad(self):
+        """dL/dparams of the UDE network from the last gradient call, in the
+        parameters' order (hg_ude_grad)."""
+        g = np.zeros(getattr(self, "_ude_nparams", 0))
+        self._chk(lib().hg_ude_grad(self.h, _d(g), len(g)))
         return g
 
     def set_ude(self, choice, hidden, activations, params, output_bounds, h_bounds, u_bounds=(0.0, 1.0),
@@ -188,6 +196,7 @@ class SWE2D:
         prm = np.ascontiguousarray(params, dtype=np.float64)
         ks = None if ks is None else np.ascontiguousarray(ks, dtype=np.float64)
         self._ude_keep = (hid, act, prm, ks)
+        self._ude_nparams = len(prm)
         pair = ctypes.c_double * 2
         d = HgUdeDesc(kinds[choice] if isinstance(choice, str) else int(choice), len(hid), _i(hid), _i(act), _d(prm),
                       len(prm), pair(*output_bounds), pair(*h_bounds), pair(*u_bounds), pair(*ks_bounds), _d(ks),

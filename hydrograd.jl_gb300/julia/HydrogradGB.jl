@@ -217,6 +217,21 @@ const UDE = Dict("ManningN_h" => 5, "ManningN_h_Umag_ks" => 6, "FlowResistance" 
 A UDE closure in the RHS (process_UDE.jl:3-56 network; `cfg` as the reference's
 UDE_options hold it; θ = the Lux parameters flattened in Lux's order).
 """
+"""dL/d{n_lower, n_upper, k, h_mid} of the state-dependent n function from the last gradient call."""
+function resistance_grad(ctx::Context)
+    g = zeros(4)
+    check(ctx.ptr, ccall((:hg_resistance_grad, lib), Cint, (Ptr{Cvoid}, Ptr{Float64}), ctx, g))
+    return g
+end
+
+"""dL/dθ of the UDE network from the last gradient call, θ in set_ude!'s (Lux's flattened) order:
+the gradient UDE_training (swe_2D_UDE.jl:119) takes through the solve."""
+function ude_grad(ctx::Context, nparams::Integer)
+    g = zeros(nparams)
+    check(ctx.ptr, ccall((:hg_ude_grad, lib), Cint, (Ptr{Cvoid}, Ptr{Float64}, Int64), ctx, g, Int64(nparams)))
+    return g
+end
+
 function set_ude!(ctx::Context, choice::AbstractString, cfg::AbstractDict, θ::Vector{Float64},
                   ks_cells::Vector{Float64}=Float64[])
     hid = Int32.(cfg["hidden_layers"])
@@ -238,14 +253,22 @@ it writes `p` into the context.
 """
 struct ActiveParam
     ctx::Context
-    name::String                 # "ManningN", "zb" or "Q"
+    name::String                 # "ManningN", "zb", "Q" or "UDE" (the network's weights)
     matID::Vector{Int32}         # 0-based zone of each cell (ManningN)
+    ude_choice::String           # UDE: set_ude!'s choice, cfg and ks per cell
+    ude_cfg::Dict{String,Any}
+    ks::Vector{Float64}
 end
+ActiveParam(ctx::Context, name::AbstractString, matID::AbstractVector{<:Integer}) =
+    ActiveParam(ctx, String(name), Int32.(matID), "", Dict{String,Any}(), Float64[])
+ActiveParam(ctx::Context, choice::AbstractString, cfg::AbstractDict, ks::Vector{Float64}=Float64[]) =
+    ActiveParam(ctx, "UDE", Int32[], String(choice), Dict{String,Any}(cfg), ks)
 function (a::ActiveParam)(p::AbstractVector{<:Real})
     v = Vector{Float64}(p)
     a.name == "ManningN" ? set_manning_zones!(a.ctx, a.matID, v) :
     a.name == "zb" ? set_zb!(a.ctx, v) :
-    a.name == "Q" ? set_inlet_q!(a.ctx, v) : error("active parameter: ManningN, zb or Q")
+    a.name == "Q" ? set_inlet_q!(a.ctx, v) :
+    a.name == "UDE" ? set_ude!(a.ctx, a.ude_choice, a.ude_cfg, v, a.ks) : error("active parameter: ManningN, zb, Q or UDE")
     return nothing
 end
 
@@ -379,6 +402,7 @@ end
 function param_gradient(a::ActiveParam, gn, gzb, gq, np::Integer)
     a.name == "ManningN" && return [sum(gn[a.matID .== z - 1]) for z in 1:np]
     a.name == "zb" && return gzb
+    a.name == "UDE" && return ude_grad(a.ctx, np)
     return gq[1:np]
 end
 

@@ -220,8 +220,8 @@ int hg_get_bed(hg_ctx* ctx, double* zb_cells, double* S0, double* manning_cells,
  * RHS evaluation's dL/dn is taken back into its state through
  * dn/d(h, qx, qy), so the zb and inlet-Q gradients include it, and into the
  * function's parameters (hg_resistance_grad); the per-cell n gradient is then
- * zero, n not being a parameter.  Gradients with a UDE closure (kinds 5-7)
- * are not available: HG_ERR_UNSUPPORTED. */
+ * zero, n not being a parameter.  With a UDE closure (kinds 5-7) they run
+ * through the network (hg_ude_grad). */
 enum hg_resistance {
   HG_RES_CONSTANT = 0, HG_RES_POWER_LAW = 1, HG_RES_SIGMOID = 2, HG_RES_INVERSE = 3, HG_RES_H_UMAG_KS = 4,
   HG_RES_UDE_MANNING_H = 5,          /* UDE_choice "ManningN_h": n = NN(h) */
@@ -246,7 +246,14 @@ int hg_resistance_grad(const hg_ctx* ctx, double* g_params4);
  * weight (1 x w) and bias.  LayerNorm: (x - mean) / sqrt(var + 1f-5) * scale +
  * bias, uncorrected variance; layernorm_over_batch = 1 takes mean and variance
  * over the whole (width x cells) array, as Lux's LayerNorm with its default
- * dims = Colon() does; 0 takes them over each cell's features. */
+ * dims = Colon() does; 0 takes them over each cell's features.
+ * Gradients (hg_loss_and_grad, hg_final_loss_and_grad, hg_final_vjp) run
+ * through the network, as the reference trains it by differentiating the
+ * solve (swe_2D_UDE.jl:119,522): each RHS evaluation's dL/dn (dL/dF for
+ * FlowResistance) is taken back by reverse mode into the cells' states and
+ * into the parameters (hg_ude_grad), through the batch LayerNorm's statistics
+ * too; for FlowResistance the inlet conveyance's dL/dn stays a per-cell n
+ * gradient. */
 enum hg_activation { HG_ACT_RELU = 0, HG_ACT_LEAKYRELU = 1, HG_ACT_SIGMOID = 2, HG_ACT_TANH = 3, HG_ACT_SOFTPLUS = 4 };
 typedef struct hg_ude_desc {
   int32_t kind;                  /* HG_RES_UDE_* */
@@ -263,6 +270,11 @@ typedef struct hg_ude_desc {
   int32_t layernorm_over_batch;
 } hg_ude_desc;
 int hg_set_ude(hg_ctx* ctx, const hg_ude_desc* ude);
+/* dL/dparams of the UDE network from the last hg_loss_and_grad /
+ * hg_final_loss_and_grad / hg_final_vjp call, in hg_set_ude's parameter order;
+ * n_params must be the closure's count (HG_ERR_ARG otherwise; 0 without a
+ * closure). */
+int hg_ude_grad(const hg_ctx* ctx, double* g_params, int64_t n_params);
 
 /* Change the Riemann solver (hg_riemann) of a context after hg_create: it
  * applies to every integrator, the RHS and the adjoint. */

@@ -87,9 +87,6 @@ def test_ude_rhs_and_steps_match_oracle(choice, kind, in_dim, bounds, over_batch
     Qg, _ = ctx.integrate(Q0, 50, dt=dt)
     Qo = o.rk2(Q0, 50, dt=dt, nthreads=4)
     assert block_err(Qg, Qo, N) <= STATE_TOL[precision]
-    with pytest.raises(HgError) as e:   # no gradients through the network's weights
-        ctx.loss_and_grad(Q0, 5, dt, [0, 1], [0.1, 0.1])
-    assert e.value.code == 7
 
 
 @pytest.mark.parametrize("precision", ["fp64", "fp32c"])
