@@ -54,6 +54,14 @@ struct AdjointBuffers {
   unsigned int* finTicket = nullptr;
   double* resGrad = nullptr;      // [4] the parameter gradient of a state-dependent n
   size_t udeCap = 0;              // parameters gTheta and udePart are sized for
+  float4* bndJ = nullptr;         // FP32C folded boundary VJP: flux Jacobians of a segment's states
+  size_t bndJCap = 0;             // states
+  int32_t* tileProbe = nullptr;   // folded: per interior-VJP tile its distinct probe cells (CSR)
+  size_t tileProbeCap = 0;
+  float* probeSeeds = nullptr;    // folded: a segment's probe seeds [steps][distinct probe cells]
+  size_t probeSeedCap = 0;
+  double* lossPart = nullptr;     // folded: the probe loss sum of each step's state [K]
+  size_t lossPartCap = 0;
   ~AdjointBuffers() {
     for (void* p : fixed) cudaFree(p);
     cudaFree(ckpt);
@@ -68,6 +76,10 @@ struct AdjointBuffers {
     cudaFree(finTicket);
     cudaFree(dev.gTheta);
     cudaFree(dev.udePart);
+    cudaFree(bndJ);
+    cudaFree(tileProbe);
+    cudaFree(probeSeeds);
+    cudaFree(lossPart);
   }
 };
 
@@ -201,6 +213,54 @@ int setup(hg_ctx* c) {
   ADJ_CUDA(c, falloc(b, &a.grpTA, (size_t)c->dm.nInlet));
   ADJ_CUDA(c, falloc(b, &a.tileTicket, 3));
   ADJ_CUDA(c, cudaMemset(a.tileTicket, 0, 3 * sizeof(unsigned int)));
+  // Folded boundary VJP (FP32C): the cell and slot of each boundary face, and
+  // per interior-VJP tile the inlet groups whose cells it holds.
+  if (c->precision == HG_FP32C && (int)m.inletGroups.size() <= kFoldMaxGroups) {
+    std::vector<int2> bfSlot((size_t)std::max(nbf, 1), make_int2(0, 0));
+    for (int i = 0; i < N; ++i) {
+      const int o = c->perm[i];
+      for (int k = 0; k < m.ncf[o]; ++k)
+        if (m.nbr[(size_t)o * 8 + k] < 0) bfSlot[bfOf[m.cf[(size_t)o * 8 + k]]] = make_int2(i, k);
+    }
+    const int nTiles = (N + kStageBlockF32 - 1) / kStageBlockF32;
+    std::vector<uint32_t> tileGrp((size_t)std::max(nTiles, 1), 0u);
+    std::vector<int32_t> grpTile(std::max<size_t>(m.inletGroups.size(), 1), -1);
+    for (size_t g = 0; g < m.inletGroups.size(); ++g)
+      for (int f : m.bnd[m.inletGroups[g]].faces) {
+        const int t = c->inv[m.faceC0[f]] / kStageBlockF32;
+        tileGrp[t] |= 1u << g;
+        if (grpTile[g] < 0 || t < grpTile[g]) grpTile[g] = t;
+      }
+    // per inlet CSR entry (the forward's group order): face, cell, len / area
+    std::vector<float4> inletW;
+    for (size_t g = 0; g < m.inletGroups.size(); ++g)
+      for (int f : m.bnd[m.inletGroups[g]].faces) {
+        const int bfi = bfOf[f], cell = c->inv[m.faceC0[f]];
+        float4 v;
+        std::memcpy(&v.x, &bfi, sizeof(float));
+        std::memcpy(&v.y, &cell, sizeof(float));
+        v.z = (float)m.faceLen[f] / (float)m.area[m.faceC0[f]];
+        v.w = 0.0f;
+        inletW.push_back(v);
+      }
+    float4* dInletW;
+    ADJ_CUDA(c, falloc(b, &dInletW, std::max<size_t>(inletW.size(), 1)));
+    if (!inletW.empty())
+      ADJ_CUDA(c, cudaMemcpy(dInletW, inletW.data(), inletW.size() * sizeof(float4), cudaMemcpyHostToDevice));
+    a.inletW = dInletW;
+    int2* dSlot;
+    uint32_t* dTileGrp;
+    int32_t* dGrpTile;
+    ADJ_CUDA(c, falloc(b, &dSlot, bfSlot.size()));
+    ADJ_CUDA(c, falloc(b, &dTileGrp, tileGrp.size()));
+    ADJ_CUDA(c, falloc(b, &dGrpTile, grpTile.size()));
+    ADJ_CUDA(c, cudaMemcpy(dSlot, bfSlot.data(), bfSlot.size() * sizeof(int2), cudaMemcpyHostToDevice));
+    ADJ_CUDA(c, cudaMemcpy(dTileGrp, tileGrp.data(), tileGrp.size() * 4, cudaMemcpyHostToDevice));
+    ADJ_CUDA(c, cudaMemcpy(dGrpTile, grpTile.data(), grpTile.size() * 4, cudaMemcpyHostToDevice));
+    a.bfSlot = dSlot;
+    a.tileGrp = dTileGrp;
+    a.grpTile = dGrpTile;
+  }
   return HG_OK;
 }
 
@@ -366,6 +426,25 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
     pc.idx = b->probeCsr + 2 * cells.size() + 1;
     pc.isBnd = b->probeCsr + 2 * cells.size() + 1 + P;
     pc.nCells = (int32_t)cells.size();
+    if (c->precision == HG_FP32C && P > 0) {   // per interior-VJP tile its distinct probe cells
+      const int nTiles = (N + kStageBlockF32 - 1) / kStageBlockF32;
+      std::vector<int32_t> tp(nTiles + 1 + cells.size(), 0);
+      for (int32_t cell : cells) ++tp[cell / kStageBlockF32 + 1];
+      for (int t = 0; t < nTiles; ++t) tp[t + 1] += tp[t];
+      std::vector<int32_t> fill(tp.begin(), tp.begin() + nTiles);
+      for (size_t u = 0; u < cells.size(); ++u) tp[nTiles + 1 + fill[cells[u] / kStageBlockF32]++] = (int32_t)u;
+      if (tp.size() > b->tileProbeCap) {
+        cudaFree(b->tileProbe);
+        b->tileProbe = nullptr;
+        b->tileProbeCap = 0;
+        ADJ_CUDA(c, cudaMalloc(&b->tileProbe, tp.size() * sizeof(int32_t)));
+        b->tileProbeCap = tp.size();
+      }
+      ADJ_CUDA(c, cudaMemcpy(b->tileProbe, tp.data(), tp.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+      a.tileProbeOff = b->tileProbe;
+      a.tileProbeU = b->tileProbe + nTiles + 1;
+      a.probeCell = pc.cell;
+    }
   }
   if (P > 0) {
     ADJ_CUDA(c, cudaMemcpyAsync(b->probes, pdev.data(), P * sizeof(int32_t), cudaMemcpyHostToDevice, st));
@@ -606,6 +685,36 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
     }
     ADJ_CUDA(c, copy_state(XA, sg.at(K - sLast, n)));   // the final state
     if (Qfinal) launch_scatter_state_f32(N, c->d_perm, XA, c->Quser, st);   // copied out at the end
+    // Boundary faces folded into the interior VJP where it can run (constant
+    // inlet discharges and resistance: a segment's face Jacobians are then
+    // formed in one launch before its reverse steps).
+    const bool fold = vjp_fold_usable(dm, a, XA) && !a.resChain && !a.udeChain && dm.nHydro == 0;
+    if (fold && (size_t)(2 * C + 1) > b->bndJCap) {
+      cudaFree(b->bndJ);
+      b->bndJ = nullptr;
+      b->bndJCap = 0;
+      ADJ_CUDA(c, cudaMalloc(&b->bndJ, (size_t)(2 * C + 1) * std::max(dm.nbf, 1) * 6 * sizeof(float4)));
+      b->bndJCap = (size_t)(2 * C + 1);
+    }
+    const size_t jStride = (size_t)dm.nbf * 6;   // float4 per state
+    const bool foldProbes = fold && P > 0;
+    if (foldProbes) {
+      const size_t seedNeed = (size_t)C * std::max(pc.nCells, 1);
+      if (seedNeed > b->probeSeedCap) {
+        cudaFree(b->probeSeeds);
+        b->probeSeeds = nullptr;
+        b->probeSeedCap = 0;
+        ADJ_CUDA(c, cudaMalloc(&b->probeSeeds, seedNeed * sizeof(float)));
+        b->probeSeedCap = seedNeed;
+      }
+      if ((size_t)K > b->lossPartCap) {
+        cudaFree(b->lossPart);
+        b->lossPart = nullptr;
+        b->lossPartCap = 0;
+        ADJ_CUDA(c, cudaMalloc(&b->lossPart, (size_t)K * sizeof(double)));
+        b->lossPartCap = (size_t)K;
+      }
+    }
     ADJ_CUDA(c, cudaMemsetAsync(mu2, 0, n3 * sizeof(float), st));
     // The probe loss of each state after step s and its seed, in one kernel
     // in the reverse sweep (the state after the last step first).
@@ -626,6 +735,11 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
                T0 + (i + 1) * stride);
         }
       }
+      const int sFirst = std::max(s0, 1);   // steps whose stage-1 VJP adds probe seeds
+      if (fold) c->launches += launch_bnd_jac_f32(dm, a, sg.x, 2 * C + 1, b->segTot, stride, b->bndJ, st);
+      if (foldProbes)
+        c->launches += launch_probe_seg_f32(dm, sg.x, s0, sFirst, s1 - sFirst, pc, b->probes, b->obs, P, scale,
+                                            b->probeSeeds, b->lossPart, st);
       for (int s = s1 - 1; s >= s0; --s) {
         const size_t i = (size_t)(s - s0);
         const StateF32 q0 = sg.at(i, n), q1 = sg.at(C + 1 + i, n);
@@ -635,7 +749,13 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
         hydro((s + 1) * dt);
         const bool resState = a.resChain || a.udeChain;
         if (resState) c->launches += launch_resistance_f32(dm, q1, st);   // n (or F) of the VJP's state
-        c->launches += launch_vjp_f32(m1, a, q1, mu2, nullptr, mu1, 0.5f, 0.0f, 0.5 * dt, st);
+        AdjDev aj = a;   // folded: the face Jacobians of the VJP's state
+        if (fold) {
+          aj.bndJ = b->bndJ + (C + 1 + i) * jStride;
+          c->launches += launch_vjp_f32_folded(m1, aj, q1, mu2, nullptr, mu1, 0.5f, 0.0f, 0.5 * dt, st, nullptr);
+        } else {
+          c->launches += launch_vjp_f32(m1, a, q1, mu2, nullptr, mu1, 0.5f, 0.0f, 0.5 * dt, st);
+        }
         c->launches += launch_ude_vjp_f32(dm, a, q1, mu1, st);
         hydro(s * dt);
         if (resState) c->launches += launch_resistance_f32(dm, q0, st);
@@ -648,10 +768,17 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
           pj.np = P;
           pj.scale = scale;
         }
-        c->launches += launch_vjp_f32(m0, a, q0, mu1, mu2, mu2, 1.0f, 0.5f, dt, st, &pj);
+        if (fold) {
+          aj.bndJ = b->bndJ + i * jStride;
+          aj.probeSeed = (foldProbes && s >= 1) ? b->probeSeeds + (size_t)(s - sFirst) * pc.nCells : nullptr;
+          c->launches += launch_vjp_f32_folded(m0, aj, q0, mu1, mu2, mu2, 1.0f, 0.5f, dt, st, nullptr);
+        } else {
+          c->launches += launch_vjp_f32(m0, a, q0, mu1, mu2, mu2, 1.0f, 0.5f, dt, st, &pj);
+        }
         c->launches += launch_ude_vjp_f32(dm, a, q0, mu2, st);
       }
     }
+    if (foldProbes) c->launches += launch_loss_parts(a, b->lossPart, K - 1, st);   // states K-1 .. 1, in order
   }
   if (a.accF) {
     launch_fold_accumulators_f32(dm, a, st);

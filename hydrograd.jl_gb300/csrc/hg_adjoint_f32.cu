@@ -106,10 +106,12 @@ struct GlobalSrc {
 
 // The VJP of one stage at cell j (interior faces: 3-direction duals of the
 // reference solver where a side is dry, reverse mode where both are wet; the
-// sources), written to out[j] and the cell's parameter accumulators.
-template <int NS, class Src>
+// sources), written to out[j] and the cell's parameter accumulators.  FOLD:
+// the boundary faces too, from their flux Jacobians (a.bndJ), and the inlet
+// conveyance terms with the groups' total_A cotangents grpTA.
+template <int NS, bool FOLD, class Src>
 __device__ __forceinline__ void vjp_cell(const DevMesh& m, const AdjDev& a, int j, const Src& src, float* out,
-                                         float cSelf, float cExtra, float beta) {
+                                         float cSelf, float cExtra, float beta, const double* grpTA = nullptr) {
   const int n = m.n;
   const float4 cp = src.cp();
   const float4 cs = src.cs();
@@ -180,6 +182,36 @@ __device__ __forceinline__ void vjp_cell(const DevMesh& m, const AdjDev& a, int 
       acc_add(&a.accF[(size_t)2 * n + j], beta, mj2 * m.gf * L.s.xi);
     }
   }
+  if constexpr (FOLD) {   // boundary faces: c = w . J, the terms k_vjp_bnd_f32 + k_vjp_combine_f32 give
+    float gzbB = 0.0f;
+#pragma unroll
+    for (int k = 0; k < NS; ++k) {
+      const float4 sl = src.slot(k);
+      const int32_t nb = slot_nb(sl);
+      if (nb >= 0 || nb == kNoFace) continue;
+      const int32_t bf = boundary_index(nb);
+      const float w0 = -sl.z * mj0 / Aj, w1 = -sl.z * mj1 / Aj, w2 = -sl.z * mj2 / Aj;
+      float J[24];
+#pragma unroll
+      for (int q = 0; q < 6; ++q) {
+        const float4 v = __ldg(&a.bndJ[(size_t)bf * 6 + q]);
+        J[4 * q] = v.x; J[4 * q + 1] = v.y; J[4 * q + 2] = v.z; J[4 * q + 3] = v.w;
+      }
+      g0 += w0 * J[0] + w1 * J[7] + w2 * J[14];
+      g1 += w0 * J[1] + w1 * J[8] + w2 * J[15];
+      g2 += w0 * J[2] + w1 * J[9] + w2 * J[16];
+      gn += w0 * J[3] + w1 * J[10] + w2 * J[17];
+      gzbB += w0 * J[4] + w1 * J[11] + w2 * J[18];
+      const int32_t info = __ldg(&m.bfInfo[bf]);
+      if ((info & 3) == kBcInletQ && !L.s.dry) {
+        // total_A = sum L^(5/3) h / n over the group's wet cells (bc_2D.jl:673-676)
+        const double gTA = grpTA[info >> 2], lp = m.bfLp53[bf], nm = cp.w;
+        g0 += (float)(gTA * lp / nm);
+        gn += (float)(gTA * (-lp * (double)L.s.h / (nm * nm)));
+      }
+    }
+    if (a.wantZb && gzbB != 0.0f) acc_add(&a.accF[(size_t)3 * n + j], beta, gzbB);
+  }
   if (a.resChain) {   // n = f(state): dL/dn into the state and the function's parameters
     if (gn != 0.0f) {
       const ResJac<float> J =
@@ -215,7 +247,7 @@ __global__ void __launch_bounds__(kBlock, vjp_min_blocks<NS>()) k_vjp_f32(DevMes
                                                     float cExtra, float beta) {
   pdl_release_dependents();
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j < m.n) vjp_cell<NS>(m, a, j, GlobalSrc{m, Q, mu, extra, j}, out, cSelf, cExtra, beta);
+  if (j < m.n) vjp_cell<NS, false>(m, a, j, GlobalSrc{m, Q, mu, extra, j}, out, cSelf, cExtra, beta);
   pdl_wait_prerequisites();
 }
 
@@ -261,9 +293,11 @@ struct TileSrc {
   }
 };
 
+// A tile's copies in two parts: the records that stay fixed during the
+// reverse sweep (mesh records, the stage state), and the cotangents, which
+// the kernel before this one writes.
 template <int NS>
-__device__ __forceinline__ void vjp_issue(const DevMesh& m, StateF32 Q, const float* mu, const float* extra, int t,
-                                          unsigned char* B, int hid) {
+__device__ __forceinline__ void vjp_issue_fixed(const DevMesh& m, StateF32 Q, int t, unsigned char* B, int hid) {
   using T = VjpTile<NS>;
   const int tid = threadIdx.x, n = m.n;
   const int c = t * kVTile + tid;
@@ -273,6 +307,20 @@ __device__ __forceinline__ void vjp_issue(const DevMesh& m, StateF32 Q, const fl
     cp_async16(B + T::kX + tid * 16, &Q.x[c]);
     cp_async16(B + T::kCP + tid * 16, &m.CP[c]);
     cp_async16(B + T::kCS + tid * 16, &m.CS[c]);
+  }
+  if (hid >= 0) {
+    cp_async16(B + T::kHX + tid * 16, &Q.x[hid]);
+    cp_async16(B + T::kHP + tid * 16, &m.CP[hid]);
+    cp_async4(B + T::kHA + tid * 4, &m.CS[hid].z);
+  }
+}
+template <int NS>
+__device__ __forceinline__ void vjp_issue_cot(const DevMesh& m, const float* mu, const float* extra, int t,
+                                              unsigned char* B, int hid) {
+  using T = VjpTile<NS>;
+  const int tid = threadIdx.x, n = m.n;
+  const int c = t * kVTile + tid;
+  if (c < n) {
 #pragma unroll
     for (int b = 0; b < 3; ++b) {
       cp_async4(B + T::kMU + (b * kVTile + tid) * 4, &mu[(size_t)b * n + c]);
@@ -280,26 +328,95 @@ __device__ __forceinline__ void vjp_issue(const DevMesh& m, StateF32 Q, const fl
     }
   }
   if (hid >= 0) {
-    cp_async16(B + T::kHX + tid * 16, &Q.x[hid]);
-    cp_async16(B + T::kHP + tid * 16, &m.CP[hid]);
-    cp_async4(B + T::kHA + tid * 4, &m.CS[hid].z);
 #pragma unroll
     for (int b = 0; b < 3; ++b) cp_async4(B + T::kHM + (b * kHaloMax + tid) * 4, &mu[(size_t)b * n + hid]);
+  }
+}
+template <int NS>
+__device__ __forceinline__ void vjp_issue(const DevMesh& m, StateF32 Q, const float* mu, const float* extra, int t,
+                                          unsigned char* B, int hid) {
+  vjp_issue_fixed<NS>(m, Q, t, B, hid);
+  vjp_issue_cot<NS>(m, mu, extra, t, B, hid);
+}
+
+// The inlet groups' total_A and Q cotangents of the folded boundary VJP: for
+// each group of the tile's mask gm, the whole CTA strides over the group's
+// faces, then a fixed reduction (shuffle tree per warp, the warps' sums in
+// order).  Every CTA that needs a group's total_A cotangent forms it; the CTA
+// of tile grpTile[g] alone adds the Q cotangent.  sRed: 2 x (warps) doubles.
+__device__ void fold_group_sums(const DevMesh& m, const AdjDev& a, const float* __restrict__ mu, uint32_t gm, int t,
+                                double betaD, double* sGrp, double* sRed) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5, n = m.n;
+  for (int g = 0; g < m.nInlet; ++g) {
+    if (!((gm >> g) & 1u)) continue;
+    double sTA = 0.0, sQ = 0.0;
+    constexpr int U = 4;   // faces per thread in flight at once
+    const int e1 = m.inletOff[g + 1];
+    for (int e0 = m.inletOff[g] + threadIdx.x; e0 < e1; e0 += U * blockDim.x) {
+      float4 iw[U], J1[U], J3[U], J4[U], J5[U];
+      float m0[U], m1[U], m2[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int e = e0 + u * blockDim.x;
+        iw[u] = e < e1 ? __ldg(&a.inletW[e]) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int bf = __float_as_int(iw[u].x), j = __float_as_int(iw[u].y);   // 0, 0 past the end: weight 0
+        const float4* Jp = a.bndJ + (size_t)bf * 6;
+        J1[u] = __ldg(Jp + 1); J3[u] = __ldg(Jp + 3); J4[u] = __ldg(Jp + 4); J5[u] = __ldg(Jp + 5);
+        m0[u] = mu[j]; m1[u] = mu[n + j]; m2[u] = mu[2 * n + j];
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const float w0 = -iw[u].z * m0[u], w1 = -iw[u].z * m1[u], w2 = -iw[u].z * m2[u];
+        // J[5], J[6] | J[12], J[13] | J[19], J[20]
+        sQ += (double)(w0 * J1[u].y + w1 * J3[u].x + w2 * J4[u].w);
+        sTA += (double)(w0 * J1[u].z + w1 * J3[u].y + w2 * J5[u].x);
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      sTA += __shfl_xor_sync(0xffffffffu, sTA, o);
+      sQ += __shfl_xor_sync(0xffffffffu, sQ, o);
+    }
+    if (lane == 0) {
+      sRed[w] = sTA;
+      sRed[nw + w] = sQ;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double ta = 0.0, q = 0.0;
+      for (int k = 0; k < nw; ++k) {
+        ta += sRed[k];
+        q += sRed[nw + k];
+      }
+      sGrp[g] = ta;
+      if (a.grpTile[g] == t) a.gQ[g] += betaD * q;
+    }
+    __syncthreads();
   }
 }
 
 // Tiles 0..G-1 go to the G CTAs in order, the rest to whichever CTA asks next
 // (a.tileTicket[0]): a CTA that starts late -- its SM still busy with the
-// boundary VJP beside it -- takes fewer tiles instead of finishing late.  Each
-// cell is still computed by one thread with the same arithmetic, so the
+// boundary VJP beside it, or still waiting on the kernel before it -- takes
+// fewer tiles instead of finishing late (with the boundary faces folded in,
+// static tiles b, b + G, ... measured 7 % slower per forward+adjoint step).
+// Each cell is still computed by one thread with the same arithmetic, so the
 // result does not depend on the assignment.
-template <int NS>
-__global__ void __launch_bounds__(kVTile, 2) k_vjp_pipe_f32(DevMesh m, AdjDev a, StateF32 Q, const float* mu,
+// FOLD: launched as the programmatic dependent of the kernel before it, which
+// it waits for after the first tile's fixed records are in flight (and
+// before anything that kernel writes: cotangents, accumulators, the tile
+// tickets its last CTA resets).  MINB: CTAs per SM the registers allow.
+template <int NS, bool FOLD, int MINB = 2>
+__global__ void __launch_bounds__(kVTile, MINB) k_vjp_pipe_f32(DevMesh m, AdjDev a, StateF32 Q, const float* mu,
                                                            const float* extra, float* out, float cSelf, float cExtra,
-                                                           float beta) {
+                                                           float beta, double betaD) {
   using T = VjpTile<NS>;
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ int sNext[2];   // alternate slots: a slot is rewritten two barriers after its last read
+  __shared__ double sGrp[kFoldMaxGroups];   // FOLD: the tile's inlet groups' total_A cotangents
+  __shared__ double sRed[2 * (kVTile / 32)];
   const int n = m.n, nTiles = (n + kVTile - 1) / kVTile, tid = threadIdx.x, G = gridDim.x;
   auto halo_id = [&](int t) { return (t < nTiles && tid < kHaloMax) ? m.halo[(size_t)t * kHaloMax + tid] : -1; };
   auto take = [&] { return G + (int)atomicAdd(&a.tileTicket[0], 1u); };
@@ -308,11 +425,17 @@ __global__ void __launch_bounds__(kVTile, 2) k_vjp_pipe_f32(DevMesh m, AdjDev a,
   pdl_release_dependents();
   int t = blockIdx.x;   // < nTiles: the grid is at most the tile count
   int ahead = 0;
+  if constexpr (FOLD) {
+    vjp_issue_fixed<NS>(m, Q, t, smem, halo_id(t));
+    pdl_wait_prerequisites();
+    vjp_issue_cot<NS>(m, mu, extra, t, smem, halo_id(t));
+  } else {
+    vjp_issue<NS>(m, Q, mu, extra, t, smem, halo_id(t));
+  }
   if (tid == 0) {
     sNext[0] = take();
     ahead = take();
   }
-  vjp_issue<NS>(m, Q, mu, extra, t, smem, halo_id(t));
   cp_async_commit();
   __syncthreads();
   int tn = sNext[0];
@@ -327,9 +450,22 @@ __global__ void __launch_bounds__(kVTile, 2) k_vjp_pipe_f32(DevMesh m, AdjDev a,
     const int tnn = sNext[slot];
     if (tid == 0) ahead = take();
     hidNext = halo_id(tnn);
+    if constexpr (FOLD) {
+      const uint32_t gm = m.nInlet > 0 ? __ldg(&a.tileGrp[t]) : 0u;   // the same for the whole CTA
+      if (gm) fold_group_sums(m, a, mu, gm, t, betaD, sGrp, sRed);   // ends with a barrier
+    }
     const int j = t * kVTile + tid;
-    if (j < n) vjp_cell<NS>(m, a, j, TileSrc<NS>{smem + b * T::kBuf, tid, extra != nullptr}, out, cSelf, cExtra, beta);
+    if (j < n)
+      vjp_cell<NS, FOLD>(m, a, j, TileSrc<NS>{smem + b * T::kBuf, tid, extra != nullptr}, out, cSelf, cExtra, beta,
+                         sGrp);
     __syncthreads();   // buffer b is refilled at the top of the next iteration
+    if constexpr (FOLD) {   // the step's probe seeds, after the tile's own cotangents
+      if (a.probeSeed)
+        for (int e = a.tileProbeOff[t] + tid; e < a.tileProbeOff[t + 1]; e += kVTile) {
+          const int u = a.tileProbeU[e];
+          out[a.probeCell[u]] += a.probeSeed[u];
+        }
+    }
     t = tn;
     tn = tnn;
     b ^= 1;
@@ -435,6 +571,46 @@ __global__ void __launch_bounds__(64) k_vjp_bnd_f32(DevMesh m, AdjDev a, StateF3
   }
 }
 
+// Folded boundary VJP: the flux Jacobian of boundary face bf at state s of a
+// segment (records X + s n, inlet totals tot + s totStride), by the
+// 7-direction duals k_vjp_bnd_f32 takes, without the cotangent.
+__global__ void __launch_bounds__(128) k_bnd_jac_f32(DevMesh m, AdjDev a, const float4* __restrict__ X, int nStates,
+                                                     const double* __restrict__ tot, size_t totStride, float4* J) {
+  const int nbf = m.nbf, n = m.n;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (int64_t)nStates * nbf) return;
+  const int s = (int)(t / nbf), bf = (int)(t - (int64_t)s * nbf);
+  const int2 cs = a.bfSlot[bf];
+  const int j = cs.x;
+  const float4 sl = __ldg(&m.SL[(size_t)cs.y * n + j]);
+  const float4 cp = __ldg(&m.CP[j]);
+  const SideF32 L = make_side_f32(__ldg(&X[(size_t)s * n + j]), cp, m.hsmf, m.hsmLo);
+  const float nx = sl.x, ny = sl.y;
+  const int32_t info = m.bfInfo[bf], type = info & 3, grp = info >> 2;
+  const Side<F7> L7 = seeded<F7>(L.s, 4);
+  const F7 man = F7::seed(cp.w, 3);
+  const F7 qin = F7::seed(type == kBcInletQ ? (float)m.inletQ[grp] : 0.0f, 5);
+  const F7 ta = F7::seed(type == kBcInletQ ? (float)tot[(size_t)s * totStride + grp] : 1.0f, 6);
+  const Side<F7> R7 = ghost_state<F7>(L7, type, F7(nx), F7(ny), F7(m.hsmf),
+                                      F7(type == kBcExitH ? (float)m.exitWse[grp] : 0.0f), qin, ta,
+                                      F7(m.bfLp23f[bf]), man);
+  F7 ex(L.excess);
+  if (L.s.dry) ex.d[0] = -1.0f;   // excess = h_small - (xi + hstill) for a dry cell
+  F7 dxi = (R7.h - L7.h) + ex;
+  if (type == kBcExitH && !R7.dry) dxi.v = m.bfExitRel[bf] - (L.s.xi + L.xlo);   // as the forward pass
+  F7 F[3];
+  riemann_flux<F7>(m.riemann, L7, R7, dxi, F7(m.gf), F7(nx), F7(ny), F7(m.hsmf), F);
+  float v[24];
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int d = 0; d < 7; ++d) v[7 * r + d] = F[r].d[d];
+  v[21] = v[22] = v[23] = 0.0f;
+  float4* o = J + ((size_t)s * nbf + bf) * 6;
+#pragma unroll
+  for (int q = 0; q < 6; ++q) o[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+}
+
 // After both VJP kernels: each boundary cell's terms into out (when wet) and
 // the n / zb accumulators, then its inlet total_A terms (bc_2D.jl:673-676:
 // total_A = sum L^(5/3) h / n over the group's wet cells) into out and gN.
@@ -482,6 +658,42 @@ __global__ void __launch_bounds__(256) k_probe_f32(DevMesh m, AdjDev a, StateF32
                                                    const double* __restrict__ obs, int np, double scale) {
   pdl_enter();
   probe_block(m, a, Q, mu, pc, probes, obs, np, scale, false);
+}
+
+// Folded reverse sweep: the probe terms of a segment's states, one block per
+// step s (the state after step s - 1): each distinct probe cell's seed (as
+// probe_seed adds it; 0 for a dry cell) and the loss sum (probe_block's order).
+__global__ void __launch_bounds__(256) k_probe_seg_f32(DevMesh m, const float4* __restrict__ X, int s0, int sFirst,
+                                                       ProbeCsr pc, const int32_t* __restrict__ probes,
+                                                       const double* __restrict__ obs, int np, double scale,
+                                                       float* seeds, double* lossPart) {
+  const int s = sFirst + blockIdx.x;
+  const StateF32 Q{const_cast<float4*>(X) + (size_t)(s - s0) * m.n, nullptr};
+  const double* ob = obs + (size_t)(s - 1) * np;
+  for (int u = threadIdx.x; u < pc.nCells; u += blockDim.x) {
+    const int c = pc.cell[u];
+    const SideF32 L = make_side_f32(Q.x[c], m.CP[c], m.hsmf, m.hsmLo);
+    double acc = 0.0;
+    if (!L.s.dry) {
+      const double h = depth_f64(m, Q, c);
+      for (int i = pc.off[u]; i < pc.off[u + 1]; ++i) acc += scale * 2.0 * (h - ob[pc.idx[i]]);
+    }
+    seeds[(size_t)blockIdx.x * pc.nCells + u] = (float)acc;
+  }
+  double sum = 0.0;
+  for (int p = threadIdx.x; p < np; p += blockDim.x) {
+    const double e = depth_f64(m, Q, probes[p]) - ob[p];
+    sum += e * e;
+  }
+  const double t = block_sum(sum);
+  if (threadIdx.x == 0) lossPart[s - 1] = t;
+}
+
+__global__ void k_loss_parts(AdjDev a, const double* __restrict__ lossPart, int sLast) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double l = a.loss[0];
+  for (int s = sLast; s >= 1; --s) l += lossPart[s - 1];
+  a.loss[0] = l;
 }
 
 // 256-thread blocks: the probe block reduces the loss in the order of the
@@ -568,27 +780,51 @@ bool vjp_gather_forced() {
   return on;
 }
 
+bool pipe_usable(const DevMesh& m, StateF32 Q) {
+  auto a16 = [](const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; };
+  return m.nslot <= 4 && !vjp_gather_forced() && m.SLp && m.halo && a16(m.SLp) && a16(m.CP) && a16(m.CS) &&
+         a16(Q.x);
+}
+
+// The pipelined persistent interior VJP (a grid of the CTAs resident at once).
+template <int NS, bool FOLD, int MINB = 2>
+void launch_vjp_pipe(const DevMesh& m, const AdjDev& a, StateF32 Q, const float* mu, const float* extra, float* out,
+                     float cSelf, float cExtra, float beta, double betaD, bool pdl, cudaStream_t st) {
+  using T = VjpTile<NS>;
+  static const int grid = [] {
+    cudaFuncSetAttribute(k_vjp_pipe_f32<NS, FOLD, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)T::kSmem);
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_vjp_pipe_f32<NS, FOLD, MINB>, kVTile, T::kSmem) !=
+            cudaSuccess ||
+        per < 1)
+      per = 1;
+    return (sms > 0 ? sms : 1) * per;
+  }();
+  const int tiles = (m.n + kVTile - 1) / kVTile;
+  launch_k(pdl, k_vjp_pipe_f32<NS, FOLD, MINB>, tiles < grid ? tiles : grid, kVTile, T::kSmem, st, m, a, Q, mu,
+           extra, out, cSelf, cExtra, beta, betaD);
+}
+
+// CTAs per SM of the folded interior VJP: 2 (128 registers), or 3 with
+// HG_VJP_MINB=3 (80 registers, some spilled); read once per process.
+int vjp_fold_minb() {
+  static const int v = [] {
+    const char* e = std::getenv("HG_VJP_MINB");
+    return (e && std::strcmp(e, "3") == 0) ? 3 : 2;
+  }();
+  return v;
+}
+
 // pdl: launched as the programmatic dependent of the boundary VJP just before it.
 template <int NS>
 void launch_vjp_interior(const DevMesh& m, const AdjDev& a, StateF32 Q, const float* mu, const float* extra,
                          float* out, float cSelf, float cExtra, float beta, bool pdl, cudaStream_t st) {
-  auto a16 = [](const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; };
   if constexpr (NS <= 4) {
-    if (!vjp_gather_forced() && m.SLp && m.halo && a16(m.SLp) && a16(m.CP) && a16(m.CS) && a16(Q.x)) {
-      using T = VjpTile<NS>;
-      static const int grid = [] {
-        cudaFuncSetAttribute(k_vjp_pipe_f32<NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T::kSmem);
-        int dev = 0, sms = 0, per = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_vjp_pipe_f32<NS>, kVTile, T::kSmem) != cudaSuccess ||
-            per < 1)
-          per = 1;
-        return (sms > 0 ? sms : 1) * per;
-      }();
-      const int tiles = (m.n + kVTile - 1) / kVTile;
-      launch_k(pdl, k_vjp_pipe_f32<NS>, tiles < grid ? tiles : grid, kVTile, T::kSmem, st, m, a, Q, mu, extra, out,
-               cSelf, cExtra, beta);
+    if (pipe_usable(m, Q)) {
+      launch_vjp_pipe<NS, false>(m, a, Q, mu, extra, out, cSelf, cExtra, beta, (double)beta, pdl, st);
       return;
     }
   }
@@ -616,6 +852,53 @@ int launch_vjp_ns(const DevMesh& m, const AdjDev& a, StateF32 Q, const float* mu
   return 3;
 }
 }  // namespace
+
+bool vjp_fold_usable(const DevMesh& m, const AdjDev& a, StateF32 Q) {
+  static const bool off = [] {   // HG_VJP_FOLD=0: the separate boundary and combine kernels
+    const char* e = std::getenv("HG_VJP_FOLD");
+    return e && std::strcmp(e, "0") == 0;
+  }();
+  return !off && pipe_usable(m, Q) && a.bfSlot && a.tileGrp && a.grpTile && m.nInlet <= kFoldMaxGroups;
+}
+
+int launch_bnd_jac_f32(const DevMesh& m, const AdjDev& a, const float4* X, int nStates, const double* tot,
+                       size_t totStride, float4* J, cudaStream_t st) {
+  const int64_t work = (int64_t)nStates * m.nbf;
+  if (work <= 0) return 0;
+  k_bnd_jac_f32<<<(unsigned)((work + 127) / 128), 128, 0, st>>>(m, a, X, nStates, tot, totStride, J);
+  return 1;
+}
+
+int launch_probe_seg_f32(const DevMesh& m, const float4* X, int s0, int sFirst, int nSteps, const ProbeCsr& pc,
+                         const int32_t* probes, const double* obs, int32_t np, double scale, float* seeds,
+                         double* lossPart, cudaStream_t st) {
+  if (nSteps <= 0 || np <= 0) return 0;
+  k_probe_seg_f32<<<nSteps, 256, 0, st>>>(m, X, s0, sFirst, pc, probes, obs, np, scale, seeds, lossPart);
+  return 1;
+}
+int launch_loss_parts(const AdjDev& a, const double* lossPart, int sLast, cudaStream_t st) {
+  if (sLast < 1) return 0;
+  k_loss_parts<<<1, 32, 0, st>>>(a, lossPart, sLast);
+  return 1;
+}
+
+int launch_vjp_f32_folded(const DevMesh& m, const AdjDev& a, StateF32 Q, const float* mu, const float* extra,
+                          float* out, float cSelf, float cExtra, double betaD, cudaStream_t st, const ProbeJob* pj) {
+  const float beta = (float)betaD;
+  const bool three = vjp_fold_minb() == 3;
+  if (m.nslot <= 3) {
+    if (three) launch_vjp_pipe<3, true, 3>(m, a, Q, mu, extra, out, cSelf, cExtra, beta, betaD, true, st);
+    else launch_vjp_pipe<3, true, 2>(m, a, Q, mu, extra, out, cSelf, cExtra, beta, betaD, true, st);
+  } else {
+    if (three) launch_vjp_pipe<4, true, 3>(m, a, Q, mu, extra, out, cSelf, cExtra, beta, betaD, true, st);
+    else launch_vjp_pipe<4, true, 2>(m, a, Q, mu, extra, out, cSelf, cExtra, beta, betaD, true, st);
+  }
+  if (pj && pj->np > 0) {
+    launch_k(true, k_probe_f32, 1, 256, 0, st, m, a, Q, out, pj->pc, pj->probes, pj->obs, pj->np, pj->scale);
+    return 2;
+  }
+  return 1;
+}
 
 int launch_vjp_f32(const DevMesh& m, const AdjDev& a, StateF32 Q, const float* mu, const float* extra, float* out,
                    float cSelf, float cExtra, double betaD, cudaStream_t st, const ProbeJob* pj) {

@@ -43,6 +43,30 @@ struct AdjDev {
   unsigned int* tileTicket = nullptr;
   // [nBndCells] the probe cell (ProbeCsr index) each boundary cell is, or -1.
   int32_t* bndProbe = nullptr;
+  // Boundary faces folded into the pipelined interior VJP (no boundary or
+  // combine launch per stage): every boundary face's flux Jacobian at each
+  // stage state of a segment comes from one launch per segment
+  // (k_bnd_jac_f32); the VJP of a stage contracts it with the cell's
+  // cotangent.  6 float4 per face: float 7 r + d is dF_r / dp_d, r over
+  // (F_xi, F_hu, F_hv), d over (own xi, hu, hv, n, zb, inlet Q, total_A).
+  // bndJ: the current VJP's state.  The inlet groups' total_A and Q
+  // cotangents are summed by the CTAs whose tiles hold inlet cells (tileGrp:
+  // per tile a bit per group); the CTA of tile grpTile[g] adds group g's Q
+  // cotangent to gQ.
+  const float4* bndJ = nullptr;
+  const int2* bfSlot = nullptr;       // [nbf] {device cell, slot}
+  const float4* inletW = nullptr;     // [inlet CSR entries] {face as bits, cell as bits, len / area, 0}
+  const uint32_t* tileGrp = nullptr;  // [interior VJP tiles]
+  const int32_t* grpTile = nullptr;   // [nInlet]
+  // Probe terms with the boundary faces folded: a segment's seeds (per step
+  // with probes, per distinct probe cell) and loss sums come from one launch
+  // (k_probe_seg_f32); the stage-1 VJP adds its step's seeds (probeSeed, null
+  // for none) to the probe cells of each tile it computes (tileProbeOff/U: per
+  // tile a CSR of distinct-probe-cell indices; probeCell: their cells).
+  const float* probeSeed = nullptr;
+  const int32_t* tileProbeOff = nullptr;
+  const int32_t* tileProbeU = nullptr;
+  const int32_t* probeCell = nullptr;
   // The gradients the caller asked for: the FP32C VJP accumulates the n or
   // the bed (S0, exit-H) terms only when wanted.
   int32_t wantN = 1, wantZb = 1;
@@ -73,6 +97,9 @@ struct AdjDev {
   unsigned int* udeTicket = nullptr;
 };
 
+// Inlet groups the folded boundary VJP handles (tileGrp's bits).
+constexpr int kFoldMaxGroups = 8;
+
 // Grid of the network VJP (one warp per block, a fixed grid so that the
 // per-block partial sums and their reduction have a fixed order).
 constexpr int kUdeGrid = 1216;
@@ -101,6 +128,27 @@ void launch_probe_adjoint_f64(const DevMesh& m, const double* Q, double* mu, con
 // boundary-face kernel, the interior kernel beside it (a programmatic
 // dependent launch), then the combine kernel.  beta = betaD as FP32.
 // Returns the launches made.
+// The folded boundary VJP (see AdjDev::bndJ): usable with the pipelined
+// interior kernel, at most kFoldMaxGroups inlet groups and the tables built.
+bool vjp_fold_usable(const DevMesh& m, const AdjDev& a, StateF32 Q);
+// The boundary faces' flux Jacobians of nStates consecutive FP32C states
+// (state s: records X + s n, inlet totals tot + s totStride) into J.
+int launch_bnd_jac_f32(const DevMesh& m, const AdjDev& a, const float4* X, int nStates, const double* tot,
+                       size_t totStride, float4* J, cudaStream_t st);
+// The probe seeds (seeds + (s - sFirst) nCells, per distinct probe cell) and
+// loss sums (lossPart[s - 1]) of steps s = sFirst .. sFirst + nSteps - 1 of a
+// segment starting at step s0: the state after step s - 1 has records
+// X + (s - s0) n, its observations obs + (s - 1) np.
+int launch_probe_seg_f32(const DevMesh& m, const float4* X, int s0, int sFirst, int nSteps,
+                         const struct ProbeCsr& pc, const int32_t* probes, const double* obs, int32_t np,
+                         double scale, float* seeds, double* lossPart, cudaStream_t st);
+// loss += lossPart[s - 1] for s = sLast down to 1 (the reverse sweep's order).
+int launch_loss_parts(const AdjDev& a, const double* lossPart, int sLast, cudaStream_t st);
+// One stage's VJP with the boundary faces folded in (a.bndJ of Q): the
+// interior kernel, and the probe kernel when pj has probes.
+int launch_vjp_f32_folded(const DevMesh& m, const AdjDev& a, StateF32 Q, const float* mu, const float* extra,
+                          float* out, float cSelf, float cExtra, double beta, cudaStream_t st,
+                          const struct ProbeJob* pj);
 int launch_vjp_f32(const DevMesh& m, const AdjDev& a, StateF32 Q, const float* mu, const float* extra, float* out,
                    float cSelf, float cExtra, double betaD, cudaStream_t st, const struct ProbeJob* pj = nullptr);
 // Probes grouped by cell: cell[u] (distinct, device order) holds probes idx[off[u] .. off[u+1]).
