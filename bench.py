@@ -38,6 +38,12 @@ UNIT = "cell-updates/s"
 # RK2 cell-update (two stages + the stage-2 re-read of Q^n).
 BYTES_STAGE = {"fp32c": (72.0, 20.0), "fp64": (96.0, 32.0)}   # (per cell, per face)
 BYTES_STEP_EXTRA = {"fp32c": 24.0, "fp64": 24.0}
+# The FP32C interior VJP of one stage (stage-2 form): per cell the state,
+# parameter and source records (3 x 16 B), the cotangent in and out (2 x 12 B)
+# and the n, S0x, S0y accumulators (3 compensated float pairs read and
+# written, 48 B); per face its two slot records (2 x 16 B).
+BYTES_VJP_FP32C = (120.0, 32.0)
+VJP_PROFILE = "k_vjp_pipe_f32_fold_river_tri_1M.md"
 
 
 def load_peaks():
@@ -57,9 +63,11 @@ STAGE_KERNELS = {0: ("k_stage_f32 (one block per 256-cell tile)", "k_stage_f32_r
                      "k_stage_face_f32_river_tri_1M.md")}
 
 
-def profile_traffic(precision, kernel=0):
-    """Per-cell DRAM bytes of the stage kernel from the committed ncu summary, if any."""
-    name = STAGE_KERNELS[kernel][1] if precision == "fp32c" else "k_stage_f64_river_tri_1M.md"
+def profile_traffic(precision, kernel=0, name=None):
+    """Per-cell DRAM bytes of the stage kernel (or of the profile `name`) from
+    the committed ncu summary, if any."""
+    if name is None:
+        name = STAGE_KERNELS[kernel][1] if precision == "fp32c" else "k_stage_f64_river_tri_1M.md"
     if name is None:
         return None
     p = os.path.join(ROOT, "profiles", name)
@@ -599,6 +607,13 @@ def run_ours(args):
             "grad_zb_field_rel_linf": float(np.abs(g32["g_zb"] - g64["g_zb"]).max() / np.abs(g64["g_zb"]).max()),
             "loss_rel": float(abs(g32["loss"] - g64["loss"]) / abs(g64["loss"])),
         }
+        # The interior VJP kernel alone (roofline of the reverse sweep's dominant kernel).
+        c32 = ctxs["fp32c"]
+        c32.upload(case["Q0"])
+        adj["vjp_ms"] = c32.time_vjp_kernel(20, True)
+        adj["fp32c"]["ms_per_step"] = adj["fp32c"]["seconds"] * 1e3 / args.adj_steps
+        adj["fp32c"]["reverse_over_forward"] = (adj["fp32c"]["ms_per_step"] - out["fp32c"]["ms"] / out["fp32c"]["steps"]) \
+            / (out["fp32c"]["ms"] / out["fp32c"]["steps"])
         adj["config"] = (f"{args.adj_steps} fixed-dt steps (dt = half the initial CFL step), checkpoint spacing 50 "
                          "widened by the automatic stage-state tape (all steps kept where they fit in HBM), "
                          f"{len(probes)} probes (half on the pool rim, half at the inlet), loss = mean squared "
@@ -623,6 +638,15 @@ def run_ours(args):
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": None if tr is None else tr * N, "kernel": STAGE_KERNELS[kern][0] + ", one RK2 stage pass",
             "algorithmic_bytes_per_launch": bytes_stage, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)"}
+    if adj and "vjp_ms" in adj:
+        bytes_vjp = (BYTES_VJP_FP32C[0] + nfaces_cell * BYTES_VJP_FP32C[1]) * N
+        a_vjp = bytes_vjp / (adj["vjp_ms"] * 1e-3) / 1e9
+        tv = profile_traffic("fp32c", name=VJP_PROFILE)
+        adj["roofline"] = {"bound": "hbm", "achieved": a_vjp, "peak": peak, "unit": "GB/s", "frac": a_vjp / peak,
+                           "traffic": None if tv is None else tv * N,
+                           "kernel": "k_vjp_pipe_f32 (interior VJP of one stage, boundary faces folded in)",
+                           "algorithmic_bytes_per_launch": bytes_vjp,
+                           "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)"}
     fp64_bytes = (BYTES_STAGE["fp64"][0] + nfaces_cell * BYTES_STAGE["fp64"][1]) * N
     cpu = None
     if not args.no_cpu:

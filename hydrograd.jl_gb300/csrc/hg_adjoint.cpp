@@ -315,6 +315,59 @@ F32States f32_view(double* base, size_t states, int n) {
 
 }  // namespace
 
+int adjoint_time_vjp(hg_ctx* c, int32_t reps, int32_t flushL2, double* avgMs) {
+  if (c->precision != HG_FP32C || c->dm.res.kind != kResConstant || c->dm.nHydro != 0)
+    return fail(c, HG_ERR_UNSUPPORTED,
+                "hg_time_vjp_kernel: the FP32C VJP with constant resistance and inlet discharges only");
+  int rc = setup(c);
+  if (rc) return rc;
+  AdjointBuffers* b = c->adj;
+  AdjDev a = b->dev;
+  a.wantN = a.wantZb = 1;
+  a.resChain = a.udeChain = 0;
+  const StateF32 X{c->XA, c->XQA};
+  if (!vjp_fold_usable(c->dm, a, X))
+    return fail(c, HG_ERR_UNSUPPORTED, "hg_time_vjp_kernel: the pipelined interior VJP cannot run on this mesh");
+  cudaStream_t st = c->stream;
+  const int N = c->n;
+  if (b->bndJCap < 1) {
+    cudaFree(b->bndJ);
+    b->bndJ = nullptr;
+    ADJ_CUDA(c, cudaMalloc(&b->bndJ, (size_t)std::max(c->dm.nbf, 1) * 6 * sizeof(float4)));
+    b->bndJCap = 1;
+  }
+  DevMesh m = c->dm;
+  m.totalA = c->d_tot;   // conveyance totals of the resident state
+  launch_inlet_total_f32(m, c->ds, X, st);
+  launch_bnd_jac_f32(m, a, X.x, 1, c->d_tot, 0, b->bndJ, st);
+  a.bndJ = b->bndJ;
+  float* mu = reinterpret_cast<float*>(b->mu1);
+  float* out = reinterpret_cast<float*>(b->mu2);
+  ADJ_CUDA(c, cudaMemsetAsync(mu, 0x3a, (size_t)3 * N * sizeof(float), st));   // about 7e-4 each
+  ADJ_CUDA(c, cudaMemsetAsync(a.accF, 0, (size_t)4 * N * sizeof(float2), st));
+  ADJ_CUDA(c, cudaMemsetAsync(a.gQ, 0, std::max(c->dm.nInlet, 1) * sizeof(double), st));
+  c->launches += 2;
+  cudaEvent_t e0, e1;
+  ADJ_CUDA(c, cudaEventCreate(&e0));
+  ADJ_CUDA(c, cudaEventCreate(&e1));
+  double total = 0.0;
+  for (int i = 0; i < reps; ++i) {
+    if (flushL2) c->launches += launch_flush(c->flushBuf, c->flushBytes, st);
+    cudaEventRecord(e0, st);
+    c->launches += launch_vjp_f32_folded(m, a, X, mu, nullptr, out, 0.5f, 0.0f, 1e-3, st, nullptr);
+    cudaEventRecord(e1, st);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    total += ms;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  *avgMs = total / reps;
+  ADJ_CUDA(c, cudaGetLastError());
+  return HG_OK;
+}
+
 int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int32_t C, const int32_t* probeCells,
                           const double* obs, int32_t P, double* loss, double* gManning, double* gZb, double* gInlet,
                           double* Qfinal, const FinalObs* fo, double* parts) {

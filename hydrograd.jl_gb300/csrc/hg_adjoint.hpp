@@ -25,6 +25,11 @@ int adjoint_loss_and_grad(hg_ctx* ctx, const double* Q0, int32_t nsteps, double 
                           const int32_t* probe_cells, const double* obs, int32_t n_probe, double* loss,
                           double* g_manning_cells, double* g_zb, double* g_inletq, double* Q_final,
                           const FinalObs* fo = nullptr, double* parts = nullptr);
+// Mean duration of n launches of the FP32C interior VJP kernel (boundary
+// faces folded, the stage-2 form: out = 0.5 mu + beta J^T mu) on the resident
+// state, CUDA events on the context's stream, L2 flushed between launches
+// when flushL2.
+int adjoint_time_vjp(hg_ctx* ctx, int32_t n, int32_t flushL2, double* avgMs);
 void adjoint_release(hg_ctx* ctx);
 // Free the stage-state tape and checkpoint buffers (the next gradient call allocates what it needs).
 void adjoint_release_tape(hg_ctx* ctx);

@@ -1300,6 +1300,12 @@ int hg_time_stage_kernel(hg_ctx* ctx, int32_t n, int32_t flush_l2, double* avg_m
   return HG_OK;
 }
 
+int hg_time_vjp_kernel(hg_ctx* ctx, int32_t n, int32_t flush_l2, double* avg_ms) {
+  if (!ctx || n <= 0 || !avg_ms) return fail(ctx, HG_ERR_ARG, "hg_time_vjp_kernel: bad argument");
+  cudaSetDevice(ctx->device);
+  return adjoint_time_vjp(ctx, n, flush_l2, avg_ms);
+}
+
 int hg_set_adjoint_tape(hg_ctx* ctx, int64_t bytes) {
   if (!ctx) return fail(ctx, HG_ERR_ARG, "hg_set_adjoint_tape: null context");
   cudaSetDevice(ctx->device);

@@ -108,6 +108,7 @@ SIGNATURES = {
     "hg_set_dt_min": [_vp, ctypes.c_double],
     "hg_final_vjp": [_vp, _dp, ctypes.c_int32, ctypes.c_double, ctypes.c_int32, _dp, _dp, _dp, _dp, _dp],
     "hg_time_stage_kernel": [_vp, ctypes.c_int32, ctypes.c_int32, _dp],
+    "hg_time_vjp_kernel": [_vp, ctypes.c_int32, ctypes.c_int32, _dp],
     "hg_flush_l2": [_vp],
     "hg_advance_timed": [_vp, ctypes.c_int32, ctypes.c_double, ctypes.c_double, ctypes.c_int32, _dp],
     "hg_rhs_device_noalloc": [_vp, _vp, _vp, _vp, _vp],

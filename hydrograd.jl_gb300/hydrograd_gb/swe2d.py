@@ -357,6 +357,12 @@ class SWE2D:
         self._chk(lib().hg_time_stage_kernel(self.h, int(n), 1 if flush_l2 else 0, _d(ms)))
         return float(ms[0])
 
+    def time_vjp_kernel(self, n=10, flush_l2=True):
+        """Mean ms of the FP32C interior VJP kernel alone (hg_time_vjp_kernel)."""
+        ms = np.zeros(1)
+        self._chk(lib().hg_time_vjp_kernel(self.h, int(n), 1 if flush_l2 else 0, _d(ms)))
+        return float(ms[0])
+
     def flush_l2(self):
         self._chk(lib().hg_flush_l2(self.h))
 

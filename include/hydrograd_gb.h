@@ -412,6 +412,11 @@ int hg_launch_count(const hg_ctx* ctx, int64_t* count);
 /* Time n launches of the stage kernel alone with CUDA events on the context's stream,
  * flushing L2 between launches when flush_l2 != 0; avg_ms receives the mean duration. */
 int hg_time_stage_kernel(hg_ctx* ctx, int32_t n, int32_t flush_l2, double* avg_ms);
+/* The same for the FP32C adjoint's interior VJP kernel (boundary faces folded
+ * in; one stage-2 VJP of the resident state with a constant cotangent):
+ * HG_ERR_UNSUPPORTED for FP64 contexts, a state-dependent resistance, an inlet
+ * hydrograph or a mesh the pipelined kernel cannot take. */
+int hg_time_vjp_kernel(hg_ctx* ctx, int32_t n, int32_t flush_l2, double* avg_ms);
 /* Write a device buffer larger than L2 (used between timed iterations). */
 int hg_flush_l2(hg_ctx* ctx);
 /* nsteps SSP-RK2 steps on the resident state, each bracketed by CUDA events on
