@@ -287,7 +287,11 @@ def run_dry_start(args, device):
     N = len(case["cell_node_count"])
     hst = case["wstill"] - case["zb_cells"]
     K = args.dry_steps
-    out, final = {"cells": N, "steps": K}, {}
+    # The first film the scheme seeds differently in FP32C and FP64 comes
+    # between steps 50 and 100 on this mesh; until then FP32C keeps to FP64
+    # within the 1e-5 contract at the fronts.
+    SEED_FREE = min(50, K)
+    out, final, early = {"cells": N, "steps": K}, {}, {}
     for prec in ("fp32c", "fp64"):
         c = make_ctx(case, prec, device)
         if prec == "fp32c":
@@ -300,6 +304,7 @@ def run_dry_start(args, device):
             ms = c.advance_timed(K, dt=dt, flush_l2=True)
             out["fwd"] = {"value": N * K / (ms * 1e-3), "ms_per_step": ms / K}
         final[prec], _ = c.integrate(case["Q0"], K, dt=out["dt"])
+        early[prec], _ = c.integrate(case["Q0"], SEED_FREE, dt=out["dt"])
         c.close()
     a, b = final["fp32c"], final["fp64"]
     wet0 = case["Q0"][:N] + hst > 1.5e-3
@@ -317,9 +322,17 @@ def run_dry_start(args, device):
         "front_block_rel_linf": [float(np.abs(a[j * N:(j + 1) * N][front] - b[j * N:(j + 1) * N][front]).max()
                                        / blk[j]) if len(front) else 0.0 for j in range(3)],
         "wet_dry_decisions_differing": int((wet_a != wet_b).sum())}
+    a0, b0 = early["fp32c"], early["fp64"]
+    out["error_fp32c_vs_fp64_seed_free"] = {
+        "steps": SEED_FREE, "state_rel_linf": float(np.abs(a0 - b0).max() / np.abs(b0).max()),
+        "block_rel_linf": [float(np.abs(a0[j * N:(j + 1) * N] - b0[j * N:(j + 1) * N]).max()
+                                 / max(np.abs(b0[j * N:(j + 1) * N]).max(), 1e-3 * np.abs(b0).max()))
+                           for j in range(3)]}
     out["config"] = ("configuration 2 as written: 1M-cell reach dry except a 1.5 m pool at the inlet, moving "
                      "wet/dry fronts; fixed dt = the initial CFL-0.01 step (the reference scheme diverges on a dry "
-                     "bed at CFL-sized steps); FP32C vs FP64 after the same steps")
+                     "bed at CFL-sized steps); FP32C vs FP64 after the same steps, and over the first steps, before "
+                     "the scheme seeds its first film differently in the two precisions (at the fronts it "
+                     "amplifies rounding-sized differences: FP64 runs perturbed by 1e-7 per step part by 1e-2)")
     return out
 
 

@@ -102,6 +102,7 @@ struct GlobalSrc {
     return VjpNbr{__ldg(&Q.x[nb]), __ldg(&m.CP[nb]), __ldg(&m.CS[nb]).z, mu[nb], mu[m.n + nb],
                   mu[2 * (size_t)m.n + nb]};
   }
+  __device__ int cell(int nb) const { return nb; }   // the neighbour's cell id
 };
 
 // The VJP of one stage at cell j (interior faces: 3-direction duals of the
@@ -143,8 +144,10 @@ __device__ __forceinline__ void vjp_cell(const DevMesh& m, const AdjDev& a, int 
         const Side<F3> L3 = seeded<F3>(L.s, -1);
         const Side<F3> R3 = constant<F3>(R.s);
         const F3 dxi = (R3.xi - L3.xi) + F3(R.xlo - L.xlo);
+        // the forward pass's wall test (bank_wall_f64), so that the same branch is differentiated
+        const int bank = R.s.dry ? bank_wall_f64(m, L.s.xi, L.xlo, j, src.cell(nb)) : -1;
         F3 F[3];
-        riemann_flux<F3>(m.riemann, L3, R3, dxi, F3(m.gf), F3(nx), F3(ny), F3(m.hsmf), F);
+        riemann_flux<F3>(m.riemann, L3, R3, dxi, F3(m.gf), F3(nx), F3(ny), F3(m.hsmf), F, bank);
         g0 += w0 * F[0].d[0] + w1 * F[1].d[0] + w2 * F[2].d[0];
         g1 += w0 * F[0].d[1] + w1 * F[1].d[1] + w2 * F[2].d[1];
         g2 += w0 * F[0].d[2] + w1 * F[1].d[2] + w2 * F[2].d[2];
@@ -272,6 +275,8 @@ struct TileSrc {
   const unsigned char* B;
   int tid;
   bool hasExtra;   // no cotangent carried in: the extra slab is not filled
+  int base;                  // the tile's first cell
+  const int32_t* haloIds;    // the tile's halo cell ids (DevMesh::halo)
   __device__ const float4* rec(uint32_t off) const { return reinterpret_cast<const float4*>(B + off); }
   __device__ const float* flt(uint32_t off) const { return reinterpret_cast<const float*>(B + off); }
   __device__ float4 x() const { return rec(VjpTile<NS>::kX)[tid]; }
@@ -290,6 +295,10 @@ struct TileSrc {
     return VjpNbr{rec(VjpTile<NS>::kHX)[h], rec(VjpTile<NS>::kHP)[h], flt(VjpTile<NS>::kHA)[h],
                   flt(VjpTile<NS>::kHM)[h], flt(VjpTile<NS>::kHM)[kHaloMax + h],
                   flt(VjpTile<NS>::kHM)[2 * kHaloMax + h]};
+  }
+  __device__ int cell(int nb) const {   // the neighbour's cell id
+    const int li = nb & 511;
+    return li < kVTile ? base + li : __ldg(&haloIds[li - kVTile]);
   }
 };
 
@@ -456,8 +465,10 @@ __global__ void __launch_bounds__(kVTile, MINB) k_vjp_pipe_f32(DevMesh m, AdjDev
     }
     const int j = t * kVTile + tid;
     if (j < n)
-      vjp_cell<NS, FOLD>(m, a, j, TileSrc<NS>{smem + b * T::kBuf, tid, extra != nullptr}, out, cSelf, cExtra, beta,
-                         sGrp);
+      vjp_cell<NS, FOLD>(m, a, j,
+                         TileSrc<NS>{smem + b * T::kBuf, tid, extra != nullptr, t * kVTile,
+                                     m.halo + (size_t)t * kHaloMax},
+                         out, cSelf, cExtra, beta, sGrp);
     __syncthreads();   // buffer b is refilled at the top of the next iteration
     if constexpr (FOLD) {   // the step's probe seeds, after the tile's own cotangents
       if (a.probeSeed)
@@ -543,8 +554,11 @@ __global__ void __launch_bounds__(64) k_vjp_bnd_f32(DevMesh m, AdjDev a, StateF3
       if (L.s.dry) ex.d[0] = -1.0f;   // excess = h_small - (xi + hstill) for a dry cell
       F7 dxi = (R7.h - L7.h) + ex;
       if (type == kBcExitH && !R7.dry) dxi.v = m.bfExitRel[bf] - (L.s.xi + L.xlo);   // as the forward pass
+      int bank = -1;   // the forward pass's wall test (bank_wall_f64)
+      if (type == kBcExitH && L.s.dry != R7.dry)
+        bank = L.s.dry ? bank_exit_f64(m, grp, j) : bank_wall_f64(m, L.s.xi, L.xlo, j, j);
       F7 F[3];
-      riemann_flux<F7>(m.riemann, L7, R7, dxi, F7(m.gf), F7(nx), F7(ny), F7(m.hsmf), F);
+      riemann_flux<F7>(m.riemann, L7, R7, dxi, F7(m.gf), F7(nx), F7(ny), F7(m.hsmf), F, bank);
       float c[7];
 #pragma unroll
       for (int d = 0; d < 7; ++d) c[d] = w0 * F[0].d[d] + w1 * F[1].d[d] + w2 * F[2].d[d];
@@ -598,8 +612,11 @@ __global__ void __launch_bounds__(128) k_bnd_jac_f32(DevMesh m, AdjDev a, const 
   if (L.s.dry) ex.d[0] = -1.0f;   // excess = h_small - (xi + hstill) for a dry cell
   F7 dxi = (R7.h - L7.h) + ex;
   if (type == kBcExitH && !R7.dry) dxi.v = m.bfExitRel[bf] - (L.s.xi + L.xlo);   // as the forward pass
+  int bank = -1;   // the forward pass's wall test (bank_wall_f64)
+  if (type == kBcExitH && L.s.dry != R7.dry)
+    bank = L.s.dry ? bank_exit_f64(m, grp, j) : bank_wall_f64(m, L.s.xi, L.xlo, j, j);
   F7 F[3];
-  riemann_flux<F7>(m.riemann, L7, R7, dxi, F7(m.gf), F7(nx), F7(ny), F7(m.hsmf), F);
+  riemann_flux<F7>(m.riemann, L7, R7, dxi, F7(m.gf), F7(nx), F7(ny), F7(m.hsmf), F, bank);
   float v[24];
 #pragma unroll
   for (int r = 0; r < 3; ++r)

@@ -56,14 +56,20 @@ struct Side {
 // Roe flux through a face with unit normal (nx, ny) pointing from L to R.
 // dxi = xiR - xiL is passed in so that the FP32 path can form it from its
 // hi/lo state pairs without cancellation.
+// bank: the wall test of a face with one dry side, (h_wet + zb_wet) <
+// (zb_dry + hmin), taken by the caller (1 / 0), or -1: taken here from L and R.
+// The FP32 path passes the FP64 decision (bank_wall_f64): with zb rounded to
+// FP32 its own test would differ whenever a front's surface is within ~1e-7 m
+// of the dry bank.
 template <class T>
-__device__ __forceinline__ void roe_flux(Side<T> L, Side<T> R, T dxi, T g, T nx, T ny, T hmin, T F[3]) {
+__device__ __forceinline__ void roe_flux(Side<T> L, Side<T> R, T dxi, T g, T nx, T ny, T hmin, T F[3],
+                                         int bank = -1) {
   if (L.dry && R.dry) {                                   // both dry
     F[0] = T(0); F[1] = T(0); F[2] = T(0);
     return;
-  } else if ((L.h + L.zb) < (R.zb + hmin) && R.dry) {     // wall: R <- mirrored L (xiR kept)
+  } else if (R.dry && (bank >= 0 ? bank != 0 : (L.h + L.zb) < (R.zb + hmin))) {   // wall: R <- mirrored L (xiR kept)
     R.h = L.h; R.hu = -L.hu; R.hv = -L.hv;
-  } else if ((R.h + R.zb) < (L.zb + hmin) && L.dry) {     // wall: L <- mirrored R (xiL kept)
+  } else if (L.dry && (bank >= 0 ? bank != 0 : (R.h + R.zb) < (L.zb + hmin))) {   // wall: L <- mirrored R (xiL kept)
     L.h = R.h; L.hu = -R.hu; L.hv = -R.hv;
   } else if (L.dry) {                                     // left dry: physical flux of R, h-based pressure
     T p = T(0.5) * g * smooth_pow2(R.h);
@@ -119,13 +125,14 @@ __device__ __forceinline__ void roe_flux(Side<T> L, Side<T> R, T dxi, T g, T nx,
 // and one-side-dry branches; only the wet-wet flux differs:
 //   F_L (S_L >= 0), F_R (S_R <= 0), else (S_R F_L - S_L F_R + S_L S_R dU) / (S_R - S_L).
 template <class T>
-__device__ __forceinline__ void hll_flux(Side<T> L, Side<T> R, T dxi, T g, T nx, T ny, T hmin, T F[3]) {
+__device__ __forceinline__ void hll_flux(Side<T> L, Side<T> R, T dxi, T g, T nx, T ny, T hmin, T F[3],
+                                         int bank = -1) {
   if (L.dry && R.dry) {
     F[0] = T(0); F[1] = T(0); F[2] = T(0);
     return;
-  } else if ((L.h + L.zb) < (R.zb + hmin) && R.dry) {
+  } else if (R.dry && (bank >= 0 ? bank != 0 : (L.h + L.zb) < (R.zb + hmin))) {
     R.h = L.h; R.hu = -L.hu; R.hv = -L.hv;
-  } else if ((R.h + R.zb) < (L.zb + hmin) && L.dry) {
+  } else if (L.dry && (bank >= 0 ? bank != 0 : (R.h + R.zb) < (L.zb + hmin))) {
     L.h = R.h; L.hu = -R.hu; L.hv = -R.hv;
   } else if (L.dry) {
     T p = T(0.5) * g * smooth_pow2(R.h);
@@ -172,12 +179,12 @@ __device__ __forceinline__ void hll_flux(Side<T> L, Side<T> R, T dxi, T g, T nx,
   }
 }
 
-// The face flux of the context's Riemann solver (DevMesh::riemann).
+// The face flux of the context's Riemann solver (DevMesh::riemann); bank as in roe_flux.
 template <class T>
 __device__ __forceinline__ void riemann_flux(int solver, const Side<T>& L, const Side<T>& R, T dxi, T g, T nx, T ny,
-                                             T hmin, T F[3]) {
-  if (solver == kRiemannHll) hll_flux<T>(L, R, dxi, g, nx, ny, hmin, F);
-  else roe_flux<T>(L, R, dxi, g, nx, ny, hmin, F);
+                                             T hmin, T F[3], int bank = -1) {
+  if (solver == kRiemannHll) hll_flux<T>(L, R, dxi, g, nx, ny, hmin, F, bank);
+  else roe_flux<T>(L, R, dxi, g, nx, ny, hmin, F, bank);
 }
 
 // Ghost state of a boundary face (bc_2D.jl:640-834) from the clamped state of

@@ -130,6 +130,27 @@ __device__ __forceinline__ void df_add2(float ah, float al, float bh, float bl, 
 
 __device__ __forceinline__ int32_t slot_nb(float4 s) { return __float_as_int(s.w); }
 
+// The Riemann solvers' wall test of a face whose sides differ in wetness,
+// (h_w + zb_w) < (zb_d + h_small) with w the wet cell and d the dry one
+// (swe_2D_solvers.jl:23-53), taken in FP64 as the FP64 path takes it: h_w from
+// the wet cell's xi pair and the FP64 hstill, both beds from the FP64 zb.  The
+// cell records hold zb in FP32 (rounded by up to 2.4e-7 m at 2-5 m of bed),
+// and an FP32 test would differ from the FP64 one whenever a front's surface is
+// within that distance of the dry bank -- for about one step of most front
+// crossings -- so that the two precisions flood a dry cell on different steps
+// and their states part at the fronts.  Faces with one dry side are few (the
+// fronts), so the FP64 loads and arithmetic cost nothing measurable.
+__device__ __forceinline__ int bank_wall_f64(const hg::DevMesh& m, float xh, float xl, int w, int d) {
+  const double hw = ((double)xh + (double)xl) + __ldg(&m.hst[w]);
+  return (hw + __ldg(&m.zb[w])) < (__ldg(&m.zb[d]) + m.hsm) ? 1 : 0;
+}
+// The same test for an exit-H face of cell c whose ghost is wet and c dry:
+// the ghost's depth WSE - zb (bc_2D.jl exit-H ghost) against its own bed.
+__device__ __forceinline__ int bank_exit_f64(const hg::DevMesh& m, int grp, int c) {
+  const double zb = __ldg(&m.zb[c]);
+  return ((m.exitWse[grp] - zb) + zb) < (zb + m.hsm) ? 1 : 0;
+}
+
 // Quantities of a wet cell that the Roe flux uses on every one of its faces,
 // formed once per cell: velocity, sqrt(h), pre-balanced pressure
 // p = g/2 (smooth_pow2(xi) + 2 xi hstill) and the advective flux tensor

@@ -42,13 +42,14 @@ inline int blocks_for(int n) { return (n + kBlock - 1) / kBlock; }
 // the context's at run time (DevMesh::riemann).
 template <bool LOC, int RS>
 __device__ __forceinline__ void one_face_f32(const DevMesh& m, const float4* __restrict__ X, const float4* sX,
-                                             const float4* sP, const float4* hX, const float4* hP, int base,
+                                             const float4* sP, const float4* hX, const float4* hP, int base, int c,
                                              const SideF32& L, const OwnF32& own, float2 hstPair, float4 sl, int32_t nb,
                                              const double* __restrict__ totalA, float man, int32_t* flags,
                                              float F[3]) {
   const float nx = sl.x, ny = sl.y;
   Side<float> R;
   float dxi, dhst = 0.0f;
+  int bank = -1;   // the wall test of a face with one dry side, in FP64 (bank_wall_f64)
   if (nb >= 0) {
     float4 xr, pr;
     if constexpr (LOC) {
@@ -74,6 +75,14 @@ __device__ __forceinline__ void one_face_f32(const DevMesh& m, const float4* __r
     R = r.s;
     dxi = (r.s.xi - L.s.xi) + (r.xlo - L.xlo);
     dhst = (pr.x - hstPair.x) + (pr.y - hstPair.y);   // hstill_R - hstill_L from the pairs
+    if (L.s.dry != r.s.dry) {   // a front face
+      int g = nb;               // the neighbour's cell id
+      if constexpr (LOC) {
+        const int li = nb & 511;
+        g = li < kBlock ? base + li : __ldg(&m.halo[(size_t)(base / kBlock) * kHaloMax + (li - kBlock)]);
+      }
+      bank = L.s.dry ? bank_wall_f64(m, r.s.xi, r.xlo, g, c) : bank_wall_f64(m, L.s.xi, L.xlo, c, g);
+    }
   } else {
     const int32_t bf = boundary_index(nb);
     const int32_t info = m.bfInfo[bf], type = info & 3, grp = info >> 2;
@@ -85,13 +94,15 @@ __device__ __forceinline__ void one_face_f32(const DevMesh& m, const float4* __r
     // ghost, from (WSE - zb) - hstill formed in FP64
     dxi = (R.h - L.s.h) + L.excess;
     if (type == kBcExitH && !R.dry) dxi = m.bfExitRel[bf] - (L.s.xi + L.xlo);
+    if (type == kBcExitH && L.s.dry != R.dry)   // (the other ghosts are as wet as their cell)
+      bank = L.s.dry ? bank_exit_f64(m, grp, c) : bank_wall_f64(m, L.s.xi, L.xlo, c, c);
   }
   const int rs = RS >= 0 ? RS : m.riemann;
   if (!L.s.dry && !R.dry) {
     if (rs == kRiemannHll) hll_flux_wet_f32(L.s, own, R, dxi, dhst, m.gf, nx, ny, F);
     else roe_flux_wet_f32(L.s, own, R, dxi, dhst, m.gf, nx, ny, F);
   } else {
-    riemann_flux<float>(rs, L.s, R, dxi, m.gf, nx, ny, m.hsmf, F);
+    riemann_flux<float>(rs, L.s, R, dxi, m.gf, nx, ny, m.hsmf, F, bank);
     F[1] -= own.p * nx;   // the own pressure shift (pressure_jump_f32)
     F[2] -= own.p * ny;
   }
@@ -109,7 +120,7 @@ __device__ __forceinline__ void face_sum_f32(const DevMesh& m, const float4* __r
     const int32_t nb = slot_nb(sl[k]);
     if (nb == kNoFace) continue;
     float F[3];
-    one_face_f32<LOC, RS>(m, X, sX, sP, hX, hP, base, L, own, hstPair, sl[k], nb, totalA, man, flags, F);
+    one_face_f32<LOC, RS>(m, X, sX, sP, hX, hP, base, c, L, own, hstPair, sl[k], nb, totalA, man, flags, F);
     const float len = sl[k].z;
     f0 = fmaf(F[0], len, f0);
     const float2 f12 = fma2(p2(F[1], F[2]), p2(len), p2(f1, f2));
@@ -664,10 +675,12 @@ __device__ __forceinline__ float face_pressure(const DevMesh& m, float xi, float
 }
 
 // Terms of face entry i (record rec) into C[2 i] (side a) and C[2 i + 1] (side b).
+// base: the tile's first cell; haloIds: the tile's halo cell ids (DevMesh::halo).
 template <int RS>
 __device__ __forceinline__ void face_terms(const DevMesh& m, const float4* R0, const float4* R1, const float4* R2,
                                            const float2* R3, float4* C, int i, float4 rec,
-                                           const double* __restrict__ totalA, int32_t* flags) {
+                                           const double* __restrict__ totalA, int32_t* flags, int base,
+                                           const int32_t* __restrict__ haloIds) {
   const int32_t w = __float_as_int(rec.w);
   const float nx = rec.x, ny = rec.y, len = rec.z;
   const int rs = RS >= 0 ? RS : m.riemann;
@@ -694,14 +707,20 @@ __device__ __forceinline__ void face_terms(const DevMesh& m, const float4* R0, c
       }
     } else {                                            // a dry side: each in-tile side from its own cell
       const Side<float> sa = face_side(a0, a1, a2, R3[a].x), sb = face_side(b0, b1, b2, R3[b].x);
+      int bank = -1;   // the wall test in FP64 (bank_wall_f64); the same from either side
+      if (sa.dry != sb.dry) {
+        const int ga = a < kBlock ? base + a : __ldg(&haloIds[a - kBlock]);
+        const int gb = b < kBlock ? base + b : __ldg(&haloIds[b - kBlock]);
+        bank = sa.dry ? bank_wall_f64(m, b0.x, b0.y, gb, ga) : bank_wall_f64(m, a0.x, a0.y, ga, gb);
+      }
       if (aOwn) {
         const float pa = face_pressure(m, a0.x, a0.z);
-        riemann_flux<float>(rs, sa, sb, dxi, m.gf, nx, ny, m.hsmf, F);
+        riemann_flux<float>(rs, sa, sb, dxi, m.gf, nx, ny, m.hsmf, F, bank);
         C[2 * i] = make_float4(F[0] * len, (F[1] - pa * nx) * len, (F[2] - pa * ny) * len, 0.0f);
       }
       if (bOwn) {
         const float pb = face_pressure(m, b0.x, b0.z);
-        riemann_flux<float>(rs, sb, sa, -dxi, m.gf, -nx, -ny, m.hsmf, F);
+        riemann_flux<float>(rs, sb, sa, -dxi, m.gf, -nx, -ny, m.hsmf, F, bank);
         C[2 * i + 1] = make_float4(F[0] * len, (F[1] + pb * nx) * len, (F[2] + pb * ny) * len, 0.0f);
       }
     }
@@ -718,6 +737,9 @@ __device__ __forceinline__ void face_terms(const DevMesh& m, const float4* R0, c
                                            type == kBcInletQ ? (float)totalA[grp] : 1.0f, m.bfLp23f[bf], a3.y);
   float dxi = (R.h - L.h) + a1.w;
   if (type == kBcExitH && !R.dry) dxi = m.bfExitRel[bf] - (a0.x + a0.y);
+  int bank = -1;
+  if (type == kBcExitH && L.dry != R.dry)
+    bank = L.dry ? bank_exit_f64(m, grp, base + a) : bank_wall_f64(m, a0.x, a0.y, base + a, base + a);
   const float pa = face_pressure(m, a0.x, a0.z);
   if (!L.dry && !R.dry) {
     OwnF32 o;
@@ -726,7 +748,7 @@ __device__ __forceinline__ void face_terms(const DevMesh& m, const float4* R0, c
     if (rs == kRiemannHll) hll_flux_wet_f32(L, o, R, dxi, 0.0f, m.gf, nx, ny, F);
     else roe_flux_wet_f32(L, o, R, dxi, 0.0f, m.gf, nx, ny, F);
   } else {
-    riemann_flux<float>(rs, L, R, dxi, m.gf, nx, ny, m.hsmf, F);
+    riemann_flux<float>(rs, L, R, dxi, m.gf, nx, ny, m.hsmf, F, bank);
     F[1] -= pa * nx;
     F[2] -= pa * ny;
   }
@@ -783,7 +805,8 @@ __global__ void __launch_bounds__(kBlock, MINB)
   cp_async_wait<0>();
   __syncthreads();
   // phase 2: the tile's faces
-  for (int i = tid; i < nf; i += kBlock) face_terms<RS>(m, R0, R1, R2, R3, C, i, sFL[i], totalIn, s.flags);
+  for (int i = tid; i < nf; i += kBlock)
+    face_terms<RS>(m, R0, R1, R2, R3, C, i, sFL[i], totalIn, s.flags, base, m.halo + (size_t)tile * kHaloMax);
   __syncthreads();
   // phase 3: each cell's terms in slot order, then the stage update
   float cand = INFINITY, hOut = 0.0f;

@@ -142,3 +142,48 @@ def test_films_spread_ahead_of_the_front_in_fp64():
     cx, cy = cell_centroids(case)
     assert films.sum() >= 10
     assert np.hypot(cx - 300.0, cy - 1000.0)[thin].max() > 1000.0
+
+
+def test_the_fronts_amplify_rounding_sized_perturbations():
+    """How far apart two runs at the fronts may be when their arithmetic differs.
+    FP64 runs of the dry-pool start (river_triangles(128, dry_land=True),
+    32,768 cells, fixed dt = the CFL-0.01 step), one of them with a seeded
+    relative perturbation added to the wet cells' depth and momenta after every
+    step: at 1e-7 -- FP32's rounding -- the two part by about 1e-2 of the
+    state within 20 steps, because a perturbation of that size decides whether
+    a dry cell takes a film this step or a later one (the films of the test
+    above; a film then grows to centimetres under its neighbour's one-sided
+    pressure); at 1e-14 they stay 1e-13 apart.  The FP32C path's flux
+    arithmetic rounds at 1e-7, so at dry fronts it departs from FP64 by this
+    much at the first film it seeds differently; on wet states it keeps to
+    FP64 within 2e-7 over 2,000 steps."""
+    case = river_triangles(n=128, dry_land=True)
+    N = len(case["cell_node_count"])
+    hst = case["wstill"] - case["zb_cells"]
+    o = Oracle(case)
+    o.set_wstill(case["wstill"])
+    o.set_manning_cells(case["manning_zones"][case["mat_id"]])
+    o.set_inlet_q(case["inlet_q"])
+    o.set_exit_wse(case["exit_wse"])
+    dt = o.cfl_dt(case["Q0"], 0.01)
+    steps = 20
+
+    def run(amp):
+        rng = np.random.default_rng(7)
+        Q = case["Q0"].copy()
+        for _ in range(steps):
+            Q = o.rk2(Q, 1, dt=dt, nthreads=THREADS)
+            if amp > 0.0:
+                wet = Q[:N] + hst > 1.0e-3
+                nw = int(wet.sum())
+                h = Q[:N][wet] + hst[wet]
+                Q[:N][wet] = h * (1.0 + amp * rng.standard_normal(nw)) - hst[wet]
+                Q[N:2 * N][wet] *= 1.0 + amp * rng.standard_normal(nw)
+                Q[2 * N:][wet] *= 1.0 + amp * rng.standard_normal(nw)
+        return Q
+
+    clean = run(0.0)
+    scale = np.abs(clean).max()
+    part = {amp: np.abs(run(amp) - clean).max() / scale for amp in (1e-7, 1e-14)}
+    assert part[1e-7] > 1e-3
+    assert part[1e-14] < 1e-11
