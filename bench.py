@@ -463,9 +463,9 @@ ENSEMBLE_SIZES = (5000, 10000, 20000, 40000, 60000, 100000, 150000, 200000)
 
 def run_ensemble(args, device):
     """hg_ensemble_create over 8 meshes x 32 members (about 18.7 M member-cells):
-    per member zone n ~ U[0.02, 0.06] and inlet Q ~ U[100, 800]; all members
-    share the CFL step (the smallest member's).  FP32C forward steps, then one
-    forward+adjoint with 8 probes per member."""
+    per member zone n ~ U[0.02, 0.06] and inlet Q ~ U[100, 800]; each member
+    takes its own CFL step and keeps its own clock.  FP32C forward steps, then
+    one forward+adjoint (fixed dt) with 8 probes per member."""
     from hydrograd_gb import SWE2DEnsemble
     from hydrograd_gb.workloads import Stream, probes_and_perturbation, river_triangles
     meshes = [river_triangles(n=int(round((s / 2) ** 0.5))) for s in ENSEMBLE_SIZES]
@@ -639,7 +639,8 @@ def run_ours(args):
     if args.ens_steps > 0:
         ens = run_ensemble(args, local)
         ens["config"] = ("configuration 4: 8 reach meshes x %d members, per-member zone n and inlet Q, "
-                         "FP32C, shared CFL 0.4 step, L2 flushed before every timed step" % args.ens_members)
+                         "FP32C, each member on its own CFL 0.4 step, L2 flushed before every timed step"
+                         % args.ens_members)
     if rank != 0:
         return
     peak, peak_kind = load_peaks()
