@@ -27,6 +27,7 @@
 
 #include "hg_adjoint_state.hpp"
 #include "hg_ctx.hpp"
+#include "hg_tsit5.hpp"
 
 namespace hg {
 
@@ -62,6 +63,7 @@ struct AdjointBuffers {
   size_t probeSeedCap = 0;
   double* lossPart = nullptr;     // folded: the probe loss sum of each step's state [K]
   size_t lossPartCap = 0;
+  double* tsit5 = nullptr;        // fixed-step Tsit5 adjoint: kTsit5Vectors state vectors (in fixed)
   ~AdjointBuffers() {
     for (void* p : fixed) cudaFree(p);
     cudaFree(ckpt);
@@ -371,6 +373,9 @@ int adjoint_time_vjp(hg_ctx* c, int32_t reps, int32_t flushL2, double* avgMs) {
 int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int32_t C, const int32_t* probeCells,
                           const double* obs, int32_t P, double* loss, double* gManning, double* gZb, double* gInlet,
                           double* Qfinal, const FinalObs* fo, double* parts) {
+  const bool tsit5 = c->adjIntegrator == 1;
+  if (tsit5 && c->precision != HG_FP64)
+    return fail(c, HG_ERR_UNSUPPORTED, "the fixed-step Tsit5 adjoint needs an FP64 context");
   int rc = setup(c);
   if (rc) return rc;
   AdjointBuffers* b = c->adj;
@@ -583,7 +588,129 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
   // recomputation and the VJP of that stage alike.
   auto hydro = [&](double t) { c->launches += launch_hydrograph(dm, ds, kHydroAt, t, st); };
 
-  if (f64) {
+  if (tsit5) {
+    // Fixed-step Tsit5 (hg_integrate_tsit5 with adaptive = 0): step s takes
+    // U_s at t_s = s dt to U_{s+1} = U_s + dt sum_{j<6} b_j K_j, with
+    // K_i = f(Y_i, t_s + c_i dt), Y_0 = U_s, Y_i = U_s + dt sum_{j<i} a_ij K_j
+    // (b = the tableau's last row).  Its adjoint, from lam' = dL/dU_{s+1}:
+    //   Kbar_i = dt (b_i lam' + sum_{k>i} a_ki Ybar_k),  Ybar_i = J(Y_i)^T Kbar_i   (i = 5 .. 0)
+    //   lam = lam' + sum_i Ybar_i  (+ the probe seed of U_s)
+    // the VJP kernels accumulating the parameter terms (dR/dtheta)^T Kbar_i of
+    // each stage at its own state and time.  No clamp acts on a Tsit5 state
+    // (the RHS clamps its own copy of h), so nothing is masked.
+    const Tsit5Tableau& tb = tsit5_tableau();
+    if (!b->tsit5) ADJ_CUDA(c, falloc(b, &b->tsit5, (size_t)kTsit5Vectors * n3));
+    double* Y[6];    // Y[0] = U_s (in the segment buffer); Y[1..5] here
+    double* Kv[6];   // stage RHS
+    double* Yb[6];   // stage cotangents
+    for (int i = 0; i < 6; ++i) {
+      Y[i] = i == 0 ? nullptr : b->tsit5 + (size_t)(i - 1) * n3;
+      Kv[i] = b->tsit5 + (size_t)(5 + i) * n3;
+      Yb[i] = b->tsit5 + (size_t)(11 + i) * n3;
+    }
+    double* kb = b->tsit5 + (size_t)17 * n3;
+    double* lam = b->mu1;
+    double* lamNext = b->mu2;
+    auto rhs = [&](const double* X, double* out, double t) {
+      hydro(t);
+      launch_inlet_total_f64(dm, ds, X, st);
+      launch_stage_f64(dm, ds, kModeRhs, X, nullptr, out, false, st);
+      c->launches += 1 + (dm.nInlet > 0 ? 1 : 0) + resistance_launches(dm);
+    };
+    auto terms_of = [&](int i) {   // a_ij K_j, j < i (i = 6: the new state's weights b)
+      Tsit5Terms t{};
+      for (int j = 0; j < i; ++j) {
+        t.K[j] = Kv[j];
+        t.w[j] = tb.a[i][j];
+      }
+      t.nk = i;
+      return t;
+    };
+    // The stages of step s from U (K_0 .. K_nk-1, Y_1 .. Y_5); Unext: the new state, or null.
+    auto stages = [&](int s, const double* U, int nk, double* Unext) {
+      const double t = s * dt;
+      Y[0] = const_cast<double*>(U);
+      rhs(U, Kv[0], t);
+      for (int i = 1; i < 6; ++i) {
+        launch_tsit5_combine(n3, U, terms_of(i), dt, Y[i], st);
+        if (i < nk) rhs(Y[i], Kv[i], t + tb.c[i] * dt);
+        c->launches += 1;
+      }
+      if (Unext) {
+        launch_tsit5_combine(n3, U, terms_of(6), dt, Unext, st);
+        c->launches += 1;
+      }
+    };
+    launch_gather_state_f64(N, c->d_perm, c->Quser, c->QA, st);
+    // Forward pass: a checkpoint at each segment's start; the last segment's
+    // states go straight into the segment buffer (U_s at seg + (s - sLast) n3).
+    const int sLast = seg_start(nck - 1);
+    for (int s = 0; s < K; ++s) {
+      const bool last = s >= sLast;
+      const size_t i = (size_t)(s - sLast);
+      if (!last && s == seg_start(seg_of(s)))
+        ADJ_CUDA(c, cudaMemcpyAsync(b->ckpt + (size_t)seg_of(s) * n3, c->QA, n3 * sizeof(double),
+                                    cudaMemcpyDeviceToDevice, st));
+      if (s == sLast) ADJ_CUDA(c, cudaMemcpyAsync(b->seg, c->QA, n3 * sizeof(double), cudaMemcpyDeviceToDevice, st));
+      const double* u0 = last ? b->seg + i * n3 : c->QA;
+      double* u1 = last ? b->seg + (i + 1) * n3 : c->QB;
+      stages(s, u0, 6, u1);
+      launch_probe_loss_f64(dm, a, u1, b->probes, b->obs + (size_t)s * P, P, st);
+      c->launches += P > 0 ? 1 : 0;
+      if (!last) std::swap(c->QA, c->QB);
+    }
+    const double* uK = b->seg + (size_t)(K - sLast) * n3;
+    ADJ_CUDA(c, cudaMemcpyAsync(c->QA, uK, n3 * sizeof(double), cudaMemcpyDeviceToDevice, st));   // the final state
+    if (Qfinal) launch_scatter_state_f64(N, c->d_perm, c->QA, c->Quser, st);   // copied out at the end
+    // Reverse sweep: the seed of the final state.
+    ADJ_CUDA(c, cudaMemsetAsync(lam, 0, n3 * sizeof(double), st));
+    launch_probe_adjoint_f64(dm, c->QA, lam, b->probes, b->obs + (size_t)(K - 1) * P, P, scale, st, false);
+    if (useFinal) {
+      fl.mask = 0;
+      launch_final_loss_f64(dm, fl, c->QA, lam, st);
+      c->launches += 1;
+    }
+    for (int seg = nck - 1; seg >= 0; --seg) {
+      const int s0 = seg_start(seg), s1 = seg_start(seg + 1);
+      if (seg < nck - 1) {   // the segment's states from its checkpoint (the last one's are in place)
+        ADJ_CUDA(c, cudaMemcpyAsync(b->seg, b->ckpt + (size_t)seg * n3, n3 * sizeof(double),
+                                    cudaMemcpyDeviceToDevice, st));
+        for (int s = s0; s < s1 - 1; ++s)
+          stages(s, b->seg + (size_t)(s - s0) * n3, 6, b->seg + (size_t)(s - s0 + 1) * n3);
+      }
+      for (int s = s1 - 1; s >= s0; --s) {
+        const double* U = b->seg + (size_t)(s - s0) * n3;
+        stages(s, U, 5, nullptr);   // K_0 .. K_4 and Y_1 .. Y_5 (K_5 enters only the new state)
+        for (int i = 5; i >= 0; --i) {
+          Tsit5Terms t{};   // Kbar_i = dt (b_i lam + sum_{k>i} a_ki Ybar_k)
+          t.K[0] = lam;
+          t.w[0] = tb.a[6][i];
+          for (int k = i + 1; k < 6; ++k) {
+            t.K[k - i] = Yb[k];
+            t.w[k - i] = tb.a[k][i];
+          }
+          t.nk = 6 - i;
+          launch_tsit5_combine(n3, nullptr, t, dt, kb, st);
+          hydro(s * dt + tb.c[i] * dt);
+          launch_inlet_total_f64(dm, ds, Y[i], st);   // the stage's inlet totals and resistance
+          launch_vjp_f64(dm, a, Y[i], kb, nullptr, Yb[i], 0.0, 0.0, 1.0, st, false);
+          launch_inlet_adjoint_f64(dm, a, Y[i], Yb[i], 1.0, st);
+          c->launches += launch_ude_vjp_f64(dm, a, Y[i], Yb[i], st);
+          c->launches += 3 + (dm.nInlet > 0 ? 1 + dm.nInlet : 0) + resistance_launches(dm);
+        }
+        Tsit5Terms t{};   // lam_s = lam' + sum_i Ybar_i
+        for (int i = 0; i < 6; ++i) {
+          t.K[i] = Yb[i];
+          t.w[i] = 1.0;
+        }
+        t.nk = 6;
+        launch_tsit5_combine(n3, lam, t, 1.0, lamNext, st);
+        std::swap(lam, lamNext);
+        if (s >= 1) launch_probe_adjoint_f64(dm, U, lam, b->probes, b->obs + (size_t)(s - 1) * P, P, scale, st, false);
+        c->launches += 1 + (s >= 1 && P > 0 ? 1 : 0);
+      }
+    }
+  } else if (f64) {
     launch_gather_state_f64(N, c->d_perm, c->Quser, c->QA, st);
     // Forward pass with checkpoints.  The last segment's steps write their
     // stage states straight into the segment buffer, which the reverse sweep

@@ -71,7 +71,8 @@ __device__ __forceinline__ Side<D> constant(const Side<double>& s) {
 
 __global__ void __launch_bounds__(kBlock) k_vjp_f64(DevMesh m, AdjDev a, const double* __restrict__ Q,
                                                     const double* __restrict__ mu, const double* __restrict__ extra,
-                                                    double* out, double cSelf, double cExtra, double beta) {
+                                                    double* out, double cSelf, double cExtra, double beta,
+                                                    int useMask) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= m.n) return;
   const int n = m.n;
@@ -180,7 +181,9 @@ __global__ void __launch_bounds__(kBlock) k_vjp_f64(DevMesh m, AdjDev a, const d
   }
   if (a.udeChain == 2) a.udeGn[j] = beta * gF;   // F of the flow-resistance closure
   a.gZb[j] += beta * gzb;
-  const double mask = L.dry ? 0.0 : 1.0;   // the stage clamp zeroes the derivative of a dry cell
+  // the stage clamp zeroes the derivative of a dry cell (useMask = 0: a state
+  // no clamp produced, e.g. a Tsit5 stage)
+  const double mask = (useMask && L.dry) ? 0.0 : 1.0;
   const double e0 = extra ? extra[j] : 0.0, e1 = extra ? extra[n + j] : 0.0, e2 = extra ? extra[2 * n + j] : 0.0;
   out[j] = mask * (cSelf * mj0 + cExtra * e0 + beta * g0);
   out[n + j] = mask * (cSelf * mj1 + cExtra * e1 + beta * g1);
@@ -247,12 +250,12 @@ __global__ void __launch_bounds__(256) k_probe_loss_f64(DevMesh m, AdjDev a, con
 
 __global__ void k_probe_adjoint_f64(DevMesh m, const double* __restrict__ Q, double* mu,
                                     const int32_t* __restrict__ probes, const double* __restrict__ obs, int np,
-                                    double scale) {
+                                    double scale, int useMask) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   for (int p = 0; p < np; ++p) {              // sequential: a probe cell listed twice adds twice, in order
     const int c = probes[p];
     const double h = Q[c] + m.hst[c];
-    if (h <= m.hsm) continue;                 // clamped at the step's output: derivative 0
+    if (useMask && h <= m.hsm) continue;      // clamped at the step's output: derivative 0
     mu[c] += scale * 2.0 * (h - obs[p]);
   }
 }
@@ -292,10 +295,10 @@ __global__ void __launch_bounds__(256) k_zb_gradient(DevMesh m, AdjDev a, double
 }  // namespace
 
 void launch_vjp_f64(const DevMesh& m, const AdjDev& a, const double* Q, const double* mu, const double* extra,
-                    double* out, double cSelf, double cExtra, double beta, cudaStream_t st) {
+                    double* out, double cSelf, double cExtra, double beta, cudaStream_t st, bool mask) {
   // at most the kernel's launch bound; a cell's result does not depend on its block
   const int bs = stage_block_f64(m.n) < kBlock ? stage_block_f64(m.n) : kBlock;
-  k_vjp_f64<<<(m.n + bs - 1) / bs, bs, 0, st>>>(m, a, Q, mu, extra, out, cSelf, cExtra, beta);
+  k_vjp_f64<<<(m.n + bs - 1) / bs, bs, 0, st>>>(m, a, Q, mu, extra, out, cSelf, cExtra, beta, mask ? 1 : 0);
 }
 void launch_inlet_adjoint_f64(const DevMesh& m, const AdjDev& a, const double* Q, double* out, double beta,
                               cudaStream_t st) {
@@ -306,8 +309,8 @@ void launch_probe_loss_f64(const DevMesh& m, const AdjDev& a, const double* Q, c
   if (nprobe > 0) k_probe_loss_f64<<<1, 256, 0, st>>>(m, a, Q, probes, obs, nprobe);
 }
 void launch_probe_adjoint_f64(const DevMesh& m, const double* Q, double* mu, const int32_t* probes,
-                              const double* obs, int32_t nprobe, double scale, cudaStream_t st) {
-  if (nprobe > 0) k_probe_adjoint_f64<<<1, 32, 0, st>>>(m, Q, mu, probes, obs, nprobe, scale);
+                              const double* obs, int32_t nprobe, double scale, cudaStream_t st, bool mask) {
+  if (nprobe > 0) k_probe_adjoint_f64<<<1, 32, 0, st>>>(m, Q, mu, probes, obs, nprobe, scale, mask ? 1 : 0);
 }
 namespace {
 // The gradient w.r.t. the parameters of a state-dependent n: the per-cell

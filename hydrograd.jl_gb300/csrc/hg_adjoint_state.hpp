@@ -105,9 +105,10 @@ constexpr int kFoldMaxGroups = 8;
 constexpr int kUdeGrid = 1216;
 
 // out_j = M(Q_j) (cSelf mu_j + cExtra extra_j + beta (J(Q)^T mu)_j), parameter
-// gradients += beta (dR/dtheta)^T mu; M(Q_j) = 1 when cell j of Q is wet.
+// gradients += beta (dR/dtheta)^T mu; M(Q_j) = 1 when cell j of Q is wet (the
+// stage clamp), or always without mask (a state no clamp produced).
 void launch_vjp_f64(const DevMesh& m, const AdjDev& a, const double* Q, const double* mu, const double* extra,
-                    double* out, double cSelf, double cExtra, double beta, cudaStream_t st);
+                    double* out, double cSelf, double cExtra, double beta, cudaStream_t st, bool mask = true);
 // The UDE network's VJP of one stage (after that stage's VJP kernels):
 // out += M(Q) (dn/dQ)^T udeGn, gTheta += (dn/dtheta)^T udeGn, the LayerNorm
 // statistics taken over all cells when the network normalises over the batch.
@@ -122,7 +123,7 @@ void launch_inlet_adjoint_f64(const DevMesh& m, const AdjDev& a, const double* Q
 void launch_probe_loss_f64(const DevMesh& m, const AdjDev& a, const double* Q, const int32_t* probes,
                            const double* obs, int32_t nprobe, cudaStream_t st);
 void launch_probe_adjoint_f64(const DevMesh& m, const double* Q, double* mu, const int32_t* probes,
-                              const double* obs, int32_t nprobe, double scale, cudaStream_t st);
+                              const double* obs, int32_t nprobe, double scale, cudaStream_t st, bool mask = true);
 // FP32-compensated path: the same with packed FP32 states and FP32 cotangents.
 // The whole VJP of one stage, inlet-Q terms included, on st: the
 // boundary-face kernel, the interior kernel beside it (a programmatic
@@ -189,6 +190,7 @@ struct FinalLossDev {
   double velScale = 1.0;
   double invN = 1.0;
   double* dWse = nullptr;        // [n]
+  int32_t mask = 1;              // 1: cells at h_small (clamped by the last stage) take no seed
   double* parts = nullptr;       // [2]
   double* partials = nullptr;    // [2 * kFinalLossBlocks]
   unsigned int* ticket = nullptr;

@@ -1314,6 +1314,14 @@ int hg_set_adjoint_tape(hg_ctx* ctx, int64_t bytes) {
   return HG_OK;
 }
 
+int hg_set_adjoint_integrator(hg_ctx* ctx, int32_t integrator) {
+  if (!ctx) return fail(ctx, HG_ERR_ARG, "hg_set_adjoint_integrator: null context");
+  if (integrator != HG_ADJ_SSPRK2 && integrator != HG_ADJ_TSIT5)
+    return fail(ctx, HG_ERR_ARG, "hg_set_adjoint_integrator: HG_ADJ_SSPRK2 or HG_ADJ_TSIT5");
+  ctx->adjIntegrator = integrator;
+  return HG_OK;
+}
+
 int hg_loss_and_grad(hg_ctx* ctx, const double* Q0, int32_t nsteps, double dt, int32_t ckpt_every,
                      const int32_t* probe_cells, const double* obs, int32_t n_probe, double* loss,
                      double* g_manning_cells, double* g_zb, double* g_inletq, double* Q_final) {

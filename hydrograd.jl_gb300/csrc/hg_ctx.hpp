@@ -81,6 +81,7 @@ struct hg_ctx {
   // Adjoint stage-state tape (hg_set_adjoint_tape): -1 automatic budget, 0 the
   // caller's checkpoint spacing exactly, > 0 a budget in bytes.
   int64_t adjTapeBytes = -1;
+  int32_t adjIntegrator = 0;        // the steps the adjoint differentiates: 0 SSP-RK2, 1 fixed-step Tsit5
   // State-dependent resistance (hg_set_manning_function / hg_set_ude): device
   // buffers, allocated on first use; dm.res points into them.
   double *d_resKs = nullptr, *d_resW = nullptr, *d_resStats = nullptr, *d_resPartials = nullptr, *d_fres = nullptr;

@@ -60,7 +60,7 @@ __global__ void __launch_bounds__(kBlock) k_final_loss(DevMesh m, FinalLossDev f
       gqx += f.lam[m.n + c];
       gqy += f.lam[2 * m.n + c];
     }
-    if (h > m.hsm) {   // a cell the last stage clamped does not depend on its inputs
+    if (!f.mask || h > m.hsm) {   // a cell the last stage clamped does not depend on its inputs
       mu[c] += (Mu)gxi;
       mu[m.n + c] += (Mu)gqx;
       mu[2 * m.n + c] += (Mu)gqy;

@@ -16,7 +16,7 @@ namespace {
 
 constexpr int kBlock = 256;
 
-// Y = U + dt sum_j w[j] K[j] over the nk vectors in K.
+// Y = U + dt sum_j w[j] K[j] over the nk vectors in K (U null: Y = dt sum).
 __global__ void __launch_bounds__(kBlock) k_tsit5_combine(int64_t len, const double* __restrict__ U, Tsit5Terms t,
                                                           double dt, double* __restrict__ Y) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < len; i += (int64_t)gridDim.x * blockDim.x) {
@@ -24,7 +24,7 @@ __global__ void __launch_bounds__(kBlock) k_tsit5_combine(int64_t len, const dou
 #pragma unroll
     for (int j = 0; j < kTsit5Stages; ++j)
       if (j < t.nk) s += t.w[j] * t.K[j][i];
-    Y[i] = U[i] + dt * s;
+    Y[i] = U ? U[i] + dt * s : dt * s;
   }
 }
 

@@ -15,6 +15,9 @@ namespace hg {
 
 constexpr int kTsit5Stages = 7;
 constexpr int kTsit5ErrorBlocks = 1024;   // grid of the combination / error kernels
+// State vectors of the fixed-step Tsit5 adjoint (hg_adjoint.cpp): stage states
+// Y_1..Y_5, stage RHS K_0..K_5, stage cotangents Ybar_0..Ybar_5, one Kbar.
+constexpr int kTsit5Vectors = 18;
 
 struct Tsit5Tableau {
   double c[kTsit5Stages];

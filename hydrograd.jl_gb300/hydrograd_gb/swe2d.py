@@ -344,6 +344,13 @@ class SWE2D:
         (HG_ERR_STATE); 0 turns the check off."""
         self._chk(lib().hg_set_dt_min(self.h, float(dt_min)))
 
+    def set_adjoint_integrator(self, integrator):
+        """hg_set_adjoint_integrator: the steps the gradient calls run and
+        differentiate -- "ssprk2" (default) or "tsit5" (fixed Tsit5 steps of dt,
+        FP64 contexts)."""
+        code = {"ssprk2": 0, "tsit5": 1}[integrator]
+        self._chk(lib().hg_set_adjoint_integrator(self.h, code))
+
     def set_adjoint_tape(self, nbytes=-1):
         """hg_set_adjoint_tape: memory for the adjoint's stage states.  -1 (the
         default): segments as long as fit in min(half the free device memory,
@@ -372,6 +379,8 @@ class SWE2D:
         Q0 = np.ascontiguousarray(Q0, dtype=np.float64)
         probes = np.ascontiguousarray(probes, dtype=np.int32)
         obs = np.ascontiguousarray(obs, dtype=np.float64)
+        if obs.size != int(nsteps) * len(probes):   # the library reads nsteps x n_probe values
+            raise ValueError("obs: one value per step and probe (%d x %d), got %d" % (nsteps, len(probes), obs.size))
         loss = np.zeros(1)
         gn = np.zeros(N) if "manning" in want else None
         gz = np.zeros(N) if "zb" in want else None

@@ -175,6 +175,10 @@ set_riemann_solver!(ctx::Context, s::AbstractString) =
     check(ctx.ptr, ccall((:hg_set_riemann_solver, lib), Cint, (Ptr{Cvoid}, Int32), ctx, riemann_code(s)))
 set_dt_min!(ctx::Context, dt_min::Real) =
     check(ctx.ptr, ccall((:hg_set_dt_min, lib), Cint, (Ptr{Cvoid}, Float64), ctx, Float64(dt_min)))
+# The steps the gradients differentiate: :ssprk2 (default) or :tsit5 (fixed Tsit5 steps, FP64 contexts).
+set_adjoint_integrator!(ctx::Context, integrator::Symbol) =
+    check(ctx.ptr, ccall((:hg_set_adjoint_integrator, lib), Cint, (Ptr{Cvoid}, Int32), ctx,
+                         Int32(integrator === :tsit5 ? 1 : integrator === :ssprk2 ? 0 : error("integrator"))))
 set_hydrograph!(ctx::Context, group::Integer, t::Vector{Float64}, q::Vector{Float64}) =
     check(ctx.ptr, ccall((:hg_set_inlet_hydrograph, lib), Cint, (Ptr{Cvoid}, Int32, Int32, Ptr{Float64}, Ptr{Float64}),
                          ctx, Int32(group), Int32(length(t)), t, q))

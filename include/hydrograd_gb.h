@@ -362,6 +362,24 @@ int hg_final_loss_and_grad(hg_ctx* ctx, const double* Q0, int32_t nsteps, double
  * the next one allocates what it needs. */
 int hg_set_adjoint_tape(hg_ctx* ctx, int64_t bytes);
 
+/* The time stepping the gradient calls (hg_loss_and_grad,
+ * hg_final_loss_and_grad, hg_final_vjp) run and differentiate:
+ * HG_ADJ_SSPRK2 (the default) -- nsteps SSP-RK2 steps of dt with the
+ * depth-positivity clamp after each stage; HG_ADJ_TSIT5 -- nsteps fixed Tsit5
+ * steps of dt (hg_integrate_tsit5 with adaptive = 0), the reference's own
+ * integrator (swe_2D_forward_simulation.jl:37-39, whose solve its inversion
+ * and sensitivity applications differentiate, swe_2D_inversion.jl:304-339,
+ * swe_2D_sensitivity.jl:80), with no clamp of the state, as in the reference's
+ * ODE solve.  The Tsit5 adjoint is the exact discrete adjoint of the fixed
+ * steps: per step, the six stage states recomputed from the step's start
+ * state and the stage cotangents taken back through the RHS Jacobian at each
+ * (Kbar_i = dt (b_i lam + sum_{k>i} a_ki Ybar_k), Ybar_i = J(Y_i)^T Kbar_i).
+ * FP64 contexts only (HG_ERR_UNSUPPORTED from the gradient calls of an FP32C
+ * context set to HG_ADJ_TSIT5).  The probe loss is taken at the states after
+ * each step, as with SSP-RK2. */
+enum hg_adjoint_integrator { HG_ADJ_SSPRK2 = 0, HG_ADJ_TSIT5 = 1 };
+int hg_set_adjoint_integrator(hg_ctx* ctx, int32_t integrator);
+
 /* Vector-Jacobian product of the final state: with Q_K the state after nsteps
  * SSP-RK2 steps of dt from Q0, the gradients of lambda . Q_K (lambda [3n], the
  * caller's cell order, blocks xi, qx, qy) w.r.t. the per-cell n, zb and the

@@ -952,19 +952,57 @@ struct Tsit5Stats {
   int accepted = 0, rejected = 0, evals = 0;
 };
 
+// The Tsit5 tableau: nodes c, coefficients a (row 6: the 5th-order weights b,
+// the seventh stage being the new state), and b - bhat.
+struct Tsit5Tab {
+  double C[7];
+  double A[7][6];
+  double BT[7];
+};
+inline const Tsit5Tab& tsit5_tab() {
+  static const Tsit5Tab t = {
+      {0.0, 0.161, 0.327, 0.9, 0.9800255409045097, 1.0, 1.0},
+      {{0, 0, 0, 0, 0, 0},
+       {0.161, 0, 0, 0, 0, 0},
+       {-0.008480655492356989, 0.335480655492357, 0, 0, 0, 0},
+       {2.897153057105493, -6.359448489975075, 4.3622954328695815, 0, 0, 0},
+       {5.325864828439257, -11.748883564062828, 7.4955393428898365, -0.09249506636175525, 0, 0},
+       {5.86145544294642, -12.92096931784711, 8.159367898576159, -0.071584973281401, -0.028269050394068383, 0},
+       {0.09646076681806523, 0.01, 0.4798896504144996, 1.379008574103742, -3.290069515436081, 2.324710524099774}},
+      {-0.00178001105222577714, -0.0008164344596567469, 0.007880878010261995, -0.1447110071732629,
+       0.5823571654525552, -0.45808210592918697, 0.015151515151515152}};
+  return t;
+}
+
+// One fixed Tsit5 step of size h from time t, on any scalar type (dual numbers
+// give forward-mode derivatives): the stages and the new state exactly as
+// tsit5() forms them with adaptive == false (the same operations in the same
+// order), with no clamp of the state (the RHS clamps its own copy of h).
+template <class T>
+void tsit5_fixed_step(const Case& cs, const Params<T>& p, std::vector<T>& Q, double h, int nthreads = 1,
+                      double t = 0.0) {
+  const Tsit5Tab& tb = tsit5_tab();
+  const size_t n3 = Q.size();
+  std::vector<std::vector<T>> K(6, std::vector<T>(n3));
+  std::vector<T> Y(n3);
+  Params<T> scratch;
+  rhs<T>(cs, params_at(p, scratch, t), Q.data(), K[0].data(), nthreads);
+  for (int i = 1; i < 7; ++i) {
+    for (size_t k = 0; k < n3; ++k) {
+      T s(0.0);
+      for (int j = 0; j < i; ++j) s = s + tb.A[i][j] * K[j][k];
+      Y[k] = Q[k] + h * s;
+    }
+    if (i < 6) rhs<T>(cs, params_at(p, scratch, t + tb.C[i] * h), Y.data(), K[i].data(), nthreads);
+  }
+  Q.swap(Y);
+}
+
 inline bool tsit5(const Case& cs, const Params<double>& p, std::vector<double>& Q, double t0, double t1, double abstol,
                   double reltol, double dt0, bool adaptive, int maxSteps, Tsit5Stats& st, int nthreads = 1) {
-  static const double C[7] = {0.0, 0.161, 0.327, 0.9, 0.9800255409045097, 1.0, 1.0};
-  static const double A[7][6] = {
-      {0, 0, 0, 0, 0, 0},
-      {0.161, 0, 0, 0, 0, 0},
-      {-0.008480655492356989, 0.335480655492357, 0, 0, 0, 0},
-      {2.897153057105493, -6.359448489975075, 4.3622954328695815, 0, 0, 0},
-      {5.325864828439257, -11.748883564062828, 7.4955393428898365, -0.09249506636175525, 0, 0},
-      {5.86145544294642, -12.92096931784711, 8.159367898576159, -0.071584973281401, -0.028269050394068383, 0},
-      {0.09646076681806523, 0.01, 0.4798896504144996, 1.379008574103742, -3.290069515436081, 2.324710524099774}};
-  static const double BT[7] = {-0.00178001105222577714, -0.0008164344596567469, 0.007880878010261995,
-                               -0.1447110071732629, 0.5823571654525552, -0.45808210592918697, 0.015151515151515152};
+  const double(&C)[7] = tsit5_tab().C;
+  const double(&A)[7][6] = tsit5_tab().A;
+  const double(&BT)[7] = tsit5_tab().BT;
   const size_t n3 = Q.size();
   std::vector<std::vector<double>> K(7, std::vector<double>(n3));
   std::vector<double> Y(n3), Qn(n3);

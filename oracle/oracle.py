@@ -61,6 +61,8 @@ def _load():
                                    ctypes.c_int, _ip, _dp, _dp, _dp, _dp, _dp, ctypes.c_int]
     lib.ho_rk2_loss.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int, ctypes.c_double, ctypes.c_int, _ip, _dp, _dp, _dp,
                                 ctypes.c_int]
+    lib.ho_tsit5_tangent.argtypes = lib.ho_rk2_tangent.argtypes
+    lib.ho_tsit5_loss.argtypes = lib.ho_rk2_loss.argtypes
     _lib = lib
     return lib
 
@@ -247,23 +249,33 @@ class Oracle:
         return Q
 
     def rk2_tangent(self, Q0, nsteps, dt, d_manning=None, d_zb=None, d_inlet=None, probes=None, obs=None,
-                    nthreads=1):
-        """Forward-mode run; returns (Q, dQ[nDir,3N], loss, dloss[nDir])."""
+                    nthreads=1, method="rk2"):
+        """Forward-mode run of nsteps fixed-dt SSP-RK2 steps (method "rk2") or
+        Tsit5 steps ("tsit5"); returns (Q, dQ[nDir,3N], loss, dloss[nDir])."""
         nd = max(a.shape[0] for a in (d_manning, d_zb, d_inlet) if a is not None)
         Q0 = np.ascontiguousarray(Q0, dtype=np.float64)
         Qo, dQo = np.zeros_like(Q0), np.zeros((nd, Q0.size))
         loss, dloss = np.zeros(1), np.zeros(nd)
         npb = 0 if probes is None else len(probes)
-        rc = self.lib.ho_rk2_tangent(self.h, _d(Q0), nsteps, dt, nd, _d(d_manning), _d(d_zb), _d(d_inlet), npb,
-                                     _i(probes), _d(obs), _d(Qo), _d(dQo), _d(loss), _d(dloss), nthreads)
+        fn = self.lib.ho_tsit5_tangent if method == "tsit5" else self.lib.ho_rk2_tangent
+        rc = fn(self.h, _d(Q0), nsteps, dt, nd, _d(d_manning), _d(d_zb), _d(d_inlet), npb,
+                _i(probes), _d(obs), _d(Qo), _d(dQo), _d(loss), _d(dloss), nthreads)
         if rc != 0:
             raise RuntimeError("oracle: " + self.lib.ho_last_error().decode())
         return Qo, dQo, float(loss[0]), dloss
 
-    def rk2_loss(self, Q0, nsteps, dt, probes, obs, nthreads=1):
+    def tsit5_tangent(self, Q0, nsteps, dt, **kw):
+        """rk2_tangent of nsteps fixed Tsit5 steps (hgo::tsit5_fixed_step)."""
+        return self.rk2_tangent(Q0, nsteps, dt, method="tsit5", **kw)
+
+    def rk2_loss(self, Q0, nsteps, dt, probes, obs, nthreads=1, method="rk2"):
         Q0 = np.ascontiguousarray(Q0, dtype=np.float64)
         Qo, loss = np.zeros_like(Q0), np.zeros(1)
-        if self.lib.ho_rk2_loss(self.h, _d(Q0), nsteps, dt, len(probes), _i(probes), _d(obs), _d(Qo), _d(loss),
-                                nthreads) != 0:
+        fn = self.lib.ho_tsit5_loss if method == "tsit5" else self.lib.ho_rk2_loss
+        if fn(self.h, _d(Q0), nsteps, dt, len(probes), _i(probes), _d(obs), _d(Qo), _d(loss), nthreads) != 0:
             raise RuntimeError("oracle: " + self.lib.ho_last_error().decode())
         return float(loss[0]), Qo
+
+    def tsit5_loss(self, Q0, nsteps, dt, probes, obs, nthreads=1):
+        """The probe loss of nsteps fixed Tsit5 steps and the final state."""
+        return self.rk2_loss(Q0, nsteps, dt, probes, obs, nthreads, method="tsit5")

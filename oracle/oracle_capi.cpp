@@ -61,14 +61,15 @@ Params<D<ND>> lift_params(const OracleCase& oc, int nDir, const double* dManning
 template <int ND>
 int run_tangent(OracleCase& oc, const double* Q0, int nsteps, double dt, int nDir, const double* dManning,
                 const double* dZb, const double* dInletQ, int nProbe, const int* probes, const double* obs,
-                double* Qout, double* dQout, double* loss, double* dloss, int nthreads) {
+                double* Qout, double* dQout, double* loss, double* dloss, int nthreads, int method = 0) {
   const int N = oc.cs.mesh.nCells;
   Params<D<ND>> q = lift_params<ND>(oc, nDir, dManning, dZb, dInletQ);
   std::vector<D<ND>> Q(3 * (size_t)N);
   for (size_t k = 0; k < Q.size(); ++k) Q[k] = D<ND>(Q0[k]);
   D<ND> L(0.0);
   for (int s = 0; s < nsteps; ++s) {
-    rk2_step<D<ND>>(oc.cs, q, Q, dt, nthreads, s * dt);
+    if (method == 1) tsit5_fixed_step<D<ND>>(oc.cs, q, Q, dt, nthreads, s * dt);
+    else rk2_step<D<ND>>(oc.cs, q, Q, dt, nthreads, s * dt);
     for (int pi = 0; pi < nProbe; ++pi) {
       int c = probes[pi];
       D<ND> e = (Q[c] + oc.cs.hstill[c]) - obs[(size_t)s * nProbe + pi];
@@ -399,29 +400,70 @@ int ho_euler_reference(void* h, double* Q, int nsteps, double dt, int nthreads) 
   return 0;
 }
 
-// Forward-mode tangent run of nsteps fixed-dt SSP-RK2 steps (nDir <= 8 directions).
+// Forward-mode tangent run of nsteps fixed-dt SSP-RK2 (method 0) or Tsit5
+// (method 1) steps (nDir <= 8 directions).
 // Tangent seeds: dManning [nDir*N] (per-cell n), dZb [nDir*N] (per-cell zb, the
 // active zb parameter path), dInletQ [nDir*nInlet]; any may be NULL.
-int ho_rk2_tangent(void* h, const double* Q0, int nsteps, double dt, int nDir, const double* dManning,
-                   const double* dZb, const double* dInletQ, int nProbe, const int* probes, const double* obs,
-                   double* Qout, double* dQout, double* loss, double* dloss, int nthreads) {
+static int tangent_entry(void* h, const double* Q0, int nsteps, double dt, int nDir, const double* dManning,
+                         const double* dZb, const double* dInletQ, int nProbe, const int* probes, const double* obs,
+                         double* Qout, double* dQout, double* loss, double* dloss, int nthreads, int method) {
   auto* oc = static_cast<OracleCase*>(h);
   try {
     if (nDir <= 1)
       return run_tangent<1>(*oc, Q0, nsteps, dt, nDir, dManning, dZb, dInletQ, nProbe, probes, obs, Qout, dQout, loss,
-                            dloss, nthreads);
+                            dloss, nthreads, method);
     if (nDir <= 3)
       return run_tangent<3>(*oc, Q0, nsteps, dt, nDir, dManning, dZb, dInletQ, nProbe, probes, obs, Qout, dQout, loss,
-                            dloss, nthreads);
+                            dloss, nthreads, method);
     if (nDir <= 8)
       return run_tangent<8>(*oc, Q0, nsteps, dt, nDir, dManning, dZb, dInletQ, nProbe, probes, obs, Qout, dQout, loss,
-                            dloss, nthreads);
+                            dloss, nthreads, method);
     g_err = "nDir > 8";
     return 2;
   } catch (const std::exception& e) {
     g_err = e.what();
     return 1;
   }
+}
+
+int ho_rk2_tangent(void* h, const double* Q0, int nsteps, double dt, int nDir, const double* dManning,
+                   const double* dZb, const double* dInletQ, int nProbe, const int* probes, const double* obs,
+                   double* Qout, double* dQout, double* loss, double* dloss, int nthreads) {
+  return tangent_entry(h, Q0, nsteps, dt, nDir, dManning, dZb, dInletQ, nProbe, probes, obs, Qout, dQout, loss, dloss,
+                       nthreads, 0);
+}
+
+int ho_tsit5_tangent(void* h, const double* Q0, int nsteps, double dt, int nDir, const double* dManning,
+                     const double* dZb, const double* dInletQ, int nProbe, const int* probes, const double* obs,
+                     double* Qout, double* dQout, double* loss, double* dloss, int nthreads) {
+  return tangent_entry(h, Q0, nsteps, dt, nDir, dManning, dZb, dInletQ, nProbe, probes, obs, Qout, dQout, loss, dloss,
+                       nthreads, 1);
+}
+
+// Loss of nsteps fixed Tsit5 steps without tangents (for central finite differences).
+int ho_tsit5_loss(void* h, const double* Q0, int nsteps, double dt, int nProbe, const int* probes, const double* obs,
+                  double* Qout, double* loss, int nthreads) {
+  auto* oc = static_cast<OracleCase*>(h);
+  try {
+    const int N = oc->cs.mesh.nCells;
+    std::vector<double> q(Q0, Q0 + 3 * (size_t)N);
+    double L = 0.0;
+    for (int s = 0; s < nsteps; ++s) {
+      tsit5_fixed_step<double>(oc->cs, oc->p, q, dt, nthreads, s * dt);
+      for (int pi = 0; pi < nProbe; ++pi) {
+        int c = probes[pi];
+        double e = (q[c] + oc->cs.hstill[c]) - obs[(size_t)s * nProbe + pi];
+        L = L + e * e;
+      }
+    }
+    if (nProbe > 0) L = L / (double(nsteps) * nProbe);
+    if (Qout) std::memcpy(Qout, q.data(), q.size() * sizeof(double));
+    if (loss) *loss = L;
+  } catch (const std::exception& e) {
+    g_err = e.what();
+    return 1;
+  }
+  return 0;
 }
 
 // Loss of a forward run without tangents (for central finite differences).

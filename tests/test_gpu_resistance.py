@@ -106,7 +106,7 @@ def test_graph_steps_and_constant_restore(precision):
     ctx.advance(120, dt=dt, graph=True)
     Qa = ctx.download()
     assert block_err(Qa, Qi, N) <= (0.0 if precision == "fp64" else 1e-6)
-    r = ctx.loss_and_grad(Q0, 5, dt, [0, 1], [0.1, 0.1])
+    r = ctx.loss_and_grad(Q0, 5, dt, [0, 1], np.full((5, 2), 0.1))   # one observation per step and probe
     assert np.isfinite(r["loss"]) and np.isfinite(ctx.resistance_grad()).all()
     ctx.set_manning_function("constant")
     np.testing.assert_array_equal(ctx.rhs(Q0), rhs_const)

@@ -1,0 +1,155 @@
+"""Gradients through fixed Tsit5 steps (hg_set_adjoint_integrator(HG_ADJ_TSIT5)).
+
+The reference differentiates its Tsit5 solve (swe_2D_inversion.jl:304-339,
+swe_2D_sensitivity.jl:80).  With the integrator set to Tsit5 the gradient
+calls run nsteps fixed Tsit5 steps of dt (hg_integrate_tsit5 with adaptive =
+0) and take the exact discrete adjoint of those steps.  Checked against the
+oracle's forward-mode dual numbers of the same steps (hgo::tsit5_fixed_step,
+1e-8 relative: both are the exact derivative of the same discrete map) and
+central differences of the oracle's loss (eps 1e-6, 1e-5 relative), as the
+SSP-RK2 adjoint is in tests/test_gpu_adjoint.py: the probe loss's zone-n,
+inlet-Q and directional zb gradients, several checkpoint spacings, an inlet
+hydrograph (central differences of a shift), and final-state
+vector-Jacobian products (hg_final_vjp) against the duals' final-state
+tangents.  FP32C contexts refuse the Tsit5 adjoint.
+"""
+import numpy as np
+import pytest
+
+from hydrograd_gb import HgError, SWE2D
+from hydrograd_gb.workloads import Stream, river_triangles
+from tests.test_gpu_adjoint import make_pair
+
+pytestmark = pytest.mark.gpu
+
+K = 24
+
+
+def river():
+    return river_triangles(n=24, L=400.0, inlet_q=100.0, pool_center=(60.0, 200.0), pool_radius=70.0)
+
+
+@pytest.fixture(scope="module")
+def problem():
+    case = river()
+    ctx, o, N = make_pair(case)
+    Q0 = case["Q0"]
+    dt = 0.5 * o.cfl_dt(Q0, 0.4)
+    cxy = o.mesh_arrays()["centroids"].reshape(N, 2)
+    r = np.hypot(cxy[:, 0] - case["pool_center"][0], cxy[:, 1] - case["pool_center"][1])
+    probes = np.unique(np.concatenate([np.argsort(cxy[:, 0])[:8],
+                                       np.argsort(np.abs(r - case["pool_radius"]))[:8]])).astype(np.int32)
+    hs = o.hstill()
+    # observations: the probe depths of a Tsit5 run with other zone values
+    hidden = case["manning_zones"] * (1.0 + 0.2 * np.sin(np.arange(len(case["manning_zones"])) + 1.0))
+    _, oh, _ = make_pair(case, hidden)
+    obs = np.zeros((K, len(probes)))
+    Q = Q0.copy()
+    for k in range(K):
+        _, Q = oh.tsit5_loss(Q, 1, dt, probes[:0], np.zeros((1, 0)))
+        obs[k] = Q[probes] + hs[probes]
+    zones = case["mat_id"]
+    nz = len(case["manning_zones"])
+    dman = np.zeros((nz, N))
+    for z in range(nz):
+        dman[z, zones == z] = 1.0
+    v = Stream(5).uniform(N, -1.0, 1.0)
+    dzb = v[None, :]
+    Qo, dQ, L, dL = o.tsit5_tangent(Q0, K, dt, d_manning=dman, probes=probes, obs=obs, nthreads=4)
+    _, dQz, _, dLz = o.tsit5_tangent(Q0, K, dt, d_zb=dzb, probes=probes, obs=obs, nthreads=4)
+    _, dQq, _, dLq = o.tsit5_tangent(Q0, K, dt, d_inlet=np.ones((1, 1)), probes=probes, obs=obs, nthreads=4)
+    ctx.set_adjoint_integrator("tsit5")
+    return dict(case=case, ctx=ctx, o=o, N=N, Q0=Q0, dt=dt, probes=probes, obs=obs, Qo=Qo, L=L, dL=dL, dQ=dQ,
+                v=v, dLz=dLz, dQz=dQz, dLq=dLq, dQq=dQq, zones=zones, nz=nz)
+
+
+def zone_sums(g, zones, nz):
+    return np.array([g[zones == z].sum() for z in range(nz)])
+
+
+@pytest.mark.parametrize("ckpt", [5, 50])
+def test_loss_and_gradients_match_dual_numbers(problem, ckpt):
+    p = problem
+    r = p["ctx"].loss_and_grad(p["Q0"], K, p["dt"], p["probes"], p["obs"], ckpt_every=ckpt)
+    assert abs(r["loss"] - p["L"]) <= 1e-12 * abs(p["L"])
+    assert np.abs(r["Q"] - p["Qo"]).max() <= 1e-12 * np.abs(p["Qo"]).max()   # the same forward steps
+    gz = zone_sums(r["g_manning"], p["zones"], p["nz"])
+    assert np.abs(gz - p["dL"][:p["nz"]]).max() <= 1e-8 * np.abs(p["dL"][:p["nz"]]).max()
+    assert abs(r["g_zb"] @ p["v"] - p["dLz"][0]) <= 1e-8 * abs(p["dLz"][0])
+    assert abs(r["g_inletq"][0] - p["dLq"][0]) <= 1e-8 * abs(p["dLq"][0])
+
+
+def test_checkpoint_spacing_does_not_change_the_gradient(problem):
+    p = problem
+    p["ctx"].set_adjoint_tape(0)   # segments of exactly ckpt_every steps
+    try:
+        a = p["ctx"].loss_and_grad(p["Q0"], K, p["dt"], p["probes"], p["obs"], ckpt_every=5)
+        b = p["ctx"].loss_and_grad(p["Q0"], K, p["dt"], p["probes"], p["obs"], ckpt_every=K)
+    finally:
+        p["ctx"].set_adjoint_tape(-1)
+    for k in ("g_manning", "g_zb", "g_inletq"):
+        assert np.abs(a[k] - b[k]).max() <= 1e-12 * np.abs(b[k]).max()
+
+
+def test_inlet_gradient_matches_central_differences(problem):
+    p = problem
+    o, case = p["o"], p["case"]
+    r = p["ctx"].loss_and_grad(p["Q0"], K, p["dt"], p["probes"], p["obs"])
+    q0 = case["inlet_q"][0]
+    eps = 1e-6 * q0
+    o.set_inlet_q(np.array([q0 + eps]))
+    lp, _ = o.tsit5_loss(p["Q0"], K, p["dt"], p["probes"], p["obs"])
+    o.set_inlet_q(np.array([q0 - eps]))
+    lm, _ = o.tsit5_loss(p["Q0"], K, p["dt"], p["probes"], p["obs"])
+    o.set_inlet_q(case["inlet_q"])
+    fd = (lp - lm) / (2 * eps)
+    assert abs(r["g_inletq"][0] - fd) <= 1e-5 * abs(fd)
+
+
+def test_final_vjp_matches_dual_numbers(problem):
+    """lam^T dQ_K/dtheta for a random cotangent lam of the final state."""
+    p = problem
+    lam = Stream(11).uniform(3 * p["N"], -1.0, 1.0)
+    r = p["ctx"].final_state_vjp(p["Q0"], K, p["dt"], lam)
+    ref_n = p["dQ"][:p["nz"]] @ lam
+    gz = zone_sums(r["g_manning"], p["zones"], p["nz"])
+    assert np.abs(gz - ref_n).max() <= 1e-8 * np.abs(ref_n).max()
+    assert abs(r["g_zb"] @ p["v"] - p["dQz"][0] @ lam) <= 1e-8 * abs(p["dQz"][0] @ lam)
+    assert abs(r["g_inletq"][0] - p["dQq"][0] @ lam) <= 1e-8 * abs(p["dQq"][0] @ lam)
+
+
+def test_hydrograph_run_matches_central_differences():
+    """An inlet hydrograph, evaluated at every stage's own time t_s + c_i dt in
+    the forward steps, the recomputation and the VJPs: the loss against the
+    oracle's and the inlet-Q gradient -- the derivative w.r.t. a constant
+    shift of the hydrograph -- against central differences of the oracle's
+    loss with the hydrograph shifted (eps 1e-6 relative)."""
+    case = river()
+    ctx, o, N = make_pair(case)
+    T = np.array([0.0, 3.0, 8.0])
+    Qh = np.array([60.0, 140.0, 90.0])
+    ctx.set_inlet_hydrograph(0, T, Qh)
+    dt = 0.5 * o.cfl_dt(case["Q0"], 0.4)
+    probes = np.arange(0, N, max(1, N // 12), dtype=np.int32)
+    obs = np.full((K, len(probes)), 0.5)
+    ctx.set_adjoint_integrator("tsit5")
+    r = ctx.loss_and_grad(case["Q0"], K, dt, probes, obs, ckpt_every=7)
+    loss = {}
+    for sgn in (0.0, 1.0, -1.0):
+        o.set_hydrograph(0, T, Qh + sgn * 1e-6 * Qh.mean())
+        loss[sgn], _ = o.tsit5_loss(case["Q0"], K, dt, probes, obs)
+    fd = (loss[1.0] - loss[-1.0]) / (2e-6 * Qh.mean())
+    assert abs(r["loss"] - loss[0.0]) <= 1e-12 * abs(loss[0.0])
+    assert abs(r["g_inletq"][0] - fd) <= 1e-5 * abs(fd)
+
+
+def test_fp32c_context_refuses_the_tsit5_adjoint():
+    case = river()
+    c = SWE2D(case, precision="fp32c")
+    c.set_still_water(case["wstill"])
+    c.set_manning_zones(case["mat_id"], case["manning_zones"])
+    c.set_inlet_q(case["inlet_q"])
+    c.set_exit_wse(case["exit_wse"])
+    c.set_adjoint_integrator("tsit5")
+    with pytest.raises(HgError):
+        c.loss_and_grad(case["Q0"], 4, 0.1, np.array([1], np.int32), np.zeros((4, 1)))
