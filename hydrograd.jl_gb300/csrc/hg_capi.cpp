@@ -1472,17 +1472,23 @@ int ctx_setup_device(hg_ctx* c) {
     std::vector<int32_t> inletMember(std::max<size_t>(inletCell.empty() ? 0 : m.inletGroups.size(), 1), 0);
     for (int mm = 0; mm < M; ++mm)
       for (int g = c->memberInletOff[mm]; g < c->memberInletOff[mm + 1]; ++g) inletMember[g] = mm;
-    int32_t *dOff = nullptr, *dInM = nullptr;
+    std::vector<int32_t> memberOf((size_t)N);
+    for (int mm = 0; mm < M; ++mm)
+      for (int i = c->memberCellOff[mm]; i < c->memberCellOff[mm + 1]; ++i) memberOf[i] = mm;
+    int32_t *dOff = nullptr, *dInM = nullptr, *dOf = nullptr;
     HG_CUDA(c, dalloc(c, &dOff, (size_t)M + 1));
     HG_CUDA(c, dalloc(c, &dInM, inletMember.size()));
+    HG_CUDA(c, dalloc(c, &dOf, (size_t)N));
     HG_CUDA(c, upload(c, dOff, c->memberCellOff));
     HG_CUDA(c, upload(c, dInM, inletMember));
+    HG_CUDA(c, upload(c, dOf, memberOf));
     HG_CUDA(c, dalloc(c, &c->ds.dtM, (size_t)M));
     HG_CUDA(c, dalloc(c, &c->ds.dtMf, (size_t)M));
     HG_CUDA(c, dalloc(c, &c->ds.tM, (size_t)M));
     HG_CUDA(c, dalloc(c, &c->ds.cflMinM, (size_t)M));
     HG_CUDA(c, dalloc(c, &c->ds.cflMinMF, (size_t)M));
     c->ds.memberOff = dOff;
+    c->ds.memberOfCell = dOf;
     c->ds.inletMember = dInM;
     c->ds.nMembers = M;
     HG_CUDA(c, cudaStreamSynchronize(c->stream));

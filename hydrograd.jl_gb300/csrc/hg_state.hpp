@@ -145,6 +145,7 @@ struct DevScalars {
   // step, and publish CFL candidates into the member's minimum.
   int32_t nMembers = 0;
   const int32_t* memberOff = nullptr;     // [nMembers + 1], device order
+  const int32_t* memberOfCell = nullptr;  // [n] the member of each device cell
   const int32_t* inletMember = nullptr;   // [nInlet] member of each inlet-Q group (hydrograph times)
   double* dtM = nullptr;                  // [nMembers] current step
   float* dtMf = nullptr;
