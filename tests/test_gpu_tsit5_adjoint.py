@@ -153,3 +153,77 @@ def test_fp32c_context_refuses_the_tsit5_adjoint():
     c.set_adjoint_integrator("tsit5")
     with pytest.raises(HgError):
         c.loss_and_grad(case["Q0"], 4, 0.1, np.array([1], np.int32), np.zeros((4, 1)))
+
+
+# Through a state-dependent resistance: every stage's VJP takes dL/dn back
+# through the n function (or the UDE network) at that stage's own state.
+# Against central differences of the oracle's fixed Tsit5 loss, which
+# recomputes n in its RHS alike (tolerances and steps of
+# tests/test_gpu_resistance_grad.py and tests/test_gpu_ude_grad.py).
+RK = 16
+
+
+def _flowing(c, o):
+    N = len(c["cell_node_count"])
+    hs = o.hstill()
+    Q0 = c["Q0"].copy()
+    Q0[N:2 * N] = 0.2 * (Q0[:N] + hs)   # a 0.2 m/s flow: the friction terms matter
+    dt = 0.5 * o.cfl_dt(Q0, 0.4)
+    probes = np.unique((Stream(5).uniform(40) * N).astype(np.int32))[:12]
+    obs = np.tile(Q0[probes] + hs[probes] + 0.05, (RK, 1))
+    return N, Q0, dt, probes, obs
+
+
+def test_sigmoid_n_function_gradients_match_central_differences():
+    from tests import test_gpu_resistance_grad as R
+    c = R.case()
+    params = R.PARAMS["sigmoid"]
+    o = R.oracle(c, "sigmoid", params, None)
+    N, Q0, dt, probes, obs = _flowing(c, o)
+    ctx, _ = R.make(c, "fp64", "sigmoid", params)
+    ctx.set_adjoint_integrator("tsit5")
+    r = ctx.loss_and_grad(Q0, RK, dt, probes, obs, ckpt_every=5)
+    gp = ctx.resistance_grad()
+
+    def loss(pr=params, q=None):
+        return R.oracle(c, "sigmoid", pr, None, q=q).tsit5_loss(Q0, RK, dt, probes, obs)[0]
+
+    assert abs(r["loss"] - loss()) <= 1e-10 * abs(r["loss"])
+    fd = np.zeros(4)
+    for k in range(4):
+        e = 1e-4 * max(abs(params[k]), 1e-2)
+        up, dn = list(params), list(params)
+        up[k] += e
+        dn[k] -= e
+        fd[k] = (loss(up) - loss(dn)) / (2 * e)
+    assert np.abs(gp - fd).max() <= 1e-5 * np.abs(fd).max()
+    q0 = np.asarray(c["inlet_q"], dtype=float)
+    e = 1e-6 * q0[0]
+    fdq = (loss(q=q0 + e) - loss(q=q0 - e)) / (2 * e)
+    assert abs(r["g_inletq"][0] - fdq) <= 1e-5 * abs(fdq)
+
+
+@pytest.mark.parametrize("which", [0, 1, 2, 3, 4, 5])
+def test_ude_gradients_match_central_differences(which):
+    from tests import test_gpu_ude_grad as U
+    spec = U.CASES[which]
+    c = U.case()
+    hidden, _ = U.NETS[spec[1]]
+    theta = U.ude_params(spec[2], hidden, seed=20 + spec[1])
+    o = U.oracle(c, spec, theta)
+    N, Q0, dt, probes, obs = _flowing(c, o)
+    ctx = U.make(c, "fp64", spec, theta)
+    ctx.set_adjoint_integrator("tsit5")
+    r = ctx.loss_and_grad(Q0, RK, dt, probes, obs, ckpt_every=5)
+    g = ctx.ude_grad()
+
+    def loss(th):
+        return U.oracle(c, spec, th).tsit5_loss(Q0, RK, dt, probes, obs)[0]
+
+    assert abs(r["loss"] - loss(theta)) <= 1e-10 * abs(r["loss"])
+    v = Stream(17 + which).uniform(len(theta), -1.0, 1.0)
+    fd = {}
+    for e in (1e-4, 2e-4):   # Richardson's extrapolation of central differences along v
+        fd[e] = (loss(theta + e * v) - loss(theta - e * v)) / (2 * e)
+    fdr = (4 * fd[1e-4] - fd[2e-4]) / 3
+    assert abs(g @ v - fdr) <= 1e-5 * np.linalg.norm(g) * np.linalg.norm(v)
