@@ -120,6 +120,7 @@ __device__ __forceinline__ void vjp_cell(const DevMesh& m, const AdjDev& a, int 
   const float Aj = cs.z;
   const float mj0 = src.mu_own(0), mj1 = src.mu_own(1), mj2 = src.mu_own(2);
   float g0 = 0.0f, g1 = 0.0f, g2 = 0.0f, gn = 0.0f;
+  unsigned int bnd = 0u;   // FOLD: the slots that hold boundary faces
   if (!L.s.dry) {   // a dry cell's output is masked to zero, and its faces add to nothing else
     // Wet-wet faces in reverse mode (roe_wet_vjp, the own quantities'
     // adjoints summed over the faces and taken back once); faces with a dry
@@ -130,7 +131,10 @@ __device__ __forceinline__ void vjp_cell(const DevMesh& m, const AdjDev& a, int 
     for (int k = 0; k < NS; ++k) {
       const float4 sl = src.slot(k);
       const int32_t nb = slot_nb(sl);
-      if (nb < 0) continue;   // no face, or a boundary face (k_vjp_bnd_f32)
+      if (nb < 0) {   // no face, or a boundary face (folded below, or k_vjp_bnd_f32)
+        if (FOLD && nb != kNoFace) bnd |= 1u << k;
+        continue;
+      }
       const float nx = sl.x, ny = sl.y, len = sl.z;
       const VjpNbr r = src.nbr(nb);
       const SideF32 R = make_side_f32(r.x, r.p, m.hsmf, m.hsmLo);
@@ -185,14 +189,22 @@ __device__ __forceinline__ void vjp_cell(const DevMesh& m, const AdjDev& a, int 
       acc_add(&a.accF[(size_t)2 * n + j], beta, mj2 * m.gf * L.s.xi);
     }
   }
-  if constexpr (FOLD) {   // boundary faces: c = w . J, the terms k_vjp_bnd_f32 + k_vjp_combine_f32 give
+  if constexpr (FOLD) {   // a dry cell's boundary faces (the face loop above runs for wet cells)
+    if (L.s.dry) {
+#pragma unroll
+      for (int k = 0; k < NS; ++k) {
+        const int32_t nb = slot_nb(src.slot(k));
+        if (nb < 0 && nb != kNoFace) bnd |= 1u << k;
+      }
+    }
+  }
+  if (FOLD && bnd != 0u) {   // boundary faces: c = w . J, the terms k_vjp_bnd_f32 + k_vjp_combine_f32 give
     float gzbB = 0.0f;
 #pragma unroll
     for (int k = 0; k < NS; ++k) {
+      if (!(bnd & (1u << k))) continue;
       const float4 sl = src.slot(k);
-      const int32_t nb = slot_nb(sl);
-      if (nb >= 0 || nb == kNoFace) continue;
-      const int32_t bf = boundary_index(nb);
+      const int32_t bf = boundary_index(slot_nb(sl));
       const float w0 = -sl.z * mj0 / Aj, w1 = -sl.z * mj1 / Aj, w2 = -sl.z * mj2 / Aj;
       float J[24];
 #pragma unroll
