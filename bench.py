@@ -336,6 +336,95 @@ def run_dry_start(args, device):
     return out
 
 
+def run_tsit5(args, case, device):
+    """The reference's default integrator on the device (hg_integrate_tsit5:
+    Tsit5 with abstol 1e-6 / reltol 1e-3, swe_2D_forward_simulation.jl:37-39)
+    on the 1M-cell reach over tsit5_time simulated seconds, FP32C and FP64 (wall
+    time of the call: the state is copied in and out once); then the FP64
+    discrete adjoint of fixed Tsit5 steps (hg_set_adjoint_integrator) over
+    tsit5_adj_steps steps of the initial CFL-0.4 step."""
+    from hydrograd_gb.workloads import probes_and_perturbation
+    N = len(case["cell_node_count"])
+    out, final = {"cells": N, "simulated_seconds": args.tsit5_time}, {}
+    for prec in ("fp32c", "fp64"):
+        c = make_ctx(case, prec, device)
+        c.integrate_tsit5(case["Q0"], 0.0, 0.05)   # warm-up
+        c.synchronize()
+        t0 = time.perf_counter()
+        Q, st = c.integrate_tsit5(case["Q0"], 0.0, args.tsit5_time)
+        el = time.perf_counter() - t0
+        out[prec] = {"value": N * int(st[0]) / el, "seconds": el, "accepted": int(st[0]), "rejected": int(st[1]),
+                     "rhs_evaluations": int(st[2]), "cell_rhs_per_s": N * int(st[2]) / el}
+        # FP32C against FP64 on the same steps: the adaptive runs choose their
+        # steps from their own error estimates, so they compare fixed steps of
+        # the FP64 run's mean step over the same time
+        if prec == "fp32c":
+            fixed_n = int(st[0])
+        final[prec], _ = c.integrate_tsit5(case["Q0"], 0.0, args.tsit5_time, dt0=args.tsit5_time / fixed_n,
+                                           adaptive=False)
+        if prec == "fp64" and args.tsit5_adj_steps > 0:
+            probes, _ = probes_and_perturbation(case, 64, inlet_share=0.5)
+            dt = 0.5 * c.integrate(case["Q0"], 1, cfl=0.4)[1][0]
+            K = args.tsit5_adj_steps
+            obs = np.tile((case["wstill"] - case["zb_cells"])[probes], (K, 1))
+            c.set_adjoint_integrator("tsit5")
+            c.loss_and_grad(case["Q0"], 2, dt, probes, obs[:2])   # warm-up / allocation
+            t0 = time.perf_counter()
+            c.loss_and_grad(case["Q0"], K, dt, probes, obs, ckpt_every=K)
+            el = time.perf_counter() - t0
+            out["adjoint_fp64"] = {"value": N * K / el, "seconds": el, "steps": K}
+        c.close()
+    a, b = final["fp32c"], final["fp64"]
+    out["error_fp32c_vs_fp64_state_rel_linf"] = float(np.abs(a - b).max() / np.abs(b).max())
+    out["error_steps"] = fixed_n
+    out["config"] = ("Tsit5 adaptive (abstol 1e-6, reltol 1e-3) over %g s of the 1M-cell reach from its release; "
+                     "value = accepted steps x cells / wall second; FP32C against FP64 after the same fixed steps "
+                     "(the FP32C run's step count over the same time); the FP64 fixed-step Tsit5 adjoint (probe "
+                     "loss, 64 probes) at half the initial CFL-0.4 step" % args.tsit5_time)
+    return out
+
+
+def run_resistance(args, case, device):
+    """State-dependent resistance in every RHS evaluation:
+    Manning's n = sigmoid n(h) (process_ManningN_2D.jl:102-213) and a UDE
+    closure n = NN(h) (two tanh layers of 8 with batch LayerNorm,
+    process_UDE.jl:3-56) on the 1M-cell reach, res_steps CFL-0.4 SSP-RK2 steps
+    (L2 flushed before each), FP32C and FP64, and FP32C against FP64."""
+    N = len(case["cell_node_count"])
+    rng = np.random.default_rng(12)
+    theta, din = [], 1
+    for w in (8, 8):   # Glorot-uniform weights, small biases, LayerNorm affine terms near 1 and 0
+        lim = np.sqrt(6.0 / (din + w))
+        theta += [rng.uniform(-lim, lim, w * din), rng.uniform(-0.2, 0.2, w), rng.uniform(0.5, 1.5, w),
+                  rng.uniform(-0.3, 0.3, w)]
+        din = w
+    theta += [rng.uniform(-np.sqrt(6.0 / 9.0), np.sqrt(6.0 / 9.0), 8), rng.uniform(-0.2, 0.2, 1)]
+    theta = np.concatenate(theta)
+    out = {"cells": N, "steps": args.res_steps}
+    for kind in ("sigmoid", "ude"):
+        final = {}
+        for prec in ("fp32c", "fp64"):
+            c = make_ctx(case, prec, device)
+            if kind == "sigmoid":
+                c.set_manning_function("sigmoid", [0.02, 0.06, 3.0, 0.8])
+            else:
+                c.set_ude("ManningN_h", [8, 8], ["tanh", "tanh"], theta, output_bounds=(0.02, 0.06),
+                          h_bounds=(0.0, 4.0), layernorm_over_batch=True)
+            c.upload(case["Q0"])
+            c.advance_timed(args.warmup, cfl=0.4, flush_l2=True)
+            c.upload(case["Q0"])
+            ms = c.advance_timed(args.res_steps, cfl=0.4, flush_l2=True)
+            final[prec] = c.download()
+            out.setdefault(kind, {})[prec] = {"value": N * args.res_steps / (ms * 1e-3),
+                                              "ms_per_step": ms / args.res_steps}
+            c.close()
+        a, b = final["fp32c"], final["fp64"]
+        out[kind]["error_fp32c_vs_fp64_state_rel_linf"] = float(np.abs(a - b).max() / np.abs(b).max())
+    out["config"] = ("sigmoid n(h) {0.02, 0.06, 3, 0.8} and a UDE n = NN(h) (8-8 tanh, batch LayerNorm, output in "
+                     "[0.02, 0.06]) recomputed from every RHS evaluation's state, 1M-cell reach, SSP-RK2 CFL 0.4")
+    return out
+
+
 def run_config1(args, device, cpu):
     """Configuration 1 (hydrograd_gb.workloads.dam_break): 200 x 40 quads
     (8,000 cells) over 100 x 20 m, flat bed, walls, n = 0.03, h = 1.0 / 0.5 m
@@ -632,6 +721,8 @@ def run_ours(args):
                          f"{len(probes)} probes (half on the pool rim, half at the inlet), loss = mean squared "
                          "departure of the probe depths from the lake at rest")
     hll = run_hll(args, case, local) if args.hll_steps > 0 else None
+    ts5 = run_tsit5(args, case, local) if args.tsit5_time > 0 else None
+    res = run_resistance(args, case, local) if args.res_steps > 0 else None
     dry = run_dry_start(args, local) if args.dry_steps > 0 else None
     cfg1 = run_config1(args, local, cpu=not args.no_cpu and rank == 0) if args.config1_steps > 0 else None
     cfg5 = run_config5(args, local) if args.config5_steps > 0 else None
@@ -695,6 +786,8 @@ def run_ours(args):
         "fwd_adjoint": adj,
         "ensemble": ens,
         "hll": hll,
+        "tsit5": ts5,
+        "resistance": res,
         "dry_start": dry,
         "config1": cfg1,
         "config5": cfg5,
@@ -727,6 +820,11 @@ def main():
                     help="ensemble (configuration 4) forward+adjoint steps (0: skip)")
     ap.add_argument("--ens-ckpt", type=int, default=25)
     ap.add_argument("--ens-members", type=int, default=32, help="members per mesh")
+    ap.add_argument("--tsit5-time", type=float, default=1.0,
+                    help="simulated seconds of the Tsit5 leg on the 1M-cell reach (0: skip)")
+    ap.add_argument("--tsit5-adj-steps", type=int, default=10, help="steps of the FP64 Tsit5 adjoint leg (0: skip)")
+    ap.add_argument("--res-steps", type=int, default=200,
+                    help="CFL steps of the state-dependent resistance leg (0: skip)")
     ap.add_argument("--hll-steps", type=int, default=500,
                     help="FP32C steps of the HLL-solver leg on the 1M-cell reach (0: skip)")
     ap.add_argument("--dry-steps", type=int, default=2000,
