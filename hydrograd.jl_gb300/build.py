@@ -19,10 +19,11 @@ LIB = os.path.join(OUT, "libhydrograd_gb.so")
 INCLUDE = os.path.join(ROOT, "include")
 
 CUDA_SOURCES = ["hg_forward_f64.cu", "hg_forward_f32.cu", "hg_adjoint_f64.cu", "hg_adjoint_f32.cu", "hg_noalloc.cu",
-                "hg_tsit5.cu", "hg_resistance.cu", "hg_final_loss.cu"]
+                "hg_tsit5.cu", "hg_resistance.cu", "hg_resistance_f32.cu", "hg_final_loss.cu"]
 # FP64 parity path: no fused multiply-add, as in the reference (and in the
-# Tsit5 stage sums and the resistance functions, which the oracle forms with
-# separate multiplies and adds).
+# Tsit5 stage sums and the FP64 resistance functions, which the oracle forms
+# with separate multiplies and adds; their FP32 instantiations,
+# hg_resistance_f32.cu, contract).
 NO_FMAD = {"hg_forward_f64.cu", "hg_tsit5.cu", "hg_resistance.cu"}
 # FP32-compensated path: approximate division/sqrt/log2/exp2 (a few ulp; the
 # path's contract is a 1e-5 state error against the FP64 oracle).

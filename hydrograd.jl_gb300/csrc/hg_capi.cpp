@@ -458,7 +458,7 @@ int install_resistance(hg_ctx* c, ResDev r, const double* ksUser, const double* 
     HG_CUDA(c, dalloc(c, &c->d_resW, kResMaxParams));
     HG_CUDA(c, dalloc(c, &c->d_resWf, kResMaxParams));
     HG_CUDA(c, dalloc(c, &c->d_resStats, 2 * kResMaxLayers));
-    HG_CUDA(c, dalloc(c, &c->d_resPartials, kResPartials));
+    HG_CUDA(c, dalloc(c, &c->d_resPartials, 4 * (size_t)res_stat_blocks(c->n)));
     HG_CUDA(c, dalloc(c, &c->d_resTicket, 1));
     HG_CUDA(c, dalloc(c, &c->d_fres, c->n));
     HG_CUDA(c, dalloc(c, &c->d_fresF, c->n));
@@ -479,6 +479,20 @@ int install_resistance(hg_ctx* c, ResDev r, const double* ksUser, const double* 
   r.ticket = c->d_resTicket;
   r.fres = c->d_fres;
   r.fresF = c->d_fresF;
+  if (r.kind >= kResUdeManningH && r.overBatch && r.nHidden > 0) {   // the statistics passes' cache of the hidden layers
+    size_t rows = 0;
+    for (int l = 0; l < r.nHidden; ++l) rows += (size_t)r.width[l];
+    const size_t bytes = rows * (size_t)c->n * (c->precision == HG_FP64 ? sizeof(double) : sizeof(float));
+    if (bytes > c->resActBytes) {
+      cudaFree(c->d_resAct);
+      c->d_resAct = nullptr;
+      c->resActBytes = 0;
+      HG_CUDA(c, cudaMalloc(&c->d_resAct, bytes));
+      c->resActBytes = bytes;
+    }
+    if (c->precision == HG_FP64) r.hid = static_cast<double*>(c->d_resAct);
+    else r.hidF = static_cast<float*>(c->d_resAct);
+  }
   c->dm.res = r;
   c->udeParams = r.kind >= kResUdeManningH ? nParams : 0;
   c->udeGrad.clear();
@@ -584,6 +598,7 @@ hg_ctx::~hg_ctx() {
   for (void* p : allocs) cudaFree(p);
   if (ds.dtHist) cudaFree(ds.dtHist);
   if (ds.dtHistM) cudaFree(ds.dtHistM);
+  if (d_resAct) cudaFree(d_resAct);
   adjoint_release(this);
   if (stream) cudaStreamDestroy(stream);
 }

@@ -85,6 +85,8 @@ struct hg_ctx {
   // State-dependent resistance (hg_set_manning_function / hg_set_ude): device
   // buffers, allocated on first use; dm.res points into them.
   double *d_resKs = nullptr, *d_resW = nullptr, *d_resStats = nullptr, *d_resPartials = nullptr, *d_fres = nullptr;
+  void* d_resAct = nullptr;   // the network's cached hidden-layer values (ResDev::hid / hidF)
+  size_t resActBytes = 0;
   float *d_resWf = nullptr, *d_fresF = nullptr;
   unsigned int* d_resTicket = nullptr;
   // Inlet-Q hydrographs (hg_set_inlet_hydrograph): per group its times then

@@ -22,6 +22,7 @@ struct RM<double> {
   static __device__ double sqrt(double x) { return ::sqrt(x); }
   static __device__ double abs(double x) { return ::fabs(x); }
   static __device__ double w(const hg::ResDev& r, int i) { return r.w[i]; }
+  static __device__ double* hid(const hg::ResDev& r) { return r.hid; }
 };
 template <>
 struct RM<float> {
@@ -33,6 +34,7 @@ struct RM<float> {
   static __device__ float sqrt(float x) { return ::sqrtf(x); }
   static __device__ float abs(float x) { return ::fabsf(x); }
   static __device__ float w(const hg::ResDev& r, int i) { return r.wf[i]; }
+  static __device__ float* hid(const hg::ResDev& r) { return r.hidF; }
 };
 // Dual numbers: each function's value by the scalar form above, its tangents
 // by the chain rule.

@@ -24,7 +24,11 @@ enum ResKind : int32_t {
 constexpr int kResMaxLayers = 4;     // hidden Dense + LayerNorm layers
 constexpr int kResMaxWidth = 16;     // neurons per hidden layer
 constexpr int kResMaxInputs = 3;
-constexpr int kResPartials = 1024;   // blocks of a LayerNorm statistics pass
+constexpr int kResBlock = 256;       // threads of a resistance block (one cell each)
+// Blocks of a LayerNorm statistics pass over n cells, at most (four partials
+// each: the block's sum, squared deviations about its mean, its count of
+// values, that mean).
+constexpr int64_t res_stat_blocks(int64_t n) { return (n + kResBlock - 1) / kResBlock; }
 struct ResDev {
   int32_t kind = kResConstant;
   double p[4] = {0.0, 0.0, 0.0, 0.0};   // n_lower, n_upper, k, h_mid
@@ -41,10 +45,16 @@ struct ResDev {
   // the flow-resistance closure), [2] ks
   double lo[kResMaxInputs] = {0.0, 0.0, 0.0}, hi[kResMaxInputs] = {1.0, 1.0, 1.0};
   double* stats = nullptr;              // [2 * kResMaxLayers] LayerNorm mean, variance over all cells
-  double* partials = nullptr;           // [kResPartials]
+  double* partials = nullptr;           // [4 res_stat_blocks(n)]
   unsigned int* ticket = nullptr;
   double* fres = nullptr;               // [n] friction magnitude (flow-resistance closure), FP64 path
   float* fresF = nullptr;               // the same, FP32 path
+  // LayerNorm over the batch: the hidden layers' post-activation values of
+  // every cell, [sum of widths][n] (layer l's rows from the sum of the widths
+  // before it), kept by the statistics passes so that each pass starts from
+  // the layer before instead of the inputs (FP64 path: hid; FP32 path: hidF)
+  double* hid = nullptr;
+  float* hidF = nullptr;
 };
 
 struct DevMesh {

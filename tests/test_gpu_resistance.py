@@ -9,6 +9,7 @@ import numpy as np
 import pytest
 
 from hydrograd_gb import HgError
+from hydrograd_gb._lib import ACTIVATIONS
 from tests.golden_cases import initial_state, load_fixture
 from tests.resistance_cases import UDE_CASES, truth_state, ude_params
 from tests.test_gpu_forward import block_err, rhs_err, setup_pair
@@ -86,6 +87,32 @@ def test_ude_rhs_and_steps_match_oracle(choice, kind, in_dim, bounds, over_batch
     dt = 0.5 * o.cfl_dt(Q0, 0.4)
     Qg, _ = ctx.integrate(Q0, 50, dt=dt)
     Qo = o.rk2(Q0, 50, dt=dt, nthreads=4)
+    assert block_err(Qg, Qo, N) <= STATE_TOL[precision]
+
+
+WIDTHS = [([8, 8], ["tanh", "tanh"]), ([16, 5], ["sigmoid", "softplus"]), ([2], ["relu"]),
+          ([4, 9, 3], ["leakyrelu", "tanh", "sigmoid"])]
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32c"])
+@pytest.mark.parametrize("over_batch", [True, False], ids=["ln_batch", "ln_cell"])
+@pytest.mark.parametrize("hidden,acts", WIDTHS, ids=["8-8", "16-5", "2", "4-9-3"])
+def test_ude_widths_match_oracle(hidden, acts, over_batch, precision):
+    """Networks of every register width the forward kernels take (4, 8, 16
+    values a layer) and depths 1 to 3."""
+    d = load_fixture("fwd_savannah_nks")
+    ctx, o, N = setup_pair(d, precision)
+    bounds = dict(output_bounds=(0.03, 0.06), h_bounds=(0.1, 0.5))
+    p = ude_params(1, hidden, seed=40 + sum(hidden))
+    ctx.set_ude("ManningN_h", hidden, acts, p, layernorm_over_batch=over_batch, **bounds)
+    o.set_ude(5, 1, hidden, [ACTIVATIONS[a] for a in acts], p, bounds["output_bounds"], bounds["h_bounds"],
+              (0.0, 1.0), (0.0, 1.0), None, over_batch)
+    for Q in states(d, N):
+        assert rhs_err(ctx.rhs(Q), o.rhs(Q), o, Q) <= RHS_TOL[precision]
+    Q0 = initial_state(d, N)
+    dt = 0.5 * o.cfl_dt(Q0, 0.4)
+    Qg, _ = ctx.integrate(Q0, 20, dt=dt)
+    Qo = o.rk2(Q0, 20, dt=dt, nthreads=4)
     assert block_err(Qg, Qo, N) <= STATE_TOL[precision]
 
 
