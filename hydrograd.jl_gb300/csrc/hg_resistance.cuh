@@ -55,6 +55,11 @@ __device__ __forceinline__ S activation(int a, S x) {
     default: return RM<S>::log1p(RM<S>::exp(-RM<S>::abs(x))) + (x > S(0) ? x : S(0));   // softplus
   }
 }
+// ACT >= 0: the activation fixed at compile time; ACT < 0: a, at run time.
+template <int ACT, class S>
+__device__ __forceinline__ S activation_as(int a, S x) {
+  return activation(ACT >= 0 ? ACT : a, x);
+}
 
 template <class S>
 __device__ __forceinline__ S normalise(S x, double lo, double hi) {
@@ -251,7 +256,7 @@ __device__ __forceinline__ void batch_stats(const ResDev& r, int l, S& mu, S& de
 
 // z = act(W a + b) with the staged Dense layer; each output's terms are added
 // in input order, then the bias, as dense_act does.
-template <class S, int MW>
+template <int ACT, class S, int MW>
 __device__ __forceinline__ void dense_act_staged(const LayerParams<S, MW>& P, int din, int w, int act,
                                                  const S (&a)[MW], S (&z)[MW]) {
   S s[MW];
@@ -264,7 +269,7 @@ __device__ __forceinline__ void dense_act_staged(const LayerParams<S, MW>& P, in
       for (int o = 0; o < MW; ++o) s[o] += P.W[i][o] * a[i];
     }
 #pragma unroll
-  for (int o = 0; o < MW; ++o) z[o] = o < w ? activation(act, s[o] + P.b[o]) : S(0);
+  for (int o = 0; o < MW; ++o) z[o] = o < w ? activation_as<ACT>(act, s[o] + P.b[o]) : S(0);
 }
 
 template <class S>
@@ -284,7 +289,7 @@ __device__ __forceinline__ double block_total(S v) {
 // Chan, Golub and LeVeque's pairwise update: mean = sum S_b / N,
 // M2 = sum (M2_b + N_b (m_b - mean)^2) -- the two-pass variance with one pass
 // over the layer's inputs.
-template <class S, class State, int MW>
+template <class S, class State, int MW, int ACT>
 __global__ void __launch_bounds__(kBlock) k_res_layer(DevMesh m, State Q, int l) {
   const ResDev& r = m.res;
   __shared__ LayerParams<S, MW> P;
@@ -311,7 +316,7 @@ __global__ void __launch_bounds__(kBlock) k_res_layer(DevMesh m, State Q, int l)
       load_hidden(r, l - 1, n, c, zp);
       layer_norm_staged(P, din, mu, den, zp, a);
     }
-    dense_act_staged(P, din, w, r.act[l], a, z);
+    dense_act_staged<ACT>(P, din, w, r.act[l], a, z);
 #pragma unroll
     for (int o = 0; o < MW; ++o)
       if (o < w) {
@@ -438,6 +443,13 @@ void launch_cells(const DevMesh& m, State Q, cudaStream_t st) {
   k_res_cells<S, State, MW, PATH><<<(int)(need < g ? need : g), kBlock, 0, st>>>(m, Q);
 }
 
+template <class S, class State, int MW, int ACT>
+void launch_layer(const DevMesh& m, State Q, int l, cudaStream_t st) {
+  static const int g = one_wave(k_res_layer<S, State, MW, ACT>, 1 << 30);
+  const int64_t need = res_stat_blocks(m.n);
+  k_res_layer<S, State, MW, ACT><<<(int)(need < g ? need : g), kBlock, 0, st>>>(m, Q, l);
+}
+
 template <class S, class State, int MW>
 int launch_resistance_w(const DevMesh& m, State Q, cudaStream_t st) {
   const ResDev& r = m.res;
@@ -449,10 +461,19 @@ int launch_resistance_w(const DevMesh& m, State Q, cudaStream_t st) {
     launch_cells<S, State, MW, kPathNet>(m, Q, st);
     return 1;
   }
-  static const int gLayer = one_wave(k_res_layer<S, State, MW>, 1 << 30);
-  const int64_t need = res_stat_blocks(m.n);
-  for (int l = 0; l < r.nHidden; ++l)
-    k_res_layer<S, State, MW><<<(int)(need < gLayer ? need : gLayer), kBlock, 0, st>>>(m, Q, l);
+  for (int l = 0; l < r.nHidden; ++l) {
+    if constexpr (sizeof(S) == 4) {   // the activation a template argument (FP64: read at run time)
+      switch (r.act[l]) {
+        case 0: launch_layer<S, State, MW, 0>(m, Q, l, st); break;
+        case 1: launch_layer<S, State, MW, 1>(m, Q, l, st); break;
+        case 2: launch_layer<S, State, MW, 2>(m, Q, l, st); break;
+        case 3: launch_layer<S, State, MW, 3>(m, Q, l, st); break;
+        default: launch_layer<S, State, MW, 4>(m, Q, l, st); break;
+      }
+    } else {
+      launch_layer<S, State, MW, -1>(m, Q, l, st);
+    }
+  }
   launch_cells<S, State, MW, kPathCached>(m, Q, st);
   return r.nHidden + 1;
 }
