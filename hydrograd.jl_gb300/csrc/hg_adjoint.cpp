@@ -819,6 +819,7 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
         f.ticket = c->d_ticket;
         f.blockSlot = c->d_blockSlot;
         f.nSlots = c->nSlots;
+        f.nWarps = c->nWarps;
         f.totalIn = t0;
         f.totalOut = t1;
         hydro(s * dt);

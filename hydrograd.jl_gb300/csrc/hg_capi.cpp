@@ -227,6 +227,7 @@ void enqueue_rk2_step_fused(hg_ctx* c, bool cflMode, double cfl) {
   f.ticket = c->d_ticket;
   f.blockSlot = c->d_blockSlot;
   f.nSlots = c->nSlots;
+  f.nWarps = c->nWarps;
   f.cflMode = cflMode ? 1 : 0;
   f.cfl = cfl;
   f.parity = c->parity;
@@ -305,9 +306,10 @@ int set_fixed_dt(hg_ctx* c, double dt) {
 
 // Autotuner of the fused FP32 stages.  Its candidates are kernels and shapes
 // that compute bit-identical results, so the choice changes speed only:
-//   family 0: the gather kernel with the register budget of 4 or 3 resident
-//             blocks per SM, the pipelined persistent kernel, the bulk-copy
-//             persistent kernel;
+//   family 0: the gather kernel in four shapes -- 256-cell blocks with the
+//             register budget of 4 or 3 resident per SM, 512-cell blocks at
+//             2 per SM, 128-cell blocks at 8 per SM -- the pipelined
+//             persistent kernel, the bulk-copy persistent kernel;
 //   family 1: the face-once kernel with the budget of 4 or 3 blocks per SM.
 // (The face-once kernel evaluates each wet-wet face once and so rounds
 // differently from the gather family; which family a context uses is fixed by
@@ -326,8 +328,8 @@ std::vector<TuneChoice> stage_candidates(const hg_ctx* c, StateF32 s1) {
   if (c->stageFamily == 1) {
     all = {TuneChoice{kStageFace, 0}, TuneChoice{kStageFace, 1}};
   } else {
-    all = {TuneChoice{kStageGather, 0}, TuneChoice{kStageGather, 1}, TuneChoice{kStagePipe, 0},
-           TuneChoice{kStageTma, 0}};
+    all = {TuneChoice{kStageGather, 0}, TuneChoice{kStageGather, 1}, TuneChoice{kStageGather, 2},
+           TuneChoice{kStageGather, 3}, TuneChoice{kStagePipe, 0}, TuneChoice{kStageTma, 0}};
     if (c->dm.nslot > 4) all = {TuneChoice{kStageGather, 0}};
   }
   std::vector<TuneChoice> out;
@@ -391,6 +393,7 @@ int autotune_stage(hg_ctx* c, int reps, bool useCache) {
   f.ticket = c->d_ticket;
   f.blockSlot = c->d_blockSlot;
   f.nSlots = c->nSlots;
+  f.nWarps = c->nWarps;
   for (int r = 0; r < reps; ++r)
     for (size_t i = 0; i < cand.size(); ++i) {
       DevMesh m = c->dm;
@@ -1295,6 +1298,7 @@ int hg_time_stage_kernel(hg_ctx* ctx, int32_t n, int32_t flush_l2, double* avg_m
       f.ticket = ctx->d_ticket;
       f.blockSlot = ctx->d_blockSlot;
       f.nSlots = ctx->nSlots;
+      f.nWarps = ctx->nWarps;
       f.totalIn = ctx->d_tot;
       f.totalOut = ctx->d_tot + kMaxFusedInlets;
       launch_stage_f32_fused(ctx->dm, ctx->ds, kModeStage1, xa(ctx), StateF32{}, xb(ctx), f, ctx->stream);
@@ -1518,9 +1522,17 @@ int ctx_setup_device(hg_ctx* c) {
     blockSlot.assign(nBlocks, -1);
     for (int32_t cell : inletCell) blockSlot[cell / kStageBlockF32] = 0;
     c->nSlots = 0;
+    c->nWarps = 0;
     for (int b = 0; b < nBlocks; ++b)
-      if (blockSlot[b] == 0) blockSlot[b] = c->nSlots++;
-    HG_CUDA(c, dalloc(c, &c->d_partials, (size_t)kMaxFusedInlets * std::max(c->nSlots, 1)));
+      if (blockSlot[b] == 0) {
+        blockSlot[b] = c->nSlots++;
+        const int cells = std::min(kStageBlockF32, N - b * kStageBlockF32);
+        c->nWarps += (cells + 31) / 32;
+      }
+    // warp sums of the fused inlet totals; the slots of warps past the last cell stay zero
+    const size_t np = (size_t)kMaxFusedInlets * std::max(c->nSlots, 1) * (kStageBlockF32 / 32);
+    HG_CUDA(c, dalloc(c, &c->d_partials, np));
+    HG_CUDA(c, cudaMemsetAsync(c->d_partials, 0, np * sizeof(double), c->stream));
     HG_CUDA(c, dalloc(c, &c->d_blockSlot, blockSlot.size()));
   }
   HG_CUDA(c, dalloc(c, &c->d_ticket, 1));

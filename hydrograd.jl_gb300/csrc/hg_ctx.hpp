@@ -59,6 +59,7 @@ struct hg_ctx {
   unsigned int* d_ticket = nullptr;
   int32_t* d_blockSlot = nullptr;   // slot of each stage block that holds inlet cells, else -1
   int32_t nSlots = 0;
+  int32_t nWarps = 0;   // warps of the tiles holding inlet cells (StageFuse::nWarps)
   int parity = 0;                   // CFL-minimum buffer the next fused step reads
   int graphParity = 0;              // parity the captured graph starts (and ends) with
   // Captured graph of kGraphSteps steps

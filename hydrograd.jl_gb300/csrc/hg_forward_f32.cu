@@ -40,7 +40,9 @@ inline int blocks_for(int n) { return (n + kBlock - 1) / kBlock; }
 // halo cells at [kBlock, ...) of hX / hP); otherwise a cell id.  RS: the
 // Riemann solver fixed at compile time (kRiemannRoe / kRiemannHll), or -1 for
 // the context's at run time (DevMesh::riemann).
-template <bool LOC, int RS>
+// TB: the cells of the launch's block (the non-LOC in-block test; kBlock
+// unless the gather kernel runs another tile size).
+template <bool LOC, int RS, int TB = kBlock>
 __device__ __forceinline__ void one_face_f32(const DevMesh& m, const float4* __restrict__ X, const float4* sX,
                                              const float4* sP, const float4* hX, const float4* hP, int base, int c,
                                              const SideF32& L, const OwnF32& own, float2 hstPair, float4 sl, int32_t nb,
@@ -63,7 +65,7 @@ __device__ __forceinline__ void one_face_f32(const DevMesh& m, const float4* __r
       }
     } else {
       const unsigned int ln = (unsigned int)(nb - base);   // in-block neighbour: staged record
-      if (ln < (unsigned int)kBlock) {
+      if (ln < (unsigned int)TB) {
         xr = sX[ln];
         pr = sP[ln];
       } else {
@@ -108,7 +110,7 @@ __device__ __forceinline__ void one_face_f32(const DevMesh& m, const float4* __r
   }
 }
 
-template <int NS, bool LOC, int RS>
+template <int NS, bool LOC, int RS, int TB = kBlock>
 __device__ __forceinline__ void face_sum_f32(const DevMesh& m, const float4* __restrict__ X, const float4* sX,
                                              const float4* sP, const float4* hX, const float4* hP, int base, int c,
                                              const SideF32& L, const OwnF32& own, float2 hstPair,
@@ -120,7 +122,7 @@ __device__ __forceinline__ void face_sum_f32(const DevMesh& m, const float4* __r
     const int32_t nb = slot_nb(sl[k]);
     if (nb == kNoFace) continue;
     float F[3];
-    one_face_f32<LOC, RS>(m, X, sX, sP, hX, hP, base, c, L, own, hstPair, sl[k], nb, totalA, man, flags, F);
+    one_face_f32<LOC, RS, TB>(m, X, sX, sP, hX, hP, base, c, L, own, hstPair, sl[k], nb, totalA, man, flags, F);
     const float len = sl[k].z;
     f0 = fmaf(F[0], len, f0);
     const float2 f12 = fma2(p2(F[1], F[2]), p2(len), p2(f1, f2));
@@ -149,45 +151,64 @@ __device__ __forceinline__ void load_slots(const DevMesh& m, int c, float4 (&sl)
   for (int k = 0; k < NS; ++k) sl[k] = __ldg(&m.SL[(size_t)k * m.n + c]);
 }
 
-// Inlet-Q conveyance totals of a fused stage's output state (bc_2D.jl:673-676):
-// the blocks that hold inlet cells write partial sums; the last of them adds
-// the partials in slot order.  Only those few blocks reload the slot records,
-// so the other blocks carry no extra registers for it.
+// Inlet-Q conveyance totals of a fused stage's output state (bc_2D.jl:673-676).
+// The sums are keyed to fixed tiles of kBlock cells, whatever the launch's
+// block size: each warp of a tile holding inlet cells writes its warp sum
+// (partials[g][slot][warp]), and the last warp to arrive adds them -- each
+// tile's warp sums in the fixed tree of devred::block_sum (halves folded), the
+// tiles' sums lane-strided and folded across the warp -- so every stage
+// kernel and tile size forms the same totals.  Warps past the last cell never
+// write: their partials stay at the zeros the buffer was allocated with.
+// Only the warps of those few tiles reload the slot records, so the others
+// carry no extra registers for it.
+constexpr int kTileWarps = kBlock / 32;
 template <int NS>
-__device__ __forceinline__ void fused_inlet_totals(const DevMesh& m, const StageFuse& f, int tile, int c, float hOut,
+__device__ __forceinline__ void fused_inlet_totals(const DevMesh& m, const StageFuse& f, int c, float hOut,
                                                    bool wetOut) {
-  const int slot = f.blockSlot[tile];
-  if (slot < 0) return;   // uniform over the block
-  __shared__ int isLast;
+  const int lane = threadIdx.x & 31;
+  const int c0 = c - lane;   // the warp's first cell; warps never straddle tiles (32 divides kBlock)
+  if (c0 >= m.n) return;     // uniform over the warp
+  const int slot = f.blockSlot[c0 / kBlock];
+  if (slot < 0) return;
+  const int wIdx = (c0 % kBlock) / 32;
   const int ng = m.nInlet;
   for (int g = 0; g < ng; ++g) {
-    double contrib = 0.0;
+    double v = 0.0;
     if (wetOut) {
       for (int k = 0; k < NS; ++k) {
         const int32_t nb = slot_nb(m.SL[(size_t)k * m.n + c]);
         if (nb >= 0 || nb == kNoFace) continue;
         const int32_t bf = boundary_index(nb);
-        if (m.bfInfo[bf] == (kBcInletQ | (g << 2))) contrib += m.bfLp53[bf] * (double)hOut / (double)m.CP[c].w;
+        if (m.bfInfo[bf] == (kBcInletQ | (g << 2))) v += m.bfLp53[bf] * (double)hOut / (double)m.CP[c].w;
       }
     }
-    const double t = block_sum(contrib);
-    if (threadIdx.x == 0) f.partials[(size_t)g * f.nSlots + slot] = t;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) f.partials[((size_t)g * f.nSlots + slot) * kTileWarps + wIdx] = v;
   }
-  if (threadIdx.x == 0) {
+  unsigned int last = 0u;
+  if (lane == 0) {
     __threadfence();
-    const unsigned int t = atomicAdd(f.ticket, 1u);
-    isLast = (t == (unsigned int)f.nSlots - 1u);
+    last = atomicAdd(f.ticket, 1u) == (unsigned int)f.nWarps - 1u ? 1u : 0u;
   }
-  __syncthreads();
-  if (!isLast) return;
+  if (!__shfl_sync(0xffffffffu, last, 0)) return;
   __threadfence();
   for (int g = 0; g < ng; ++g) {
     double acc = 0.0;
-    for (int b = threadIdx.x; b < f.nSlots; b += blockDim.x) acc += __ldcg(&f.partials[(size_t)g * f.nSlots + b]);
-    const double t = block_sum(acc);
-    if (threadIdx.x == 0) f.totalOut[g] = t;
+    for (int b = lane; b < f.nSlots; b += 32) {
+      const double* p = f.partials + ((size_t)g * f.nSlots + b) * kTileWarps;
+      double r[kTileWarps];
+#pragma unroll
+      for (int i = 0; i < kTileWarps; ++i) r[i] = __ldcg(&p[i]);
+#pragma unroll
+      for (int h = kTileWarps / 2; h >= 1; h >>= 1)
+#pragma unroll
+        for (int i = 0; i < h; ++i) r[i] += r[i + h];
+      acc += r[0];
+    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) f.totalOut[g] = acc;
   }
-  if (threadIdx.x == 0) *f.ticket = 0u;
+  if (lane == 0) *f.ticket = 0u;
 }
 
 // dt of a fused step: from the published CFL minimum (CFL mode) or the fixed dt.
@@ -219,7 +240,7 @@ __device__ __forceinline__ void stage_finish(const DevMesh& m, const DevScalars&
 // kBlock) for in-block neighbours.  The input state's lo parts and (stage 2)
 // the base state are read at qinP[k], xbP[k], qbP[k] -- global arrays (k = c)
 // or a tile staged in shared memory -- where they are used.
-template <int NS, int MODE, bool LOC = false, int RS = -1>
+template <int NS, int MODE, bool LOC = false, int RS = -1, int TB = kBlock>
 __device__ __forceinline__ void stage_cell(const DevMesh& m, const DevScalars& s, const float4* __restrict__ X,
                                            const float4* sX, const float4* sP, const float4* hX, const float4* hP,
                                            int base, int c,
@@ -230,7 +251,7 @@ __device__ __forceinline__ void stage_cell(const DevMesh& m, const DevScalars& s
   const SideF32 L = make_side_f32(xin, cp, m.hsmf, m.hsmLo);
   const OwnF32 own = own_f32(L.s, m.gf);
   float f0, f1, f2;
-  face_sum_f32<NS, LOC, RS>(m, X, sX, sP, hX, hP, base, c, L, own, make_float2(cp.x, cp.y), sl, totalIn, cp.w, s.flags, f0, f1, f2);
+  face_sum_f32<NS, LOC, RS, TB>(m, X, sX, sP, hX, hP, base, c, L, own, make_float2(cp.x, cp.y), sl, totalIn, cp.w, s.flags, f0, f1, f2);
   stage_finish<NS, MODE>(m, s, L, f0, f1, f2, c, sl, xin, cp, cs, qinP, xbP, qbP, k, dt, Xout, Rout, cfl, cand, hOut,
                          wetOut);
 }
@@ -325,12 +346,14 @@ __device__ __forceinline__ void fused_record(const DevScalars& s, const StageFus
 // the fused step's dt is formed once per block.
 // MINB > 0: the register budget of MINB resident blocks per SM (a shape the
 // autotuner chooses among; the arithmetic does not depend on it).
-template <int NS, bool FUSED, int MODE, int RS = -1, int MINB = 0>
-__global__ void __launch_bounds__(kBlock, MINB > 0 ? MINB : stage_min_blocks<NS>())
+// TB: cells per block (the autotuner's tile-size candidates: 128, 256, 512;
+// a cell's arithmetic does not depend on it).
+template <int NS, bool FUSED, int MODE, int RS = -1, int MINB = 0, int TB = kBlock>
+__global__ void __launch_bounds__(TB, MINB > 0 ? MINB : stage_min_blocks<NS>())
     k_stage_f32(DevMesh m, DevScalars s, StateF32 Xin, StateF32 Xbase, StateF32 Xout, double* Rout, int cfl,
                 StageFuse f) {
   pdl_enter();
-  const int base = blockIdx.x * kBlock;
+  const int base = blockIdx.x * TB;
   const int c = base + threadIdx.x;
   const bool active = c < m.n;
   float cand = INFINITY;
@@ -340,7 +363,7 @@ __global__ void __launch_bounds__(kBlock, MINB > 0 ? MINB : stage_min_blocks<NS>
   // the block (most of them, in Hilbert order): every global load of the block
   // is issued before the barrier, and in-block neighbour reads skip a second
   // round trip to L2/DRAM.
-  __shared__ float4 sX[kBlock], sP[kBlock];
+  __shared__ float4 sX[TB], sP[TB];
   __shared__ float dtShared;
   float4 sl[NS], xin, cp, cs;
   if (active) {
@@ -358,14 +381,14 @@ __global__ void __launch_bounds__(kBlock, MINB > 0 ? MINB : stage_min_blocks<NS>
   const int mem = (!FUSED && s.nMembers > 0 && active) ? member_of(s, c) : -1;   // an ensemble member's own step
   if (active) {
     const float dt = MODE == kModeRhs ? 0.0f : (FUSED ? dtShared : (mem >= 0 ? s.dtMf[mem] : *s.dtf));
-    stage_cell<NS, MODE, false, RS>(m, s, Xin.x, sX, sP, nullptr, nullptr, base, c, sl, xin, cp, cs, Xin.q, Xbase.x,
+    stage_cell<NS, MODE, false, RS, TB>(m, s, Xin.x, sX, sP, nullptr, nullptr, base, c, sl, xin, cp, cs, Xin.q, Xbase.x,
                                      Xbase.q, c,
                          dt, FUSED ? f.totalIn : m.totalA, Xout, Rout, cfl, cand, hOut, wetOut);
   }
   if (FUSED && f.record && blockIdx.x == 0 && threadIdx.x == 0) fused_record(s, f);
   if (cfl && !FUSED && s.nMembers > 0) member_min_publish_f(s, cand, mem);
   else if (cfl) block_min_publish_f(cand, FUSED ? s.cflMinF + (1 - f.parity) : s.cflMinF);
-  if (FUSED && m.nInlet > 0) fused_inlet_totals<NS>(m, f, blockIdx.x, c, hOut, wetOut);
+  if (FUSED && m.nInlet > 0) fused_inlet_totals<NS>(m, f, c, hOut, wetOut);
 }
 
 // ---------------------------------------------------------------------------
@@ -484,7 +507,7 @@ __global__ void __launch_bounds__(kBlock, kTmaCtasPerSm)
                                       bQ, bXB,
                            bQB, tid, dt, f.totalIn, Xout, nullptr, cfl, cand, hOut, wetOut);
     }
-    if (m.nInlet > 0) fused_inlet_totals<NS>(m, f, t, c, hOut, wetOut);
+    if (m.nInlet > 0) fused_inlet_totals<NS>(m, f, c, hOut, wetOut);
     __syncthreads();   // buffer b is refilled by the copy issued at the top of the iteration after next
   }
   if (f.record && blockIdx.x == 0 && tid == 0) fused_record(s, f);
@@ -597,7 +620,7 @@ __global__ void __launch_bounds__(kBlock, kPipeCtasPerSm)
       member_min_publish_f(s, cand, mem);
       cand = INFINITY;
     }
-    if (FUSED && m.nInlet > 0) fused_inlet_totals<NS>(m, f, t, c, hOut, wetOut);
+    if (FUSED && m.nInlet > 0) fused_inlet_totals<NS>(m, f, c, hOut, wetOut);
     __syncthreads();   // buffer b is refilled at the top of the next iteration
   }
   cp_async_wait<0>();
@@ -840,7 +863,7 @@ __global__ void __launch_bounds__(kBlock, MINB)
   }
   if (FUSED && f.record && blockIdx.x == 0 && tid == 0) fused_record(s, f);
   if (cfl) block_min_publish_f(cand, FUSED ? s.cflMinF + (1 - f.parity) : s.cflMinF);
-  if (FUSED && m.nInlet > 0) fused_inlet_totals<NS>(m, f, tile, c, hOut, wetOut);
+  if (FUSED && m.nInlet > 0) fused_inlet_totals<NS>(m, f, c, hOut, wetOut);
 }
 
 template <int NS>
@@ -1018,21 +1041,38 @@ void launch_inlet_total_f32(const DevMesh& m, const DevScalars& s, StateF32 X, c
   if (m.nInlet > 0) k_inlet_total_f32<<<m.nInlet, kBlock, 0, st>>>(m, s, X);
 }
 namespace {
+// The fused gather kernel's shapes (DevMesh::stageVariant, the autotuner's
+// candidates; the same arithmetic in each): 0 the default, 256-cell blocks
+// with the register budget of 4 resident per SM (64 registers); 1 the same
+// blocks at 3 per SM (80 registers); 2 512-cell blocks at 2 per SM and 3
+// 128-cell blocks at 8 per SM (64 registers, as 0).
+template <int NS, int MODE, int RS>
+void launch_gather_shape(int v, const DevMesh& m, const DevScalars& s, StateF32 Xin, StateF32 Xbase, StateF32 Xout,
+                         double* Rout, int cfl, const StageFuse& f, cudaStream_t st) {
+  auto grid = [&](int tb) { return (m.n + tb - 1) / tb; };
+  if (v == 1)
+    launch_k(true, k_stage_f32<NS, true, MODE, RS, 3>, grid(kBlock), kBlock, 0, st, m, s, Xin, Xbase, Xout, Rout, cfl, f);
+  else if (v == 2)
+    launch_k(true, k_stage_f32<NS, true, MODE, RS, 2, 512>, grid(512), 512, 0, st, m, s, Xin, Xbase, Xout, Rout, cfl, f);
+  else if (v == 3)
+    launch_k(true, k_stage_f32<NS, true, MODE, RS, 8, 128>, grid(128), 128, 0, st, m, s, Xin, Xbase, Xout, Rout, cfl, f);
+  else
+    launch_k(true, k_stage_f32<NS, true, MODE, RS>, grid(kBlock), kBlock, 0, st, m, s, Xin, Xbase, Xout, Rout, cfl, f);
+}
+
 template <int NS, bool FUSED>
 void launch_stage_ns(const DevMesh& m, const DevScalars& s, int mode, StateF32 Xin, StateF32 Xbase, StateF32 Xout,
                      double* Rout, int cfl, const StageFuse& f, cudaStream_t st) {
   const int nb = blocks_for(m.n);
-  if constexpr (FUSED) {   // the fused stages: the solver fixed per instance, the register budget by variant
+  if constexpr (FUSED) {   // the fused stages: the solver fixed per instance, the shape by variant
     const bool hll = m.riemann == kRiemannHll;
-    const bool v3 = NS <= 4 && m.stageVariant == 1;   // 3 blocks per SM (80 registers) instead of 4
+    const int v = NS <= 4 ? m.stageVariant : 0;
     if (mode == kModeStage1) {
-      auto k = hll ? (v3 ? k_stage_f32<NS, true, kModeStage1, kRiemannHll, 3> : k_stage_f32<NS, true, kModeStage1, kRiemannHll>)
-                   : (v3 ? k_stage_f32<NS, true, kModeStage1, kRiemannRoe, 3> : k_stage_f32<NS, true, kModeStage1, kRiemannRoe>);
-      launch_k(true, k, nb, kBlock, 0, st, m, s, Xin, Xbase, Xout, Rout, cfl, f);
+      if (hll) launch_gather_shape<NS, kModeStage1, kRiemannHll>(v, m, s, Xin, Xbase, Xout, Rout, cfl, f, st);
+      else launch_gather_shape<NS, kModeStage1, kRiemannRoe>(v, m, s, Xin, Xbase, Xout, Rout, cfl, f, st);
     } else if (mode == kModeStage2) {
-      auto k = hll ? (v3 ? k_stage_f32<NS, true, kModeStage2, kRiemannHll, 3> : k_stage_f32<NS, true, kModeStage2, kRiemannHll>)
-                   : (v3 ? k_stage_f32<NS, true, kModeStage2, kRiemannRoe, 3> : k_stage_f32<NS, true, kModeStage2, kRiemannRoe>);
-      launch_k(true, k, nb, kBlock, 0, st, m, s, Xin, Xbase, Xout, Rout, cfl, f);
+      if (hll) launch_gather_shape<NS, kModeStage2, kRiemannHll>(v, m, s, Xin, Xbase, Xout, Rout, cfl, f, st);
+      else launch_gather_shape<NS, kModeStage2, kRiemannRoe>(v, m, s, Xin, Xbase, Xout, Rout, cfl, f, st);
     }
   } else if (mode == kModeStage1) {
     launch_k(true, k_stage_f32<NS, false, kModeStage1>, nb, kBlock, 0, st, m, s, Xin, Xbase, Xout, Rout, cfl, f);
@@ -1177,7 +1217,7 @@ int stage_kernel_forced() { return forced_stage_kernel(); }
 int stage_variant_forced() {
   static const int v = [] {
     const char* e = std::getenv("HG_STAGE_VARIANT");
-    return (e && (e[0] == '0' || e[0] == '1') && e[1] == 0) ? e[0] - '0' : -1;
+    return (e && e[0] >= '0' && e[0] <= '3' && e[1] == 0) ? e[0] - '0' : -1;
   }();
   return v;
 }

@@ -181,10 +181,11 @@ constexpr int kMaxFusedInlets = 4;
 struct StageFuse {
   const double* totalIn = nullptr;   // conveyance totals of the input state (replaces DevMesh::totalA)
   double* totalOut = nullptr;        // totals of the output state
-  double* partials = nullptr;        // [kMaxFusedInlets][nSlots]
+  double* partials = nullptr;        // [kMaxFusedInlets][nSlots][kStageBlockF32 / 32] warp sums
   unsigned int* ticket = nullptr;
-  const int32_t* blockSlot = nullptr;   // [blocks] slot of a block holding inlet cells, else -1
+  const int32_t* blockSlot = nullptr;   // [tiles of kStageBlockF32 cells] slot of a tile holding inlet cells, else -1
   int32_t nSlots = 0;
+  int32_t nWarps = 0;                // the warps of those tiles that hold cells (arrivals before the last)
   int32_t record = 0;                // stage 1: block 0 records the step and clears the other CFL buffer
   int32_t cflMode = 0;
   int32_t parity = 0;
@@ -232,7 +233,7 @@ constexpr int32_t kFaceBoundary = INT32_MIN;
 constexpr int kFaceMaxPerTile = 1024;
 int stage_blocks_f32(const DevMesh& m);
 // The kernel HG_STAGE_KERNEL forces (gather / pipe / tma / face), else -1;
-// the shape HG_STAGE_VARIANT forces (0 / 1), else -1.
+// the shape HG_STAGE_VARIANT forces (0 to 3), else -1.
 int stage_kernel_forced();
 int stage_variant_forced();
 // Whether kernel k can run the fused stages of this mesh and these states.

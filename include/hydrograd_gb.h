@@ -395,14 +395,17 @@ int hg_final_vjp(hg_ctx* ctx, const double* Q0, int32_t nsteps, double dt, int32
 /* The autotuner of the FP32-compensated fused stages (no counterpart in the
  * reference, which has no GPU kernels).  It chooses among kernels and shapes
  * that compute bit-identical results, in one of two families:
- *   family 0: kernel 0 gather (one block per 256-cell tile) with the register
- *             budget of 4 or 3 resident blocks per SM (variant 0 / 1);
+ *   family 0: kernel 0 gather (one block per tile) in four shapes: 256-cell
+ *             tiles with the register budget of 4 or 3 resident blocks per
+ *             SM (variant 0 / 1), 512-cell tiles at 2 per SM (variant 2),
+ *             128-cell tiles at 8 per SM (variant 3);
  *             kernel 1 pipe (persistent, the next tile and its halo
  *             prefetched by asynchronous copies); kernel 2 tma (persistent,
  *             bulk-copy prefetch of the next tile);
  *   family 1: kernel 3 face (each wet-wet face evaluated once for both of its
- *             cells), variant 0 / 1 as above, where the mesh has the face
- *             tables (degree <= 4).  Family 0 is the default.
+ *             cells), variant 0 / 1 the 256-cell budgets above, where the
+ *             mesh has the face tables (degree <= 4).
+ *             Family 0 is the default.
  * The two families round differently (the face kernel forms each face's flux
  * once); a context's family is fixed (hg_set_stage_family, HG_STAGE_FAMILY=
  * gather|face), never chosen by timing.  Each usable candidate is timed on the
@@ -412,7 +415,7 @@ int hg_final_vjp(hg_ctx* ctx, const double* Q0, int32_t nsteps, double dt, int32
  * disables it) under a key of the GPU, the mesh's face tables, the Riemann
  * solver and the family.  The first RK2 steps of a context take the cached
  * choice, or tune once by themselves and store it.  HG_STAGE_KERNEL=
- * gather|pipe|tma|face and HG_STAGE_VARIANT=0|1 in the environment force a
+ * gather|pipe|tma|face and HG_STAGE_VARIANT=0..3 in the environment force a
  * candidate.  kernel (may be NULL) receives the kernel; reps = 0 only
  * reports it. */
 int hg_autotune(hg_ctx* ctx, int32_t reps, int32_t* kernel);

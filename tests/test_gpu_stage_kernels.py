@@ -4,9 +4,10 @@ shape computes the same results, and the choice is cached per mesh and GPU.
 Each candidate is forced in a child process (HG_STAGE_KERNEL, HG_STAGE_VARIANT,
 HG_STAGE_FAMILY, read once per process) and the states after graph-captured CFL
 steps and hg_integrate steps are compared bit for bit:
-  family 0 (gather): gather with the register budget of 4 and 3 blocks per SM,
-                     pipe, tma, and the autotuned default (the family of a new
-                     context);
+  family 0 (gather): gather in its four shapes (256-cell blocks with the
+                     register budget of 4 and 3 blocks per SM, 512-cell blocks,
+                     128-cell blocks), pipe, tma, and the autotuned default
+                     (the family of a new context);
   family 1 (face):   face with both budgets, and the family's autotuned choice.
 Unfused steps take a fixed kernel (pipe where it can run, so runs
 reproduce); their gather instance agrees within 1e-6.  hg_autotune leaves the
@@ -69,11 +70,14 @@ def test_gather_family_candidates_give_identical_states(tmp_path):
     runs = {
         "gather0": run_child("g0", {"HG_STAGE_KERNEL": "gather", "HG_STAGE_VARIANT": "0"}, tmp_path),
         "gather1": run_child("g1", {"HG_STAGE_KERNEL": "gather", "HG_STAGE_VARIANT": "1"}, tmp_path),
+        "gather512": run_child("g2", {"HG_STAGE_KERNEL": "gather", "HG_STAGE_VARIANT": "2"}, tmp_path),
+        "gather128": run_child("g3", {"HG_STAGE_KERNEL": "gather", "HG_STAGE_VARIANT": "3"}, tmp_path),
         "pipe": run_child("p", {"HG_STAGE_KERNEL": "pipe"}, tmp_path),
         "tma": run_child("t", {"HG_STAGE_KERNEL": "tma"}, tmp_path),
         "tuned": run_child("d", {}, tmp_path),
     }
     assert runs["pipe"]["kernel"] == 1 and runs["tma"]["kernel"] == 2 and runs["gather1"]["variant"] == 1
+    assert runs["gather512"]["variant"] == 2 and runs["gather128"]["variant"] == 3
     assert runs["tuned"]["kernel"] in (0, 1, 2) and runs["tuned"]["source"] == 1
     for k, r in runs.items():
         assert r["advance"] == runs["gather0"]["advance"], k
