@@ -62,8 +62,32 @@ __device__ __forceinline__ S activation_as(int a, S x) {
 }
 
 template <class S>
-__device__ __forceinline__ S normalise(S x, double lo, double hi) {
-  return S(2.0) * (x - S(lo)) / (S(hi) - S(lo)) - S(1.0);
+__device__ __forceinline__ S normalise(S x, S lo, S hi) {
+  return S(2.0) * (x - lo) / (hi - lo) - S(1.0);
+}
+
+// The network's input bounds and output bound in the kernel's precision,
+// converted once per thread (a double-to-float conversion runs on the FP64
+// pipe).
+template <class S>
+struct NetConsts {
+  S lo[kResMaxInputs], hi[kResMaxInputs];
+  S qlo, qhi;   // the flow-resistance closure's discharge bounds (h bounds x velocity-magnitude bounds)
+  S outLo, outHi;
+};
+template <class S>
+__device__ __forceinline__ NetConsts<S> net_consts(const ResDev& r) {
+  NetConsts<S> k;
+#pragma unroll
+  for (int i = 0; i < kResMaxInputs; ++i) {
+    k.lo[i] = S(r.lo[i]);
+    k.hi[i] = S(r.hi[i]);
+  }
+  k.qlo = S(r.lo[0] * r.lo[1]);
+  k.qhi = S(r.hi[0] * r.hi[1]);
+  k.outLo = S(r.outLo);
+  k.outHi = S(r.outHi);
+  return k;
 }
 
 // Clamped state of cell c (semi_discretize_swe_2D.jl:101-106).
@@ -93,18 +117,23 @@ __device__ __forceinline__ bool cell_dry(const DevMesh& m, StateF32 X, int c) {
 // (MW: the register arrays' length, a bound on the widths; the forward kernels
 // take the smallest of 4, 8, 16 that holds the network.)
 template <class S, int MW>
-__device__ __forceinline__ void ude_inputs(const ResDev& r, int c, S h, S qx, S qy, S (&a)[MW]) {
+__device__ __forceinline__ void ude_inputs(const ResDev& r, const NetConsts<S>& k, int c, S h, S qx, S qy,
+                                           S (&a)[MW]) {
   static_assert(MW >= kResMaxInputs, "the inputs need kResMaxInputs values");
 #pragma unroll
   for (int i = 0; i < MW; ++i) a[i] = S(0);
-  a[0] = normalise(h, r.lo[0], r.hi[0]);
+  a[0] = normalise(h, k.lo[0], k.hi[0]);
   if (r.kind == kResUdeManningHUmagKs) {
     const S u = qx / h, v = qy / h;
-    a[1] = normalise(RM<S>::sqrt(u * u + v * v), r.lo[1], r.hi[1]);
-    a[2] = normalise(S(r.ks[c]), r.lo[2], r.hi[2]);
-  } else if (r.kind == kResUdeFlowResistance) {   // q bounds = h bounds x velocity-magnitude bounds
-    a[1] = normalise(smooth_sqrt(qx * qx + qy * qy), r.lo[0] * r.lo[1], r.hi[0] * r.hi[1]);
+    a[1] = normalise(RM<S>::sqrt(u * u + v * v), k.lo[1], k.hi[1]);
+    a[2] = normalise(S(r.ks[c]), k.lo[2], k.hi[2]);
+  } else if (r.kind == kResUdeFlowResistance) {
+    a[1] = normalise(smooth_sqrt(qx * qx + qy * qy), k.qlo, k.qhi);
   }
+}
+template <class S, int MW>
+__device__ __forceinline__ void ude_inputs(const ResDev& r, int c, S h, S qx, S qy, S (&a)[MW]) {
+  ude_inputs(r, net_consts<S>(r), c, h, qx, qy, a);
 }
 
 // z = act(W a + b) of one Dense layer (weights at offset off, out x din column-major).
@@ -301,6 +330,7 @@ __global__ void __launch_bounds__(kBlock) k_res_layer(DevMesh m, State Q, int l)
   stage_params(r, off, din, w, l > 0 ? off - 2 * din : -1, P);
   S mu = S(0), den = S(1);
   if (l > 0) batch_stats(r, l - 1, mu, den);
+  const NetConsts<S> nk = net_consts<S>(r);
   const int n = m.n, stride = gridDim.x * blockDim.x;
   S* __restrict__ hid = RM<S>::hid(r) + (size_t)hidden_row(r, l) * n;
   S sum = S(0);
@@ -310,7 +340,7 @@ __global__ void __launch_bounds__(kBlock) k_res_layer(DevMesh m, State Q, int l)
     if (l == 0) {
       S h, qx, qy;
       cell_state(m, Q, c, h, qx, qy);
-      ude_inputs(r, c, h, qx, qy, a);
+      ude_inputs(r, nk, c, h, qx, qy, a);
     } else {
       S zp[MW];
       load_hidden(r, l - 1, n, c, zp);
@@ -387,6 +417,7 @@ __global__ void __launch_bounds__(kBlock) k_res_cells(DevMesh m, State Q) {
   __shared__ LayerParams<S, MW> P;   // the output layer and the last hidden layer's LayerNorm
   int din = 0;
   S mu = S(0), den = S(1);
+  const NetConsts<S> nk = net_consts<S>(r);
   if constexpr (cached) {
     const int offOut = layer_offset(r, r.nHidden, din);
     stage_params(r, offOut, din, 1, offOut - 2 * din, P);
@@ -407,11 +438,11 @@ __global__ void __launch_bounds__(kBlock) k_res_cells(DevMesh m, State Q) {
 #pragma unroll
       for (int i = 0; i < MW; ++i)
         if (i < din) t += P.W[i][0] * a[i];
-      out = S(r.outLo) + (S(r.outHi) - S(r.outLo)) * sigmoid_nn(t + P.b[0]);
+      out = nk.outLo + (nk.outHi - nk.outLo) * sigmoid_nn(t + P.b[0]);
     } else {
       S a[MW], z[MW];
       int dl;
-      ude_inputs(r, c, h, qx, qy, a);
+      ude_inputs(r, nk, c, h, qx, qy, a);
       const int off = mlp_run(r, r.nHidden, a, z, dl);
       out = mlp_output(r, off, dl, a);
     }
