@@ -55,7 +55,10 @@ def load_peaks():
 
 
 # The FP32C stage kernels hg_autotune chooses among: (name, ncu summary under profiles/)
-STAGE_KERNELS = {0: ("k_stage_f32 (one block per 256-cell tile)", "k_stage_f32_river_tri_1M.md"),
+# and the gather kernel's shapes (variant: cells per block, register budget as resident blocks per SM).
+GATHER_SHAPES = {0: "256-cell tiles, 4 blocks per SM", 1: "256-cell tiles, 3 blocks per SM",
+                 2: "512-cell tiles, 2 blocks per SM", 3: "128-cell tiles, 8 blocks per SM"}
+STAGE_KERNELS = {0: ("k_stage_f32 (one block per tile)", "k_stage_f32_river_tri_1M.md"),
                  1: ("k_stage_pipe_f32 (persistent; the next tile and its halo prefetched by cp.async)",
                      "k_stage_pipe_f32_river_tri_1M.md"),
                  2: ("k_stage_tma_f32 (persistent; the next tile prefetched by bulk copies)", None),
@@ -652,6 +655,7 @@ def run_ours(args):
         out[prec]["stage_ms"] = ctx.time_stage_kernel(20, True)
         if prec == "fp32c":
             out[prec]["stage_kernel"] = ctx.autotune(0)   # the kernel the autotuner chose
+            out[prec]["stage_variant"] = ctx.autotune_info()[1]
     # FP32C error vs the FP64 path over the whole run (same CFL rule; the FP64
     # path itself is checked against the oracle below and by the GPU tests).
     a, b = out["fp32c"]["state"], out["fp64"]["state"]
@@ -739,9 +743,12 @@ def run_ours(args):
     bytes_stage = (cell_b + nfaces_cell * face_b) * N
     achieved = bytes_stage / (out["fp32c"]["stage_ms"] * 1e-3) / 1e9
     kern = out["fp32c"]["stage_kernel"]
+    kname = STAGE_KERNELS[kern][0]
+    if kern == 0:
+        kname = kname[:-1] + "; " + GATHER_SHAPES.get(out["fp32c"].get("stage_variant", 0), "") + ")"
     tr = profile_traffic("fp32c", kern)
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": None if tr is None else tr * N, "kernel": STAGE_KERNELS[kern][0] + ", one RK2 stage pass",
+            "traffic": None if tr is None else tr * N, "kernel": kname + ", one RK2 stage pass",
             "algorithmic_bytes_per_launch": bytes_stage, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)"}
     if adj and "vjp_ms" in adj:
         bytes_vjp = (BYTES_VJP_FP32C[0] + nfaces_cell * BYTES_VJP_FP32C[1]) * N
