@@ -280,6 +280,9 @@ __device__ __forceinline__ void stage_finish(const DevMesh& m, const DevScalars&
   const float2 d12 = add2(r12, src);
   if constexpr (MODE == kModeRhs) {
     Rout[c] = d0; Rout[m.n + c] = d12.x; Rout[2 * m.n + c] = d12.y;
+  } else if constexpr (MODE == kModeRhsF32) {
+    float* R = reinterpret_cast<float*>(Rout);
+    R[c] = d0; R[m.n + c] = d12.x; R[2 * m.n + c] = d12.y;
   } else {
     const float2 qin = qinP[k];
     const float inc0 = dt * d0;
@@ -380,7 +383,8 @@ __global__ void __launch_bounds__(TB, MINB > 0 ? MINB : stage_min_blocks<NS>())
   __syncthreads();
   const int mem = (!FUSED && s.nMembers > 0 && active) ? member_of(s, c) : -1;   // an ensemble member's own step
   if (active) {
-    const float dt = MODE == kModeRhs ? 0.0f : (FUSED ? dtShared : (mem >= 0 ? s.dtMf[mem] : *s.dtf));
+    const float dt = (MODE == kModeRhs || MODE == kModeRhsF32) ? 0.0f
+                                                               : (FUSED ? dtShared : (mem >= 0 ? s.dtMf[mem] : *s.dtf));
     stage_cell<NS, MODE, false, RS, TB>(m, s, Xin.x, sX, sP, nullptr, nullptr, base, c, sl, xin, cp, cs, Xin.q, Xbase.x,
                                      Xbase.q, c,
                          dt, FUSED ? f.totalIn : m.totalA, Xout, Rout, cfl, cand, hOut, wetOut);
@@ -1081,6 +1085,8 @@ void launch_stage_ns(const DevMesh& m, const DevScalars& s, int mode, StateF32 X
   } else {
     if (mode == kModeRhs)
       launch_k(true, k_stage_f32<NS, false, kModeRhs>, nb, kBlock, 0, st, m, s, Xin, Xbase, Xout, Rout, cfl, f);
+    else if (mode == kModeRhsF32)
+      launch_k(true, k_stage_f32<NS, false, kModeRhsF32>, nb, kBlock, 0, st, m, s, Xin, Xbase, Xout, Rout, cfl, f);
     else
       launch_k(true, k_stage_f32<NS, false, kModeEulerRef>, nb, kBlock, 0, st, m, s, Xin, Xbase, Xout, Rout, cfl, f);
   }

@@ -165,7 +165,9 @@ struct DevScalars {
   double* dtHistM = nullptr;              // [dtCap][nMembers] steps taken
 };
 
-enum StageMode : int32_t { kModeRhs = 0, kModeStage1 = 1, kModeStage2 = 2, kModeEulerRef = 3 };
+// kModeRhsF32: the RHS as float (the FP32 stage kernel only; Rout then points
+// at [3n] floats).
+enum StageMode : int32_t { kModeRhs = 0, kModeStage1 = 1, kModeStage2 = 2, kModeEulerRef = 3, kModeRhsF32 = 4 };
 
 // Fused FP32 stepping: one RK2 step is two launches.
 //  * dt: in CFL mode thread 0 of every block forms dt = cfl * min from the

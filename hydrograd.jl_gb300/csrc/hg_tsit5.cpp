@@ -3,9 +3,10 @@
 // Hairer, Norsett & Wanner, "Solving ODEs I", II.4 (embedded error estimate in
 // a weighted RMS norm, PI controller, Hairer's initial step).
 //
-// The state lives on the device as one FP64 vector U = [xi | qx | qy] in the
-// device cell order; each stage's RHS is the context's RHS kernel (FP64, or
-// the FP32-compensated kernel on the stage state split into hi + lo pairs).
+// The state lives on the device in the device cell order: one FP64 vector
+// U = [xi | qx | qy] in an FP64 context, hi + lo records in an
+// FP32-compensated one (VecsF64 / VecsF32 below); each stage's RHS is the
+// context's RHS kernel.
 // As in the reference's ODE solve, the RHS clamps depths internally and the
 // integrator adds no clamp of its own.  One 8-byte read-back per step (the
 // error norm) drives the controller.
@@ -80,6 +81,96 @@ struct Tsit5Buffers {
   }
 };
 
+// The integrator's vectors and kernels by precision.  FP64 contexts: plain
+// [3n] FP64 vectors, the FP64 RHS, combinations and norm in FP64 (the
+// oracle's arithmetic).  FP32-compensated contexts: stage states as hi + lo
+// records, RHS vectors in FP32 (the FP32 stage kernel's own precision), the
+// weighted sums in FP32 added to the states with compensated sums, the norm's
+// terms in FP32 -- GB300 issues FP64 at a small fraction of the FP32 rate, and
+// the FP64 combinations were most of an FP32-compensated step.
+struct VecsF64 {
+  using State = double*;
+  using Deriv = double*;
+  hg_ctx* c;
+  double abstol, reltol;
+  double *partials, *norm2;
+  unsigned int* ticket;
+  int64_t len() const { return (int64_t)3 * c->n; }
+  cudaError_t alloc(Tsit5Buffers& B, State& v) { return B.alloc(&v, len()); }
+  cudaError_t allocD(Tsit5Buffers& B, Deriv& v) { return B.alloc(&v, len()); }
+  void load(State U) { launch_gather_state_f64(c->n, c->d_perm, c->Quser, U, c->stream); }
+  void unload(State U) { launch_scatter_state_f64(c->n, c->d_perm, U, c->Quser, c->stream); }
+  void rhs(State X, Deriv out) {
+    launch_inlet_total_f64(c->dm, c->ds, X, c->stream);
+    launch_stage_f64(c->dm, c->ds, kModeRhs, X, nullptr, out, false, c->stream);
+  }
+  static Tsit5Terms terms(const Deriv* K, const double* w, int nk) {
+    Tsit5Terms t{};
+    for (int j = 0; j < nk; ++j) {
+      t.K[j] = K[j];
+      t.w[j] = w[j];
+    }
+    t.nk = nk;
+    return t;
+  }
+  void combine(State U, const Deriv* K, const double* w, int nk, double h, State Y) {
+    launch_tsit5_combine(len(), U, terms(K, w, nk), h, Y, c->stream);
+  }
+  void error(State Ua, State Ub, const Deriv* K, const double* w, int nk, double h) {
+    launch_tsit5_error(len(), Ua, Ub, terms(K, w, nk), h, abstol, reltol, partials, ticket, norm2, c->stream);
+  }
+  void state_norm(State U) {   // the state itself as the vector
+    const double one = 1.0;
+    launch_tsit5_error(len(), U, U, terms(&U, &one, 1), 1.0, abstol, reltol, partials, ticket, norm2, c->stream);
+  }
+};
+
+struct VecsF32 {
+  using State = StateF32;
+  using Deriv = float*;
+  hg_ctx* c;
+  double abstol, reltol;
+  double *partials, *norm2;
+  unsigned int* ticket;
+  int64_t len() const { return (int64_t)3 * c->n; }
+  cudaError_t alloc(Tsit5Buffers& B, State& v) {
+    cudaError_t e = B.alloc(&v.x, (size_t)c->n);
+    return e == cudaSuccess ? B.alloc(&v.q, (size_t)c->n) : e;
+  }
+  cudaError_t allocD(Tsit5Buffers& B, Deriv& v) { return B.alloc(&v, len()); }
+  void load(State U) { launch_gather_state_f32(c->n, c->d_perm, c->Quser, U, c->stream); }
+  void unload(State U) { launch_scatter_state_f32(c->n, c->d_perm, U, c->Quser, c->stream); }
+  void rhs(State X, Deriv out) {
+    launch_inlet_total_f32(c->dm, c->ds, X, c->stream);
+    launch_stage_f32(c->dm, c->ds, kModeRhsF32, X, StateF32{}, StateF32{}, reinterpret_cast<double*>(out), false,
+                     c->stream);
+  }
+  static Tsit5TermsF terms(const Deriv* K, const double* w, int nk, double h) {
+    Tsit5TermsF t{};
+    for (int j = 0; j < nk; ++j) {
+      t.K[j] = K[j];
+      t.w[j] = (float)(w[j] * h);
+    }
+    t.nk = nk;
+    return t;
+  }
+  void combine(State U, const Deriv* K, const double* w, int nk, double h, State Y) {
+    launch_tsit5_combine_f32(c->n, U, terms(K, w, nk, h), Y, c->stream);
+  }
+  void error(State Ua, State Ub, const Deriv* K, const double* w, int nk, double h) {
+    launch_tsit5_error_f32(c->n, Ua, Ub, terms(K, w, nk, h), (float)abstol, (float)reltol, partials, ticket, norm2,
+                           c->stream);
+  }
+  void state_norm(State U) {
+    launch_tsit5_error_f32(c->n, U, U, Tsit5TermsF{}, (float)abstol, (float)reltol, partials, ticket, norm2,
+                           c->stream);
+  }
+};
+
+template <class V>
+int run_tsit5(hg_ctx* ctx, V& vec, double* Q, double t0, double t1, double dt0, int32_t adaptive, int32_t max_steps,
+              int32_t n_save, const double* t_save, double* saves, int32_t* stats);
+
 }  // namespace
 }  // namespace hg
 
@@ -109,74 +200,76 @@ int hg_integrate_tsit5(hg_ctx* ctx, double* Q, double t0, double t1, double abst
       return fail(ctx, HG_ERR_ARG, "hg_integrate_tsit5: save times must ascend within (t0, t1]");
   if (max_steps <= 0) max_steps = 10000000;
   cudaSetDevice(ctx->device);
+  if (ctx->precision == HG_FP64) {
+    VecsF64 v{ctx, abstol, reltol, nullptr, nullptr, nullptr};
+    return run_tsit5(ctx, v, Q, t0, t1, dt0, adaptive, max_steps, n_save, t_save, saves, stats);
+  }
+  VecsF32 v{ctx, abstol, reltol, nullptr, nullptr, nullptr};
+  return run_tsit5(ctx, v, Q, t0, t1, dt0, adaptive, max_steps, n_save, t_save, saves, stats);
+}
+
+namespace hg {
+namespace {
+
+template <class V>
+int run_tsit5(hg_ctx* ctx, V& vec, double* Q, double t0, double t1, double dt0, int32_t adaptive, int32_t max_steps,
+              int32_t n_save, const double* t_save, double* saves, int32_t* stats) {
+  using State = typename V::State;
+  using Deriv = typename V::Deriv;
   const Tsit5Tableau& tb = tsit5_tableau();
   const int n = ctx->n;
   const int64_t len = (int64_t)3 * n;
   cudaStream_t st = ctx->stream;
   Tsit5Buffers B;
-  double *U, *Unew, *Y, *K[kTsit5Stages], *partials, *norm2;
-  unsigned int* ticket;
-  TS_CUDA(ctx, B.alloc(&U, len));
-  TS_CUDA(ctx, B.alloc(&Unew, len));
-  TS_CUDA(ctx, B.alloc(&Y, len));
-  for (auto& k : K) TS_CUDA(ctx, B.alloc(&k, len));
-  TS_CUDA(ctx, B.alloc(&partials, kTsit5ErrorBlocks));
-  TS_CUDA(ctx, B.alloc(&norm2, 1));
-  TS_CUDA(ctx, B.alloc(&ticket, 1));
-  TS_CUDA(ctx, cudaMemsetAsync(ticket, 0, sizeof(unsigned int), st));
+  State U{}, Unew{}, Y{};
+  Deriv K[kTsit5Stages];
+  TS_CUDA(ctx, vec.alloc(B, U));
+  TS_CUDA(ctx, vec.alloc(B, Unew));
+  TS_CUDA(ctx, vec.alloc(B, Y));
+  for (auto& k : K) TS_CUDA(ctx, vec.allocD(B, k));
+  TS_CUDA(ctx, B.alloc(&vec.partials, kTsit5ErrorBlocks));
+  TS_CUDA(ctx, B.alloc(&vec.norm2, 1));
+  TS_CUDA(ctx, B.alloc(&vec.ticket, 1));
+  TS_CUDA(ctx, cudaMemsetAsync(vec.ticket, 0, sizeof(unsigned int), st));
   TS_CUDA(ctx, cudaMemsetAsync(ctx->ds.flags, 0, sizeof(int32_t), st));
   // State in: caller order -> device order.
   TS_CUDA(ctx, cudaMemcpyAsync(ctx->Quser, Q, len * sizeof(double), cudaMemcpyHostToDevice, st));
-  launch_gather_state_f64(n, ctx->d_perm, ctx->Quser, U, st);
+  vec.load(U);
   ctx->launches += 1;
-  const StateF32 xs{ctx->XB, ctx->XQB};
-  auto rhs = [&](const double* X, double* out, double tx) {
+  auto rhs = [&](State X, Deriv out, double tx) {
     ctx->launches += launch_hydrograph(ctx->dm, ctx->ds, kHydroAt, tx, st);   // inlet discharges at tx
-    if (ctx->precision == HG_FP64) {
-      launch_inlet_total_f64(ctx->dm, ctx->ds, X, st);
-      launch_stage_f64(ctx->dm, ctx->ds, kModeRhs, X, nullptr, out, false, st);
-    } else {
-      launch_f64_to_f32(n, X, xs, st);
-      launch_inlet_total_f32(ctx->dm, ctx->ds, xs, st);
-      launch_stage_f32(ctx->dm, ctx->ds, kModeRhs, xs, StateF32{}, StateF32{}, out, false, st);
-      ctx->launches += 1;
-    }
+    vec.rhs(X, out);
     ctx->launches += 1 + (ctx->dm.nInlet > 0 ? 1 : 0) + resistance_launches(ctx->dm);
   };
-  // Weighted RMS norm of sum_j w_j V_j (scale abstol + reltol max(|Ua|, |Ub|)).
-  auto wnorm = [&](const double* Ua, const double* Ub, Tsit5Terms terms, double h, double& out) -> int {
-    launch_tsit5_error(len, Ua, Ub, terms, h, abstol, reltol, partials, ticket, norm2, st);
+  // Weighted RMS norm (scale abstol + reltol max(|Ua|, |Ub|)) of the vector
+  // the last error launch formed.
+  auto read_norm = [&](double& out) -> int {
     ctx->launches += 1;
     double v = 0.0;
-    TS_CUDA(ctx, cudaMemcpyAsync(&v, norm2, sizeof(double), cudaMemcpyDeviceToHost, st));
+    TS_CUDA(ctx, cudaMemcpyAsync(&v, vec.norm2, sizeof(double), cudaMemcpyDeviceToHost, st));
     TS_CUDA(ctx, cudaStreamSynchronize(st));
     out = std::sqrt(v / (double)len);
     return HG_OK;
   };
-  auto one = [](const double* v, double w) {
-    Tsit5Terms t{};
-    t.K[0] = v;
-    t.w[0] = w;
-    t.nk = 1;
-    return t;
-  };
+  const double unit = 1.0;
   rhs(U, K[0], t0);
   double dt = dt0;
   if (adaptive && !(dt > 0)) {   // Hairer, Norsett & Wanner II.4: starting step size
     double d0, d1, d2;
-    int rc = wnorm(U, U, one(U, 1.0), 1.0, d0);
-    if (!rc) rc = wnorm(U, U, one(K[0], 1.0), 1.0, d1);
+    vec.state_norm(U);
+    int rc = read_norm(d0);
+    if (!rc) {
+      vec.error(U, U, K, &unit, 1, 1.0);
+      rc = read_norm(d1);
+    }
     if (rc) return rc;
     const double h0 = (d0 < 1e-5 || d1 < 1e-5) ? 1e-6 : 0.01 * d0 / d1;
-    launch_tsit5_combine(len, U, one(K[0], 1.0), h0, Y, st);
+    vec.combine(U, K, &unit, 1, h0, Y);
     rhs(Y, K[1], t0 + h0);
-    Tsit5Terms dk{};
-    dk.K[0] = K[1];
-    dk.K[1] = K[0];
-    dk.w[0] = 1.0 / h0;
-    dk.w[1] = -1.0 / h0;
-    dk.nk = 2;
-    rc = wnorm(U, U, dk, 1.0, d2);
+    const Deriv dk[2] = {K[1], K[0]};
+    const double wk[2] = {1.0 / h0, -1.0 / h0};
+    vec.error(U, U, dk, wk, 2, 1.0);
+    rc = read_norm(d2);
     if (rc) return rc;
     const double m = std::max(d1, d2);
     const double h1 = m <= 1e-15 ? std::max(1e-6, h0 * 1e-3) : std::pow(0.01 / m, 1.0 / 5.0);
@@ -199,27 +292,16 @@ int hg_integrate_tsit5(hg_ctx* ctx, double* Q, double t0, double t1, double abst
       hit = true;
     }
     for (int i = 1; i < kTsit5Stages; ++i) {   // stages 2..7; stage 7's state is the new state
-      Tsit5Terms terms{};
-      for (int j = 0; j < i; ++j) {
-        terms.K[j] = K[j];
-        terms.w[j] = tb.a[i][j];
-      }
-      terms.nk = i;
-      double* dst = (i == kTsit5Stages - 1) ? Unew : Y;
-      launch_tsit5_combine(len, U, terms, h, dst, st);
+      State dst = (i == kTsit5Stages - 1) ? Unew : Y;
+      vec.combine(U, K, tb.a[i], i, h, dst);
       rhs(dst, K[i], t + tb.c[i] * h);
       ctx->launches += 1;
     }
     evals += kTsit5Stages - 1;
     double eest = 0.0;
     if (adaptive) {
-      Tsit5Terms et{};
-      for (int j = 0; j < kTsit5Stages; ++j) {
-        et.K[j] = K[j];
-        et.w[j] = tb.btilde[j];
-      }
-      et.nk = kTsit5Stages;
-      int rc = wnorm(U, Unew, et, h, eest);
+      vec.error(U, Unew, K, tb.btilde, kTsit5Stages, h);
+      int rc = read_norm(eest);
       if (rc) return rc;
     }
     if (eest <= 1.0) {
@@ -234,7 +316,7 @@ int hg_integrate_tsit5(hg_ctx* ctx, double* Q, double t0, double t1, double abst
         dt = h * fac;
       }
       if (hit && saved < n_save) {
-        launch_scatter_state_f64(n, ctx->d_perm, U, ctx->Quser, st);
+        vec.unload(U);
         ctx->launches += 1;
         TS_CUDA(ctx, cudaMemcpyAsync(saves + (size_t)saved * len, ctx->Quser, len * sizeof(double),
                                      cudaMemcpyDeviceToHost, st));
@@ -248,7 +330,7 @@ int hg_integrate_tsit5(hg_ctx* ctx, double* Q, double t0, double t1, double abst
         return fail(ctx, HG_ERR_STATE, "hg_integrate_tsit5: step size underflow");
     }
   }
-  launch_scatter_state_f64(n, ctx->d_perm, U, ctx->Quser, st);
+  vec.unload(U);
   ctx->launches += 1;
   TS_CUDA(ctx, cudaMemcpyAsync(Q, ctx->Quser, len * sizeof(double), cudaMemcpyDeviceToHost, st));
   int32_t flags = 0;
@@ -263,3 +345,6 @@ int hg_integrate_tsit5(hg_ctx* ctx, double* Q, double t0, double t1, double abst
   if (flags & 1) return fail(ctx, HG_ERR_STATE, "non-finite value in the state");
   return HG_OK;
 }
+
+}  // namespace
+}  // namespace hg

@@ -4,6 +4,7 @@
 // cell order.
 #include <cmath>
 
+#include "hg_f32.cuh"
 #include "hg_reduce.cuh"
 #include "hg_state.hpp"
 #include "hg_tsit5.hpp"
@@ -11,6 +12,7 @@
 namespace hg {
 
 using namespace devred;
+using hgd::df_add;
 
 namespace {
 
@@ -47,6 +49,82 @@ __global__ void __launch_bounds__(kBlock) k_tsit5_error(int64_t len, const doubl
     acc += r * r;
   }
   const double b = block_sum(acc);
+  __shared__ int isLast;
+  if (threadIdx.x == 0) {
+    partials[blockIdx.x] = b;
+    __threadfence();
+    isLast = (atomicAdd(ticket, 1u) == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!isLast) return;
+  __threadfence();
+  double s = 0.0;
+  for (int k = threadIdx.x; k < (int)gridDim.x; k += blockDim.x) s += __ldcg(&partials[k]);
+  const double tot = block_sum(s);
+  if (threadIdx.x == 0) {
+    *norm2 = tot;
+    *ticket = 0u;
+  }
+}
+
+// FP32-compensated stage state: Y = U + sum_j w_j K_j per cell, the sums in
+// FP32 in stage order, added to the hi + lo pairs exactly (df_add).
+__global__ void __launch_bounds__(kBlock) k_tsit5_combine_f32(int32_t n, StateF32 U, Tsit5TermsF t, StateF32 Y) {
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
+    float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f;
+#pragma unroll
+    for (int j = 0; j < kTsit5Stages; ++j)
+      if (j < t.nk) {
+        const float w = t.w[j];
+        const float* __restrict__ K = t.K[j];
+        s0 = fmaf(w, __ldg(&K[c]), s0);
+        s1 = fmaf(w, __ldg(&K[n + c]), s1);
+        s2 = fmaf(w, __ldg(&K[2 * n + c]), s2);
+      }
+    const float4 u = U.x[c];
+    const float2 q = U.q[c];
+    float xh, xl, uh, ul, vh, vl;
+    df_add(u.x, u.y, s0, xh, xl);
+    df_add(u.z, q.x, s1, uh, ul);
+    df_add(u.w, q.y, s2, vh, vl);
+    Y.x[c] = make_float4(xh, xl, uh, vh);
+    Y.q[c] = make_float2(ul, vl);
+  }
+}
+
+// The weighted RMS terms of an FP32-compensated run, in FP32 per value and
+// per thread, the block sums carried exactly to double (block_sum_f32); the
+// last block adds the partials in block order.
+__global__ void __launch_bounds__(kBlock) k_tsit5_error_f32(int32_t n, StateF32 U, StateF32 Unew, Tsit5TermsF t,
+                                                            float abstol, float reltol, double* partials,
+                                                            unsigned int* ticket, double* norm2) {
+  float acc = 0.0f;
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
+    const float4 u = U.x[c], un = Unew.x[c];
+    const float2 q = U.q[c];
+    float e[3] = {0.0f, 0.0f, 0.0f};
+    if (t.nk == 0) {   // the state itself
+      e[0] = u.x + u.y;
+      e[1] = u.z + q.x;
+      e[2] = u.w + q.y;
+    }
+#pragma unroll
+    for (int j = 0; j < kTsit5Stages; ++j)
+      if (j < t.nk) {
+        const float w = t.w[j];
+        const float* __restrict__ K = t.K[j];
+        e[0] = fmaf(w, __ldg(&K[c]), e[0]);
+        e[1] = fmaf(w, __ldg(&K[n + c]), e[1]);
+        e[2] = fmaf(w, __ldg(&K[2 * n + c]), e[2]);
+      }
+    const float a[3] = {u.x, u.z, u.w}, b[3] = {un.x, un.z, un.w};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const float r = e[k] / (abstol + reltol * fmaxf(fabsf(a[k]), fabsf(b[k])));
+      acc = fmaf(r, r, acc);
+    }
+  }
+  const double b = block_sum_f32(acc);
   __shared__ int isLast;
   if (threadIdx.x == 0) {
     partials[blockIdx.x] = b;
@@ -103,6 +181,15 @@ void launch_tsit5_combine(int64_t len, const double* U, const Tsit5Terms& t, dou
 void launch_tsit5_error(int64_t len, const double* U, const double* Unew, const Tsit5Terms& t, double dt, double abstol,
                         double reltol, double* partials, unsigned int* ticket, double* norm2, cudaStream_t st) {
   k_tsit5_error<<<grid_for(len), kBlock, 0, st>>>(len, U, Unew, t, dt, abstol, reltol, partials, ticket, norm2);
+}
+
+void launch_tsit5_combine_f32(int32_t n, StateF32 U, const Tsit5TermsF& t, StateF32 Y, cudaStream_t st) {
+  k_tsit5_combine_f32<<<grid_for(n), kBlock, 0, st>>>(n, U, t, Y);
+}
+
+void launch_tsit5_error_f32(int32_t n, StateF32 U, StateF32 Unew, const Tsit5TermsF& t, float abstol, float reltol,
+                            double* partials, unsigned int* ticket, double* norm2, cudaStream_t st) {
+  k_tsit5_error_f32<<<grid_for(n), kBlock, 0, st>>>(n, U, Unew, t, abstol, reltol, partials, ticket, norm2);
 }
 
 void launch_f32_to_f64(int32_t n, StateF32 X, double* Q, cudaStream_t st) {

@@ -38,6 +38,21 @@ void launch_tsit5_combine(int64_t len, const double* U, const Tsit5Terms& t, dou
 // *norm2 = sum_i (dt sum_j w_j K_j[i] / (abstol + reltol max(|U_i|, |Unew_i|)))^2 (partials: kTsit5ErrorBlocks).
 void launch_tsit5_error(int64_t len, const double* U, const double* Unew, const Tsit5Terms& t, double dt, double abstol,
                         double reltol, double* partials, unsigned int* ticket, double* norm2, cudaStream_t st);
+// FP32-compensated contexts: the stage states are hi + lo records (StateF32),
+// the stage RHS vectors [3n] floats, and the weights carry the step (w_j dt,
+// rounded to float once).  The sums run in FP32 -- the RHS vectors hold
+// FP32-accurate values -- and are added to the state with a compensated sum.
+struct Tsit5TermsF {
+  const float* K[kTsit5Stages];
+  float w[kTsit5Stages];
+  int nk;
+};
+// Y = U + sum_j w[j] K[j].
+void launch_tsit5_combine_f32(int32_t n, StateF32 U, const Tsit5TermsF& t, StateF32 Y, cudaStream_t st);
+// *norm2 = sum over the 3n values of (sum_j w_j K_j / (abstol + reltol max(|U|, |Unew|)))^2;
+// with nk = 0 the values are U's own (the initial step's norm of the state).
+void launch_tsit5_error_f32(int32_t n, StateF32 U, StateF32 Unew, const Tsit5TermsF& t, float abstol, float reltol,
+                            double* partials, unsigned int* ticket, double* norm2, cudaStream_t st);
 void launch_f32_to_f64(int32_t n, StateF32 X, double* Q, cudaStream_t st);
 void launch_f64_to_f32(int32_t n, const double* Q, StateF32 X, cudaStream_t st);
 
