@@ -59,15 +59,21 @@ __device__ __forceinline__ Side<D> constant(const Side<float>& s) {
 
 // acc += b * g with the product exact (fma residual) and the sum compensated:
 // FP32 instructions only, about 2^-44 relative over thousands of terms.
-__device__ __forceinline__ void acc_add(float2* p, float b, float g) {
+__device__ __forceinline__ void acc_add_from(float2* p, float2 a, float b, float g) {
   const float prod = b * g;
   const float perr = fmaf(b, g, -prod);
-  float2 a = *p;
   float s, e;
   two_sum(a.x, prod, s, e);
   e += a.y + perr;
   fast_two_sum(s, e, a.x, a.y);
   *p = a;
+}
+__device__ __forceinline__ void acc_add(float2* p, float b, float g) { acc_add_from(p, *p, b, g); }
+
+// The accumulators a VJP cell updates from its own values (q: 0 n, 1 S0x,
+// 2 S0y), prefetched with the tile where the kernel is pipelined.
+__device__ __forceinline__ bool acc_prefetched(const AdjDev& a, int q) {
+  return q == 0 ? (a.wantN && !a.resChain && !a.udeChain) : a.wantZb != 0;
 }
 
 // Interior faces (3-direction duals: d/d own xi, hu, hv) and the source
@@ -103,6 +109,7 @@ struct GlobalSrc {
                   mu[2 * (size_t)m.n + nb]};
   }
   __device__ int cell(int nb) const { return nb; }   // the neighbour's cell id
+  __device__ float2 acc(int, const float2* p) const { return *p; }
 };
 
 // The VJP of one stage at cell j (interior faces: 3-direction duals of the
@@ -185,8 +192,8 @@ __device__ __forceinline__ void vjp_cell(const DevMesh& m, const AdjDev& a, int 
     g1 += mj1 * (-k - hu * dkdqx) + mj2 * (-hv * dkdqx);
     g2 += mj1 * (-hu * dkdqy) + mj2 * (-k - hv * dkdqy);
     if (a.wantZb) {
-      acc_add(&a.accF[(size_t)n + j], beta, mj1 * m.gf * L.s.xi);
-      acc_add(&a.accF[(size_t)2 * n + j], beta, mj2 * m.gf * L.s.xi);
+      acc_add_from(&a.accF[(size_t)n + j], src.acc(1, &a.accF[(size_t)n + j]), beta, mj1 * m.gf * L.s.xi);
+      acc_add_from(&a.accF[(size_t)2 * n + j], src.acc(2, &a.accF[(size_t)2 * n + j]), beta, mj2 * m.gf * L.s.xi);
     }
   }
   if constexpr (FOLD) {   // a dry cell's boundary faces (the face loop above runs for wet cells)
@@ -240,7 +247,7 @@ __device__ __forceinline__ void vjp_cell(const DevMesh& m, const AdjDev& a, int 
   } else if (a.udeChain) {   // the network's VJP takes it on (dL/dn, or dL/dF of the closure)
     a.udeGn[j] = (double)(beta * gn);
   } else if (a.wantN && gn != 0.0f) {
-    acc_add(&a.accF[j], beta, gn);
+    acc_add_from(&a.accF[j], src.acc(0, &a.accF[j]), beta, gn);
   }
   const float mask = L.s.dry ? 0.0f : 1.0f;
   const float e0 = src.extra_own(0), e1 = src.extra_own(1), e2 = src.extra_own(2);
@@ -279,7 +286,8 @@ struct VjpTile {
   static constexpr uint32_t kSL = 0, kX = NS * kRec, kCP = kX + kRec, kCS = kCP + kRec;
   static constexpr uint32_t kMU = kCS + kRec, kEX = kMU + 3 * kF;
   static constexpr uint32_t kHX = kEX + 3 * kF, kHP = kHX + kH16, kHA = kHP + kH16, kHM = kHA + kH4;
-  static constexpr uint32_t kBuf = (kHM + 3 * kH4 + 127u) & ~127u;
+  static constexpr uint32_t kACC = (kHM + 3 * kH4 + 15u) & ~15u;   // the own cells' accumulators (acc_prefetched)
+  static constexpr uint32_t kBuf = (kACC + 3 * kVTile * (uint32_t)sizeof(float2) + 127u) & ~127u;
   static constexpr uint32_t kSmem = 2 * kBuf;
 };
 template <int NS>
@@ -289,6 +297,7 @@ struct TileSrc {
   bool hasExtra;   // no cotangent carried in: the extra slab is not filled
   int base;                  // the tile's first cell
   const int32_t* haloIds;    // the tile's halo cell ids (DevMesh::halo)
+  const AdjDev* ad;          // which accumulators the tile holds (acc_prefetched)
   __device__ const float4* rec(uint32_t off) const { return reinterpret_cast<const float4*>(B + off); }
   __device__ const float* flt(uint32_t off) const { return reinterpret_cast<const float*>(B + off); }
   __device__ float4 x() const { return rec(VjpTile<NS>::kX)[tid]; }
@@ -311,6 +320,9 @@ struct TileSrc {
   __device__ int cell(int nb) const {   // the neighbour's cell id
     const int li = nb & 511;
     return li < kVTile ? base + li : __ldg(&haloIds[li - kVTile]);
+  }
+  __device__ float2 acc(int q, const float2* p) const {
+    return acc_prefetched(*ad, q) ? reinterpret_cast<const float2*>(B + VjpTile<NS>::kACC)[q * kVTile + tid] : *p;
   }
 };
 
@@ -336,8 +348,8 @@ __device__ __forceinline__ void vjp_issue_fixed(const DevMesh& m, StateF32 Q, in
   }
 }
 template <int NS>
-__device__ __forceinline__ void vjp_issue_cot(const DevMesh& m, const float* mu, const float* extra, int t,
-                                              unsigned char* B, int hid) {
+__device__ __forceinline__ void vjp_issue_cot(const DevMesh& m, const AdjDev& a, const float* mu, const float* extra,
+                                              int t, unsigned char* B, int hid) {
   using T = VjpTile<NS>;
   const int tid = threadIdx.x, n = m.n;
   const int c = t * kVTile + tid;
@@ -346,6 +358,8 @@ __device__ __forceinline__ void vjp_issue_cot(const DevMesh& m, const float* mu,
     for (int b = 0; b < 3; ++b) {
       cp_async4(B + T::kMU + (b * kVTile + tid) * 4, &mu[(size_t)b * n + c]);
       if (extra) cp_async4(B + T::kEX + (b * kVTile + tid) * 4, &extra[(size_t)b * n + c]);
+      // the accumulators, which the kernel before this one may have updated
+      if (acc_prefetched(a, b)) cp_async8(B + T::kACC + (b * kVTile + tid) * 8, &a.accF[(size_t)b * n + c]);
     }
   }
   if (hid >= 0) {
@@ -354,10 +368,10 @@ __device__ __forceinline__ void vjp_issue_cot(const DevMesh& m, const float* mu,
   }
 }
 template <int NS>
-__device__ __forceinline__ void vjp_issue(const DevMesh& m, StateF32 Q, const float* mu, const float* extra, int t,
-                                          unsigned char* B, int hid) {
+__device__ __forceinline__ void vjp_issue(const DevMesh& m, const AdjDev& a, StateF32 Q, const float* mu,
+                                          const float* extra, int t, unsigned char* B, int hid) {
   vjp_issue_fixed<NS>(m, Q, t, B, hid);
-  vjp_issue_cot<NS>(m, mu, extra, t, B, hid);
+  vjp_issue_cot<NS>(m, a, mu, extra, t, B, hid);
 }
 
 // The inlet groups' total_A and Q cotangents of the folded boundary VJP: for
@@ -449,9 +463,9 @@ __global__ void __launch_bounds__(kVTile, MINB) k_vjp_pipe_f32(DevMesh m, AdjDev
   if constexpr (FOLD) {
     vjp_issue_fixed<NS>(m, Q, t, smem, halo_id(t));
     pdl_wait_prerequisites();
-    vjp_issue_cot<NS>(m, mu, extra, t, smem, halo_id(t));
+    vjp_issue_cot<NS>(m, a, mu, extra, t, smem, halo_id(t));
   } else {
-    vjp_issue<NS>(m, Q, mu, extra, t, smem, halo_id(t));
+    vjp_issue<NS>(m, a, Q, mu, extra, t, smem, halo_id(t));
   }
   if (tid == 0) {
     sNext[0] = take();
@@ -463,7 +477,7 @@ __global__ void __launch_bounds__(kVTile, MINB) k_vjp_pipe_f32(DevMesh m, AdjDev
   int hidNext = halo_id(tn);
   int b = 0, slot = 1;
   while (t < nTiles) {
-    if (tn < nTiles) vjp_issue<NS>(m, Q, mu, extra, tn, smem + (b ^ 1) * T::kBuf, hidNext);
+    if (tn < nTiles) vjp_issue<NS>(m, a, Q, mu, extra, tn, smem + (b ^ 1) * T::kBuf, hidNext);
     cp_async_commit();
     if (tid == 0) sNext[slot] = ahead;
     cp_async_wait<1>();
@@ -479,7 +493,7 @@ __global__ void __launch_bounds__(kVTile, MINB) k_vjp_pipe_f32(DevMesh m, AdjDev
     if (j < n)
       vjp_cell<NS, FOLD>(m, a, j,
                          TileSrc<NS>{smem + b * T::kBuf, tid, extra != nullptr, t * kVTile,
-                                     m.halo + (size_t)t * kHaloMax},
+                                     m.halo + (size_t)t * kHaloMax, &a},
                          out, cSelf, cExtra, beta, sGrp);
     __syncthreads();   // buffer b is refilled at the top of the next iteration
     if constexpr (FOLD) {   // the step's probe seeds, after the tile's own cotangents
