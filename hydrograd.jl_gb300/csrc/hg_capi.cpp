@@ -1459,6 +1459,19 @@ int ctx_setup_device(hg_ctx* c) {
   HG_CUDA(c, dalloc(c, &c->d_inletQ, std::max<size_t>(c->inletQ.size(), 1)));
   HG_CUDA(c, dalloc(c, &c->d_exitWse, std::max<size_t>(c->exitWse.size(), 1)));
   HG_CUDA(c, dalloc(c, &c->d_totalA, std::max<size_t>(c->inletQ.size(), 1)));
+  // the FP32 unfused conveyance totals' blocks per group (k_inlet_total_f32)
+  size_t inletMost = 1;
+  for (size_t g = 0; g + 1 < inletOff.size(); ++g)
+    inletMost = std::max<size_t>(inletMost, (size_t)(inletOff[g + 1] - inletOff[g]));
+  const int32_t inletParts = (int32_t)((inletMost + kStageBlockF32 - 1) / kStageBlockF32);
+  double* d_inletPart = nullptr;
+  unsigned int* d_inletTicket = nullptr;
+  {
+    const size_t groups = std::max<size_t>(c->inletQ.size(), 1);
+    HG_CUDA(c, dalloc(c, &d_inletPart, groups * (size_t)inletParts));
+    HG_CUDA(c, dalloc(c, &d_inletTicket, groups));
+    HG_CUDA(c, cudaMemsetAsync(d_inletTicket, 0, groups * sizeof(unsigned int), c->stream));
+  }
   HG_CUDA(c, dalloc(c, &c->d_perm, (size_t)N));
   HG_CUDA(c, dalloc(c, &c->Quser, (size_t)3 * N));
   HG_CUDA(c, dalloc(c, &c->QB, (size_t)3 * N));   // FP64 stage buffer; also the FP32 path's RHS output
@@ -1673,6 +1686,7 @@ int ctx_setup_device(hg_ctx* c) {
   dm.area = d_area; dm.hst = c->d_hst; dm.zb = c->d_zb; dm.man = c->d_man; dm.s0x = c->d_s0x; dm.s0y = c->d_s0y;
   dm.CP = c->d_CP; dm.CS = c->d_CS;
   dm.exitWse = c->d_exitWse; dm.inletQ = c->d_inletQ; dm.totalA = c->d_totalA;
+  dm.inletPart = d_inletPart; dm.inletTicket = d_inletTicket; dm.inletParts = inletParts;
   dm.g = c->k.g; dm.kn2 = c->k.k_n * c->k.k_n; dm.hsm = c->k.h_small;
   dm.gf = (float)c->k.g; dm.kn2f = (float)(c->k.k_n * c->k.k_n); dm.hsmf = (float)c->k.h_small;
   dm.hsmLo = (float)(c->k.h_small - (double)dm.hsmf);

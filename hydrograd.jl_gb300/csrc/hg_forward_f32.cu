@@ -885,21 +885,37 @@ __global__ void __launch_bounds__(kBlock) k_cfl_f32(DevMesh m, DevScalars s, Sta
   else block_min_publish_f(cand, s.cflMinF);
 }
 
+// Group g = blockIdx.y, its faces [o0 + p kBlock, o0 + (p + 1) kBlock) in
+// block p = blockIdx.x, one a thread (a group's faces over m.inletParts blocks
+// instead of one, whose threads each took several faces one after another);
+// the last block of the group to finish adds the blocks' sums in block order
+// (deterministic).
 __global__ void __launch_bounds__(kBlock) k_inlet_total_f32(DevMesh m, DevScalars s, StateF32 X) {
-  const int g = blockIdx.x;
+  const int g = blockIdx.y, p = blockIdx.x, P = gridDim.x;
   const int o0 = m.inletOff[g], o1 = m.inletOff[g + 1];
-  double acc = 0.0;
-  for (int i = o0 + threadIdx.x; i < o1; i += blockDim.x) {
+  const int i = o0 + p * kBlock + threadIdx.x;
+  double v = 0.0;
+  if (i < o1) {
     const int c = m.inletCell[i];
     const float4 cp = m.CP[c];
     const SideF32 L = make_side_f32(X.x[c], cp, m.hsmf, m.hsmLo);
-    acc += L.s.dry ? 0.0 : m.inletLp53[i] * (double)L.s.h / (double)cp.w;
+    v = L.s.dry ? 0.0 : m.inletLp53[i] * (double)L.s.h / (double)cp.w;
   }
-  const double t = block_sum(acc);
+  const double b = block_sum(v);
+  __shared__ int isLast;
   if (threadIdx.x == 0) {
-    m.totalA[g] = t;
-    if (!(t > 1e-10)) atomicOr(s.flags, 2);
+    m.inletPart[(size_t)g * P + p] = b;
+    __threadfence();
+    isLast = atomicAdd(&m.inletTicket[g], 1u) == (unsigned int)P - 1u;
   }
+  __syncthreads();
+  if (!isLast || threadIdx.x != 0) return;
+  __threadfence();
+  double t = 0.0;
+  for (int q = 0; q < P; ++q) t += __ldcg(&m.inletPart[(size_t)g * P + q]);
+  m.totalA[g] = t;
+  if (!(t > 1e-10)) atomicOr(s.flags, 2);
+  m.inletTicket[g] = 0u;
 }
 
 // ---------------------------------------------------------------------------
@@ -1042,7 +1058,7 @@ __global__ void k_flush_read(uint4* buf, size_t n16) {
 
 void launch_inlet_total_f32(const DevMesh& m, const DevScalars& s, StateF32 X, cudaStream_t st) {
   launch_resistance_f32(m, X, st);
-  if (m.nInlet > 0) k_inlet_total_f32<<<m.nInlet, kBlock, 0, st>>>(m, s, X);
+  if (m.nInlet > 0) k_inlet_total_f32<<<dim3(m.inletParts, m.nInlet), kBlock, 0, st>>>(m, s, X);
 }
 namespace {
 // The fused gather kernel's shapes (DevMesh::stageVariant, the autotuner's

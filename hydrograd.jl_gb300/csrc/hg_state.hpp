@@ -115,6 +115,12 @@ struct DevMesh {
   const double* exitWse = nullptr;   // [nExit]
   const double* inletQ = nullptr;    // [nInlet]
   double* totalA = nullptr;          // [nInlet] conveyance of the current stage input
+  // FP32 unfused conveyance totals (k_inlet_total_f32): each group's faces
+  // split over inletParts blocks of kInletBlock, per-block partial sums and a
+  // per-group arrival count.
+  double* inletPart = nullptr;       // [nInlet][inletParts]
+  unsigned int* inletTicket = nullptr;   // [nInlet], zero between launches
+  int32_t inletParts = 1;
   double g = 9.81, kn2 = 1.0, hsm = 1e-3;
   ResDev res;
   // Inlet-Q hydrographs (hg_set_inlet_hydrograph): for each inlet-Q group g
