@@ -343,12 +343,14 @@ def run_tsit5(args, case, device):
     """The reference's default integrator on the device (hg_integrate_tsit5:
     Tsit5 with abstol 1e-6 / reltol 1e-3, swe_2D_forward_simulation.jl:37-39)
     on the 1M-cell reach over tsit5_time simulated seconds, FP32C and FP64 (wall
-    time of the call: the state is copied in and out once); then the FP64
+    time of the call: the state is copied in and out once); then the
     discrete adjoint of fixed Tsit5 steps (hg_set_adjoint_integrator) over
-    tsit5_adj_steps steps of the initial CFL-0.4 step."""
+    tsit5_adj_steps steps of half the initial CFL-0.4 step, FP32C and FP64,
+    and the FP32C gradients against the FP64 ones."""
     from hydrograd_gb.workloads import probes_and_perturbation
     N = len(case["cell_node_count"])
-    out, final = {"cells": N, "simulated_seconds": args.tsit5_time}, {}
+    out, final, grads = {"cells": N, "simulated_seconds": args.tsit5_time}, {}, {}
+    adj_dt = None
     for prec in ("fp32c", "fp64"):
         c = make_ctx(case, prec, device)
         c.integrate_tsit5(case["Q0"], 0.0, 0.05)   # warm-up
@@ -365,25 +367,33 @@ def run_tsit5(args, case, device):
             fixed_n = int(st[0])
         final[prec], _ = c.integrate_tsit5(case["Q0"], 0.0, args.tsit5_time, dt0=args.tsit5_time / fixed_n,
                                            adaptive=False)
-        if prec == "fp64" and args.tsit5_adj_steps > 0:
+        if args.tsit5_adj_steps > 0:
             probes, _ = probes_and_perturbation(case, 64, inlet_share=0.5)
-            dt = 0.5 * c.integrate(case["Q0"], 1, cfl=0.4)[1][0]
+            if adj_dt is None:   # the same steps in both precisions
+                adj_dt = 0.5 * c.integrate(case["Q0"], 1, cfl=0.4)[1][0]
             K = args.tsit5_adj_steps
             obs = np.tile((case["wstill"] - case["zb_cells"])[probes], (K, 1))
             c.set_adjoint_integrator("tsit5")
-            c.loss_and_grad(case["Q0"], 2, dt, probes, obs[:2])   # warm-up / allocation
+            c.loss_and_grad(case["Q0"], 2, adj_dt, probes, obs[:2])   # warm-up / allocation
             t0 = time.perf_counter()
-            c.loss_and_grad(case["Q0"], K, dt, probes, obs, ckpt_every=K)
+            grads[prec] = c.loss_and_grad(case["Q0"], K, adj_dt, probes, obs, ckpt_every=K)
             el = time.perf_counter() - t0
-            out["adjoint_fp64"] = {"value": N * K / el, "seconds": el, "steps": K}
+            out["adjoint_" + prec] = {"value": N * K / el, "seconds": el, "steps": K}
         c.close()
+    if len(grads) == 2:
+        g32, g64 = grads["fp32c"], grads["fp64"]
+        rel = lambda x, y: float(np.abs(np.asarray(x) - np.asarray(y)).max() / np.abs(np.asarray(y)).max())
+        out["adjoint_error_fp32c_vs_fp64"] = {"loss_rel": rel(g32["loss"], g64["loss"]),
+                                              "grad_manning_rel_linf": rel(g32["g_manning"], g64["g_manning"]),
+                                              "grad_inlet_q_rel": rel(g32["g_inletq"], g64["g_inletq"]),
+                                              "grad_zb_rel_linf": rel(g32["g_zb"], g64["g_zb"])}
     a, b = final["fp32c"], final["fp64"]
     out["error_fp32c_vs_fp64_state_rel_linf"] = float(np.abs(a - b).max() / np.abs(b).max())
     out["error_steps"] = fixed_n
     out["config"] = ("Tsit5 adaptive (abstol 1e-6, reltol 1e-3) over %g s of the 1M-cell reach from its release; "
                      "value = accepted steps x cells / wall second; FP32C against FP64 after the same fixed steps "
-                     "(the FP32C run's step count over the same time); the FP64 fixed-step Tsit5 adjoint (probe "
-                     "loss, 64 probes) at half the initial CFL-0.4 step" % args.tsit5_time)
+                     "(the FP32C run's step count over the same time); the fixed-step Tsit5 adjoint (probe "
+                     "loss, 64 probes) at half the initial CFL-0.4 step, FP32C and FP64" % args.tsit5_time)
     return out
 
 
@@ -829,7 +839,7 @@ def main():
     ap.add_argument("--ens-members", type=int, default=32, help="members per mesh")
     ap.add_argument("--tsit5-time", type=float, default=1.0,
                     help="simulated seconds of the Tsit5 leg on the 1M-cell reach (0: skip)")
-    ap.add_argument("--tsit5-adj-steps", type=int, default=10, help="steps of the FP64 Tsit5 adjoint leg (0: skip)")
+    ap.add_argument("--tsit5-adj-steps", type=int, default=10, help="steps of the Tsit5 adjoint leg, FP32C and FP64 (0: skip)")
     ap.add_argument("--res-steps", type=int, default=200,
                     help="CFL steps of the state-dependent resistance leg (0: skip)")
     ap.add_argument("--hll-steps", type=int, default=500,

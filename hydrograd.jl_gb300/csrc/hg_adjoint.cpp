@@ -374,14 +374,13 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
                           const double* obs, int32_t P, double* loss, double* gManning, double* gZb, double* gInlet,
                           double* Qfinal, const FinalObs* fo, double* parts) {
   const bool tsit5 = c->adjIntegrator == 1;
-  if (tsit5 && c->precision != HG_FP64)
-    return fail(c, HG_ERR_UNSUPPORTED, "the fixed-step Tsit5 adjoint needs an FP64 context");
   int rc = setup(c);
   if (rc) return rc;
   AdjointBuffers* b = c->adj;
   AdjDev& a = b->dev;
   a.wantN = gManning ? 1 : 0;   // the FP32C VJP skips the accumulators of gradients not asked for
   a.wantZb = gZb ? 1 : 0;
+  a.noMask = tsit5 ? 1 : 0;   // FP32 VJP kernels: the RHS VJP of Tsit5 stages, no clamp masks
   const int N = c->n;
   // A state-dependent Manning n (the n functions): dL/dn is chained into the
   // state and the function's parameters instead of accumulated per cell.
@@ -588,7 +587,138 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
   // recomputation and the VJP of that stage alike.
   auto hydro = [&](double t) { c->launches += launch_hydrograph(dm, ds, kHydroAt, t, st); };
 
-  if (tsit5) {
+  if (tsit5 && !f64) {
+    // The fixed-step Tsit5 adjoint below in an FP32-compensated context: the
+    // states and stage states as hi + lo records, the stage RHS, the stage
+    // cotangents, Kbar and lam as FP32 vectors (the FP32 VJP kernels' own
+    // precision); the forward arithmetic is hg_integrate_tsit5's (FP32 sums
+    // of the stage terms added to the state's pairs, kModeRhsF32), and the VJP
+    // kernels run unmasked (AdjDev::noMask).
+    const int n = N;
+    const Tsit5Tableau& tb = tsit5_tableau();
+    if (!b->tsit5) ADJ_CUDA(c, falloc(b, &b->tsit5, (size_t)kTsit5Vectors * n3));
+    const F32States ck = f32_view(b->ckpt, (size_t)nck, n);
+    const F32States sg = f32_view(b->seg, (size_t)(2 * C + 1), n);
+    // The Tsit5 buffer (18 x 24 B per cell): Y_1 .. Y_5 records (their x
+    // parts, then their lo parts), then K_0 .. K_5, Ybar_0 .. Ybar_5 and Kbar.
+    char* base = reinterpret_cast<char*>(b->tsit5);
+    const F32States yv = f32_view(b->tsit5, 5, n);
+    StateF32 Y[6];
+    float *Kv[6], *Yb[6];
+    for (int i = 1; i < 6; ++i) Y[i] = yv.at((size_t)(i - 1), n);
+    float* fbase = reinterpret_cast<float*>(base + (size_t)5 * n * (sizeof(float4) + sizeof(float2)));
+    for (int i = 0; i < 6; ++i) {
+      Kv[i] = fbase + (size_t)i * n3;
+      Yb[i] = fbase + (size_t)(6 + i) * n3;
+    }
+    float* kb = fbase + (size_t)12 * n3;
+    float* lam = reinterpret_cast<float*>(b->mu1);
+    float* lamNext = reinterpret_cast<float*>(b->mu2);
+    StateF32 XA{c->XA, c->XQA}, XB{c->XB, c->XQB};
+    auto rhs = [&](StateF32 X, float* out, double t) {
+      hydro(t);
+      launch_inlet_total_f32(dm, ds, X, st);   // the RHS's inlet totals (and resistance) of X
+      launch_stage_f32(dm, ds, kModeRhsF32, X, StateF32{}, StateF32{}, reinterpret_cast<double*>(out), false, st);
+      c->launches += 1 + (dm.nInlet > 0 ? 1 : 0) + resistance_launches(dm);
+    };
+    auto terms_f = [&](const float* const* K, const double* w, int nk, double h) {
+      Tsit5TermsF t{};
+      for (int j = 0; j < nk; ++j) {
+        t.K[j] = K[j];
+        t.w[j] = (float)(w[j] * h);
+      }
+      t.nk = nk;
+      return t;
+    };
+    // The stages of step s from U (K_0 .. K_nk-1, Y_1 .. Y_5); Unext: the new state, or null.
+    auto stages = [&](int s, StateF32 U, int nk, const StateF32* Unext) {
+      const double t = s * dt;
+      Y[0] = U;
+      rhs(U, Kv[0], t);
+      for (int i = 1; i < 6; ++i) {
+        launch_tsit5_combine_f32(n, U, terms_f(Kv, tb.a[i], i, dt), Y[i], st);
+        if (i < nk) rhs(Y[i], Kv[i], t + tb.c[i] * dt);
+        c->launches += 1;
+      }
+      if (Unext) {
+        launch_tsit5_combine_f32(n, U, terms_f(Kv, tb.a[6], 6, dt), *Unext, st);
+        c->launches += 1;
+      }
+    };
+    auto copy_state = [&](StateF32 dst, StateF32 src) -> cudaError_t {
+      cudaError_t e = cudaMemcpyAsync(dst.x, src.x, (size_t)n * sizeof(float4), cudaMemcpyDeviceToDevice, st);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(dst.q, src.q, (size_t)n * sizeof(float2), cudaMemcpyDeviceToDevice, st);
+      return e;
+    };
+    launch_gather_state_f32(N, c->d_perm, c->Quser, XA, st);
+    const int sLast = seg_start(nck - 1);
+    for (int s = 0; s < K; ++s) {
+      const bool last = s >= sLast;
+      const size_t i = (size_t)(s - sLast);
+      if (!last && s == seg_start(seg_of(s))) ADJ_CUDA(c, copy_state(ck.at(seg_of(s), n), XA));
+      if (s == sLast) ADJ_CUDA(c, copy_state(sg.at(0, n), XA));
+      const StateF32 u0 = last ? sg.at(i, n) : XA;
+      const StateF32 u1 = last ? sg.at(i + 1, n) : XB;
+      stages(s, u0, 6, &u1);
+      if (!last) std::swap(XA, XB);
+    }
+    ADJ_CUDA(c, copy_state(XA, sg.at((size_t)(K - sLast), n)));   // the final state
+    if (Qfinal) launch_scatter_state_f32(N, c->d_perm, XA, c->Quser, st);   // copied out at the end
+    // Reverse sweep: the probe terms (loss and seed) of the final state, unmasked.
+    ADJ_CUDA(c, cudaMemsetAsync(lam, 0, n3 * sizeof(float), st));
+    launch_probe_f32(dm, a, XA, lam, pc, b->probes, b->obs + (size_t)(K - 1) * P, P, scale, st);
+    c->launches += P > 0 ? 1 : 0;
+    if (useFinal) {
+      fl.mask = 0;
+      launch_final_loss_f32(dm, fl, XA, lam, st);
+      c->launches += 1;
+    }
+    for (int seg = nck - 1; seg >= 0; --seg) {
+      const int s0 = seg_start(seg), s1 = seg_start(seg + 1);
+      if (seg < nck - 1) {   // the segment's states from its checkpoint (the last one's are in place)
+        ADJ_CUDA(c, copy_state(sg.at(0, n), ck.at(seg, n)));
+        for (int s = s0; s < s1 - 1; ++s) {
+          const StateF32 nx = sg.at((size_t)(s - s0 + 1), n);
+          stages(s, sg.at((size_t)(s - s0), n), 6, &nx);
+        }
+      }
+      for (int s = s1 - 1; s >= s0; --s) {
+        const StateF32 U = sg.at((size_t)(s - s0), n);
+        stages(s, U, 5, nullptr);   // K_0 .. K_4 and Y_1 .. Y_5
+        for (int i = 5; i >= 0; --i) {
+          Tsit5TermsF t{};   // Kbar_i = dt (b_i lam + sum_{k>i} a_ki Ybar_k)
+          t.K[0] = lam;
+          t.w[0] = (float)(tb.a[6][i] * dt);
+          for (int k = i + 1; k < 6; ++k) {
+            t.K[k - i] = Yb[k];
+            t.w[k - i] = (float)(tb.a[k][i] * dt);
+          }
+          t.nk = 6 - i;
+          launch_tsit5_lin_f32(n3, t, kb, st);
+          hydro(s * dt + tb.c[i] * dt);
+          launch_inlet_total_f32(dm, ds, Y[i], st);   // the stage's inlet totals and resistance
+          c->launches += launch_vjp_f32(dm, a, Y[i], kb, nullptr, Yb[i], 0.0f, 0.0f, 1.0, st, nullptr);
+          c->launches += launch_ude_vjp_f32(dm, a, Y[i], Yb[i], st);
+          c->launches += 1 + (dm.nInlet > 0 ? 1 : 0) + resistance_launches(dm);
+        }
+        Tsit5TermsF t{};   // lam_s = lam' + sum_i Ybar_i
+        t.K[0] = lam;
+        t.w[0] = 1.0f;
+        for (int i = 0; i < 6; ++i) {
+          t.K[1 + i] = Yb[i];
+          t.w[1 + i] = 1.0f;
+        }
+        t.nk = 7;
+        launch_tsit5_lin_f32(n3, t, lamNext, st);
+        std::swap(lam, lamNext);
+        c->launches += 1;
+        if (s >= 1) {
+          launch_probe_f32(dm, a, U, lam, pc, b->probes, b->obs + (size_t)(s - 1) * P, P, scale, st);
+          c->launches += P > 0 ? 1 : 0;
+        }
+      }
+    }
+  } else if (tsit5) {
     // Fixed-step Tsit5 (hg_integrate_tsit5 with adaptive = 0): step s takes
     // U_s at t_s = s dt to U_{s+1} = U_s + dt sum_{j<6} b_j K_j, with
     // K_i = f(Y_i, t_s + c_i dt), Y_0 = U_s, Y_i = U_s + dt sum_{j<i} a_ij K_j

@@ -117,7 +117,11 @@ struct GlobalSrc {
 // sources), written to out[j] and the cell's parameter accumulators.  FOLD:
 // the boundary faces too, from their flux Jacobians (a.bndJ), and the inlet
 // conveyance terms with the groups' total_A cotangents grpTA.
-template <int NS, bool FOLD, class Src>
+// NOMASK: the VJP of the RHS alone (the stages of a Tsit5 step, which no clamp
+// of the stage state follows): a dry cell's output is not masked, and its
+// interior faces, through which the RHS depends on the cell's own xi, are
+// differentiated by the dual-number path.
+template <int NS, bool FOLD, class Src, bool NOMASK = false>
 __device__ __forceinline__ void vjp_cell(const DevMesh& m, const AdjDev& a, int j, const Src& src, float* out,
                                          float cSelf, float cExtra, float beta, const double* grpTA = nullptr) {
   const int n = m.n;
@@ -128,7 +132,7 @@ __device__ __forceinline__ void vjp_cell(const DevMesh& m, const AdjDev& a, int 
   const float mj0 = src.mu_own(0), mj1 = src.mu_own(1), mj2 = src.mu_own(2);
   float g0 = 0.0f, g1 = 0.0f, g2 = 0.0f, gn = 0.0f;
   unsigned int bnd = 0u;   // FOLD: the slots that hold boundary faces
-  if (!L.s.dry) {   // a dry cell's output is masked to zero, and its faces add to nothing else
+  if (!L.s.dry || NOMASK) {   // (masked: a dry cell's output is zero, and its faces add to nothing else)
     // Wet-wet faces in reverse mode (roe_wet_vjp, the own quantities'
     // adjoints summed over the faces and taken back once); faces with a dry
     // neighbour through 3-direction duals of the reference solver.
@@ -149,14 +153,16 @@ __device__ __forceinline__ void vjp_cell(const DevMesh& m, const AdjDev& a, int 
       const float w0 = len * (r.m0 / An - mj0 / Aj);
       const float w1 = len * (r.m1 / An - mj1 / Aj);
       const float w2 = len * (r.m2 / An - mj2 / Aj);
-      if (!R.s.dry && m.riemann == kRiemannRoe) {
+      if (!L.s.dry && !R.s.dry && m.riemann == kRiemannRoe) {
         roe_wet_vjp<float>(L.s, o, R.s, (R.s.xi - L.s.xi) + (R.xlo - L.xlo), m.gf, nx, ny, w0, w1, w2, b);
       } else {
         const Side<F3> L3 = seeded<F3>(L.s, -1);
         const Side<F3> R3 = constant<F3>(R.s);
         const F3 dxi = (R3.xi - L3.xi) + F3(R.xlo - L.xlo);
         // the forward pass's wall test (bank_wall_f64), so that the same branch is differentiated
-        const int bank = R.s.dry ? bank_wall_f64(m, L.s.xi, L.xlo, j, src.cell(nb)) : -1;
+        int bank = -1;
+        if (R.s.dry && !L.s.dry) bank = bank_wall_f64(m, L.s.xi, L.xlo, j, src.cell(nb));
+        else if (NOMASK && L.s.dry && !R.s.dry) bank = bank_wall_f64(m, R.s.xi, R.xlo, src.cell(nb), j);
         F3 F[3];
         riemann_flux<F3>(m.riemann, L3, R3, dxi, F3(m.gf), F3(nx), F3(ny), F3(m.hsmf), F, bank);
         g0 += w0 * F[0].d[0] + w1 * F[1].d[0] + w2 * F[2].d[0];
@@ -164,6 +170,7 @@ __device__ __forceinline__ void vjp_cell(const DevMesh& m, const AdjDev& a, int 
         g2 += w0 * F[0].d[2] + w1 * F[1].d[2] + w2 * F[2].d[2];
       }
     }
+    if (!L.s.dry) {   // (a dry cell -- NOMASK -- has no wet-wet face and no source term)
     float gx, gu, gv;
     own_vjp<float>(L.s, o, m.gf, b, gx, gu, gv);
     g0 += gx;
@@ -194,6 +201,7 @@ __device__ __forceinline__ void vjp_cell(const DevMesh& m, const AdjDev& a, int 
     if (a.wantZb) {
       acc_add_from(&a.accF[(size_t)n + j], src.acc(1, &a.accF[(size_t)n + j]), beta, mj1 * m.gf * L.s.xi);
       acc_add_from(&a.accF[(size_t)2 * n + j], src.acc(2, &a.accF[(size_t)2 * n + j]), beta, mj2 * m.gf * L.s.xi);
+    }
     }
   }
   if constexpr (FOLD) {   // a dry cell's boundary faces (the face loop above runs for wet cells)
@@ -249,7 +257,7 @@ __device__ __forceinline__ void vjp_cell(const DevMesh& m, const AdjDev& a, int 
   } else if (a.wantN && gn != 0.0f) {
     acc_add_from(&a.accF[j], src.acc(0, &a.accF[j]), beta, gn);
   }
-  const float mask = L.s.dry ? 0.0f : 1.0f;
+  const float mask = (L.s.dry && !NOMASK) ? 0.0f : 1.0f;
   const float e0 = src.extra_own(0), e1 = src.extra_own(1), e2 = src.extra_own(2);
   out[j] = mask * (cSelf * mj0 + cExtra * e0 + beta * g0);
   out[n + j] = mask * (cSelf * mj1 + cExtra * e1 + beta * g1);
@@ -263,13 +271,13 @@ __device__ __forceinline__ void vjp_cell(const DevMesh& m, const AdjDev& a, int 
 // before it exits (it reads nothing the boundary kernel writes), so the
 // kernels after it see both.
 
-template <int NS>
+template <int NS, bool NOMASK = false>
 __global__ void __launch_bounds__(kBlock, vjp_min_blocks<NS>()) k_vjp_f32(DevMesh m, AdjDev a, StateF32 Q, const float* __restrict__ mu,
                                                     const float* __restrict__ extra, float* out, float cSelf,
                                                     float cExtra, float beta) {
   pdl_release_dependents();
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j < m.n) vjp_cell<NS, false>(m, a, j, GlobalSrc{m, Q, mu, extra, j}, out, cSelf, cExtra, beta);
+  if (j < m.n) vjp_cell<NS, false, GlobalSrc, NOMASK>(m, a, j, GlobalSrc{m, Q, mu, extra, j}, out, cSelf, cExtra, beta);
   pdl_wait_prerequisites();
 }
 
@@ -664,13 +672,14 @@ __device__ __forceinline__ double depth_f64(const DevMesh& m, StateF32 Q, int c)
 }
 
 // The seed of distinct probe cell u: mu_xi[c] += sum over the probes at c (in
-// probe order) of scale 2 (h - obs_p), when c is wet.
+// probe order) of scale 2 (h - obs_p), when c is wet (mask; otherwise in any
+// case: a state no clamp follows, as Tsit5's).
 __device__ __forceinline__ void probe_seed(const DevMesh& m, StateF32 Q, float* mu, const ProbeCsr& pc,
-                                           const double* __restrict__ obs, double scale, int u) {
+                                           const double* __restrict__ obs, double scale, int u, bool mask) {
   const int c = pc.cell[u];
   const float4 cp = m.CP[c];
   const SideF32 L = make_side_f32(Q.x[c], cp, m.hsmf, m.hsmLo);
-  if (L.s.dry) return;
+  if (mask && L.s.dry) return;
   const double h = depth_f64(m, Q, c);
   double acc = 0.0;
   for (int i = pc.off[u]; i < pc.off[u + 1]; ++i) acc += scale * 2.0 * (h - obs[pc.idx[i]]);
@@ -685,7 +694,7 @@ __device__ __forceinline__ void probe_block(const DevMesh& m, const AdjDev& a, S
                                             const ProbeCsr& pc, const int32_t* __restrict__ probes,
                                             const double* __restrict__ obs, int np, double scale, bool skipBnd) {
   for (int u = threadIdx.x; u < pc.nCells; u += blockDim.x)
-    if (!skipBnd || !pc.isBnd[u]) probe_seed(m, Q, mu, pc, obs, scale, u);
+    if (!skipBnd || !pc.isBnd[u]) probe_seed(m, Q, mu, pc, obs, scale, u, !a.noMask);
   double s = 0.0;
   for (int p = threadIdx.x; p < np; p += blockDim.x) {
     const double e = depth_f64(m, Q, probes[p]) - obs[p];
@@ -763,14 +772,15 @@ __global__ void __launch_bounds__(kCombineBlock) k_vjp_combine_f32(DevMesh m, Ad
   const bool chainN = a.resChain || a.udeChain == 1;   // dL/dn of the cell goes to n's function
   if (a.wantN && !chainN && g[3] != 0.0f) acc_add(&a.accF[j], beta, g[3]);
   if (a.wantZb && g[4] != 0.0f) acc_add(&a.accF[(size_t)3 * n + j], beta, g[4]);
-  if (L.s.dry) return;
+  if (L.s.dry && !a.noMask) return;
   // n = f(state): the boundary faces' and the inlet conveyance's dL/dn of the
   // cell into its state and the function's parameters
   double gnRes = chainN ? (double)g[3] : 0.0;
   out[j] += beta * g[0];
   out[n + j] += beta * g[1];
   out[2 * n + j] += beta * g[2];
-  for (int p = a.bndInOff[i]; p < a.bndInOff[i + 1]; ++p) {
+  // (total_A sums the wet cells only: a dry cell's state does not enter it)
+  for (int p = L.s.dry ? a.bndInOff[i + 1] : a.bndInOff[i]; p < a.bndInOff[i + 1]; ++p) {
     const double gTA = a.grpTA[a.bndInGrp[p]];
     const double coef = a.bndInCoef[p], nm = cp.w;
     out[j] += (float)(betaD * gTA * coef / nm);
@@ -781,13 +791,13 @@ __global__ void __launch_bounds__(kCombineBlock) k_vjp_combine_f32(DevMesh m, Ad
   if (a.udeChain == 1 && gnRes != 0.0) a.udeGn[j] += betaD * gnRes;
   if (a.resChain && gnRes != 0.0) {
     const ResJac<double> J = manning_jac<double>(m.res, (double)L.s.h, (double)L.s.hu, (double)L.s.hv,
-                                                 m.res.ks ? m.res.ks[j] : 0.0, false);
+                                                 m.res.ks ? m.res.ks[j] : 0.0, L.s.dry);
     out[j] += (float)(betaD * gnRes * J.dh);
     out[n + j] += (float)(betaD * gnRes * J.dqx);
     out[2 * n + j] += (float)(betaD * gnRes * J.dqy);
     for (int k = 0; k < 4; ++k) a.gResP[(size_t)k * n + j] += betaD * gnRes * J.dp[k];
   }
-  if (pj.np > 0 && a.bndProbe[i] >= 0) probe_seed(m, Q, out, pj.pc, pj.obs, pj.scale, a.bndProbe[i]);
+  if (pj.np > 0 && a.bndProbe[i] >= 0) probe_seed(m, Q, out, pj.pc, pj.obs, pj.scale, a.bndProbe[i], !a.noMask);
 }
 
 __global__ void k_fold_accumulators_f32(DevMesh m, AdjDev a) {
@@ -865,6 +875,10 @@ int vjp_fold_minb() {
 template <int NS>
 void launch_vjp_interior(const DevMesh& m, const AdjDev& a, StateF32 Q, const float* mu, const float* extra,
                          float* out, float cSelf, float cExtra, float beta, bool pdl, cudaStream_t st) {
+  if (a.noMask) {   // the RHS VJP of Tsit5 stages: the gather kernel's unmasked instance
+    launch_k(pdl, k_vjp_f32<NS, true>, blocks_for(m.n), kBlock, 0, st, m, a, Q, mu, extra, out, cSelf, cExtra, beta);
+    return;
+  }
   if constexpr (NS <= 4) {
     if (pipe_usable(m, Q)) {
       launch_vjp_pipe<NS, false>(m, a, Q, mu, extra, out, cSelf, cExtra, beta, (double)beta, pdl, st);

@@ -78,6 +78,10 @@ struct AdjDev {
   // gResP [4][n]; the FP32C VJP adds into compensated pairs accRes, folded in
   // at the end).
   int32_t resChain = 0;
+  // The FP32 VJP kernels as the VJP of the RHS alone (the stages of a Tsit5
+  // step, which no clamp of the stage state follows): no dry-cell masks in
+  // the VJP, its boundary terms or the probe seeds.
+  int32_t noMask = 0;
   double* gResP = nullptr;
   float2* accRes = nullptr;
   // A UDE closure (hg_set_ude): udeChain = 1 when the network gives n

@@ -143,6 +143,16 @@ __global__ void __launch_bounds__(kBlock) k_tsit5_error_f32(int32_t n, StateF32 
   }
 }
 
+__global__ void __launch_bounds__(kBlock) k_tsit5_lin_f32(int64_t len, Tsit5TermsF t, float* __restrict__ Y) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < len; i += (int64_t)gridDim.x * blockDim.x) {
+    float s = 0.0f;
+#pragma unroll
+    for (int j = 0; j < kTsit5Stages; ++j)
+      if (j < t.nk) s = fmaf(t.w[j], __ldg(&t.K[j][i]), s);
+    Y[i] = s;
+  }
+}
+
 __global__ void k_f32_to_f64(int32_t n, StateF32 X, double* __restrict__ Q) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -190,6 +200,10 @@ void launch_tsit5_combine_f32(int32_t n, StateF32 U, const Tsit5TermsF& t, State
 void launch_tsit5_error_f32(int32_t n, StateF32 U, StateF32 Unew, const Tsit5TermsF& t, float abstol, float reltol,
                             double* partials, unsigned int* ticket, double* norm2, cudaStream_t st) {
   k_tsit5_error_f32<<<grid_for(n), kBlock, 0, st>>>(n, U, Unew, t, abstol, reltol, partials, ticket, norm2);
+}
+
+void launch_tsit5_lin_f32(int64_t len, const Tsit5TermsF& t, float* Y, cudaStream_t st) {
+  k_tsit5_lin_f32<<<grid_for(len), kBlock, 0, st>>>(len, t, Y);
 }
 
 void launch_f32_to_f64(int32_t n, StateF32 X, double* Q, cudaStream_t st) {

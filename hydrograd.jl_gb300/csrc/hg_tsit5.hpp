@@ -53,6 +53,9 @@ void launch_tsit5_combine_f32(int32_t n, StateF32 U, const Tsit5TermsF& t, State
 // with nk = 0 the values are U's own (the initial step's norm of the state).
 void launch_tsit5_error_f32(int32_t n, StateF32 U, StateF32 Unew, const Tsit5TermsF& t, float abstol, float reltol,
                             double* partials, unsigned int* ticket, double* norm2, cudaStream_t st);
+// Y = sum_j w[j] K[j] over float vectors of length len (the FP32-compensated
+// Tsit5 adjoint's cotangent combinations).
+void launch_tsit5_lin_f32(int64_t len, const Tsit5TermsF& t, float* Y, cudaStream_t st);
 void launch_f32_to_f64(int32_t n, StateF32 X, double* Q, cudaStream_t st);
 void launch_f64_to_f32(int32_t n, const double* Q, StateF32 X, cudaStream_t st);
 

@@ -346,8 +346,8 @@ class SWE2D:
 
     def set_adjoint_integrator(self, integrator):
         """hg_set_adjoint_integrator: the steps the gradient calls run and
-        differentiate -- "ssprk2" (default) or "tsit5" (fixed Tsit5 steps of dt,
-        FP64 contexts)."""
+        differentiate -- "ssprk2" (default) or "tsit5" (fixed Tsit5 steps of dt;
+        an FP32C context runs them on FP32 vectors)."""
         code = {"ssprk2": 0, "tsit5": 1}[integrator]
         self._chk(lib().hg_set_adjoint_integrator(self.h, code))
 

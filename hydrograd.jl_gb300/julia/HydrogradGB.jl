@@ -175,7 +175,7 @@ set_riemann_solver!(ctx::Context, s::AbstractString) =
     check(ctx.ptr, ccall((:hg_set_riemann_solver, lib), Cint, (Ptr{Cvoid}, Int32), ctx, riemann_code(s)))
 set_dt_min!(ctx::Context, dt_min::Real) =
     check(ctx.ptr, ccall((:hg_set_dt_min, lib), Cint, (Ptr{Cvoid}, Float64), ctx, Float64(dt_min)))
-# The steps the gradients differentiate: :ssprk2 (default) or :tsit5 (fixed Tsit5 steps, FP64 contexts).
+# The steps the gradients differentiate: :ssprk2 (default) or :tsit5 (fixed Tsit5 steps).
 set_adjoint_integrator!(ctx::Context, integrator::Symbol) =
     check(ctx.ptr, ccall((:hg_set_adjoint_integrator, lib), Cint, (Ptr{Cvoid}, Int32), ctx,
                          Int32(integrator === :tsit5 ? 1 : integrator === :ssprk2 ? 0 : error("integrator"))))

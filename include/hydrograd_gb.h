@@ -374,9 +374,10 @@ int hg_set_adjoint_tape(hg_ctx* ctx, int64_t bytes);
  * steps: per step, the six stage states recomputed from the step's start
  * state and the stage cotangents taken back through the RHS Jacobian at each
  * (Kbar_i = dt (b_i lam + sum_{k>i} a_ki Ybar_k), Ybar_i = J(Y_i)^T Kbar_i).
- * FP64 contexts only (HG_ERR_UNSUPPORTED from the gradient calls of an FP32C
- * context set to HG_ADJ_TSIT5).  The probe loss is taken at the states after
- * each step, as with SSP-RK2. */
+ * In an FP32C context the same steps run on FP32 vectors (the states as hi + lo
+ * records, as hg_integrate_tsit5 keeps them; the cotangents in FP32) through
+ * the FP32 VJP kernels without the clamp masks.  The probe loss is taken at
+ * the states after each step, as with SSP-RK2. */
 enum hg_adjoint_integrator { HG_ADJ_SSPRK2 = 0, HG_ADJ_TSIT5 = 1 };
 int hg_set_adjoint_integrator(hg_ctx* ctx, int32_t integrator);
 

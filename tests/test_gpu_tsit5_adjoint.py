@@ -11,7 +11,9 @@ SSP-RK2 adjoint is in tests/test_gpu_adjoint.py: the probe loss's zone-n,
 inlet-Q and directional zb gradients, several checkpoint spacings, an inlet
 hydrograph (central differences of a shift), and final-state
 vector-Jacobian products (hg_final_vjp) against the duals' final-state
-tangents.  FP32C contexts refuse the Tsit5 adjoint.
+tangents.  FP32C contexts run the same adjoint on FP32 vectors (the unmasked
+FP32 VJP kernels): against the same duals at FP32C tolerances, and through a
+sigmoid n and a UDE closure against the FP64 device adjoint.
 """
 import numpy as np
 import pytest
@@ -143,16 +145,54 @@ def test_hydrograph_run_matches_central_differences():
     assert abs(r["g_inletq"][0] - fd) <= 1e-5 * abs(fd)
 
 
-def test_fp32c_context_refuses_the_tsit5_adjoint():
-    case = river()
+def fp32c_ctx(case):
     c = SWE2D(case, precision="fp32c")
     c.set_still_water(case["wstill"])
     c.set_manning_zones(case["mat_id"], case["manning_zones"])
     c.set_inlet_q(case["inlet_q"])
     c.set_exit_wse(case["exit_wse"])
     c.set_adjoint_integrator("tsit5")
-    with pytest.raises(HgError):
-        c.loss_and_grad(case["Q0"], 4, 0.1, np.array([1], np.int32), np.zeros((4, 1)))
+    return c
+
+
+# FP32C against the FP64 duals: the forward states within 1e-5 of scale (the
+# FP32C state error), the gradients within 1e-3 of their largest component
+# (FP32 cotangents through 24 steps of six stages).
+@pytest.mark.parametrize("ckpt", [5, 50])
+def test_fp32c_loss_and_gradients_match_dual_numbers(problem, ckpt):
+    p = problem
+    c = fp32c_ctx(p["case"])
+    r = c.loss_and_grad(p["Q0"], K, p["dt"], p["probes"], p["obs"], ckpt_every=ckpt)
+    assert np.abs(r["Q"] - p["Qo"]).max() <= 1e-5 * np.abs(p["Qo"]).max()
+    assert abs(r["loss"] - p["L"]) <= 1e-4 * abs(p["L"])
+    gz = zone_sums(r["g_manning"], p["zones"], p["nz"])
+    assert np.abs(gz - p["dL"][:p["nz"]]).max() <= 1e-3 * np.abs(p["dL"][:p["nz"]]).max()
+    assert abs(r["g_zb"] @ p["v"] - p["dLz"][0]) <= 1e-3 * abs(p["dLz"][0])
+    assert abs(r["g_inletq"][0] - p["dLq"][0]) <= 1e-3 * abs(p["dLq"][0])
+
+
+def test_fp32c_checkpoint_spacing_and_repeat_give_the_same_bits(problem):
+    p = problem
+    c = fp32c_ctx(p["case"])
+    a = c.loss_and_grad(p["Q0"], K, p["dt"], p["probes"], p["obs"], ckpt_every=5)
+    b = c.loss_and_grad(p["Q0"], K, p["dt"], p["probes"], p["obs"], ckpt_every=7)
+    d = c.loss_and_grad(p["Q0"], K, p["dt"], p["probes"], p["obs"], ckpt_every=5)
+    for k in ("g_manning", "g_zb", "g_inletq"):
+        np.testing.assert_array_equal(a[k], b[k])
+        np.testing.assert_array_equal(a[k], d[k])
+    assert a["loss"] == b["loss"] == d["loss"]
+
+
+def test_fp32c_final_vjp_matches_dual_numbers(problem):
+    p = problem
+    c = fp32c_ctx(p["case"])
+    lam = Stream(11).uniform(3 * p["N"], -1.0, 1.0)
+    r = c.final_state_vjp(p["Q0"], K, p["dt"], lam)
+    ref_n = p["dQ"][:p["nz"]] @ lam
+    gz = zone_sums(r["g_manning"], p["zones"], p["nz"])
+    assert np.abs(gz - ref_n).max() <= 1e-3 * np.abs(ref_n).max()
+    assert abs(r["g_zb"] @ p["v"] - p["dQz"][0] @ lam) <= 1e-3 * abs(p["dQz"][0] @ lam)
+    assert abs(r["g_inletq"][0] - p["dQq"][0] @ lam) <= 1e-3 * abs(p["dQq"][0] @ lam)
 
 
 # Through a state-dependent resistance: every stage's VJP takes dL/dn back
@@ -201,6 +241,13 @@ def test_sigmoid_n_function_gradients_match_central_differences():
     e = 1e-6 * q0[0]
     fdq = (loss(q=q0 + e) - loss(q=q0 - e)) / (2 * e)
     assert abs(r["g_inletq"][0] - fdq) <= 1e-5 * abs(fdq)
+    # FP32C against the FP64 device adjoint
+    c32, _ = R.make(c, "fp32c", "sigmoid", params)
+    c32.set_adjoint_integrator("tsit5")
+    r32 = c32.loss_and_grad(Q0, RK, dt, probes, obs, ckpt_every=5)
+    assert abs(r32["loss"] - r["loss"]) <= 1e-4 * abs(r["loss"])
+    assert np.abs(c32.resistance_grad() - gp).max() <= 1e-3 * np.abs(gp).max()
+    assert abs(r32["g_inletq"][0] - r["g_inletq"][0]) <= 1e-3 * abs(r["g_inletq"][0])
 
 
 @pytest.mark.parametrize("which", [0, 1, 2, 3, 4, 5])
@@ -227,3 +274,9 @@ def test_ude_gradients_match_central_differences(which):
         fd[e] = (loss(theta + e * v) - loss(theta - e * v)) / (2 * e)
     fdr = (4 * fd[1e-4] - fd[2e-4]) / 3
     assert abs(g @ v - fdr) <= 1e-5 * np.linalg.norm(g) * np.linalg.norm(v)
+    # FP32C against the FP64 device adjoint
+    c32 = U.make(c, "fp32c", spec, theta)
+    c32.set_adjoint_integrator("tsit5")
+    r32 = c32.loss_and_grad(Q0, RK, dt, probes, obs, ckpt_every=5)
+    assert abs(r32["loss"] - r["loss"]) <= 1e-4 * abs(r["loss"])
+    assert np.linalg.norm(c32.ude_grad() - g) <= 1e-3 * np.linalg.norm(g)
