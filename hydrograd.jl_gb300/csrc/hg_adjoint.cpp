@@ -374,6 +374,8 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
                           const double* obs, int32_t P, double* loss, double* gManning, double* gZb, double* gInlet,
                           double* Qfinal, const FinalObs* fo, double* parts) {
   const bool tsit5 = c->adjIntegrator == 1;
+  if (tsit5 && !c->adjSteps.empty() && (size_t)K > c->adjSteps.size())
+    return fail(c, HG_ERR_ARG, "more steps than the step sizes set by hg_set_adjoint_steps");
   int rc = setup(c);
   if (rc) return rc;
   AdjointBuffers* b = c->adj;
@@ -586,6 +588,17 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
   // step s at s dt, stage 2 at (s + 1) dt -- in the forward pass, the
   // recomputation and the VJP of that stage alike.
   auto hydro = [&](double t) { c->launches += launch_hydrograph(dm, ds, kHydroAt, t, st); };
+  // Tsit5: the step sizes differentiated -- dt each, or the sequence
+  // hg_set_adjoint_steps gave (the accepted steps of an adaptive solve, held
+  // fixed), step s then starting at the sum of the sizes before it.
+  const bool stepList = tsit5 && !c->adjSteps.empty();
+  std::vector<double> tStart;
+  if (stepList) {
+    tStart.assign((size_t)K + 1, 0.0);
+    for (int s = 0; s < K; ++s) tStart[s + 1] = tStart[s] + c->adjSteps[s];
+  }
+  auto dtOf = [&](int s) { return stepList ? c->adjSteps[s] : dt; };
+  auto tOf = [&](int s) { return stepList ? tStart[s] : s * dt; };
 
   if (tsit5 && !f64) {
     // The fixed-step Tsit5 adjoint below in an FP32-compensated context: the
@@ -632,16 +645,16 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
     };
     // The stages of step s from U (K_0 .. K_nk-1, Y_1 .. Y_5); Unext: the new state, or null.
     auto stages = [&](int s, StateF32 U, int nk, const StateF32* Unext) {
-      const double t = s * dt;
+      const double t = tOf(s), h = dtOf(s);
       Y[0] = U;
       rhs(U, Kv[0], t);
       for (int i = 1; i < 6; ++i) {
-        launch_tsit5_combine_f32(n, U, terms_f(Kv, tb.a[i], i, dt), Y[i], st);
-        if (i < nk) rhs(Y[i], Kv[i], t + tb.c[i] * dt);
+        launch_tsit5_combine_f32(n, U, terms_f(Kv, tb.a[i], i, h), Y[i], st);
+        if (i < nk) rhs(Y[i], Kv[i], t + tb.c[i] * h);
         c->launches += 1;
       }
       if (Unext) {
-        launch_tsit5_combine_f32(n, U, terms_f(Kv, tb.a[6], 6, dt), *Unext, st);
+        launch_tsit5_combine_f32(n, U, terms_f(Kv, tb.a[6], 6, h), *Unext, st);
         c->launches += 1;
       }
     };
@@ -688,14 +701,14 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
         for (int i = 5; i >= 0; --i) {
           Tsit5TermsF t{};   // Kbar_i = dt (b_i lam + sum_{k>i} a_ki Ybar_k)
           t.K[0] = lam;
-          t.w[0] = (float)(tb.a[6][i] * dt);
+          t.w[0] = (float)(tb.a[6][i] * dtOf(s));
           for (int k = i + 1; k < 6; ++k) {
             t.K[k - i] = Yb[k];
-            t.w[k - i] = (float)(tb.a[k][i] * dt);
+            t.w[k - i] = (float)(tb.a[k][i] * dtOf(s));
           }
           t.nk = 6 - i;
           launch_tsit5_lin_f32(n3, t, kb, st);
-          hydro(s * dt + tb.c[i] * dt);
+          hydro(tOf(s) + tb.c[i] * dtOf(s));
           launch_inlet_total_f32(dm, ds, Y[i], st);   // the stage's inlet totals and resistance
           c->launches += launch_vjp_f32(dm, a, Y[i], kb, nullptr, Yb[i], 0.0f, 0.0f, 1.0, st, nullptr);
           c->launches += launch_ude_vjp_f32(dm, a, Y[i], Yb[i], st);
@@ -758,16 +771,16 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
     };
     // The stages of step s from U (K_0 .. K_nk-1, Y_1 .. Y_5); Unext: the new state, or null.
     auto stages = [&](int s, const double* U, int nk, double* Unext) {
-      const double t = s * dt;
+      const double t = tOf(s), h = dtOf(s);
       Y[0] = const_cast<double*>(U);
       rhs(U, Kv[0], t);
       for (int i = 1; i < 6; ++i) {
-        launch_tsit5_combine(n3, U, terms_of(i), dt, Y[i], st);
-        if (i < nk) rhs(Y[i], Kv[i], t + tb.c[i] * dt);
+        launch_tsit5_combine(n3, U, terms_of(i), h, Y[i], st);
+        if (i < nk) rhs(Y[i], Kv[i], t + tb.c[i] * h);
         c->launches += 1;
       }
       if (Unext) {
-        launch_tsit5_combine(n3, U, terms_of(6), dt, Unext, st);
+        launch_tsit5_combine(n3, U, terms_of(6), h, Unext, st);
         c->launches += 1;
       }
     };
@@ -820,8 +833,8 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
             t.w[k - i] = tb.a[k][i];
           }
           t.nk = 6 - i;
-          launch_tsit5_combine(n3, nullptr, t, dt, kb, st);
-          hydro(s * dt + tb.c[i] * dt);
+          launch_tsit5_combine(n3, nullptr, t, dtOf(s), kb, st);
+          hydro(tOf(s) + tb.c[i] * dtOf(s));
           launch_inlet_total_f64(dm, ds, Y[i], st);   // the stage's inlet totals and resistance
           launch_vjp_f64(dm, a, Y[i], kb, nullptr, Yb[i], 0.0, 0.0, 1.0, st, false);
           launch_inlet_adjoint_f64(dm, a, Y[i], Yb[i], 1.0, st);

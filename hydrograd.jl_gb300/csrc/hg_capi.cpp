@@ -1341,6 +1341,24 @@ int hg_set_adjoint_integrator(hg_ctx* ctx, int32_t integrator) {
   return HG_OK;
 }
 
+int hg_set_adjoint_steps(hg_ctx* ctx, const double* dts, int32_t n) {
+  if (!ctx) return fail(ctx, HG_ERR_ARG, "hg_set_adjoint_steps: null context");
+  if (n < 0 || (n > 0 && !dts)) return fail(ctx, HG_ERR_ARG, "hg_set_adjoint_steps: bad argument");
+  for (int i = 0; i < n; ++i)
+    if (!(dts[i] > 0) || !std::isfinite(dts[i]))
+      return fail(ctx, HG_ERR_ARG, "hg_set_adjoint_steps: step sizes must be positive and finite");
+  ctx->adjSteps.assign(dts, dts + n);
+  return HG_OK;
+}
+
+int hg_tsit5_steps(const hg_ctx* ctx, double* dts, int32_t cap, int32_t* count) {
+  if (!ctx || cap < 0 || (cap > 0 && !dts)) return HG_ERR_ARG;
+  const size_t m = std::min(ctx->tsit5Steps.size(), (size_t)cap);
+  for (size_t i = 0; i < m; ++i) dts[i] = ctx->tsit5Steps[i];
+  if (count) *count = (int32_t)ctx->tsit5Steps.size();
+  return HG_OK;
+}
+
 int hg_loss_and_grad(hg_ctx* ctx, const double* Q0, int32_t nsteps, double dt, int32_t ckpt_every,
                      const int32_t* probe_cells, const double* obs, int32_t n_probe, double* loss,
                      double* g_manning_cells, double* g_zb, double* g_inletq, double* Q_final) {

@@ -83,6 +83,8 @@ struct hg_ctx {
   // caller's checkpoint spacing exactly, > 0 a budget in bytes.
   int64_t adjTapeBytes = -1;
   int32_t adjIntegrator = 0;        // the steps the adjoint differentiates: 0 SSP-RK2, 1 fixed-step Tsit5
+  std::vector<double> adjSteps;     // hg_set_adjoint_steps: the Tsit5 adjoint's step sizes (empty: dt each)
+  std::vector<double> tsit5Steps;   // the step sizes the last hg_integrate_tsit5 accepted (hg_tsit5_steps)
   // State-dependent resistance (hg_set_manning_function / hg_set_ude): device
   // buffers, allocated on first use; dm.res points into them.
   double *d_resKs = nullptr, *d_resW = nullptr, *d_resStats = nullptr, *d_resPartials = nullptr, *d_fres = nullptr;

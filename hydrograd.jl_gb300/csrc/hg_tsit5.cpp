@@ -281,6 +281,7 @@ int run_tsit5(hg_ctx* ctx, V& vec, double* Q, double t0, double t1, double dt0, 
   double errOld = 1e-4;
   double t = t0;
   int accepted = 0, rejected = 0, saved = 0;
+  ctx->tsit5Steps.clear();
   int evals = (adaptive && !(dt0 > 0)) ? 2 : 1;   // RHS evaluations so far: K1, and the starting-step probe
   while (t1 - t > 1e-14 * std::max(1.0, std::fabs(t1))) {
     if (accepted + rejected >= max_steps) return fail(ctx, HG_ERR_ARG, "hg_integrate_tsit5: max_steps reached");
@@ -305,6 +306,7 @@ int run_tsit5(hg_ctx* ctx, V& vec, double* Q, double t0, double t1, double dt0, 
       if (rc) return rc;
     }
     if (eest <= 1.0) {
+      ctx->tsit5Steps.push_back(h);
       t = hit ? target : t + h;
       std::swap(U, Unew);
       std::swap(K[0], K[kTsit5Stages - 1]);   // first same as last

@@ -107,6 +107,8 @@ SIGNATURES = {
     "hg_set_riemann_solver": [_vp, ctypes.c_int32],
     "hg_set_dt_min": [_vp, ctypes.c_double],
     "hg_set_adjoint_integrator": [_vp, ctypes.c_int32],
+    "hg_set_adjoint_steps": [_vp, _dp, ctypes.c_int32],
+    "hg_tsit5_steps": [_vp, _dp, ctypes.c_int32, _ip],
     "hg_final_vjp": [_vp, _dp, ctypes.c_int32, ctypes.c_double, ctypes.c_int32, _dp, _dp, _dp, _dp, _dp],
     "hg_time_stage_kernel": [_vp, ctypes.c_int32, ctypes.c_int32, _dp],
     "hg_time_vjp_kernel": [_vp, ctypes.c_int32, ctypes.c_int32, _dp],

@@ -263,6 +263,22 @@ class SWE2D:
         stats = tuple(int(v) for v in st)
         return (Q, stats, saves) if saves is not None else (Q, stats)
 
+    def tsit5_steps(self):
+        """hg_tsit5_steps: the step sizes the last integrate_tsit5 accepted."""
+        cnt = np.zeros(1, dtype=np.int32)
+        self._chk(lib().hg_tsit5_steps(self.h, None, 0, _i(cnt)))
+        out = np.zeros(int(cnt[0]))
+        if len(out):
+            self._chk(lib().hg_tsit5_steps(self.h, _d(out), len(out), _i(cnt)))
+        return out
+
+    def set_adjoint_steps(self, dts=None):
+        """hg_set_adjoint_steps: the step sizes the Tsit5 adjoint
+        differentiates (e.g. tsit5_steps() of an adaptive run); None: steps of
+        the gradient call's dt."""
+        d = np.ascontiguousarray(dts if dts is not None else [], dtype=np.float64)
+        self._chk(lib().hg_set_adjoint_steps(self.h, _d(d) if len(d) else None, len(d)))
+
     def upload(self, Q):
         self._chk(lib().hg_state_upload(self.h, _d(np.ascontiguousarray(Q, dtype=np.float64))))
 

@@ -179,6 +179,21 @@ set_dt_min!(ctx::Context, dt_min::Real) =
 set_adjoint_integrator!(ctx::Context, integrator::Symbol) =
     check(ctx.ptr, ccall((:hg_set_adjoint_integrator, lib), Cint, (Ptr{Cvoid}, Int32), ctx,
                          Int32(integrator === :tsit5 ? 1 : integrator === :ssprk2 ? 0 : error("integrator"))))
+# The step sizes the Tsit5 gradients differentiate (e.g. tsit5_steps of an adaptive solve);
+# an empty vector returns to steps of the call's dt.
+set_adjoint_steps!(ctx::Context, dts::Vector{Float64}) =
+    check(ctx.ptr, ccall((:hg_set_adjoint_steps, lib), Cint, (Ptr{Cvoid}, Ptr{Float64}, Int32), ctx,
+                         isempty(dts) ? C_NULL : dts, Int32(length(dts))))
+# The step sizes the last solve_tsit5! accepted.
+function tsit5_steps(ctx::Context)
+    cnt = Ref{Int32}(0)
+    check(ctx.ptr, ccall((:hg_tsit5_steps, lib), Cint, (Ptr{Cvoid}, Ptr{Float64}, Int32, Ref{Int32}), ctx, C_NULL,
+                         Int32(0), cnt))
+    out = zeros(Float64, cnt[])
+    isempty(out) || check(ctx.ptr, ccall((:hg_tsit5_steps, lib), Cint, (Ptr{Cvoid}, Ptr{Float64}, Int32, Ref{Int32}),
+                                         ctx, out, Int32(length(out)), cnt))
+    return out
+end
 set_hydrograph!(ctx::Context, group::Integer, t::Vector{Float64}, q::Vector{Float64}) =
     check(ctx.ptr, ccall((:hg_set_inlet_hydrograph, lib), Cint, (Ptr{Cvoid}, Int32, Int32, Ptr{Float64}, Ptr{Float64}),
                          ctx, Int32(group), Int32(length(t)), t, q))

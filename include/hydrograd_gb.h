@@ -172,6 +172,11 @@ int hg_ensemble_steps(hg_ctx* ctx, int32_t nsteps, double* dts, double* t_elapse
 int hg_integrate_tsit5(hg_ctx* ctx, double* Q, double t0, double t1, double abstol, double reltol, double dt0,
                        int32_t adaptive, int32_t max_steps, int32_t n_save, const double* t_save, double* saves,
                        int32_t* stats);
+/* The step sizes the last hg_integrate_tsit5 call accepted, in order (the
+ * adaptive solve's steps, which hg_set_adjoint_steps hands to the gradient
+ * calls): the first min(cap, count) into dts, their number into *count (may
+ * be NULL).  Returns HG_ERR_ARG (no message) for a null context or dts. */
+int hg_tsit5_steps(const hg_ctx* ctx, double* dts, int32_t cap, int32_t* count);
 /* The Butcher tableau in use: c[7], a[7][7] (row-major, lower triangle), b[7], btilde[7] = b - bhat. */
 int hg_tsit5_tableau(double* c7, double* a49, double* b7, double* btilde7);
 
@@ -380,6 +385,15 @@ int hg_set_adjoint_tape(hg_ctx* ctx, int64_t bytes);
  * the states after each step, as with SSP-RK2. */
 enum hg_adjoint_integrator { HG_ADJ_SSPRK2 = 0, HG_ADJ_TSIT5 = 1 };
 int hg_set_adjoint_integrator(hg_ctx* ctx, int32_t integrator);
+/* The step sizes the Tsit5 adjoint differentiates (HG_ADJ_TSIT5): with n > 0,
+ * the gradient calls take step s of size dts[s] from t_s = dts[0] + ... +
+ * dts[s-1] (their dt argument then unused; nsteps <= n, else HG_ERR_ARG) --
+ * typically the accepted steps of an adaptive hg_integrate_tsit5 run
+ * (hg_tsit5_steps), held fixed as ForwardDiff through the reference's adaptive
+ * solve holds them (its step-size control acts on the values, not the
+ * derivatives).  n = 0 returns to steps of dt.  The SSP-RK2 adjoint ignores
+ * them. */
+int hg_set_adjoint_steps(hg_ctx* ctx, const double* dts, int32_t n);
 
 /* Vector-Jacobian product of the final state: with Q_K the state after nsteps
  * SSP-RK2 steps of dt from Q0, the gradients of lambda . Q_K (lambda [3n], the

@@ -195,6 +195,66 @@ def test_fp32c_final_vjp_matches_dual_numbers(problem):
     assert abs(r["g_inletq"][0] - p["dQq"][0] @ lam) <= 1e-3 * abs(p["dQq"][0] @ lam)
 
 
+def test_adaptive_solve_steps_are_differentiated(problem):
+    """hg_set_adjoint_steps: the accepted steps of an adaptive solve
+    (hg_tsit5_steps), held fixed and differentiated.  Equal steps of dt give
+    the fixed-step gradient bit for bit; the adaptive sequence's gradients
+    agree with central differences of the device's own loss over the same
+    steps (zone n, inlet Q; FP64), and FP32C with FP64 within 1e-3."""
+    p = problem
+    ctx, case = p["ctx"], p["case"]
+    args = (p["probes"], p["obs"])
+    ctx.set_adjoint_steps(np.full(K, p["dt"]))
+    a = ctx.loss_and_grad(p["Q0"], K, p["dt"], *args, ckpt_every=5)
+    ctx.set_adjoint_steps(None)
+    b = ctx.loss_and_grad(p["Q0"], K, p["dt"], *args, ckpt_every=5)
+    for k in ("g_manning", "g_zb", "g_inletq"):
+        np.testing.assert_array_equal(a[k], b[k])
+    assert a["loss"] == b["loss"]
+    # the adaptive solve over the same span, and its steps
+    ctx.integrate_tsit5(p["Q0"], 0.0, K * p["dt"])
+    steps = ctx.tsit5_steps()
+    M = len(steps)
+    assert M >= 3 and abs(steps.sum() - K * p["dt"]) <= 1e-9 * K * p["dt"]
+    assert np.ptp(steps) > 0.0   # not all one size
+    obs = np.resize(p["obs"], (M, len(p["probes"])))
+    ctx.set_adjoint_steps(steps)
+    try:
+        r = ctx.loss_and_grad(p["Q0"], M, 1.0, p["probes"], obs, ckpt_every=4)
+        gz = zone_sums(r["g_manning"], p["zones"], p["nz"])
+        zones = np.array(case["manning_zones"], dtype=float)
+        loss = lambda: ctx.loss_and_grad(p["Q0"], M, 1.0, p["probes"], obs, ckpt_every=4)["loss"]
+        for z in range(p["nz"]):
+            e = 1e-6 * zones[z]
+            lz = []
+            for sgn in (1.0, -1.0):
+                zz = zones.copy()
+                zz[z] += sgn * e
+                ctx.set_manning_zones(case["mat_id"], zz)
+                lz.append(loss())
+            ctx.set_manning_zones(case["mat_id"], zones)
+            fd = (lz[0] - lz[1]) / (2 * e)
+            assert abs(gz[z] - fd) <= 1e-5 * np.abs(gz).max(), z
+        q0 = np.asarray(case["inlet_q"], dtype=float)
+        lq = []
+        for sgn in (1.0, -1.0):
+            ctx.set_inlet_q(q0 + sgn * 1e-6 * q0)
+            lq.append(loss())
+        ctx.set_inlet_q(q0)
+        fdq = (lq[0] - lq[1]) / (2e-6 * q0[0])
+        assert abs(r["g_inletq"][0] - fdq) <= 1e-5 * abs(fdq)
+        with pytest.raises(HgError):   # more steps than sizes given
+            ctx.loss_and_grad(p["Q0"], M + 1, 1.0, p["probes"], np.resize(obs, (M + 1, len(p["probes"]))))
+        c32 = fp32c_ctx(case)
+        c32.set_adjoint_steps(steps)
+        r32 = c32.loss_and_grad(p["Q0"], M, 1.0, p["probes"], obs, ckpt_every=4)
+        g32 = zone_sums(r32["g_manning"], p["zones"], p["nz"])
+        assert np.abs(g32 - gz).max() <= 1e-3 * np.abs(gz).max()
+        assert abs(r32["g_inletq"][0] - r["g_inletq"][0]) <= 1e-3 * abs(r["g_inletq"][0])
+    finally:
+        ctx.set_adjoint_steps(None)
+
+
 # Through a state-dependent resistance: every stage's VJP takes dL/dn back
 # through the n function (or the UDE network) at that stage's own state.
 # Against central differences of the oracle's fixed Tsit5 loss, which
