@@ -245,6 +245,10 @@ def test_adaptive_solve_steps_are_differentiated(problem):
         assert abs(r["g_inletq"][0] - fdq) <= 1e-5 * abs(fdq)
         with pytest.raises(HgError):   # more steps than sizes given
             ctx.loss_and_grad(p["Q0"], M + 1, 1.0, p["probes"], np.resize(obs, (M + 1, len(p["probes"]))))
+        for bad in ([p["dt"], -p["dt"]], [p["dt"], np.nan], [0.0]):   # sizes must be positive and finite
+            with pytest.raises(HgError):
+                ctx.set_adjoint_steps(bad)
+        ctx.set_adjoint_steps(steps)   # a refused call leaves the sizes set before it
         c32 = fp32c_ctx(case)
         c32.set_adjoint_steps(steps)
         r32 = c32.loss_and_grad(p["Q0"], M, 1.0, p["probes"], obs, ckpt_every=4)
