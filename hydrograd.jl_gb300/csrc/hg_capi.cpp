@@ -197,9 +197,13 @@ int enqueue_download(hg_ctx* c, double* Q) {
 // The FP32 path steps with two fused launches when the inlet groups fit and
 // the resistance does not depend on the state (the fused stage forms the next
 // stage's conveyance totals from its output state with the resident n).
+// Fused FP32C steps: constant n, or n from an n(h, Umag, ks) function of the
+// state, which the fused kernels evaluate themselves (not the UDE closures,
+// whose LayerNorm statistics span all cells).
 bool fused(const hg_ctx* c) {
-  return c->precision == HG_FP32C && c->dm.nInlet <= kMaxFusedInlets && c->dm.res.kind == kResConstant &&
-         c->ds.nMembers == 0;
+  const int32_t k = c->dm.res.kind;
+  return c->precision == HG_FP32C && c->dm.nInlet <= kMaxFusedInlets &&
+         (k == kResConstant || (k >= kResPowerLaw && k <= kResHUmagKs)) && c->ds.nMembers == 0;
 }
 
 // Kernels per RHS evaluation besides the stage: resistance, inlet totals.
@@ -359,7 +363,7 @@ void set_stage_choice(hg_ctx* c, const TuneChoice& t) {
 // useCache: take a cached choice instead of timing (the automatic tune of a
 // context's first steps); an explicit hg_autotune times and rewrites it.
 int autotune_stage(hg_ctx* c, int reps, bool useCache) {
-  if (!fused(c)) return HG_OK;
+  if (!fused(c) || c->dm.res.kind != kResConstant) return HG_OK;   // (n functions: one fixed kernel)
   const size_t n = (size_t)c->n;
   const size_t rec = (n * sizeof(float4) + 255) & ~(size_t)255, lo = (n * sizeof(float2) + 255) & ~(size_t)255;
   if (2 * (rec + lo) > c->flushBytes) return HG_OK;   // no scratch: keep the default

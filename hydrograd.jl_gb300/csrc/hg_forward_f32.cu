@@ -20,6 +20,7 @@
 #include "hg_members.cuh"
 #include "hg_pdl.cuh"
 #include "hg_reduce.cuh"
+#include "hg_resfn.cuh"
 #include "hg_state.hpp"
 #include "hg_tma.cuh"
 
@@ -162,9 +163,21 @@ __device__ __forceinline__ void load_slots(const DevMesh& m, int c, float4 (&sl)
 // Only the warps of those few tiles reload the slot records, so the others
 // carry no extra registers for it.
 constexpr int kTileWarps = kBlock / 32;
-template <int NS>
+
+// Manning's n of a cell from its clamped side state, for the n(h, Umag, ks)
+// functions (ResDev kinds power law .. h_Umag_ks) evaluated in the fused
+// stages (RESFN) instead of a separate resistance pass: as k_res_cells forms
+// it, Umag = |q| / h of the clamped state.
+__device__ __forceinline__ float own_manning_f32(const DevMesh& m, const Side<float>& s, int c) {
+  const float u = s.hu / s.h, v = s.hv / s.h;
+  return manning_fn<float>(m.res, s.h, sqrtf(u * u + v * v), m.res.ks ? (float)m.res.ks[c] : 0.0f);
+}
+
+// RESFN: n of the output state from the function (Xo: the output records),
+// not the resident CP.w.
+template <int NS, bool RESFN = false>
 __device__ __forceinline__ void fused_inlet_totals(const DevMesh& m, const StageFuse& f, int c, float hOut,
-                                                   bool wetOut) {
+                                                   bool wetOut, const float4* Xo = nullptr) {
   const int lane = threadIdx.x & 31;
   const int c0 = c - lane;   // the warp's first cell; warps never straddle tiles (32 divides kBlock)
   if (c0 >= m.n) return;     // uniform over the warp
@@ -172,6 +185,11 @@ __device__ __forceinline__ void fused_inlet_totals(const DevMesh& m, const Stage
   if (slot < 0) return;
   const int wIdx = (c0 % kBlock) / 32;
   const int ng = m.nInlet;
+  float nOut = 0.0f;
+  if (wetOut) {
+    if constexpr (RESFN) nOut = own_manning_f32(m, make_side_f32(Xo[c], m.CP[c], m.hsmf, m.hsmLo).s, c);
+    else nOut = m.CP[c].w;
+  }
   for (int g = 0; g < ng; ++g) {
     double v = 0.0;
     if (wetOut) {
@@ -179,7 +197,7 @@ __device__ __forceinline__ void fused_inlet_totals(const DevMesh& m, const Stage
         const int32_t nb = slot_nb(m.SL[(size_t)k * m.n + c]);
         if (nb >= 0 || nb == kNoFace) continue;
         const int32_t bf = boundary_index(nb);
-        if (m.bfInfo[bf] == (kBcInletQ | (g << 2))) v += m.bfLp53[bf] * (double)hOut / (double)m.CP[c].w;
+        if (m.bfInfo[bf] == (kBcInletQ | (g << 2))) v += m.bfLp53[bf] * (double)hOut / (double)nOut;
       }
     }
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -240,7 +258,7 @@ __device__ __forceinline__ void stage_finish(const DevMesh& m, const DevScalars&
 // kBlock) for in-block neighbours.  The input state's lo parts and (stage 2)
 // the base state are read at qinP[k], xbP[k], qbP[k] -- global arrays (k = c)
 // or a tile staged in shared memory -- where they are used.
-template <int NS, int MODE, bool LOC = false, int RS = -1, int TB = kBlock>
+template <int NS, int MODE, bool LOC = false, int RS = -1, int TB = kBlock, bool RESFN = false>
 __device__ __forceinline__ void stage_cell(const DevMesh& m, const DevScalars& s, const float4* __restrict__ X,
                                            const float4* sX, const float4* sP, const float4* hX, const float4* hP,
                                            int base, int c,
@@ -250,9 +268,11 @@ __device__ __forceinline__ void stage_cell(const DevMesh& m, const DevScalars& s
                                            float& cand, float& hOut, bool& wetOut) {
   const SideF32 L = make_side_f32(xin, cp, m.hsmf, m.hsmLo);
   const OwnF32 own = own_f32(L.s, m.gf);
+  float4 cpn = cp;   // RESFN: the cell's n from its own state, for the friction and the inlet ghost
+  if constexpr (RESFN) cpn.w = own_manning_f32(m, L.s, c);
   float f0, f1, f2;
-  face_sum_f32<NS, LOC, RS, TB>(m, X, sX, sP, hX, hP, base, c, L, own, make_float2(cp.x, cp.y), sl, totalIn, cp.w, s.flags, f0, f1, f2);
-  stage_finish<NS, MODE>(m, s, L, f0, f1, f2, c, sl, xin, cp, cs, qinP, xbP, qbP, k, dt, Xout, Rout, cfl, cand, hOut,
+  face_sum_f32<NS, LOC, RS, TB>(m, X, sX, sP, hX, hP, base, c, L, own, make_float2(cp.x, cp.y), sl, totalIn, cpn.w, s.flags, f0, f1, f2);
+  stage_finish<NS, MODE>(m, s, L, f0, f1, f2, c, sl, xin, cpn, cs, qinP, xbP, qbP, k, dt, Xout, Rout, cfl, cand, hOut,
                          wetOut);
 }
 
@@ -351,7 +371,9 @@ __device__ __forceinline__ void fused_record(const DevScalars& s, const StageFus
 // autotuner chooses among; the arithmetic does not depend on it).
 // TB: cells per block (the autotuner's tile-size candidates: 128, 256, 512;
 // a cell's arithmetic does not depend on it).
-template <int NS, bool FUSED, int MODE, int RS = -1, int MINB = 0, int TB = kBlock>
+// RESFN: Manning's n from an n(h, Umag, ks) function of the state, evaluated
+// here (DevMesh::res) instead of read from CP.w.
+template <int NS, bool FUSED, int MODE, int RS = -1, int MINB = 0, int TB = kBlock, bool RESFN = false>
 __global__ void __launch_bounds__(TB, MINB > 0 ? MINB : stage_min_blocks<NS>())
     k_stage_f32(DevMesh m, DevScalars s, StateF32 Xin, StateF32 Xbase, StateF32 Xout, double* Rout, int cfl,
                 StageFuse f) {
@@ -385,14 +407,14 @@ __global__ void __launch_bounds__(TB, MINB > 0 ? MINB : stage_min_blocks<NS>())
   if (active) {
     const float dt = (MODE == kModeRhs || MODE == kModeRhsF32) ? 0.0f
                                                                : (FUSED ? dtShared : (mem >= 0 ? s.dtMf[mem] : *s.dtf));
-    stage_cell<NS, MODE, false, RS, TB>(m, s, Xin.x, sX, sP, nullptr, nullptr, base, c, sl, xin, cp, cs, Xin.q, Xbase.x,
+    stage_cell<NS, MODE, false, RS, TB, RESFN>(m, s, Xin.x, sX, sP, nullptr, nullptr, base, c, sl, xin, cp, cs, Xin.q, Xbase.x,
                                      Xbase.q, c,
                          dt, FUSED ? f.totalIn : m.totalA, Xout, Rout, cfl, cand, hOut, wetOut);
   }
   if (FUSED && f.record && blockIdx.x == 0 && threadIdx.x == 0) fused_record(s, f);
   if (cfl && !FUSED && s.nMembers > 0) member_min_publish_f(s, cand, mem);
   else if (cfl) block_min_publish_f(cand, FUSED ? s.cflMinF + (1 - f.parity) : s.cflMinF);
-  if (FUSED && m.nInlet > 0) fused_inlet_totals<NS>(m, f, c, hOut, wetOut);
+  if (FUSED && m.nInlet > 0) fused_inlet_totals<NS, RESFN>(m, f, c, hOut, wetOut, Xout.x);
 }
 
 // ---------------------------------------------------------------------------
@@ -1283,9 +1305,36 @@ void launch_stage_f32(const DevMesh& m, const DevScalars& s, int mode, StateF32 
   else launch_stage_ns<8, false>(m, s, mode, Xin, Xbase, Xout, Rout, f, nf, st);
 }
 
+namespace {
+// Fused stages with Manning's n from a function of the state (RESFN): the
+// gather kernel in its default shape.
+template <int NS>
+void launch_stage_resfn(const DevMesh& m, const DevScalars& s, int mode, StateF32 Xin, StateF32 Xbase, StateF32 Xout,
+                        int cfl, const StageFuse& f, cudaStream_t st) {
+  const bool hll = m.riemann == kRiemannHll;
+  const int nb = blocks_for(m.n);
+  double* none = nullptr;
+  if (mode == kModeStage1) {
+    auto k = hll ? k_stage_f32<NS, true, kModeStage1, kRiemannHll, 0, kBlock, true>
+                 : k_stage_f32<NS, true, kModeStage1, kRiemannRoe, 0, kBlock, true>;
+    launch_k(true, k, nb, kBlock, 0, st, m, s, Xin, Xbase, Xout, none, cfl, f);
+  } else if (mode == kModeStage2) {
+    auto k = hll ? k_stage_f32<NS, true, kModeStage2, kRiemannHll, 0, kBlock, true>
+                 : k_stage_f32<NS, true, kModeStage2, kRiemannRoe, 0, kBlock, true>;
+    launch_k(true, k, nb, kBlock, 0, st, m, s, Xin, Xbase, Xout, none, cfl, f);
+  }
+}
+}  // namespace
+
 void launch_stage_f32_fused(const DevMesh& m0, const DevScalars& s, int mode, StateF32 Xin, StateF32 Xbase,
                             StateF32 Xout, const StageFuse& fu, cudaStream_t st) {
   const int f = (!fu.record && fu.cflMode) ? 1 : 0;   // stage 2 publishes the next CFL minimum
+  if (m0.res.kind != kResConstant) {   // n(h, Umag, ks) of the state, in the kernel
+    if (m0.nslot <= 3) launch_stage_resfn<3>(m0, s, mode, Xin, Xbase, Xout, f, fu, st);
+    else if (m0.nslot <= 4) launch_stage_resfn<4>(m0, s, mode, Xin, Xbase, Xout, f, fu, st);
+    else launch_stage_resfn<8>(m0, s, mode, Xin, Xbase, Xout, f, fu, st);
+    return;
+  }
   const int forced = forced_stage_kernel();
   DevMesh m = m0;
   if (stage_variant_forced() >= 0) m.stageVariant = stage_variant_forced();
