@@ -934,8 +934,10 @@ int adjoint_loss_and_grad(hg_ctx* c, const double* Q0, int32_t K, double dt, int
     // instead of recomputed: T0[i] of Q0s[i] (i = 0..C) and T1[i] of Q1s[i].
     // When the inlet groups fit the fused stage kernels, those kernels produce
     // the totals of their output states; otherwise k_inlet_total does.
-    // (not with a state-dependent n: the fused stages form the totals with the resident n)
-    const bool fz = dm.nInlet <= kMaxFusedInlets && dm.res.kind == kResConstant;
+    // (with a constant n, or an n(h, Umag, ks) function the fused stages evaluate
+    // themselves -- as hg_integrate's steps do; not with a UDE closure)
+    const bool fz = dm.nInlet <= kMaxFusedInlets &&
+                    (dm.res.kind == kResConstant || (dm.res.kind >= kResPowerLaw && dm.res.kind <= kResHUmagKs));
     const size_t stride = (size_t)std::max(dm.nInlet, kMaxFusedInlets);
     const size_t totNeed = (size_t)(2 * C + 1) * stride;
     if (totNeed > b->segTotCap) {
