@@ -754,9 +754,12 @@ def run_ours(args):
     achieved = bytes_stage / (out["fp32c"]["stage_ms"] * 1e-3) / 1e9
     kern = out["fp32c"]["stage_kernel"]
     kname = STAGE_KERNELS[kern][0]
+    variant = out["fp32c"].get("stage_variant", 0)
     if kern == 0:
-        kname = kname[:-1] + "; " + GATHER_SHAPES.get(out["fp32c"].get("stage_variant", 0), "") + ")"
-    tr = profile_traffic("fp32c", kern)
+        kname = kname[:-1] + "; " + GATHER_SHAPES.get(variant, "") + ")"
+    # the DRAM traffic from the capture of the chosen kernel (and shape, where it has its own)
+    tr = profile_traffic("fp32c", name="k_stage_f32_t128_river_tri_1M.md") if (kern == 0 and variant == 3) \
+        else profile_traffic("fp32c", kern)
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": None if tr is None else tr * N, "kernel": kname + ", one RK2 stage pass",
             "algorithmic_bytes_per_launch": bytes_stage, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)"}
