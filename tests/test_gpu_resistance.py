@@ -116,6 +116,27 @@ def test_ude_widths_match_oracle(hidden, acts, over_batch, precision):
     assert block_err(Qg, Qo, N) <= STATE_TOL[precision]
 
 
+@pytest.mark.parametrize("solver", ["Roe", "HLL"])
+@pytest.mark.parametrize("name,fn,params", FN_CASES, ids=[f"{c[0]}-{c[1]}" for c in FN_CASES])
+def test_fused_fp32c_steps_with_n_functions(name, fn, params, solver):
+    """The fused FP32C steps evaluate the n function in the stage kernel
+    (both Riemann solvers): CFL steps against the oracle's steps of the same
+    sizes, and the resident steps (hg_advance) the same as hg_integrate's."""
+    d = load_fixture(name)
+    ctx, o, N = setup_pair(d, "fp32c")
+    set_fn(ctx, o, d, fn, params)
+    ctx.set_riemann_solver(solver)
+    o.set_riemann_solver(solver)
+    Q0 = initial_state(d, N)
+    dt = 0.5 * o.cfl_dt(Q0, 0.4)
+    Qg, _ = ctx.integrate(Q0, 60, dt=dt)
+    Qo = o.rk2(Q0, 60, dt=dt, nthreads=4)
+    assert block_err(Qg, Qo, N) <= STATE_TOL["fp32c"]
+    ctx.upload(Q0)
+    ctx.advance(60, dt=dt, graph=True)
+    assert block_err(ctx.download(), Qg, N) <= 1e-6
+
+
 @pytest.mark.parametrize("precision", ["fp64", "fp32c"])
 def test_graph_steps_and_constant_restore(precision):
     """Resident steps (hg_advance, captured in a graph) see the state-dependent
